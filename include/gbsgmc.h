@@ -1,0 +1,345 @@
+/*
+ * gbsgmc.h -- C ABI of the GB300 SG-MCMC hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns an
+ * int status (GBSGMC_OK == 0) and never throws.  Pointers named `*_dev` or
+ * documented as "device" are CUDA device pointers owned by the caller; the
+ * library only owns the memory behind a gbsgmc_plan handle.  Launches are
+ * ordered on the caller's stream and never synchronise the host, except the
+ * plan calls, which say so.  Errors raised inside a kernel (an observation
+ * index outside [0, N), a non-finite potential, a bounded wait that gave up)
+ * are written to a caller-owned device status word `status_dev`; the first
+ * error code written wins (atomicCAS from 0).
+ *
+ * The reference (jax_sgmc 0.1.5) has no C ABI: its boundary is the Python API.
+ * Each declaration below names the reference function whose arithmetic it
+ * replaces (paths relative to the jax-sgmc project root).
+ */
+#ifndef GBSGMC_H_
+#define GBSGMC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A cudaStream_t, passed as an opaque pointer (NULL = legacy default stream). */
+typedef void* gbsgmc_stream_t;
+
+/* Status codes (return values and device status words). */
+#define GBSGMC_OK 0
+#define GBSGMC_ERR_ARG 1         /* null pointer, negative size, bad stride   */
+#define GBSGMC_ERR_SHAPE 2       /* shape outside the supported range         */
+#define GBSGMC_ERR_INDEX 3       /* observation index outside [0, N)          */
+#define GBSGMC_ERR_NONFINITE 4   /* potential or gradient is NaN / Inf        */
+#define GBSGMC_ERR_TIMEOUT 5     /* a bounded device wait gave up             */
+#define GBSGMC_ERR_CUDA 6        /* CUDA runtime error (message in last_error) */
+#define GBSGMC_ERR_UNSUPPORTED 7 /* feature not available in this build        */
+
+/* Likelihood families of the generalised-linear kernels. */
+#define GBSGMC_GLM_LINEAR_GAUSSIAN 0 /* lk = log N(y | x.w, sigma^2)          */
+#define GBSGMC_GLM_LOGISTIC 1        /* lk = y*z - softplus(z), z = x.w       */
+#define GBSGMC_GLM_LINEAR 2          /* lk = z = x.w (y unused)               */
+
+/* Noise stream tags (fourth Philox counter word). */
+#define GBSGMC_TAG_SGLD 0u
+#define GBSGMC_TAG_OBABO_1 1u
+#define GBSGMC_TAG_OBABO_2 2u
+#define GBSGMC_TAG_SGHMC_RESAMPLE 3u
+#define GBSGMC_TAG_SGHMC_STEP 4u
+#define GBSGMC_TAG_SWAP 5u
+#define GBSGMC_TAG_INDEX 6u
+
+/* Thread-local message for the last non-zero status returned on this thread. */
+const char* gbsgmc_last_error(void);
+/* ABI version (major*10000 + minor*100 + patch). */
+int gbsgmc_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Random streams                                                            */
+/* ------------------------------------------------------------------------ */
+
+/* numpy PCG64 bit-generator state (numpy's bit_generator.state dict:
+ * state.state, state.inc, has_uint32, uinteger), 128-bit words split in
+ * 64-bit halves.  40 bytes, 8-byte aligned. */
+typedef struct gbsgmc_pcg64 {
+  uint64_t state_hi, state_lo;
+  uint64_t inc_hi, inc_lo;
+  uint32_t has_uint32, uinteger;
+} gbsgmc_pcg64;
+
+/* Draws `draws` indices in [0, n_obs) for each of `chains` numpy PCG64 streams,
+ * bit-identical to numpy's Generator.choice(arange(n_obs), draws,
+ * replace=True) (== Generator.integers(0, n_obs, dtype=int64)), and advances
+ * `states_dev` exactly as numpy would.  Draw j of chain c is written to
+ * idx_dev[c*chain_stride + (j / per_step)*step_stride + j % per_step].
+ * n_obs in [1, 2^31).
+ * Replaces NumpyDataLoader._draw_indices (jax_sgmc/data/numpy_loader.py:382-389)
+ * called cache_size times by _get_indices (numpy_loader.py:342-355). */
+int gbsgmc_index_draw_pcg64(gbsgmc_pcg64* states_dev, int chains,
+                            int64_t n_obs, int64_t draws, int per_step,
+                            int32_t* idx_dev, int64_t chain_stride,
+                            int64_t step_stride, int* status_dev,
+                            gbsgmc_stream_t stream);
+
+/* Counter-based index draws: idx = floor(u32 * n_obs / 2^32) with u32 from
+ * Philox4x32-10(counter = (j/4, step, chain_base + c, TAG_INDEX),
+ * key = seed).  `steps` consecutive steps starting at `first_step`, `per_step`
+ * draws each, laid out as in gbsgmc_index_draw_pcg64.
+ * Replaces DeviceNumpyDataLoader.get_random_data
+ * (jax_sgmc/data/numpy_loader.py:128-141), whose threefry stream is not
+ * reproduced. */
+int gbsgmc_index_draw_philox(uint64_t seed, int chain_base, int chains,
+                             int64_t first_step, int steps, int per_step,
+                             int64_t n_obs, int32_t* idx_dev,
+                             int64_t chain_stride, int64_t step_stride,
+                             gbsgmc_stream_t stream);
+
+/* Standard normals from the production noise stream: out[c*stride + j] =
+ * N(0,1) from Philox4x32-10(counter = (j/4, step, chain_base + c, tag),
+ * key = seed) through Box-Muller on the pairs (u0,u1), (u2,u3).
+ * Replaces integrator.random_tree (jax_sgmc/integrator.py:119-135). */
+int gbsgmc_philox_normal(uint64_t seed, int chain_base, int chains,
+                         int64_t step, uint32_t tag, int64_t count,
+                         float* out_dev, int64_t stride,
+                         gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Generalised-linear minibatch potential and its adjoint                    */
+/* ------------------------------------------------------------------------ */
+
+/* Model + dataset description (all pointers are device pointers). */
+typedef struct gbsgmc_glm {
+  int family;          /* GBSGMC_GLM_*                                       */
+  int d;               /* features = parameters per chain, 1..1024            */
+  int64_t n_obs;       /* N, observations in the dataset (the N/n scale)     */
+  int64_t ld;          /* row stride of X in floats (>= d)                    */
+  const float* X;      /* [n_obs, ld] fp32 features                           */
+  const float* y;      /* [n_obs] fp32 targets                                */
+  float sigma;         /* linear-Gaussian noise sd                            */
+  float prior_scale;   /* Gaussian prior N(0, s^2 I) sd; <= 0: flat prior     */
+  float temperature;   /* potential temperature T: U = (-N/n sum lk - log p)/T */
+  int _pad;
+} gbsgmc_glm;
+
+/* Bytes of workspace needed by gbsgmc_glm_value_and_grad for `chains` chains of
+ * minibatch size n.  The workspace must be zero-filled before its first use;
+ * calls leave it zeroed again. */
+size_t gbsgmc_glm_workspace_bytes(int chains, int n, int d);
+
+/* For each chain c: U[c] = (-N/n * sum_i m_i lk_i - log p(w_c)) / T,
+ * grad[c] = dU/dw_c, lk[c, i] = lk_i and lk_var[c] = var_i(lk_i), where row i
+ * of the minibatch is observation idx[c*idx_stride + i] and m_i = mask[c*n+i]
+ * (all ones when mask is NULL).  grad, lk, lk_var may be NULL.
+ * Replaces minibatch_potential's potential_function
+ * (jax_sgmc/potential.py:159-214) under jax.value_and_grad
+ * (jax_sgmc/integrator.py:792) plus jnp.var(likelihoods) (integrator.py:880). */
+int gbsgmc_glm_value_and_grad(const gbsgmc_glm* model, int chains, int n,
+                              const int32_t* idx_dev, int64_t idx_stride,
+                              const float* mask_dev, const float* w_dev,
+                              double* U_dev, float* grad_dev, float* lk_dev,
+                              double* lk_var_dev, void* workspace_dev,
+                              size_t workspace_bytes, int* status_dev,
+                              gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Integrator updates (elementwise over [chains, P])                         */
+/* ------------------------------------------------------------------------ */
+
+/* Per-step schedule read on the device, so that captured launches can be
+ * replayed: step k = (*base_dev) + offset (base_dev NULL: k = offset);
+ * h = step_size_dev[k] (or step_size when NULL), T likewise. */
+typedef struct gbsgmc_sched {
+  const float* step_size_dev;
+  const float* temperature_dev;
+  const int64_t* base_dev;
+  const int32_t* keep_slot_dev; /* sample slot of step k, -1 = not kept */
+  int64_t offset;
+  float step_size;
+  float temperature;
+} gbsgmc_sched;
+
+/* Noise source: injected normals noise_dev[c*noise_stride + j] when noise_dev
+ * is not NULL, else Philox normals (seed, chain_base + c, step k, tag). */
+typedef struct gbsgmc_noise {
+  const float* noise_dev;
+  int64_t noise_stride;
+  uint64_t seed;
+  int chain_base;
+  int _pad;
+} gbsgmc_noise;
+
+/* SGLD step with optional RMSprop on [chains, P]:
+ *   v <- alpha v + (1-alpha) g^2;  G = 1/(lmbd + sqrt v)         (rms_prop)
+ *   x <- x + G (-h g) + sqrt(G) sqrt(2 T h) xi                    (rms_prop)
+ *   x <- x + (-h g) + sqrt(2 T h) xi                              (plain)
+ * `v_dev` NULL selects plain SGLD.  When the step is kept, the new x is copied
+ * to samples_dev[slot*chains*P + c*P + j].
+ * Replaces langevin_diffusion.update_fn (jax_sgmc/integrator.py:860-922) and
+ * adaption.rms_prop update/get (jax_sgmc/adaption.py:254-291). */
+int gbsgmc_sgld_update(int chains, int64_t P, float* x_dev, const float* g_dev,
+                       float* v_dev, float alpha, float lmbd,
+                       const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                       float* samples_dev, gbsgmc_stream_t stream);
+
+/* OBABO, first half: O (p <- sqrt(e^{-f h}) p + sqrt((1-e^{-f h}) T) sqrt(m) xi1),
+ * ke_start[c] += 0.5 p.p/m, B (p <- p - h/2 g1), A (x <- x + h p/m).
+ * `mass_dev` [P] NULL = unit mass.  Noise tag GBSGMC_TAG_OBABO_1.
+ * Replaces obabo._leapfrog_steps up to the second gradient
+ * (jax_sgmc/integrator.py:209-241). */
+int gbsgmc_obabo_first(int chains, int64_t P, float* x_dev, float* p_dev,
+                       const float* g1_dev, const float* mass_dev,
+                       float friction, double* ke_start_dev,
+                       const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                       gbsgmc_stream_t stream);
+
+/* OBABO, second half: B (p <- p - h/2 g2), ke_end[c] += 0.5 p.p/m, O with xi2.
+ * Noise tag GBSGMC_TAG_OBABO_2.  Replaces jax_sgmc/integrator.py:243-273. */
+int gbsgmc_obabo_second(int chains, int64_t P, float* p_dev,
+                        const float* g2_dev, const float* mass_dev,
+                        float friction, double* ke_end_dev,
+                        const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                        gbsgmc_stream_t stream);
+
+/* SGHMC momentum resample p = sqrt(m) xi (tag GBSGMC_TAG_SGHMC_RESAMPLE).
+ * Replaces friction_leapfrog.integrate (jax_sgmc/integrator.py:735-738). */
+int gbsgmc_sghmc_resample(int chains, int64_t P, float* p_dev,
+                          const float* mass_dev, const gbsgmc_sched* sched,
+                          const gbsgmc_noise* noise, gbsgmc_stream_t stream);
+
+/* SGHMC position update x <- x + h p/m and friction decay
+ * p <- p - h f (p/m).  Replaces jax_sgmc/integrator.py:610-619. */
+int gbsgmc_sghmc_position(int chains, int64_t P, float* x_dev, float* p_dev,
+                          const float* mass_dev, const float* friction_dev,
+                          float friction, const gbsgmc_sched* sched,
+                          gbsgmc_stream_t stream);
+
+/* SGHMC force and noise: p <- p - h g + f sqrt(2h) xi (tag
+ * GBSGMC_TAG_SGHMC_STEP).  `friction_dev` [P] or NULL (scalar friction).
+ * Replaces jax_sgmc/integrator.py:621-655 (noise_model = None). */
+int gbsgmc_sghmc_momentum(int chains, int64_t P, float* p_dev,
+                          const float* g_dev, const float* friction_dev,
+                          float friction, const gbsgmc_sched* sched,
+                          const gbsgmc_noise* noise, gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Replica exchange                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* reSGLD exchange for `pairs` (normal, hot) replica pairs, in FP64:
+ *   k += 1;  ssq <- (1 - 1/k) ssq + (1/k) var_normal
+ *   dbeta = 1/T_normal - 1/T_hot
+ *   log_s = dbeta (U_normal - U_hot - dbeta ssq / F)
+ *   swapped = !(log u < log s)      (the reference keeps the pair when
+ *                                    log u < log s and exchanges otherwise)
+ * u is given in u_dev[pair] (uniform in (0,1)), or drawn from Philox
+ * (tag GBSGMC_TAG_SWAP, counter (pair, step)) when u_dev is NULL.
+ * perm_dev[pair] receives 1 when the pair exchanged its states.  The caller
+ * exchanges the replica buffers (gbsgmc_swap_rows).
+ * Replaces solver.parallel_tempering.update (jax_sgmc/solver.py:264-293). */
+int gbsgmc_resgld_swap_f64(int pairs, const double* U_normal_dev,
+                           const double* U_hot_dev,
+                           const double* var_normal_dev, const double* T_normal_dev,
+                           const double* T_hot_dev, double F, double* ssq_dev,
+                           int64_t* k_dev, const double* u_dev, uint64_t seed,
+                           int64_t step, double* log_s_dev, int32_t* perm_dev,
+                           gbsgmc_stream_t stream);
+
+/* Exchanges rows a[pair] <-> b[pair] ([pairs, width] fp32) where
+ * perm_dev[pair] == 1.  Used for positions, RMSprop state and potentials. */
+int gbsgmc_swap_rows(int pairs, int64_t width, float* a_dev, float* b_dev,
+                     const int32_t* perm_dev, gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Fused SGLD step for the generalised-linear families                       */
+/* ------------------------------------------------------------------------ */
+
+/* One fused launch: gather of the minibatch rows (TMA bulk copies into shared
+ * memory), likelihood, adjoint, N/n-scaled reduction, Gaussian prior,
+ * RMSprop, noise and the SGLD update of every chain, plus on-device sample
+ * collection (samples_dev[slot, c, :] = new w, sample_lik_dev[slot, c] =
+ * -U(old w)).  U_dev / lk_var_dev receive the potential at the pre-update
+ * position and the variance of the per-observation log-likelihoods.
+ * `v_dev` NULL = plain SGLD.
+ * Replaces one lax.scan iteration of solver.mcmc over
+ * langevin_diffusion.update_fn (jax_sgmc/solver.py:94-123,
+ * jax_sgmc/integrator.py:860-922, jax_sgmc/adaption.py:254-291,
+ * jax_sgmc/potential.py:159-214). */
+int gbsgmc_sgld_glm_step(const gbsgmc_glm* model, int chains, int n,
+                         const int32_t* idx_dev, int64_t idx_stride,
+                         float* w_dev, float* v_dev, float alpha, float lmbd,
+                         const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                         double* U_dev, double* lk_var_dev, float* samples_dev,
+                         double* sample_lik_dev, void* workspace_dev,
+                         size_t workspace_bytes, int* status_dev,
+                         gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Plans: many steps replayed from a CUDA graph                              */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gbsgmc_plan gbsgmc_plan;
+
+/* Index source of a plan: numpy-identical PCG64 streams (pcg_dev != NULL,
+ * advanced in place) or Philox indices from index_seed. */
+typedef struct gbsgmc_index_src {
+  gbsgmc_pcg64* pcg_dev;
+  uint64_t index_seed;
+  int chain_base;
+  int _pad;
+} gbsgmc_index_src;
+
+/* Builds a plan that runs SGLD(+RMSprop) on a GLM for `chains` chains: per
+ * block of `block_steps` steps one index-draw launch and `block_steps` fused
+ * step launches, captured once into a CUDA graph on an internal stream.  All
+ * pointers are baked into the graph and must stay valid while the plan
+ * lives.  The schedule tables in `sched` must hold every step that will be
+ * run.  Replaces solver.mcmc's jit(lax.scan) driver (jax_sgmc/solver.py:152-185)
+ * for alias.sgld (jax_sgmc/alias.py:30-120). */
+int gbsgmc_sgld_glm_plan_create(gbsgmc_plan** plan, const gbsgmc_glm* model,
+                                int chains, int n, float* w_dev, float* v_dev,
+                                float alpha, float lmbd,
+                                const gbsgmc_sched* sched,
+                                const gbsgmc_noise* noise,
+                                const gbsgmc_index_src* index_src,
+                                double* U_dev, double* lk_var_dev,
+                                float* samples_dev, double* sample_lik_dev,
+                                int block_steps, int* status_dev);
+
+/* Runs steps [first_step, first_step + steps) of the plan, ordered after prior
+ * work on `stream`; later work on `stream` waits for it.  Does not block the
+ * host. */
+int gbsgmc_plan_run(gbsgmc_plan* plan, int64_t first_step, int64_t steps,
+                    gbsgmc_stream_t stream);
+
+/* Kernel launches one plan_run of `steps` steps performs (for accounting). */
+int64_t gbsgmc_plan_launches(const gbsgmc_plan* plan, int64_t steps);
+
+/* Releases the plan's graphs, stream and workspace (synchronises the plan's
+ * internal stream first). */
+int gbsgmc_plan_destroy(gbsgmc_plan* plan);
+
+/* ------------------------------------------------------------------------ */
+/* Plain (unfused) one-chain form, kept as the GPU comparison baseline       */
+/* ------------------------------------------------------------------------ */
+
+/* One SGLD(+RMSprop) step of ONE chain as separate kernels, the way an
+ * op-by-op compiler lays it out: gather rows into a buffer, forward GEMV,
+ * link, backward GEMV, reductions, prior, RMSprop, noise, update (8 launches).
+ * `buf_dev` must hold gbsgmc_plain_buffer_bytes(n, d) bytes. */
+size_t gbsgmc_plain_buffer_bytes(int n, int d);
+int gbsgmc_plain_sgld_glm_step(const gbsgmc_glm* model, int n,
+                               const int32_t* idx_dev, float* w_dev,
+                               float* v_dev, float alpha, float lmbd,
+                               const gbsgmc_sched* sched,
+                               const gbsgmc_noise* noise, double* U_dev,
+                               void* buf_dev, int* status_dev,
+                               gbsgmc_stream_t stream);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* GBSGMC_H_ */

@@ -1,0 +1,34 @@
+// Declarations shared between the translation units of libgbsgmc (not ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/gbsgmc.h"
+
+namespace gbsgmc {
+
+int set_error(int code, const char* fmt, ...);
+int check_launch(const char* what);
+
+// glm.cu
+size_t glm_ws_bytes(int chains, int n, int d);
+int glm_prepare();
+int glm_default_slices(int chains, int n);
+int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
+                  const int32_t* idx_dev, int64_t idx_stride, float* w_dev,
+                  float* v_dev, float alpha, float lmbd,
+                  const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                  double* U_dev, double* lk_var_dev, float* samples_dev,
+                  double* sample_lik_dev, void* ws, size_t ws_size,
+                  int* status_dev, cudaStream_t stream, int slices);
+
+// rng.cu
+int launch_philox_index(uint64_t seed, int chain_base, int chains,
+                        const int64_t* base, int64_t first_step, int steps,
+                        int per_step, int64_t n_obs, int32_t* idx,
+                        int64_t chain_stride, int64_t step_stride,
+                        cudaStream_t stream);
+
+}  // namespace gbsgmc

@@ -1,0 +1,230 @@
+// Plans: the multi-step driver of the SGLD hot path.
+//
+// A plan owns an internal non-blocking stream, the fused-step workspace, an
+// index buffer for one block of steps and a device step counter.  One block
+// of G steps is: index draw for G steps (numpy PCG64 streams, or Philox),
+// G fused SGLD launches whose step index is read from the device counter
+// (k = counter + j), and a one-thread launch that advances the counter by G.
+// The block is captured once into a CUDA graph and replayed, so a run of K
+// steps costs K/G graph launches on the host.  The schedule tables (step
+// size, temperature, keep slots) are read on the device at step k.
+#include <cstdlib>
+#include <new>
+
+#include "common.cuh"
+#include "internal.h"
+
+struct gbsgmc_plan {
+  gbsgmc_glm model;
+  int chains, n;
+  float* w;
+  float* v;
+  float alpha, lmbd;
+  gbsgmc_sched sched;
+  gbsgmc_noise noise;
+  gbsgmc_index_src isrc;
+  double* U;
+  double* lk_var;
+  float* samples;
+  double* sample_lik;
+  int* status;
+  int G;
+  int slices;
+  bool use_graph;
+  cudaStream_t stream;
+  void* ws;
+  size_t ws_size;
+  int32_t* idx;
+  int64_t* base;
+  cudaGraphExec_t exec;
+  cudaEvent_t ev_in, ev_out;
+};
+
+namespace gbsgmc {
+namespace {
+
+__global__ void set_counter_kernel(int64_t* c, int64_t v) { *c = v; }
+__global__ void advance_counter_kernel(int64_t* c, int64_t by) { *c += by; }
+
+int cuda_err(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return GBSGMC_OK;
+  return set_error(GBSGMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int enqueue_block(gbsgmc_plan* p, int g, cudaStream_t s) {
+  int rc;
+  const int64_t cn = static_cast<int64_t>(p->chains) * p->n;
+  if (p->isrc.pcg_dev != nullptr) {
+    rc = gbsgmc_index_draw_pcg64(p->isrc.pcg_dev, p->chains, p->model.n_obs,
+                                 static_cast<int64_t>(g) * p->n, p->n, p->idx,
+                                 p->n, cn, p->status, s);
+  } else {
+    rc = launch_philox_index(p->isrc.index_seed, p->isrc.chain_base, p->chains,
+                             p->base, 0, g, p->n, p->model.n_obs, p->idx, p->n,
+                             cn, s);
+  }
+  if (rc != GBSGMC_OK) return rc;
+  for (int j = 0; j < g; ++j) {
+    gbsgmc_sched sj = p->sched;
+    sj.base_dev = p->base;
+    sj.offset = j;
+    rc = glm_sgld_step(&p->model, p->chains, p->n, p->idx + j * cn, p->n, p->w,
+                       p->v, p->alpha, p->lmbd, &sj, &p->noise, p->U,
+                       p->lk_var, p->samples, p->sample_lik, p->ws, p->ws_size,
+                       p->status, s, p->slices);
+    if (rc != GBSGMC_OK) return rc;
+  }
+  advance_counter_kernel<<<1, 1, 0, s>>>(p->base, g);
+  return check_launch("plan: advance counter");
+}
+
+void release(gbsgmc_plan* p) {
+  if (p == nullptr) return;
+  if (p->stream != nullptr) cudaStreamSynchronize(p->stream);
+  if (p->exec != nullptr) cudaGraphExecDestroy(p->exec);
+  if (p->ws != nullptr) cudaFree(p->ws);
+  if (p->idx != nullptr) cudaFree(p->idx);
+  if (p->base != nullptr) cudaFree(p->base);
+  if (p->ev_in != nullptr) cudaEventDestroy(p->ev_in);
+  if (p->ev_out != nullptr) cudaEventDestroy(p->ev_out);
+  if (p->stream != nullptr) cudaStreamDestroy(p->stream);
+  delete p;
+}
+
+}  // namespace
+}  // namespace gbsgmc
+
+using namespace gbsgmc;
+
+extern "C" int gbsgmc_sgld_glm_plan_create(
+    gbsgmc_plan** out, const gbsgmc_glm* model, int chains, int n,
+    float* w_dev, float* v_dev, float alpha, float lmbd,
+    const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+    const gbsgmc_index_src* index_src, double* U_dev, double* lk_var_dev,
+    float* samples_dev, double* sample_lik_dev, int block_steps,
+    int* status_dev) {
+  if (out == nullptr || model == nullptr || sched == nullptr ||
+      noise == nullptr || index_src == nullptr || w_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "plan_create: null argument");
+  *out = nullptr;
+  if (chains <= 0 || n <= 0 || block_steps <= 0 || block_steps > 100000)
+    return set_error(GBSGMC_ERR_ARG, "plan_create: bad chains/n/block_steps");
+  if (sched->keep_slot_dev != nullptr && samples_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG,
+                     "plan_create: keep table given without sample buffer");
+  gbsgmc_plan* p = new (std::nothrow) gbsgmc_plan();
+  if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "plan_create: out of memory");
+  p->model = *model;
+  p->chains = chains;
+  p->n = n;
+  p->w = w_dev;
+  p->v = v_dev;
+  p->alpha = alpha;
+  p->lmbd = lmbd;
+  p->sched = *sched;
+  p->noise = *noise;
+  p->isrc = *index_src;
+  p->U = U_dev;
+  p->lk_var = lk_var_dev;
+  p->samples = samples_dev;
+  p->sample_lik = sample_lik_dev;
+  p->status = status_dev;
+  p->G = block_steps;
+  const char* env = std::getenv("GBSGMC_NO_GRAPH");
+  p->use_graph = !(env != nullptr && env[0] == '1');
+  int rc = GBSGMC_OK;
+  do {
+    if ((rc = cuda_err(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking),
+                       "plan_create: stream")))
+      break;
+    if ((rc = cuda_err(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming),
+                       "plan_create: event")))
+      break;
+    if ((rc = cuda_err(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming),
+                       "plan_create: event")))
+      break;
+    p->ws_size = glm_ws_bytes(chains, n, model->d);
+    if ((rc = cuda_err(cudaMalloc(&p->ws, p->ws_size), "plan_create: workspace")))
+      break;
+    if ((rc = cuda_err(cudaMalloc(&p->idx, sizeof(int32_t) * static_cast<size_t>(
+                                                   block_steps) * chains * n),
+                       "plan_create: index buffer")))
+      break;
+    if ((rc = cuda_err(cudaMalloc(&p->base, sizeof(int64_t)), "plan_create: counter")))
+      break;
+    if ((rc = cuda_err(cudaMemsetAsync(p->ws, 0, p->ws_size, p->stream),
+                       "plan_create: memset")))
+      break;
+    if ((rc = cuda_err(cudaMemsetAsync(p->base, 0, sizeof(int64_t), p->stream),
+                       "plan_create: memset")))
+      break;
+    if ((rc = glm_prepare())) break;
+    p->slices = glm_default_slices(chains, n);
+    if (p->use_graph) {
+      if ((rc = cuda_err(cudaStreamBeginCapture(p->stream,
+                                                cudaStreamCaptureModeThreadLocal),
+                         "plan_create: begin capture")))
+        break;
+      rc = enqueue_block(p, p->G, p->stream);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(p->stream, &graph);
+      if (rc != GBSGMC_OK) {
+        if (graph != nullptr) cudaGraphDestroy(graph);
+        break;
+      }
+      if ((rc = cuda_err(e, "plan_create: end capture"))) break;
+      rc = cuda_err(cudaGraphInstantiate(&p->exec, graph, 0),
+                    "plan_create: instantiate");
+      cudaGraphDestroy(graph);
+      if (rc) break;
+    }
+    rc = cuda_err(cudaStreamSynchronize(p->stream), "plan_create: sync");
+  } while (false);
+  if (rc != GBSGMC_OK) {
+    release(p);
+    return rc;
+  }
+  *out = p;
+  return GBSGMC_OK;
+}
+
+extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
+                               int64_t steps, gbsgmc_stream_t stream) {
+  if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "plan_run: null plan");
+  if (first_step < 0 || steps < 0)
+    return set_error(GBSGMC_ERR_ARG, "plan_run: negative step");
+  if (steps == 0) return GBSGMC_OK;
+  cudaStream_t us = static_cast<cudaStream_t>(stream);
+  int rc;
+  if ((rc = cuda_err(cudaEventRecord(p->ev_in, us), "plan_run: record"))) return rc;
+  if ((rc = cuda_err(cudaStreamWaitEvent(p->stream, p->ev_in, 0), "plan_run: wait")))
+    return rc;
+  set_counter_kernel<<<1, 1, 0, p->stream>>>(p->base, first_step);
+  if ((rc = check_launch("plan_run: set counter"))) return rc;
+  const int64_t full = steps / p->G;
+  const int rem = static_cast<int>(steps % p->G);
+  for (int64_t b = 0; b < full; ++b) {
+    if (p->use_graph) {
+      if ((rc = cuda_err(cudaGraphLaunch(p->exec, p->stream), "plan_run: graph")))
+        return rc;
+    } else if ((rc = enqueue_block(p, p->G, p->stream))) {
+      return rc;
+    }
+  }
+  if (rem > 0 && (rc = enqueue_block(p, rem, p->stream))) return rc;
+  if ((rc = cuda_err(cudaEventRecord(p->ev_out, p->stream), "plan_run: record")))
+    return rc;
+  return cuda_err(cudaStreamWaitEvent(us, p->ev_out, 0), "plan_run: wait");
+}
+
+extern "C" int64_t gbsgmc_plan_launches(const gbsgmc_plan* p, int64_t steps) {
+  if (p == nullptr || steps <= 0) return 0;
+  const int64_t full = steps / p->G;
+  const int64_t rem = steps % p->G;
+  return 1 + full * (p->G + 2) + (rem > 0 ? rem + 2 : 0);
+}
+
+extern "C" int gbsgmc_plan_destroy(gbsgmc_plan* p) {
+  release(p);
+  return GBSGMC_OK;
+}

@@ -1,0 +1,267 @@
+// Index and noise streams.
+//
+// * gbsgmc_index_draw_pcg64 reproduces numpy's Generator.choice(arange(N), n,
+//   replace=True) bit for bit.  numpy draws each index as a 32-bit Lemire
+//   bounded integer (Lemire 2019, "Fast random integer generation in an
+//   interval"): x = next_uint32(); m = x * N; accept when (m mod 2^32) >=
+//   2^32 mod N, the index being m >> 32.  next_uint32 hands out the low half
+//   of a fresh PCG64 output and keeps the high half for the next call.  The
+//   accept test depends only on the 32-bit value, so a CTA expands 256 PCG64
+//   outputs at once by LCG jump-ahead (Brown 1994, "Random number generation
+//   with arbitrary strides"), tests the 512 halves, and compacts the accepted
+//   ones with a block scan.  The chain's stream state (128-bit LCG state,
+//   buffered half) is advanced exactly as numpy advances it.
+// * gbsgmc_index_draw_philox and gbsgmc_philox_normal use Philox4x32-10.
+#include "common.cuh"
+
+namespace gbsgmc {
+namespace {
+
+constexpr int kDrawThreads = 256;
+
+// Block-wide exclusive scan of small non-negative ints; returns the exclusive
+// prefix and sets *total.  Contains __syncthreads.
+__device__ __forceinline__ int block_excl_scan(int v, int* warp_tot,
+                                               int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  __syncthreads();
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  int before = 0, all = 0;
+#pragma unroll
+  for (int w = 0; w < kDrawThreads / 32; ++w) {
+    const int t = warp_tot[w];
+    before += (w < warp) ? t : 0;
+    all += t;
+  }
+  *total = all;
+  return before + incl - v;
+}
+
+__global__ void __launch_bounds__(kDrawThreads)
+    pcg64_draw_kernel(gbsgmc_pcg64* states, int64_t n_obs, int64_t draws,
+                      int per_step, int32_t* idx, int64_t chain_stride,
+                      int64_t step_stride) {
+  __shared__ Affine pow2[9];  // the LCG map applied 1, 2, 4, ..., 256 times
+  __shared__ int warp_tot[kDrawThreads / 32];
+
+  const int c = blockIdx.x;
+  const int t = threadIdx.x;
+  gbsgmc_pcg64* st = states + c;
+  int32_t* out = idx + static_cast<int64_t>(c) * chain_stride;
+  auto put = [&](int64_t pos, int32_t v) {
+    out[(pos / per_step) * step_stride + pos % per_step] = v;
+  };
+
+  if (draws <= 0) return;
+  if (n_obs == 1) {  // numpy returns the offset without consuming randomness
+    for (int64_t j = t; j < draws; j += kDrawThreads) put(j, 0);
+    return;
+  }
+
+  U128 s{st->state_hi, st->state_lo};
+  const U128 inc{st->inc_hi, st->inc_lo};
+  uint32_t has = st->has_uint32;
+  const uint32_t buffered = st->uinteger;
+  const uint64_t N = static_cast<uint64_t>(n_obs);
+  const uint32_t threshold = static_cast<uint32_t>((1ull << 32) % N);
+
+  if (t == 0) {
+    pow2[0].a = pcg_multiplier();
+    pow2[0].c = inc;
+    for (int i = 1; i < 9; ++i) pow2[i] = compose(pow2[i - 1], pow2[i - 1]);
+  }
+  __syncthreads();
+  // This thread's output is the (t+1)-th LCG step of the round.
+  Affine jump{U128{0, 1}, U128{0, 0}};
+  {
+    const int k = t + 1;
+    for (int i = 0; i < 9; ++i)
+      if ((k >> i) & 1) jump = compose(jump, pow2[i]);
+  }
+  const Affine round_jump = pow2[8];
+
+  int64_t produced = 0;
+  if (has) {  // the half buffered by the previous call comes first
+    const bool acc = static_cast<uint32_t>(buffered * N) >= threshold;
+    if (acc) {
+      if (t == 0) put(0, static_cast<int32_t>((buffered * N) >> 32));
+      produced = 1;
+    }
+    has = 0;
+    if (produced == draws) {
+      __syncthreads();
+      if (t == 0) st->has_uint32 = 0u;
+      return;
+    }
+  }
+
+  for (;;) {
+    const U128 sj = apply(jump, s);
+    const uint64_t o = pcg_output(sj);
+    const uint32_t lo = static_cast<uint32_t>(o);
+    const uint32_t hi = static_cast<uint32_t>(o >> 32);
+    const int a0 = static_cast<uint32_t>(lo * N) >= threshold ? 1 : 0;
+    const int a1 = static_cast<uint32_t>(hi * N) >= threshold ? 1 : 0;
+    const int cnt = a0 + a1;
+    int total;
+    const int excl = block_excl_scan(cnt, warp_tot, &total);
+    const int64_t base = produced + excl;
+    if (a0 && base < draws) put(base, static_cast<int32_t>((lo * N) >> 32));
+    if (a1 && base + a0 < draws)
+      put(base + a0, static_cast<int32_t>((hi * N) >> 32));
+    if (produced + total >= draws) {
+      const int64_t r = draws - 1 - produced;  // rank of the last value used
+      if (cnt > 0 && r >= excl && r < excl + cnt) {
+        const bool last_is_low = a0 && r == excl;
+        st->state_hi = sj.hi;
+        st->state_lo = sj.lo;
+        st->has_uint32 = last_is_low ? 1u : 0u;
+        st->uinteger = hi;
+      }
+      return;
+    }
+    produced += total;
+    s = apply(round_jump, s);
+  }
+}
+
+__global__ void philox_index_kernel(uint64_t seed, int chain_base, int chains,
+                                    const int64_t* base, int64_t first_step,
+                                    int steps,
+                                    int per_step, int64_t n_obs, int32_t* idx,
+                                    int64_t chain_stride,
+                                    int64_t step_stride) {
+  // One thread per pair of draws: a 64-bit uniform per draw keeps the
+  // multiply-shift bias below n_obs / 2^64.
+  const int pairs = (per_step + 1) / 2;
+  const int64_t total = static_cast<int64_t>(chains) * steps * pairs;
+  const uint64_t N = static_cast<uint64_t>(n_obs);
+  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       g < total; g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int p = static_cast<int>(g % pairs);
+    const int64_t cs = g / pairs;
+    const int sidx = static_cast<int>(cs % steps);
+    const int c = static_cast<int>(cs / steps);
+    const int64_t step = (base != nullptr ? *base : 0) + first_step + sidx;
+    const U32x4 r = philox4x32_10(
+        U32x4{static_cast<uint32_t>(p), static_cast<uint32_t>(step),
+              static_cast<uint32_t>(chain_base + c), GBSGMC_TAG_INDEX},
+        static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    const uint64_t u0 = (static_cast<uint64_t>(r.y) << 32) | r.x;
+    const uint64_t u1 = (static_cast<uint64_t>(r.w) << 32) | r.z;
+    int32_t* o = idx + c * chain_stride + sidx * step_stride;
+    const int j0 = 2 * p;
+    o[j0] = static_cast<int32_t>(__umul64hi(u0, N));
+    if (j0 + 1 < per_step) o[j0 + 1] = static_cast<int32_t>(__umul64hi(u1, N));
+  }
+}
+
+__global__ void philox_normal_kernel(uint64_t seed, int chain_base,
+                                     int chains, int64_t step, uint32_t tag,
+                                     int64_t count, float* out,
+                                     int64_t stride) {
+  const int64_t groups = (count + 3) / 4;
+  const int64_t total = groups * chains;
+  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       g < total; g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>(g / groups);
+    const int64_t q = g % groups;
+    float z[4];
+    philox_normal4(seed, static_cast<uint32_t>(q), static_cast<uint32_t>(step),
+                   static_cast<uint32_t>(chain_base + c), tag, z);
+    float* o = out + c * stride + 4 * q;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (4 * q + i < count) o[i] = z[i];
+  }
+}
+
+int grid_for(int64_t work, int threads) {
+  int64_t b = (work + threads - 1) / threads;
+  if (b > 152 * 32) b = 152 * 32;
+  if (b < 1) b = 1;
+  return static_cast<int>(b);
+}
+
+}  // namespace
+
+int launch_philox_index(uint64_t seed, int chain_base, int chains,
+                        const int64_t* base, int64_t first_step, int steps,
+                        int per_step, int64_t n_obs, int32_t* idx,
+                        int64_t chain_stride, int64_t step_stride,
+                        cudaStream_t stream) {
+  const int64_t work =
+      static_cast<int64_t>(chains) * steps * ((per_step + 1) / 2);
+  if (work == 0) return GBSGMC_OK;
+  philox_index_kernel<<<grid_for(work, 256), 256, 0, stream>>>(
+      seed, chain_base, chains, base, first_step, steps, per_step, n_obs, idx,
+      chain_stride, step_stride);
+  return check_launch("index_draw_philox");
+}
+
+}  // namespace gbsgmc
+
+using namespace gbsgmc;
+
+extern "C" int gbsgmc_index_draw_pcg64(gbsgmc_pcg64* states_dev, int chains,
+                                       int64_t n_obs, int64_t draws,
+                                       int per_step, int32_t* idx_dev,
+                                       int64_t chain_stride,
+                                       int64_t step_stride, int* status_dev,
+                                       gbsgmc_stream_t stream) {
+  (void)status_dev;
+  if (states_dev == nullptr || idx_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "index_draw_pcg64: null pointer");
+  if (chains < 0 || draws < 0 || per_step <= 0)
+    return set_error(GBSGMC_ERR_ARG, "index_draw_pcg64: negative size");
+  if (n_obs < 1 || n_obs >= (1ll << 31))
+    return set_error(GBSGMC_ERR_SHAPE,
+                     "index_draw_pcg64: n_obs must be in [1, 2^31), got %lld",
+                     static_cast<long long>(n_obs));
+  if (chains == 0 || draws == 0) return GBSGMC_OK;
+  pcg64_draw_kernel<<<chains, kDrawThreads, 0,
+                      static_cast<cudaStream_t>(stream)>>>(
+      states_dev, n_obs, draws, per_step, idx_dev, chain_stride, step_stride);
+  return check_launch("index_draw_pcg64");
+}
+
+extern "C" int gbsgmc_index_draw_philox(uint64_t seed, int chain_base,
+                                        int chains, int64_t first_step,
+                                        int steps, int per_step, int64_t n_obs,
+                                        int32_t* idx_dev, int64_t chain_stride,
+                                        int64_t step_stride,
+                                        gbsgmc_stream_t stream) {
+  if (idx_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "index_draw_philox: null pointer");
+  if (chains < 0 || steps < 0 || per_step <= 0)
+    return set_error(GBSGMC_ERR_ARG, "index_draw_philox: negative size");
+  if (n_obs < 1 || n_obs >= (1ll << 31))
+    return set_error(GBSGMC_ERR_SHAPE,
+                     "index_draw_philox: n_obs must be in [1, 2^31)");
+  return launch_philox_index(seed, chain_base, chains, nullptr, first_step,
+                             steps, per_step, n_obs, idx_dev, chain_stride,
+                             step_stride, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gbsgmc_philox_normal(uint64_t seed, int chain_base, int chains,
+                                    int64_t step, uint32_t tag, int64_t count,
+                                    float* out_dev, int64_t stride,
+                                    gbsgmc_stream_t stream) {
+  if (out_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "philox_normal: null pointer");
+  if (chains < 0 || count < 0 || stride < count)
+    return set_error(GBSGMC_ERR_ARG, "philox_normal: bad size or stride");
+  const int64_t work = static_cast<int64_t>(chains) * ((count + 3) / 4);
+  if (work == 0) return GBSGMC_OK;
+  philox_normal_kernel<<<grid_for(work, 256), 256, 0,
+                         static_cast<cudaStream_t>(stream)>>>(
+      seed, chain_base, chains, step, tag, count, out_dev, stride);
+  return check_launch("philox_normal");
+}

@@ -1,0 +1,411 @@
+// Elementwise integrator updates over [chains, P] and the reSGLD exchange.
+//
+// Each kernel mirrors the operation order of the reference tree arithmetic so
+// that fp32 results agree to rounding: e.g. the OBABO refresh is
+// sqrt(e^{-f h}) p + sqrt((1 - e^{-f h}) T) (sqrt(m) xi), evaluated as the
+// reference's _momentum_resampling writes it.  Grid: (groups, chains), four
+// parameters per thread so that one Philox call feeds one thread.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace gbsgmc {
+namespace {
+
+constexpr int kThreads = 256;
+
+struct Grid4 {
+  dim3 grid;
+  int64_t groups;
+};
+
+Grid4 grid4(int chains, int64_t P) {
+  Grid4 g;
+  g.groups = (P + 3) / 4;
+  int64_t bx = (g.groups + kThreads - 1) / kThreads;
+  bx = std::min<int64_t>(bx, 65535);
+  g.grid = dim3(static_cast<unsigned>(std::max<int64_t>(bx, 1)),
+                static_cast<unsigned>(chains));
+  return g;
+}
+
+__device__ __forceinline__ float mass_inv(const float* m, int64_t j) {
+  return m != nullptr ? 1.0f / __ldg(m + j) : 1.0f;
+}
+__device__ __forceinline__ float mass_sqrt(const float* m, int64_t j) {
+  return m != nullptr ? sqrtf(__ldg(m + j)) : 1.0f;
+}
+
+__global__ void sgld_update_kernel(int chains, int64_t P, float* x,
+                                   const float* g, float* v, float alpha,
+                                   float lmbd, Sched sched, Noise noise,
+                                   float* samples) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const float h = sched.step_size(k);
+  const float T = sched.temperature(k);
+  const int slot = sched.keep_slot(k);
+  const float noise_scale = sqrtf(2.0f * T * h);
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xi[4];
+    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_SGLD, xi);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      const float gj = g[off + j];
+      const float scaled_gradient = -h * gj;
+      const float scaled_noise = noise_scale * xi[e];
+      float xn;
+      if (v != nullptr) {
+        const float vn = alpha * v[off + j] + (1.0f - alpha) * (gj * gj);
+        const float G = 1.0f / (lmbd + sqrtf(vn));
+        v[off + j] = vn;
+        xn = x[off + j] + ((0.0f + G * scaled_gradient) + sqrtf(G) * scaled_noise);
+      } else {
+        xn = x[off + j] + (scaled_gradient + scaled_noise);
+      }
+      x[off + j] = xn;
+      if (slot >= 0) samples[(static_cast<int64_t>(slot) * chains + c) * P + j] = xn;
+    }
+  }
+}
+
+__device__ __forceinline__ void add_ke(double* ke, int c, double part) {
+  part = warp_sum(part);
+  if ((threadIdx.x & 31) == 0 && ke != nullptr) atomicAdd(ke + c, part);
+}
+
+__global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
+                                   const float* g1, const float* mass,
+                                   float friction, double* ke_start,
+                                   Sched sched, Noise noise) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const float h = sched.step_size(k);
+  const float T = sched.temperature(k);
+  const float permanence = expf(-friction * h);
+  const float keep = sqrtf(permanence);
+  const float inject = sqrtf((1.0f - permanence) * T);
+  const float half = 0.5f * h;
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  double ke = 0.0;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xi[4];
+    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_OBABO_1, xi);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      const float mi = mass_inv(mass, j);
+      float pj = keep * p[off + j] + inject * (mass_sqrt(mass, j) * xi[e]);
+      ke += 0.5 * static_cast<double>(pj) * static_cast<double>(mi * pj);
+      pj = -half * g1[off + j] + pj;
+      p[off + j] = pj;
+      x[off + j] = x[off + j] + h * (mi * pj);
+    }
+  }
+  add_ke(ke_start, c, ke);
+}
+
+__global__ void obabo_second_kernel(int chains, int64_t P, float* p,
+                                    const float* g2, const float* mass,
+                                    float friction, double* ke_end,
+                                    Sched sched, Noise noise) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const float h = sched.step_size(k);
+  const float T = sched.temperature(k);
+  const float permanence = expf(-friction * h);
+  const float keep = sqrtf(permanence);
+  const float inject = sqrtf((1.0f - permanence) * T);
+  const float half = 0.5f * h;
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  double ke = 0.0;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xi[4];
+    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_OBABO_2, xi);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      const float mi = mass_inv(mass, j);
+      float pj = -half * g2[off + j] + p[off + j];
+      ke += 0.5 * static_cast<double>(pj) * static_cast<double>(mi * pj);
+      pj = keep * pj + inject * (mass_sqrt(mass, j) * xi[e]);
+      p[off + j] = pj;
+    }
+  }
+  add_ke(ke_end, c, ke);
+}
+
+__global__ void sghmc_resample_kernel(int chains, int64_t P, float* p,
+                                      const float* mass, Sched sched,
+                                      Noise noise) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xi[4];
+    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_SGHMC_RESAMPLE, xi);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      p[off + j] = mass_sqrt(mass, j) * xi[e];
+    }
+  }
+}
+
+__global__ void sghmc_position_kernel(int chains, int64_t P, float* x,
+                                      float* p, const float* mass,
+                                      const float* fric, float friction,
+                                      Sched sched) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const float h = sched.step_size(k);
+  const int64_t off = static_cast<int64_t>(c) * P;
+  for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       j < P; j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const float f = fric != nullptr ? __ldg(fric + j) : friction;
+    const float pj = p[off + j];
+    const float sm = mass_inv(mass, j) * pj;
+    x[off + j] = x[off + j] + h * sm;
+    p[off + j] = pj + (-h * f) * sm;
+  }
+}
+
+__global__ void sghmc_momentum_kernel(int chains, int64_t P, float* p,
+                                      const float* g, const float* fric,
+                                      float friction, Sched sched,
+                                      Noise noise) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const float h = sched.step_size(k);
+  const float noise_scale = sqrtf(2.0f * h);
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xi[4];
+    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_SGHMC_STEP, xi);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      const float f = fric != nullptr ? __ldg(fric + j) : friction;
+      float pj = p[off + j] + (-h) * g[off + j];
+      pj = pj + f * (noise_scale * xi[e]);
+      p[off + j] = pj;
+    }
+  }
+}
+
+__global__ void resgld_swap_kernel(int pairs, const double* Un,
+                                   const double* Uh, const double* var_n,
+                                   const double* Tn, const double* Th,
+                                   double F, double* ssq, int64_t* kc,
+                                   const double* u_in, uint64_t seed,
+                                   int64_t step, double* log_s_out,
+                                   int32_t* perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= pairs) return;
+  const int64_t k = kc[i] + 1;
+  kc[i] = k;
+  const double sa = 1.0 / static_cast<double>(k);
+  const double s2 = (1.0 - sa) * ssq[i] + sa * var_n[i];
+  ssq[i] = s2;
+  const double dbeta = 1.0 / Tn[i] - 1.0 / Th[i];
+  const double correction = dbeta * s2 / F;
+  const double log_s = dbeta * (Un[i] - Uh[i] - correction);
+  double u;
+  if (u_in != nullptr) {
+    u = u_in[i];
+  } else {
+    const U32x4 r = philox4x32_10(
+        U32x4{static_cast<uint32_t>(i), static_cast<uint32_t>(step), 0u,
+              GBSGMC_TAG_SWAP},
+        static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    const uint64_t bits = ((static_cast<uint64_t>(r.x) >> 5) << 26) |
+                          (static_cast<uint64_t>(r.y) >> 6);
+    u = (static_cast<double>(bits) + 0.5) * (1.0 / 9007199254740992.0);
+  }
+  if (log_s_out != nullptr) log_s_out[i] = log_s;
+  perm[i] = (log(u) < log_s) ? 0 : 1;
+}
+
+__global__ void swap_rows_kernel(int pairs, int64_t width, float* a, float* b,
+                                 const int32_t* perm) {
+  const int i = blockIdx.y;
+  if (perm[i] == 0) return;
+  const int64_t off = static_cast<int64_t>(i) * width;
+  for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       j < width; j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const float t = a[off + j];
+    a[off + j] = b[off + j];
+    b[off + j] = t;
+  }
+}
+
+int check_ec(int chains, int64_t P, const char* what) {
+  if (chains < 0 || P < 0 || chains > 65535)
+    return set_error(GBSGMC_ERR_ARG, "%s: bad chains/P", what);
+  return GBSGMC_OK;
+}
+
+}  // namespace
+}  // namespace gbsgmc
+
+using namespace gbsgmc;
+
+extern "C" int gbsgmc_sgld_update(int chains, int64_t P, float* x_dev,
+                                  const float* g_dev, float* v_dev,
+                                  float alpha, float lmbd,
+                                  const gbsgmc_sched* sched,
+                                  const gbsgmc_noise* noise,
+                                  float* samples_dev, gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "sgld_update");
+  if (rc) return rc;
+  if (!x_dev || !g_dev || !sched || !noise)
+    return set_error(GBSGMC_ERR_ARG, "sgld_update: null pointer");
+  if (sched->keep_slot_dev && !samples_dev)
+    return set_error(GBSGMC_ERR_ARG, "sgld_update: keep table without samples");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, P);
+  sgld_update_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, x_dev, g_dev, v_dev, alpha, lmbd, to_sched(sched),
+      to_noise(noise), samples_dev);
+  return check_launch("sgld_update");
+}
+
+extern "C" int gbsgmc_obabo_first(int chains, int64_t P, float* x_dev,
+                                  float* p_dev, const float* g1_dev,
+                                  const float* mass_dev, float friction,
+                                  double* ke_start_dev,
+                                  const gbsgmc_sched* sched,
+                                  const gbsgmc_noise* noise,
+                                  gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "obabo_first");
+  if (rc) return rc;
+  if (!x_dev || !p_dev || !g1_dev || !sched || !noise)
+    return set_error(GBSGMC_ERR_ARG, "obabo_first: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, P);
+  obabo_first_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, x_dev, p_dev, g1_dev, mass_dev, friction, ke_start_dev,
+      to_sched(sched), to_noise(noise));
+  return check_launch("obabo_first");
+}
+
+extern "C" int gbsgmc_obabo_second(int chains, int64_t P, float* p_dev,
+                                   const float* g2_dev, const float* mass_dev,
+                                   float friction, double* ke_end_dev,
+                                   const gbsgmc_sched* sched,
+                                   const gbsgmc_noise* noise,
+                                   gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "obabo_second");
+  if (rc) return rc;
+  if (!p_dev || !g2_dev || !sched || !noise)
+    return set_error(GBSGMC_ERR_ARG, "obabo_second: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, P);
+  obabo_second_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, p_dev, g2_dev, mass_dev, friction, ke_end_dev,
+      to_sched(sched), to_noise(noise));
+  return check_launch("obabo_second");
+}
+
+extern "C" int gbsgmc_sghmc_resample(int chains, int64_t P, float* p_dev,
+                                     const float* mass_dev,
+                                     const gbsgmc_sched* sched,
+                                     const gbsgmc_noise* noise,
+                                     gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "sghmc_resample");
+  if (rc) return rc;
+  if (!p_dev || !sched || !noise)
+    return set_error(GBSGMC_ERR_ARG, "sghmc_resample: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, P);
+  sghmc_resample_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, p_dev, mass_dev, to_sched(sched), to_noise(noise));
+  return check_launch("sghmc_resample");
+}
+
+extern "C" int gbsgmc_sghmc_position(int chains, int64_t P, float* x_dev,
+                                     float* p_dev, const float* mass_dev,
+                                     const float* friction_dev, float friction,
+                                     const gbsgmc_sched* sched,
+                                     gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "sghmc_position");
+  if (rc) return rc;
+  if (!x_dev || !p_dev || !sched)
+    return set_error(GBSGMC_ERR_ARG, "sghmc_position: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  int64_t bx = std::min<int64_t>((P + kThreads - 1) / kThreads, 65535);
+  dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(chains));
+  sghmc_position_kernel<<<grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, x_dev, p_dev, mass_dev, friction_dev, friction,
+      to_sched(sched));
+  return check_launch("sghmc_position");
+}
+
+extern "C" int gbsgmc_sghmc_momentum(int chains, int64_t P, float* p_dev,
+                                     const float* g_dev,
+                                     const float* friction_dev, float friction,
+                                     const gbsgmc_sched* sched,
+                                     const gbsgmc_noise* noise,
+                                     gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "sghmc_momentum");
+  if (rc) return rc;
+  if (!p_dev || !g_dev || !sched || !noise)
+    return set_error(GBSGMC_ERR_ARG, "sghmc_momentum: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, P);
+  sghmc_momentum_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, p_dev, g_dev, friction_dev, friction, to_sched(sched),
+      to_noise(noise));
+  return check_launch("sghmc_momentum");
+}
+
+extern "C" int gbsgmc_resgld_swap_f64(
+    int pairs, const double* U_normal_dev, const double* U_hot_dev,
+    const double* var_normal_dev, const double* T_normal_dev,
+    const double* T_hot_dev, double F, double* ssq_dev, int64_t* k_dev,
+    const double* u_dev, uint64_t seed, int64_t step, double* log_s_dev,
+    int32_t* perm_dev, gbsgmc_stream_t stream) {
+  if (pairs < 0) return set_error(GBSGMC_ERR_ARG, "resgld_swap: pairs < 0");
+  if (pairs == 0) return GBSGMC_OK;
+  if (!U_normal_dev || !U_hot_dev || !var_normal_dev || !T_normal_dev ||
+      !T_hot_dev || !ssq_dev || !k_dev || !perm_dev)
+    return set_error(GBSGMC_ERR_ARG, "resgld_swap: null pointer");
+  if (!(F != 0.0)) return set_error(GBSGMC_ERR_ARG, "resgld_swap: F == 0");
+  resgld_swap_kernel<<<(pairs + 127) / 128, 128, 0,
+                       static_cast<cudaStream_t>(stream)>>>(
+      pairs, U_normal_dev, U_hot_dev, var_normal_dev, T_normal_dev, T_hot_dev,
+      F, ssq_dev, k_dev, u_dev, seed, step, log_s_dev, perm_dev);
+  return check_launch("resgld_swap");
+}
+
+extern "C" int gbsgmc_swap_rows(int pairs, int64_t width, float* a_dev,
+                                float* b_dev, const int32_t* perm_dev,
+                                gbsgmc_stream_t stream) {
+  if (pairs < 0 || width < 0 || pairs > 65535)
+    return set_error(GBSGMC_ERR_ARG, "swap_rows: bad size");
+  if (pairs == 0 || width == 0) return GBSGMC_OK;
+  if (!a_dev || !b_dev || !perm_dev)
+    return set_error(GBSGMC_ERR_ARG, "swap_rows: null pointer");
+  int64_t bx = std::min<int64_t>((width + kThreads - 1) / kThreads, 4096);
+  dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(pairs));
+  swap_rows_kernel<<<grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      pairs, width, a_dev, b_dev, perm_dev);
+  return check_launch("swap_rows");
+}

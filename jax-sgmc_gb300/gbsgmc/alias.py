@@ -1,0 +1,147 @@
+"""Ready-to-use samplers (mirrors jax_sgmc/alias.py).
+
+Same factory signatures and defaults as the reference; each returns
+``run_fn(*init_samples, init_model_state=None, iterations=1000)`` producing
+one result dict per chain.  ``sgld`` chains on a GLM potential run as one
+fused GPU plan; the other presets step each chain through the C ABI.
+"""
+
+from __future__ import annotations
+
+from functools import partial
+from typing import Any, Union
+
+from . import adaption, data, integrator, io, scheduler, solver
+
+Pytree = Any
+
+
+def _schedule(first_step_size, last_step_size, burn_in, accepted_samples,
+              progress_bar, temperature=None):
+  step_size_schedule = scheduler.polynomial_step_size_first_last(
+      first=first_step_size, last=last_step_size)
+  burn_in_schedule = scheduler.initial_burn_in(burn_in)
+  random_thinning_schedule = scheduler.random_thinning(
+      step_size_schedule, burn_in_schedule, selections=accepted_samples)
+  return scheduler.init_scheduler(step_size=step_size_schedule,
+                                  burn_in=burn_in_schedule,
+                                  thinning=random_thinning_schedule,
+                                  temperature=temperature,
+                                  progress_bar=progress_bar)
+
+
+def sgld(potential_fn, data_loader, cache_size: int = 512,
+         batch_size: int = 32, first_step_size: float = 0.05,
+         last_step_size: float = 0.001, burn_in: int = 0,
+         accepted_samples: int = 1000, rms_prop: bool = False,
+         alpha: float = 0.9, lmbd: float = 1e-5, save_to_numpy: bool = True,
+         progress_bar: bool = True):
+  """Stochastic Gradient Langevin Dynamics (alias.py:30-120)."""
+  random_data = data.random_reference_data(data_loader, cache_size, batch_size)
+  rms = adaption.rms_prop() if rms_prop else None
+  rms_integrator = integrator.langevin_diffusion(potential_fn, random_data,
+                                                 adaption=rms)
+  schedule = _schedule(first_step_size, last_step_size, burn_in,
+                       accepted_samples, progress_bar)
+  saving = io.save(io.MemoryCollector()) if save_to_numpy else None
+  sgld_solver = solver.sgmc(rms_integrator)
+  mcmc = solver.mcmc(sgld_solver, schedule, strategy='map', saving=saving)
+
+  def run_fn(*init_samples, init_model_state: Pytree = None, iterations=1000):
+    init = partial(sgld_solver[0],
+                   adaption_kwargs={'alpha': alpha, 'lmbd': lmbd},
+                   init_model_state=init_model_state)
+    states = [init(s) for s in init_samples]
+    return mcmc(*states, iterations=iterations)
+
+  return run_fn
+
+
+def re_sgld(potential_fn, data_loader, cache_size: int = 512,
+            batch_size: int = 32, temperature: float = 1000.0,
+            first_step_size: float = 0.05, last_step_size: float = 0.001,
+            burn_in: int = 0, accepted_samples: int = 100,
+            save_to_numpy: bool = True, progress_bar: bool = True):
+  """Replica-exchange SGLD with one hot helper chain (alias.py:122-208)."""
+  del progress_bar
+  random_data = data.random_reference_data(data_loader, cache_size, batch_size)
+  resgld_integrator = integrator.langevin_diffusion(potential_fn, random_data)
+  schedule = _schedule(first_step_size, last_step_size, burn_in,
+                       accepted_samples, False,
+                       temperature=scheduler.constant_temperature(1.0))
+  saving = io.save(io.MemoryCollector()) if save_to_numpy else None
+  resgld_solver = solver.parallel_tempering(resgld_integrator)
+  mcmc = solver.mcmc(resgld_solver, schedule, strategy='map', saving=saving)
+
+  def run_fn(*init_samples, init_model_state: Pytree = None, iterations=1000):
+    init = partial(resgld_solver[0], init_model_state=init_model_state)
+    states = [init(*pair) for pair in init_samples]
+    return mcmc(*states, iterations=iterations,
+                schedulers=[{'temperature': {'tau': temperature}}])
+
+  return run_fn
+
+
+def sghmc(potential_fn, data_loader, cache_size: int = 512,
+          batch_size: int = 32, integration_steps: int = 10,
+          friction: Union[float, Pytree] = 1.0, mass: Pytree = None,
+          first_step_size: float = 0.05, last_step_size: float = 0.001,
+          burn_in: int = 0, accepted_samples: int = 1000,
+          adapt_noise_model: bool = False, diagonal_noise: bool = True,
+          save_to_numpy: bool = True, progress_bar: bool = True):
+  """Stochastic Gradient Hamiltonian Monte Carlo (alias.py:451-540)."""
+  if adapt_noise_model:
+    raise NotImplementedError("adapt_noise_model needs fisher_information, "
+                              "which is not part of the GPU hot path")
+  random_data = data.random_reference_data(data_loader, cache_size, batch_size)
+  leapfrog = integrator.friction_leapfrog(potential_fn, random_data,
+                                          friction=friction, const_mass=mass,
+                                          steps=integration_steps)
+  schedule = _schedule(first_step_size, last_step_size, burn_in,
+                       accepted_samples, progress_bar)
+  saving = io.save(io.MemoryCollector()) if save_to_numpy else None
+  sghmc_solver = solver.sgmc(leapfrog)
+  mcmc = solver.mcmc(sghmc_solver, schedule, strategy='map', saving=saving)
+
+  def run_fn(*init_samples, init_model_state: Pytree = None, iterations=1000):
+    init = partial(sghmc_solver[0], init_model_state=init_model_state)
+    states = [init(s) for s in init_samples]
+    return mcmc(*states, iterations=iterations)
+
+  return run_fn
+
+
+def obabo(potential_fn, data_loader, cache_size: int = 512,
+          batch_size: int = 32, integration_steps: int = 10,
+          friction: Union[float, Pytree] = 1.0, mass: Pytree = None,
+          first_step_size: float = 0.05, last_step_size: float = 0.001,
+          burn_in: int = 0, accepted_samples: int = 1000,
+          save_to_numpy: bool = True, progress_bar: bool = True):
+  """Langevin Monte Carlo with partial momentum refreshment (alias.py:542-619)."""
+  random_data = data.random_reference_data(data_loader, cache_size, batch_size)
+  obabo_integrator = integrator.obabo(potential_fn=potential_fn,
+                                      batch_fn=random_data,
+                                      steps=integration_steps,
+                                      friction=friction, const_mass=mass)
+  schedule = _schedule(first_step_size, last_step_size, burn_in,
+                       accepted_samples, progress_bar)
+  saving = io.save(io.MemoryCollector()) if save_to_numpy else None
+  obabo_solver = solver.sgmc(obabo_integrator)
+  mcmc = solver.mcmc(obabo_solver, schedule, strategy='map', saving=saving)
+
+  def run_fn(*init_samples, init_model_state: Pytree = None, iterations=1000):
+    init = partial(obabo_solver[0], init_model_state=init_model_state)
+    states = [init(s) for s in init_samples]
+    return mcmc(*states, iterations=iterations)
+
+  return run_fn
+
+
+def amagold(*args, **kwargs):
+  raise NotImplementedError("AMAGOLD (reversible leapfrog + full-data MH) is "
+                            "not part of the GPU hot path yet")
+
+
+def sggmc(*args, **kwargs):
+  raise NotImplementedError("SGGMC (gradient-guided MH) is not part of the "
+                            "GPU hot path yet")

@@ -1,0 +1,225 @@
+"""Numpy data loaders (mirrors jax_sgmc/data/numpy_loader.py).
+
+``NumpyDataLoader`` keeps the reference's host semantics -- one numpy
+``Generator(PCG64)`` per registered chain, seeded with
+``SeedSequence(seed).spawn(1)[0]`` and ``seed`` defaulting to the chain id
+(numpy_loader.py:231-282), checkpointable through ``save_state`` /
+``load_state`` -- and additionally exposes its arrays resident in HBM.  The
+GPU draws of :mod:`gbsgmc.data.core` continue each chain's PCG64 stream
+bit for bit, so host ``get_batches`` and device draws see the same indices.
+
+``DeviceNumpyDataLoader`` draws indices with Philox4x32-10 on the device
+(the reference uses ``jax.random.randint``, numpy_loader.py:128-141, whose
+threefry stream is not reproduced).
+"""
+
+from __future__ import annotations
+
+import itertools
+import math
+from copy import deepcopy
+from typing import Any, Dict, List, Tuple
+
+import numpy as onp
+
+from .core import (DeviceDataLoader, HostDataLoader, DataLoader,
+                   MiniBatchInformation)
+
+PyTree = Any
+
+
+class NumpyBase(DataLoader):
+
+  def __init__(self, on_device: bool = True, copy=True, **reference_data):
+    super().__init__()
+    observation_counts = []
+    self._reference_data = {}
+    for name, array in reference_data.items():
+      observation_counts.append(len(array))
+      self._reference_data[name] = onp.array(array, copy=copy)
+    if observation_counts:
+      if onp.any(onp.array(observation_counts) != observation_counts[0]):
+        raise ValueError("All reference_data arrays must have the same length "
+                         "in the first dimension.")
+      self._observation_count = observation_counts[0]
+    else:
+      self._observation_count = 0
+
+  @property
+  def reference_data(self):
+    """Returns the reference data as a dictionary."""
+    return self._reference_data
+
+  @property
+  def _format(self):
+    return {name: (tuple(int(s) for s in a.shape[1:]), a.dtype)
+            for name, a in self._reference_data.items()}
+
+  @property
+  def static_information(self):
+    return {"observation_count": self._observation_count}
+
+
+class DeviceNumpyDataLoader(NumpyBase, DeviceDataLoader):
+  """Whole dataset in HBM; random draws by Philox on the device."""
+
+  def __init__(self, copy=True, **reference_data):
+    super().__init__(on_device=True, copy=copy, **reference_data)
+
+  def init_random_data(self, *args, **kwargs) -> PyTree:
+    del args
+    key = kwargs.get("key", 0)
+    key = onp.asarray(key, dtype=onp.uint64).ravel()
+    seed = 0
+    for k in key:
+      seed = ((seed << 32) | (int(k) & 0xFFFFFFFF)) & ((1 << 64) - 1)
+    return seed
+
+  def get_random_data(self, state, batch_size):
+    raise NotImplementedError("use data.random_reference_data: draws happen "
+                              "on the device inside the batch function")
+
+  def get_full_data(self) -> Dict:
+    return self._reference_data
+
+
+class NumpyDataLoader(NumpyBase, HostDataLoader):
+  """Load complete dataset into memory from multiple numpy arrays."""
+
+  def __init__(self, copy=True, **reference_data):
+    super().__init__(on_device=False, copy=copy, **reference_data)
+    self._chains: List = []
+
+  def save_state(self, chain_id: int) -> PyTree:
+    chain_data = self._chains[chain_id]
+    if chain_data['type'] == 'random':
+      data = {key: deepcopy(value)
+              for key, value in chain_data.items() if key != 'rng'}
+      return {'random': (chain_data['rng'].bit_generator.state, data)}
+    elif chain_data['type'] == 'ordered':
+      return {'ordered': chain_data['idx_offset']}
+    raise ValueError(f"Chain type {chain_data['type']} is unknown.")
+
+  def load_state(self, chain_id: int, data) -> None:
+    kind, value = data.popitem()
+    if kind == 'random':
+      rng_state, chain_data = value
+      self._chains[chain_id]['rng'].bit_generator.state = rng_state
+      for key, val in chain_data.items():
+        self._chains[chain_id][key] = val
+    elif kind == 'ordered':
+      self._chains[chain_id]['idx_offset'] = value
+    else:
+      raise ValueError(f"Chain type {kind} is unknown.")
+
+  def register_random_pipeline(self, cache_size: int = 1, mb_size: int = None,
+                               in_epochs: bool = False, shuffle: bool = False,
+                               **kwargs: Any) -> int:
+    """Registers a random chain (numpy_loader.py:231-282)."""
+    if mb_size > self._observation_count:
+      raise ValueError(f"The batch size cannot be bigger than the observation "
+                       f"count. Provided {mb_size} and "
+                       f"{self._observation_count}")
+    if not shuffle and in_epochs:
+      raise ValueError("in_epochs = True can only be used for shuffle = True.")
+    chain_id = len(self._chains)
+    seed = kwargs.get("seed", chain_id)
+    rng = onp.random.default_rng(onp.random.SeedSequence(seed).spawn(1)[0])
+    self._chains.append({'type': 'random', 'rng': rng, 'idx_offset': None,
+                         'in_epochs': in_epochs, 'shuffle': shuffle,
+                         'remaining_samples': 0,
+                         'draws': math.ceil(self._observation_count / mb_size),
+                         'random_indices': None, 'mb_size': mb_size,
+                         'cache_size': cache_size})
+    return chain_id
+
+  def register_ordered_pipeline(self, cache_size: int = 1, mb_size: int = None,
+                                **kwargs) -> int:
+    assert mb_size <= self._observation_count, \
+      (f"The batch size cannot be bigger than the observation count. Provided "
+       f"{mb_size} and {self._observation_count}")
+    chain_id = len(self._chains)
+    self._chains.append({'type': 'ordered', 'rng': None, 'idx_offset': 0,
+                         'mb_size': mb_size, 'cache_size': cache_size})
+    return chain_id
+
+  def get_batches(self, chain_id: int):
+    """Host gather of ``cache_size`` batches (numpy_loader.py:314-340)."""
+    selections_idx, selections_mask = self._get_indices(chain_id)
+    selected = {}
+    for key, data in self._reference_data.items():
+      selected[key] = data[selections_idx]
+    return selected, onp.array(selections_mask, dtype=onp.bool_)
+
+  def _get_indices(self, chain_id: int):
+    chain = self._chains[chain_id]
+    if chain['type'] == 'ordered':
+      index_fn = self._ordered_indices
+    elif chain['in_epochs']:
+      index_fn = self._shuffle_in_epochs
+    elif chain['shuffle']:
+      index_fn = self._shuffle_indices
+    else:
+      index_fn = self._draw_indices
+    indices, masks = list(zip(*[index_fn(chain)
+                                for _ in range(chain['cache_size'])]))
+    return onp.array(indices), onp.array(masks, dtype=onp.bool_)
+
+  def _ordered_indices(self, chain):
+    idcs = onp.arange(chain['mb_size']) + chain['idx_offset']
+    mask = idcs < self._observation_count
+    if chain['idx_offset'] + chain['mb_size'] >= self._observation_count:
+      chain['idx_offset'] = 0
+    else:
+      chain['idx_offset'] += chain['mb_size']
+    return onp.mod(idcs, self._observation_count), mask
+
+  def _draw_indices(self, chain):
+    selections = chain['rng'].choice(onp.arange(0, self._observation_count),
+                                     size=chain['mb_size'], replace=True)
+    return selections, onp.ones(chain['mb_size'], dtype=onp.bool_)
+
+  def _shuffle_indices(self, chain):
+    floor_draws = math.floor(self._observation_count / chain['mb_size'])
+    ceil_draws = floor_draws + 2
+    if chain['remaining_samples'] < chain['mb_size']:
+      new_indices = chain['rng'].choice(onp.arange(0, self._observation_count),
+                                        size=self._observation_count,
+                                        replace=False)
+      if chain['random_indices'] is None:
+        chain['draws'] = 0
+        chain['random_indices'] = onp.zeros(ceil_draws * chain['mb_size'],
+                                            dtype=onp.int_)
+      update_idxs = onp.mod(onp.arange(self._observation_count)
+                            + chain['draws'] * chain['mb_size']
+                            + chain['remaining_samples'],
+                            ceil_draws * chain['mb_size'])
+      chain['random_indices'][update_idxs] = new_indices
+      chain['remaining_samples'] += self._observation_count
+    mask = onp.ones(chain['mb_size'], dtype=onp.bool_)
+    selections_idxs = onp.mod(onp.arange(chain['mb_size'])
+                              + chain['draws'] * chain['mb_size'],
+                              chain['mb_size'] * ceil_draws)
+    selections = onp.copy(chain['random_indices'][selections_idxs])
+    chain['draws'] = (chain['draws'] + 1) % ceil_draws
+    chain['remaining_samples'] -= chain['mb_size']
+    return selections, mask
+
+  def _shuffle_in_epochs(self, chain):
+    ceil_draws = math.ceil(self._observation_count / chain['mb_size'])
+    if chain['draws'] == ceil_draws:
+      new_indices = chain['rng'].choice(onp.arange(0, self._observation_count),
+                                        size=self._observation_count,
+                                        replace=False)
+      if chain['random_indices'] is None:
+        chain['draws'] = 0
+        chain['random_indices'] = onp.zeros(ceil_draws * chain['mb_size'],
+                                            dtype=onp.int_)
+      chain['random_indices'][0:self._observation_count] = new_indices
+      chain['draws'] = 0
+    start_idx = chain['mb_size'] * chain['draws']
+    end_idx = chain['mb_size'] * (chain['draws'] + 1)
+    mask = onp.arange(start_idx, end_idx) < self._observation_count
+    selections = onp.copy(chain['random_indices'][start_idx:end_idx])
+    chain['draws'] += 1
+    return selections, mask

@@ -1,0 +1,192 @@
+"""The fused many-chain SGLD driver.
+
+``run_sgld_glm`` runs C chains of SGLD(+RMSprop) on a GLM potential as one
+``gbsgmc_sgld_glm_plan``: per step ONE kernel launch for all chains (gather,
+likelihood, adjoint, reduction, prior, RMSprop, noise, update, sample
+store), with the index draws of a block of steps in one more launch and the
+block replayed from a CUDA graph.  It replaces ``solver.mcmc``'s per-chain
+``jit(lax.scan)`` over ``langevin_diffusion.update_fn``
+(jax_sgmc/solver.py:152-171, jax_sgmc/integrator.py:860-922).
+"""
+
+from __future__ import annotations
+
+from typing import List, NamedTuple
+
+import numpy as np
+
+from . import _lib, io, scheduler as sched_mod
+from .data.core import RandomBatchFn
+
+DEFAULT_BLOCK_STEPS = 50
+
+# When False, solver.mcmc steps every chain through the per-step C ABI calls
+# instead of the fused plan (used to cross-check the two paths).
+FUSED_ENABLED = True
+
+
+class SgldRun(NamedTuple):
+  w: object            # fp32 [C, d] final positions
+  v: object            # fp32 [C, d] RMSprop state or None
+  U: object            # fp64 [C] potential at the last pre-update position
+  lk_var: object       # fp64 [C]
+  samples: object      # fp32 [S, C, d]
+  sample_lik: object   # fp64 [S, C]
+  launches: int
+
+
+class SgldGlmPlan:
+  """Owns a ``gbsgmc_plan`` and the device buffers baked into it."""
+
+  def __init__(self, potential, dataset, W, V, alpha, lmbd, n, h_tab, t_tab,
+               keep_tab, n_kept, index_src, noise_seed, chain_base=0,
+               block_steps=DEFAULT_BLOCK_STEPS, noise_dev=None):
+    import torch
+    self.potential = potential
+    C, d = W.shape
+    self.C, self.d, self.n = C, d, n
+    self.model, self._keep_alive = potential.model(dataset)
+    self.W = W
+    self.V = V
+    self.U = torch.zeros(C, dtype=torch.float64, device="cuda")
+    self.lk_var = torch.zeros(C, dtype=torch.float64, device="cuda")
+    self.samples = torch.empty((max(n_kept, 1), C, d), dtype=torch.float32,
+                               device="cuda")
+    self.sample_lik = torch.empty((max(n_kept, 1), C), dtype=torch.float64,
+                                  device="cuda")
+    self.n_kept = n_kept
+    self.h_tab, self.t_tab, self.keep_tab = h_tab, t_tab, keep_tab
+    self.status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    self.index_src = index_src
+    self.sched = _lib.sched(step_size_dev=h_tab, temperature_dev=t_tab,
+                            keep_slot_dev=keep_tab)
+    self.noise = _lib.noise(noise_seed, chain_base)
+    handle = _lib.C.c_void_p()
+    _lib.call("gbsgmc_sgld_glm_plan_create", _lib.C.byref(handle), self.model,
+              C, n, _lib.ptr(W), _lib.ptr(V), float(alpha), float(lmbd),
+              self.sched, self.noise, index_src.struct, _lib.ptr(self.U),
+              _lib.ptr(self.lk_var), _lib.ptr(self.samples),
+              _lib.ptr(self.sample_lik), int(block_steps),
+              _lib.ptr(self.status))
+    self.handle = handle
+
+  def run(self, first_step, steps):
+    _lib.call("gbsgmc_plan_run", self.handle, int(first_step), int(steps),
+              _lib.stream_handle())
+
+  def launches(self, steps) -> int:
+    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps)))
+
+  def check_status(self):
+    code = int(self.status.item())
+    if code != 0:
+      raise _lib.GbsgmcError(code, "device status of the SGLD plan")
+
+  def close(self):
+    if getattr(self, "handle", None):
+      _lib.load().gbsgmc_plan_destroy(self.handle)
+      self.handle = None
+
+  def __del__(self):
+    try:
+      self.close()
+    except Exception:  # pragma: no cover - interpreter shutdown
+      pass
+
+
+class IndexSource:
+  """PCG64 streams (device [C] gbsgmc_pcg64, advanced in place) or Philox."""
+
+  def __init__(self, pcg=None, seed=0, chain_base=0):
+    self.pcg = pcg
+    self.struct = _lib.IndexSrc(_lib.ptr(pcg), int(seed) & (2**64 - 1),
+                                int(chain_base), 0)
+
+
+def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
+                 index_src, noise_seed=0, chain_base=0, alpha=0.9, lmbd=1e-5,
+                 block_steps=None) -> SgldRun:
+  """Runs ``iterations`` fused SGLD steps for all chains (W, V updated in
+  place) and returns the final state and the kept samples."""
+  import torch
+  if block_steps is None:
+    block_steps = min(DEFAULT_BLOCK_STEPS, max(1, iterations))
+  h_tab = torch.from_numpy(np.asarray(h, np.float32)).cuda()
+  t_tab = torch.from_numpy(np.asarray(t, np.float32)).cuda()
+  k_tab = torch.from_numpy(np.asarray(keep, np.int32)).cuda()
+  plan = SgldGlmPlan(potential, dataset, W, V, alpha, lmbd, n, h_tab, t_tab,
+                     k_tab, n_kept, index_src, noise_seed, chain_base,
+                     block_steps)
+  try:
+    plan.run(0, iterations)
+    plan.check_status()
+    return SgldRun(W, V, plan.U, plan.lk_var, plan.samples[:n_kept],
+                   plan.sample_lik[:n_kept], plan.launches(iterations))
+  finally:
+    plan.close()
+
+
+def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
+  """Runs the chains through :func:`run_sgld_glm` when they qualify;
+  returns None otherwise (the caller then steps chain by chain)."""
+  import torch
+  from .potential import StochasticPotential
+  meta = getattr(solver, "meta", {})
+  if not FUSED_ENABLED or meta.get("kind") != "sgmc" or schedulers:
+    return None
+  integ = meta.get("integrator")
+  im = getattr(integ, "meta", {})
+  if im.get("kind") != "langevin" or im.get("noise_source") is not None:
+    return None
+  pot = im.get("potential")
+  bfn = im.get("batch_fn")
+  if not isinstance(pot, StochasticPotential) or not states:
+    return None
+  if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn):
+    return None
+  rbf = bfn[1]
+  keys = {s.key for s in states}
+  if len(keys) != 1:
+    return None
+  adapt = [s.adapt_state for s in states]
+  if any(a is None for a in adapt) and not all(a is None for a in adapt):
+    return None
+  chain_ids = [int(s.chain) for s in states]
+  if chain_ids != list(range(chain_ids[0], chain_ids[0] + len(states))):
+    return None
+  if rbf.kind == "host":
+    ds_list = [s.data_state for s in states]
+    if any(d.state is None or d.cached_batches is not None for d in ds_list):
+      return None   # shuffled streams, or draws already consumed
+    pcg = torch.stack([d.state for d in ds_list]).contiguous()
+    index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
+  else:
+    seeds = {s.data_state.state[0] for s in states}
+    if len(seeds) != 1 or any(s.data_state.state[1] != 0 for s in states):
+      return None
+    index_src = IndexSource(seed=seeds.pop(), chain_base=chain_ids[0])
+  dataset = rbf.loader.device_dataset()
+  W = torch.stack([s.latent_variables for s in states]).contiguous()
+  if W.shape[1] != pot.dim(dataset):
+    return None
+  if adapt[0] is not None:
+    V = torch.stack([a.v for a in adapt]).contiguous()
+    alpha, lmbd = adapt[0].alpha, adapt[0].lmbd
+  else:
+    V, alpha, lmbd = None, 0.9, 1e-5
+  h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
+  block = min(rbf.cached_batches_count, DEFAULT_BLOCK_STEPS, max(iterations, 1))
+  res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,
+                     n_kept, index_src, noise_seed=states[0].key,
+                     chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,
+                     block_steps=block)
+  if rbf.kind == "host":
+    for c, s in enumerate(states):   # the streams advanced on the device
+      s.data_state.state.copy_(index_src.pcg[c])
+  out = []
+  for c, s in enumerate(states):
+    out.append(io.postprocess(saving or io.no_save(), n_kept,
+                              res.samples[:, c], s.treedef,
+                              {"likelihood": res.sample_lik[:, c]},
+                              s.model_state))
+  return out

@@ -1,0 +1,305 @@
+"""Integrators (mirrors jax_sgmc/integrator.py) driving the CUDA kernels.
+
+Each factory returns the reference's ``(init_fn, update_fn, get_fn)`` triplet
+for ONE chain, stepping through the C ABI: index draw -> GLM value and
+adjoint -> elementwise integrator kernel.  Chain parameters are flat fp32
+device vectors updated in place (a state passed to ``update_fn`` must not be
+reused afterwards).  ``solver.mcmc`` runs many chains of
+``langevin_diffusion`` in one fused, graph-captured plan instead
+(:mod:`gbsgmc.engine`).
+
+Noise: Philox4x32-10 normals keyed by the chain's ``key`` and indexed by
+(chain id, chain-step counter, stream tag), replacing JAX's threefry
+``random_tree`` (integrator.py:119-135).  ``noise_source(step, chain, tag)``
+may inject explicit normals instead (used to compare trajectories with the
+oracle on identical noise).
+"""
+
+from __future__ import annotations
+
+from typing import Any, Callable, NamedTuple
+
+import numpy as np
+
+from . import _lib, util
+from .adaption import AdaptionStrategy, MassMatrix, RmsPropState
+
+PyTree = Any
+
+
+class IntegratorTriplet(tuple):
+  """``(init_fn, update_fn, get_fn)`` plus what the fused driver needs."""
+
+  def __new__(cls, init_fn, update_fn, get_fn, **meta):
+    obj = super().__new__(cls, (init_fn, update_fn, get_fn))
+    obj.meta = meta
+    return obj
+
+
+class LangevinState(NamedTuple):
+  latent_variables: Any      # fp32 device [P]
+  model_state: Any
+  key: Any                   # Philox seed (int)
+  adapt_state: Any           # RmsPropState or None
+  data_state: Any
+  potential: Any             # fp64 device scalar
+  variance: Any              # fp64 device scalar
+  step: int = 0              # chain-steps taken (noise counter)
+  chain: int = 0             # chain index in the noise counter
+  treedef: Any = None
+
+
+class ObaboState(NamedTuple):
+  positions: Any
+  momentum: Any
+  potential: Any
+  model_state: Any
+  data_state: Any
+  key: Any
+  kinetic_energy_start: Any
+  kinetic_energy_end: Any
+  step: int = 0
+  chain: int = 0
+  treedef: Any = None
+
+
+class LeapfrogState(NamedTuple):
+  positions: Any
+  momentum: Any
+  potential: Any
+  model_state: Any
+  data_state: Any
+  key: Any
+  extra_fields: Any = None
+  step: int = 0
+  chain: int = 0
+  treedef: Any = None
+
+
+def key_to_seed(key) -> int:
+  """An int seed, or a JAX-style 2-word key, as the 64-bit Philox key."""
+  if key is None:
+    return 0
+  a = np.asarray(key).ravel()
+  seed = 0
+  for k in a:
+    seed = ((seed << 32) | (int(k) & 0xFFFFFFFF)) & ((1 << 64) - 1)
+  return seed
+
+
+def _flat(sample):
+  import torch
+  flat, tdef = util.ravel(sample)
+  return torch.from_numpy(flat).cuda(), tdef
+
+
+def _flat_tree_like(tree, P, fill=None):
+  """Mass / friction pytree (or scalar) -> fp32 device [P] or None."""
+  import torch
+  if tree is None:
+    return None
+  if np.isscalar(tree):
+    return torch.full((P,), float(tree), dtype=torch.float32, device="cuda")
+  flat, _ = util.ravel(tree)
+  if flat.size != P:
+    raise ValueError(f"tree has {flat.size} entries, sample has {P}")
+  return torch.from_numpy(flat).cuda()
+
+
+def _noise(seed, chain, buf=None):
+  if buf is not None:
+    return _lib.noise(seed, chain, noise_dev=buf, noise_stride=buf.numel())
+  return _lib.noise(seed, chain)
+
+
+def _injected(noise_source, step, chain, tag):
+  if noise_source is None:
+    return None
+  import torch
+  z = noise_source(step, chain, tag)
+  return torch.as_tensor(z, dtype=torch.float32).reshape(-1).cuda().contiguous()
+
+
+def _eval(potential_fn, w, batch, info, want_grad=True):
+  ds = batch.dataset
+  n_obs = info.observation_count if info is not None else ds.observation_count
+  mask = None
+  return potential_fn.evaluate(w.view(1, -1), batch.indices.view(1, -1), ds,
+                               mask=mask, grad=want_grad,
+                               observation_count=n_obs)
+
+
+def langevin_diffusion(potential_fn, batch_fn, adaption: AdaptionStrategy = None,
+                       noise_source: Callable = None):
+  """SGLD with optional RMSprop (integrator.py:767-924)."""
+  batch_init, batch_get, _ = batch_fn
+
+  def init_fn(init_sample, key=0, adaption_kwargs=None, batch_kwargs=None,
+              init_model_state=None):
+    import torch
+    adaption_kwargs = adaption_kwargs or {}
+    batch_kwargs = batch_kwargs or {}
+    w, tdef = _flat(init_sample)
+    adapt_state = None if adaption is None else adaption.init(w, **adaption_kwargs)
+    data_state = batch_init(**batch_kwargs)
+    chain = int(data_state.chain_id or 0)
+    return LangevinState(
+        latent_variables=w, model_state=init_model_state,
+        key=key_to_seed(key), adapt_state=adapt_state, data_state=data_state,
+        potential=torch.zeros((), dtype=torch.float64, device="cuda"),
+        variance=torch.ones((), dtype=torch.float64, device="cuda"),
+        step=0, chain=chain, treedef=tdef)
+
+  def get_fn(state: LangevinState):
+    return {"variables": state.latent_variables,
+            "likelihood": -state.potential,
+            "model_state": state.model_state}
+
+  def update_fn(state: LangevinState, parameters):
+    data_state, (batch, info) = batch_get(state.data_state, information=True)
+    r = _eval(potential_fn, state.latent_variables, batch, info)
+    w = state.latent_variables
+    v = None if state.adapt_state is None else state.adapt_state.v
+    alpha = 0.9 if state.adapt_state is None else state.adapt_state.alpha
+    lmbd = 1e-5 if state.adapt_state is None else state.adapt_state.lmbd
+    buf = _injected(noise_source, state.step, state.chain, _lib.TAG_SGLD)
+    sch = _lib.sched(step_size=float(parameters.step_size),
+                     temperature=float(parameters.temperature),
+                     offset=state.step)
+    _lib.call("gbsgmc_sgld_update", 1, w.numel(), _lib.ptr(w),
+              _lib.ptr(r.grad), _lib.ptr(v), alpha, lmbd, sch,
+              _noise(state.key, state.chain, buf), None, _lib.stream_handle())
+    return state._replace(data_state=data_state, potential=r.U[0],
+                          variance=r.lk_var[0], step=state.step + 1)
+
+  return IntegratorTriplet(init_fn, update_fn, get_fn, kind="langevin",
+                           potential=potential_fn, batch_fn=batch_fn,
+                           adaption=adaption, noise_source=noise_source)
+
+
+def init_mass(mass) -> MassMatrix:
+  """Diagonal mass (integrator.py:99-116): inverse and square root."""
+  return MassMatrix(inv=1.0 / mass, sqrt=mass ** 0.5)
+
+
+def obabo(potential_fn, batch_fn, steps=10, friction=1.0, const_mass=None,
+          noise_source: Callable = None):
+  """OBABO integrator with two minibatches per step (integrator.py:138-346)."""
+  init_data, get_data, _ = batch_fn
+
+  def init_fn(init_sample, key=None, batch_kwargs=None, init_model_state=None):
+    import torch
+    batch_kwargs = batch_kwargs or {}
+    data_state = init_data(**batch_kwargs)
+    w, tdef = _flat(init_sample)
+    return ObaboState(
+        positions=w, momentum=torch.zeros_like(w),
+        potential=torch.zeros((), dtype=torch.float64, device="cuda"),
+        model_state=init_model_state, data_state=data_state,
+        key=key_to_seed(key),
+        kinetic_energy_start=torch.zeros(1, dtype=torch.float64, device="cuda"),
+        kinetic_energy_end=torch.zeros(1, dtype=torch.float64, device="cuda"),
+        step=0, chain=int(data_state.chain_id or 0), treedef=tdef)
+
+  def integrate(state: ObaboState, parameters, mass=None):
+    x, p = state.positions, state.momentum
+    P = x.numel()
+    m = _flat_tree_like(const_mass, P)
+    data_state = state.data_state
+    step = state.step
+    pot = state.potential
+    for _ in range(steps):
+      sch = _lib.sched(step_size=float(parameters.step_size),
+                       temperature=float(parameters.temperature), offset=step)
+      data_state, (b1, i1) = get_data(data_state, information=True)
+      r1 = _eval(potential_fn, x, b1, i1)
+      buf1 = _injected(noise_source, step, state.chain, _lib.TAG_OBABO_1)
+      _lib.call("gbsgmc_obabo_first", 1, P, _lib.ptr(x), _lib.ptr(p),
+                _lib.ptr(r1.grad), _lib.ptr(m), float(friction),
+                _lib.ptr(state.kinetic_energy_start), sch,
+                _noise(state.key, state.chain, buf1), _lib.stream_handle())
+      data_state, (b2, i2) = get_data(data_state, information=True)
+      r2 = _eval(potential_fn, x, b2, i2)
+      buf2 = _injected(noise_source, step, state.chain, _lib.TAG_OBABO_2)
+      _lib.call("gbsgmc_obabo_second", 1, P, _lib.ptr(p), _lib.ptr(r2.grad),
+                _lib.ptr(m), float(friction),
+                _lib.ptr(state.kinetic_energy_end), sch,
+                _noise(state.key, state.chain, buf2), _lib.stream_handle())
+      pot = 0.5 * (r1.U[0] + r2.U[0])
+      step += 1
+    return state._replace(potential=pot, data_state=data_state, step=step)
+
+  def get_fn(state):
+    return {"variables": state.positions, "energy": state.potential,
+            "model_state": state.model_state}
+
+  return IntegratorTriplet(init_fn, integrate, get_fn, kind="obabo",
+                           potential=potential_fn, batch_fn=batch_fn,
+                           steps=steps, friction=friction,
+                           const_mass=const_mass, noise_source=noise_source)
+
+
+def friction_leapfrog(potential_fn, batch_fn, steps=10, friction=0.25,
+                      const_mass=None, noise_model=None,
+                      noise_source: Callable = None):
+  """Original SGHMC leapfrog (integrator.py:563-765), no noise model."""
+  if noise_model is not None:
+    raise NotImplementedError("noise models (fisher_information) are not part "
+                              "of the GPU hot path")
+  init_data, get_data, _ = batch_fn
+
+  def init_fn(init_sample, key=None, batch_kwargs=None, init_model_state=None):
+    import torch
+    batch_kwargs = batch_kwargs or {}
+    data_state = init_data(**batch_kwargs)
+    w, tdef = _flat(init_sample)
+    return LeapfrogState(
+        positions=w, momentum=w.clone(),
+        potential=torch.zeros((), dtype=torch.float64, device="cuda"),
+        model_state=init_model_state, data_state=data_state,
+        key=key_to_seed(key), step=0, chain=int(data_state.chain_id or 0),
+        treedef=tdef)
+
+  def integrate(state: LeapfrogState, parameters, mass=None):
+    x, p = state.positions, state.momentum
+    P = x.numel()
+    m = _flat_tree_like(const_mass, P)
+    scalar_friction = np.isscalar(friction)
+    fric = None if scalar_friction else _flat_tree_like(friction, P)
+    f = float(friction) if scalar_friction else 0.0
+    step = state.step
+    sch0 = _lib.sched(step_size=float(parameters.step_size),
+                      temperature=float(parameters.temperature), offset=step)
+    buf = _injected(noise_source, step, state.chain, _lib.TAG_SGHMC_RESAMPLE)
+    _lib.call("gbsgmc_sghmc_resample", 1, P, _lib.ptr(p), _lib.ptr(m), sch0,
+              _noise(state.key, state.chain, buf), _lib.stream_handle())
+    data_state = state.data_state
+    pot = state.potential
+    for _ in range(steps):
+      sch = _lib.sched(step_size=float(parameters.step_size),
+                       temperature=float(parameters.temperature), offset=step)
+      _lib.call("gbsgmc_sghmc_position", 1, P, _lib.ptr(x), _lib.ptr(p),
+                _lib.ptr(m), _lib.ptr(fric), f, sch, _lib.stream_handle())
+      data_state, (b, i) = get_data(data_state, information=True)
+      r = _eval(potential_fn, x, b, i)
+      buf = _injected(noise_source, step, state.chain, _lib.TAG_SGHMC_STEP)
+      _lib.call("gbsgmc_sghmc_momentum", 1, P, _lib.ptr(p), _lib.ptr(r.grad),
+                _lib.ptr(fric), f, sch, _noise(state.key, state.chain, buf),
+                _lib.stream_handle())
+      pot = r.U[0]
+      step += 1
+    return state._replace(potential=pot, data_state=data_state, step=step)
+
+  def get_fn(state):
+    return {"variables": state.positions, "energy": state.potential,
+            "model_state": state.model_state}
+
+  return IntegratorTriplet(init_fn, integrate, get_fn, kind="sghmc",
+                           potential=potential_fn, batch_fn=batch_fn,
+                           steps=steps, friction=friction,
+                           const_mass=const_mass, noise_source=noise_source)
+
+
+def reversible_leapfrog(*args, **kwargs):
+  raise NotImplementedError("the AMAGOLD reversible leapfrog is not part of "
+                            "the GPU hot path yet")

@@ -1,0 +1,88 @@
+"""Sample collection (mirrors jax_sgmc/io.py).
+
+The reference streams each kept sample to the host with
+``host_callback.id_tap`` (io.py:626-771).  Here kept samples are written on
+the device by the step kernels into a ``[kept, chains, P]`` buffer (the
+``keep_slot`` table says which step goes to which row) and copied to the
+host once at the end.  The result format is the reference's
+``{'sample_count': S, 'samples': {'variables': pytree of [S, ...], ...}}``
+(io.py:768-769).  ``save(MemoryCollector())`` returns numpy arrays (written
+to ``save_dir/chain_{i}.npz`` when a directory is given); ``no_save()``
+returns device tensors.
+"""
+
+from __future__ import annotations
+
+from pathlib import Path
+from typing import Any, NamedTuple
+
+import numpy as np
+
+from . import util
+
+
+class MemoryCollector:
+  """Collects samples in host memory (io.py:502-619)."""
+
+  def __init__(self, save_dir=None):
+    self._dir = save_dir
+    self._count = 0
+
+  def finalize(self, samples: dict) -> dict:
+    chain_id = self._count
+    self._count += 1
+    if self._dir:
+      out = Path(self._dir)
+      out.mkdir(exist_ok=True, parents=True)
+      flat = {}
+
+      def walk(prefix, t):
+        if isinstance(t, dict):
+          for k, v in t.items():
+            walk(f"{prefix}/{k}" if prefix else str(k), v)
+        elif isinstance(t, (list, tuple)):
+          for i, v in enumerate(t):
+            walk(f"{prefix}/{i}" if prefix else str(i), v)
+        elif t is not None:
+          flat[prefix] = np.asarray(t)
+      walk("", samples)
+      np.savez(out / f"chain_{chain_id}.npz", **flat)
+    return samples
+
+
+class Saving(NamedTuple):
+  kind: str                 # 'memory' | 'device'
+  collector: Any = None
+
+
+def save(data_collector=None, checkpoint_every: int = 0) -> Saving:
+  """Keeps accepted samples and returns them as numpy arrays."""
+  del checkpoint_every
+  return Saving("memory", data_collector or MemoryCollector())
+
+
+def no_save() -> Saving:
+  """Keeps accepted samples on the device (torch tensors)."""
+  return Saving("device", None)
+
+
+def postprocess(saving: Saving, count: int, variables, treedef, extras: dict,
+                model_state=None) -> dict:
+  """Builds one chain's result dict from its device sample buffers."""
+  if saving is None or saving.kind == "device":
+    # Device results: one torch view per leaf of the [count, P] buffer.
+    leaves, o = [], 0
+    for shape in util.leaf_shapes(treedef):
+      n = int(np.prod(shape, dtype=np.int64))
+      leaves.append(variables[:, o:o + n].reshape((count,) + tuple(shape)))
+      o += n
+    var_tree = util.tree_unflatten(treedef, leaves)
+    samples = {"variables": var_tree, **extras, "model_state": model_state}
+    return {"sample_count": count, "samples": samples}
+  host = variables.detach().cpu().numpy()
+  samples = {"variables": util.unravel(treedef, host)}
+  for k, v in extras.items():
+    samples[k] = v.detach().cpu().numpy() if hasattr(v, "detach") else v
+  samples["model_state"] = model_state
+  samples = saving.collector.finalize(samples)
+  return {"sample_count": count, "samples": samples}

@@ -1,0 +1,173 @@
+"""Solvers and the MCMC driver (mirrors jax_sgmc/solver.py).
+
+``mcmc(solver, scheduler, strategy, saving)`` returns ``run(*states,
+schedulers=None, iterations)``.  The reference runs each chain's
+``jit(lax.scan)`` in turn (solver.py:152-171).  Here, when every chain is an
+SGLD chain on a kernel-backed GLM potential, all chains run together in one
+fused, CUDA-graph-captured plan (:func:`gbsgmc.engine.run_sgld_glm`);
+otherwise each chain steps through the per-step C ABI calls.  Results have
+the reference's per-chain format either way.
+"""
+
+from __future__ import annotations
+
+from typing import Any, NamedTuple
+
+import numpy as np
+
+from . import _lib, engine, io, scheduler as sched_mod
+
+
+class SolverTriplet(tuple):
+
+  def __new__(cls, init, update, get, **meta):
+    obj = super().__new__(cls, (init, update, get))
+    obj.meta = meta
+    return obj
+
+
+def sgmc(integrator):
+  """Plain SG-MCMC: integrate without MH step or tempering (solver.py:188-217)."""
+  init_integrator, update_integrator, get_integrator = integrator
+
+  def init(*args, **kwargs):
+    return init_integrator(*args, **kwargs)
+
+  def update(state, schedule):
+    return update_integrator(state, schedule), None
+
+  def get(state):
+    return get_integrator(state)
+
+  return SolverTriplet(init, update, get, kind="sgmc", integrator=integrator)
+
+
+class TemperingState(NamedTuple):
+  normal: Any
+  hot: Any
+  ssq: Any        # fp64 device [1]
+  F: float
+  step: Any       # int64 device [1]
+  key: int
+
+
+def parallel_tempering(integrator, sa_schedule=None):
+  """reSGLD: a normal and a hot chain exchanging states (solver.py:220-299).
+
+  The exchange test runs in FP64 on the device (``gbsgmc_resgld_swap_f64``)
+  with the reference's rule: the pair keeps its states when
+  ``log u < log s`` and exchanges them otherwise (solver.py:283-291).
+  Only the reference's stochastic-approximation schedule 1/n is supported.
+  """
+  if sa_schedule is not None:
+    probe = [sa_schedule(n) for n in (1, 2, 7)]
+    if not np.allclose(probe, [1.0, 0.5, 1 / 7]):
+      raise NotImplementedError("only sa_schedule = 1/n is implemented")
+  init_integrator, update_integrator, get_integrator = integrator
+
+  def init(normal_sample, tempered_sample, ssq_init=0.0, key=0, F=1.0,
+           **kwargs):
+    import torch
+    seed = int(np.asarray(key).ravel()[-1]) if key is not None else 0
+    normal = init_integrator(normal_sample, key=(seed, 1), **kwargs)
+    hot = init_integrator(tempered_sample, key=(seed, 2), **kwargs)
+    return TemperingState(
+        normal, hot,
+        torch.full((1,), float(ssq_init), dtype=torch.float64, device="cuda"),
+        float(F), torch.zeros(1, dtype=torch.int64, device="cuda"), seed)
+
+  def update(state: TemperingState, normal_schedule, hot_schedule,
+             uniform=None):
+    import torch
+    normal = update_integrator(state.normal, normal_schedule)
+    hot = update_integrator(state.hot, hot_schedule)
+    dev = lambda v: torch.tensor([float(v)], dtype=torch.float64, device="cuda")
+    perm = torch.zeros(1, dtype=torch.int32, device="cuda")
+    u = None if uniform is None else dev(uniform)
+    step = int(normal.step)
+    _lib.call("gbsgmc_resgld_swap_f64", 1,
+              _lib.ptr(normal.potential.reshape(1)),
+              _lib.ptr(hot.potential.reshape(1)),
+              _lib.ptr(normal.variance.reshape(1)),
+              _lib.ptr(dev(normal_schedule.temperature)),
+              _lib.ptr(dev(hot_schedule.temperature)), state.F,
+              _lib.ptr(state.ssq), _lib.ptr(state.step), _lib.ptr(u),
+              state.key, step, None, _lib.ptr(perm), _lib.stream_handle())
+    if int(perm.item()) == 1:
+      normal, hot = hot, normal
+    return state._replace(normal=normal, hot=hot), None
+
+  def get(state: TemperingState):
+    return get_integrator(state.normal)
+
+  return SolverTriplet(init, update, get, kind="parallel_tempering",
+                       integrator=integrator)
+
+
+def amagold(*args, **kwargs):
+  raise NotImplementedError("AMAGOLD is not part of the GPU hot path yet")
+
+
+def sggmc(*args, **kwargs):
+  raise NotImplementedError("SGGMC is not part of the GPU hot path yet")
+
+
+def _flat_of(sample_dict):
+  v = sample_dict["variables"]
+  return v.reshape(-1)
+
+
+def mcmc(solver, scheduler, strategy="map", saving=None, loading=None):
+  """Runs the solver for multiple chains and collects the samples."""
+  if strategy not in ("map", "vmap", "pmap"):
+    raise NotImplementedError(f"Strategy {strategy} is unknown. ")
+  _, solver_update, solver_get = solver
+
+  def run_single(state, iterations, schedulers):
+    import torch
+    main_kwargs = {}
+    h, t, keep, n_kept, static = sched_mod.tables(scheduler, iterations,
+                                                  **main_kwargs)
+    init_fn, update_fn, get_fn = scheduler
+    states = [init_fn(iterations)[0]]
+    for kw in (schedulers or []):
+      states.append(init_fn(iterations, **kw)[0])
+    probe = solver_get(state)
+    P = _flat_of(probe).numel()
+    samples = torch.empty((n_kept, P), dtype=torch.float32, device="cuda")
+    extra_key = "likelihood" if "likelihood" in probe else "energy"
+    extra = torch.empty((n_kept,), dtype=torch.float64, device="cuda")
+    for k in range(iterations):
+      schedules = [get_fn(s) for s in states]
+      state, _ = solver_update(state, *schedules)
+      if keep[k] >= 0:
+        got = solver_get(state)
+        samples[keep[k]] = _flat_of(got)
+        extra[keep[k]] = got[extra_key].reshape(())
+      states = [update_fn(s) for s in states]
+    treedef = _treedef_of(state)
+    return io.postprocess(saving or io.no_save(), n_kept, samples, treedef,
+                          {extra_key: extra})
+
+  def run(*states, schedulers=None, iterations=100000):
+    iterations = int(iterations)
+    if loading is not None:
+      raise NotImplementedError("Loading of checkpoints is currently not "
+                                "supported.")
+    states = list(states)
+    fused = engine.try_fused_sgld(solver, scheduler, states, schedulers,
+                                  iterations, saving)
+    if fused is not None:
+      return fused
+    return [run_single(s, iterations, schedulers) for s in states]
+
+  return run
+
+
+def _treedef_of(state):
+  for name in ("treedef",):
+    if hasattr(state, name) and getattr(state, name) is not None:
+      return getattr(state, name)
+  if hasattr(state, "normal"):
+    return _treedef_of(state.normal)
+  raise ValueError("state carries no sample tree definition")

@@ -1,0 +1,399 @@
+"""CPU restatement of jax_sgmc's sampling hot path -- TEST INFRASTRUCTURE ONLY.
+
+Used as the checker by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline; never by the product path.  numpy only.  Each function cites the
+reference (jax_sgmc 0.1.5) file:line it follows; float32 variants follow the
+reference's operation order so that results agree with the fp32 kernels to
+rounding, float64 variants serve as the accuracy oracle.
+"""
+
+from __future__ import annotations
+
+import math
+from typing import NamedTuple
+
+import numpy as np
+
+# ---------------------------------------------------------------------------
+# Index streams
+# ---------------------------------------------------------------------------
+
+
+def loader_rng(seed: int) -> np.random.Generator:
+  """The per-chain generator of NumpyDataLoader.register_random_pipeline
+  (jax_sgmc/data/numpy_loader.py:261-265)."""
+  return np.random.default_rng(np.random.SeedSequence(seed).spawn(1)[0])
+
+
+def loader_draws(rng: np.random.Generator, n_obs: int, mb_size: int,
+                 batches: int) -> np.ndarray:
+  """``batches`` consecutive minibatches of NumpyDataLoader._draw_indices
+  (jax_sgmc/data/numpy_loader.py:382-389), shape [batches, mb_size]."""
+  return np.stack([rng.choice(np.arange(0, n_obs), size=mb_size, replace=True)
+                   for _ in range(batches)])
+
+
+_M128 = (1 << 128) - 1
+_PCG_MULT = 0x2360ED051FC65DA44385DF649FCCF645
+
+
+def _pcg_out(s: int) -> int:
+  hi, lo = s >> 64, s & ((1 << 64) - 1)
+  x, rot = hi ^ lo, s >> 122
+  return ((x >> rot) | (x << ((64 - rot) & 63))) & ((1 << 64) - 1)
+
+
+def pcg64_bounded(state: dict, n_obs: int, count: int):
+  """Restatement of numpy's bounded int64 draws on PCG64 (pure Python ints).
+
+  PCG64 = 128-bit LCG with XSL-RR output (O'Neill 2014); next_uint32 returns
+  the low half of a fresh output and buffers the high half
+  (has_uint32/uinteger); Generator.integers(0, N) for N < 2^32 uses Lemire's
+  bounded method on those 32-bit values (Lemire 2019).  Returns
+  (indices, new_state) with new_state shaped like numpy's state dict.
+  """
+  s = state["state"]["state"]
+  inc = state["state"]["inc"]
+  has = state["has_uint32"]
+  u = state["uinteger"]
+  out = np.empty(count, np.int64)
+  if n_obs == 1:
+    out[:] = 0
+    return out, dict(state)
+  thr = (1 << 32) % n_obs
+  for i in range(count):
+    while True:
+      if has:
+        has, x = 0, u
+      else:
+        s = (s * _PCG_MULT + inc) & _M128
+        o = _pcg_out(s)
+        has, u, x = 1, o >> 32, o & 0xFFFFFFFF
+      m = x * n_obs
+      if (m & 0xFFFFFFFF) >= thr:
+        break
+    out[i] = m >> 32
+  new = {"bit_generator": "PCG64", "state": {"state": s, "inc": inc},
+         "has_uint32": has, "uinteger": u}
+  return out, new
+
+
+# ---------------------------------------------------------------------------
+# Philox4x32-10 (Salmon et al., SC'11) and the production noise mapping
+# ---------------------------------------------------------------------------
+
+_M0, _M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+_W0, _W1 = 0x9E3779B9, 0xBB67AE85
+
+
+def philox4x32_10(ctr, key):
+  """Vectorised Philox4x32-10.  ctr: uint32 [..., 4]; key: (k0, k1)."""
+  c = np.asarray(ctr, dtype=np.uint64) & np.uint64(0xFFFFFFFF)
+  c0, c1, c2, c3 = (c[..., i].copy() for i in range(4))
+  k0, k1 = int(key[0]) & 0xFFFFFFFF, int(key[1]) & 0xFFFFFFFF
+  mask = np.uint64(0xFFFFFFFF)
+  for r in range(10):
+    if r:
+      k0 = (k0 + _W0) & 0xFFFFFFFF
+      k1 = (k1 + _W1) & 0xFFFFFFFF
+    p0 = _M0 * c0
+    p1 = _M1 * c2
+    n0 = ((p1 >> np.uint64(32)) ^ c1 ^ np.uint64(k0)) & mask
+    n1 = p1 & mask
+    n2 = ((p0 >> np.uint64(32)) ^ c3 ^ np.uint64(k1)) & mask
+    n3 = p0 & mask
+    c0, c1, c2, c3 = n0, n1, n2, n3
+  return np.stack([c0, c1, c2, c3], axis=-1).astype(np.uint32)
+
+
+def _open01(v):
+  return ((v.astype(np.uint64) >> np.uint64(8)).astype(np.float64) + 0.5) / 16777216.0
+
+
+def philox_normals(seed: int, chain: int, step: int, tag: int, count: int):
+  """Normals of one chain/step/tag: group g of 4 parameters uses
+  Philox(counter=(g, step, chain, tag), key=seed) and Box-Muller on the pairs
+  (u0,u1), (u2,u3) with u = (top 24 bits + 0.5) / 2^24 (float64)."""
+  groups = (count + 3) // 4
+  ctr = np.zeros((groups, 4), np.uint64)
+  ctr[:, 0] = np.arange(groups)
+  ctr[:, 1] = step & 0xFFFFFFFF
+  ctr[:, 2] = chain & 0xFFFFFFFF
+  ctr[:, 3] = tag
+  r = philox4x32_10(ctr, (seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF))
+  out = np.empty((groups, 4), np.float64)
+  for a, b, i in ((0, 1, 0), (2, 3, 2)):
+    u1, u2 = _open01(r[:, a]), _open01(r[:, b])
+    rad = np.sqrt(-2.0 * np.log(u1))
+    out[:, i] = rad * np.cos(2 * np.pi * u2)
+    out[:, i + 1] = rad * np.sin(2 * np.pi * u2)
+  return out.reshape(-1)[:count]
+
+
+def philox_indices(seed: int, chain: int, step: int, per_step: int, n_obs: int):
+  """Counter-based index draws: pair p uses Philox(counter=(p, step, chain,
+  6), key=seed); draw 2p = floor(((r1<<32)|r0) * N / 2^64), 2p+1 from
+  (r3, r2)."""
+  pairs = (per_step + 1) // 2
+  ctr = np.zeros((pairs, 4), np.uint64)
+  ctr[:, 0] = np.arange(pairs)
+  ctr[:, 1] = step & 0xFFFFFFFF
+  ctr[:, 2] = chain & 0xFFFFFFFF
+  ctr[:, 3] = 6
+  r = philox4x32_10(ctr, (seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF))
+  out = np.empty(2 * pairs, np.int64)
+  for j, (lo, hi) in enumerate(((0, 1), (2, 3))):
+    u = (r[:, hi].astype(object) << 32) | r[:, lo].astype(object)
+    out[j::2] = np.array([(int(x) * n_obs) >> 64 for x in u], dtype=np.int64)
+  return out[:per_step]
+
+
+# ---------------------------------------------------------------------------
+# Likelihood families and the stochastic potential
+# ---------------------------------------------------------------------------
+
+LINEAR_GAUSSIAN, LOGISTIC, LINEAR = 0, 1, 2
+
+
+def glm_lk(family, z, y, sigma=1.0):
+  """Per-observation log-likelihood and dlk/dz (float64)."""
+  z = np.asarray(z, np.float64)
+  y = np.asarray(y, np.float64)
+  if family == LOGISTIC:
+    sp = np.maximum(z, 0.0) + np.log1p(np.exp(-np.abs(z)))
+    return y * z - sp, y - 1.0 / (1.0 + np.exp(-z))
+  if family == LINEAR:
+    return z.copy(), np.ones_like(z)
+  r = y - z
+  return (-0.5 * r * r / sigma ** 2 - math.log(sigma) - 0.5 * math.log(2 * math.pi),
+          r / sigma ** 2)
+
+
+def log_prior(w, prior_scale):
+  """sum_j norm.logpdf(w_j, 0, prior_scale); 0 for prior_scale <= 0."""
+  w = np.asarray(w, np.float64)
+  if prior_scale is None or prior_scale <= 0:
+    return np.zeros(w.shape[:-1]), np.zeros_like(w)
+  s2 = prior_scale ** 2
+  d = w.shape[-1]
+  lp = -0.5 * np.sum(w * w, -1) / s2 - d * (math.log(prior_scale)
+                                           + 0.5 * math.log(2 * math.pi))
+  return lp, -w / s2
+
+
+class Potential(NamedTuple):
+  U: np.ndarray
+  grad: np.ndarray
+  lk: np.ndarray
+  var: np.ndarray
+
+
+def glm_potential(W, X, y, idx, n_obs, family, sigma=1.0, prior_scale=0.0,
+                  temperature=1.0, mask=None) -> Potential:
+  """Minibatch potential and gradient for C chains, float64.
+
+  U = (-N * mean_i lk_i - log p(w)) / T, or with a mask
+  U = (-N/n * sum_i mask_i lk_i - log p(w)) / T
+  (jax_sgmc/potential.py:159-214); var = jnp.var(lk) (integrator.py:880).
+  W [C, d], idx [C, n].
+  """
+  W = np.atleast_2d(np.asarray(W, np.float64))
+  idx = np.atleast_2d(np.asarray(idx))
+  Xb = np.asarray(X, np.float64)[idx]              # [C, n, d]
+  yb = np.asarray(y, np.float64)[idx]              # [C, n]
+  z = np.einsum("cnd,cd->cn", Xb, W)
+  lk, dz = glm_lk(family, z, yb, sigma)
+  n = idx.shape[-1]
+  m = np.ones_like(lk) if mask is None else np.asarray(mask, np.float64).reshape(lk.shape)
+  lp, dlp = log_prior(W, prior_scale)
+  U = (-(n_obs / n) * np.sum(m * lk, -1) - lp) / temperature
+  grad = (-(n_obs / n) * np.einsum("cn,cnd->cd", m * dz, Xb) - dlp) / temperature
+  return Potential(U, grad, lk, np.var(lk, axis=-1))
+
+
+def full_potential(w, X, y, family, sigma=1.0, prior_scale=0.0,
+                   temperature=1.0):
+  """Full-data potential (-sum_i lk_i - log p) / T (potential.py:219-293)."""
+  w = np.asarray(w, np.float64)
+  z = np.asarray(X, np.float64) @ w
+  lk, dz = glm_lk(family, z, y, sigma)
+  lp, dlp = log_prior(w[None], prior_scale)
+  U = (-np.sum(lk) - lp[0]) / temperature
+  g = (-(dz @ np.asarray(X, np.float64)) - dlp[0]) / temperature
+  return U, g
+
+
+def linear_posterior(X, y, sigma, prior_scale):
+  """Closed-form posterior of Bayesian linear regression with known noise:
+  Sigma = (X^T X / s^2 + I / p^2)^-1, mu = Sigma X^T y / s^2."""
+  X = np.asarray(X, np.float64)
+  d = X.shape[1]
+  prec = X.T @ X / sigma ** 2 + np.eye(d) / prior_scale ** 2
+  cov = np.linalg.inv(prec)
+  mu = cov @ (X.T @ np.asarray(y, np.float64)) / sigma ** 2
+  return mu, cov
+
+
+# ---------------------------------------------------------------------------
+# Integrator steps (float32, reference operation order)
+# ---------------------------------------------------------------------------
+
+f32 = np.float32
+
+
+def sgld_step(x, g, v, xi, h, T, alpha=0.9, lmbd=1e-5, rms_prop=True):
+  """langevin_diffusion.update_fn (jax_sgmc/integrator.py:882-912) with
+  rms_prop update-then-get (jax_sgmc/adaption.py:254-291).  Returns (x', v')."""
+  x, g, xi = (np.asarray(a, f32) for a in (x, g, xi))
+  h, T = f32(h), f32(T)
+  scaled_gradient = (-h) * g
+  scaled_noise = np.sqrt(f32(2.0) * T * h, dtype=f32) * xi
+  if not rms_prop:
+    return (x + (scaled_gradient + scaled_noise)).astype(f32), v
+  a = f32(alpha)
+  v = (a * np.asarray(v, f32) + (f32(1.0) - a) * (g * g)).astype(f32)
+  G = (f32(1.0) / (f32(lmbd) + np.sqrt(v, dtype=f32))).astype(f32)
+  upd = (f32(0.0) + G * scaled_gradient) + np.sqrt(G, dtype=f32) * scaled_noise
+  return (x + upd).astype(f32), v
+
+
+def obabo_first(x, p, g1, xi1, h, T, friction, mass=None):
+  """O, KE_start, B, A of obabo._leapfrog_steps (integrator.py:192-241)."""
+  x, p, g1, xi1 = (np.asarray(a, f32) for a in (x, p, g1, xi1))
+  h, T, f = f32(h), f32(T), f32(friction)
+  mi = f32(1.0) if mass is None else (f32(1.0) / np.asarray(mass, f32))
+  ms = f32(1.0) if mass is None else np.sqrt(np.asarray(mass, f32))
+  perm = np.exp(-f * h, dtype=f32)
+  p = np.sqrt(perm, dtype=f32) * p + np.sqrt((f32(1) - perm) * T, dtype=f32) * (ms * xi1)
+  ke = 0.5 * np.sum(p.astype(np.float64) * (mi * p).astype(np.float64), -1)
+  p = (-(f32(0.5) * h)) * g1 + p
+  x = x + h * (mi * p)
+  return x.astype(f32), p.astype(f32), ke
+
+
+def obabo_second(p, g2, xi2, h, T, friction, mass=None):
+  """B, KE_end, O of obabo._leapfrog_steps (integrator.py:243-273)."""
+  p, g2, xi2 = (np.asarray(a, f32) for a in (p, g2, xi2))
+  h, T, f = f32(h), f32(T), f32(friction)
+  mi = f32(1.0) if mass is None else (f32(1.0) / np.asarray(mass, f32))
+  ms = f32(1.0) if mass is None else np.sqrt(np.asarray(mass, f32))
+  p = (-(f32(0.5) * h)) * g2 + p
+  ke = 0.5 * np.sum(p.astype(np.float64) * (mi * p).astype(np.float64), -1)
+  perm = np.exp(-f * h, dtype=f32)
+  p = np.sqrt(perm, dtype=f32) * p + np.sqrt((f32(1) - perm) * T, dtype=f32) * (ms * xi2)
+  return p.astype(f32), ke
+
+
+def sghmc_resample(xi, mass=None):
+  """p = sqrt(M) xi (integrator.py:735-738)."""
+  ms = f32(1.0) if mass is None else np.sqrt(np.asarray(mass, f32))
+  return (ms * np.asarray(xi, f32)).astype(f32)
+
+
+def sghmc_position(x, p, h, friction, mass=None):
+  """x += h M^-1 p; p += (-h f) M^-1 p (integrator.py:608-619)."""
+  x, p = np.asarray(x, f32), np.asarray(p, f32)
+  h = f32(h)
+  f = np.asarray(friction, f32)
+  mi = f32(1.0) if mass is None else (f32(1.0) / np.asarray(mass, f32))
+  sm = mi * p
+  return (x + h * sm).astype(f32), (p + ((-h) * f) * sm).astype(f32)
+
+
+def sghmc_momentum(p, g, xi, h, friction):
+  """p += -h g; p += f sqrt(2h) xi (integrator.py:621-655, no noise model)."""
+  p, g, xi = (np.asarray(a, f32) for a in (p, g, xi))
+  h = f32(h)
+  f = np.asarray(friction, f32)
+  p = p + (-h) * g
+  return (p + f * (np.sqrt(f32(2.0) * h, dtype=f32) * xi)).astype(f32)
+
+
+def resgld_swap(U_n, U_h, var_n, T_n, T_h, ssq, k, u, F=1.0):
+  """solver.parallel_tempering.update exchange step (solver.py:273-291), FP64.
+  Returns (swapped, ssq', k', log_s); swapped is True when NOT log u < log s
+  (lax.cond keeps the pair in its true branch)."""
+  k = k + 1
+  sa = 1.0 / k
+  ssq = (1 - sa) * ssq + sa * var_n
+  dbeta = 1.0 / T_n - 1.0 / T_h
+  log_s = dbeta * (U_n - U_h - dbeta * ssq / F)
+  swapped = not (math.log(u) < log_s)
+  return swapped, ssq, k, log_s
+
+
+# ---------------------------------------------------------------------------
+# Scheduler
+# ---------------------------------------------------------------------------
+
+def polynomial_first_last(first, last, gamma, iterations):
+  """polynomial_step_size_first_last (scheduler.py:494-542), float64."""
+  ginv = 1.0 / gamma
+  apow = (last ** -ginv - first ** -ginv) / (iterations - 1)
+  a = apow ** -gamma
+  b = (first / a) ** -ginv
+  return a * (b + np.arange(iterations)) ** -gamma
+
+
+# ---------------------------------------------------------------------------
+# Trajectories
+# ---------------------------------------------------------------------------
+
+def sgld_glm_trajectory(X, y, w0, idx, xi, h, T, family, sigma=1.0,
+                        prior_scale=0.0, temperature=1.0, rms_prop=True,
+                        alpha=0.9, lmbd=1e-5):
+  """K SGLD steps of C chains with given minibatch indices idx [K, C, n] and
+  injected normals xi [K, C, d]; gradients in float64, updates in float32.
+  Returns (W [K+1, C, d], U [K, C], var [K, C])."""
+  W = np.atleast_2d(np.asarray(w0, f32)).copy()
+  V = np.ones_like(W)
+  K = idx.shape[0]
+  Ws, Us, Vs = [W.copy()], [], []
+  n_obs = X.shape[0]
+  for k in range(K):
+    pot = glm_potential(W, X, y, idx[k], n_obs, family, sigma, prior_scale,
+                        temperature)
+    W, V = sgld_step(W, pot.grad.astype(f32), V, xi[k], h[k], T[k], alpha,
+                     lmbd, rms_prop)
+    Ws.append(W.copy())
+    Us.append(pot.U)
+    Vs.append(pot.var)
+  return np.stack(Ws), np.stack(Us), np.stack(Vs)
+
+
+def sgld_glm_cpu_steps(X, y, W, V, rngs, steps, h, T, family, sigma=1.0,
+                       prior_scale=0.0, temperature=1.0, alpha=0.9,
+                       lmbd=1e-5, noise_rng=None, threads=1):
+  """The reference's SGLD(+RMSprop) hot loop on the CPU in float32 for C
+  chains: per chain and step the loader's index draw (numpy_loader.py:
+  382-389), the host gather (numpy_loader.py:330-340), the GLM potential and
+  gradient, RMSprop and the update.  Used as the timed CPU baseline.  Chains
+  are split over ``threads`` worker threads."""
+  import concurrent.futures as cf
+  C, d = W.shape
+  n_obs = X.shape[0]
+  noise_rng = noise_rng or np.random.default_rng(0)
+  Xf = np.asarray(X, f32)
+  yf = np.asarray(y, f32)
+  inv_p2 = f32(0.0) if not prior_scale else f32(1.0 / prior_scale ** 2)
+
+  def chain_block(cs, k, xi):
+    for c in cs:
+      idx = rngs[c].choice(np.arange(0, n_obs), size=steps_n, replace=True)
+      xb, yb = Xf[idx], yf[idx]
+      z = xb @ W[c]
+      if family == LOGISTIC:
+        dz = yb - f32(1.0) / (f32(1.0) + np.exp(-z))
+      else:
+        dz = (yb - z) / f32(sigma ** 2)
+      g = (-(f32(n_obs / steps_n)) * (dz @ xb) + W[c] * inv_p2) / f32(temperature)
+      W[c], V[c] = sgld_step(W[c], g, V[c], xi[c], h[k], T[k], alpha, lmbd, True)
+
+  steps_n = steps[1]
+  K = steps[0]
+  blocks = np.array_split(np.arange(C), max(1, threads))
+  with cf.ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+    for k in range(K):
+      xi = noise_rng.standard_normal((C, d), dtype=f32)
+      list(ex.map(lambda cs: chain_block(cs, k, xi), blocks))
+  return W, V

@@ -1,0 +1,181 @@
+"""Host-side logic and the C ABI library on the CPU (no GPU needed)."""
+
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+  text = (ROOT / "include" / "gbsgmc.h").read_text()
+  text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+  return sorted(set(re.findall(r"\b(gbsgmc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_builds_loads_and_exports_every_declared_symbol():
+  from gbsgmc import _build, _lib
+  _build.build()
+  lib = _lib.load()
+  names = declared_functions()
+  assert len(names) >= 20
+  for name in names:
+    assert hasattr(lib, name), name
+    assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+  assert lib.gbsgmc_version() == 100
+
+
+def test_argument_validation_without_a_gpu():
+  from gbsgmc import _lib
+  lib = _lib.load()
+  assert lib.gbsgmc_index_draw_pcg64(None, 1, 10, 4, 4, None, 4, 4, None,
+                                     None) == _lib.ERR_ARG
+  assert b"null" in lib.gbsgmc_last_error()
+  assert lib.gbsgmc_glm_value_and_grad(None, 1, 1, None, 1, None, None, None,
+                                       None, None, None, None, 0, None,
+                                       None) == _lib.ERR_ARG
+  assert lib.gbsgmc_resgld_swap_f64(-1, None, None, None, None, None, 1.0,
+                                    None, None, None, 0, 0, None, None,
+                                    None) == _lib.ERR_ARG
+  assert lib.gbsgmc_glm_workspace_bytes(0, 1, 1) == 0
+  assert lib.gbsgmc_glm_workspace_bytes(256, 1024, 256) > 256 * 1024
+
+
+def test_ravel_matches_ravel_pytree_order():
+  from gbsgmc import util
+  tree = {"b": np.arange(6.0).reshape(2, 3), "a": np.float32(7.0),
+          "c": [np.ones(2), (np.zeros(1),)]}
+  flat, tdef = util.ravel(tree)
+  np.testing.assert_array_equal(flat, [7, 0, 1, 2, 3, 4, 5, 1, 1, 0])
+  back = util.unravel(tdef, flat)
+  np.testing.assert_array_equal(back["b"], tree["b"])
+  assert back["c"][1][0].shape == (1,)
+  batched = util.unravel(tdef, np.stack([flat, flat + 1]))
+  assert batched["b"].shape == (2, 2, 3)
+
+
+class TestScheduler:
+  """Ports of tests/test_scheduler.py to the host scheduler."""
+
+  @pytest.mark.parametrize("first,last,gamma,its",
+                           [(1.0, 0.01, 0.33, 100), (0.05, 0.0009, 0.55, 14723),
+                            (1.0, 0.0009, 0.33, 14723), (0.05, 0.01, 0.55, 100)])
+  def test_first_last(self, first, last, gamma, its):
+    from gbsgmc import scheduler
+    sched = scheduler.polynomial_step_size_first_last(first, last, gamma)
+    state = sched.init(its)
+    assert sched.get(state, 0) == pytest.approx(first, rel=1e-5)
+    assert sched.get(state, its - 1) == pytest.approx(last, rel=1e-5)
+
+  @pytest.mark.parametrize("n", [123, 243])
+  def test_initial_burn_in(self, n):
+    from gbsgmc import scheduler
+    burn_in = scheduler.initial_burn_in(n=n)
+    state, _ = burn_in.init(1000)
+    for idx in range(n):
+      assert burn_in.get(state, idx) == 0.0
+      state = burn_in.update(state, idx)
+    assert burn_in.get(state, n + 1) == 1.0
+
+  def test_tables_keep_slots(self):
+    from gbsgmc import scheduler
+    ss = scheduler.polynomial_step_size_first_last(0.05, 0.001)
+    bi = scheduler.initial_burn_in(30)
+    th = scheduler.random_thinning(ss, bi, selections=20)
+    sched = scheduler.init_scheduler(step_size=ss, burn_in=bi, thinning=th)
+    h, t, keep, n_kept, static = scheduler.tables(sched, 100)
+    assert n_kept == 20 == static.samples_collected
+    assert np.all(keep[:30] == -1)
+    assert sorted(keep[keep >= 0]) == list(range(20))
+    assert h[0] == pytest.approx(0.05, rel=1e-5)
+    assert np.all(t == 1.0)
+
+  def test_random_thinning_respects_burn_in(self):
+    from gbsgmc import scheduler
+    accepted = np.random.default_rng(0).random(100) < 0.3
+    burn_in = scheduler.specific_scheduler(lambda *a: (None, int(accepted.sum())),
+                                           lambda *a, **k: None,
+                                           lambda _, it, **k: float(accepted[it]))
+    step = scheduler.polynomial_step_size(a=1.0, b=1.0, gamma=1.0)
+    sel = int(0.5 * accepted.sum())
+    thin = scheduler.random_thinning(step, burn_in, selections=sel)
+    state, _ = thin.init(100)
+    picked = [i for i in range(100) if thin.get(state, i)]
+    assert len(picked) == sel and all(accepted[i] for i in picked)
+
+
+class TestNumpyLoader:
+  """Host semantics of NumpyDataLoader (tests/test_data.py)."""
+
+  def loader(self):
+    from gbsgmc.data import NumpyDataLoader
+    return NumpyDataLoader(ordered_indices=np.arange(50), x=np.ones((50, 3)))
+
+  def test_invalid_arguments_raise(self):
+    from gbsgmc import data
+    loader = self.loader()
+    with pytest.raises(ValueError):
+      loader.register_random_pipeline(cache_size=2, mb_size=51)
+    with pytest.raises(ValueError):
+      loader.register_random_pipeline(cache_size=2, mb_size=3, in_epochs=True)
+    with pytest.raises(ValueError):
+      data.random_reference_data(loader, 1, 51)
+    with pytest.raises(ValueError):
+      data.random_reference_data(loader, 0, 5)
+    with pytest.raises(ValueError):
+      data.NumpyDataLoader(a=np.zeros(3), b=np.zeros(4))
+
+  def test_seeding(self):
+    loader = self.loader()
+    a1 = loader.register_random_pipeline(1, 1, seed=1)
+    a2 = loader.register_random_pipeline(1, 1, seed=1)
+    b = loader.register_random_pipeline(1, 1, seed=2)
+    ga, gb, gc = (loader.get_batches(c)[0]["ordered_indices"] for c in (a1, a2, b))
+    assert ga == gb and gc != gb
+
+  @pytest.mark.parametrize("shuffle,in_epochs", [(False, False), (True, False), (True, True)])
+  def test_cache_size_order(self, shuffle, in_epochs):
+    loader = self.loader()
+    small = loader.register_random_pipeline(3, 2, seed=0, shuffle=shuffle,
+                                            in_epochs=in_epochs)
+    big = loader.register_random_pipeline(5, 2, seed=0, shuffle=shuffle,
+                                          in_epochs=in_epochs)
+    sb, _ = loader.get_batches(small)
+    bb, _ = loader.get_batches(big)
+    np.testing.assert_array_equal(sb["ordered_indices"], bb["ordered_indices"][:3])
+
+  @pytest.mark.parametrize("shuffle,in_epochs", [(False, False), (True, False), (True, True)])
+  def test_checkpoint(self, shuffle, in_epochs):
+    loader = self.loader()
+    a = loader.register_random_pipeline(3, 2, shuffle=shuffle, in_epochs=in_epochs)
+    for _ in range(8):
+      loader.get_batches(a)
+    ck = loader.save_state(a)
+    want = loader.get_batches(a)
+    b = loader.register_random_pipeline(3, 2, shuffle=shuffle, in_epochs=in_epochs)
+    loader.load_state(b, ck)
+    got = loader.get_batches(b)
+    np.testing.assert_array_equal(want[0]["ordered_indices"], got[0]["ordered_indices"])
+    np.testing.assert_array_equal(want[1], got[1])
+
+
+def test_potential_rejects_arbitrary_callables():
+  from gbsgmc import likelihoods as L, potential
+  with pytest.raises(TypeError):
+    potential.minibatch_potential(lambda w: 0.0, L.Logistic())
+  with pytest.raises(TypeError):
+    potential.minibatch_potential(L.FlatPrior(), lambda w, x: 0.0)
+  with pytest.raises(NotImplementedError):
+    potential.minibatch_potential(L.FlatPrior(), L.Logistic(), strategy="smap")
+  with pytest.raises(ValueError):
+    L.LinearGaussian(sigma=0.0)
+
+
+def test_unported_presets_raise():
+  from gbsgmc import alias, adaption
+  with pytest.raises(NotImplementedError):
+    alias.amagold()
+  with pytest.raises(NotImplementedError):
+    adaption.fisher_information()

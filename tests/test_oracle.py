@@ -1,0 +1,191 @@
+"""Pins the CPU oracle against the reference's own call sites, known-answer
+tests and the golden fixtures (CPU only)."""
+
+import itertools
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import sgmc_oracle as O
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def words_to_state(w):
+  w = [int(x) for x in w]
+  return {"bit_generator": "PCG64",
+          "state": {"state": (w[0] << 64) | w[1], "inc": (w[2] << 64) | w[3]},
+          "has_uint32": w[4], "uinteger": w[5]}
+
+
+@pytest.fixture(scope="module")
+def streams():
+  return np.load(GOLDEN / "index_streams.npz")
+
+
+@pytest.mark.parametrize("seed,N,n", itertools.product(range(8), (10_000, 1_000_000),
+                                                       (128, 1024)))
+def test_golden_streams_match_reference_loader(streams, seed, N, n):
+  """The fixture is the reference loader's own draw (numpy_loader.py:382-389)."""
+  key = f"s{seed}_N{N}_n{n}"
+  rng = O.loader_rng(seed)
+  np.testing.assert_array_equal(O.loader_draws(rng, N, n, 3), streams[key + "_idx"])
+
+
+@pytest.mark.parametrize("seed,N,n", [(0, 10_000, 128), (3, 1_000_000, 1024),
+                                      (7, 1_000_000, 128), (5, 10_000, 1024)])
+def test_pcg64_restatement_matches_golden(streams, seed, N, n):
+  key = f"s{seed}_N{N}_n{n}"
+  before = words_to_state(streams[key + "_before"])
+  idx, after = O.pcg64_bounded(before, N, 3 * n)
+  np.testing.assert_array_equal(idx.reshape(3, n), streams[key + "_idx"])
+  want = words_to_state(streams[key + "_after"])
+  assert after["state"] == want["state"]
+  assert after["has_uint32"] == want["has_uint32"]
+  assert after["uinteger"] == want["uinteger"]
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 10, 12345677, 2**31 - 1, 3 * 10**9])
+def test_pcg64_restatement_edge_ranges(N):
+  rng = O.loader_rng(11)
+  st = rng.bit_generator.state
+  want = rng.integers(0, N, 777, dtype=np.int64)
+  got, new = O.pcg64_bounded(st, N, 777)
+  np.testing.assert_array_equal(got, want)
+  assert new["state"] == rng.bit_generator.state["state"]
+
+
+def test_seeding_and_cache_size_order():
+  """Same seed -> same draws (test_data.py:255-274); the cache size does not
+  change the order (test_data.py:281-297): the stream is consecutive draws."""
+  a = O.loader_draws(O.loader_rng(1), 50, 2, 5)
+  b = O.loader_draws(O.loader_rng(1), 50, 2, 3)
+  c = O.loader_draws(O.loader_rng(2), 50, 2, 3)
+  np.testing.assert_array_equal(a[:3], b)
+  assert not np.array_equal(b, c)
+
+
+def test_philox_kat():
+  for case in json.loads((GOLDEN / "philox_kat.json").read_text()):
+    out = O.philox4x32_10(np.array([case["ctr"]], np.uint64), case["key"])[0]
+    assert [int(x) for x in out] == case["out"]
+
+
+def test_philox_normals_are_standard():
+  z = O.philox_normals(1234, 3, 9, 0, 200_000)
+  assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
+
+
+def test_philox_indices_in_range():
+  idx = O.philox_indices(7, 2, 5, 1001, 999_983)
+  assert idx.min() >= 0 and idx.max() < 999_983 and idx.size == 1001
+
+
+@pytest.mark.parametrize("case", json.loads((GOLDEN / "potential_kat.json").read_text()))
+def test_linear_potential_closed_form(case):
+  """tests/test_potential.py:66-92 restated: lk = sum(sample * x)."""
+  obs, dim = case["obs"], case["dim"]
+  X = np.tile(np.arange(4.0), (dim, 1))
+  pot = O.glm_potential(np.ones(4), X, np.zeros(dim), np.arange(dim)[None],
+                        obs, O.LINEAR)
+  assert pot.U[0] == pytest.approx(case["U_flat_prior"], rel=1e-12)
+  # the reference's prior sum(sample) = 4 enters as -4
+  assert pot.U[0] - 4.0 == pytest.approx(case["U_sum_prior"], rel=1e-12)
+
+
+@pytest.mark.parametrize("obs,dim", list(itertools.product([7, 11], [3, 5])))
+def test_zero_potential(obs, dim):
+  """tests/test_potential.py:95-122: zero likelihood gives exactly -0.0."""
+  rng = np.random.default_rng(0)
+  X = rng.exponential(size=(obs, dim))
+  pot = O.glm_potential(np.zeros(dim), X, np.zeros(obs), np.arange(obs)[None],
+                        obs, O.LINEAR)
+  assert pot.U[0] == 0.0
+  assert np.all(pot.grad == -1.0 * X.sum(0))  # -N/n * sum x_i
+
+
+@pytest.mark.parametrize("family", [O.LINEAR_GAUSSIAN, O.LOGISTIC])
+def test_gradient_finite_differences(family):
+  rng = np.random.default_rng(5)
+  X = rng.normal(size=(50, 6))
+  y = rng.integers(0, 2, 50).astype(float) if family == O.LOGISTIC else rng.normal(size=50)
+  w = rng.normal(size=(1, 6)) * 0.3
+  idx = rng.integers(0, 50, (1, 20))
+  pot = O.glm_potential(w, X, y, idx, 50, family, 0.7, 2.0, 1.3)
+  eps = 1e-6
+  for j in range(6):
+    wp, wm = w.copy(), w.copy()
+    wp[0, j] += eps
+    wm[0, j] -= eps
+    fd = (O.glm_potential(wp, X, y, idx, 50, family, 0.7, 2.0, 1.3).U[0]
+          - O.glm_potential(wm, X, y, idx, 50, family, 0.7, 2.0, 1.3).U[0]) / (2 * eps)
+    assert fd == pytest.approx(pot.grad[0, j], rel=1e-6, abs=1e-6)
+
+
+@pytest.mark.parametrize("obs,dim,mb", list(itertools.product([7, 11], [3, 5], [2, 3])))
+def test_full_equals_minibatch_over_all(obs, dim, mb):
+  """tests/test_potential.py:299-333: full potential == minibatch potential
+  over all observations."""
+  rng = np.random.default_rng(obs * dim)
+  X = rng.exponential(size=(obs, dim))
+  y = rng.normal(size=obs)
+  w = rng.normal(size=dim)
+  mb_pot = O.glm_potential(w, X, y, np.arange(obs)[None], obs,
+                           O.LINEAR_GAUSSIAN, 0.5, 3.0)
+  U, g = O.full_potential(w, X, y, O.LINEAR_GAUSSIAN, 0.5, 3.0)
+  assert U == pytest.approx(mb_pot.U[0], rel=1e-12)
+  np.testing.assert_allclose(g, mb_pot.grad[0], rtol=1e-12)
+
+
+def test_variance_matches_single_observation_evaluations():
+  """tests/test_potential.py:336-367."""
+  rng = np.random.default_rng(3)
+  X = rng.normal(size=(9, 4))
+  y = rng.normal(size=9)
+  w = rng.normal(size=4)
+  pot = O.glm_potential(w, X, y, np.arange(9)[None], 9, O.LINEAR_GAUSSIAN, 0.5)
+  singles = [O.glm_potential(w, X, y, np.array([[i]]), 1, O.LINEAR_GAUSSIAN,
+                             0.5).lk[0, 0] for i in range(9)]
+  assert pot.var[0] == pytest.approx(np.var(singles), rel=1e-12)
+
+
+@pytest.mark.parametrize("first,last,gamma,its",
+                         itertools.product([1.0, 0.05], [0.01, 0.0009],
+                                           [0.33, 0.55], [100, 14723]))
+def test_step_size_first_last(first, last, gamma, its):
+  """tests/test_scheduler.py:83-102 (rtol 1e-5)."""
+  h = O.polynomial_first_last(first, last, gamma, its)
+  assert h[0] == pytest.approx(first, rel=1e-5)
+  assert h[-1] == pytest.approx(last, rel=1e-5)
+
+
+def test_sgld_rmsprop_step_against_formula():
+  rng = np.random.default_rng(0)
+  x, g, xi = rng.normal(size=(3, 8)).astype(np.float32)
+  v = np.ones(8, np.float32)
+  x1, v1 = O.sgld_step(x, g, v, xi, 1e-3, 1.0, 0.9, 1e-5, True)
+  v_ref = 0.9 * v + 0.1 * g * g
+  G = 1 / (1e-5 + np.sqrt(v_ref))
+  x_ref = x - 1e-3 * G * g + np.sqrt(G) * np.sqrt(2e-3) * xi
+  np.testing.assert_allclose(v1, v_ref, rtol=1e-6)
+  np.testing.assert_allclose(x1, x_ref, rtol=1e-5, atol=1e-6)
+
+
+def test_swap_rule_follows_reference_cond():
+  """solver.py:283-291: lax.cond(log_u < log_s, keep, exchange)."""
+  sw, ssq, k, log_s = O.resgld_swap(10.0, 12.0, 0.5, 1.0, 10.0, 0.0, 0, 0.5)
+  assert k == 1 and ssq == pytest.approx(0.5)
+  assert log_s == pytest.approx(0.9 * (10.0 - 12.0 - 0.9 * 0.5))
+  assert sw == (not (math.log(0.5) < log_s))
+
+
+def test_linear_posterior_is_the_normal_equations():
+  rng = np.random.default_rng(1)
+  X = rng.normal(size=(200, 3))
+  y = X @ np.array([1.0, -2.0, 0.5]) + 0.1 * rng.normal(size=200)
+  mu, cov = O.linear_posterior(X, y, 0.1, 1e6)
+  np.testing.assert_allclose(mu, np.linalg.lstsq(X, y, rcond=None)[0], rtol=1e-6)
+  assert np.all(np.linalg.eigvalsh(cov) > 0)
