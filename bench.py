@@ -201,48 +201,107 @@ def run_reference(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 
+class Setup:
+  """Data resident in HBM, the potential, and the chains of this rank."""
+
+  def __init__(self, rank):
+    import torch
+    from gbsgmc import _build, _lib, data, likelihoods as L, potential
+    _build.build()
+    self.lib = _lib.load()
+    self.X, self.y = make_data()
+    self.loader = data.NumpyDataLoader(x=self.X, y=self.y)
+    self.ds = self.loader.device_dataset()
+    self.pot = potential.minibatch_potential(L.GaussianPrior(1.0), L.Logistic(),
+                                             strategy="vmap")
+    self.chain_base = rank * CHAINS
+    self.W = torch.zeros((CHAINS, D), dtype=torch.float32, device="cuda")
+    self.V = torch.ones((CHAINS, D), dtype=torch.float32, device="cuda")
+
+  def plan(self, total):
+    import torch
+    from gbsgmc import engine
+    h, T, keep, n_kept, _ = step_tables(total)
+    words = np.array([pcg_words(self.chain_base + c) for c in range(CHAINS)],
+                     np.uint64).view(np.int64)
+    self.pcg = torch.from_numpy(words.copy()).cuda()
+    self.tabs = [torch.from_numpy(a).cuda() for a in (h, T, keep)]
+    return engine.SgldGlmPlan(
+        self.pot, self.ds, self.W, self.V, 0.9, 1e-5, MB, *self.tabs, n_kept,
+        engine.IndexSource(pcg=self.pcg, chain_base=self.chain_base),
+        noise_seed=0, chain_base=self.chain_base, block_steps=50)
+
+
+class FusedLauncher:
+  """Direct launches of the fused step kernel on torch's current stream."""
+
+  def __init__(self, s):
+    import torch
+    from gbsgmc import _lib
+    self._lib = _lib
+    self.ws = s.pot.workspace(CHAINS, MB, D)
+    self.status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    self.idx = torch.empty((8, CHAINS, MB), dtype=torch.int32, device="cuda")
+    self.stream = _lib.stream_handle()
+    _lib.call("gbsgmc_index_draw_philox", 99, 0, CHAINS, 0, 8, MB, N_OBS,
+              _lib.ptr(self.idx), MB, CHAINS * MB, self.stream)
+    self.model, self._keep = s.pot.model(s.ds)
+    self.W, self.V = s.W.clone(), s.V.clone()
+    self.sched = _lib.sched(step_size=1e-5, temperature=1.0, offset=0)
+    self.noise = _lib.noise(seed=5)
+
+  def __call__(self, i):
+    L = self._lib
+    L.call("gbsgmc_sgld_glm_step", self.model, CHAINS, MB, L.ptr(self.idx[i % 8]),
+           MB, L.ptr(self.W), L.ptr(self.V), 0.9, 1e-5, self.sched, self.noise,
+           None, None, None, None, L.ptr(self.ws), self.ws.numel(),
+           L.ptr(self.status), self.stream)
+
+
+def kernel_only(args):
+  """A short run for profilers: three plan steps, ten more, then five direct
+  launches of the fused step kernel."""
+  import torch
+  rank, _, local = dist_env()
+  torch.cuda.set_device(local)
+  s = Setup(rank)
+  plan = s.plan(args.warmup + 10)
+  plan.run(0, args.warmup)
+  plan.run(args.warmup, 10)
+  torch.cuda.synchronize()
+  plan.check_status()
+  plan.close()
+  f = FusedLauncher(s)
+  for i in range(5):
+    f(i)
+  torch.cuda.synchronize()
+  assert int(f.status.item()) == 0
+
+
 def run_gbsgmc(args):
   import torch
   import torch.distributed as dist
-  from gbsgmc import (_build, _lib, alias, data, engine, likelihoods as L,
-                      potential)
+  from gbsgmc import _lib, alias
   rank, world, local = dist_env()
   torch.cuda.set_device(local)
   if world > 1:
     dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-  _build.build()
-  lib = _lib.load()
 
   def barrier():
     if world > 1:
       dist.barrier()
     torch.cuda.synchronize()
 
-  X, y = make_data()
-  loader = data.NumpyDataLoader(x=X, y=y)
-  ds = loader.device_dataset()
-  pot = potential.minibatch_potential(L.GaussianPrior(1.0), L.Logistic(),
-                                      strategy="vmap")
-  chain_base = rank * CHAINS
-  total = args.warmup + args.steps
-  h, T, keep, n_kept, _ = step_tables(total)
-  pcg = torch.tensor(np.array([pcg_words(chain_base + c) for c in range(CHAINS)],
-                              np.uint64).view(np.int64), device="cuda")
-  W = torch.zeros((CHAINS, D), dtype=torch.float32, device="cuda")
-  V = torch.ones((CHAINS, D), dtype=torch.float32, device="cuda")
-  h_t = torch.from_numpy(h).cuda()
-  T_t = torch.from_numpy(T).cuda()
-  k_t = torch.from_numpy(keep).cuda()
-  plan = engine.SgldGlmPlan(pot, ds, W, V, 0.9, 1e-5, MB, h_t, T_t, k_t, n_kept,
-                            engine.IndexSource(pcg=pcg, chain_base=chain_base),
-                            noise_seed=0, chain_base=chain_base, block_steps=50)
+  s = Setup(rank)
+  plan = s.plan(args.warmup + args.steps)
 
-  # Warm-up, then exactly K timed steps.
+  # W untimed warm-up steps, then exactly K timed steps (device events).
   plan.run(0, args.warmup)
   barrier()
   clocks = Clocks(local)
   clocks.start()
-  start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  start = torch.cuda.Event(enable_timing=True)
+  end = torch.cuda.Event(enable_timing=True)
   barrier()
   start.record()
   plan.run(args.warmup, args.steps)
@@ -257,55 +316,40 @@ def run_gbsgmc(args):
     ms = float(t.item())
   value = world * CHAINS * args.steps / (ms / 1e3)
   launches = plan.launches(args.steps)
-  finite = bool(torch.isfinite(W).all().item())
+  finite = bool(torch.isfinite(s.W).all().item())
   plan.close()
 
-  # The fused step kernel alone: average launch time on the launching stream.
-  ws = pot.workspace(CHAINS, MB, D)
-  status = torch.zeros(1, dtype=torch.int32, device="cuda")
-  idx_buf = torch.empty((8, CHAINS, MB), dtype=torch.int32, device="cuda")
-  _lib.call("gbsgmc_index_draw_philox", 99, 0, CHAINS, 0, 8, MB, N_OBS,
-            _lib.ptr(idx_buf), MB, CHAINS * MB, _lib.stream_handle())
-  m, keep_alive = pot.model(ds)
-  Wk, Vk = W.clone(), V.clone()
-  sch = _lib.sched(step_size=1e-5, temperature=1.0, offset=0)
-  nz = _lib.noise(seed=5)
-  stream = _lib.stream_handle()
-
-  def fused_launch(i):
-    _lib.call("gbsgmc_sgld_glm_step", m, CHAINS, MB, _lib.ptr(idx_buf[i % 8]), MB,
-              _lib.ptr(Wk), _lib.ptr(Vk), 0.9, 1e-5, sch, nz, None, None, None,
-              None, _lib.ptr(ws), ws.numel(), _lib.ptr(status), stream)
-
+  # The fused step kernel alone: average launch time on its stream.
+  f = FusedLauncher(s)
   for i in range(5):
-    fused_launch(i)
+    f(i)
   reps = 200
   torch.cuda.synchronize()
-  k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  k0 = torch.cuda.Event(enable_timing=True)
+  k1 = torch.cuda.Event(enable_timing=True)
   k0.record()
   for i in range(reps):
-    fused_launch(i)
+    f(i)
   k1.record()
   torch.cuda.synchronize()
   kernel_ms = k0.elapsed_time(k1) / reps
   bytes_per_launch = CHAINS * BYTES_PER_CHAIN_STEP
   achieved = bytes_per_launch / (kernel_ms / 1e3) / 1e9
   peak, peak_kind = measured_peak_hbm()
-  traffic = profiled_traffic()
 
   # Plain one-chain unfused GPU form (8 launches per step).
   plain_steps = 300
-  buf = torch.zeros(int(lib.gbsgmc_plain_buffer_bytes(MB, D)), dtype=torch.uint8,
-                    device="cuda")
+  buf = torch.zeros(int(s.lib.gbsgmc_plain_buffer_bytes(MB, D)),
+                    dtype=torch.uint8, device="cuda")
   w1 = torch.zeros((1, D), dtype=torch.float32, device="cuda")
   v1 = torch.ones((1, D), dtype=torch.float32, device="cuda")
   U1 = torch.zeros(1, dtype=torch.float64, device="cuda")
 
   def plain_step(k):
-    _lib.call("gbsgmc_plain_sgld_glm_step", m, MB, _lib.ptr(idx_buf[k % 8, 0]),
+    _lib.call("gbsgmc_plain_sgld_glm_step", f.model, MB, _lib.ptr(f.idx[k % 8, 0]),
               _lib.ptr(w1), _lib.ptr(v1), 0.9, 1e-5,
-              _lib.sched(step_size=1e-5, temperature=1.0, offset=k), nz,
-              _lib.ptr(U1), _lib.ptr(buf), _lib.ptr(status), stream)
+              _lib.sched(step_size=1e-5, temperature=1.0, offset=k), f.noise,
+              _lib.ptr(U1), _lib.ptr(buf), _lib.ptr(f.status), f.stream)
 
   for k in range(10):
     plain_step(k)
@@ -318,11 +362,13 @@ def run_gbsgmc(args):
 
   # End to end through the public API: alias.sgld with host samples in and
   # numpy samples out; the dataset stays resident in HBM between calls.
-  e2e_run = alias.sgld(pot, loader, cache_size=512, batch_size=MB,
-                       first_step_size=FIRST, last_step_size=LAST,
-                       accepted_samples=min(1000, args.steps), rms_prop=True)
+  kw = dict(cache_size=512, batch_size=MB, first_step_size=FIRST,
+            last_step_size=LAST, rms_prop=True)
   init = [{"w": np.zeros(D, np.float32)} for _ in range(CHAINS)]
-  e2e_run(*init[:2], iterations=max(args.warmup, 3))   # warm the path
+  alias.sgld(s.pot, s.loader, accepted_samples=1, **kw)(
+      *init[:2], iterations=args.warmup)          # warm the path
+  e2e_run = alias.sgld(s.pot, s.loader, accepted_samples=min(1000, args.steps),
+                       **kw)
   barrier()
   e0 = time.perf_counter()
   results = e2e_run(*init, iterations=args.steps)
@@ -337,12 +383,12 @@ def run_gbsgmc(args):
   cpu = None
   if rank == 0:
     threads = os.cpu_count() or 1
-    val, dt = cpu_chain_steps(X, y, 2 * threads, 2, threads)
-    cpu = {"value": val, "unit": "chain-steps/s", "cores": threads, "kind": "port",
+    val, _ = cpu_chain_steps(s.X, s.y, 2 * threads, 2, threads)
+    cpu = {"value": val, "unit": "chain-steps/s", "cores": threads,
+           "kind": "port",
            "sample": f"{2 * threads} chains x 2 steps (numpy restatement, "
                      f"{threads} threads)"}
 
-  status_code = int(status.item())
   if rank == 0:
     line = {
         "metric": METRIC, "value": value, "unit": "chain-steps/s",
@@ -360,7 +406,8 @@ def run_gbsgmc(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "traffic": profiled_traffic(),
+                     "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": "glm_kernel (fused SGLD step)",
                      "kernel_ms": kernel_ms,
                      "algorithmic_bytes_per_launch": bytes_per_launch},
@@ -372,8 +419,8 @@ def run_gbsgmc(args):
         "plain_gpu": {"value": plain_value, "unit": "chain-steps/s",
                       "form": "one chain, 8 unfused launches per step",
                       "fused_over_plain": value / world / plain_value},
-        "clocks": clk,
-        "finite": finite, "device_status": status_code,
+        "clocks": clk, "finite": finite,
+        "device_status": int(f.status.item()),
     }
     print(json.dumps(line), flush=True)
   if world > 1:
@@ -386,11 +433,15 @@ def main():
   ap.add_argument("--steps", type=int, default=K_CONFIG)
   ap.add_argument("--warmup", type=int, default=5)
   ap.add_argument("--impl", default="gbsgmc", choices=["gbsgmc", "reference"])
+  ap.add_argument("--kernel-only", action="store_true",
+                  help="short run of the fused kernel for profilers; no JSON line")
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error("--warmup must be at least 3")
   if args.impl == "reference":
     run_reference(args)
+  elif args.kernel_only:
+    kernel_only(args)
   else:
     run_gbsgmc(args)
 

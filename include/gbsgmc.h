@@ -114,7 +114,7 @@ int gbsgmc_philox_normal(uint64_t seed, int chain_base, int chains,
 typedef struct gbsgmc_glm {
   int family;          /* GBSGMC_GLM_*                                       */
   int d;               /* features = parameters per chain, 1..1024            */
-  int64_t n_obs;       /* N, observations in the dataset (the N/n scale)     */
+  int64_t n_obs;       /* N of the N/n scale (observations in the dataset)   */
   int64_t ld;          /* row stride of X in floats (>= d)                    */
   const float* X;      /* [n_obs, ld] fp32 features                           */
   const float* y;      /* [n_obs] fp32 targets                                */
@@ -122,6 +122,7 @@ typedef struct gbsgmc_glm {
   float prior_scale;   /* Gaussian prior N(0, s^2 I) sd; <= 0: flat prior     */
   float temperature;   /* potential temperature T: U = (-N/n sum lk - log p)/T */
   int _pad;
+  int64_t n_rows;      /* rows of X and y (index bound); 0 means n_obs        */
 } gbsgmc_glm;
 
 /* Bytes of workspace needed by gbsgmc_glm_value_and_grad for `chains` chains of

@@ -101,9 +101,10 @@ __device__ __forceinline__ U32x4 philox4x32_10(U32x4 c, uint32_t k0,
   return c;
 }
 
-// Uniform in (0,1): the top 24 bits plus one half, exactly representable.
+// Uniform in (0,1): the top 23 bits plus one half, (2m+1)/2^24, which fp32
+// represents exactly over the whole interval.
 __device__ __forceinline__ float u32_to_open01(uint32_t v) {
-  return (static_cast<float>(v >> 8) + 0.5f) * (1.0f / 16777216.0f);
+  return (static_cast<float>(v >> 9) + 0.5f) * (1.0f / 8388608.0f);
 }
 
 // Box-Muller: (a, b) uniform words -> two standard normals.

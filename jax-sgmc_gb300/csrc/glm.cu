@@ -34,7 +34,7 @@ enum Mode { kValueGrad = 0, kSgldStep = 1 };
 
 struct GlmArgs {
   int family, d, dq;
-  int64_t n_obs, ld;
+  int64_t n_obs, n_rows, ld;
   const float* X;
   const float* y;
   float inv_s2;     // 1/sigma^2 (linear-Gaussian)
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kThreads)
   for (int r = tid; r < R; r += kThreads) {
     const int i = row0 + r;
     int32_t o = __ldg(a.idx + c * a.idx_stride + i);
-    if (o < 0 || o >= a.n_obs) {
+    if (o < 0 || o >= a.n_rows) {
       raise_status(a.status, GBSGMC_ERR_INDEX);
       o = -1;
     }
@@ -579,8 +579,9 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
     return set_error(GBSGMC_ERR_ARG, "glm: unknown family %d", m->family);
   if (m->d < 1 || m->d > 1024)
     return set_error(GBSGMC_ERR_SHAPE, "glm: d must be in [1, 1024], got %d", m->d);
-  if (m->ld < m->d || m->n_obs < 1 || m->n_obs >= (1ll << 31))
-    return set_error(GBSGMC_ERR_ARG, "glm: bad ld or n_obs");
+  if (m->ld < m->d || m->n_obs < 1 || m->n_rows < 0 ||
+      m->n_rows >= (1ll << 31) || (m->n_rows == 0 && m->n_obs >= (1ll << 31)))
+    return set_error(GBSGMC_ERR_ARG, "glm: bad ld, n_obs or n_rows");
   if (chains < 0 || n < 0 || n > kMaxRowsPerSlice * 64)
     return set_error(GBSGMC_ERR_SHAPE, "glm: chains/n out of range");
   if (idx_stride < n) return set_error(GBSGMC_ERR_ARG, "glm: idx_stride < n");
@@ -602,6 +603,7 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.d = m->d;
   a.dq = (m->d + 3) / 4;
   a.n_obs = m->n_obs;
+  a.n_rows = m->n_rows > 0 ? m->n_rows : m->n_obs;
   a.ld = m->ld;
   a.X = m->X;
   a.y = m->y;

@@ -191,8 +191,9 @@ extern "C" int gbsgmc_plain_sgld_glm_step(
   }
   const double n_over = static_cast<double>(m->n_obs) / n;
   const Sched sc = to_sched(sched);
-  gather_kernel<<<n, 128, 0, s>>>(m->X, m->ld, m->y, idx_dev, n, d, m->n_obs,
-                                  b.xb, b.yb, status_dev);
+  gather_kernel<<<n, 128, 0, s>>>(m->X, m->ld, m->y, idx_dev, n, d,
+                                  m->n_rows > 0 ? m->n_rows : m->n_obs, b.xb,
+                                  b.yb, status_dev);
   gemv_kernel<<<(n + 7) / 8, 256, 0, s>>>(b.xb, w_dev, n, d, b.z);
   link_kernel<<<(n + 255) / 256, 256, 0, s>>>(m->family, b.z, b.yb, n, inv_s2,
                                               log_norm, b.lk, b.dz);

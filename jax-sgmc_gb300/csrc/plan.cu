@@ -54,13 +54,14 @@ int cuda_err(cudaError_t e, const char* what) {
 int enqueue_block(gbsgmc_plan* p, int g, cudaStream_t s) {
   int rc;
   const int64_t cn = static_cast<int64_t>(p->chains) * p->n;
+  const int64_t rows = p->model.n_rows > 0 ? p->model.n_rows : p->model.n_obs;
   if (p->isrc.pcg_dev != nullptr) {
-    rc = gbsgmc_index_draw_pcg64(p->isrc.pcg_dev, p->chains, p->model.n_obs,
+    rc = gbsgmc_index_draw_pcg64(p->isrc.pcg_dev, p->chains, rows,
                                  static_cast<int64_t>(g) * p->n, p->n, p->idx,
                                  p->n, cn, p->status, s);
   } else {
     rc = launch_philox_index(p->isrc.index_seed, p->isrc.chain_base, p->chains,
-                             p->base, 0, g, p->n, p->model.n_obs, p->idx, p->n,
+                             p->base, 0, g, p->n, rows, p->idx, p->n,
                              cn, s);
   }
   if (rc != GBSGMC_OK) return rc;

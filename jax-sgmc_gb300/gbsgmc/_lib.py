@@ -51,7 +51,8 @@ class Glm(C.Structure):
   _fields_ = [("family", C.c_int), ("d", C.c_int), ("n_obs", C.c_int64),
               ("ld", C.c_int64), ("X", C.c_void_p), ("y", C.c_void_p),
               ("sigma", C.c_float), ("prior_scale", C.c_float),
-              ("temperature", C.c_float), ("_pad", C.c_int)]
+              ("temperature", C.c_float), ("_pad", C.c_int),
+              ("n_rows", C.c_int64)]
 
 
 class Sched(C.Structure):

@@ -82,7 +82,8 @@ class StochasticPotential:
         else observation_count
     return _lib.Glm(self.likelihood.family, d, int(n_obs), ld, X.data_ptr(),
                     _lib.ptr(y), float(self.likelihood.sigma),
-                    float(self.prior.scale), float(self.temperature), 0), (X, y)
+                    float(self.prior.scale), float(self.temperature), 0,
+                    int(dataset.observation_count)), (X, y)
 
   def dim(self, dataset) -> int:
     return dataset.matrix(self.likelihood.x)[1]
@@ -129,12 +130,13 @@ class StochasticPotential:
     g = torch.empty((C, d), dtype=torch.float32, device="cuda") if grad else None
     lko = torch.empty((C, n), dtype=torch.float32, device="cuda") if lk else None
     ws = self.workspace(C, n, d)
+    W = W.to(torch.float32).contiguous()
     idx = idx.to(torch.int32).contiguous()
     if mask is not None:
       mask = mask.to(device="cuda", dtype=torch.float32).reshape(C, n).contiguous()
     _lib.call("gbsgmc_glm_value_and_grad", m, C, n, _lib.ptr(idx),
               idx.stride(0) if idx.dim() == 2 else n, _lib.ptr(mask),
-              _lib.ptr(W.contiguous()), _lib.ptr(U), _lib.ptr(g),
+              _lib.ptr(W), _lib.ptr(U), _lib.ptr(g),
               _lib.ptr(lko), _lib.ptr(var), _lib.ptr(ws), ws.numel(),
               _lib.ptr(self.status()), _lib.stream_handle())
     return GlmEval(U, g, lko, var)

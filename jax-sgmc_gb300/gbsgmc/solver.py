@@ -81,17 +81,20 @@ def parallel_tempering(integrator, sa_schedule=None):
     import torch
     normal = update_integrator(state.normal, normal_schedule)
     hot = update_integrator(state.hot, hot_schedule)
-    dev = lambda v: torch.tensor([float(v)], dtype=torch.float64, device="cuda")
+    # Every buffer is bound to a name until the launch is enqueued.
+    temps = torch.tensor([float(normal_schedule.temperature),
+                          float(hot_schedule.temperature)],
+                         dtype=torch.float64, device="cuda")
     perm = torch.zeros(1, dtype=torch.int32, device="cuda")
-    u = None if uniform is None else dev(uniform)
+    u = None if uniform is None else torch.tensor(
+        [float(uniform)], dtype=torch.float64, device="cuda")
+    Un = normal.potential.reshape(1)
+    Uh = hot.potential.reshape(1)
+    var = normal.variance.reshape(1)
     step = int(normal.step)
-    _lib.call("gbsgmc_resgld_swap_f64", 1,
-              _lib.ptr(normal.potential.reshape(1)),
-              _lib.ptr(hot.potential.reshape(1)),
-              _lib.ptr(normal.variance.reshape(1)),
-              _lib.ptr(dev(normal_schedule.temperature)),
-              _lib.ptr(dev(hot_schedule.temperature)), state.F,
-              _lib.ptr(state.ssq), _lib.ptr(state.step), _lib.ptr(u),
+    _lib.call("gbsgmc_resgld_swap_f64", 1, _lib.ptr(Un), _lib.ptr(Uh),
+              _lib.ptr(var), _lib.ptr(temps[0:1]), _lib.ptr(temps[1:2]),
+              state.F, _lib.ptr(state.ssq), _lib.ptr(state.step), _lib.ptr(u),
               state.key, step, None, _lib.ptr(perm), _lib.stream_handle())
     if int(perm.item()) == 1:
       normal, hot = hot, normal

@@ -107,13 +107,13 @@ def philox4x32_10(ctr, key):
 
 
 def _open01(v):
-  return ((v.astype(np.uint64) >> np.uint64(8)).astype(np.float64) + 0.5) / 16777216.0
+  return ((v.astype(np.uint64) >> np.uint64(9)).astype(np.float64) + 0.5) / 8388608.0
 
 
 def philox_normals(seed: int, chain: int, step: int, tag: int, count: int):
   """Normals of one chain/step/tag: group g of 4 parameters uses
   Philox(counter=(g, step, chain, tag), key=seed) and Box-Muller on the pairs
-  (u0,u1), (u2,u3) with u = (top 24 bits + 0.5) / 2^24 (float64)."""
+  (u0,u1), (u2,u3) with u = (top 23 bits + 0.5) / 2^23 (float64)."""
   groups = (count + 3) // 4
   ctr = np.zeros((groups, 4), np.uint64)
   ctr[:, 0] = np.arange(groups)

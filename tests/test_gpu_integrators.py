@@ -35,9 +35,10 @@ def test_sgld_update_rmsprop_and_plain(lib):
     xd, gd, vd, nd = cuda(x), cuda(g), cuda(v), cuda(xi)
     samples = torch.zeros((2, C, P), dtype=torch.float32, device="cuda")
     keep = cuda(np.array([-1, -1, 1], np.int32))
-    sch = _lib.sched(step_size=0, temperature=0, step_size_dev=cuda(
-        np.array([0, 0, 1e-3], np.float32)), temperature_dev=cuda(
-        np.array([1, 1, 0.7], np.float32)), keep_slot_dev=keep, offset=2)
+    h_tab = cuda(np.array([0, 0, 1e-3], np.float32))
+    t_tab = cuda(np.array([1, 1, 0.7], np.float32))
+    sch = _lib.sched(step_size=0, temperature=0, step_size_dev=h_tab,
+                     temperature_dev=t_tab, keep_slot_dev=keep, offset=2)
     _lib.call("gbsgmc_sgld_update", C, P, _lib.ptr(xd), _lib.ptr(gd),
               _lib.ptr(vd) if rms else None, 0.9, 1e-5, sch,
               _lib.noise(noise_dev=nd, noise_stride=P), _lib.ptr(samples), None)
@@ -56,15 +57,16 @@ def test_obabo_halves(lib):
   x, p, g1, g2, xi1, xi2 = (rng.normal(size=(C, P)).astype(np.float32) for _ in range(6))
   mass = (rng.random(P) + 0.5).astype(np.float32)
   xd, pd = cuda(x), cuda(p)
+  g1d, g2d, md, x1d, x2d = cuda(g1), cuda(g2), cuda(mass), cuda(xi1), cuda(xi2)
   ke0 = torch.zeros(C, dtype=torch.float64, device="cuda")
   ke1 = torch.zeros(C, dtype=torch.float64, device="cuda")
   sch = _lib.sched(step_size=0.01, temperature=0.8, offset=3)
-  _lib.call("gbsgmc_obabo_first", C, P, _lib.ptr(xd), _lib.ptr(pd), _lib.ptr(cuda(g1)),
-            _lib.ptr(cuda(mass)), 0.7, _lib.ptr(ke0), sch,
-            _lib.noise(noise_dev=cuda(xi1), noise_stride=P), None)
-  _lib.call("gbsgmc_obabo_second", C, P, _lib.ptr(pd), _lib.ptr(cuda(g2)),
-            _lib.ptr(cuda(mass)), 0.7, _lib.ptr(ke1), sch,
-            _lib.noise(noise_dev=cuda(xi2), noise_stride=P), None)
+  _lib.call("gbsgmc_obabo_first", C, P, _lib.ptr(xd), _lib.ptr(pd), _lib.ptr(g1d),
+            _lib.ptr(md), 0.7, _lib.ptr(ke0), sch,
+            _lib.noise(noise_dev=x1d, noise_stride=P), None)
+  _lib.call("gbsgmc_obabo_second", C, P, _lib.ptr(pd), _lib.ptr(g2d),
+            _lib.ptr(md), 0.7, _lib.ptr(ke1), sch,
+            _lib.noise(noise_dev=x2d, noise_stride=P), None)
   xr, pr, ker0 = O.obabo_first(x, p, g1, xi1, 0.01, 0.8, 0.7, mass)
   pr, ker1 = O.obabo_second(pr, g2, xi2, 0.01, 0.8, 0.7, mass)
   np.testing.assert_allclose(xd.cpu().numpy(), xr, rtol=1e-5, atol=1e-6)
@@ -82,14 +84,15 @@ def test_sghmc_pieces(lib):
   mass = (rng.random(P) + 0.5).astype(np.float32)
   xd = cuda(x)
   pd = cuda(np.zeros((C, P), np.float32))
+  md, fd, gd, x0d, x1d = cuda(mass), cuda(fric), cuda(g), cuda(xi0), cuda(xi1)
   sch = _lib.sched(step_size=0.02, temperature=1.0, offset=0)
-  _lib.call("gbsgmc_sghmc_resample", C, P, _lib.ptr(pd), _lib.ptr(cuda(mass)), sch,
-            _lib.noise(noise_dev=cuda(xi0), noise_stride=P), None)
+  _lib.call("gbsgmc_sghmc_resample", C, P, _lib.ptr(pd), _lib.ptr(md), sch,
+            _lib.noise(noise_dev=x0d, noise_stride=P), None)
   _lib.call("gbsgmc_sghmc_position", C, P, _lib.ptr(xd), _lib.ptr(pd),
-            _lib.ptr(cuda(mass)), _lib.ptr(cuda(fric)), 0.0, sch, None)
-  _lib.call("gbsgmc_sghmc_momentum", C, P, _lib.ptr(pd), _lib.ptr(cuda(g)),
-            _lib.ptr(cuda(fric)), 0.0, sch,
-            _lib.noise(noise_dev=cuda(xi1), noise_stride=P), None)
+            _lib.ptr(md), _lib.ptr(fd), 0.0, sch, None)
+  _lib.call("gbsgmc_sghmc_momentum", C, P, _lib.ptr(pd), _lib.ptr(gd),
+            _lib.ptr(fd), 0.0, sch,
+            _lib.noise(noise_dev=x1d, noise_stride=P), None)
   p = O.sghmc_resample(xi0, mass)
   xr, p = O.sghmc_position(x, p, 0.02, fric, mass)
   p = O.sghmc_momentum(p, g, xi1, 0.02, fric)
@@ -110,11 +113,12 @@ def test_resgld_swap_kernel(lib):
   u = rng.random(pairs)
   d = lambda a: cuda(np.asarray(a, np.float64))
   ssq_d, k_d = d(ssq), cuda(k)
+  Un_d, Uh_d, var_d, Tn_d, Th_d, u_d = d(Un), d(Uh), d(var), d(Tn), d(Th), d(u)
   perm = torch.zeros(pairs, dtype=torch.int32, device="cuda")
   log_s = torch.zeros(pairs, dtype=torch.float64, device="cuda")
-  _lib.call("gbsgmc_resgld_swap_f64", pairs, _lib.ptr(d(Un)), _lib.ptr(d(Uh)),
-            _lib.ptr(d(var)), _lib.ptr(d(Tn)), _lib.ptr(d(Th)), 1.5,
-            _lib.ptr(ssq_d), _lib.ptr(k_d), _lib.ptr(d(u)), 0, 0,
+  _lib.call("gbsgmc_resgld_swap_f64", pairs, _lib.ptr(Un_d), _lib.ptr(Uh_d),
+            _lib.ptr(var_d), _lib.ptr(Tn_d), _lib.ptr(Th_d), 1.5,
+            _lib.ptr(ssq_d), _lib.ptr(k_d), _lib.ptr(u_d), 0, 0,
             _lib.ptr(log_s), _lib.ptr(perm), None)
   for i in range(pairs):
     sw, s2, kk, ls = O.resgld_swap(Un[i], Uh[i], var[i], Tn[i], Th[i], ssq[i],
@@ -165,11 +169,12 @@ def test_fused_step_matches_oracle_with_injected_noise(lib, family, rms):
   slik = torch.zeros((1, C), dtype=torch.float64, device="cuda")
   ws = pot.workspace(C, n, d)
   status = torch.zeros(1, dtype=torch.int32, device="cuda")
-  sch = _lib.sched(step_size=2e-4, temperature=0.9,
-                   keep_slot_dev=cuda(np.array([0], np.int32)), offset=0)
-  _lib.call("gbsgmc_sgld_glm_step", m, C, n, _lib.ptr(cuda(idx)), n, _lib.ptr(Wd),
+  keep_d, idx_d, xi_d = cuda(np.array([0], np.int32)), cuda(idx), cuda(xi)
+  sch = _lib.sched(step_size=2e-4, temperature=0.9, keep_slot_dev=keep_d,
+                   offset=0)
+  _lib.call("gbsgmc_sgld_glm_step", m, C, n, _lib.ptr(idx_d), n, _lib.ptr(Wd),
             _lib.ptr(Vd) if rms else None, 0.9, 1e-5, sch,
-            _lib.noise(noise_dev=cuda(xi), noise_stride=d), _lib.ptr(U),
+            _lib.noise(noise_dev=xi_d, noise_stride=d), _lib.ptr(U),
             _lib.ptr(var), _lib.ptr(samples), _lib.ptr(slik), _lib.ptr(ws),
             ws.numel(), _lib.ptr(status), None)
   ref = O.glm_potential(W, X, y, idx, N, family, 0.5, 2.0, 1.3)
