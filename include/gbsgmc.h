@@ -277,6 +277,36 @@ int gbsgmc_sgld_glm_step(const gbsgmc_glm* model, int chains, int n,
                          size_t workspace_bytes, int* status_dev,
                          gbsgmc_stream_t stream);
 
+/* Size of the scratch array compiled into the library for
+ * gbsgmc_sgld_glm_step_noalloc (8 MiB per GPU that loads the library). */
+#define GBSGMC_STATIC_SCRATCH_BYTES (8u << 20)
+
+/* gbsgmc_sgld_glm_step for callers that cannot allocate device memory --
+ * code running inside another runtime's memory pool, code issued during a
+ * CUDA graph capture, or loops that must not pay for cudaMalloc/cudaFree.
+ * It has no counterpart in the reference.  Same arguments and results as
+ * gbsgmc_sgld_glm_step minus the workspace: the scratch is an array of
+ * GBSGMC_STATIC_SCRATCH_BYTES inside the library, held by every GPU that loads
+ * it until the process exits.  Shapes whose scratch
+ * (gbsgmc_glm_workspace_bytes(chains, n, d)) exceeds that size are rejected
+ * with GBSGMC_ERR_SHAPE (256 chains with d <= 256 and n <= 16384 fit).  It
+ * calls no cudaMalloc, cudaFree or other allocating routine.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress, with that device current); make that first call
+ *     before any stream capture.
+ *   - Each call clears the part of the array it uses, on `stream`.
+ *   - All calls share the one array: calls that may overlap on the GPU
+ *     (different streams without an ordering between them) race and must be
+ *     serialised by the caller. */
+int gbsgmc_sgld_glm_step_noalloc(const gbsgmc_glm* model, int chains, int n,
+                                 const int32_t* idx_dev, int64_t idx_stride,
+                                 float* w_dev, float* v_dev, float alpha,
+                                 float lmbd, const gbsgmc_sched* sched,
+                                 const gbsgmc_noise* noise, double* U_dev,
+                                 double* lk_var_dev, float* samples_dev,
+                                 double* sample_lik_dev, int* status_dev,
+                                 gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Plans: many steps replayed from a CUDA graph                              */
 /* ------------------------------------------------------------------------ */

@@ -28,6 +28,7 @@ STATUS_NAMES = {0: "ok", 1: "bad argument", 2: "unsupported shape",
 GLM_LINEAR_GAUSSIAN = 0
 GLM_LOGISTIC = 1
 GLM_LINEAR = 2
+STATIC_SCRATCH_BYTES = 8 << 20
 
 TAG_SGLD, TAG_OBABO_1, TAG_OBABO_2, TAG_SGHMC_RESAMPLE, TAG_SGHMC_STEP, \
   TAG_SWAP, TAG_INDEX = range(7)
@@ -110,6 +111,9 @@ SIGNATURES = {
     "gbsgmc_sgld_glm_step": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp, _f, _f,
                                   _P(Sched), _P(Noise), _vp, _vp, _vp, _vp,
                                   _vp, _sz, _vp, _vp]),
+    "gbsgmc_sgld_glm_step_noalloc": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp,
+                                          _f, _f, _P(Sched), _P(Noise), _vp,
+                                          _vp, _vp, _vp, _vp, _vp]),
     "gbsgmc_sgld_glm_plan_create": (_i, [_P(_vp), _P(Glm), _i, _i, _vp, _vp,
                                          _f, _f, _P(Sched), _P(Noise),
                                          _P(IndexSrc), _vp, _vp, _vp, _vp, _i,
