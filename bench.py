@@ -316,6 +316,7 @@ def run_gbsgmc(args):
     ms = float(t.item())
   value = world * CHAINS * args.steps / (ms / 1e3)
   launches = plan.launches(args.steps)
+  shape = plan.launch_shape()
   finite = bool(torch.isfinite(s.W).all().item())
   plan.close()
 
@@ -402,7 +403,10 @@ def run_gbsgmc(args):
                    "noise": "Philox4x32-10",
                    "l2": "inputs larger than L2 (X 1.02 GB, random rows)",
                    "parallelism": f"chains sharded, {world} replica(s)",
-                   "graph_block_steps": 50},
+                   "graph_block_steps": 50,
+                   "launch_shape": {"ctas_per_chain": shape[0],
+                                    "rows_per_warp": shape[1],
+                                    "chosen_by": "autotuner"}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,

@@ -121,7 +121,8 @@ typedef struct gbsgmc_glm {
   float sigma;         /* linear-Gaussian noise sd                            */
   float prior_scale;   /* Gaussian prior N(0, s^2 I) sd; <= 0: flat prior     */
   float temperature;   /* potential temperature T: U = (-N/n sum lk - log p)/T */
-  int _pad;
+  int y_inline;        /* 1: the target of row i is X[i*ld + d] (y unused and
+                          ld >= d+1); 0: the target is y[i]                 */
   int64_t n_rows;      /* rows of X and y (index bound); 0 means n_obs        */
 } gbsgmc_glm;
 
@@ -344,6 +345,15 @@ int gbsgmc_sgld_glm_plan_create(gbsgmc_plan** plan, const gbsgmc_glm* model,
  * host. */
 int gbsgmc_plan_run(gbsgmc_plan* plan, int64_t first_step, int64_t steps,
                     gbsgmc_stream_t stream);
+
+/* The launch shape the plan's autotuner chose for the fused step: CTAs per
+ * chain and rows per warp (0 = the library default).  The autotuner times a
+ * few candidate shapes on scratch copies of the chain state when the plan is
+ * created (GBSGMC_AUTOTUNE=0 disables it) and caches the choice per problem
+ * shape for the process.  No reference counterpart: launch configuration
+ * only. */
+int gbsgmc_plan_launch_shape(const gbsgmc_plan* plan, int* slices,
+                             int* rows_per_warp);
 
 /* Kernel launches one plan_run of `steps` steps performs (for accounting). */
 int64_t gbsgmc_plan_launches(const gbsgmc_plan* plan, int64_t steps);

@@ -1,39 +1,53 @@
 // Generalised-linear minibatch potential, its adjoint, and the fused SGLD step.
 //
 // Grid (slices, chains).  CTA (s, c) owns rows [s*R, (s+1)*R) of chain c's
-// minibatch.  One producer warp stages the gathered rows X[idx_i] into a ring
-// of shared-memory stages with cp.async.bulk (one 16-byte-aligned copy per
-// row, completing on the stage's mbarrier); eight consumer warps each take a
-// row at a time: z = x.w by a warp reduction, the family's log-likelihood
-// lk(z, y) and dlk/dz, and acc += dlk/dz * x kept in registers.  The warp
-// partials are reduced through shared memory.  With several slices per chain,
-// each CTA writes its partial gradient and partial sums to the workspace and
-// the last CTA of the chain to finish (ticket counter) adds them in slice
-// order -- the result does not depend on which CTA finishes last -- and runs
-// the epilogue:
+// minibatch; its 8 warps take tiles of RW rows in turn.  A warp gathers the
+// RW rows of its tile straight from HBM with 128-bit loads that do not
+// allocate in L1 (each row is read once), every lane holding RW x QPL float4
+// of x in registers, so RW rows' worth of loads are in flight per warp:
+//   * each lane forms partial dot products x.w over its columns for the RW
+//     rows; a transposed butterfly (log2 RW halving exchanges, then plain
+//     xor steps) leaves lane group g = lane / (32/RW) with z of row g --
+//     6 shuffles for 4 rows instead of 20;
+//   * each lane group evaluates the family's lk(z, y) and dlk/dz for its row,
+//     so the link function runs once per row, not 32 times;
+//   * the RW coefficients are broadcast back and acc += coef * x accumulates
+//     the gradient from the rows still held in registers.
+// The dataset stores the target at column d of each feature row (y_inline),
+// in the same sectors as the row, so no separate scattered gather of y is
+// needed.  (Staging rows through shared memory with one cp.async.bulk per
+// 1 KB row was measured slower: per-request cost held it near 13 GB/s per SM.)
+// The warp partials are reduced through shared memory in a fixed order.  With
+// several slices per chain, each CTA writes its partial gradient and partial
+// sums to the workspace and the last CTA of the chain to finish (ticket
+// counter) adds them in slice order -- the result does not depend on which
+// CTA finishes last -- and runs the epilogue:
 //   U = (-N/n sum_i m_i lk_i - log p(w)) / T_pot
 //   g = (-N/n sum_i m_i dlk_i/dw + w / s^2) / T_pot
 // then either stores (U, g) or applies the SGLD(+RMSprop) update in place.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "common.cuh"
+#include "internal.h"
 
 namespace gbsgmc {
 namespace {
 
-constexpr int kConsumerWarps = 8;
-constexpr int kThreads = (kConsumerWarps + 1) * 32;
-constexpr int kRowsPerWarpStage = 2;
-constexpr int kRowsPerStage = kConsumerWarps * kRowsPerWarpStage;
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
 constexpr int kMaxRowsPerSlice = 1024;
 constexpr int kMinSlicesAlloc = 16;
-constexpr size_t kRingBudget = 96 * 1024;
 
 enum Mode { kValueGrad = 0, kSgldStep = 1 };
 
 struct GlmArgs {
   int family, d, dq;
+  int y_inline;
   int64_t n_obs, n_rows, ld;
   const float* X;
   const float* y;
@@ -61,72 +75,229 @@ struct GlmArgs {
   float4* ws_part;
   double* ws_sums;
   unsigned* ws_ticket;
+  void* ws_base;
+  size_t ws_size;
+  int slices_fixed;   // > 0: slices per chain chosen by the caller
+  int rw_fixed;       // > 0: rows per warp chosen by the caller
   int* status;
-  int bulk;
-  int stages;
+  int vec4;   // rows are 16-byte aligned: 128-bit loads
 };
 
 struct SmemLayout {
-  size_t bars, abort_flag, idx, y, m, ring, red, sums, total;
+  size_t flags, idx, m, red, sums, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) {
   return (x + a - 1) / a * a;
 }
 
-__host__ __device__ inline SmemLayout smem_layout(int rows_per_slice, int dq,
-                                                  int stages) {
+__host__ __device__ inline SmemLayout smem_layout(int rows_per_slice, int dq) {
   SmemLayout L;
   size_t o = 0;
-  L.bars = o;
-  o += sizeof(uint64_t) * 2 * stages;
-  L.abort_flag = o;
+  L.flags = o;
   o += 16;
-  o = align_up(o, 16);
   L.idx = o;
   o += sizeof(int32_t) * rows_per_slice;
   o = align_up(o, 16);
-  L.y = o;
-  o += sizeof(float) * rows_per_slice;
-  o = align_up(o, 16);
   L.m = o;
   o += sizeof(float) * rows_per_slice;
-  o = align_up(o, 128);
-  L.ring = o;
-  o += static_cast<size_t>(stages) * kRowsPerStage * dq * 16;
   o = align_up(o, 16);
   L.red = o;
-  o += static_cast<size_t>(kConsumerWarps) * dq * 16;
+  o += static_cast<size_t>(kWarps) * dq * 16;
   o = align_up(o, 16);
   L.sums = o;
-  o += sizeof(double) * 4 * (kConsumerWarps + 1);
+  o += sizeof(double) * 4 * (kWarps + 1);
   L.total = o;
   return L;
 }
 
-__device__ __forceinline__ float softplusf(float z) {
-  return fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z)));
+// Bernoulli-logit log-likelihood y z - softplus(z) and its derivative
+// y - sigmoid(z), from one exponential: e = exp(-|z|),
+// softplus(z) = max(z, 0) + log1p(e), sigmoid(z) = 1/(1+e) or e/(1+e).
+__device__ __forceinline__ void logistic_link(float z, float y, float& lk,
+                                              float& dz) {
+  const float e = expf(-fabsf(z));
+  const float r = 1.0f / (1.0f + e);
+  lk = y * z - (fmaxf(z, 0.0f) + log1pf(e));
+  dz = y - (z >= 0.0f ? r : e * r);
 }
 
-__device__ __forceinline__ float sigmoidf(float z) {
-  if (z >= 0.0f) return 1.0f / (1.0f + expf(-z));
-  const float e = expf(z);
-  return e / (1.0f + e);
+// 128-bit read-only load that does not allocate in L1 (rows are read once).
+__device__ __forceinline__ float4 ld_row4(const float* p) {
+  float4 v;
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
 }
 
+__device__ __forceinline__ float ld_row1(const float* p) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
+template <int RW>
+struct Log2;
+template <>
+struct Log2<1> { static constexpr int v = 0; };
+template <>
+struct Log2<2> { static constexpr int v = 1; };
+template <>
+struct Log2<4> { static constexpr int v = 2; };
+template <>
+struct Log2<8> { static constexpr int v = 3; };
+
+// Sum of p[r] over the 32 lanes for RW rows at once.  Returns, in every lane
+// of group g = lane >> (5 - log2 RW), the full sum of row g.
+template <int RW>
+__device__ __forceinline__ float transposed_warp_sum(float (&p)[RW], int lane) {
+  constexpr int LOG = Log2<RW>::v;
+#pragma unroll
+  for (int t = 0; t < LOG; ++t) {
+    const int o = 16 >> t;
+    const int half = RW >> (t + 1);
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < half; ++i) {
+      const float send = upper ? p[i] : p[i + half];
+      const float keep = upper ? p[i + half] : p[i];
+      p[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  float z = p[0];
+#pragma unroll
+  for (int o = 16 >> LOG; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+  return z;
+}
+
+// Issues every load of the tile of rows [r0, r0 + RW): x of the RW rows and
+// the target of this lane's row r0 + g.  Rows past R or with an invalid
+// index read as zero.
+template <int QPL, int RW>
+__device__ __forceinline__ void load_tile(const GlmArgs& a, const int32_t* idx_s,
+                                          int R, int r0, int lane, int g,
+                                          float4 (&xv)[RW][QPL], float& yv,
+                                          int& og) {
+#pragma unroll
+  for (int r = 0; r < RW; ++r) {
+    const int o = r0 + r < R ? idx_s[r0 + r] : -1;
+    const float* row = a.X + static_cast<int64_t>(o) * a.ld;
+#pragma unroll
+    for (int k = 0; k < QPL; ++k) {
+      const int q = lane + 32 * k;
+      if (o >= 0 && q < a.dq) {
+        if (a.vec4) {
+          xv[r][k] = ld_row4(row + 4 * q);
+        } else {
+          const int j = 4 * q;
+          xv[r][k].x = ld_row1(row + j);
+          xv[r][k].y = j + 1 < a.d ? ld_row1(row + j + 1) : 0.0f;
+          xv[r][k].z = j + 2 < a.d ? ld_row1(row + j + 2) : 0.0f;
+          xv[r][k].w = j + 3 < a.d ? ld_row1(row + j + 3) : 0.0f;
+        }
+      } else {
+        xv[r][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+  }
+  og = r0 + g < R ? idx_s[r0 + g] : -1;
+  yv = 0.0f;
+  if (og >= 0) {
+    if (a.y_inline) {
+      yv = ld_row1(a.X + static_cast<int64_t>(og) * a.ld + a.d);
+    } else if (a.y != nullptr) {
+      yv = ld_row1(a.y + og);
+    }
+  }
+}
+
+// Per-lane accumulators of one CTA row stream.  The likelihood sums stay in
+// fp32 per lane (a lane sees a few dozen rows); they are widened to fp64 for
+// the warp and block reductions.  GB300's fp64 pipe runs at a small fraction
+// of the fp32 rate, so per-row fp64 arithmetic would throttle the kernel.
+//
+// The variance needs E[lk^2] - E[lk]^2, which cancels badly when |lk| is
+// large, so each lane sums around its first value K: s1 = sum(lk - K),
+// s2 = sum((lk - K)^2); the widening to fp64 restores sum(lk) and sum(lk^2).
 template <int QPL>
-__global__ void __launch_bounds__(kThreads)
+struct Accum {
+  float4 acc[QPL];
+  float mlk, K, s1, s2;
+  int cnt;
+};
+
+// Likelihood, adjoint and accumulation for a loaded tile (see load_tile).
+template <int QPL, int RW>
+__device__ __forceinline__ void consume_tile(const GlmArgs& a, const float* m_s,
+                                             float* lk_out, int r0, int lane,
+                                             int g, bool leader,
+                                             const float4 (&wq)[QPL],
+                                             const float4 (&xv)[RW][QPL],
+                                             float yv, int og, Accum<QPL>& A) {
+  constexpr int GROUP = 32 / RW;
+  float p[RW];
+#pragma unroll
+  for (int r = 0; r < RW; ++r) {
+    float z = 0.0f;
+#pragma unroll
+    for (int k = 0; k < QPL; ++k) {
+      z = fmaf(xv[r][k].x, wq[k].x, z);
+      z = fmaf(xv[r][k].y, wq[k].y, z);
+      z = fmaf(xv[r][k].z, wq[k].z, z);
+      z = fmaf(xv[r][k].w, wq[k].w, z);
+    }
+    p[r] = z;
+  }
+  const float z = transposed_warp_sum<RW>(p, lane);
+  const bool ok = og >= 0;
+  const int row = r0 + g;
+  const float mw = (ok && a.mask != nullptr) ? m_s[row] : 1.0f;
+  float lkv, dz;
+  if (a.family == GBSGMC_GLM_LOGISTIC) {
+    logistic_link(z, yv, lkv, dz);
+  } else if (a.family == GBSGMC_GLM_LINEAR) {
+    lkv = z;
+    dz = 1.0f;
+  } else {
+    const float res = yv - z;
+    lkv = -0.5f * res * res * a.inv_s2 - a.log_norm;
+    dz = res * a.inv_s2;
+  }
+  const float coef = ok ? mw * dz : 0.0f;
+  if (ok && leader) {
+    A.mlk = fmaf(mw, lkv, A.mlk);
+    if (A.cnt == 0) A.K = lkv;
+    const float dk = lkv - A.K;
+    A.s1 += dk;
+    A.s2 = fmaf(dk, dk, A.s2);
+    A.cnt += 1;
+    if (lk_out != nullptr) lk_out[row] = lkv;
+  }
+#pragma unroll
+  for (int r = 0; r < RW; ++r) {
+    const float cr = __shfl_sync(0xffffffffu, coef, r * GROUP);
+#pragma unroll
+    for (int k = 0; k < QPL; ++k) {
+      A.acc[k].x = fmaf(cr, xv[r][k].x, A.acc[k].x);
+      A.acc[k].y = fmaf(cr, xv[r][k].y, A.acc[k].y);
+      A.acc[k].z = fmaf(cr, xv[r][k].z, A.acc[k].z);
+      A.acc[k].w = fmaf(cr, xv[r][k].w, A.acc[k].w);
+    }
+  }
+}
+
+template <int QPL, int RW, bool PF, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
     glm_kernel(const GlmArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const SmemLayout L = smem_layout(a.rows_per_slice, a.dq, a.stages);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars);
-  uint64_t* empty = full + a.stages;
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + L.abort_flag);
-  int* is_last = reinterpret_cast<int*>(smem + L.abort_flag + 4);
+  constexpr int LOG = Log2<RW>::v;
+  constexpr int GROUP = 32 >> LOG;  // lanes per row in the link phase
+  const int dq = a.dq;
+  const SmemLayout L = smem_layout(a.rows_per_slice, dq);
+  int* is_last = reinterpret_cast<int*>(smem + L.flags);
   int32_t* idx_s = reinterpret_cast<int32_t*>(smem + L.idx);
-  float* y_s = reinterpret_cast<float*>(smem + L.y);
   float* m_s = reinterpret_cast<float*>(smem + L.m);
-  float4* ring = reinterpret_cast<float4*>(smem + L.ring);
   float4* red = reinterpret_cast<float4*>(smem + L.red);
   double* sums = reinterpret_cast<double*>(smem + L.sums);
 
@@ -134,181 +305,90 @@ __global__ void __launch_bounds__(kThreads)
   const int s = blockIdx.x, c = blockIdx.y;
   const int row0 = s * a.rows_per_slice;
   const int R = max(0, min(a.rows_per_slice, a.n - row0));
-  const int dq = a.dq;
 
-  if (tid == 0) {
-    for (int i = 0; i < a.stages; ++i) {
-      mbar_init(&full[i], a.bulk ? 1u : 32u);
-      mbar_init(&empty[i], static_cast<uint32_t>(kConsumerWarps));
-    }
-    *abort_flag = 0;
-    *is_last = 0;
-    mbar_fence_init();
-  }
-  // Indices, targets and mask weights of this slice.
+  if (tid == 0) *is_last = 0;
+  // Observation indices (and mask weights) of this slice.
   for (int r = tid; r < R; r += kThreads) {
-    const int i = row0 + r;
-    int32_t o = __ldg(a.idx + c * a.idx_stride + i);
+    int32_t o = __ldg(a.idx + c * a.idx_stride + row0 + r);
     if (o < 0 || o >= a.n_rows) {
       raise_status(a.status, GBSGMC_ERR_INDEX);
       o = -1;
     }
     idx_s[r] = o;
-    y_s[r] = (o >= 0 && a.y != nullptr) ? __ldg(a.y + o) : 0.0f;
-    m_s[r] = a.mask != nullptr ? __ldg(a.mask + static_cast<int64_t>(c) * a.n + i)
-                               : 1.0f;
+    if (a.mask != nullptr)
+      m_s[r] = __ldg(a.mask + static_cast<int64_t>(c) * a.n + row0 + r);
   }
   __syncthreads();
 
-  const int n_stages = (R + kRowsPerStage - 1) / kRowsPerStage;
-  const uint32_t row_bytes = static_cast<uint32_t>(dq) * 16u;
-
-  double my_mlk = 0.0, my_lk = 0.0, my_lk2 = 0.0;
-
-  if (warp == kConsumerWarps) {
-    // ------------------------------ producer ------------------------------
-    int issued = 0;
-    for (int st = 0; st < n_stages; ++st) {
-      const int slot = st % a.stages;
-      const uint32_t ph = static_cast<uint32_t>(st / a.stages) & 1u;
-      if (!mbar_wait_bounded(&empty[slot], ph ^ 1u, abort_flag)) {
-        if (lane == 0) {
-          raise_status(a.status, GBSGMC_ERR_TIMEOUT);
-          *abort_flag = 1;
-        }
-        break;
-      }
-      const int r0 = st * kRowsPerStage;
-      const int cnt = min(kRowsPerStage, R - r0);
-      float4* dst = ring + static_cast<size_t>(slot) * kRowsPerStage * dq;
-      if (a.bulk) {
-        if (lane == 0) {
-          uint32_t bytes = 0;
-          for (int r = 0; r < cnt; ++r) bytes += idx_s[r0 + r] >= 0 ? row_bytes : 0u;
-          mbar_arrive_expect_tx(&full[slot], bytes);
-          for (int r = 0; r < cnt; ++r) {
-            const int32_t o = idx_s[r0 + r];
-            if (o >= 0)
-              bulk_g2s(dst + static_cast<size_t>(r) * dq, a.X + o * a.ld,
-                       row_bytes, &full[slot]);
-          }
-        }
-      } else {
-        float* dsts = reinterpret_cast<float*>(dst);
-        for (int r = 0; r < cnt; ++r) {
-          const int32_t o = idx_s[r0 + r];
-          for (int j = lane; j < dq * 4; j += 32)
-            dsts[r * dq * 4 + j] =
-                (o >= 0 && j < a.d) ? __ldg(a.X + o * a.ld + j) : 0.0f;
-        }
-        mbar_arrive(&full[slot]);
-      }
-      issued = st + 1;
-    }
-    if (*abort_flag && a.bulk && lane == 0) {
-      // Let the copies already issued land before the CTA exits.
-      for (int st = max(0, issued - a.stages); st < issued; ++st)
-        mbar_wait_bounded(&full[st % a.stages],
-                          static_cast<uint32_t>(st / a.stages) & 1u, nullptr);
+  float4 wq[QPL];
+  Accum<QPL> A;
+  const float* w_in = a.w + static_cast<int64_t>(c) * a.d;
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    const int j = 4 * (lane + 32 * k);
+    wq[k].x = j + 0 < a.d ? w_in[j + 0] : 0.0f;
+    wq[k].y = j + 1 < a.d ? w_in[j + 1] : 0.0f;
+    wq[k].z = j + 2 < a.d ? w_in[j + 2] : 0.0f;
+    wq[k].w = j + 3 < a.d ? w_in[j + 3] : 0.0f;
+    A.acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  A.mlk = A.K = A.s1 = A.s2 = 0.0f;
+  A.cnt = 0;
+  const int g = lane >> (5 - LOG);           // my row in the link phase
+  const bool leader = (lane & (GROUP - 1)) == 0;
+  float* lk_out = a.lk != nullptr ? a.lk + static_cast<int64_t>(c) * a.n + row0
+                                  : nullptr;
+  constexpr int kStride = kWarps * RW;
+  if (PF) {
+    // Two register tiles: the loads of the next tile are in flight while
+    // the current one is consumed.
+    float4 xa[RW][QPL], xb[RW][QPL];
+    float ya, yb;
+    int oa, ob;
+    int r0 = warp * RW;
+    load_tile<QPL, RW>(a, idx_s, R, r0, lane, g, xa, ya, oa);
+    while (r0 < R) {
+      load_tile<QPL, RW>(a, idx_s, R, r0 + kStride, lane, g, xb, yb, ob);
+      consume_tile<QPL, RW>(a, m_s, lk_out, r0, lane, g, leader, wq, xa, ya, oa, A);
+      r0 += kStride;
+      if (r0 >= R) break;
+      load_tile<QPL, RW>(a, idx_s, R, r0 + kStride, lane, g, xa, ya, oa);
+      consume_tile<QPL, RW>(a, m_s, lk_out, r0, lane, g, leader, wq, xb, yb, ob, A);
+      r0 += kStride;
     }
   } else {
-    // ------------------------------ consumers -----------------------------
-    float4 wq[QPL];
-    float4 acc[QPL];
-    const float* wc = a.w + static_cast<int64_t>(c) * a.d;
-#pragma unroll
-    for (int k = 0; k < QPL; ++k) {
-      const int j = 4 * (lane + 32 * k);
-      wq[k].x = j + 0 < a.d ? wc[j + 0] : 0.0f;
-      wq[k].y = j + 1 < a.d ? wc[j + 1] : 0.0f;
-      wq[k].z = j + 2 < a.d ? wc[j + 2] : 0.0f;
-      wq[k].w = j + 3 < a.d ? wc[j + 3] : 0.0f;
-      acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int r0 = warp * RW; r0 < R; r0 += kStride) {
+      float4 xv[RW][QPL];
+      float yv;
+      int og;
+      load_tile<QPL, RW>(a, idx_s, R, r0, lane, g, xv, yv, og);
+      consume_tile<QPL, RW>(a, m_s, lk_out, r0, lane, g, leader, wq, xv, yv, og, A);
     }
-    float* lk_out = a.lk != nullptr ? a.lk + static_cast<int64_t>(c) * a.n + row0
-                                    : nullptr;
-    for (int st = 0; st < n_stages; ++st) {
-      const int slot = st % a.stages;
-      const uint32_t ph = static_cast<uint32_t>(st / a.stages) & 1u;
-      if (!mbar_wait_bounded(&full[slot], ph, abort_flag)) {
-        if (lane == 0) {
-          raise_status(a.status, GBSGMC_ERR_TIMEOUT);
-          *abort_flag = 1;
-        }
-        break;
-      }
-      const float4* src = ring + static_cast<size_t>(slot) * kRowsPerStage * dq;
+  }
+  // Widen once: sum(lk) = s1 + n K, sum(lk^2) = s2 + 2 K s1 + n K^2.
+  const double K = A.K, n_l = A.cnt;
+  double my_mlk = A.mlk;
+  double my_lk = static_cast<double>(A.s1) + n_l * K;
+  double my_lk2 = static_cast<double>(A.s2) + 2.0 * K * A.s1 + n_l * K * K;
+  my_mlk = warp_sum(my_mlk);
+  my_lk = warp_sum(my_lk);
+  my_lk2 = warp_sum(my_lk2);
 #pragma unroll
-      for (int rr = 0; rr < kRowsPerWarpStage; ++rr) {
-        const int r = rr * kConsumerWarps + warp;
-        const int row = st * kRowsPerStage + r;
-        if (row >= R || idx_s[row] < 0) continue;
-        const float4* xr = src + static_cast<size_t>(r) * dq;
-        float4 xv[QPL];
-        float z = 0.0f;
-#pragma unroll
-        for (int k = 0; k < QPL; ++k) {
-          const int q = lane + 32 * k;
-          if (q < dq) {
-            xv[k] = xr[q];
-            z = fmaf(xv[k].x, wq[k].x, z);
-            z = fmaf(xv[k].y, wq[k].y, z);
-            z = fmaf(xv[k].z, wq[k].z, z);
-            z = fmaf(xv[k].w, wq[k].w, z);
-          } else {
-            xv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-        }
-        z = warp_sum(z);
-        const float yv = y_s[row];
-        float lkv, dz;
-        if (a.family == GBSGMC_GLM_LOGISTIC) {
-          lkv = yv * z - softplusf(z);
-          dz = yv - sigmoidf(z);
-        } else if (a.family == GBSGMC_GLM_LINEAR) {
-          lkv = z;
-          dz = 1.0f;
-        } else {
-          const float res = yv - z;
-          lkv = -0.5f * res * res * a.inv_s2 - a.log_norm;
-          dz = res * a.inv_s2;
-        }
-        const float mw = m_s[row];
-        const float coef = mw * dz;
-#pragma unroll
-        for (int k = 0; k < QPL; ++k) {
-          acc[k].x = fmaf(coef, xv[k].x, acc[k].x);
-          acc[k].y = fmaf(coef, xv[k].y, acc[k].y);
-          acc[k].z = fmaf(coef, xv[k].z, acc[k].z);
-          acc[k].w = fmaf(coef, xv[k].w, acc[k].w);
-        }
-        if (lane == 0) {
-          my_mlk += static_cast<double>(mw) * lkv;
-          my_lk += lkv;
-          my_lk2 += static_cast<double>(lkv) * lkv;
-          if (lk_out != nullptr) lk_out[row] = lkv;
-        }
-      }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[slot]);
-    }
-#pragma unroll
-    for (int k = 0; k < QPL; ++k) {
-      const int q = lane + 32 * k;
-      if (q < dq) red[warp * dq + q] = acc[k];
-    }
-    if (lane == 0) {
-      sums[warp * 4 + 0] = my_mlk;
-      sums[warp * 4 + 1] = my_lk;
-      sums[warp * 4 + 2] = my_lk2;
-    }
+  for (int k = 0; k < QPL; ++k) {
+    const int q = lane + 32 * k;
+    if (q < dq) red[warp * dq + q] = A.acc[k];
+  }
+  if (lane == 0) {
+    sums[warp * 4 + 0] = my_mlk;
+    sums[warp * 4 + 1] = my_lk;
+    sums[warp * 4 + 2] = my_lk2;
   }
   __syncthreads();
 
   // Reduce the warp partials in a fixed order: partial gradient in red[0..dq).
   for (int q = tid; q < dq; q += kThreads) {
     float4 t = red[q];
-    for (int w = 1; w < kConsumerWarps; ++w) {
+    for (int w = 1; w < kWarps; ++w) {
       const float4 u = red[w * dq + q];
       t.x += u.x;
       t.y += u.y;
@@ -319,14 +399,14 @@ __global__ void __launch_bounds__(kThreads)
   }
   if (tid == 0) {
     double t0 = 0.0, t1 = 0.0, t2 = 0.0;
-    for (int w = 0; w < kConsumerWarps; ++w) {
+    for (int w = 0; w < kWarps; ++w) {
       t0 += sums[w * 4 + 0];
       t1 += sums[w * 4 + 1];
       t2 += sums[w * 4 + 2];
     }
-    sums[kConsumerWarps * 4 + 0] = t0;
-    sums[kConsumerWarps * 4 + 1] = t1;
-    sums[kConsumerWarps * 4 + 2] = t2;
+    sums[kWarps * 4 + 0] = t0;
+    sums[kWarps * 4 + 1] = t1;
+    sums[kWarps * 4 + 2] = t2;
   }
   __syncthreads();
 
@@ -334,9 +414,9 @@ __global__ void __launch_bounds__(kThreads)
     const int64_t pc = static_cast<int64_t>(c) * a.slices + s;
     for (int q = tid; q < dq; q += kThreads) a.ws_part[pc * dq + q] = red[q];
     if (tid == 0) {
-      a.ws_sums[pc * 4 + 0] = sums[kConsumerWarps * 4 + 0];
-      a.ws_sums[pc * 4 + 1] = sums[kConsumerWarps * 4 + 1];
-      a.ws_sums[pc * 4 + 2] = sums[kConsumerWarps * 4 + 2];
+      a.ws_sums[pc * 4 + 0] = sums[kWarps * 4 + 0];
+      a.ws_sums[pc * 4 + 1] = sums[kWarps * 4 + 1];
+      a.ws_sums[pc * 4 + 2] = sums[kWarps * 4 + 2];
     }
     __threadfence();
     __syncthreads();
@@ -369,17 +449,17 @@ __global__ void __launch_bounds__(kThreads)
         t1 += __ldcg(ps + k * 4 + 1);
         t2 += __ldcg(ps + k * 4 + 2);
       }
-      sums[kConsumerWarps * 4 + 0] = t0;
-      sums[kConsumerWarps * 4 + 1] = t1;
-      sums[kConsumerWarps * 4 + 2] = t2;
+      sums[kWarps * 4 + 0] = t0;
+      sums[kWarps * 4 + 1] = t1;
+      sums[kWarps * 4 + 2] = t2;
     }
     __syncthreads();
   }
 
   // ------------------------------ epilogue ---------------------------------
-  const double sum_mlk = sums[kConsumerWarps * 4 + 0];
-  const double sum_lk = sums[kConsumerWarps * 4 + 1];
-  const double sum_lk2 = sums[kConsumerWarps * 4 + 2];
+  const double sum_mlk = sums[kWarps * 4 + 0];
+  const double sum_lk = sums[kWarps * 4 + 1];
+  const double sum_lk2 = sums[kWarps * 4 + 2];
   float* wc = a.w + static_cast<int64_t>(c) * a.d;
   const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n);
 
@@ -513,67 +593,150 @@ int sm_count() {
   return cached;
 }
 
-int choose_stages(int dq) {
-  const size_t stage_bytes = static_cast<size_t>(kRowsPerStage) * dq * 16;
-  int st = static_cast<int>(kRingBudget / stage_bytes);
-  return std::max(2, std::min(8, st));
+// Rows a warp holds at once, and the CTAs per SM the register budget is set
+// for, per float4-column count QPL.  More rows per warp cut the per-row
+// instruction count (one transposed reduction and one link evaluation per
+// lane group) at the price of registers and resident warps; for d <= 256 the
+// measured best is 4 rows per warp at 3 CTAs/SM.  Plans autotune this.
+__host__ __device__ constexpr int default_rows_per_warp(int qpl) {
+  return qpl <= 2 ? 4 : (qpl == 4 ? 2 : 1);
 }
 
-// Slices per chain: enough CTAs for about three waves of two CTAs per SM,
-// at most kMaxRowsPerSlice rows and at least 32 rows per slice.
-int choose_slices(int chains, int n) {
-  const int need = ceil_div(n, kMaxRowsPerSlice);
-  const int target = 3 * 2 * sm_count();
-  int s = std::max(1, ceil_div(target, std::max(chains, 1)));
-  s = std::min(s, std::max(1, n / 32));
-  s = std::max(s, need);
-  s = std::min(s, slices_alloc(n));
-  return s;
+int qpl_for(int dq) { return dq <= 32 ? 1 : (dq <= 64 ? 2 : (dq <= 128 ? 4 : 8)); }
+
+int env_int(const char* name, int fallback) {
+  const char* v = std::getenv(name);
+  if (v == nullptr || *v == 0) return fallback;
+  const int x = std::atoi(v);
+  return x > 0 ? x : fallback;
+}
+
+int clamp_slices(int s, int n) {
+  return std::min(std::max(s, ceil_div(n, kMaxRowsPerSlice)),
+                  std::min(slices_alloc(n), std::max(1, n)));
+}
+
+// Slices per chain when the caller does not choose: enough rows per CTA to
+// amortise its prologue and epilogue (about 384 KB of rows; the per-CTA fixed
+// cost was measured at tens of rows), but at least one CTA per SM for small
+// problems so that their latency is spread.  Plans autotune this choice.
+int choose_slices(int chains, int n, int row_bytes) {
+  const int forced = env_int("GBSGMC_GLM_SLICES", 0);
+  if (forced > 0) return clamp_slices(forced, n);
+  const double target = 384.0 * 1024.0;
+  int s = static_cast<int>(std::ceil(static_cast<double>(n) * row_bytes / target));
+  if (static_cast<int64_t>(chains) * s < sm_count())
+    s = std::max(s, std::min(ceil_div(sm_count(), std::max(chains, 1)), n / 32));
+  return clamp_slices(std::max(s, 1), n);
 }
 
 constexpr int kMaxDynSmem = 227 * 1024;
 
-template <int QPL>
-int prepare_q() {
-  static int done = 0;
-  if (done) return GBSGMC_OK;
-  const cudaError_t e = cudaFuncSetAttribute(
-      glm_kernel<QPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
-  if (e != cudaSuccess)
-    return set_error(GBSGMC_ERR_CUDA, "glm: cudaFuncSetAttribute: %s",
-                     cudaGetErrorString(e));
-  done = 1;
-  return GBSGMC_OK;
+// Register double-buffering of row tiles (GBSGMC_GLM_PREFETCH=1 enables).
+bool prefetch_tiles() {
+  const char* v = std::getenv("GBSGMC_GLM_PREFETCH");
+  return v != nullptr && v[0] == '1';
 }
+
+template <int QPL, int RW, bool PF, int MINB>
+struct Variant {
+  static int prepare() {
+    static int done = 0;
+    if (done) return GBSGMC_OK;
+    const cudaError_t e = cudaFuncSetAttribute(
+        glm_kernel<QPL, RW, PF, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        kMaxDynSmem);
+    if (e != cudaSuccess)
+      return set_error(GBSGMC_ERR_CUDA, "glm: cudaFuncSetAttribute: %s",
+                       cudaGetErrorString(e));
+    done = 1;
+    return GBSGMC_OK;
+  }
+  // Resident CTAs per SM for this variant at `smem` bytes (cached per size).
+  static int occupancy(size_t smem) {
+    static size_t last_smem = 0;
+    static int last = 0;
+    if (last > 0 && last_smem == smem) return last;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, glm_kernel<QPL, RW, PF, MINB>, kThreads, smem) != cudaSuccess ||
+        nb < 1)
+      nb = 1;
+    last_smem = smem;
+    last = nb;
+    return nb;
+  }
+  static int launch(GlmArgs a, size_t smem, cudaStream_t st) {
+    const int rc = prepare();
+    if (rc != GBSGMC_OK) return rc;
+    a.slices = a.slices_fixed > 0
+                   ? clamp_slices(a.slices_fixed, a.n)
+                   : choose_slices(a.chains, a.n,
+                                   static_cast<int>(std::min<int64_t>(a.ld, 1 << 20)) * 4);
+    a.rows_per_slice = ceil_div(a.n, a.slices);
+    if (a.slices > 1) {
+      if (a.ws_base == nullptr || a.ws_size < ws_bytes(a.chains, a.n, a.d))
+        return set_error(GBSGMC_ERR_ARG,
+                         "glm: workspace missing or too small (need %zu bytes)",
+                         ws_bytes(a.chains, a.n, a.d));
+      const WsView v = ws_view(a.ws_base, a.chains, a.n, a.d);
+      a.ws_part = v.part;
+      a.ws_sums = v.sums;
+      a.ws_ticket = v.ticket;
+    }
+    dim3 grid(a.slices, a.chains);
+    glm_kernel<QPL, RW, PF, MINB><<<grid, kThreads, smem, st>>>(a);
+    return check_launch("glm_kernel");
+  }
+};
+
+// Tile shape for the d <= 256 kernels: GBSGMC_GLM_RW = 1, 2 or 4 rows per
+// warp (default 2); GBSGMC_GLM_PREFETCH=1 double-buffers row tiles.
+int rows_override() { return env_int("GBSGMC_GLM_RW", 0); }
 
 template <int QPL>
 int launch_q(const GlmArgs& a, size_t smem, cudaStream_t st) {
-  const int rc = prepare_q<QPL>();
-  if (rc != GBSGMC_OK) return rc;
-  dim3 grid(a.slices, a.chains);
-  glm_kernel<QPL><<<grid, kThreads, smem, st>>>(a);
-  return check_launch("glm_kernel");
+  const bool pf = prefetch_tiles();
+  if constexpr (QPL <= 2) {
+    const int rw = a.rw_fixed > 0 ? a.rw_fixed
+                   : (rows_override() > 0 ? rows_override()
+                                          : default_rows_per_warp(QPL));
+    if (rw == 1) return pf ? Variant<QPL, 1, true, 4>::launch(a, smem, st)
+                           : Variant<QPL, 1, false, 6>::launch(a, smem, st);
+    if (rw == 4) return pf ? Variant<QPL, 4, true, 2>::launch(a, smem, st)
+                           : Variant<QPL, 4, false, 3>::launch(a, smem, st);
+    return pf ? Variant<QPL, 2, true, 3>::launch(a, smem, st)
+              : Variant<QPL, 2, false, 4>::launch(a, smem, st);
+  } else if constexpr (QPL == 4) {
+    return pf ? Variant<4, 2, true, 2>::launch(a, smem, st)
+              : Variant<4, 2, false, 2>::launch(a, smem, st);
+  } else {
+    return Variant<8, 1, false, 2>::launch(a, smem, st);
+  }
 }
 
 int launch_glm(GlmArgs& a, cudaStream_t st) {
   if (a.chains == 0 || a.n == 0) return GBSGMC_OK;
-  a.stages = choose_stages(a.dq);
-  const SmemLayout L = smem_layout(a.rows_per_slice, a.dq, a.stages);
+  const int qpl = qpl_for(a.dq);
+  // Shared memory sized for the largest slice any choice can give.
+  const SmemLayout L = smem_layout(std::min(a.n, kMaxRowsPerSlice), a.dq);
   if (L.total > 227 * 1024)
     return set_error(GBSGMC_ERR_SHAPE, "glm: shared memory %zu too large",
                      L.total);
-  if (a.dq <= 32) return launch_q<1>(a, L.total, st);
-  if (a.dq <= 64) return launch_q<2>(a, L.total, st);
-  if (a.dq <= 128) return launch_q<4>(a, L.total, st);
+  if (qpl == 1) return launch_q<1>(a, L.total, st);
+  if (qpl == 2) return launch_q<2>(a, L.total, st);
+  if (qpl == 4) return launch_q<4>(a, L.total, st);
   return launch_q<8>(a, L.total, st);
 }
 
 int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
                 const int32_t* idx, int64_t idx_stride, const float* mask,
-                void* ws, size_t ws_size, int* status, int slices_override = 0) {
+                void* ws, size_t ws_size, int* status, GlmTune tune = GlmTune{}) {
   if (m == nullptr || m->X == nullptr || idx == nullptr ||
-      (m->y == nullptr && m->family != GBSGMC_GLM_LINEAR))
+      (m->y == nullptr && !m->y_inline && m->family != GBSGMC_GLM_LINEAR))
     return set_error(GBSGMC_ERR_ARG, "glm: null model, data or index pointer");
+  if (m->y_inline && m->ld < static_cast<int64_t>(m->d) + 1)
+    return set_error(GBSGMC_ERR_ARG, "glm: y_inline needs ld >= d + 1");
   if (m->family != GBSGMC_GLM_LINEAR_GAUSSIAN && m->family != GBSGMC_GLM_LOGISTIC &&
       m->family != GBSGMC_GLM_LINEAR)
     return set_error(GBSGMC_ERR_ARG, "glm: unknown family %d", m->family);
@@ -589,19 +752,10 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
     return set_error(GBSGMC_ERR_ARG, "glm: sigma must be positive");
   if (!(m->temperature > 0.0f))
     return set_error(GBSGMC_ERR_ARG, "glm: temperature must be positive");
-  int S = choose_slices(chains, n);
-  if (slices_override > 0)
-    S = std::min(std::max(slices_override, ceil_div(n, kMaxRowsPerSlice)),
-                 std::min(slices_alloc(n), std::max(1, n)));
-  if (S > 1) {
-    if (ws == nullptr || ws_size < ws_bytes(chains, n, m->d))
-      return set_error(GBSGMC_ERR_ARG, "glm: workspace missing or too small "
-                                       "(need %zu bytes)",
-                       ws_bytes(chains, n, m->d));
-  }
   a.family = m->family;
   a.d = m->d;
   a.dq = (m->d + 3) / 4;
+  a.y_inline = m->y_inline ? 1 : 0;
   a.n_obs = m->n_obs;
   a.n_rows = m->n_rows > 0 ? m->n_rows : m->n_obs;
   a.ld = m->ld;
@@ -621,25 +775,23 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.inv_temp = 1.0f / m->temperature;
   a.chains = chains;
   a.n = n;
-  a.slices = S;
-  a.rows_per_slice = ceil_div(n, S);
+  a.slices = 0;
+  a.rows_per_slice = 0;
+  if (tune.slices == 0 && tune.rows_per_warp == 0)
+    glm_tune_lookup(chains, n, m->d, m->ld, &tune);
+  a.slices_fixed = tune.slices;
+  a.rw_fixed = tune.rows_per_warp;
+  a.ws_base = ws;
+  a.ws_size = ws_size;
+  a.ws_part = nullptr;
+  a.ws_sums = nullptr;
+  a.ws_ticket = nullptr;
   a.idx = idx;
   a.idx_stride = idx_stride;
   a.mask = mask;
-  if (S > 1) {
-    const WsView v = ws_view(ws, chains, n, m->d);
-    a.ws_part = v.part;
-    a.ws_sums = v.sums;
-    a.ws_ticket = v.ticket;
-  } else {
-    a.ws_part = nullptr;
-    a.ws_sums = nullptr;
-    a.ws_ticket = nullptr;
-  }
   a.status = status;
-  const bool aligned = (reinterpret_cast<uintptr_t>(m->X) % 16 == 0) &&
-                       (m->ld % 4 == 0) && (m->d % 4 == 0);
-  a.bulk = aligned ? 1 : 0;
+  // 128-bit row loads need every row 16-byte aligned.
+  a.vec4 = (reinterpret_cast<uintptr_t>(m->X) % 16 == 0) && (m->ld % 4 == 0) ? 1 : 0;
   a.lk = nullptr;
   a.lk_var = nullptr;
   a.grad = nullptr;
@@ -654,20 +806,44 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   return GBSGMC_OK;
 }
 
+struct TuneKey {
+  int chains, n, d;
+  int64_t ld;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(chains, n, d, ld) < std::tie(o.chains, o.n, o.d, o.ld);
+  }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, GlmTune> g_tune_cache;
+
 }  // namespace
+
+bool glm_tune_lookup(int chains, int n, int d, int64_t ld, GlmTune* out) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tune_cache.find(TuneKey{chains, n, d, ld});
+  if (it == g_tune_cache.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+void glm_tune_store(int chains, int n, int d, int64_t ld, GlmTune t) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tune_cache[TuneKey{chains, n, d, ld}] = t;
+}
 
 // Shared with the plan implementation.
 size_t glm_ws_bytes(int chains, int n, int d) { return ws_bytes(chains, n, d); }
 
 int glm_prepare() {
-  int rc = prepare_q<1>();
-  if (rc == GBSGMC_OK) rc = prepare_q<2>();
-  if (rc == GBSGMC_OK) rc = prepare_q<4>();
-  if (rc == GBSGMC_OK) rc = prepare_q<8>();
+  // Sets the shared-memory attribute of the default variants before any
+  // stream capture; others are prepared on their first launch.
+  int rc = Variant<1, 2, false, 4>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 2, false, 4>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<4, 2, false, 2>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<8, 1, false, 2>::prepare();
   return rc;
 }
 
-int glm_default_slices(int chains, int n) { return choose_slices(chains, n); }
 
 int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   const int32_t* idx_dev, int64_t idx_stride, float* w_dev,
@@ -675,10 +851,10 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   const gbsgmc_sched* sched, const gbsgmc_noise* noise,
                   double* U_dev, double* lk_var_dev, float* samples_dev,
                   double* sample_lik_dev, void* ws, size_t ws_size,
-                  int* status_dev, cudaStream_t stream, int slices) {
+                  int* status_dev, cudaStream_t stream, GlmTune tune) {
   GlmArgs a;
   int rc = fill_common(a, model, chains, n, idx_dev, idx_stride, nullptr, ws,
-                       ws_size, status_dev, slices);
+                       ws_size, status_dev, tune);
   if (rc != GBSGMC_OK) return rc;
   if (w_dev == nullptr || sched == nullptr || noise == nullptr)
     return set_error(GBSGMC_ERR_ARG, "sgld_glm_step: null w, sched or noise");
@@ -742,5 +918,5 @@ extern "C" int gbsgmc_sgld_glm_step(
                        alpha, lmbd, sched, noise, U_dev, lk_var_dev,
                        samples_dev, sample_lik_dev, workspace_dev,
                        workspace_bytes, status_dev,
-                       static_cast<cudaStream_t>(stream), 0);
+                       static_cast<cudaStream_t>(stream), GlmTune{});
 }

@@ -13,16 +13,24 @@ int set_error(int code, const char* fmt, ...);
 int check_launch(const char* what);
 
 // glm.cu
+// Launch shape of the GLM kernel; 0 lets the library choose.
+struct GlmTune {
+  int slices = 0;         // CTAs per chain
+  int rows_per_warp = 0;  // 1, 2 or 4 (d <= 256 only)
+};
+
 size_t glm_ws_bytes(int chains, int n, int d);
+// Launch shapes chosen by the plan autotuner, per problem shape.
+bool glm_tune_lookup(int chains, int n, int d, int64_t ld, GlmTune* out);
+void glm_tune_store(int chains, int n, int d, int64_t ld, GlmTune t);
 int glm_prepare();
-int glm_default_slices(int chains, int n);
 int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   const int32_t* idx_dev, int64_t idx_stride, float* w_dev,
                   float* v_dev, float alpha, float lmbd,
                   const gbsgmc_sched* sched, const gbsgmc_noise* noise,
                   double* U_dev, double* lk_var_dev, float* samples_dev,
                   double* sample_lik_dev, void* ws, size_t ws_size,
-                  int* status_dev, cudaStream_t stream, int slices);
+                  int* status_dev, cudaStream_t stream, GlmTune tune);
 
 // rng.cu
 int launch_philox_index(uint64_t seed, int chain_base, int chains,

@@ -90,5 +90,5 @@ extern "C" int gbsgmc_sgld_glm_step_noalloc(
   return glm_sgld_step(model, chains, n, idx_dev, idx_stride, w_dev, v_dev,
                        alpha, lmbd, sched, noise, U_dev, lk_var_dev,
                        samples_dev, sample_lik_dev, scratch,
-                       kStaticScratchBytes, status_dev, s, 0);
+                       kStaticScratchBytes, status_dev, s, GlmTune{});
 }

@@ -48,8 +48,8 @@ PlainBuf carve(void* buf, int n, int d) {
 }
 
 __global__ void gather_kernel(const float* X, int64_t ld, const float* y,
-                              const int32_t* idx, int n, int d, int64_t n_obs,
-                              float* xb, float* yb, int* status) {
+                              int y_inline, const int32_t* idx, int n, int d,
+                              int64_t n_obs, float* xb, float* yb, int* status) {
   const int i = blockIdx.x;
   int32_t o = idx[i];
   if (o < 0 || o >= n_obs) {
@@ -58,7 +58,8 @@ __global__ void gather_kernel(const float* X, int64_t ld, const float* y,
   }
   for (int j = threadIdx.x; j < d; j += blockDim.x)
     xb[static_cast<int64_t>(i) * d + j] = X[o * ld + j];
-  if (threadIdx.x == 0) yb[i] = y != nullptr ? y[o] : 0.0f;
+  if (threadIdx.x == 0)
+    yb[i] = y_inline ? X[o * ld + d] : (y != nullptr ? y[o] : 0.0f);
 }
 
 __global__ void gemv_kernel(const float* xb, const float* w, int n, int d,
@@ -191,7 +192,7 @@ extern "C" int gbsgmc_plain_sgld_glm_step(
   }
   const double n_over = static_cast<double>(m->n_obs) / n;
   const Sched sc = to_sched(sched);
-  gather_kernel<<<n, 128, 0, s>>>(m->X, m->ld, m->y, idx_dev, n, d,
+  gather_kernel<<<n, 128, 0, s>>>(m->X, m->ld, m->y, m->y_inline, idx_dev, n, d,
                                   m->n_rows > 0 ? m->n_rows : m->n_obs, b.xb,
                                   b.yb, status_dev);
   gemv_kernel<<<(n + 7) / 8, 256, 0, s>>>(b.xb, w_dev, n, d, b.z);

@@ -8,8 +8,13 @@
 // The block is captured once into a CUDA graph and replayed, so a run of K
 // steps costs K/G graph launches on the host.  The schedule tables (step
 // size, temperature, keep slots) are read on the device at step k.
+#include <cmath>
 #include <cstdlib>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
+#include <vector>
 
 #include "common.cuh"
 #include "internal.h"
@@ -29,7 +34,7 @@ struct gbsgmc_plan {
   double* sample_lik;
   int* status;
   int G;
-  int slices;
+  gbsgmc::GlmTune tune;
   bool use_graph;
   cudaStream_t stream;
   void* ws;
@@ -72,11 +77,106 @@ int enqueue_block(gbsgmc_plan* p, int g, cudaStream_t s) {
     rc = glm_sgld_step(&p->model, p->chains, p->n, p->idx + j * cn, p->n, p->w,
                        p->v, p->alpha, p->lmbd, &sj, &p->noise, p->U,
                        p->lk_var, p->samples, p->sample_lik, p->ws, p->ws_size,
-                       p->status, s, p->slices);
+                       p->status, s, p->tune);
     if (rc != GBSGMC_OK) return rc;
   }
   advance_counter_kernel<<<1, 1, 0, s>>>(p->base, g);
   return check_launch("plan: advance counter");
+}
+
+// Autotuner: times candidate launch shapes of the fused step (CTAs per chain
+// and rows per warp) on scratch copies of the chain state and keeps the
+// fastest.  The choice is cached per problem shape for the process, and
+// direct step launches of that shape use it too.
+int autotune(gbsgmc_plan* p) {
+  const char* env = std::getenv("GBSGMC_AUTOTUNE");
+  if (env != nullptr && env[0] == '0') return GBSGMC_OK;
+  if (glm_tune_lookup(p->chains, p->n, p->model.d, p->model.ld, &p->tune))
+    return GBSGMC_OK;
+  const int C = p->chains, n = p->n, d = p->model.d;
+  const size_t wbytes = sizeof(float) * static_cast<size_t>(C) * d;
+  float* w = nullptr;
+  float* v = nullptr;
+  int* status = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = GBSGMC_OK;
+  std::vector<GlmTune> cands;
+  {
+    const double rows_per_cta = (384.0 * 1024.0) / (4.0 * std::max<int64_t>(p->model.ld, 1));
+    const int base = std::max(1, static_cast<int>(std::ceil(n / rows_per_cta)));
+    const int ss[] = {base / 2, base - 1, base, base + 1, base + 2, 2 * base, 4 * base};
+    const int rws[] = {2, 4};
+    for (int s : ss) {
+      if (s < 1 || s > 64 || (s > 1 && n / s < 32)) continue;
+      if (d <= 256) {
+        for (int r : rws) cands.push_back(GlmTune{s, r});
+      } else {
+        cands.push_back(GlmTune{s, 0});
+      }
+    }
+  }
+  if (cands.size() <= 1) {
+    if (!cands.empty()) p->tune = cands[0];
+    return GBSGMC_OK;
+  }
+  do {
+    if ((rc = cuda_err(cudaMalloc(&w, wbytes), "autotune: scratch"))) break;
+    if ((rc = cuda_err(cudaMalloc(&v, wbytes), "autotune: scratch"))) break;
+    if ((rc = cuda_err(cudaMalloc(&status, sizeof(int)), "autotune: scratch"))) break;
+    if ((rc = cuda_err(cudaMemcpyAsync(w, p->w, wbytes, cudaMemcpyDeviceToDevice,
+                                       p->stream), "autotune: copy")))
+      break;
+    if (p->v != nullptr &&
+        (rc = cuda_err(cudaMemcpyAsync(v, p->v, wbytes, cudaMemcpyDeviceToDevice,
+                                       p->stream), "autotune: copy")))
+      break;
+    if ((rc = cuda_err(cudaMemsetAsync(status, 0, sizeof(int), p->stream),
+                       "autotune: memset")))
+      break;
+    if ((rc = cuda_err(cudaEventCreate(&e0), "autotune: event"))) break;
+    if ((rc = cuda_err(cudaEventCreate(&e1), "autotune: event"))) break;
+    const int64_t rows = p->model.n_rows > 0 ? p->model.n_rows : p->model.n_obs;
+    const int trials = std::min(8, p->G);
+    if ((rc = launch_philox_index(0x5EEDull, 0, C, nullptr, 0, trials, n, rows,
+                                  p->idx, n, static_cast<int64_t>(C) * n,
+                                  p->stream)))
+      break;
+    gbsgmc_sched sch = p->sched;
+    sch.base_dev = nullptr;
+    sch.keep_slot_dev = nullptr;
+    sch.offset = 0;
+    float best_ms = 1e30f;
+    GlmTune best = cands[0];
+    for (const GlmTune& t : cands) {
+      for (int rep = 0; rep < 2 + 6 && rc == GBSGMC_OK; ++rep) {
+        if (rep == 2) cudaEventRecord(e0, p->stream);
+        const int j = rep % trials;
+        rc = glm_sgld_step(&p->model, C, n, p->idx + static_cast<int64_t>(j) * C * n,
+                           n, w, p->v != nullptr ? v : nullptr, p->alpha, p->lmbd,
+                           &sch, &p->noise, p->U, p->lk_var, nullptr, nullptr,
+                           p->ws, p->ws_size, status, p->stream, t);
+      }
+      if (rc != GBSGMC_OK) break;
+      cudaEventRecord(e1, p->stream);
+      if ((rc = cuda_err(cudaEventSynchronize(e1), "autotune: sync"))) break;
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = t;
+      }
+    }
+    if (rc != GBSGMC_OK) break;
+    p->tune = best;
+    glm_tune_store(p->chains, p->n, p->model.d, p->model.ld, best);
+  } while (false);
+  cudaStreamSynchronize(p->stream);
+  if (e0 != nullptr) cudaEventDestroy(e0);
+  if (e1 != nullptr) cudaEventDestroy(e1);
+  if (w != nullptr) cudaFree(w);
+  if (v != nullptr) cudaFree(v);
+  if (status != nullptr) cudaFree(status);
+  return rc;
 }
 
 void release(gbsgmc_plan* p) {
@@ -160,7 +260,7 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
                        "plan_create: memset")))
       break;
     if ((rc = glm_prepare())) break;
-    p->slices = glm_default_slices(chains, n);
+    if ((rc = autotune(p))) break;
     if (p->use_graph) {
       if ((rc = cuda_err(cudaStreamBeginCapture(p->stream,
                                                 cudaStreamCaptureModeThreadLocal),
@@ -216,6 +316,15 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
   if ((rc = cuda_err(cudaEventRecord(p->ev_out, p->stream), "plan_run: record")))
     return rc;
   return cuda_err(cudaStreamWaitEvent(us, p->ev_out, 0), "plan_run: wait");
+}
+
+extern "C" int gbsgmc_plan_launch_shape(const gbsgmc_plan* p, int* slices,
+                                        int* rows_per_warp) {
+  if (p == nullptr || slices == nullptr || rows_per_warp == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "plan_launch_shape: null argument");
+  *slices = p->tune.slices;
+  *rows_per_warp = p->tune.rows_per_warp;
+  return GBSGMC_OK;
 }
 
 extern "C" int64_t gbsgmc_plan_launches(const gbsgmc_plan* p, int64_t steps) {

@@ -74,9 +74,11 @@ __global__ void sgld_update_kernel(int chains, int64_t P, float* x,
   }
 }
 
-__device__ __forceinline__ void add_ke(double* ke, int c, double part) {
-  part = warp_sum(part);
-  if ((threadIdx.x & 31) == 0 && ke != nullptr) atomicAdd(ke + c, part);
+// Per-thread kinetic-energy partials are fp32 (a thread sees few
+// parameters); the warp sum and the accumulation across warps are fp64.
+__device__ __forceinline__ void add_ke(double* ke, int c, float part) {
+  const double w = warp_sum(static_cast<double>(part));
+  if ((threadIdx.x & 31) == 0 && ke != nullptr) atomicAdd(ke + c, w);
 }
 
 __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
@@ -93,7 +95,7 @@ __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
   const float half = 0.5f * h;
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
-  double ke = 0.0;
+  float ke = 0.0f;
   for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     float xi[4];
@@ -104,7 +106,7 @@ __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
       if (j >= P) break;
       const float mi = mass_inv(mass, j);
       float pj = keep * p[off + j] + inject * (mass_sqrt(mass, j) * xi[e]);
-      ke += 0.5 * static_cast<double>(pj) * static_cast<double>(mi * pj);
+      ke = fmaf(0.5f * pj, mi * pj, ke);
       pj = -half * g1[off + j] + pj;
       p[off + j] = pj;
       x[off + j] = x[off + j] + h * (mi * pj);
@@ -127,7 +129,7 @@ __global__ void obabo_second_kernel(int chains, int64_t P, float* p,
   const float half = 0.5f * h;
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
-  double ke = 0.0;
+  float ke = 0.0f;
   for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     float xi[4];
@@ -138,7 +140,7 @@ __global__ void obabo_second_kernel(int chains, int64_t P, float* p,
       if (j >= P) break;
       const float mi = mass_inv(mass, j);
       float pj = -half * g2[off + j] + p[off + j];
-      ke += 0.5 * static_cast<double>(pj) * static_cast<double>(mi * pj);
+      ke = fmaf(0.5f * pj, mi * pj, ke);
       pj = keep * pj + inject * (mass_sqrt(mass, j) * xi[e]);
       p[off + j] = pj;
     }

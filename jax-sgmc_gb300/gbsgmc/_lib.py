@@ -52,7 +52,7 @@ class Glm(C.Structure):
   _fields_ = [("family", C.c_int), ("d", C.c_int), ("n_obs", C.c_int64),
               ("ld", C.c_int64), ("X", C.c_void_p), ("y", C.c_void_p),
               ("sigma", C.c_float), ("prior_scale", C.c_float),
-              ("temperature", C.c_float), ("_pad", C.c_int),
+              ("temperature", C.c_float), ("y_inline", C.c_int),
               ("n_rows", C.c_int64)]
 
 
@@ -120,6 +120,7 @@ SIGNATURES = {
                                          _vp]),
     "gbsgmc_plan_run": (_i, [_vp, _i64, _i64, _vp]),
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
+    "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i)]),
     "gbsgmc_plan_destroy": (_i, [_vp]),
     "gbsgmc_plain_buffer_bytes": (_sz, [_i, _i]),
     "gbsgmc_plain_sgld_glm_step": (_i, [_P(Glm), _i, _vp, _vp, _vp, _f, _f,

@@ -149,47 +149,95 @@ class HostDataLoader(DataLoader, metaclass=abc.ABCMeta):
 # ---------------------------------------------------------------------------
 
 class DeviceDataset:
-  """All fields of a loader resident in HBM as fp32.
+  """A loader's arrays resident in HBM as fp32, uploaded on first use.
 
-  A 2-D field ``[N, d]`` is stored row-major with the row stride rounded up to
-  a multiple of four floats (16 bytes) and zero padding, so that every row
-  starts 16-byte aligned and can be fetched with one bulk copy.  1-D fields
-  (targets) are stored as ``[N]``.
+  * ``matrix(name)``: a 2-D field ``[N, d]`` stored row-major with the row
+    stride rounded up to a multiple of four floats and zero padding, so that
+    every row starts 16-byte aligned and can be fetched with one bulk copy.
+  * ``vector(name)``: a width-1 field (targets) as ``[N]``.
+  * ``glm_view(x, y)``: the layout the GLM kernels read -- row i holds
+    ``[x_i (d floats), y_i, zero padding]`` with a stride that is a multiple
+    of eight floats, so every row starts on a 32-byte sector and the target
+    arrives in the row's own sectors.
   """
 
   def __init__(self, arrays: Dict[str, np.ndarray]):
     import torch
     if not torch.cuda.is_available():
       raise RuntimeError("gbsgmc needs a CUDA device: the dataset lives in HBM")
-    self.fields = {}
+    self._host = {k: np.asarray(v) for k, v in arrays.items()}
+    self._fields = {}
+    self._views = {}
     self.observation_count = None
-    for name, a in arrays.items():
-      a = np.asarray(a)
-      if self.observation_count is None:
-        self.observation_count = a.shape[0]
-      if a.ndim == 1 or int(np.prod(a.shape[1:])) == 1:
-        flat = np.ascontiguousarray(a.reshape(-1), dtype=np.float32)
-        self.fields[name] = (torch.from_numpy(flat).cuda(), 1, 1)
-      else:
-        flat = a.reshape(a.shape[0], -1).astype(np.float32)
-        d = flat.shape[1]
-        ld = (d + 3) // 4 * 4
-        t = torch.zeros((a.shape[0], ld), dtype=torch.float32, device="cuda")
-        t[:, :d] = torch.from_numpy(np.ascontiguousarray(flat)).cuda()
-        self.fields[name] = (t, d, ld)
+    for a in self._host.values():
+      self.observation_count = a.shape[0]
+      break
+
+  def keys(self):
+    return self._host.keys()
+
+  def __contains__(self, name):
+    return name in self._host
+
+  def field(self, name: str):
+    """(tensor, d, ld) of a field, uploaded on first use."""
+    import torch
+    got = self._fields.get(name)
+    if got is not None:
+      return got
+    a = self._host[name]
+    if a.ndim == 1 or int(np.prod(a.shape[1:])) == 1:
+      flat = np.ascontiguousarray(a.reshape(-1), dtype=np.float32)
+      got = (torch.from_numpy(flat).cuda(), 1, 1)
+    else:
+      flat = a.reshape(a.shape[0], -1)
+      d = flat.shape[1]
+      ld = (d + 3) // 4 * 4
+      t = torch.zeros((a.shape[0], ld), dtype=torch.float32, device="cuda")
+      t[:, :d].copy_(torch.from_numpy(np.ascontiguousarray(flat, np.float32)))
+      got = (t, d, ld)
+    self._fields[name] = got
+    return got
+
+  @property
+  def fields(self):
+    return {k: self.field(k) for k in self._host}
 
   def matrix(self, name: str):
     """(tensor [N, ld], d, ld) of a feature field; 1-D fields give d = 1."""
-    t, d, ld = self.fields[name]
+    t, d, ld = self.field(name)
     if t.dim() == 1:
       return t.view(-1, 1), 1, 1
     return t, d, ld
 
   def vector(self, name: str):
-    t, d, _ = self.fields[name]
+    t, d, _ = self.field(name)
     if t.dim() != 1:
       raise ValueError(f"field {name!r} is not a vector (width {d})")
     return t
+
+  def feature_dim(self, name: str) -> int:
+    a = self._host[name]
+    return 1 if a.ndim == 1 else int(np.prod(a.shape[1:]))
+
+  def glm_view(self, x: str, y: str):
+    """(tensor [N, ld], d, ld) with y_i stored at column d of row i."""
+    import torch
+    key = (x, y)
+    got = self._views.get(key)
+    if got is not None:
+      return got
+    xa = self._host[x]
+    flat = xa.reshape(xa.shape[0], -1)
+    d = flat.shape[1]
+    ld = (d + 1 + 7) // 8 * 8     # whole 32-byte sectors per row
+    t = torch.zeros((xa.shape[0], ld), dtype=torch.float32, device="cuda")
+    t[:, :d].copy_(torch.from_numpy(np.ascontiguousarray(flat, np.float32)))
+    t[:, d].copy_(torch.from_numpy(
+        np.ascontiguousarray(self._host[y].reshape(-1), np.float32)))
+    got = (t, d, ld)
+    self._views[key] = got
+    return got
 
 
 class IndexedBatch:
@@ -205,13 +253,12 @@ class IndexedBatch:
     self.loader = loader
 
   def __getitem__(self, name):
-    import torch
-    t, d, _ = self.dataset.fields[name]
+    t, d, _ = self.dataset.field(name)
     rows = t.index_select(0, self.indices.long())
     return rows if t.dim() == 1 else rows[:, :d]
 
   def keys(self):
-    return self.dataset.fields.keys()
+    return self.dataset.keys()
 
   def __len__(self):
     return int(self.indices.numel())

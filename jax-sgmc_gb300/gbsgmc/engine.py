@@ -74,6 +74,13 @@ class SgldGlmPlan:
     _lib.call("gbsgmc_plan_run", self.handle, int(first_step), int(steps),
               _lib.stream_handle())
 
+  def launch_shape(self):
+    """(CTAs per chain, rows per warp) chosen by the autotuner."""
+    s, r = _lib.C.c_int(), _lib.C.c_int()
+    _lib.call("gbsgmc_plan_launch_shape", self.handle, _lib.C.byref(s),
+              _lib.C.byref(r))
+    return s.value, r.value
+
   def launches(self, steps) -> int:
     return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps)))
 

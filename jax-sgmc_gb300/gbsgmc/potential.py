@@ -75,18 +75,23 @@ class StochasticPotential:
 
   # -- model description ---------------------------------------------------
   def model(self, dataset, observation_count=None):
-    """``gbsgmc_glm`` for a device dataset."""
-    X, d, ld = dataset.matrix(self.likelihood.x)
-    y = None if self.likelihood.y is None else dataset.vector(self.likelihood.y)
+    """``gbsgmc_glm`` for a device dataset (targets stored inline in the
+    feature rows, see DeviceDataset.glm_view)."""
     n_obs = dataset.observation_count if observation_count is None \
         else observation_count
+    if self.likelihood.y is None:
+      X, d, ld = dataset.matrix(self.likelihood.x)
+      inline = 0
+    else:
+      X, d, ld = dataset.glm_view(self.likelihood.x, self.likelihood.y)
+      inline = 1
     return _lib.Glm(self.likelihood.family, d, int(n_obs), ld, X.data_ptr(),
-                    _lib.ptr(y), float(self.likelihood.sigma),
-                    float(self.prior.scale), float(self.temperature), 0,
-                    int(dataset.observation_count)), (X, y)
+                    None, float(self.likelihood.sigma),
+                    float(self.prior.scale), float(self.temperature), inline,
+                    int(dataset.observation_count)), (X,)
 
   def dim(self, dataset) -> int:
-    return dataset.matrix(self.likelihood.x)[1]
+    return dataset.feature_dim(self.likelihood.x)
 
   def status(self):
     import torch
@@ -155,7 +160,7 @@ class StochasticPotential:
   def _eval_sample(self, sample, reference_data, mask, grad, lk):
     batch, info = self._unpack(reference_data)
     ds = batch.dataset
-    self.likelihood.check_data(ds.fields)
+    self.likelihood.check_data(ds)
     d = self.dim(ds)
     w = _flat_device(sample, d).view(1, d)
     idx = batch.indices.reshape(1, -1)

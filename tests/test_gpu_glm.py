@@ -211,3 +211,36 @@ def test_out_of_range_index_sets_status(lib):
   pot.check_status()
 
 
+
+
+@pytest.mark.parametrize("d,ld,inline", [(6, 6, 0), (8, 8, 0), (5, 6, 1), (7, 12, 1),
+                                         (256, 256, 0)])
+def test_row_layouts_through_the_abi(lib, d, ld, inline):
+  """Targets in a separate array or inline at column d; row strides that do
+  (bulk copies) or do not (plain loads) allow 16-byte aligned rows."""
+  import torch
+  from gbsgmc import _lib
+  N, C, n = 3000, 3, 200
+  X, y = make_data(N, d, O.LOGISTIC, seed=d + ld)
+  Xd = torch.zeros((N, ld), dtype=torch.float32, device="cuda")
+  Xd[:, :d] = torch.from_numpy(X).cuda()
+  yd = torch.from_numpy(y).cuda()
+  if inline:
+    Xd[:, d] = yd
+  m = _lib.Glm(_lib.GLM_LOGISTIC, d, N, ld, Xd.data_ptr(),
+               None if inline else yd.data_ptr(), 1.0, 2.0, 1.0, inline, N)
+  rng = np.random.default_rng(d)
+  W = (rng.normal(size=(C, d)) / np.sqrt(d)).astype(np.float32)
+  idx = rng.integers(0, N, (C, n)).astype(np.int32)
+  Wd, idxd = torch.from_numpy(W).cuda(), torch.from_numpy(idx).cuda()
+  U = torch.zeros(C, dtype=torch.float64, device="cuda")
+  G = torch.zeros((C, d), dtype=torch.float32, device="cuda")
+  var = torch.zeros(C, dtype=torch.float64, device="cuda")
+  ws = torch.zeros(int(lib.gbsgmc_glm_workspace_bytes(C, n, d)), dtype=torch.uint8,
+                   device="cuda")
+  _lib.call("gbsgmc_glm_value_and_grad", m, C, n, _lib.ptr(idxd), n, None,
+            _lib.ptr(Wd), _lib.ptr(U), _lib.ptr(G), None, _lib.ptr(var),
+            _lib.ptr(ws), ws.numel(), None, None)
+  ref = O.glm_potential(W, X, y, idx, N, O.LOGISTIC, 1.0, 2.0, 1.0)
+  from types import SimpleNamespace
+  check(SimpleNamespace(U=U, grad=G, lk_var=var), ref)
