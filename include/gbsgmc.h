@@ -255,6 +255,23 @@ int gbsgmc_swap_rows(int pairs, int64_t width, float* a_dev, float* b_dev,
                      const int32_t* perm_dev, gbsgmc_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Tensor-core GEMM (building block of the network likelihoods)              */
+/* ------------------------------------------------------------------------ */
+
+/* C[b] = A[b] * B[b]^T for b < batch on the tcgen05 tensor cores: A is M x K
+ * and B is N x K, both BF16 row-major with K contiguous (leading dimensions
+ * lda, ldb, multiples of 8; base addresses 16-byte aligned); C is M x N fp32
+ * (ldc a multiple of 4).  Needs M % 128 == 0, N % 128 == 0, K % 64 == 0.
+ * Replaces the XLA dot_general that jax.grad of a dense-network likelihood
+ * lowers to (the reference's likelihood is user code, e.g.
+ * examples/cifar.md:203-210). */
+int gbsgmc_gemm_bf16_nt(const void* A_dev, int64_t lda, int64_t a_batch_stride,
+                        const void* B_dev, int64_t ldb, int64_t b_batch_stride,
+                        float* C_dev, int64_t ldc, int64_t c_batch_stride,
+                        int batch, int M, int N, int K, int* status_dev,
+                        gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* Fused SGLD step for the generalised-linear families                       */
 /* ------------------------------------------------------------------------ */
 
@@ -347,13 +364,13 @@ int gbsgmc_plan_run(gbsgmc_plan* plan, int64_t first_step, int64_t steps,
                     gbsgmc_stream_t stream);
 
 /* The launch shape the plan's autotuner chose for the fused step: CTAs per
- * chain and rows per warp (0 = the library default).  The autotuner times a
+ * chain, rows per warp and warps per CTA (0 = the library default).  The autotuner times a
  * few candidate shapes on scratch copies of the chain state when the plan is
  * created (GBSGMC_AUTOTUNE=0 disables it) and caches the choice per problem
  * shape for the process.  No reference counterpart: launch configuration
  * only. */
 int gbsgmc_plan_launch_shape(const gbsgmc_plan* plan, int* slices,
-                             int* rows_per_warp);
+                             int* rows_per_warp, int* warps);
 
 /* Kernel launches one plan_run of `steps` steps performs (for accounting). */
 int64_t gbsgmc_plan_launches(const gbsgmc_plan* plan, int64_t steps);

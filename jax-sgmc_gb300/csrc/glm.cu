@@ -38,8 +38,7 @@
 namespace gbsgmc {
 namespace {
 
-constexpr int kWarps = 8;
-constexpr int kThreads = kWarps * 32;
+constexpr int kMaxWarps = 16;   // warps per CTA: 8 or 16 (a kernel parameter)
 constexpr int kMaxRowsPerSlice = 1024;
 constexpr int kMinSlicesAlloc = 16;
 
@@ -79,6 +78,7 @@ struct GlmArgs {
   size_t ws_size;
   int slices_fixed;   // > 0: slices per chain chosen by the caller
   int rw_fixed;       // > 0: rows per warp chosen by the caller
+  int warps_fixed;    // > 0: warps per CTA chosen by the caller
   int* status;
   int vec4;   // rows are 16-byte aligned: 128-bit loads
 };
@@ -91,7 +91,8 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) {
   return (x + a - 1) / a * a;
 }
 
-__host__ __device__ inline SmemLayout smem_layout(int rows_per_slice, int dq) {
+__host__ __device__ inline SmemLayout smem_layout(int rows_per_slice, int dq,
+                                                  int warps) {
   SmemLayout L;
   size_t o = 0;
   L.flags = o;
@@ -103,10 +104,10 @@ __host__ __device__ inline SmemLayout smem_layout(int rows_per_slice, int dq) {
   o += sizeof(float) * rows_per_slice;
   o = align_up(o, 16);
   L.red = o;
-  o += static_cast<size_t>(kWarps) * dq * 16;
+  o += static_cast<size_t>(warps) * dq * 16;
   o = align_up(o, 16);
   L.sums = o;
-  o += sizeof(double) * 4 * (kWarps + 1);
+  o += sizeof(double) * 4 * (warps + 1);
   L.total = o;
   return L;
 }
@@ -287,14 +288,14 @@ __device__ __forceinline__ void consume_tile(const GlmArgs& a, const float* m_s,
   }
 }
 
-template <int QPL, int RW, bool PF, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB)
+template <int QPL, int RW, bool PF, int MINB, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, MINB)
     glm_kernel(const GlmArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int LOG = Log2<RW>::v;
   constexpr int GROUP = 32 >> LOG;  // lanes per row in the link phase
   const int dq = a.dq;
-  const SmemLayout L = smem_layout(a.rows_per_slice, dq);
+  const SmemLayout L = smem_layout(a.rows_per_slice, dq, WARPS);
   int* is_last = reinterpret_cast<int*>(smem + L.flags);
   int32_t* idx_s = reinterpret_cast<int32_t*>(smem + L.idx);
   float* m_s = reinterpret_cast<float*>(smem + L.m);
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
 
   if (tid == 0) *is_last = 0;
   // Observation indices (and mask weights) of this slice.
-  for (int r = tid; r < R; r += kThreads) {
+  for (int r = tid; r < R; r += (WARPS * 32)) {
     int32_t o = __ldg(a.idx + c * a.idx_stride + row0 + r);
     if (o < 0 || o >= a.n_rows) {
       raise_status(a.status, GBSGMC_ERR_INDEX);
@@ -338,7 +339,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
   const bool leader = (lane & (GROUP - 1)) == 0;
   float* lk_out = a.lk != nullptr ? a.lk + static_cast<int64_t>(c) * a.n + row0
                                   : nullptr;
-  constexpr int kStride = kWarps * RW;
+  constexpr int kStride = WARPS * RW;
   if (PF) {
     // Two register tiles: the loads of the next tile are in flight while
     // the current one is consumed.
@@ -386,9 +387,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
   __syncthreads();
 
   // Reduce the warp partials in a fixed order: partial gradient in red[0..dq).
-  for (int q = tid; q < dq; q += kThreads) {
+  for (int q = tid; q < dq; q += (WARPS * 32)) {
     float4 t = red[q];
-    for (int w = 1; w < kWarps; ++w) {
+    for (int w = 1; w < WARPS; ++w) {
       const float4 u = red[w * dq + q];
       t.x += u.x;
       t.y += u.y;
@@ -399,24 +400,24 @@ __global__ void __launch_bounds__(kThreads, MINB)
   }
   if (tid == 0) {
     double t0 = 0.0, t1 = 0.0, t2 = 0.0;
-    for (int w = 0; w < kWarps; ++w) {
+    for (int w = 0; w < WARPS; ++w) {
       t0 += sums[w * 4 + 0];
       t1 += sums[w * 4 + 1];
       t2 += sums[w * 4 + 2];
     }
-    sums[kWarps * 4 + 0] = t0;
-    sums[kWarps * 4 + 1] = t1;
-    sums[kWarps * 4 + 2] = t2;
+    sums[WARPS * 4 + 0] = t0;
+    sums[WARPS * 4 + 1] = t1;
+    sums[WARPS * 4 + 2] = t2;
   }
   __syncthreads();
 
   if (a.slices > 1) {
     const int64_t pc = static_cast<int64_t>(c) * a.slices + s;
-    for (int q = tid; q < dq; q += kThreads) a.ws_part[pc * dq + q] = red[q];
+    for (int q = tid; q < dq; q += (WARPS * 32)) a.ws_part[pc * dq + q] = red[q];
     if (tid == 0) {
-      a.ws_sums[pc * 4 + 0] = sums[kWarps * 4 + 0];
-      a.ws_sums[pc * 4 + 1] = sums[kWarps * 4 + 1];
-      a.ws_sums[pc * 4 + 2] = sums[kWarps * 4 + 2];
+      a.ws_sums[pc * 4 + 0] = sums[WARPS * 4 + 0];
+      a.ws_sums[pc * 4 + 1] = sums[WARPS * 4 + 1];
+      a.ws_sums[pc * 4 + 2] = sums[WARPS * 4 + 2];
     }
     __threadfence();
     __syncthreads();
@@ -430,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
     if (!*is_last) return;
     __threadfence();
     const float4* part = a.ws_part + static_cast<int64_t>(c) * a.slices * dq;
-    for (int q = tid; q < dq; q += kThreads) {
+    for (int q = tid; q < dq; q += (WARPS * 32)) {
       float4 t = __ldcg(part + q);
       for (int k = 1; k < a.slices; ++k) {
         const float4 u = __ldcg(part + static_cast<int64_t>(k) * dq + q);
@@ -449,23 +450,23 @@ __global__ void __launch_bounds__(kThreads, MINB)
         t1 += __ldcg(ps + k * 4 + 1);
         t2 += __ldcg(ps + k * 4 + 2);
       }
-      sums[kWarps * 4 + 0] = t0;
-      sums[kWarps * 4 + 1] = t1;
-      sums[kWarps * 4 + 2] = t2;
+      sums[WARPS * 4 + 0] = t0;
+      sums[WARPS * 4 + 1] = t1;
+      sums[WARPS * 4 + 2] = t2;
     }
     __syncthreads();
   }
 
   // ------------------------------ epilogue ---------------------------------
-  const double sum_mlk = sums[kWarps * 4 + 0];
-  const double sum_lk = sums[kWarps * 4 + 1];
-  const double sum_lk2 = sums[kWarps * 4 + 2];
+  const double sum_mlk = sums[WARPS * 4 + 0];
+  const double sum_lk = sums[WARPS * 4 + 1];
+  const double sum_lk2 = sums[WARPS * 4 + 2];
   float* wc = a.w + static_cast<int64_t>(c) * a.d;
   const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n);
 
   double ww = 0.0;
   if (a.inv_p2 > 0.0f) {
-    for (int j = tid; j < a.d; j += kThreads) {
+    for (int j = tid; j < a.d; j += (WARPS * 32)) {
       const double wj = wc[j];
       ww += wj * wj;
     }
@@ -487,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
   if (a.mode == kValueGrad) {
     if (a.grad != nullptr) {
       float* gc = a.grad + static_cast<int64_t>(c) * a.d;
-      for (int j = tid; j < a.d; j += kThreads)
+      for (int j = tid; j < a.d; j += (WARPS * 32))
         gc[j] = (-scale * gl[j] + wc[j] * a.inv_p2) * a.inv_temp;
     }
     if (tid == 0) {
@@ -507,7 +508,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
   float* smp = slot >= 0 ? a.samples + (static_cast<int64_t>(slot) * a.chains + c) * a.d
                          : nullptr;
   bool bad = false;
-  for (int q = tid; q < dq; q += kThreads) {
+  for (int q = tid; q < dq; q += (WARPS * 32)) {
     float xi[4];
     noise4(a.noise, c, 4 * q, a.d, k, GBSGMC_TAG_SGLD, xi);
 #pragma unroll
@@ -632,19 +633,13 @@ int choose_slices(int chains, int n, int row_bytes) {
 
 constexpr int kMaxDynSmem = 227 * 1024;
 
-// Register double-buffering of row tiles (GBSGMC_GLM_PREFETCH=1 enables).
-bool prefetch_tiles() {
-  const char* v = std::getenv("GBSGMC_GLM_PREFETCH");
-  return v != nullptr && v[0] == '1';
-}
-
-template <int QPL, int RW, bool PF, int MINB>
+template <int QPL, int RW, bool PF, int MINB, int WARPS>
 struct Variant {
   static int prepare() {
     static int done = 0;
     if (done) return GBSGMC_OK;
     const cudaError_t e = cudaFuncSetAttribute(
-        glm_kernel<QPL, RW, PF, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        glm_kernel<QPL, RW, PF, MINB, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
         kMaxDynSmem);
     if (e != cudaSuccess)
       return set_error(GBSGMC_ERR_CUDA, "glm: cudaFuncSetAttribute: %s",
@@ -659,7 +654,7 @@ struct Variant {
     if (last > 0 && last_smem == smem) return last;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, glm_kernel<QPL, RW, PF, MINB>, kThreads, smem) != cudaSuccess ||
+            &nb, glm_kernel<QPL, RW, PF, MINB, WARPS>, WARPS * 32, smem) != cudaSuccess ||
         nb < 1)
       nb = 1;
     last_smem = smem;
@@ -685,33 +680,39 @@ struct Variant {
       a.ws_ticket = v.ticket;
     }
     dim3 grid(a.slices, a.chains);
-    glm_kernel<QPL, RW, PF, MINB><<<grid, kThreads, smem, st>>>(a);
+    glm_kernel<QPL, RW, PF, MINB, WARPS><<<grid, WARPS * 32, smem, st>>>(a);
     return check_launch("glm_kernel");
   }
 };
 
-// Tile shape for the d <= 256 kernels: GBSGMC_GLM_RW = 1, 2 or 4 rows per
-// warp (default 2); GBSGMC_GLM_PREFETCH=1 double-buffers row tiles.
+// Launch-shape overrides for experiments: GBSGMC_GLM_RW (2 or 4 rows per
+// warp, d <= 256), GBSGMC_GLM_WARPS (8 or 16 warps per CTA),
+// GBSGMC_GLM_SLICES (CTAs per chain).
 int rows_override() { return env_int("GBSGMC_GLM_RW", 0); }
+int warps_override() { return env_int("GBSGMC_GLM_WARPS", 0); }
 
+// Dispatch over the tuned shape: rows per warp (RW) and warps per CTA.  The
+// register budget (MINB) is 3 CTAs/SM for 8-warp CTAs with RW = 4, otherwise
+// what fits without spilling.
 template <int QPL>
 int launch_q(const GlmArgs& a, size_t smem, cudaStream_t st) {
-  const bool pf = prefetch_tiles();
+  const int warps = a.warps_fixed > 0 ? a.warps_fixed
+                    : (warps_override() > 0 ? warps_override() : 8);
+  const bool big = warps >= 16;
   if constexpr (QPL <= 2) {
     const int rw = a.rw_fixed > 0 ? a.rw_fixed
                    : (rows_override() > 0 ? rows_override()
                                           : default_rows_per_warp(QPL));
-    if (rw == 1) return pf ? Variant<QPL, 1, true, 4>::launch(a, smem, st)
-                           : Variant<QPL, 1, false, 6>::launch(a, smem, st);
-    if (rw == 4) return pf ? Variant<QPL, 4, true, 2>::launch(a, smem, st)
-                           : Variant<QPL, 4, false, 3>::launch(a, smem, st);
-    return pf ? Variant<QPL, 2, true, 3>::launch(a, smem, st)
-              : Variant<QPL, 2, false, 4>::launch(a, smem, st);
+    if (rw == 4) return big ? Variant<QPL, 4, false, 1, 16>::launch(a, smem, st)
+                            : Variant<QPL, 4, false, 3, 8>::launch(a, smem, st);
+    return big ? Variant<QPL, 2, false, 2, 16>::launch(a, smem, st)
+               : Variant<QPL, 2, false, 4, 8>::launch(a, smem, st);
   } else if constexpr (QPL == 4) {
-    return pf ? Variant<4, 2, true, 2>::launch(a, smem, st)
-              : Variant<4, 2, false, 2>::launch(a, smem, st);
+    return big ? Variant<4, 2, false, 1, 16>::launch(a, smem, st)
+               : Variant<4, 2, false, 2, 8>::launch(a, smem, st);
   } else {
-    return Variant<8, 1, false, 2>::launch(a, smem, st);
+    return big ? Variant<8, 1, false, 1, 16>::launch(a, smem, st)
+               : Variant<8, 1, false, 2, 8>::launch(a, smem, st);
   }
 }
 
@@ -719,7 +720,7 @@ int launch_glm(GlmArgs& a, cudaStream_t st) {
   if (a.chains == 0 || a.n == 0) return GBSGMC_OK;
   const int qpl = qpl_for(a.dq);
   // Shared memory sized for the largest slice any choice can give.
-  const SmemLayout L = smem_layout(std::min(a.n, kMaxRowsPerSlice), a.dq);
+  const SmemLayout L = smem_layout(std::min(a.n, kMaxRowsPerSlice), a.dq, kMaxWarps);
   if (L.total > 227 * 1024)
     return set_error(GBSGMC_ERR_SHAPE, "glm: shared memory %zu too large",
                      L.total);
@@ -777,10 +778,11 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.n = n;
   a.slices = 0;
   a.rows_per_slice = 0;
-  if (tune.slices == 0 && tune.rows_per_warp == 0)
+  if (tune.slices == 0 && tune.rows_per_warp == 0 && tune.warps == 0)
     glm_tune_lookup(chains, n, m->d, m->ld, &tune);
   a.slices_fixed = tune.slices;
   a.rw_fixed = tune.rows_per_warp;
+  a.warps_fixed = tune.warps;
   a.ws_base = ws;
   a.ws_size = ws_size;
   a.ws_part = nullptr;
@@ -835,15 +837,22 @@ void glm_tune_store(int chains, int n, int d, int64_t ld, GlmTune t) {
 size_t glm_ws_bytes(int chains, int n, int d) { return ws_bytes(chains, n, d); }
 
 int glm_prepare() {
-  // Sets the shared-memory attribute of the default variants before any
-  // stream capture; others are prepared on their first launch.
-  int rc = Variant<1, 2, false, 4>::prepare();
-  if (rc == GBSGMC_OK) rc = Variant<2, 2, false, 4>::prepare();
-  if (rc == GBSGMC_OK) rc = Variant<4, 2, false, 2>::prepare();
-  if (rc == GBSGMC_OK) rc = Variant<8, 1, false, 2>::prepare();
+  // Sets the shared-memory attribute of every variant before any stream
+  // capture.
+  int rc = Variant<1, 4, false, 3, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<1, 4, false, 1, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<1, 2, false, 4, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<1, 2, false, 2, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 4, false, 3, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 4, false, 1, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 2, false, 4, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 2, false, 2, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<4, 2, false, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<4, 2, false, 1, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<8, 1, false, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<8, 1, false, 1, 16>::prepare();
   return rc;
 }
-
 
 int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   const int32_t* idx_dev, int64_t idx_stride, float* w_dev,

@@ -9,6 +9,7 @@
 // steps costs K/G graph launches on the host.  The schedule tables (step
 // size, temperature, keep slots) are read on the device at step k.
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <map>
 #include <mutex>
@@ -104,14 +105,17 @@ int autotune(gbsgmc_plan* p) {
   {
     const double rows_per_cta = (384.0 * 1024.0) / (4.0 * std::max<int64_t>(p->model.ld, 1));
     const int base = std::max(1, static_cast<int>(std::ceil(n / rows_per_cta)));
-    const int ss[] = {base / 2, base - 1, base, base + 1, base + 2, 2 * base, 4 * base};
+    const int ss[] = {1, base / 2, base, base + 1, 2 * base};
     const int rws[] = {2, 4};
+    const int wps[] = {8, 16};
     for (int s : ss) {
       if (s < 1 || s > 64 || (s > 1 && n / s < 32)) continue;
-      if (d <= 256) {
-        for (int r : rws) cands.push_back(GlmTune{s, r});
-      } else {
-        cands.push_back(GlmTune{s, 0});
+      for (int w : wps) {
+        if (d <= 256) {
+          for (int r : rws) cands.push_back(GlmTune{s, r, w});
+        } else {
+          cands.push_back(GlmTune{s, 0, w});
+        }
       }
     }
   }
@@ -147,6 +151,8 @@ int autotune(gbsgmc_plan* p) {
     sch.offset = 0;
     float best_ms = 1e30f;
     GlmTune best = cands[0];
+    const char* vb = std::getenv("GBSGMC_AUTOTUNE_VERBOSE");
+    const bool verbose = vb != nullptr && vb[0] == '1';
     for (const GlmTune& t : cands) {
       for (int rep = 0; rep < 2 + 6 && rc == GBSGMC_OK; ++rep) {
         if (rep == 2) cudaEventRecord(e0, p->stream);
@@ -161,6 +167,9 @@ int autotune(gbsgmc_plan* p) {
       if ((rc = cuda_err(cudaEventSynchronize(e1), "autotune: sync"))) break;
       float ms = 0.0f;
       cudaEventElapsedTime(&ms, e0, e1);
+      if (verbose)
+        std::fprintf(stderr, "gbsgmc autotune: slices %d rows/warp %d warps %d: %.4f ms\n",
+                     t.slices, t.rows_per_warp, t.warps, ms / 6.0f);
       if (ms < best_ms) {
         best_ms = ms;
         best = t;
@@ -319,11 +328,13 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
 }
 
 extern "C" int gbsgmc_plan_launch_shape(const gbsgmc_plan* p, int* slices,
-                                        int* rows_per_warp) {
-  if (p == nullptr || slices == nullptr || rows_per_warp == nullptr)
+                                        int* rows_per_warp, int* warps) {
+  if (p == nullptr || slices == nullptr || rows_per_warp == nullptr ||
+      warps == nullptr)
     return set_error(GBSGMC_ERR_ARG, "plan_launch_shape: null argument");
   *slices = p->tune.slices;
   *rows_per_warp = p->tune.rows_per_warp;
+  *warps = p->tune.warps;
   return GBSGMC_OK;
 }
 

@@ -1,0 +1,40 @@
+"""The tcgen05 BF16 GEMM (C = A B^T, fp32 accumulation) against torch.
+
+Inputs are BF16, so products are exact in fp32; the tolerance covers fp32
+summation order over K: |C - C_ref| <= 1e-3 * (|A| |B|^T) elementwise bound.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("batch,M,N,K", [(1, 128, 128, 64), (1, 128, 256, 64),
+                                         (2, 256, 256, 128), (3, 384, 512, 1024),
+                                         (1, 2048, 1024, 1024), (2, 128, 384, 320)])
+def test_gemm_matches_torch(lib, batch, M, N, K):
+  import torch
+  from gbsgmc import _lib
+  g = torch.Generator(device="cuda").manual_seed(M + N + K)
+  A = torch.randn((batch, M, K), generator=g, device="cuda").to(torch.bfloat16)
+  B = torch.randn((batch, N, K), generator=g, device="cuda").to(torch.bfloat16)
+  C = torch.full((batch, M, N), float("nan"), device="cuda")
+  status = torch.zeros(1, dtype=torch.int32, device="cuda")
+  _lib.call("gbsgmc_gemm_bf16_nt", A.data_ptr(), K, M * K, B.data_ptr(), K, N * K,
+            C.data_ptr(), N, M * N, batch, M, N, K, status.data_ptr(),
+            _lib.stream_handle())
+  torch.cuda.synchronize()
+  assert int(status.item()) == 0
+  ref = torch.bmm(A.float(), B.float().transpose(1, 2))
+  bound = torch.bmm(A.float().abs(), B.float().abs().transpose(1, 2))
+  err = (C - ref).abs()
+  assert torch.isfinite(C).all()
+  assert bool((err <= 1e-3 * bound + 1e-4).all()), float((err / (bound + 1e-6)).max())
+
+
+def test_gemm_rejects_unsupported_shapes(lib):
+  from gbsgmc import _lib
+  rc = lib.gbsgmc_gemm_bf16_nt(16, 64, 0, 16, 64, 0, 16, 100, 0, 1, 100, 128, 64,
+                               None, None)
+  assert rc == _lib.ERR_SHAPE
