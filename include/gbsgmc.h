@@ -272,6 +272,47 @@ int gbsgmc_gemm_bf16_nt(const void* A_dev, int64_t lda, int64_t a_batch_stride,
                         gbsgmc_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Dense tanh network (MLP) with a Gaussian likelihood                       */
+/* ------------------------------------------------------------------------ */
+
+/* out(x) = W3^T tanh(W2^T tanh(W1^T x + b1) + b2) + b3 with
+ * lk = log N(y | out(x), sigma^2).  The flat parameter vector of a chain is
+ * the ravel of the pytree {W1 [d_in,h1], W2 [h1,h2], W3 [h2,1], b1 [h1],
+ * b2 [h2], b3 [1]} in sorted key order:
+ *   W1 | W2 | W3 | b1 | b2 | b3,  P = d_in h1 + h1 h2 + h2 + h1 + h2 + 1.
+ * GEMMs run in BF16 with FP32 accumulation on the tensor cores; tanh uses the
+ * hardware approximation.  Needs d_in % 64 == 0, h1 % 256 == 0,
+ * h2 % 256 == 0, n % 128 == 0. */
+typedef struct gbsgmc_mlp {
+  int d_in, h1, h2;
+  int y_inline;        /* 1: target of row i at X[i*ld + d_in]; 0: y[i]     */
+  int64_t n_obs;       /* N of the N/n scale                                */
+  int64_t n_rows;      /* rows of X (index bound); 0 means n_obs           */
+  int64_t ld;          /* row stride of X in floats                         */
+  const float* X;
+  const float* y;
+  float sigma, prior_scale, temperature;
+  int _reserved;
+} gbsgmc_mlp;
+
+int64_t gbsgmc_mlp_param_count(const gbsgmc_mlp* model);
+size_t gbsgmc_mlp_workspace_bytes(const gbsgmc_mlp* model, int chains, int n);
+
+/* As gbsgmc_glm_value_and_grad for the dense network: U[c], grad[c] = dU/dw_c
+ * (grad may be NULL: value only), lk[c, i] and lk_var[c] for `chains` chains
+ * whose flat parameters are the rows of w [chains, P].  The workspace needs
+ * no initialisation.  Replaces minibatch_potential (jax_sgmc/potential.py:
+ * 159-214) under jax.value_and_grad (jax_sgmc/integrator.py:166,593,792) for
+ * a dense-network likelihood. */
+int gbsgmc_mlp_value_and_grad(const gbsgmc_mlp* model, int chains, int n,
+                              const int32_t* idx_dev, int64_t idx_stride,
+                              const float* mask_dev, const float* w_dev,
+                              double* U_dev, float* grad_dev, float* lk_dev,
+                              double* lk_var_dev, void* workspace_dev,
+                              size_t workspace_bytes, int* status_dev,
+                              gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* Fused SGLD step for the generalised-linear families                       */
 /* ------------------------------------------------------------------------ */
 

@@ -56,6 +56,15 @@ class Glm(C.Structure):
               ("n_rows", C.c_int64)]
 
 
+class Mlp(C.Structure):
+  _fields_ = [("d_in", C.c_int), ("h1", C.c_int), ("h2", C.c_int),
+              ("y_inline", C.c_int), ("n_obs", C.c_int64),
+              ("n_rows", C.c_int64), ("ld", C.c_int64), ("X", C.c_void_p),
+              ("y", C.c_void_p), ("sigma", C.c_float),
+              ("prior_scale", C.c_float), ("temperature", C.c_float),
+              ("_reserved", C.c_int)]
+
+
 class Sched(C.Structure):
   _fields_ = [("step_size_dev", C.c_void_p), ("temperature_dev", C.c_void_p),
               ("base_dev", C.c_void_p), ("keep_slot_dev", C.c_void_p),
@@ -91,6 +100,11 @@ SIGNATURES = {
                                   _i64, _vp]),
     "gbsgmc_glm_workspace_bytes": (_sz, [_i, _i, _i]),
     "gbsgmc_glm_value_and_grad": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp,
+                                       _vp, _vp, _vp, _vp, _vp, _sz, _vp,
+                                       _vp]),
+    "gbsgmc_mlp_param_count": (_i64, [_P(Mlp)]),
+    "gbsgmc_mlp_workspace_bytes": (_sz, [_P(Mlp), _i, _i]),
+    "gbsgmc_mlp_value_and_grad": (_i, [_P(Mlp), _i, _i, _vp, _i64, _vp, _vp,
                                        _vp, _vp, _vp, _vp, _vp, _sz, _vp,
                                        _vp]),
     "gbsgmc_sgld_update": (_i, [_i, _i64, _vp, _vp, _vp, _f, _f, _P(Sched),

@@ -15,6 +15,12 @@ Families (per observation i, z_i = x_i . w):
 * :class:`Linear` -- ``lk_i = z_i`` (the linear likelihood
   ``jnp.sum(sample * reference_data)`` of tests/test_potential.py:26-31).
 
+Dense network (per observation, the parameters a pytree of matrices):
+
+* :class:`MLPGaussian` -- ``out = tanh(tanh(x W1 + b1) W2 + b2) W3 + b3``,
+  ``lk = log N(y | out, sigma^2)``; BF16 tensor-core GEMMs with fp32
+  accumulation.
+
 Priors: :class:`GaussianPrior` (``sum norm.logpdf(w, 0, scale)``, constants
 included) and :class:`FlatPrior` (``log p = 0``).
 """
@@ -94,9 +100,75 @@ class Linear(GLMLikelihood):
       raise KeyError(f"reference data has no field {self.x!r}")
 
 
+@dataclass(frozen=True)
+class MLPGaussian:
+  """Two-hidden-layer tanh network with a Gaussian likelihood.
+
+  The sample is the pytree ``{"W1": [d_in, h1], "W2": [h1, h2], "W3": [h2, 1],
+  "b1": [h1], "b2": [h2], "b3": [1]}`` (or its ravel in that sorted key
+  order, as jax.flatten_util.ravel_pytree produces it).  The kernels need
+  d_in % 64 == 0, h1 % 256 == 0, h2 % 256 == 0 and minibatches of a multiple
+  of 128 observations.
+  """
+  d_in: int = 64
+  h1: int = 1024
+  h2: int = 1024
+  sigma: float = 0.1
+  x: str = "x"
+  y: str = "y"
+
+  def __post_init__(self):
+    if not self.sigma > 0:
+      raise ValueError(f"sigma must be positive, got {self.sigma}")
+    if self.d_in % 64 or self.h1 % 256 or self.h2 % 256:
+      raise ValueError("MLPGaussian needs d_in % 64 == 0, h1 % 256 == 0 and "
+                       f"h2 % 256 == 0 (got {self.d_in}, {self.h1}, {self.h2})")
+
+  def shapes(self):
+    return {"W1": (self.d_in, self.h1), "W2": (self.h1, self.h2),
+            "W3": (self.h2, 1), "b1": (self.h1,), "b2": (self.h2,),
+            "b3": (1,)}
+
+  @property
+  def param_count(self) -> int:
+    return sum(math.prod(v) for v in self.shapes().values())
+
+  def init(self, rng, scale: float = 1.0):
+    """Random parameters (N(0, scale^2 / fan_in) weights, zero biases) as the
+    flat float32 vector."""
+    import numpy as np
+    parts = []
+    for name, shp in self.shapes().items():
+      if name.startswith("W"):
+        parts.append(rng.normal(0.0, scale / math.sqrt(shp[0]), size=shp))
+      else:
+        parts.append(np.zeros(shp))
+    return np.concatenate([p.reshape(-1) for p in parts]).astype(np.float32)
+
+  def unravel(self, flat):
+    """Flat vector -> dict of leaves (views for numpy and torch inputs)."""
+    out, o = {}, 0
+    for name, shp in self.shapes().items():
+      k = math.prod(shp)
+      out[name] = flat[..., o:o + k].reshape(tuple(flat.shape[:-1]) + shp)
+      o += k
+    return out
+
+  def check_data(self, data: dict) -> None:
+    for k in (self.x, self.y):
+      if k not in data:
+        raise KeyError(f"reference data has no field {k!r} "
+                       f"(fields: {sorted(data)})")
+
+
 def is_prior(p) -> bool:
   return isinstance(p, (GaussianPrior, FlatPrior))
 
 
 def is_likelihood(l) -> bool:
-  return isinstance(l, GLMLikelihood) and l.family >= 0
+  return (isinstance(l, GLMLikelihood) and l.family >= 0) or \
+      isinstance(l, MLPGaussian)
+
+
+def is_mlp(l) -> bool:
+  return isinstance(l, MLPGaussian)

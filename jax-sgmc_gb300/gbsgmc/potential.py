@@ -60,8 +60,8 @@ class StochasticPotential:
                       "no kernel")
     if not lkmod.is_likelihood(likelihood):
       raise TypeError("likelihood must be a gbsgmc.likelihoods family "
-                      "(LinearGaussian, Logistic): arbitrary callables have "
-                      "no kernel")
+                      "(LinearGaussian, Logistic, Linear, MLPGaussian): "
+                      "arbitrary callables have no kernel")
     if not temperature > 0:
       raise ValueError("temperature must be positive")
     self.prior = prior
@@ -74,11 +74,25 @@ class StochasticPotential:
     self._status = None
 
   # -- model description ---------------------------------------------------
+  @property
+  def is_mlp(self) -> bool:
+    return lkmod.is_mlp(self.likelihood)
+
   def model(self, dataset, observation_count=None):
-    """``gbsgmc_glm`` for a device dataset (targets stored inline in the
-    feature rows, see DeviceDataset.glm_view)."""
+    """``gbsgmc_glm`` (or ``gbsgmc_mlp``) for a device dataset, targets
+    stored inline in the feature rows (DeviceDataset.glm_view)."""
     n_obs = dataset.observation_count if observation_count is None \
         else observation_count
+    if self.is_mlp:
+      lik = self.likelihood
+      X, d, ld = dataset.glm_view(lik.x, lik.y)
+      if d != lik.d_in:
+        raise ValueError(f"field {lik.x!r} has {d} features, the network "
+                         f"takes {lik.d_in}")
+      return _lib.Mlp(lik.d_in, lik.h1, lik.h2, 1, int(n_obs),
+                      int(dataset.observation_count), ld, X.data_ptr(), None,
+                      float(lik.sigma), float(self.prior.scale),
+                      float(self.temperature), 0), (X,)
     if self.likelihood.y is None:
       X, d, ld = dataset.matrix(self.likelihood.x)
       inline = 0
@@ -91,6 +105,8 @@ class StochasticPotential:
                     int(dataset.observation_count)), (X,)
 
   def dim(self, dataset) -> int:
+    if self.is_mlp:
+      return self.likelihood.param_count
     return dataset.feature_dim(self.likelihood.x)
 
   def status(self):
@@ -107,12 +123,19 @@ class StochasticPotential:
         self._status.zero_()
         raise _lib.GbsgmcError(code, "device status")
 
-  def workspace(self, chains, n, d):
+  def workspace(self, chains, n, d, model=None):
     import torch
     key = (chains, n, d)
     ws = self._ws.get(key)
     if ws is None:
-      nbytes = int(_lib.load().gbsgmc_glm_workspace_bytes(chains, n, d))
+      if self.is_mlp:
+        nbytes = int(_lib.load().gbsgmc_mlp_workspace_bytes(model, chains, n))
+        if nbytes == 0:
+          raise _lib.GbsgmcError(_lib.ERR_SHAPE,
+                                 f"MLP minibatch of {n} rows: needs a "
+                                 "positive multiple of 128")
+      else:
+        nbytes = int(_lib.load().gbsgmc_glm_workspace_bytes(chains, n, d))
       ws = torch.zeros(max(nbytes, 16), dtype=torch.uint8, device="cuda")
       self._ws[key] = ws
     return ws
@@ -128,18 +151,24 @@ class StochasticPotential:
       m, keep = self.model(dataset, observation_count)
     else:
       m, keep = model
-    if m.d != d:
+    if self.is_mlp:
+      if d != self.likelihood.param_count:
+        raise ValueError(f"parameters per chain {d} != network parameters "
+                         f"{self.likelihood.param_count}")
+    elif m.d != d:
       raise ValueError(f"parameters per chain {d} != features {m.d}")
     U = torch.empty(C, dtype=torch.float64, device="cuda")
     var = torch.empty(C, dtype=torch.float64, device="cuda")
     g = torch.empty((C, d), dtype=torch.float32, device="cuda") if grad else None
     lko = torch.empty((C, n), dtype=torch.float32, device="cuda") if lk else None
-    ws = self.workspace(C, n, d)
+    ws = self.workspace(C, n, d, m)
     W = W.to(torch.float32).contiguous()
     idx = idx.to(torch.int32).contiguous()
     if mask is not None:
       mask = mask.to(device="cuda", dtype=torch.float32).reshape(C, n).contiguous()
-    _lib.call("gbsgmc_glm_value_and_grad", m, C, n, _lib.ptr(idx),
+    fn = "gbsgmc_mlp_value_and_grad" if self.is_mlp else \
+        "gbsgmc_glm_value_and_grad"
+    _lib.call(fn, m, C, n, _lib.ptr(idx),
               idx.stride(0) if idx.dim() == 2 else n, _lib.ptr(mask),
               _lib.ptr(W), _lib.ptr(U), _lib.ptr(g),
               _lib.ptr(lko), _lib.ptr(var), _lib.ptr(ws), ws.numel(),
@@ -248,11 +277,22 @@ class FullPotential:
     g = torch.zeros((C, d), dtype=torch.float32, device="cuda")
     for start in range(0, N, self.CHUNK):
       n = min(self.CHUNK, N - start)
-      idx = torch.arange(start, start + n, dtype=torch.int32,
-                         device="cuda").expand(C, n)
+      idx = torch.arange(start, start + n, dtype=torch.int32, device="cuda")
+      mask = None
+      if self._unit.is_mlp and n % 128:
+        # The network kernels take whole 128-row tiles: pad with row 0 at
+        # mask weight 0.
+        pad = 128 - n % 128
+        idx = torch.cat([idx, torch.zeros(pad, dtype=torch.int32,
+                                          device="cuda")])
+        mask = torch.cat([torch.ones(n, device="cuda"),
+                          torch.zeros(pad, device="cuda")]).expand(C, -1)
+        n += pad
+      idx = idx.expand(C, n)
       pot = self._unit if start == 0 else self._flat
       # n_obs = n makes the N/n scale 1: the chunk contributes -sum lk.
-      r = pot.evaluate(W, idx, dataset, grad=True, observation_count=n)
+      r = pot.evaluate(W, idx, dataset, mask=mask, grad=True,
+                       observation_count=n)
       U += r.U
       g += r.grad
     return U / self.temperature, g / self.temperature

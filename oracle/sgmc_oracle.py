@@ -223,6 +223,78 @@ def full_potential(w, X, y, family, sigma=1.0, prior_scale=0.0,
   return U, g
 
 
+# ---------------------------------------------------------------------------
+# Dense tanh network with a Gaussian likelihood
+# ---------------------------------------------------------------------------
+# The reference leaves the likelihood to user code (minibatch_potential's
+# ``likelihood`` argument, jax_sgmc/potential.py:94-99) and differentiates the
+# potential with jax.value_and_grad (integrator.py:166,593,792).  The network
+# below is the one of the MLP regression workload: parameters are the pytree
+# {W1 [D,H1], W2 [H1,H2], W3 [H2,1], b1 [H1], b2 [H2], b3 [1]}, raveled in
+# sorted key order as jax.flatten_util.ravel_pytree does.  The adjoint is the
+# chain rule written out; tests pin it to torch autograd and to central
+# finite differences.
+
+
+def mlp_offsets(d_in, h1, h2):
+  """Offsets of W1, W2, W3, b1, b2, b3 in the flat vector, and P."""
+  sizes = [d_in * h1, h1 * h2, h2, h1, h2, 1]
+  off = np.concatenate([[0], np.cumsum(sizes)])
+  return [int(v) for v in off[:-1]], int(off[-1])
+
+
+def mlp_unravel(w, d_in, h1, h2):
+  """Leaves of the flat vector (numpy arrays, or views of a torch tensor)."""
+  if not hasattr(w, "reshape"):
+    w = np.asarray(w)
+  (o1, o2, o3, ob1, ob2, ob3), _ = mlp_offsets(d_in, h1, h2)
+  return (w[..., o1:o2].reshape(w.shape[:-1] + (d_in, h1)),
+          w[..., o2:o3].reshape(w.shape[:-1] + (h1, h2)),
+          w[..., o3:ob1], w[..., ob1:ob2], w[..., ob2:ob3], w[..., ob3])
+
+
+def mlp_forward(W, Xb, d_in, h1, h2):
+  """out [C, n] and the hidden activations Z1, Z2 for rows Xb [C, n, D]."""
+  W1, W2, W3, b1, b2, b3 = mlp_unravel(W, d_in, h1, h2)
+  Z1 = np.tanh(Xb @ W1 + b1[:, None, :])
+  Z2 = np.tanh(Z1 @ W2 + b2[:, None, :])
+  out = (Z2 @ W3[..., None])[..., 0] + b3[:, None]
+  return out, Z1, Z2
+
+
+def mlp_potential(W, X, y, idx, n_obs, d_in, h1, h2, sigma, prior_scale=0.0,
+                  temperature=1.0, mask=None) -> Potential:
+  """Minibatch potential of the tanh network for C chains, float64.
+
+  out = tanh(tanh(x W1 + b1) W2 + b2) W3 + b3, lk = log N(y | out, sigma^2),
+  U = (-N/n sum_i m_i lk_i - log p(w)) / T (potential.py:159-214), var =
+  jnp.var(lk) (integrator.py:880).  W [C, P], idx [C, n].
+  """
+  W = np.atleast_2d(np.asarray(W, np.float64))
+  idx = np.atleast_2d(np.asarray(idx))
+  C, P = W.shape
+  W1, W2, W3, b1, b2, b3 = mlp_unravel(W, d_in, h1, h2)
+  Xb = np.asarray(X, np.float64)[idx][..., :d_in]   # [C, n, D]
+  yb = np.asarray(y, np.float64)[idx]                # [C, n]
+  n = idx.shape[-1]
+  out, Z1, Z2 = mlp_forward(W, Xb, d_in, h1, h2)
+  r = yb - out
+  lk = -0.5 * (r / sigma) ** 2 - math.log(sigma) - 0.5 * math.log(2 * math.pi)
+  m = np.ones_like(lk) if mask is None else np.asarray(mask, np.float64).reshape(lk.shape)
+  lp, dlp = log_prior(W, prior_scale)
+  U = (-(n_obs / n) * np.sum(m * lk, -1) - lp) / temperature
+  g = -(n_obs / n) * m * r / sigma ** 2 / temperature          # dU/dout
+  G2 = g[..., None] * W3[:, None, :] * (1.0 - Z2 ** 2)
+  G1 = (G2 @ W2.transpose(0, 2, 1)) * (1.0 - Z1 ** 2)
+  grad = np.concatenate([
+      (Xb.transpose(0, 2, 1) @ G1).reshape(C, -1),
+      (Z1.transpose(0, 2, 1) @ G2).reshape(C, -1),
+      (g[:, None, :] @ Z2)[:, 0, :],
+      G1.sum(1), G2.sum(1), g.sum(1, keepdims=True)], axis=1)
+  grad = grad - dlp / temperature
+  return Potential(U, grad, lk, np.var(lk, axis=-1))
+
+
 def linear_posterior(X, y, sigma, prior_scale):
   """Closed-form posterior of Bayesian linear regression with known noise:
   Sigma = (X^T X / s^2 + I / p^2)^-1, mu = Sigma X^T y / s^2."""

@@ -43,6 +43,46 @@ def test_argument_validation_without_a_gpu():
   assert lib.gbsgmc_glm_workspace_bytes(256, 1024, 256) > 256 * 1024
 
 
+def test_mlp_abi_shapes_and_validation_without_a_gpu():
+  import ctypes as C
+  from gbsgmc import _lib, likelihoods as L
+  lib = _lib.load()
+  m = _lib.Mlp(64, 1024, 1024, 1, 500_000, 500_000, 72, 16, None, 0.1, 1.0,
+               1.0, 0)
+  assert lib.gbsgmc_mlp_param_count(C.byref(m)) == 1_117_185
+  assert L.MLPGaussian().param_count == 1_117_185
+  ws = lib.gbsgmc_mlp_workspace_bytes(C.byref(m), 64, 2048)
+  assert 64 * 24 * 2**20 < ws < 64 * 28 * 2**20
+  assert lib.gbsgmc_mlp_workspace_bytes(C.byref(m), 64, 2000) == 0
+  args = lambda n, mm=m: (C.byref(mm), 2, n, 16, n, None, 16, 16, None, None,
+                          None, 256, 1 << 40, 16, None)
+  assert lib.gbsgmc_mlp_value_and_grad(*args(200)) == _lib.ERR_SHAPE
+  bad = _lib.Mlp(64, 1000, 1024, 1, 10, 10, 72, 16, None, 0.1, 1.0, 1.0, 0)
+  assert lib.gbsgmc_mlp_value_and_grad(*args(256, bad)) == _lib.ERR_SHAPE
+  neg = _lib.Mlp(64, 1024, 1024, 1, 10, 10, 72, 16, None, -0.1, 1.0, 1.0, 0)
+  assert lib.gbsgmc_mlp_value_and_grad(*args(256, neg)) == _lib.ERR_ARG
+  short = _lib.Mlp(64, 1024, 1024, 1, 10, 10, 64, 16, None, 0.1, 1.0, 1.0, 0)
+  assert lib.gbsgmc_mlp_value_and_grad(*args(256, short)) == _lib.ERR_ARG
+  # Too small a workspace is caught before anything is launched.
+  small = (C.byref(m), 2, 256, 16, 256, None, 16, 16, None, None, None, 256,
+           1024, 16, None)
+  assert lib.gbsgmc_mlp_value_and_grad(*small) == _lib.ERR_ARG
+  assert b"workspace" in lib.gbsgmc_last_error()
+  with pytest.raises(ValueError):
+    L.MLPGaussian(d_in=60)
+
+
+def test_mlp_unravel_follows_sorted_keys():
+  from gbsgmc import likelihoods as L, util
+  lik = L.MLPGaussian(d_in=64, h1=256, h2=512)
+  flat = lik.init(np.random.default_rng(0))
+  tree = lik.unravel(flat)
+  assert list(tree) == sorted(tree)
+  again, _ = util.ravel(tree)
+  np.testing.assert_array_equal(again, flat)
+  assert tree["W3"].shape == (512, 1) and tree["b3"].shape == (1,)
+
+
 def test_ravel_matches_ravel_pytree_order():
   from gbsgmc import util
   tree = {"b": np.arange(6.0).reshape(2, 3), "a": np.float32(7.0),
