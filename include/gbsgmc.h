@@ -271,6 +271,17 @@ int gbsgmc_gemm_bf16_nt(const void* A_dev, int64_t lda, int64_t a_batch_stride,
                         int batch, int M, int N, int K, int* status_dev,
                         gbsgmc_stream_t stream);
 
+/* As gbsgmc_gemm_bf16_nt with a choice of operand layout: a_mn != 0 means A
+ * is stored transposed (K x M, row-major with M contiguous, lda >= M),
+ * b_mn != 0 that B is stored K x N (ldb >= N).  The transposed forms let the
+ * adjoint GEMMs of a network (X^T G, Z^T G) read activations where the
+ * forward pass wrote them. */
+int gbsgmc_gemm_bf16(int a_mn, int b_mn, const void* A_dev, int64_t lda,
+                     int64_t a_batch_stride, const void* B_dev, int64_t ldb,
+                     int64_t b_batch_stride, float* C_dev, int64_t ldc,
+                     int64_t c_batch_stride, int batch, int M, int N, int K,
+                     int* status_dev, gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Dense tanh network (MLP) with a Gaussian likelihood                       */
 /* ------------------------------------------------------------------------ */

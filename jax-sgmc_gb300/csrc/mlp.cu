@@ -14,21 +14,23 @@
 // hand.  Nothing of the forward pass is kept beyond the BF16 activations the
 // adjoint GEMMs consume.
 //
-// Launch sequence (each batched over chains; GEMMs are C = A B^T with both
-// operands K-major BF16, fp32 accumulation in TMEM):
-//   1 mlp_prep_kernel     W1 -> W1t [H1,D], W2 -> W2t [H2,H1] and W2b [H1,H2]
-//                         (BF16), partial sums of w^2 for the prior
-//   2 mlp_gather_kernel   X rows -> Xb [n,D], Xt [D,n] (BF16), targets
-//   3 GEMM Xb  . W1t^T    epilogue tanh(+b1) -> Z1 [n,H1], Z1t [H1,n]
-//   4 GEMM Z1  . W2t^T    epilogue tanh(+b2) -> Z2 [n,H2], partial Z2 . W3
-//   5 mlp_out_kernel      out, lk, g; G2 in place of Z2, G2t [H2,n], partial
-//                         column sums for dW3 and db2
-//   6 GEMM G2  . W2b^T    epilogue *(1 - Z1^2) -> G1t [H1,n], partial db1
-//   7 GEMM Z1t . G2t^T    epilogue + prior -> dW2
-//   8 GEMM G1t . Xt^T     epilogue + prior -> dW1 (written transposed)
-//   9 mlp_finalize_kernel db1, db2, dW3, db3, U and var(lk)
-// Without a gradient only 1-5 and 9 run, and the transposed copies are not
-// written.
+// Launch sequence (each batched over chains; GEMMs are C = A B^T on the
+// tcgen05 tensor cores, BF16 operands read K-major or MN-major straight from
+// where the previous step wrote them, fp32 accumulation in TMEM):
+//   1 mlp_prep_kernel     W1 | W2 -> BF16 copy Wb, partial sums of w^2
+//   2 mlp_gather_kernel   X rows -> Xb [n,D] (BF16), targets
+//   3 GEMM Xb . W1        epilogue tanh(+b1) -> Z1 [n,H1]
+//   4 GEMM Z1 . W2        epilogue tanh(+b2) -> Z2 [n,H2], partial Z2 . W3
+//   5 mlp_out_kernel      out, lk, g; G2 in place of Z2, partial column sums
+//                         for dW3 and db2
+//   6 GEMM Z1^T . G2      epilogue -> dW2
+//   7 GEMM G2 . W2^T      epilogue *(1 - Z1^2) -> G1 in place of Z1,
+//                         partial db1
+//   8 GEMM G1^T . Xb      epilogue -> dW1 (written transposed)
+//   8b mlp_prior_kernel   dW1, dW2 += w / (s^2 T)
+//   9 mlp_finalize_kernel db1, db2, dW3, db3 (with their prior terms), U and
+//                         var(lk)
+// Without a gradient only 1-5 and 9 run.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -43,8 +45,8 @@ namespace {
 using bf16 = __nv_bfloat16;
 
 constexpr int kTile = 64;      // rows / columns of a prep, gather or out tile
-constexpr int kOutCols = 256;  // columns of an out-kernel tile
 constexpr int kBN = 256;       // N tile of the H1- and H2-wide GEMMs
+constexpr int kSlot = kBN / kGemmSplit;  // columns of one epilogue warp
 
 __device__ __forceinline__ float tanh_approx(float x) {
   float y;
@@ -62,35 +64,6 @@ __device__ __forceinline__ void unpack_bf16x2(uint32_t u, float& lo, float& hi) 
   const float2 f = __bfloat1622float2(p);
   lo = f.x;
   hi = f.y;
-}
-
-// Stores 16 floats as BF16 at a 32-byte aligned address.
-__device__ __forceinline__ void store_bf16x16(bf16* dst, const float (&x)[16]) {
-  uint4 a, b;
-  a.x = pack_bf16x2(x[0], x[1]);
-  a.y = pack_bf16x2(x[2], x[3]);
-  a.z = pack_bf16x2(x[4], x[5]);
-  a.w = pack_bf16x2(x[6], x[7]);
-  b.x = pack_bf16x2(x[8], x[9]);
-  b.y = pack_bf16x2(x[10], x[11]);
-  b.z = pack_bf16x2(x[12], x[13]);
-  b.w = pack_bf16x2(x[14], x[15]);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-  d[0] = a;
-  d[1] = b;
-}
-
-__device__ __forceinline__ void load_bf16x16(const bf16* src, float (&x)[16]) {
-  const uint4* s = reinterpret_cast<const uint4*>(src);
-  const uint4 a = s[0], b = s[1];
-  unpack_bf16x2(a.x, x[0], x[1]);
-  unpack_bf16x2(a.y, x[2], x[3]);
-  unpack_bf16x2(a.z, x[4], x[5]);
-  unpack_bf16x2(a.w, x[6], x[7]);
-  unpack_bf16x2(b.x, x[8], x[9]);
-  unpack_bf16x2(b.y, x[10], x[11]);
-  unpack_bf16x2(b.z, x[12], x[13]);
-  unpack_bf16x2(b.w, x[14], x[15]);
 }
 
 // Sum over the 32 lanes of each of v[0..15]; lane l returns the total of
@@ -145,15 +118,20 @@ MlpShape mlp_shape(int D, int H1, int H2) {
   return s;
 }
 
+constexpr int kPrepPairs = 16;                   // weight pairs per prep thread
+constexpr int kPrepPerBlock = 2 * 256 * kPrepPairs;  // weights per prep block
+
+__host__ __device__ inline int64_t matrix_params(const MlpShape& s) { return s.oW3; }  // |W1| + |W2|
+
 int prep_blocks(const MlpShape& s) {
-  return (s.D / kTile) * (s.H1 / kTile) + (s.H1 / kTile) * (s.H2 / kTile) + 1;
+  return static_cast<int>((matrix_params(s) + kPrepPerBlock - 1) / kPrepPerBlock) + 1;
 }
 
 // Workspace regions, each [chains, per-chain size], 256-byte aligned.
 struct MlpLayout {
-  size_t w1t, w2t, w2b, xb, xt, z1, z1t, z2g, g2t, g1t;  // BF16
-  size_t yv, outp, pw3, pb2, pb1;                        // fp32
-  size_t psq, plk;                                       // fp64
+  size_t wb, xb, z1, z2g;           // BF16
+  size_t yv, outp, pw3, pb2, pb1;   // fp32
+  size_t psq, plk;                  // fp64
   size_t total;
 };
 
@@ -166,18 +144,12 @@ MlpLayout mlp_layout(const MlpShape& s, int chains, int n) {
     return at;
   };
   const size_t D = s.D, H1 = s.H1, H2 = s.H2, N = n;
-  L.w1t = take(2 * H1 * D);
-  L.w2t = take(2 * H2 * H1);
-  L.w2b = take(2 * H1 * H2);
+  L.wb = take(2 * static_cast<size_t>(matrix_params(s)));
   L.xb = take(2 * N * D);
-  L.xt = take(2 * D * N);
   L.z1 = take(2 * N * H1);
-  L.z1t = take(2 * H1 * N);
   L.z2g = take(2 * N * H2);
-  L.g2t = take(2 * H2 * N);
-  L.g1t = take(2 * H1 * N);
   L.yv = take(4 * N);
-  L.outp = take(4 * (H2 / kBN) * N);
+  L.outp = take(4 * (H2 / kSlot) * N);
   L.pw3 = take(4 * (N / kTile) * H2);
   L.pb2 = take(4 * (N / kTile) * H2);
   L.pb1 = take(4 * (N / 32) * H1);
@@ -203,57 +175,42 @@ struct MlpArgs {
   double* lk_var;
   int* status;
   // workspace views
-  bf16 *w1t, *w2t, *w2b, *xb, *xt, *z1, *z1t, *z2g, *g2t, *g1t;
+  bf16 *wb, *xb, *z1, *z2g;
   float *yv, *outp, *pw3, *pb2, *pb1;
   double *psq, *plk;
 };
 
 // ---------------------------------------------------------------------------
-// 1. Weights to BF16 (W1 transposed; W2 straight and transposed) and partial
-//    sums of squares of every parameter.  Grid (prep_blocks, chains).
+// 1. W1 | W2 to BF16 (same layout) and partial sums of squares of every
+//    parameter.  Grid (prep_blocks, chains); the last block of a chain sums
+//    the vector leaves W3 | b1 | b2 | b3.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) mlp_prep_kernel(const MlpArgs a) {
-  __shared__ float tile[kTile][kTile + 1];
   __shared__ double red[32];
   const MlpShape& s = a.s;
   const int c = blockIdx.y, blk = blockIdx.x, t = threadIdx.x;
   const float* w = a.w + static_cast<int64_t>(c) * s.P;
-  const int nt1 = (s.D / kTile) * (s.H1 / kTile);
-  const int nt2 = (s.H1 / kTile) * (s.H2 / kTile);
+  const int64_t pw = matrix_params(s);
   float sq = 0.f;
-  if (blk < nt1 + nt2) {
-    const bool first = blk < nt1;
-    const int tt = first ? blk : blk - nt1;
-    const int R = first ? s.D : s.H1, Cc = first ? s.H1 : s.H2;
-    const int ti = tt / (Cc / kTile), tj = tt % (Cc / kTile);
-    const float* src = w + (first ? s.oW1 : s.oW2);
-    const int col = t & 63;
-    bf16* straight = (!first && a.want_grad)
-                         ? a.w2b + static_cast<int64_t>(c) * s.H1 * s.H2
-                         : nullptr;
-#pragma unroll 4
-    for (int k = 0; k < 16; ++k) {
-      const int r = (t >> 6) + 4 * k;
-      const int64_t e = static_cast<int64_t>(ti * kTile + r) * Cc + tj * kTile + col;
-      const float v = __ldg(src + e);
-      sq = fmaf(v, v, sq);
-      tile[r][col] = v;
-      if (straight != nullptr) straight[e] = __float2bfloat16_rn(v);
-    }
-    __syncthreads();
-    bf16* dstT = first ? a.w1t + static_cast<int64_t>(c) * s.H1 * s.D
-                       : a.w2t + static_cast<int64_t>(c) * s.H2 * s.H1;
+  if (blk + 1 < static_cast<int>(gridDim.x)) {
+    uint32_t* dst = reinterpret_cast<uint32_t*>(a.wb + static_cast<int64_t>(c) * pw);
+    const int64_t e0 = static_cast<int64_t>(blk) * kPrepPerBlock + 2 * t;
+    float v0[kPrepPairs], v1[kPrepPairs];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int i = t + 256 * k;
-      const int cc = i >> 5, r2 = (i & 31) * 2;
-      const int64_t e = static_cast<int64_t>(tj * kTile + cc) * R + ti * kTile + r2;
-      *reinterpret_cast<uint32_t*>(dstT + e) = pack_bf16x2(tile[r2][cc], tile[r2 + 1][cc]);
+    for (int k = 0; k < kPrepPairs; ++k) {  // pw is even: pairs never straddle the end
+      const int64_t e = e0 + 512 * k;
+      v0[k] = e < pw ? __ldg(w + e) : 0.f;
+      v1[k] = e < pw ? __ldg(w + e + 1) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kPrepPairs; ++k) {
+      const int64_t e = e0 + 512 * k;
+      sq = fmaf(v0[k], v0[k], fmaf(v1[k], v1[k], sq));
+      if (e < pw) dst[e >> 1] = pack_bf16x2(v0[k], v1[k]);
     }
   } else {
-    const int64_t tail = s.P - s.oW3;
-    for (int64_t i = t; i < tail; i += 256) {
-      const float v = __ldg(w + s.oW3 + i);
+    for (int64_t i = pw + t; i < s.P; i += 256) {
+      const float v = __ldg(w + i);
       sq = fmaf(v, v, sq);
     }
   }
@@ -262,11 +219,10 @@ __global__ void __launch_bounds__(256) mlp_prep_kernel(const MlpArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// 2. Minibatch rows to BF16, row-major and transposed, plus targets.
+// 2. Minibatch rows to BF16 plus targets.
 //    Grid (n/64, D/64, chains).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) mlp_gather_kernel(const MlpArgs a) {
-  __shared__ float tile[kTile][kTile + 1];
   __shared__ int64_t rows[kTile];
   const MlpShape& s = a.s;
   const int i0 = blockIdx.x * kTile, f0 = blockIdx.y * kTile, c = blockIdx.z;
@@ -290,21 +246,9 @@ __global__ void __launch_bounds__(256) mlp_gather_kernel(const MlpArgs a) {
     const int r = warp * 8 + j;
     const float* src = a.X + rows[r] * a.ld + f0;
     const float v0 = __ldg(src + lane), v1 = __ldg(src + 32 + lane);
-    tile[r][lane] = v0;
-    tile[r][lane + 32] = v1;
     bf16* d = xb + static_cast<int64_t>(i0 + r) * s.D + f0;
     d[lane] = __float2bfloat16_rn(v0);
     d[lane + 32] = __float2bfloat16_rn(v1);
-  }
-  if (!a.want_grad) return;
-  __syncthreads();
-  bf16* xt = a.xt + static_cast<int64_t>(c) * s.D * a.n;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int i = t + 256 * k;
-    const int f = i >> 5, r2 = (i & 31) * 2;
-    *reinterpret_cast<uint32_t*>(xt + static_cast<int64_t>(f0 + f) * a.n + i0 + r2) =
-        pack_bf16x2(tile[r2][f], tile[r2 + 1][f]);
   }
 }
 
@@ -312,202 +256,310 @@ __global__ void __launch_bounds__(256) mlp_gather_kernel(const MlpArgs a) {
 // GEMM epilogues.
 // ---------------------------------------------------------------------------
 
-// 3: Z1 = tanh(acc + b1) -> Z1 [n, H1] and (with a gradient) Z1t [H1, n].
+// Bias + tanh over one 64-column block of the lane's row, packed to BF16
+// pairs: pk[j] holds columns 2j, 2j + 1 of the block.  With w3 the fp32 dot
+// product of the block with w3 is added to `dot`.
+template <class Load>
+__device__ __forceinline__ void tanh_block(const Load& load, int blk, const float* bias,
+                                           uint32_t (&pk)[32], const float* w3, float& dot) {
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    float v[32];
+    load(2 * blk + half, v);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int k = 64 * blk + 32 * half + 2 * j;
+      const float z0 = tanh_approx(v[2 * j] + __ldg(bias + k));
+      const float z1 = tanh_approx(v[2 * j + 1] + __ldg(bias + k + 1));
+      if (w3 != nullptr) dot = fmaf(z0, __ldg(w3 + k), fmaf(z1, __ldg(w3 + k + 1), dot));
+      pk[16 * half + j] = pack_bf16x2(z0, z1);
+    }
+  }
+}
+
+// Writes the packed 64-column block of the warp's 32 rows, one 128-byte row
+// segment per store.
+__device__ __forceinline__ void store_block(uint32_t* dst, int64_t ld_words, int blk,
+                                            const uint32_t (&pk)[32], uint32_t* st) {
+  epi::put_rows(st, pk);
+#pragma unroll 4
+  for (int r = 0; r < 32; ++r) dst[r * ld_words + 32 * blk] = epi::get(st, r);
+}
+
+// 3: Z1 = tanh(acc + b1) -> Z1 [n, H1].
 struct EpiHidden1 {
   const float* w;
   int64_t P, ob1;
   int H1, n;
   bf16* z1;
-  bf16* z1t;  // null: not written
-  template <int BN, class Load>
-  __device__ __forceinline__ void tile(int b, int row, int col0, const Load& load) const {
-    const float* b1 = w + b * P + ob1;
-    bf16* dst = z1 + (static_cast<int64_t>(b) * n + row) * H1 + col0;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    const float* b1 = w + b * P + ob1 + col0;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(z1 + (static_cast<int64_t>(b) * n + row0) * H1 +
+                                                col0) + epi::lane_id();
+    float unused = 0.f;
 #pragma unroll 1
-    for (int c = 0; c < BN / 16; ++c) {
-      float v[16];
-      load(c, v);
-#pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] = tanh_approx(v[k] + __ldg(b1 + col0 + 16 * c + k));
-      store_bf16x16(dst + 16 * c, v);
-      if (z1t != nullptr) {
-        bf16* tr = z1t + (static_cast<int64_t>(b) * H1 + col0 + 16 * c) * n + row;
-#pragma unroll
-        for (int k = 0; k < 16; ++k) tr[static_cast<int64_t>(k) * n] = __float2bfloat16_rn(v[k]);
-      }
+    for (int blk = 0; blk < NC / 64; ++blk) {
+      uint32_t pk[32];
+      tanh_block(load, blk, b1, pk, nullptr, unused);
+      store_block(dst, H1 / 2, blk, pk, st);
     }
   }
 };
 
-// 4: Z2 = tanh(acc + b2) -> Z2 [n, H2]; the fp32 partial Z2 . W3 over this
-//    tile's columns -> outp [H2/BN, n].
+// 4: Z2 = tanh(acc + b2) -> Z2 [n, H2]; the fp32 partial Z2 . W3 over the
+//    warp's NC columns -> outp [H2 / NC, n].
 struct EpiHidden2 {
   const float* w;
   int64_t P, ob2, oW3;
   int H2, n;
   bf16* z2;
   float* outp;
-  template <int BN, class Load>
-  __device__ __forceinline__ void tile(int b, int row, int col0, const Load& load) const {
-    const float* b2 = w + b * P + ob2;
-    const float* w3 = w + b * P + oW3;
-    bf16* dst = z2 + (static_cast<int64_t>(b) * n + row) * H2 + col0;
-    float acc = 0.f;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    const float* b2 = w + b * P + ob2 + col0;
+    const float* w3 = w + b * P + oW3 + col0;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(z2 + (static_cast<int64_t>(b) * n + row0) * H2 +
+                                                col0) + epi::lane_id();
+    float dot = 0.f;
 #pragma unroll 1
-    for (int c = 0; c < BN / 16; ++c) {
-      float v[16];
-      load(c, v);
-#pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        const int j = col0 + 16 * c + k;
-        v[k] = tanh_approx(v[k] + __ldg(b2 + j));
-        acc = fmaf(v[k], __ldg(w3 + j), acc);
-      }
-      store_bf16x16(dst + 16 * c, v);
+    for (int blk = 0; blk < NC / 64; ++blk) {
+      uint32_t pk[32];
+      tanh_block(load, blk, b2, pk, w3, dot);
+      store_block(dst, H2 / 2, blk, pk, st);
     }
-    outp[(static_cast<int64_t>(b) * (H2 / BN) + col0 / BN) * n + row] = acc;
+    outp[(static_cast<int64_t>(b) * (H2 / NC) + col0 / NC) * n + row0 + epi::lane_id()] = dot;
   }
 };
 
-// 6: G1 = acc * (1 - Z1^2) -> G1t [H1, n]; per-warp column sums -> pb1
+// 7: G1 = acc * (1 - Z1^2) written over Z1 [n, H1] (the block is read and
+//    then rewritten by the same warp); per-warp column sums -> pb1
 //    [n/32, H1].
 struct EpiAdjoint1 {
-  const bf16* z1;
-  bf16* g1t;
+  bf16* z1;
   float* pb1;
   int H1, n;
-  template <int BN, class Load>
-  __device__ __forceinline__ void tile(int b, int row, int col0, const Load& load) const {
-    const int lane = threadIdx.x & 31;
-    const bf16* zr = z1 + (static_cast<int64_t>(b) * n + row) * H1 + col0;
-    float* part = pb1 + (static_cast<int64_t>(b) * (n / 32) + row / 32) * H1 + col0;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    const int lane = epi::lane_id();
+    uint32_t* zrow = reinterpret_cast<uint32_t*>(z1 + (static_cast<int64_t>(b) * n + row0) * H1 +
+                                                 col0) + lane;
+    float* part = pb1 + (static_cast<int64_t>(b) * (n / 32) + row0 / 32) * H1 + col0;
 #pragma unroll 1
-    for (int c = 0; c < BN / 16; ++c) {
-      float v[16], z[16];
-      load(c, v);
-      load_bf16x16(zr + 16 * c, z);
+    for (int blk = 0; blk < NC / 64; ++blk) {
+      uint32_t zw[32];
 #pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] *= 1.f - z[k] * z[k];
-      bf16* tr = g1t + (static_cast<int64_t>(b) * H1 + col0 + 16 * c) * n + row;
+      for (int r = 0; r < 32; ++r) zw[r] = zrow[static_cast<int64_t>(r) * (H1 / 2) + 32 * blk];
 #pragma unroll
-      for (int k = 0; k < 16; ++k) tr[static_cast<int64_t>(k) * n] = __float2bfloat16_rn(v[k]);
-      const float cs = warp_colsum16(v, lane);
-      if ((lane & 1) == 0) part[16 * c + (lane >> 1)] = cs;
+      for (int r = 0; r < 32; ++r) epi::set(st, r, zw[r]);
+      epi::get_row(st, zw);
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        float v[32];
+        load(2 * blk + half, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float za, zb;
+          unpack_bf16x2(zw[16 * half + j], za, zb);
+          v[2 * j] *= 1.f - za * za;
+          v[2 * j + 1] *= 1.f - zb * zb;
+          zw[16 * half + j] = pack_bf16x2(v[2 * j], v[2 * j + 1]);
+        }
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          float v16[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) v16[k] = v[16 * g + k];
+          const float cs = warp_colsum16(v16, lane);
+          if ((lane & 1) == 0) part[64 * blk + 32 * half + 16 * g + (lane >> 1)] = cs;
+        }
+      }
+      epi::put_rows(st, zw);
+#pragma unroll 4
+      for (int r = 0; r < 32; ++r) zrow[static_cast<int64_t>(r) * (H1 / 2) + 32 * blk] = epi::get(st, r);
     }
   }
 };
 
-// 7 and 8: gradient of a weight matrix plus the prior term.  Element
-// (row, col) of the GEMM lands at grad[b*P + off + row*rs + col*cs].
-struct EpiWeightGrad {
-  const float* w;
+// 6: likelihood gradient of a row-major weight matrix (GEMM row = matrix
+//    row), grad[b*P + off + row*ld + col]; the prior term is added by
+//    mlp_prior_kernel.
+struct EpiGradRows {
   float* grad;
-  int64_t P, off, rs, cs;
-  float pf;  // 1 / (s^2 T); 0 for a flat prior
-  template <int BN, class Load>
-  __device__ __forceinline__ void tile(int b, int row, int col0, const Load& load) const {
-    const int64_t base = b * P + off + row * rs;
+  int64_t P, off, ld;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    float* dst = grad + b * P + off + row0 * ld + col0 + epi::lane_id();
 #pragma unroll 1
-    for (int c = 0; c < BN / 16; ++c) {
-      float v[16];
+    for (int c = 0; c < NC / 32; ++c) {
+      float v[32];
+      uint32_t u[32];
       load(c, v);
 #pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        const int64_t e = base + static_cast<int64_t>(col0 + 16 * c + k) * cs;
-        grad[e] = fmaf(pf, __ldg(w + e), v[k]);
-      }
+      for (int j = 0; j < 32; ++j) u[j] = __float_as_uint(v[j]);
+      epi::put_rows(st, u);
+#pragma unroll 4
+      for (int r = 0; r < 32; ++r) dst[r * ld + 32 * c] = __uint_as_float(epi::get(st, r));
     }
   }
 };
+
+// 8: likelihood gradient of a matrix stored transposed to the GEMM (GEMM row
+//    = matrix column): grad[b*P + off + col*ld + row]; lanes hold consecutive
+//    rows, so each store is already one contiguous segment.
+struct EpiGradCols {
+  float* grad;
+  int64_t P, off, ld;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t*) const {
+    float* dst = grad + b * P + off + row0 + epi::lane_id();
+#pragma unroll 1
+    for (int c = 0; c < NC / 32; ++c) {
+      float v[32];
+      load(c, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) dst[static_cast<int64_t>(col0 + 32 * c + j) * ld] = v[j];
+    }
+  }
+};
+
+// grad[W1 | W2] += w / (s^2 T) for every chain.  Grid (prep_blocks - 1,
+// chains); same element pairing as mlp_prep_kernel.
+__global__ void __launch_bounds__(256) mlp_prior_kernel(const MlpArgs a, float pf) {
+  const MlpShape& s = a.s;
+  const int c = blockIdx.y, t = threadIdx.x;
+  const int64_t pw = matrix_params(s);
+  const float* w = a.w + static_cast<int64_t>(c) * s.P;
+  float* g = a.grad + static_cast<int64_t>(c) * s.P;
+  const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kPrepPerBlock + 2 * t;
+  float v0[kPrepPairs], v1[kPrepPairs], g0[kPrepPairs], g1[kPrepPairs];
+#pragma unroll
+  for (int k = 0; k < kPrepPairs; ++k) {
+    const int64_t e = e0 + 512 * k;
+    const bool in = e < pw;
+    v0[k] = in ? __ldg(w + e) : 0.f;
+    v1[k] = in ? __ldg(w + e + 1) : 0.f;
+    g0[k] = in ? g[e] : 0.f;
+    g1[k] = in ? g[e + 1] : 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < kPrepPairs; ++k) {
+    const int64_t e = e0 + 512 * k;
+    if (e < pw) {
+      g[e] = fmaf(pf, v0[k], g0[k]);
+      g[e + 1] = fmaf(pf, v1[k], g1[k]);
+    }
+  }
+}
 
 // ---------------------------------------------------------------------------
-// 5. Output layer, likelihood and the first adjoint.  Grid (H2/256, n/64,
-//    chains) with a gradient, (1, n/64, chains) without.
+// 5. Output layer, likelihood and the first adjoint for 64 rows of a chain.
+//    Grid (n/64, chains).  With a gradient the block then streams its
+//    64 x H2 block of Z2 in 16-byte vectors, writes G2 over it and leaves
+//    per-block column sums for dW3 (sum_i g_i Z2_ij) and db2 (sum_i G2_ij).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
   __shared__ float g_s[kTile];
-  __shared__ double red[32];
-  __shared__ float colp[2][2][kOutCols];
-  __shared__ __align__(16) bf16 tileT[kOutCols][kTile + 2];  // 33-word rows
+  __shared__ double red[2][4];
+  __shared__ float colp[2][256 * 8];
   const MlpShape& s = a.s;
-  const int c = blockIdx.z, rb = blockIdx.y, i0 = rb * kTile, c0 = blockIdx.x * kOutCols;
-  const int t = threadIdx.x;
+  const int c = blockIdx.y, rb = blockIdx.x, i0 = rb * kTile;
+  const int t = threadIdx.x, lane = t & 31;
   const float* w = a.w + static_cast<int64_t>(c) * s.P;
-  const float inv_s2 = 1.f / (a.sigma * a.sigma);
-  const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n / a.temperature);
-  double lk_m = 0.0, lk_sum = 0.0, lk_sq = 0.0, g_sum = 0.0;
   if (t < kTile) {
+    const float inv_s2 = 1.f / (a.sigma * a.sigma);
+    const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n / a.temperature);
     const int i = i0 + t;
-    const int ntile = s.H2 / kBN;
+    const int nslot = s.H2 / kSlot;
     float out = __ldg(w + s.ob3);
-    for (int q = 0; q < ntile; ++q)
-      out += a.outp[(static_cast<int64_t>(c) * ntile + q) * a.n + i];
+    for (int q = 0; q < nslot; ++q) out += a.outp[(static_cast<int64_t>(c) * nslot + q) * a.n + i];
     const float r = a.yv[static_cast<int64_t>(c) * a.n + i] - out;
     const float lk = -0.5f * r * r * inv_s2 - logf(a.sigma) - 0.91893853320467274f;
     const float m = a.mask != nullptr ? __ldg(a.mask + static_cast<int64_t>(c) * a.n + i) : 1.f;
     const float g = -scale * m * r * inv_s2;
     g_s[t] = g;
-    lk_m = static_cast<double>(m) * lk;
-    lk_sum = lk;
-    lk_sq = static_cast<double>(lk) * lk;
-    g_sum = g;
-    if (blockIdx.x == 0 && a.lk != nullptr) a.lk[static_cast<int64_t>(c) * a.n + i] = lk;
-  }
-  if (blockIdx.x == 0) {
+    if (a.lk != nullptr) a.lk[static_cast<int64_t>(c) * a.n + i] = lk;
     // var(lk) is over all n values, masked or not (jnp.var, integrator.py:880).
-    const double s0 = block_sum(lk_m, red);
-    const double s1 = block_sum(lk_sum, red);
-    const double s2 = block_sum(lk_sq, red);
-    const double s3 = block_sum(g_sum, red);
-    if (t == 0) {
-      double* p = a.plk + (static_cast<int64_t>(c) * (a.n / kTile) + rb) * 4;
-      p[0] = s0;
-      p[1] = s1;
-      p[2] = s2;
-      p[3] = s3;
-    }
+    double v4[4] = {static_cast<double>(m) * lk, lk, static_cast<double>(lk) * lk, g};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v4[k] = warp_sum(v4[k]);
+    if (lane == 0)
+      for (int k = 0; k < 4; ++k) red[t >> 5][k] = v4[k];
+  }
+  __syncthreads();
+  if (t == 0) {
+    double* p = a.plk + (static_cast<int64_t>(c) * (a.n / kTile) + rb) * 4;
+    for (int k = 0; k < 4; ++k) p[k] = red[0][k] + red[1][k];
   }
   if (!a.want_grad) return;
-  __syncthreads();
-  // Thread t handles columns c0 + 2p, c0 + 2p + 1 on rows rg, rg + 2, ...
-  const int p = t & 127, rg = t >> 7;
-  const int j = c0 + 2 * p;
-  const float w3a = __ldg(w + s.oW3 + j), w3b = __ldg(w + s.oW3 + j + 1);
-  bf16* z2g = a.z2g + static_cast<int64_t>(c) * a.n * s.H2;
-  float aw3a = 0.f, aw3b = 0.f, ab2a = 0.f, ab2b = 0.f;
-#pragma unroll 4
-  for (int r = rg; r < kTile; r += 2) {
-    uint32_t* cell = reinterpret_cast<uint32_t*>(z2g + static_cast<int64_t>(i0 + r) * s.H2 + j);
-    float za, zb;
-    unpack_bf16x2(*cell, za, zb);
-    const float g = g_s[r];
-    const float ga = g * w3a * (1.f - za * za), gb = g * w3b * (1.f - zb * zb);
-    *cell = pack_bf16x2(ga, gb);
-    aw3a = fmaf(g, za, aw3a);
-    aw3b = fmaf(g, zb, aw3b);
-    ab2a += ga;
-    ab2b += gb;
-    tileT[2 * p][r] = __float2bfloat16_rn(ga);
-    tileT[2 * p + 1][r] = __float2bfloat16_rn(gb);
-  }
-  colp[0][rg][2 * p] = aw3a;
-  colp[0][rg][2 * p + 1] = aw3b;
-  colp[1][rg][2 * p] = ab2a;
-  colp[1][rg][2 * p + 1] = ab2b;
-  __syncthreads();
-  {
-    const int64_t pr = (static_cast<int64_t>(c) * (a.n / kTile) + rb) * s.H2 + c0 + t;
-    a.pw3[pr] = colp[0][0][t] + colp[0][1][t];
-    a.pb2[pr] = colp[1][0][t] + colp[1][1][t];
-  }
-  // G2t rows: 64 contiguous BF16 (128 bytes) per column.
-  bf16* g2t = a.g2t + static_cast<int64_t>(c) * s.H2 * a.n;
-  const int lane = t & 31, warp = t >> 5;
-#pragma unroll 4
-  for (int k = 0; k < kOutCols / 8; ++k) {
-    const int jj = warp * (kOutCols / 8) + k;
-    *reinterpret_cast<uint32_t*>(g2t + static_cast<int64_t>(c0 + jj) * a.n + i0 + 2 * lane) =
-        *reinterpret_cast<const uint32_t*>(&tileT[jj][2 * lane]);
+  // Threads: CT column threads (8 columns each) x RG row groups.
+  const int cpr = s.H2 / 8;
+  const int CT = cpr < 256 ? cpr : 256, RG = 256 / CT;
+  const int ct = t % CT, rg = t / CT;
+  uint4* z2 = reinterpret_cast<uint4*>(a.z2g + (static_cast<int64_t>(c) * a.n + i0) * s.H2);
+  // Every thread runs the same number of passes (the barriers below).
+  for (int base = 0; base < cpr; base += CT) {
+    const int ch = base + ct;
+    const bool active = ch < cpr;
+    float w3[8], aw[8], ab[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      w3[k] = active ? __ldg(w + s.oW3 + 8 * ch + k) : 0.f;
+      aw[k] = 0.f;
+      ab[k] = 0.f;
+    }
+    for (int r0 = rg; active && r0 < kTile; r0 += 8 * RG) {
+      uint4 cell[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (r0 + k * RG < kTile) cell[k] = z2[static_cast<int64_t>(r0 + k * RG) * cpr + ch];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int r = r0 + k * RG;
+        if (r >= kTile) break;
+        const float g = g_s[r];
+        uint32_t* u = reinterpret_cast<uint32_t*>(&cell[k]);
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          float za, zb;
+          unpack_bf16x2(u[h], za, zb);
+          const float ga = g * w3[2 * h] * (1.f - za * za);
+          const float gb = g * w3[2 * h + 1] * (1.f - zb * zb);
+          aw[2 * h] = fmaf(g, za, aw[2 * h]);
+          aw[2 * h + 1] = fmaf(g, zb, aw[2 * h + 1]);
+          ab[2 * h] += ga;
+          ab[2 * h + 1] += gb;
+          u[h] = pack_bf16x2(ga, gb);
+        }
+        z2[static_cast<int64_t>(r) * cpr + ch] = cell[k];
+      }
+    }
+    // Column sums over the RG row groups.
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      colp[0][t * 8 + k] = aw[k];
+      colp[1][t * 8 + k] = ab[k];
+    }
+    __syncthreads();
+    if (rg == 0 && active) {
+      const int64_t pr = (static_cast<int64_t>(c) * (a.n / kTile) + rb) * s.H2 + 8 * ch;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        float sw = 0.f, sb = 0.f;
+        for (int q = 0; q < RG; ++q) {
+          sw += colp[0][(q * CT + ct) * 8 + k];
+          sb += colp[1][(q * CT + ct) * 8 + k];
+        }
+        a.pw3[pr + k] = sw;
+        a.pb2[pr + k] = sb;
+      }
+    }
   }
 }
 
@@ -614,16 +666,10 @@ T* view(void* ws, size_t off) {
 
 int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   const MlpShape& s = a.s;
-  a.w1t = view<bf16>(ws, L.w1t);
-  a.w2t = view<bf16>(ws, L.w2t);
-  a.w2b = view<bf16>(ws, L.w2b);
+  a.wb = view<bf16>(ws, L.wb);
   a.xb = view<bf16>(ws, L.xb);
-  a.xt = view<bf16>(ws, L.xt);
   a.z1 = view<bf16>(ws, L.z1);
-  a.z1t = view<bf16>(ws, L.z1t);
   a.z2g = view<bf16>(ws, L.z2g);
-  a.g2t = view<bf16>(ws, L.g2t);
-  a.g1t = view<bf16>(ws, L.g1t);
   a.yv = view<float>(ws, L.yv);
   a.outp = view<float>(ws, L.outp);
   a.pw3 = view<float>(ws, L.pw3);
@@ -632,7 +678,10 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   a.psq = view<double>(ws, L.psq);
   a.plk = view<double>(ws, L.plk);
   const int C = a.chains, n = a.n, D = s.D, H1 = s.H1, H2 = s.H2;
+  const int64_t pw = matrix_params(s);
   const int nprep = prep_blocks(s);
+  const bf16* w1b = a.wb;
+  const bf16* w2b = a.wb + s.oW2;
   int rc;
 
   mlp_prep_kernel<<<dim3(nprep, C), 256, 0, st>>>(a);
@@ -640,41 +689,53 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   mlp_gather_kernel<<<dim3(n / kTile, D / kTile, C), 256, 0, st>>>(a);
   if ((rc = check_launch("mlp_gather_kernel")) != GBSGMC_OK) return rc;
 
-  // Tensor maps: (K columns, rows, chains), box 64 x {128 | BN}.
-  CUtensorMap m_xb, m_w1t, m_z1, m_w2t;
-  if ((rc = make_tmap_bf16_3d(&m_xb, a.xb, D, n, C, D, int64_t(n) * D, kGemmBK, kGemmBM)) ||
-      (rc = make_tmap_bf16_3d(&m_w1t, a.w1t, D, H1, C, D, int64_t(H1) * D, kGemmBK, kBN)) ||
-      (rc = make_tmap_bf16_3d(&m_z1, a.z1, H1, n, C, H1, int64_t(n) * H1, kGemmBK, kGemmBM)) ||
-      (rc = make_tmap_bf16_3d(&m_w2t, a.w2t, H1, H2, C, H1, int64_t(H2) * H1, kGemmBK, kBN)))
+  // Tensor maps (columns, rows, chains).  K-major operands use 64 x 128 (A)
+  // or 64 x BN (B) boxes, MN-major ones 64 x 64 boxes.
+  const int64_t sx = int64_t(n) * D, s1 = int64_t(n) * H1, s2 = int64_t(n) * H2;
+  CUtensorMap m_xb, m_w1, m_z1, m_w2;
+  if ((rc = make_tmap_bf16_3d(&m_xb, a.xb, D, n, C, D, sx, kGemmBK, kGemmBM)) ||
+      (rc = make_tmap_bf16_3d(&m_w1, w1b, H1, D, C, H1, pw, 64, 64)) ||
+      (rc = make_tmap_bf16_3d(&m_z1, a.z1, H1, n, C, H1, s1, kGemmBK, kGemmBM)) ||
+      (rc = make_tmap_bf16_3d(&m_w2, w2b, H2, H1, C, H2, pw, 64, 64)))
     return rc;
-
-  const EpiHidden1 e1{a.w, s.P, s.ob1, H1, n, a.z1, a.want_grad ? a.z1t : nullptr};
-  if ((rc = launch_gemm<kBN>(m_xb, m_w1t, C, n, H1, D, a.status, e1, st))) return rc;
+  // 3: A1 = Xb W1 (W1 [D, H1] is the MN-major B operand).
+  const EpiHidden1 e1{a.w, s.P, s.ob1, H1, n, a.z1};
+  if ((rc = launch_gemm<kBN, false, true>(m_xb, m_w1, C, n, H1, D, a.status, e1, st))) return rc;
+  // 4: A2 = Z1 W2.
   const EpiHidden2 e2{a.w, s.P, s.ob2, s.oW3, H2, n, a.z2g, a.outp};
-  if ((rc = launch_gemm<kBN>(m_z1, m_w2t, C, n, H2, H1, a.status, e2, st))) return rc;
+  if ((rc = launch_gemm<kBN, false, true>(m_z1, m_w2, C, n, H2, H1, a.status, e2, st))) return rc;
 
-  mlp_out_kernel<<<dim3(a.want_grad ? H2 / kOutCols : 1, n / kTile, C), 256, 0, st>>>(a);
+  mlp_out_kernel<<<dim3(n / kTile, C), 256, 0, st>>>(a);
   if ((rc = check_launch("mlp_out_kernel")) != GBSGMC_OK) return rc;
 
   if (a.want_grad) {
-    CUtensorMap m_g2, m_w2b, m_z1t, m_g2t, m_g1t, m_xt;
-    if ((rc = make_tmap_bf16_3d(&m_g2, a.z2g, H2, n, C, H2, int64_t(n) * H2, kGemmBK, kGemmBM)) ||
-        (rc = make_tmap_bf16_3d(&m_w2b, a.w2b, H2, H1, C, H2, int64_t(H1) * H2, kGemmBK, kBN)) ||
-        (rc = make_tmap_bf16_3d(&m_z1t, a.z1t, n, H1, C, n, int64_t(H1) * n, kGemmBK, kGemmBM)) ||
-        (rc = make_tmap_bf16_3d(&m_g2t, a.g2t, n, H2, C, n, int64_t(H2) * n, kGemmBK, kBN)) ||
-        (rc = make_tmap_bf16_3d(&m_g1t, a.g1t, n, H1, C, n, int64_t(H1) * n, kGemmBK, kGemmBM)) ||
-        (rc = make_tmap_bf16_3d(&m_xt, a.xt, n, D, C, n, int64_t(D) * n, kGemmBK, 64)))
+    CUtensorMap m_z1mn, m_g2mn, m_g2, m_w2k, m_xbmn;
+    if ((rc = make_tmap_bf16_3d(&m_z1mn, a.z1, H1, n, C, H1, s1, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_g2mn, a.z2g, H2, n, C, H2, s2, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_g2, a.z2g, H2, n, C, H2, s2, kGemmBK, kGemmBM)) ||
+        (rc = make_tmap_bf16_3d(&m_w2k, w2b, H2, H1, C, H2, pw, kGemmBK, kBN)) ||
+        (rc = make_tmap_bf16_3d(&m_xbmn, a.xb, D, n, C, D, sx, 64, 64)))
       return rc;
-    const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;
-    const float pf = a.prior_scale > 0.f ? static_cast<float>(1.0 / (s2 * a.temperature)) : 0.f;
-    const EpiAdjoint1 e3{a.z1, a.g1t, a.pb1, H1, n};
-    if ((rc = launch_gemm<kBN>(m_g2, m_w2b, C, n, H1, H2, a.status, e3, st))) return rc;
-    // dW2[i, j] (row i of H1, column j of H2) = sum_r Z1t[i, r] G2t[j, r].
-    const EpiWeightGrad e4{a.w, a.grad, s.P, s.oW2, H2, 1, pf};
-    if ((rc = launch_gemm<kBN>(m_z1t, m_g2t, C, H1, H2, n, a.status, e4, st))) return rc;
-    // dW1[f, i] = sum_r G1t[i, r] Xt[f, r]: GEMM row i, column f.
-    const EpiWeightGrad e5{a.w, a.grad, s.P, s.oW1, 1, H1, pf};
-    if ((rc = launch_gemm<64>(m_g1t, m_xt, C, H1, D, n, a.status, e5, st))) return rc;
+    const double sc2 = static_cast<double>(a.prior_scale) * a.prior_scale;
+    const float pf = a.prior_scale > 0.f ? static_cast<float>(1.0 / (sc2 * a.temperature)) : 0.f;
+    // 6: dW2 [H1, H2] = Z1^T G2 (both operands MN-major), before step 7
+    //    overwrites Z1.
+    const EpiGradRows e6{a.grad, s.P, s.oW2, H2};
+    if ((rc = launch_gemm<kBN, true, true>(m_z1mn, m_g2mn, C, H1, H2, n, a.status, e6, st)))
+      return rc;
+    // 7: G1 = (G2 W2^T) * (1 - Z1^2); W2 [H1, H2] is the K-major B operand.
+    const EpiAdjoint1 e7{a.z1, a.pb1, H1, n};
+    if ((rc = launch_gemm<kBN, false, false>(m_g2, m_w2k, C, n, H1, H2, a.status, e7, st)))
+      return rc;
+    // 8: dW1^T [H1, D] = G1^T Xb: GEMM row i (hidden unit), column f
+    //    (feature) lands at dW1[f, i].
+    const EpiGradCols e8{a.grad, s.P, s.oW1, H1};
+    if ((rc = launch_gemm<64, true, true>(m_z1mn, m_xbmn, C, H1, D, n, a.status, e8, st)))
+      return rc;
+    if (pf != 0.f) {
+      mlp_prior_kernel<<<dim3(nprep - 1, C), 256, 0, st>>>(a, pf);
+      if ((rc = check_launch("mlp_prior_kernel")) != GBSGMC_OK) return rc;
+    }
   }
   const int fx = a.want_grad ? ceil_div(H1 > H2 ? H1 : H2, 256) : 1;
   mlp_finalize_kernel<<<dim3(fx, C), 256, 0, st>>>(a, nprep);

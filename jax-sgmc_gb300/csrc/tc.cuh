@@ -66,16 +66,41 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// As tmem_ld16 for 32 consecutive columns (one wait for all 32).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
+        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // ---------------------------------------------------------------------------
 // MMA.
 // ---------------------------------------------------------------------------
 
 // Instruction descriptor of tcgen05.mma kind::f16: BF16 A and B, FP32 D,
-// both operands K-major, M x N tile.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+// M x N tile; a_mn / b_mn select the MN-major ("transposed") layout of an
+// operand instead of K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N, bool a_mn = false,
+                                                      bool b_mn = false) {
   return (1u << 4)                                   // D format: F32
          | (1u << 7)                                 // A format: BF16
          | (1u << 10)                                // B format: BF16
+         | (static_cast<uint32_t>(a_mn) << 15)       // A major: MN
+         | (static_cast<uint32_t>(b_mn) << 16)       // B major: MN
          | (static_cast<uint32_t>(N >> 3) << 17)     // N / 8
          | (static_cast<uint32_t>(M >> 4) << 24);    // M / 16
 }
@@ -90,6 +115,22 @@ __device__ __forceinline__ uint64_t sdesc_k_sw128(const void* tile) {
   d |= static_cast<uint64_t>(1024 >> 4) << 32;    // stride byte offset
   d |= 1ull << 46;                                // descriptor version
   d |= 2ull << 61;                                // 128-byte swizzle
+  return d;
+}
+
+// Shared-memory descriptor of an MN-major tile in the 128-byte swizzled
+// layout: each K row holds 64 consecutive MN elements (128 bytes), 8-row
+// groups are 1024 bytes apart (stride byte offset) and consecutive 64-wide
+// MN blocks `mn_block_bytes` apart (leading byte offset).  One K=16 slice
+// spans two 8-row groups, so the next slice starts 2048 bytes further on.
+__device__ __forceinline__ uint64_t sdesc_mn_sw128(const void* tile,
+                                                   uint32_t mn_block_bytes) {
+  const uint64_t addr = smem_addr(tile);
+  uint64_t d = (addr >> 4) & 0x3FFFull;
+  d |= static_cast<uint64_t>((mn_block_bytes >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;
+  d |= 1ull << 46;
+  d |= 2ull << 61;
   return d;
 }
 

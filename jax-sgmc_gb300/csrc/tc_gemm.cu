@@ -1,16 +1,10 @@
 // Batched BF16 GEMM on the 5th-generation tensor cores:
 //   C[b] (M x N, fp32) = A[b] (M x K) * B[b] (N x K)^T,
-// A and B row-major with K contiguous ("K-major"), both BF16.
-//
-// One CTA computes a 128 x BN tile of one batch entry.  Warp 0 (one lane)
-// streams 128x64 A tiles and BNx64 B tiles into a 4-stage shared-memory ring
-// with TMA (128-byte swizzle), warp 1 allocates BN TMEM columns and one of
-// its lanes issues tcgen05.mma (M=128, N=BN, K=16, four per 64-wide K tile),
-// committing each stage back to the producer; warps 2-5 read the 128 x BN
-// fp32 accumulator out of TMEM (each warp its 32-lane quarter, tcgen05.ld
-// 32x32b) and hand 16 columns at a time to the epilogue.  Every wait is
-// bounded: after kWaitLimitNs the CTA records GBSGMC_ERR_TIMEOUT, lets the
-// work it issued drain, frees its TMEM and returns.
+// with each operand stored K-major (row-major with K contiguous) or
+// MN-major (stored transposed).  The kernel itself (persistent, TMA ring,
+// double-buffered TMEM accumulators) is in tc_gemm.cuh so that other
+// translation units instantiate it with fused epilogues; this file holds
+// the tensor-map encoder and the plain fp32-output entry points.
 #include <cuda.h>
 
 #include <mutex>
@@ -79,22 +73,24 @@ int make_tmap_bf16_3d(CUtensorMap* map, const void* base, int64_t cols,
 
 namespace {
 
-// Plain fp32 store of the accumulator.
+// Plain fp32 store of the accumulator, one 128-byte row segment per store.
 struct StoreF32 {
   float* C;
   int64_t ldc, batch_stride;
-  template <int BN, class Load>
-  __device__ __forceinline__ void tile(int b, int row, int col0,
-                                       const Load& load) const {
-    float* dst = C + b * batch_stride + static_cast<int64_t>(row) * ldc + col0;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    float* dst = C + b * batch_stride + static_cast<int64_t>(row0) * ldc + col0 + epi::lane_id();
 #pragma unroll 1
-    for (int c = 0; c < BN / 16; ++c) {
-      float v[16];
+    for (int c = 0; c < NC / 32; ++c) {
+      float v[32];
+      uint32_t w[32];
       load(c, v);
-      float4* out = reinterpret_cast<float4*>(dst + 16 * c);
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-        out[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+      for (int j = 0; j < 32; ++j) w[j] = __float_as_uint(v[j]);
+      epi::put_rows(st, w);
+#pragma unroll 4
+      for (int r = 0; r < 32; ++r) dst[r * ldc + 32 * c] = __uint_as_float(epi::get(st, r));
     }
   }
 };
@@ -104,12 +100,58 @@ struct StoreF32 {
 size_t gemm_smem_bytes(int bn) {
   return 1024 + static_cast<size_t>(kGemmStages) *
                     (kGemmBM * kGemmBK * 2 + static_cast<size_t>(bn) * kGemmBK * 2) +
-         (2 * kGemmStages + 1) * 8 + 16;
+         static_cast<size_t>(kGemmEpiWarps) * kStageWords * 4 + (2 * kGemmStages + 5) * 8 + 16;
 }
 
 }  // namespace gbsgmc
 
 using namespace gbsgmc;
+
+namespace {
+
+template <int BN>
+int dispatch_layout(bool a_mn, bool b_mn, const CUtensorMap& ta, const CUtensorMap& tb,
+                    int batch, int M, int N, int K, int* status, const StoreF32& epi,
+                    cudaStream_t st) {
+  if (a_mn)
+    return b_mn ? launch_gemm<BN, true, true>(ta, tb, batch, M, N, K, status, epi, st)
+                : launch_gemm<BN, true, false>(ta, tb, batch, M, N, K, status, epi, st);
+  return b_mn ? launch_gemm<BN, false, true>(ta, tb, batch, M, N, K, status, epi, st)
+              : launch_gemm<BN, false, false>(ta, tb, batch, M, N, K, status, epi, st);
+}
+
+}  // namespace
+
+extern "C" int gbsgmc_gemm_bf16(int a_mn, int b_mn, const void* A_dev, int64_t lda,
+                                int64_t a_batch_stride, const void* B_dev, int64_t ldb,
+                                int64_t b_batch_stride, float* C_dev, int64_t ldc,
+                                int64_t c_batch_stride, int batch, int M, int N, int K,
+                                int* status_dev, gbsgmc_stream_t stream) {
+  if (A_dev == nullptr || B_dev == nullptr || C_dev == nullptr || status_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "gemm_bf16: null pointer");
+  if (batch <= 0 || M <= 0 || N <= 0 || K <= 0 || batch > (1 << 20))
+    return set_error(GBSGMC_ERR_ARG, "gemm_bf16: sizes must be positive");
+  if (M % kGemmBM != 0 || N % 128 != 0 || K % kGemmBK != 0)
+    return set_error(GBSGMC_ERR_SHAPE,
+                     "gemm_bf16: needs M %% 128 == 0, N %% 128 == 0, "
+                     "K %% 64 == 0 (got %d, %d, %d)", M, N, K);
+  if (lda < (a_mn ? M : K) || ldb < (b_mn ? N : K) || ldc < N || ldc % 4 != 0 ||
+      reinterpret_cast<uintptr_t>(C_dev) % 16 != 0 || c_batch_stride % 4 != 0)
+    return set_error(GBSGMC_ERR_ARG, "gemm_bf16: bad leading dimension");
+  const int bn = N % 256 == 0 ? 256 : 128;
+  CUtensorMap ta, tb;
+  int rc = a_mn ? make_tmap_bf16_3d(&ta, A_dev, M, K, batch, lda, a_batch_stride, 64, 64)
+                : make_tmap_bf16_3d(&ta, A_dev, K, M, batch, lda, a_batch_stride,
+                                    kGemmBK, kGemmBM);
+  if (rc != GBSGMC_OK) return rc;
+  rc = b_mn ? make_tmap_bf16_3d(&tb, B_dev, N, K, batch, ldb, b_batch_stride, 64, 64)
+            : make_tmap_bf16_3d(&tb, B_dev, K, N, batch, ldb, b_batch_stride, kGemmBK, bn);
+  if (rc != GBSGMC_OK) return rc;
+  const StoreF32 epi{C_dev, ldc, c_batch_stride};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return bn == 256 ? dispatch_layout<256>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st)
+                   : dispatch_layout<128>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st);
+}
 
 extern "C" int gbsgmc_gemm_bf16_nt(const void* A_dev, int64_t lda,
                                    int64_t a_batch_stride, const void* B_dev,
@@ -118,27 +160,6 @@ extern "C" int gbsgmc_gemm_bf16_nt(const void* A_dev, int64_t lda,
                                    int64_t c_batch_stride, int batch, int M,
                                    int N, int K, int* status_dev,
                                    gbsgmc_stream_t stream) {
-  if (A_dev == nullptr || B_dev == nullptr || C_dev == nullptr)
-    return set_error(GBSGMC_ERR_ARG, "gemm_bf16_nt: null pointer");
-  if (batch <= 0 || M <= 0 || N <= 0 || K <= 0)
-    return set_error(GBSGMC_ERR_ARG, "gemm_bf16_nt: sizes must be positive");
-  if (M % kGemmBM != 0 || N % 128 != 0 || K % kGemmBK != 0)
-    return set_error(GBSGMC_ERR_SHAPE,
-                     "gemm_bf16_nt: needs M %% 128 == 0, N %% 128 == 0, "
-                     "K %% 64 == 0 (got %d, %d, %d)", M, N, K);
-  if (lda < K || ldb < K || ldc < N || ldc % 4 != 0 ||
-      reinterpret_cast<uintptr_t>(C_dev) % 16 != 0)
-    return set_error(GBSGMC_ERR_ARG, "gemm_bf16_nt: bad leading dimension");
-  const bool wide = N % 256 == 0;
-  CUtensorMap ta, tb;
-  int rc = make_tmap_bf16_3d(&ta, A_dev, K, M, batch, lda, a_batch_stride,
-                             kGemmBK, kGemmBM);
-  if (rc != GBSGMC_OK) return rc;
-  rc = make_tmap_bf16_3d(&tb, B_dev, K, N, batch, ldb, b_batch_stride, kGemmBK,
-                         wide ? 256 : 128);
-  if (rc != GBSGMC_OK) return rc;
-  const StoreF32 epi{C_dev, ldc, c_batch_stride};
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  return wide ? launch_gemm<256>(ta, tb, batch, M, N, K, status_dev, epi, st)
-              : launch_gemm<128>(ta, tb, batch, M, N, K, status_dev, epi, st);
+  return gbsgmc_gemm_bf16(0, 0, A_dev, lda, a_batch_stride, B_dev, ldb, b_batch_stride,
+                          C_dev, ldc, c_batch_stride, batch, M, N, K, status_dev, stream);
 }

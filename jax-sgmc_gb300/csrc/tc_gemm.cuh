@@ -11,10 +11,51 @@
 
 namespace gbsgmc {
 
-constexpr int kGemmBM = 128;       // rows of a CTA tile (UMMA M)
-constexpr int kGemmBK = 64;        // K per stage: one 128-byte swizzle row
-constexpr int kGemmStages = 4;     // shared-memory ring depth
-constexpr int kGemmThreads = 192;  // producer, MMA, 4 epilogue warps
+constexpr int kGemmBM = 128;     // rows of a CTA tile (UMMA M)
+constexpr int kGemmBK = 64;      // K per stage: one 128-byte swizzle row
+constexpr int kGemmStages = 4;   // shared-memory ring depth
+constexpr int kGemmSplit = 2;    // epilogue warps per TMEM lane quarter
+constexpr int kGemmEpiWarps = 4 * kGemmSplit;
+constexpr int kGemmThreads = 64 + 32 * kGemmEpiWarps;  // producer, MMA, epilogue
+constexpr int kStageWords = 32 * 33;  // per-warp staging tile (32 x 32 words, padded)
+
+// Epilogue staging helpers.  A warp's 32 lanes own 32 consecutive
+// accumulator rows; these move a 32-row block between that row-per-lane form
+// and row-contiguous global memory through the warp's staging tile, so that
+// every global access is one 128-byte row segment.
+namespace epi {
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+
+// Lane l's 32 words go to staging row l; afterwards any lane may read row r.
+__device__ __forceinline__ void put_rows(uint32_t* st, const uint32_t (&w)[32]) {
+  const int l = lane_id();
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 32; ++j) st[l * 33 + j] = w[j];
+  __syncwarp();
+}
+
+// Word `lane` of staging row r.
+__device__ __forceinline__ uint32_t get(const uint32_t* st, int r) {
+  return st[r * 33 + lane_id()];
+}
+
+// The reverse: word `lane` of row r was written by the whole warp (set),
+// and lane l collects its own row.
+__device__ __forceinline__ void set(uint32_t* st, int r, uint32_t v) {
+  st[r * 33 + lane_id()] = v;
+}
+__device__ __forceinline__ void get_row(const uint32_t* st, uint32_t (&w)[32]) {
+  const int l = lane_id();
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 32; ++j) w[j] = st[l * 33 + j];
+  __syncwarp();
+}
+
+}  // namespace epi
 
 // 3-D BF16 tensor map (cols innermost, rows, batch) with a 128-byte swizzled
 // box of box_cols x box_rows; strides in elements.
@@ -24,31 +65,59 @@ int make_tmap_bf16_3d(CUtensorMap* map, const void* base, int64_t cols,
 
 size_t gemm_smem_bytes(int bn);
 
-// Batched GEMM kernel C[b] = A[b] * B[b]^T (see tc_gemm.cu).  Each epilogue
-// thread owns one accumulator row of the CTA tile and calls
-//   epi.template tile<BN>(batch, row, first column of the tile, load)
-// where load(c, v) fills v[16] with columns [16c, 16c + 16) of that row
-// (warp-collective: all 32 lanes must call it with the same c).
-template <int BN, class Epi>
+// Persistent batched GEMM C[b] = A[b] * B[b]^T on the tcgen05 tensor cores.
+//
+// A is M x K and B is N x K, BF16; each is either K-major (rows of K
+// contiguous elements, A_MN / B_MN false) or MN-major (stored transposed:
+// rows of M or N contiguous elements).  The grid holds at most one CTA per
+// resident slot; CTA i takes output tiles i, i + gridDim.x, ... in the order
+// (batch, M tile, N tile), N fastest.  Roles:
+//   warp 0 (one lane)  TMA producer into a kGemmStages-deep ring of 64-wide
+//                      K slices (128-byte swizzle)
+//   warp 1             allocates two BN-column TMEM accumulators; one lane
+//                      issues tcgen05.mma (M=128, N=BN, K=16) into them
+//   warps 2..          epilogue, kGemmSplit warps per TMEM lane quarter:
+//                      warp w reads lanes 32 (w % 4) .. + 31 of the finished
+//                      accumulator, columns [h NC, (h + 1) NC) with
+//                      h = (w - 2) / 4 and NC = BN / kGemmSplit, while the
+//                      MMA warp fills the other accumulator with the next tile
+// Each epilogue lane owns one accumulator row and the warp calls
+//   epi.template tile<NC>(batch, row0, col0, load, stage)
+// with row0 the first of the warp's 32 rows (lane l holds row row0 + l),
+// col0 its first column, load(c, v) filling v[32] with columns
+// [32c, 32c + 32) of the lane's row (warp-collective), and stage a private
+// 32 x 33-word shared-memory tile for the epi:: helpers.
+//
+// Every wait is bounded (kWaitLimitNs): on a timeout the CTA records
+// GBSGMC_ERR_TIMEOUT, stops issuing work, waits for what it issued, frees
+// its TMEM and returns.
+template <int BN, bool A_MN, bool B_MN, class Epi>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta,
-                   const __grid_constant__ CUtensorMap tb, int K, int* status,
-                   Epi epi) {
+                   const __grid_constant__ CUtensorMap tb, int M, int N, int K,
+                   int batch, int* status, Epi epi) {
   constexpr int BM = kGemmBM, BK = kGemmBK, STAGES = kGemmStages;
   constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
+  constexpr uint32_t BLOCK_BYTES = 64 * BK * 2;  // one 64 x 64 MN-major box
+  constexpr uint32_t TMEM_COLS = 2 * BN;
+  static_assert(BN == 64 || BN == 128 || BN == 256, "BN");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   uint8_t* sa = smem;
   uint8_t* sb = smem + STAGES * A_BYTES;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sb + STAGES * B_BYTES);
+  uint32_t* stage_all = reinterpret_cast<uint32_t*>(sb + STAGES * B_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(stage_all + kGemmEpiWarps * kStageWords);
   uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* tfull = empty + STAGES;  // [2] accumulator ready for the epilogue
+  uint64_t* tempty = tfull + 2;      // [2] accumulator drained by the epilogue
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_tile = blockIdx.x, m_tile = blockIdx.y, b = blockIdx.z;
+  const int tiles_n = N / BN, per_batch = (M / BM) * tiles_n;
+  const int tiles = per_batch * batch;
   const int KB = K / BK;
 
   if (threadIdx.x == 0) {
@@ -56,12 +125,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       mbar_init(&full[i], 1);
       mbar_init(&empty[i], 1);
     }
-    mbar_init(accum, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], kGemmEpiWarps);
+    }
+    mbar_init(drain, 1);
     *abort_flag = 0;
     mbar_fence_init();
   }
   if (warp == 1) {
-    tc::tmem_alloc(tmem_slot, BN);
+    tc::tmem_alloc(tmem_slot, TMEM_COLS);
     tc::tmem_relinquish();
   }
   tc::fence_before_sync();
@@ -71,90 +144,153 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued = 0;
-      for (int kb = 0; kb < KB; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
-        if (!mbar_wait_bounded(&empty[s], ph ^ 1u, abort_flag)) {
-          raise_status(status, GBSGMC_ERR_TIMEOUT);
-          *abort_flag = 1;
-          break;
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x) {
+        const int b = t / per_batch, r = t - b * per_batch;
+        const int m0 = (r / tiles_n) * BM, n0 = (r % tiles_n) * BN;
+        for (int kb = 0; kb < KB; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1u;
+          if (!mbar_wait_bounded(&empty[s], ph ^ 1u, abort_flag)) {
+            raise_status(status, GBSGMC_ERR_TIMEOUT);
+            *abort_flag = 1;
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], A_BYTES + B_BYTES);
+          const int k0 = kb * BK;
+          if constexpr (A_MN) {
+#pragma unroll
+            for (int j = 0; j < BM / 64; ++j)
+              tc::tma_load_3d(sa + s * A_BYTES + j * BLOCK_BYTES, &ta, m0 + 64 * j, k0, b,
+                              &full[s]);
+          } else {
+            tc::tma_load_3d(sa + s * A_BYTES, &ta, k0, m0, b, &full[s]);
+          }
+          if constexpr (B_MN) {
+#pragma unroll
+            for (int j = 0; j < BN / 64; ++j)
+              tc::tma_load_3d(sb + s * B_BYTES + j * BLOCK_BYTES, &tb, n0 + 64 * j, k0, b,
+                              &full[s]);
+          } else {
+            tc::tma_load_3d(sb + s * B_BYTES, &tb, k0, n0, b, &full[s]);
+          }
         }
-        mbar_arrive_expect_tx(&full[s], A_BYTES + B_BYTES);
-        tc::tma_load_3d(sa + s * A_BYTES, &ta, kb * BK, m_tile * BM, b, &full[s]);
-        tc::tma_load_3d(sb + s * B_BYTES, &tb, kb * BK, n_tile * BN, b, &full[s]);
-        issued = kb + 1;
       }
-      if (*abort_flag) {
-        for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb)
-          mbar_wait_bounded(&full[kb % STAGES],
-                            static_cast<uint32_t>(kb / STAGES) & 1u, nullptr);
+      if (!ok) {
+        // Let the copies still in flight land before the CTA exits.
+        for (uint32_t i = (it > STAGES ? it - STAGES : 0); i < it; ++i)
+          mbar_wait_bounded(&full[i % STAGES], (i / STAGES) & 1u, nullptr);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(BM, BN);
-      for (int kb = 0; kb < KB; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
-        if (!mbar_wait_bounded(&full[s], ph, abort_flag)) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(BM, BN, A_MN, B_MN);
+      uint32_t it = 0, acc = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x, ++acc) {
+        const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
+        if (!mbar_wait_bounded(&tempty[buf], aph ^ 1u, abort_flag)) {
           raise_status(status, GBSGMC_ERR_TIMEOUT);
           *abort_flag = 1;
           break;
         }
         tc::fence_after_sync();
-        const uint64_t a0 = tc::sdesc_k_sw128(sa + s * A_BYTES);
-        const uint64_t b0 = tc::sdesc_k_sw128(sb + s * B_BYTES);
+        const uint32_t d = tmem + buf * BN;
+        for (int kb = 0; kb < KB; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1u;
+          if (!mbar_wait_bounded(&full[s], ph, abort_flag)) {
+            raise_status(status, GBSGMC_ERR_TIMEOUT);
+            *abort_flag = 1;
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint64_t a0 = A_MN ? tc::sdesc_mn_sw128(sa + s * A_BYTES, BLOCK_BYTES)
+                                   : tc::sdesc_k_sw128(sa + s * A_BYTES);
+          const uint64_t b0 = B_MN ? tc::sdesc_mn_sw128(sb + s * B_BYTES, BLOCK_BYTES)
+                                   : tc::sdesc_k_sw128(sb + s * B_BYTES);
 #pragma unroll
-        for (int k = 0; k < BK / 16; ++k)
-          tc::mma_bf16(tmem, a0 + 2 * k, b0 + 2 * k, idesc, (kb | k) != 0);
-        tc::mma_commit(&empty[s]);
+          for (int k = 0; k < BK / 16; ++k) {
+            // K=16 advances 32 bytes along a K-major row, or two 8-row
+            // groups (2048 bytes) of an MN-major tile; descriptors count 16 B.
+            const uint64_t da = A_MN ? 128u * k : 2u * k;
+            const uint64_t db = B_MN ? 128u * k : 2u * k;
+            tc::mma_bf16(d, a0 + da, b0 + db, idesc, (kb | k) != 0);
+          }
+          tc::mma_commit(&empty[s]);
+        }
+        if (ok) tc::mma_commit(&tfull[buf]);
       }
-      // Signals the epilogue; also lets every issued MMA finish on abort.
-      tc::mma_commit(accum);
-      if (*abort_flag) mbar_wait_bounded(accum, 0, nullptr);
+      // Every MMA issued by this CTA has completed once `drain` flips.
+      tc::mma_commit(drain);
+      mbar_wait_bounded(drain, 0, nullptr);
     }
   } else {
+    constexpr int NC = BN / kGemmSplit;
     const int q = warp & 3;  // TMEM lane quarter this warp may access
-    const bool ok = mbar_wait_bounded(accum, 0, abort_flag);
-    if (!ok && lane == 0) {
-      raise_status(status, GBSGMC_ERR_TIMEOUT);
-      *abort_flag = 1;
-    }
-    if (__all_sync(0xffffffffu, ok)) {
+    const int h = (warp - 2) >> 2;
+    uint32_t* stage = stage_all + (warp - 2) * kStageWords;
+    uint32_t acc = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++acc) {
+      const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
+      const bool ok = mbar_wait_bounded(&tfull[buf], aph, abort_flag);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0 && !*abort_flag) {
+          raise_status(status, GBSGMC_ERR_TIMEOUT);
+          *abort_flag = 1;
+        }
+        break;
+      }
       tc::fence_after_sync();
-      const int row = m_tile * BM + q * 32 + lane;
-      const uint32_t tbase = tmem + (static_cast<uint32_t>(q * 32) << 16);
-      auto load = [tbase](int c, float(&v)[16]) {
-        tc::tmem_ld16(tbase + static_cast<uint32_t>(c * 16), v);
+      const int b = t / per_batch, r = t - b * per_batch;
+      const int row0 = (r / tiles_n) * BM + q * 32;
+      const uint32_t tbase =
+          tmem + buf * BN + h * NC + (static_cast<uint32_t>(q * 32) << 16);
+      auto load = [tbase](int c, float(&v)[32]) {
+        tc::tmem_ld32(tbase + static_cast<uint32_t>(c * 32), v);
       };
-      epi.template tile<BN>(b, row, n_tile * BN, load);
+      epi.template tile<NC>(b, row0, (r % tiles_n) * BN + h * NC, load, stage);
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[buf]);
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 1) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tmem, BN);
+    tc::tmem_dealloc(tmem, TMEM_COLS);
   }
 }
 
-template <int BN, class Epi>
+// Launches the persistent GEMM on `st`: one CTA per resident slot (at most
+// one per output tile).  ta / tb: tensor maps made by make_tmap_bf16_3d with
+// boxes of 64 x 128 (A, K-major), 64 x BN (B, K-major) or 64 x 64 (MN-major).
+template <int BN, bool A_MN, bool B_MN, class Epi>
 int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, int batch, int M,
                 int N, int K, int* status, const Epi& epi, cudaStream_t st) {
+  auto kern = tc_gemm_kernel<BN, A_MN, B_MN, Epi>;
   const size_t smem = gemm_smem_bytes(BN);
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(
-        tc_gemm_kernel<BN, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        static_cast<int>(smem));
-    if (e != cudaSuccess)
-      return set_error(GBSGMC_ERR_CUDA, "gemm: cudaFuncSetAttribute: %s",
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kGemmThreads, smem);
+    if (e != cudaSuccess || per_sm < 1)
+      return set_error(GBSGMC_ERR_CUDA, "gemm: cannot configure the kernel: %s",
                        cudaGetErrorString(e));
-    attr = true;
   }
-  dim3 grid(N / BN, M / kGemmBM, batch);
-  tc_gemm_kernel<BN, Epi><<<grid, kGemmThreads, smem, st>>>(ta, tb, K, status, epi);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return set_error(GBSGMC_ERR_CUDA, "gemm: cannot query the device");
+  const int64_t tiles = static_cast<int64_t>(M / kGemmBM) * (N / BN) * batch;
+  const int grid = static_cast<int>(tiles < int64_t(sms) * per_sm ? tiles : int64_t(sms) * per_sm);
+  kern<<<grid, kGemmThreads, smem, st>>>(ta, tb, M, N, K, batch, status, epi);
   return check_launch("tc_gemm_kernel");
 }
 

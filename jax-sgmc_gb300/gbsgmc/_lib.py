@@ -136,6 +136,8 @@ SIGNATURES = {
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
     "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i)]),
     "gbsgmc_plan_destroy": (_i, [_vp]),
+    "gbsgmc_gemm_bf16": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64, _vp,
+                              _i64, _i64, _i, _i, _i, _i, _vp, _vp]),
     "gbsgmc_gemm_bf16_nt": (_i, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64,
                                  _i64, _i, _i, _i, _i, _vp, _vp]),
     "gbsgmc_plain_buffer_bytes": (_sz, [_i, _i]),

@@ -100,6 +100,7 @@ def check(lik, r, ref, W, X, y, idx, n_obs, mask=None, T=1.0):
 
 @pytest.mark.parametrize("shape", [(64, 256, 256, 2000, 3, 128),
                                    (128, 512, 256, 3000, 2, 256),
+                                   (64, 256, 2304, 700, 1, 128),
                                    (64, 1024, 1024, 8192, 2, 2048)])
 def test_mlp_matches_oracle(lib, shape):
   D, H1, H2, N, C, n = shape

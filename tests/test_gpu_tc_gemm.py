@@ -33,8 +33,38 @@ def test_gemm_matches_torch(lib, batch, M, N, K):
   assert bool((err <= 1e-3 * bound + 1e-4).all()), float((err / (bound + 1e-6)).max())
 
 
+@pytest.mark.parametrize("a_mn,b_mn", [(0, 1), (1, 0), (1, 1), (0, 0)])
+@pytest.mark.parametrize("batch,M,N,K", [(1, 128, 128, 64), (2, 256, 256, 128),
+                                         (3, 384, 512, 1024), (2, 128, 384, 320),
+                                         (1, 1024, 1024, 2048)])
+def test_gemm_operand_layouts(lib, a_mn, b_mn, batch, M, N, K):
+  """MN-major ("transposed") operands: A stored K x M, B stored K x N."""
+  import torch
+  from gbsgmc import _lib
+  g = torch.Generator(device="cuda").manual_seed(7 * M + N + K + 2 * a_mn + b_mn)
+  A = torch.randn((batch, M, K), generator=g, device="cuda").to(torch.bfloat16)
+  B = torch.randn((batch, N, K), generator=g, device="cuda").to(torch.bfloat16)
+  As = A.transpose(1, 2).contiguous() if a_mn else A
+  Bs = B.transpose(1, 2).contiguous() if b_mn else B
+  C = torch.full((batch, M, N), float("nan"), device="cuda")
+  status = torch.zeros(1, dtype=torch.int32, device="cuda")
+  _lib.call("gbsgmc_gemm_bf16", a_mn, b_mn, As.data_ptr(), M if a_mn else K,
+            M * K, Bs.data_ptr(), N if b_mn else K, N * K, C.data_ptr(), N,
+            M * N, batch, M, N, K, status.data_ptr(), _lib.stream_handle())
+  torch.cuda.synchronize()
+  assert int(status.item()) == 0
+  ref = torch.bmm(A.float(), B.float().transpose(1, 2))
+  bound = torch.bmm(A.float().abs(), B.float().abs().transpose(1, 2))
+  err = (C - ref).abs()
+  assert torch.isfinite(C).all()
+  assert bool((err <= 1e-3 * bound + 1e-4).all()), float((err / (bound + 1e-6)).max())
+
+
 def test_gemm_rejects_unsupported_shapes(lib):
   from gbsgmc import _lib
   rc = lib.gbsgmc_gemm_bf16_nt(16, 64, 0, 16, 64, 0, 16, 100, 0, 1, 100, 128, 64,
-                               None, None)
+                               16, None)
   assert rc == _lib.ERR_SHAPE
+  rc = lib.gbsgmc_gemm_bf16(1, 0, 16, 64, 0, 16, 64, 0, 16, 128, 0, 1, 128, 128,
+                            64, None, None)
+  assert rc == _lib.ERR_ARG
