@@ -409,6 +409,42 @@ int gbsgmc_sgld_glm_plan_create(gbsgmc_plan** plan, const gbsgmc_glm* model,
                                 float* samples_dev, double* sample_lik_dev,
                                 int block_steps, int* status_dev);
 
+/* Integrator of a network plan. */
+#define GBSGMC_INTEGRATOR_SGLD 0  /* langevin_diffusion, rms_prop when aux != NULL */
+#define GBSGMC_INTEGRATOR_OBABO 1 /* obabo: two minibatches per step             */
+#define GBSGMC_INTEGRATOR_SGHMC 2 /* friction_leapfrog: one minibatch per step   */
+
+typedef struct gbsgmc_integrator {
+  int kind;
+  int leapfrog_steps; /* SGHMC: steps between momentum resamples (>= 1)     */
+  float friction;     /* OBABO and SGHMC                                    */
+  float alpha, lmbd;  /* rms_prop of SGLD                                   */
+  int _pad;
+  const float* mass_dev; /* diagonal mass [P] or NULL (identity)            */
+} gbsgmc_integrator;
+
+/* Builds a plan that runs `chains` chains of an integrator on the dense
+ * network: per step the index draw(s), gbsgmc_mlp_value_and_grad over all
+ * chains and the integrator's elementwise update(s), `block_steps` steps per
+ * captured CUDA graph.  x_dev [chains, P] holds the positions; aux_dev the
+ * rms_prop state (SGLD, may be NULL) or the momentum (OBABO, SGHMC; the
+ * caller initialises it).  After each step U_dev [chains] holds the
+ * potential (OBABO: the mean of its two evaluations), lk_var_dev [chains]
+ * (may be NULL) the variance of the last evaluation's lk, and ke_dev
+ * [2 * chains] (OBABO, may be NULL) accumulates the kinetic energies after
+ * the first and before the last quarter step.  For SGHMC the momentum is
+ * resampled every leapfrog_steps steps, so plan_run's first step and step
+ * count must be multiples of it.  Replaces solver.mcmc's scan
+ * (jax_sgmc/solver.py:152-185) over alias.sgld / obabo / sghmc
+ * (jax_sgmc/alias.py) for this likelihood. */
+int gbsgmc_mlp_plan_create(gbsgmc_plan** plan, const gbsgmc_mlp* model,
+                           int chains, int n, const gbsgmc_integrator* integrator,
+                           float* x_dev, float* aux_dev,
+                           const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                           const gbsgmc_index_src* index_src, double* U_dev,
+                           double* lk_var_dev, double* ke_dev, int block_steps,
+                           int* status_dev);
+
 /* Runs steps [first_step, first_step + steps) of the plan, ordered after prior
  * work on `stream`; later work on `stream` waits for it.  Does not block the
  * host. */

@@ -1,0 +1,214 @@
+// Plans over the network likelihoods: many chains of SGLD(+RMSprop), OBABO
+// or SGHMC stepped together, one CUDA graph per block of steps.
+//
+// Per step: index draw(s) for all chains (one per minibatch the integrator
+// consumes), the batched value-and-gradient of the network over all chains,
+// and the integrator's elementwise kernels over [chains, P].  The integrator
+// kernels read their step index from the plan's device counter, so the Philox
+// noise of step k is the same whether the step runs inside a graph or alone.
+#include <functional>
+#include <new>
+
+#include "common.cuh"
+#include "internal.h"
+#include "plan.cuh"
+
+namespace gbsgmc {
+namespace {
+
+__global__ void mean_pair_kernel(int chains, double* a, const double* b) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < chains) a[c] = 0.5 * (a[c] + b[c]);
+}
+
+// Value and gradient over all chains: (idx, idx_stride, U, lk_var, stream).
+using GradFn = std::function<int(const int32_t*, int64_t, double*, double*, cudaStream_t)>;
+
+struct NetPlan final : gbsgmc_plan {
+  GradFn grad_fn;
+  int chains = 0, n = 0;
+  int64_t P = 0, rows = 0;
+  gbsgmc_integrator integ{};
+  float* x = nullptr;
+  float* aux = nullptr;
+  float* grad = nullptr;  // owned [chains, P]
+  gbsgmc_sched sched{};
+  gbsgmc_noise noise{};
+  gbsgmc_index_src isrc{};
+  double* U = nullptr;
+  double* U2 = nullptr;   // owned (OBABO)
+  double* lk_var = nullptr;
+  double* ke = nullptr;
+  int* status = nullptr;
+  int32_t* idx = nullptr;  // owned [G, chains, draws * n]
+  void* ws = nullptr;      // owned
+  size_t ws_size = 0;
+
+  int draws() const { return integ.kind == GBSGMC_INTEGRATOR_OBABO ? 2 : 1; }
+
+  ~NetPlan() override {
+    if (stream != nullptr) cudaStreamSynchronize(stream);
+    cudaFree(grad);
+    cudaFree(U2);
+    cudaFree(idx);
+    cudaFree(ws);
+  }
+
+  int step_multiple() const override {
+    return integ.kind == GBSGMC_INTEGRATOR_SGHMC ? integ.leapfrog_steps : 1;
+  }
+
+  int64_t launches_per_block(int g) const override {
+    // Kernels of one value-and-gradient call are counted by the caller.
+    switch (integ.kind) {
+      case GBSGMC_INTEGRATOR_OBABO: return 2 + 3 * static_cast<int64_t>(g);
+      case GBSGMC_INTEGRATOR_SGHMC:
+        return 2 + 2 * static_cast<int64_t>(g) + g / integ.leapfrog_steps;
+      default: return 2 + static_cast<int64_t>(g);
+    }
+  }
+
+  int enqueue(int g, cudaStream_t s) override {
+    const int per = draws() * n;
+    const int64_t cn = static_cast<int64_t>(chains) * per;
+    int rc;
+    if (isrc.pcg_dev != nullptr) {
+      rc = gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows, static_cast<int64_t>(g) * per,
+                                   per, idx, per, cn, status, s);
+    } else {
+      rc = launch_philox_index(isrc.index_seed, isrc.chain_base, chains, base, 0, g, per,
+                               rows, idx, per, cn, s);
+    }
+    if (rc != GBSGMC_OK) return rc;
+    double* ke_start = ke;
+    double* ke_end = ke != nullptr ? ke + chains : nullptr;
+    for (int j = 0; j < g; ++j) {
+      gbsgmc_sched sj = sched;
+      sj.base_dev = base;
+      sj.offset = j;
+      const int32_t* ij = idx + j * cn;
+      switch (integ.kind) {
+        case GBSGMC_INTEGRATOR_SGLD:
+          if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+          rc = gbsgmc_sgld_update(chains, P, x, grad, aux, integ.alpha, integ.lmbd, &sj,
+                                  &noise, nullptr, s);
+          break;
+        case GBSGMC_INTEGRATOR_OBABO:
+          if ((rc = grad_fn(ij, per, U, nullptr, s))) return rc;
+          if ((rc = gbsgmc_obabo_first(chains, P, x, aux, grad, integ.mass_dev, integ.friction,
+                                       ke_start, &sj, &noise, s)))
+            return rc;
+          if ((rc = grad_fn(ij + n, per, U2, lk_var, s))) return rc;
+          if ((rc = gbsgmc_obabo_second(chains, P, aux, grad, integ.mass_dev, integ.friction,
+                                        ke_end, &sj, &noise, s)))
+            return rc;
+          mean_pair_kernel<<<(chains + 127) / 128, 128, 0, s>>>(chains, U, U2);
+          rc = check_launch("plan: potential mean");
+          break;
+        default:  // SGHMC
+          if (j % integ.leapfrog_steps == 0 &&
+              (rc = gbsgmc_sghmc_resample(chains, P, aux, integ.mass_dev, &sj, &noise, s)))
+            return rc;
+          if ((rc = gbsgmc_sghmc_position(chains, P, x, aux, integ.mass_dev, nullptr,
+                                          integ.friction, &sj, s)))
+            return rc;
+          if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+          rc = gbsgmc_sghmc_momentum(chains, P, aux, grad, nullptr, integ.friction, &sj,
+                                     &noise, s);
+          break;
+      }
+      if (rc != GBSGMC_OK) return rc;
+    }
+    return plan_advance(this, g, s);
+  }
+};
+
+int check_common(const gbsgmc_integrator* integ, int chains, int n, float* x, float* aux,
+                 const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                 const gbsgmc_index_src* isrc, double* U, int block_steps, int* status) {
+  if (integ == nullptr || x == nullptr || sched == nullptr || noise == nullptr ||
+      isrc == nullptr || U == nullptr || status == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "net plan: null argument");
+  if (chains <= 0 || n <= 0 || block_steps <= 0 || block_steps > 100000)
+    return set_error(GBSGMC_ERR_ARG, "net plan: bad chains/n/block_steps");
+  if (integ->kind < GBSGMC_INTEGRATOR_SGLD || integ->kind > GBSGMC_INTEGRATOR_SGHMC)
+    return set_error(GBSGMC_ERR_ARG, "net plan: unknown integrator %d", integ->kind);
+  if (integ->kind != GBSGMC_INTEGRATOR_SGLD && aux == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "net plan: OBABO and SGHMC need a momentum buffer");
+  if (integ->kind == GBSGMC_INTEGRATOR_SGHMC &&
+      (integ->leapfrog_steps < 1 || block_steps % integ->leapfrog_steps != 0))
+    return set_error(GBSGMC_ERR_ARG,
+                     "net plan: block_steps must be a multiple of leapfrog_steps");
+  if (sched->keep_slot_dev != nullptr)
+    return set_error(GBSGMC_ERR_UNSUPPORTED,
+                     "net plan: samples are collected by the caller between runs");
+  return GBSGMC_OK;
+}
+
+}  // namespace
+}  // namespace gbsgmc
+
+using namespace gbsgmc;
+
+extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model,
+                                      int chains, int n, const gbsgmc_integrator* integ,
+                                      float* x_dev, float* aux_dev,
+                                      const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                                      const gbsgmc_index_src* isrc, double* U_dev,
+                                      double* lk_var_dev, double* ke_dev, int block_steps,
+                                      int* status_dev) {
+  if (out == nullptr) return set_error(GBSGMC_ERR_ARG, "mlp_plan_create: null plan");
+  *out = nullptr;
+  int rc = check_common(integ, chains, n, x_dev, aux_dev, sched, noise, isrc, U_dev,
+                        block_steps, status_dev);
+  if (rc != GBSGMC_OK) return rc;
+  if (model == nullptr) return set_error(GBSGMC_ERR_ARG, "mlp_plan_create: null model");
+  const size_t ws = gbsgmc_mlp_workspace_bytes(model, chains, n);
+  if (ws == 0)
+    return set_error(GBSGMC_ERR_SHAPE, "mlp_plan_create: unsupported shape (n %% 128)");
+  NetPlan* p = new (std::nothrow) NetPlan();
+  if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "mlp_plan_create: out of memory");
+  p->chains = chains;
+  p->n = n;
+  p->P = gbsgmc_mlp_param_count(model);
+  p->rows = model->n_rows > 0 ? model->n_rows : model->n_obs;
+  p->integ = *integ;
+  p->x = x_dev;
+  p->aux = aux_dev;
+  p->sched = *sched;
+  p->noise = *noise;
+  p->isrc = *isrc;
+  p->U = U_dev;
+  p->lk_var = lk_var_dev;
+  p->ke = ke_dev;
+  p->status = status_dev;
+  p->ws_size = ws;
+  do {
+    if ((rc = plan_init(p, block_steps))) break;
+    const size_t gbytes = sizeof(float) * static_cast<size_t>(chains) * p->P;
+    const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
+                          p->draws() * n;
+    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "mlp_plan_create: gradient"))) break;
+    if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "mlp_plan_create: U")))
+      break;
+    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "mlp_plan_create: index buffer"))) break;
+    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "mlp_plan_create: workspace"))) break;
+    const gbsgmc_mlp m = *model;
+    float* grad = p->grad;
+    void* wsp = p->ws;
+    const float* x = x_dev;
+    p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
+                     const int32_t* idx, int64_t stride, double* U, double* var,
+                     cudaStream_t s) {
+      return gbsgmc_mlp_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
+                                       nullptr, var, wsp, ws, status_dev, s);
+    };
+    rc = plan_capture(p);
+  } while (false);
+  if (rc != GBSGMC_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return GBSGMC_OK;
+}

@@ -1,13 +1,13 @@
-// Plans: the multi-step driver of the SGLD hot path.
+// Plans: the multi-step driver of the SGLD hot path on the GLM families, and
+// the plan machinery shared with the network plans (plan.cuh).
 //
-// A plan owns an internal non-blocking stream, the fused-step workspace, an
-// index buffer for one block of steps and a device step counter.  One block
-// of G steps is: index draw for G steps (numpy PCG64 streams, or Philox),
-// G fused SGLD launches whose step index is read from the device counter
-// (k = counter + j), and a one-thread launch that advances the counter by G.
-// The block is captured once into a CUDA graph and replayed, so a run of K
-// steps costs K/G graph launches on the host.  The schedule tables (step
-// size, temperature, keep slots) are read on the device at step k.
+// One block of G GLM steps is: index draw for G steps (numpy PCG64 streams,
+// or Philox), G fused SGLD launches whose step index is read from the device
+// counter (k = counter + j), and a one-thread launch that advances the
+// counter by G.  The block is captured once into a CUDA graph and replayed,
+// so a run of K steps costs K/G graph launches on the host.  The schedule
+// tables (step size, temperature, keep slots) are read on the device at
+// step k.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -19,8 +19,20 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "plan.cuh"
 
-struct gbsgmc_plan {
+gbsgmc_plan::~gbsgmc_plan() {
+  if (stream != nullptr) cudaStreamSynchronize(stream);
+  if (exec != nullptr) cudaGraphExecDestroy(exec);
+  if (base != nullptr) cudaFree(base);
+  if (ev_in != nullptr) cudaEventDestroy(ev_in);
+  if (ev_out != nullptr) cudaEventDestroy(ev_out);
+  if (stream != nullptr) cudaStreamDestroy(stream);
+}
+
+namespace {
+
+struct GlmPlan final : gbsgmc_plan {
   gbsgmc_glm model;
   int chains, n;
   float* w;
@@ -34,31 +46,87 @@ struct gbsgmc_plan {
   float* samples;
   double* sample_lik;
   int* status;
-  int G;
   gbsgmc::GlmTune tune;
-  bool use_graph;
-  cudaStream_t stream;
-  void* ws;
-  size_t ws_size;
-  int32_t* idx;
-  int64_t* base;
-  cudaGraphExec_t exec;
-  cudaEvent_t ev_in, ev_out;
+  void* ws = nullptr;
+  size_t ws_size = 0;
+  int32_t* idx = nullptr;
+
+  ~GlmPlan() override {
+    if (stream != nullptr) cudaStreamSynchronize(stream);
+    if (ws != nullptr) cudaFree(ws);
+    if (idx != nullptr) cudaFree(idx);
+  }
+  int enqueue(int g, cudaStream_t s) override;
+  int64_t launches_per_block(int g) const override { return g + 2; }
 };
 
-namespace gbsgmc {
-namespace {
+}  // namespace
 
+namespace gbsgmc {
+
+namespace {
 __global__ void set_counter_kernel(int64_t* c, int64_t v) { *c = v; }
 __global__ void advance_counter_kernel(int64_t* c, int64_t by) { *c += by; }
+}  // namespace
 
 int cuda_err(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return GBSGMC_OK;
   return set_error(GBSGMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-int enqueue_block(gbsgmc_plan* p, int g, cudaStream_t s) {
+int plan_init(gbsgmc_plan* p, int G) {
+  p->G = G;
+  const char* env = std::getenv("GBSGMC_NO_GRAPH");
+  p->use_graph = !(env != nullptr && env[0] == '1');
   int rc;
+  if ((rc = cuda_err(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking),
+                     "plan: stream")))
+    return rc;
+  if ((rc = cuda_err(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming),
+                     "plan: event")))
+    return rc;
+  if ((rc = cuda_err(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming),
+                     "plan: event")))
+    return rc;
+  if ((rc = cuda_err(cudaMalloc(&p->base, sizeof(int64_t)), "plan: counter"))) return rc;
+  return cuda_err(cudaMemsetAsync(p->base, 0, sizeof(int64_t), p->stream), "plan: memset");
+}
+
+int plan_capture(gbsgmc_plan* p) {
+  int rc = GBSGMC_OK;
+  if (p->use_graph) {
+    if ((rc = cuda_err(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal),
+                       "plan: begin capture")))
+      return rc;
+    rc = p->enqueue(p->G, p->stream);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(p->stream, &graph);
+    if (rc != GBSGMC_OK) {
+      if (graph != nullptr) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if ((rc = cuda_err(e, "plan: end capture"))) return rc;
+    rc = cuda_err(cudaGraphInstantiate(&p->exec, graph, 0), "plan: instantiate");
+    cudaGraphDestroy(graph);
+    if (rc) return rc;
+  }
+  return cuda_err(cudaStreamSynchronize(p->stream), "plan: sync");
+}
+
+int plan_advance(gbsgmc_plan* p, int g, cudaStream_t s) {
+  advance_counter_kernel<<<1, 1, 0, s>>>(p->base, g);
+  return check_launch("plan: advance counter");
+}
+
+namespace {
+
+}  // namespace
+}  // namespace gbsgmc
+
+int GlmPlan::enqueue(int g, cudaStream_t s) {
+  using namespace gbsgmc;
+  int rc;
+  GlmPlan* p = this;
   const int64_t cn = static_cast<int64_t>(p->chains) * p->n;
   const int64_t rows = p->model.n_rows > 0 ? p->model.n_rows : p->model.n_obs;
   if (p->isrc.pcg_dev != nullptr) {
@@ -81,15 +149,17 @@ int enqueue_block(gbsgmc_plan* p, int g, cudaStream_t s) {
                        p->status, s, p->tune);
     if (rc != GBSGMC_OK) return rc;
   }
-  advance_counter_kernel<<<1, 1, 0, s>>>(p->base, g);
-  return check_launch("plan: advance counter");
+  return plan_advance(p, g, s);
 }
+
+namespace gbsgmc {
+namespace {
 
 // Autotuner: times candidate launch shapes of the fused step (CTAs per chain
 // and rows per warp) on scratch copies of the chain state and keeps the
 // fastest.  The choice is cached per problem shape for the process, and
 // direct step launches of that shape use it too.
-int autotune(gbsgmc_plan* p) {
+int autotune(GlmPlan* p) {
   const char* env = std::getenv("GBSGMC_AUTOTUNE");
   if (env != nullptr && env[0] == '0') return GBSGMC_OK;
   if (glm_tune_lookup(p->chains, p->n, p->model.d, p->model.ld, &p->tune))
@@ -188,19 +258,6 @@ int autotune(gbsgmc_plan* p) {
   return rc;
 }
 
-void release(gbsgmc_plan* p) {
-  if (p == nullptr) return;
-  if (p->stream != nullptr) cudaStreamSynchronize(p->stream);
-  if (p->exec != nullptr) cudaGraphExecDestroy(p->exec);
-  if (p->ws != nullptr) cudaFree(p->ws);
-  if (p->idx != nullptr) cudaFree(p->idx);
-  if (p->base != nullptr) cudaFree(p->base);
-  if (p->ev_in != nullptr) cudaEventDestroy(p->ev_in);
-  if (p->ev_out != nullptr) cudaEventDestroy(p->ev_out);
-  if (p->stream != nullptr) cudaStreamDestroy(p->stream);
-  delete p;
-}
-
 }  // namespace
 }  // namespace gbsgmc
 
@@ -222,7 +279,7 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
   if (sched->keep_slot_dev != nullptr && samples_dev == nullptr)
     return set_error(GBSGMC_ERR_ARG,
                      "plan_create: keep table given without sample buffer");
-  gbsgmc_plan* p = new (std::nothrow) gbsgmc_plan();
+  GlmPlan* p = new (std::nothrow) GlmPlan();
   if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "plan_create: out of memory");
   p->model = *model;
   p->chains = chains;
@@ -239,20 +296,9 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
   p->samples = samples_dev;
   p->sample_lik = sample_lik_dev;
   p->status = status_dev;
-  p->G = block_steps;
-  const char* env = std::getenv("GBSGMC_NO_GRAPH");
-  p->use_graph = !(env != nullptr && env[0] == '1');
   int rc = GBSGMC_OK;
   do {
-    if ((rc = cuda_err(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking),
-                       "plan_create: stream")))
-      break;
-    if ((rc = cuda_err(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming),
-                       "plan_create: event")))
-      break;
-    if ((rc = cuda_err(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming),
-                       "plan_create: event")))
-      break;
+    if ((rc = plan_init(p, block_steps))) break;
     p->ws_size = glm_ws_bytes(chains, n, model->d);
     if ((rc = cuda_err(cudaMalloc(&p->ws, p->ws_size), "plan_create: workspace")))
       break;
@@ -260,38 +306,15 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
                                                    block_steps) * chains * n),
                        "plan_create: index buffer")))
       break;
-    if ((rc = cuda_err(cudaMalloc(&p->base, sizeof(int64_t)), "plan_create: counter")))
-      break;
     if ((rc = cuda_err(cudaMemsetAsync(p->ws, 0, p->ws_size, p->stream),
-                       "plan_create: memset")))
-      break;
-    if ((rc = cuda_err(cudaMemsetAsync(p->base, 0, sizeof(int64_t), p->stream),
                        "plan_create: memset")))
       break;
     if ((rc = glm_prepare())) break;
     if ((rc = autotune(p))) break;
-    if (p->use_graph) {
-      if ((rc = cuda_err(cudaStreamBeginCapture(p->stream,
-                                                cudaStreamCaptureModeThreadLocal),
-                         "plan_create: begin capture")))
-        break;
-      rc = enqueue_block(p, p->G, p->stream);
-      cudaGraph_t graph = nullptr;
-      const cudaError_t e = cudaStreamEndCapture(p->stream, &graph);
-      if (rc != GBSGMC_OK) {
-        if (graph != nullptr) cudaGraphDestroy(graph);
-        break;
-      }
-      if ((rc = cuda_err(e, "plan_create: end capture"))) break;
-      rc = cuda_err(cudaGraphInstantiate(&p->exec, graph, 0),
-                    "plan_create: instantiate");
-      cudaGraphDestroy(graph);
-      if (rc) break;
-    }
-    rc = cuda_err(cudaStreamSynchronize(p->stream), "plan_create: sync");
+    rc = plan_capture(p);
   } while (false);
   if (rc != GBSGMC_OK) {
-    release(p);
+    delete p;
     return rc;
   }
   *out = p;
@@ -303,6 +326,10 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
   if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "plan_run: null plan");
   if (first_step < 0 || steps < 0)
     return set_error(GBSGMC_ERR_ARG, "plan_run: negative step");
+  const int m = p->step_multiple();
+  if (first_step % m != 0 || steps % m != 0)
+    return set_error(GBSGMC_ERR_ARG,
+                     "plan_run: first_step and steps must be multiples of %d", m);
   if (steps == 0) return GBSGMC_OK;
   cudaStream_t us = static_cast<cudaStream_t>(stream);
   int rc;
@@ -317,11 +344,11 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
     if (p->use_graph) {
       if ((rc = cuda_err(cudaGraphLaunch(p->exec, p->stream), "plan_run: graph")))
         return rc;
-    } else if ((rc = enqueue_block(p, p->G, p->stream))) {
+    } else if ((rc = p->enqueue(p->G, p->stream))) {
       return rc;
     }
   }
-  if (rem > 0 && (rc = enqueue_block(p, rem, p->stream))) return rc;
+  if (rem > 0 && (rc = p->enqueue(rem, p->stream))) return rc;
   if ((rc = cuda_err(cudaEventRecord(p->ev_out, p->stream), "plan_run: record")))
     return rc;
   return cuda_err(cudaStreamWaitEvent(us, p->ev_out, 0), "plan_run: wait");
@@ -332,9 +359,12 @@ extern "C" int gbsgmc_plan_launch_shape(const gbsgmc_plan* p, int* slices,
   if (p == nullptr || slices == nullptr || rows_per_warp == nullptr ||
       warps == nullptr)
     return set_error(GBSGMC_ERR_ARG, "plan_launch_shape: null argument");
-  *slices = p->tune.slices;
-  *rows_per_warp = p->tune.rows_per_warp;
-  *warps = p->tune.warps;
+  *slices = *rows_per_warp = *warps = 0;
+  if (const GlmPlan* g = dynamic_cast<const GlmPlan*>(p)) {
+    *slices = g->tune.slices;
+    *rows_per_warp = g->tune.rows_per_warp;
+    *warps = g->tune.warps;
+  }
   return GBSGMC_OK;
 }
 
@@ -342,10 +372,11 @@ extern "C" int64_t gbsgmc_plan_launches(const gbsgmc_plan* p, int64_t steps) {
   if (p == nullptr || steps <= 0) return 0;
   const int64_t full = steps / p->G;
   const int64_t rem = steps % p->G;
-  return 1 + full * (p->G + 2) + (rem > 0 ? rem + 2 : 0);
+  return 1 + full * p->launches_per_block(p->G) +
+         (rem > 0 ? p->launches_per_block(static_cast<int>(rem)) : 0);
 }
 
 extern "C" int gbsgmc_plan_destroy(gbsgmc_plan* p) {
-  release(p);
+  delete p;
   return GBSGMC_OK;
 }

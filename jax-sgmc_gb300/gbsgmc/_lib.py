@@ -65,6 +65,16 @@ class Mlp(C.Structure):
               ("_reserved", C.c_int)]
 
 
+class Integrator(C.Structure):
+  _fields_ = [("kind", C.c_int), ("leapfrog_steps", C.c_int),
+              ("friction", C.c_float), ("alpha", C.c_float),
+              ("lmbd", C.c_float), ("_pad", C.c_int),
+              ("mass_dev", C.c_void_p)]
+
+
+INTEGRATOR_SGLD, INTEGRATOR_OBABO, INTEGRATOR_SGHMC = 0, 1, 2
+
+
 class Sched(C.Structure):
   _fields_ = [("step_size_dev", C.c_void_p), ("temperature_dev", C.c_void_p),
               ("base_dev", C.c_void_p), ("keep_slot_dev", C.c_void_p),
@@ -132,6 +142,9 @@ SIGNATURES = {
                                          _f, _f, _P(Sched), _P(Noise),
                                          _P(IndexSrc), _vp, _vp, _vp, _vp, _i,
                                          _vp]),
+    "gbsgmc_mlp_plan_create": (_i, [_P(_vp), _P(Mlp), _i, _i, _P(Integrator),
+                                    _vp, _vp, _P(Sched), _P(Noise),
+                                    _P(IndexSrc), _vp, _vp, _vp, _i, _vp]),
     "gbsgmc_plan_run": (_i, [_vp, _i64, _i64, _vp]),
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
     "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i)]),

@@ -133,6 +133,158 @@ def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
     plan.close()
 
 
+class NetPlan:
+  """Owns a network plan (``gbsgmc_mlp_plan_create``): C chains of SGLD,
+  OBABO or SGHMC on a dense-network potential, one CUDA graph per block of
+  steps.  ``X`` [C, P] (positions) and ``AUX`` (rms_prop state, or momentum)
+  are updated in place."""
+
+  KINDS = {"langevin": _lib.INTEGRATOR_SGLD, "obabo": _lib.INTEGRATOR_OBABO,
+           "sghmc": _lib.INTEGRATOR_SGHMC}
+
+  def __init__(self, potential, dataset, X, AUX, n, kind, h_tab, t_tab,
+               index_src, noise_seed, chain_base=0, block_steps=None,
+               friction=0.0, leapfrog_steps=1, alpha=0.9, lmbd=1e-5,
+               mass=None, observation_count=None):
+    import torch
+    C, P = X.shape
+    self.C, self.P, self.n, self.kind = C, P, n, kind
+    self.model, self._keep_alive = potential.model(dataset, observation_count)
+    self.X, self.AUX, self.mass = X, AUX, mass
+    self.U = torch.zeros(C, dtype=torch.float64, device="cuda")
+    self.lk_var = torch.zeros(C, dtype=torch.float64, device="cuda")
+    self.ke = torch.zeros(2 * C, dtype=torch.float64, device="cuda")
+    self.status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    self.h_tab, self.t_tab = h_tab, t_tab
+    self.index_src = index_src
+    self.sched = _lib.sched(step_size_dev=h_tab, temperature_dev=t_tab)
+    self.noise = _lib.noise(noise_seed, chain_base)
+    lf = int(leapfrog_steps) if kind == "sghmc" else 1
+    if block_steps is None:
+      block_steps = DEFAULT_BLOCK_STEPS
+    block_steps = max(lf, block_steps // lf * lf)
+    self.integ = _lib.Integrator(self.KINDS[kind], lf, float(friction),
+                                 float(alpha), float(lmbd), 0, _lib.ptr(mass))
+    handle = _lib.C.c_void_p()
+    _lib.call("gbsgmc_mlp_plan_create", _lib.C.byref(handle), self.model, C, n,
+              self.integ, _lib.ptr(X), _lib.ptr(AUX), self.sched, self.noise,
+              index_src.struct, _lib.ptr(self.U), _lib.ptr(self.lk_var),
+              _lib.ptr(self.ke), int(block_steps), _lib.ptr(self.status))
+    self.handle = handle
+
+  def run(self, first_step, steps):
+    _lib.call("gbsgmc_plan_run", self.handle, int(first_step), int(steps),
+              _lib.stream_handle())
+
+  def launches(self, steps) -> int:
+    """Kernel launches of ``steps`` steps (value-and-gradient kernels
+    included)."""
+    per_grad = 10 if self.kind != "langevin" else 10
+    grads = {"obabo": 2}.get(self.kind, 1) * int(steps)
+    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps))) + \
+        per_grad * grads
+
+  def check_status(self):
+    code = int(self.status.item())
+    if code != 0:
+      raise _lib.GbsgmcError(code, "device status of the network plan")
+
+  def close(self):
+    if getattr(self, "handle", None):
+      _lib.load().gbsgmc_plan_destroy(self.handle)
+      self.handle = None
+
+  def __del__(self):
+    try:
+      self.close()
+    except Exception:  # pragma: no cover - interpreter shutdown
+      pass
+
+
+def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
+  """Runs sgmc chains of langevin_diffusion / obabo / friction_leapfrog on a
+  dense-network potential through one :class:`NetPlan`; returns None when
+  the chains do not qualify (the caller steps them one by one)."""
+  import torch
+  from .potential import StochasticPotential
+  meta = getattr(solver, "meta", {})
+  if not FUSED_ENABLED or meta.get("kind") != "sgmc" or schedulers:
+    return None
+  integ = meta.get("integrator")
+  im = getattr(integ, "meta", {})
+  kind = im.get("kind")
+  if kind not in NetPlan.KINDS or im.get("noise_source") is not None:
+    return None
+  pot = im.get("potential")
+  bfn = im.get("batch_fn")
+  if not isinstance(pot, StochasticPotential) or not pot.is_mlp or not states:
+    return None
+  if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn):
+    return None
+  rbf = bfn[1]
+  if len({s.key for s in states}) != 1:
+    return None
+  chain_ids = [int(s.chain) for s in states]
+  if chain_ids != list(range(chain_ids[0], chain_ids[0] + len(states))):
+    return None
+  if rbf.kind != "host":
+    return None
+  ds_list = [s.data_state for s in states]
+  if any(d.state is None or d.cached_batches is not None for d in ds_list):
+    return None
+  steps = int(im.get("steps", 1)) if kind != "langevin" else 1
+  if kind == "langevin":
+    adapt = [s.adapt_state for s in states]
+    if any(a is None for a in adapt) and not all(a is None for a in adapt):
+      return None
+    X = torch.stack([s.latent_variables for s in states]).contiguous()
+    AUX = torch.stack([a.v for a in adapt]).contiguous() \
+        if adapt[0] is not None else None
+    kw = dict(alpha=adapt[0].alpha, lmbd=adapt[0].lmbd) \
+        if adapt[0] is not None else {}
+    if any(int(s.step) != 0 for s in states):
+      return None
+  else:
+    X = torch.stack([s.positions for s in states]).contiguous()
+    AUX = torch.stack([s.momentum for s in states]).contiguous()
+    if im.get("const_mass") is not None or not np.isscalar(im.get("friction")):
+      return None
+    kw = dict(friction=float(im["friction"]), leapfrog_steps=steps)
+    if any(int(s.step) != 0 for s in states):
+      return None
+  pcg = torch.stack([d.state for d in ds_list]).contiguous()
+  index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
+  dataset = rbf.loader.device_dataset()
+  h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
+  # One solver iteration is `steps` integrator steps with the same schedule.
+  h_tab = torch.from_numpy(np.repeat(np.asarray(h, np.float32), steps)).cuda()
+  t_tab = torch.from_numpy(np.repeat(np.asarray(t, np.float32), steps)).cuda()
+  plan = NetPlan(pot, dataset, X, AUX, rbf.mb_size, kind, h_tab, t_tab,
+                 index_src, states[0].key, chain_ids[0], **kw)
+  C = len(states)
+  samples = torch.empty((max(n_kept, 1), C, X.shape[1]), dtype=torch.float32,
+                        device="cuda")
+  extra = torch.empty((max(n_kept, 1), C), dtype=torch.float64, device="cuda")
+  try:
+    done = 0
+    for k in np.nonzero(np.asarray(keep) >= 0)[0]:
+      plan.run(done * steps, (k + 1 - done) * steps)
+      done = k + 1
+      samples[keep[k]] = X
+      extra[keep[k]] = -plan.U if kind == "langevin" else plan.U
+    if done < iterations:
+      plan.run(done * steps, (iterations - done) * steps)
+    plan.check_status()
+  finally:
+    plan.close()
+  for c, s in enumerate(states):   # the streams advanced on the device
+    s.data_state.state.copy_(pcg[c])
+  key = "likelihood" if kind == "langevin" else "energy"
+  return [io.postprocess(saving or io.no_save(), n_kept, samples[:n_kept, c],
+                         s.treedef, {key: extra[:n_kept, c]}, s.model_state)
+          for c, s in enumerate(states)]
+
+
 def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
   """Runs the chains through :func:`run_sgld_glm` when they qualify;
   returns None otherwise (the caller then steps chain by chain)."""
@@ -147,7 +299,7 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
     return None
   pot = im.get("potential")
   bfn = im.get("batch_fn")
-  if not isinstance(pot, StochasticPotential) or not states:
+  if not isinstance(pot, StochasticPotential) or pot.is_mlp or not states:
     return None
   if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn):
     return None

@@ -160,6 +160,9 @@ def mcmc(solver, scheduler, strategy="map", saving=None, loading=None):
     states = list(states)
     fused = engine.try_fused_sgld(solver, scheduler, states, schedulers,
                                   iterations, saving)
+    if fused is None:
+      fused = engine.try_fused_net(solver, scheduler, states, schedulers,
+                                   iterations, saving)
     if fused is not None:
       return fused
     return [run_single(s, iterations, schedulers) for s in states]
