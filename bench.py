@@ -432,18 +432,260 @@ def run_gbsgmc(args):
     dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# MLP regression workload: 64 chains of OBABO on the 64-1024-1024-1 tanh
+# network (BF16 tcgen05 GEMMs), minibatch 2048 of N = 500,000.
+# ---------------------------------------------------------------------------
+MLP_N, MLP_D, MLP_H, MLP_CHAINS, MLP_MB = 500_000, 64, 1024, 64, 2048
+MLP_PMATMUL = MLP_D * MLP_H + MLP_H * MLP_H + MLP_H
+MLP_FLOP_PER_GRAD = 6 * MLP_MB * MLP_PMATMUL      # forward 2, adjoint 4
+MLP_WORKLOAD = ("Bayesian MLP regression, OBABO: 64-1024-1024-1 tanh "
+                "(1,117,185 params/chain), sigma=0.1, N=500,000, 64 chains, "
+                "minibatch 2048, BF16 GEMMs with FP32 accumulation")
+
+
+def mlp_data():
+  """X ~ N(0,1) [N, 64], targets from a random teacher network + N(0, 0.1^2)."""
+  from gbsgmc import likelihoods as L
+  from oracle import sgmc_oracle as O
+  rng = np.random.default_rng(20261203 + 3)
+  lik = L.MLPGaussian(d_in=MLP_D, h1=MLP_H, h2=MLP_H, sigma=0.1)
+  X = rng.standard_normal((MLP_N, MLP_D), dtype=np.float32)
+  teacher = lik.init(rng).astype(np.float64)
+  y = np.empty(MLP_N, np.float32)
+  for a in range(0, MLP_N, 50_000):
+    f, _, _ = O.mlp_forward(teacher[None], X[None, a:a + 50_000].astype(np.float64),
+                            MLP_D, MLP_H, MLP_H)
+    y[a:a + 50_000] = f[0] + 0.1 * rng.standard_normal(min(50_000, MLP_N - a))
+  inits = np.stack([lik.init(np.random.default_rng(1000 + c))
+                    for c in range(MLP_CHAINS)])
+  return lik, X, y, inits
+
+
+def mlp_cpu_grad_rate(lik, X, y, W, reps, threads):
+  """Gradients/s of the float64 oracle on one chain (bounded sample)."""
+  from oracle import sgmc_oracle as O
+  os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+  rng = np.random.default_rng(5)
+  t0 = time.perf_counter()
+  for _ in range(reps):
+    idx = rng.integers(0, MLP_N, size=(1, MLP_MB))
+    O.mlp_potential(W[:1], X, y, idx, MLP_N, MLP_D, MLP_H, MLP_H, 0.1,
+                    prior_scale=1.0)
+  return reps / (time.perf_counter() - t0)
+
+
+def run_mlp_reference(args):
+  """The oracle on all host cores for the MLP workload (rank 0 only)."""
+  rank, _, _ = dist_env()
+  if rank != 0:
+    return
+  lik, X, y, inits = mlp_data()
+  threads = os.cpu_count() or 1
+  for _ in range(args.warmup):
+    mlp_cpu_grad_rate(lik, X, y, inits, 1, threads)
+  rate = mlp_cpu_grad_rate(lik, X, y, inits, max(1, args.steps // 50), threads) / 2.0
+  print(json.dumps({
+      "impl": "reference", "metric": METRIC, "value": rate, "unit": "chain-steps/s",
+      "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+      "higher_is_better": True, "config": {"workload": MLP_WORKLOAD},
+      "cpu_baseline": {"value": rate, "unit": "chain-steps/s", "cores": threads,
+                       "kind": "port", "sample": "float64 oracle gradients of one chain"},
+      "e2e": {"value": rate, "unit": "chain-steps/s", "h2d_bytes_per_step": 0,
+              "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def mlp_kernel_only(args):
+  """`--steps` batched value-and-gradient calls of the 64-chain workload and
+  nothing else (a short run for profilers); no JSON line."""
+  import torch
+  from gbsgmc import data, likelihoods as L, potential
+  rng = np.random.default_rng(20261203 + 3)
+  lik = L.MLPGaussian(d_in=MLP_D, h1=MLP_H, h2=MLP_H, sigma=0.1)
+  X = rng.standard_normal((MLP_N, MLP_D), dtype=np.float32)
+  y = rng.standard_normal(MLP_N).astype(np.float32)
+  ds = data.NumpyDataLoader(x=X, y=y).device_dataset()
+  pot = potential.minibatch_potential(L.GaussianPrior(1.0), lik)
+  W = torch.from_numpy(np.stack([lik.init(rng) for _ in range(MLP_CHAINS)])).cuda()
+  idx = torch.randint(0, MLP_N, (MLP_CHAINS, MLP_MB), dtype=torch.int32, device="cuda")
+  for _ in range(args.steps):
+    pot.evaluate(W, idx, ds, grad=True)
+  torch.cuda.synchronize()
+  pot.check_status()
+
+
+def run_mlp(args):
+  import torch
+  from gbsgmc import _lib, alias, data, engine, likelihoods as L, potential
+  rank, world, local = dist_env()
+  torch.cuda.set_device(local)
+  lik, X, y, inits = mlp_data()
+  loader = data.NumpyDataLoader(x=X, y=y)
+  ds = loader.device_dataset()
+  pot = potential.minibatch_potential(L.GaussianPrior(1.0), lik)
+  total = args.warmup + args.steps
+  h = torch.full((total,), 1e-7, dtype=torch.float32, device="cuda")
+  t = torch.ones(total, dtype=torch.float32, device="cuda")
+  Xd = torch.from_numpy(inits).cuda()
+  Pd = torch.zeros_like(Xd)
+  words = np.array([pcg_words(MLP_CHAINS * rank + c) for c in range(MLP_CHAINS)],
+                   np.uint64).view(np.int64)
+  pcg = torch.from_numpy(words.copy()).cuda()
+  isrc = engine.IndexSource(pcg=pcg, chain_base=MLP_CHAINS * rank)
+  plan = engine.NetPlan(pot, ds, Xd, Pd, MLP_MB, "obabo", h, t, isrc,
+                        noise_seed=7, chain_base=MLP_CHAINS * rank, friction=1.0)
+  plan.run(0, args.warmup)
+  torch.cuda.synchronize()
+  clocks = Clocks(local)
+  clocks.start()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  torch.cuda.synchronize()
+  e0.record()
+  plan.run(args.warmup, args.steps)
+  e1.record()
+  torch.cuda.synchronize()
+  clk = clocks.stop()
+  ms = e0.elapsed_time(e1)
+  plan.check_status()
+  finite = bool(torch.isfinite(Xd).all().item())
+  value = world * MLP_CHAINS * args.steps / (ms / 1e3)
+  launches = plan.launches(args.steps)
+  plan.close()
+
+  # The batched value-and-gradient alone (the tensor-core part of a step).
+  idx = torch.randint(0, MLP_N, (MLP_CHAINS, MLP_MB), dtype=torch.int32, device="cuda")
+  for _ in range(3):
+    pot.evaluate(Xd, idx, ds, grad=True)
+  torch.cuda.synchronize()
+  g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  reps = 10
+  g0.record()
+  for _ in range(reps):
+    pot.evaluate(Xd, idx, ds, grad=True)
+  g1.record()
+  torch.cuda.synchronize()
+  grad_ms = g0.elapsed_time(g1) / reps
+  flops = MLP_CHAINS * MLP_FLOP_PER_GRAD
+  achieved = flops / (grad_ms / 1e3) / 1e12
+  peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+      if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+  peak = peaks.get("bf16_tflops_sustained", 1700.0)
+
+  # Plain one-chain FP32 GPU form: the same network in torch fp32 ops,
+  # differentiated by autograd, one OBABO step (two gradients) per chain.
+  w = Xd[0].clone()
+  p = torch.zeros_like(w)
+  Xt = torch.from_numpy(X).cuda()
+  yt = torch.from_numpy(y).cuda()
+
+  def plain_grad(w, rows):
+    w = w.detach().requires_grad_(True)
+    q = lik.unravel(w)
+    z1 = torch.tanh(Xt[rows] @ q["W1"] + q["b1"])
+    z2 = torch.tanh(z1 @ q["W2"] + q["b2"])
+    out = (z2 @ q["W3"])[:, 0] + q["b3"]
+    lk = torch.distributions.Normal(out, 0.1).log_prob(yt[rows])
+    U = -(MLP_N / MLP_MB) * lk.sum() + 0.5 * (w * w).sum()
+    U.backward()
+    return w.grad
+
+  def plain_step():
+    nonlocal w, p
+    hh, keep = 1e-7, math.exp(-1e-7)
+    p = math.sqrt(keep) * p + math.sqrt(1 - keep) * torch.randn_like(p)
+    p = p - 0.5 * hh * plain_grad(w, torch.randint(0, MLP_N, (MLP_MB,), device="cuda"))
+    w = w + hh * p
+    p = p - 0.5 * hh * plain_grad(w, torch.randint(0, MLP_N, (MLP_MB,), device="cuda"))
+    p = math.sqrt(keep) * p + math.sqrt(1 - keep) * torch.randn_like(p)
+
+  for _ in range(3):
+    plain_step()
+  torch.cuda.synchronize()
+  q0 = time.perf_counter()
+  plain_n = 20
+  for _ in range(plain_n):
+    plain_step()
+  torch.cuda.synchronize()
+  plain_value = plain_n / (time.perf_counter() - q0)
+
+  # End to end through alias.obabo: host samples in, one kept sample out.
+  kw = dict(cache_size=64, batch_size=MLP_MB, integration_steps=10,
+            friction=1.0, first_step_size=1e-7, last_step_size=1e-8)
+  init_trees = [lik.unravel(inits[c]) for c in range(MLP_CHAINS)]
+  alias.obabo(pot, loader, accepted_samples=1, **kw)(*init_trees[:2], iterations=2)
+  its = max(2, args.steps // 10)
+  torch.cuda.synchronize()
+  s0 = time.perf_counter()
+  res = alias.obabo(pot, loader, accepted_samples=1, **kw)(*init_trees, iterations=its)
+  torch.cuda.synchronize()
+  e2e_s = time.perf_counter() - s0
+  e2e_value = MLP_CHAINS * its * 10 / e2e_s
+  P = lik.param_count
+  h2d = MLP_CHAINS * P * 4 / (its * 10)
+  d2h = MLP_CHAINS * res[0]["sample_count"] * (P * 4 + 8) / (its * 10)
+
+  cpu = None
+  if rank == 0:
+    threads = os.cpu_count() or 1
+    g_rate = mlp_cpu_grad_rate(lik, X, y, inits, 3, threads)
+    cpu = {"value": g_rate / 2.0, "unit": "chain-steps/s", "cores": threads,
+           "kind": "port",
+           "sample": f"3 float64 gradients of one chain (numpy oracle, {threads} "
+                     "threads); an OBABO step is two gradients"}
+  if rank == 0:
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "chain-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 GEMMs, f32 state",
+        "data": "synthetic (teacher MLP targets, numpy default_rng(20261206)); "
+                "X 144 MB resident in HBM",
+        "config": {"workload": MLP_WORKLOAD, "n_obs": MLP_N, "chains_per_gpu": MLP_CHAINS,
+                   "minibatch": MLP_MB, "integrator": "OBABO (2 gradients per step)",
+                   "index_stream": "numpy PCG64 per chain, bit-exact",
+                   "noise": "Philox4x32-10", "l2": "activations 1.4 GB per gradient, "
+                   "larger than L2", "graph_block_steps": 50},
+        "gpu_launches": launches,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": "measured bf16_tflops_sustained",
+                     "kernel": "batched value-and-gradient (5 tcgen05 GEMMs + "
+                               "elementwise kernels), 64 chains",
+                     "kernel_ms": grad_ms,
+                     "algorithmic_flop_per_launch": flops},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "chain-steps/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": "gbsgmc.alias.obabo(...)(*64 samples, iterations=K/10)"},
+        "plain_gpu": {"value": plain_value, "unit": "chain-steps/s",
+                      "form": "one chain, torch fp32 ops + autograd per gradient",
+                      "fused_over_plain": value / world / plain_value},
+        "clocks": clk, "finite": finite,
+    }), flush=True)
+
+
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument("--gpus", type=int, default=1)
   ap.add_argument("--steps", type=int, default=K_CONFIG)
   ap.add_argument("--warmup", type=int, default=5)
   ap.add_argument("--impl", default="gbsgmc", choices=["gbsgmc", "reference"])
+  ap.add_argument("--workload", default="logistic", choices=["logistic", "mlp"],
+                  help="logistic: 256-chain SGLD headline; mlp: 64-chain OBABO "
+                       "on the tanh network")
   ap.add_argument("--kernel-only", action="store_true",
                   help="short run of the fused kernel for profilers; no JSON line")
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error("--warmup must be at least 3")
-  if args.impl == "reference":
+  if args.workload == "mlp":
+    if args.impl == "reference":
+      run_mlp_reference(args)
+    elif args.kernel_only:
+      mlp_kernel_only(args)
+    else:
+      run_mlp(args)
+  elif args.impl == "reference":
     run_reference(args)
   elif args.kernel_only:
     kernel_only(args)
