@@ -161,6 +161,9 @@ typedef struct gbsgmc_sched {
   int64_t offset;
   float step_size;
   float temperature;
+  /* Per-chain factor of the temperature (replica c runs at T_k * f[c]), or
+   * NULL for 1: the temperature ladder of tempering replicas. */
+  const float* chain_temperature_dev;
 } gbsgmc_sched;
 
 /* Noise source: injected normals noise_dev[c*noise_stride + j] when noise_dev
@@ -254,6 +257,36 @@ int gbsgmc_resgld_swap_f64(int pairs, const double* U_normal_dev,
 int gbsgmc_swap_rows(int pairs, int64_t width, float* a_dev, float* b_dev,
                      const int32_t* perm_dev, gbsgmc_stream_t stream);
 
+/* Replica-exchange over a temperature ladder of R replicas (rows of [R, P]
+ * arrays, coldest first), the adjacent-pair generalisation of
+ * solver.parallel_tempering (jax_sgmc/solver.py:264-293), which pairs one
+ * normal and one hot chain.  Pair r = (r, r + 1) keeps its own estimate
+ * ssq[r] of the variance, fed by replica r's var(lk) as the reference feeds
+ * it the normal chain's:
+ *   k += 1;  ssq[r] <- (1 - 1/k) ssq[r] + (1/k) var[r]     (every step) */
+int gbsgmc_resgld_sa_update(int replicas, const double* lk_var_dev,
+                            double* ssq_dev, int64_t* k_dev,
+                            gbsgmc_stream_t stream);
+
+/* Exchange attempt at step k = sched's step (the caller attempts when
+ * (k + 1) % every == 0): round = (k + 1) / every selects the pairs r of
+ * parity round % 2 (alternating even and odd pairs).  For each, in FP64,
+ *   dbeta = 1/T(k, r) - 1/T(k, r+1),  T(k, c) = t_k * chain_temperature[c]
+ *   log_s = dbeta (U[r] - U[r+1] - dbeta ssq[r] / F)
+ *   exchanged = !(log u < log s)    (the reference's lax.cond rule)
+ * with u = u_dev[r], or Philox (seed, counter (r, round, 0, GBSGMC_TAG_SWAP))
+ * when u_dev is NULL.  An exchanging pair swaps its rows of x (and v when
+ * not NULL), U and lk_var; flags_dev[r] = 1 for it, counts_dev[r] (may be
+ * NULL) counts exchanges, log_s_dev (may be NULL) receives log s. */
+int gbsgmc_resgld_exchange_adjacent(int replicas, int64_t P, float* x_dev,
+                                    float* v_dev, double* U_dev,
+                                    double* lk_var_dev,
+                                    const gbsgmc_sched* sched, int every,
+                                    const double* ssq_dev, double F,
+                                    uint64_t seed, const double* u_dev,
+                                    int32_t* flags_dev, int32_t* counts_dev,
+                                    double* log_s_dev, gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Tensor-core GEMM (building block of the network likelihoods)              */
 /* ------------------------------------------------------------------------ */
@@ -322,6 +355,24 @@ int gbsgmc_mlp_value_and_grad(const gbsgmc_mlp* model, int chains, int n,
                               double* lk_var_dev, void* workspace_dev,
                               size_t workspace_bytes, int* status_dev,
                               gbsgmc_stream_t stream);
+
+/* As gbsgmc_mlp_value_and_grad with a minibatch of n_dev[c] rows for chain c
+ * (1 <= n_dev[c] <= n_max, device memory): row i of chain c is observation
+ * idx[c*idx_stride + i] for i < n_dev[c]; the N/n scale, the sums and
+ * var(lk) of chain c use its own n_dev[c], lk[c, i >= n_dev[c]] is 0.  The
+ * tensor cores only work on each chain's own rows (rounded up to 128).  The
+ * workspace is gbsgmc_mlp_workspace_bytes(model, chains, n_max), n_max a
+ * multiple of 128.  For tempering replicas that draw minibatches of
+ * different sizes; no reference counterpart (its replicas share one batch
+ * size). */
+int gbsgmc_mlp_value_and_grad_ragged(const gbsgmc_mlp* model, int chains,
+                                     int n_max, const int32_t* n_dev,
+                                     const int32_t* idx_dev, int64_t idx_stride,
+                                     const float* mask_dev, const float* w_dev,
+                                     double* U_dev, float* grad_dev,
+                                     float* lk_dev, double* lk_var_dev,
+                                     void* workspace_dev, size_t workspace_bytes,
+                                     int* status_dev, gbsgmc_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* Fused SGLD step for the generalised-linear families                       */
@@ -444,6 +495,43 @@ int gbsgmc_mlp_plan_create(gbsgmc_plan** plan, const gbsgmc_mlp* model,
                            const gbsgmc_index_src* index_src, double* U_dev,
                            double* lk_var_dev, double* ke_dev, int block_steps,
                            int* status_dev);
+
+/* Tempering of a network plan: replica r of R runs at the schedule's
+ * temperature times chain_temperature_dev[r] (set in the plan's sched), and
+ * every `every` steps adjacent replicas attempt an exchange
+ * (gbsgmc_resgld_exchange_adjacent).  ssq_dev [R - 1], k_dev [1] (the SA
+ * counter) and counts_dev [R - 1] are the caller's and persist across runs;
+ * flags_dev [R - 1] receives the last round's exchanges. */
+typedef struct gbsgmc_tempering {
+  int every;
+  int _pad;
+  double F;
+  uint64_t seed;
+  double* ssq_dev;
+  int64_t* k_dev;
+  int32_t* counts_dev;
+  int32_t* flags_dev;
+} gbsgmc_tempering;
+
+/* reSGLD on the dense network: R replicas of SGLD (+ rms_prop when v_dev is
+ * not NULL) with per-replica minibatch sizes n_dev[r] <= n_max (device
+ * memory, fixed for the plan's life), per-replica temperatures and the
+ * adjacent exchanges above, `block_steps` steps per captured CUDA graph
+ * (a multiple of `every`; plan_run's first step and step count must be
+ * multiples of `every`).  Per step: index draws of n_max per replica (the
+ * first n_dev[r] are used), gbsgmc_mlp_value_and_grad_ragged, the SGLD
+ * update, the SA variance update, and at exchange steps the exchange.
+ * Replaces alias.re_sgld (jax_sgmc/alias.py:121-229) run through
+ * solver.mcmc, generalised from 2 replicas to R. */
+int gbsgmc_mlp_resgld_plan_create(gbsgmc_plan** plan, const gbsgmc_mlp* model,
+                                  int replicas, int n_max, const int32_t* n_dev,
+                                  float* x_dev, float* v_dev, float alpha,
+                                  float lmbd, const gbsgmc_sched* sched,
+                                  const gbsgmc_noise* noise,
+                                  const gbsgmc_index_src* index_src,
+                                  const gbsgmc_tempering* tempering,
+                                  double* U_dev, double* lk_var_dev,
+                                  int block_steps, int* status_dev);
 
 /* Runs steps [first_step, first_step + steps) of the plan, ordered after prior
  * work on `stream`; later work on `stream` waits for it.  Does not block the

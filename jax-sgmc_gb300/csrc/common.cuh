@@ -41,6 +41,7 @@ struct Sched {
   const float* t_tab;
   const int64_t* base;
   const int32_t* keep;
+  const float* chain_t;
   int64_t offset;
   float h, t;
 
@@ -50,8 +51,10 @@ struct Sched {
   __device__ __forceinline__ float step_size(int64_t k) const {
     return h_tab != nullptr ? __ldg(h_tab + k) : h;
   }
-  __device__ __forceinline__ float temperature(int64_t k) const {
-    return t_tab != nullptr ? __ldg(t_tab + k) : t;
+  // Temperature of chain c at step k.
+  __device__ __forceinline__ float temperature(int64_t k, int c) const {
+    const float tk = t_tab != nullptr ? __ldg(t_tab + k) : t;
+    return chain_t != nullptr ? tk * __ldg(chain_t + c) : tk;
   }
   __device__ __forceinline__ int keep_slot(int64_t k) const {
     return keep != nullptr ? __ldg(keep + k) : -1;
@@ -64,6 +67,7 @@ inline Sched to_sched(const gbsgmc_sched* s) {
   r.t_tab = s->temperature_dev;
   r.base = s->base_dev;
   r.keep = s->keep_slot_dev;
+  r.chain_t = s->chain_temperature_dev;
   r.offset = s->offset;
   r.h = s->step_size;
   r.t = s->temperature;

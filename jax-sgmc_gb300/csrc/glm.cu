@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   // SGLD (+RMSprop) update of chain c, four parameters per thread.
   const int64_t k = a.sched.step();
   const float h = a.sched.step_size(k);
-  const float T = a.sched.temperature(k);
+  const float T = a.sched.temperature(k, c);
   const int slot = a.sched.keep_slot(k);
   const float noise_scale = sqrtf(2.0f * T * h);
   float* vc = a.v != nullptr ? a.v + static_cast<int64_t>(c) * a.d : nullptr;
@@ -803,7 +803,7 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.v = nullptr;
   a.alpha = 0.9f;
   a.lmbd = 1e-5f;
-  a.sched = Sched{nullptr, nullptr, nullptr, nullptr, 0, 0.0f, 1.0f};
+  a.sched = Sched{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0.0f, 1.0f};
   a.noise = Noise{nullptr, 0, 0, 0};
   return GBSGMC_OK;
 }

@@ -132,6 +132,7 @@ struct MlpLayout {
   size_t wb, xb, z1, z2g;           // BF16
   size_t yv, outp, pw3, pb2, pb1;   // fp32
   size_t psq, plk;                  // fp64
+  size_t rag;                       // int tables of a ragged batch
   size_t total;
 };
 
@@ -155,6 +156,7 @@ MlpLayout mlp_layout(const MlpShape& s, int chains, int n) {
   L.pb1 = take(4 * (N / 32) * H1);
   L.psq = take(8 * static_cast<size_t>(prep_blocks(s)));
   L.plk = take(8 * 4 * (N / kTile));
+  L.rag = take(4 * 5);  // tile prefixes [C + 1] x 2, K slices [C]
   L.total = off;
   return L;
 }
@@ -174,11 +176,41 @@ struct MlpArgs {
   float* lk;
   double* lk_var;
   int* status;
+  // Ragged batch: rows of chain c are n_true[c] <= n (null: all n).
+  const int32_t* n_true;
+  int *prefix1, *prefix2, *kblocks;
   // workspace views
   bf16 *wb, *xb, *z1, *z2g;
   float *yv, *outp, *pw3, *pb2, *pb1;
   double *psq, *plk;
 };
+
+// Rows of chain c, and the rows its GEMMs cover (a multiple of 128).
+__device__ __forceinline__ int chain_rows(const MlpArgs& a, int c) {
+  if (a.n_true == nullptr) return a.n;
+  const int v = __ldg(a.n_true + c);
+  return v < 1 ? 1 : (v > a.n ? a.n : v);
+}
+__device__ __forceinline__ int chain_rows_padded(const MlpArgs& a, int c) {
+  return (chain_rows(a, c) + 127) & ~127;
+}
+
+// Tile tables of a ragged batch for the GEMMs (one thread).
+__global__ void mlp_ragged_kernel(const MlpArgs a) {
+  int p1 = 0, p2 = 0;
+  a.prefix1[0] = 0;
+  a.prefix2[0] = 0;
+  for (int c = 0; c < a.chains; ++c) {
+    const int v = __ldg(a.n_true + c);
+    if (v < 1 || v > a.n) raise_status(a.status, GBSGMC_ERR_SHAPE);
+    const int np = chain_rows_padded(a, c);
+    p1 += (np / 128) * (a.s.H1 / kBN);
+    p2 += (np / 128) * (a.s.H2 / kBN);
+    a.prefix1[c + 1] = p1;
+    a.prefix2[c + 1] = p2;
+    a.kblocks[c] = np / kGemmBK;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // 1. W1 | W2 to BF16 (same layout) and partial sums of squares of every
@@ -227,15 +259,21 @@ __global__ void __launch_bounds__(256) mlp_gather_kernel(const MlpArgs a) {
   const MlpShape& s = a.s;
   const int i0 = blockIdx.x * kTile, f0 = blockIdx.y * kTile, c = blockIdx.z;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int nc = chain_rows(a, c);
+  if (i0 >= chain_rows_padded(a, c)) return;
   if (t < kTile) {
-    int64_t o = a.idx[static_cast<int64_t>(c) * a.idx_stride + i0 + t];
-    if (o < 0 || o >= a.n_rows) {
-      raise_status(a.status, GBSGMC_ERR_INDEX);
-      o = 0;
+    // Rows past the chain's minibatch (ragged batches) are zero.
+    int64_t o = -1;
+    if (i0 + t < nc) {
+      o = a.idx[static_cast<int64_t>(c) * a.idx_stride + i0 + t];
+      if (o < 0 || o >= a.n_rows) {
+        raise_status(a.status, GBSGMC_ERR_INDEX);
+        o = 0;
+      }
     }
     rows[t] = o;
     if (blockIdx.y == 0) {
-      const float yy = a.y_inline ? __ldg(a.X + o * a.ld + s.D) : __ldg(a.y + o);
+      const float yy = o < 0 ? 0.f : a.y_inline ? __ldg(a.X + o * a.ld + s.D) : __ldg(a.y + o);
       a.yv[static_cast<int64_t>(c) * a.n + i0 + t] = yy;
     }
   }
@@ -244,8 +282,12 @@ __global__ void __launch_bounds__(256) mlp_gather_kernel(const MlpArgs a) {
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int r = warp * 8 + j;
-    const float* src = a.X + rows[r] * a.ld + f0;
-    const float v0 = __ldg(src + lane), v1 = __ldg(src + 32 + lane);
+    float v0 = 0.f, v1 = 0.f;
+    if (rows[r] >= 0) {
+      const float* src = a.X + rows[r] * a.ld + f0;
+      v0 = __ldg(src + lane);
+      v1 = __ldg(src + 32 + lane);
+    }
     bf16* d = xb + static_cast<int64_t>(i0 + r) * s.D + f0;
     d[lane] = __float2bfloat16_rn(v0);
     d[lane + 32] = __float2bfloat16_rn(v1);
@@ -471,21 +513,30 @@ __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
   const int c = blockIdx.y, rb = blockIdx.x, i0 = rb * kTile;
   const int t = threadIdx.x, lane = t & 31;
   const float* w = a.w + static_cast<int64_t>(c) * s.P;
+  const int nc = chain_rows(a, c);
+  if (i0 >= chain_rows_padded(a, c)) {
+    if (a.lk != nullptr && t < kTile) a.lk[static_cast<int64_t>(c) * a.n + i0 + t] = 0.f;
+    return;
+  }
   if (t < kTile) {
     const float inv_s2 = 1.f / (a.sigma * a.sigma);
-    const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n / a.temperature);
+    const float scale = static_cast<float>(static_cast<double>(a.n_obs) / nc / a.temperature);
     const int i = i0 + t;
+    const bool live = i < nc;  // rows past a ragged chain's minibatch add nothing
     const int nslot = s.H2 / kSlot;
     float out = __ldg(w + s.ob3);
     for (int q = 0; q < nslot; ++q) out += a.outp[(static_cast<int64_t>(c) * nslot + q) * a.n + i];
     const float r = a.yv[static_cast<int64_t>(c) * a.n + i] - out;
     const float lk = -0.5f * r * r * inv_s2 - logf(a.sigma) - 0.91893853320467274f;
-    const float m = a.mask != nullptr ? __ldg(a.mask + static_cast<int64_t>(c) * a.n + i) : 1.f;
+    const float m = !live ? 0.f
+                    : a.mask != nullptr ? __ldg(a.mask + static_cast<int64_t>(c) * a.n + i)
+                                        : 1.f;
     const float g = -scale * m * r * inv_s2;
     g_s[t] = g;
-    if (a.lk != nullptr) a.lk[static_cast<int64_t>(c) * a.n + i] = lk;
+    if (a.lk != nullptr) a.lk[static_cast<int64_t>(c) * a.n + i] = live ? lk : 0.f;
     // var(lk) is over all n values, masked or not (jnp.var, integrator.py:880).
-    double v4[4] = {static_cast<double>(m) * lk, lk, static_cast<double>(lk) * lk, g};
+    const double lkl = live ? lk : 0.0;
+    double v4[4] = {static_cast<double>(m) * lkl, lkl, lkl * lkl, g};
 #pragma unroll
     for (int k = 0; k < 4; ++k) v4[k] = warp_sum(v4[k]);
     if (lane == 0)
@@ -576,18 +627,19 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
   const float pf = a.prior_scale > 0.f
                        ? static_cast<float>(1.0 / (s2 * a.temperature))
                        : 0.f;
-  const int nb64 = a.n / kTile, nb32 = a.n / 32;
+  const int nc = chain_rows(a, c), npad = chain_rows_padded(a, c);
+  const int nb64 = npad / kTile, nb32 = npad / 32;
   if (a.want_grad) {
     float* g = a.grad + static_cast<int64_t>(c) * s.P;
     const int j = blockIdx.x * 256 + t;
     if (j < s.H1) {
-      const float* p = a.pb1 + static_cast<int64_t>(c) * nb32 * s.H1 + j;
+      const float* p = a.pb1 + static_cast<int64_t>(c) * (a.n / 32) * s.H1 + j;
       float acc = 0.f;
       for (int r = 0; r < nb32; ++r) acc += p[static_cast<int64_t>(r) * s.H1];
       g[s.ob1 + j] = fmaf(pf, __ldg(w + s.ob1 + j), acc);
     }
     if (j < s.H2) {
-      const int64_t base = static_cast<int64_t>(c) * nb64 * s.H2 + j;
+      const int64_t base = static_cast<int64_t>(c) * (a.n / kTile) * s.H2 + j;
       float acc2 = 0.f, acc3 = 0.f;
       for (int r = 0; r < nb64; ++r) {
         acc2 += a.pb2[base + static_cast<int64_t>(r) * s.H2];
@@ -601,7 +653,7 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
   double sq = 0.0, lm = 0.0, l1 = 0.0, l2 = 0.0, gs = 0.0;
   for (int i = t; i < nprep; i += 256) sq += a.psq[static_cast<int64_t>(c) * nprep + i];
   for (int i = t; i < nb64; i += 256) {
-    const double* p = a.plk + (static_cast<int64_t>(c) * nb64 + i) * 4;
+    const double* p = a.plk + (static_cast<int64_t>(c) * (a.n / kTile) + i) * 4;
     lm += p[0];
     l1 += p[1];
     l2 += p[2];
@@ -619,12 +671,12 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
                 static_cast<double>(s.P) * (log(static_cast<double>(a.prior_scale)) +
                                             0.91893853320467274178);
   // -N * mean(lk) without a mask, -N/n * (lk . mask) with one (potential.py:183-185).
-  const double lik = -static_cast<double>(a.n_obs) * (lm / a.n);
+  const double lik = -static_cast<double>(a.n_obs) * (lm / nc);
   const double U = (lik - log_prior) / a.temperature;
   a.U[c] = U;
   if (a.lk_var != nullptr) {
-    const double mean = l1 / a.n;
-    a.lk_var[c] = fmax(l2 / a.n - mean * mean, 0.0);
+    const double mean = l1 / nc;
+    a.lk_var[c] = fmax(l2 / nc - mean * mean, 0.0);
   }
   if (!isfinite(U)) raise_status(a.status, GBSGMC_ERR_NONFINITE);
   if (a.want_grad)
@@ -677,7 +729,20 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   a.pb1 = view<float>(ws, L.pb1);
   a.psq = view<double>(ws, L.psq);
   a.plk = view<double>(ws, L.plk);
+  a.prefix1 = view<int>(ws, L.rag);
+  a.prefix2 = a.prefix1 + (a.chains + 1);
+  a.kblocks = a.prefix2 + (a.chains + 1);
   const int C = a.chains, n = a.n, D = s.D, H1 = s.H1, H2 = s.H2;
+  // Ragged batches: GEMM tiles only over each chain's own rows.
+  GemmRagged rows_h1, rows_h2, ksl;
+  if (a.n_true != nullptr) {
+    mlp_ragged_kernel<<<1, 1, 0, st>>>(a);
+    int rc0 = check_launch("mlp_ragged_kernel");
+    if (rc0 != GBSGMC_OK) return rc0;
+    rows_h1.tile_prefix = a.prefix1;
+    rows_h2.tile_prefix = a.prefix2;
+    ksl.kblocks = a.kblocks;
+  }
   const int64_t pw = matrix_params(s);
   const int nprep = prep_blocks(s);
   const bf16* w1b = a.wb;
@@ -700,10 +765,12 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     return rc;
   // 3: A1 = Xb W1 (W1 [D, H1] is the MN-major B operand).
   const EpiHidden1 e1{a.w, s.P, s.ob1, H1, n, a.z1};
-  if ((rc = launch_gemm<kBN, false, true>(m_xb, m_w1, C, n, H1, D, a.status, e1, st))) return rc;
+  if ((rc = launch_gemm<kBN, false, true>(m_xb, m_w1, C, n, H1, D, a.status, e1, st, rows_h1)))
+    return rc;
   // 4: A2 = Z1 W2.
   const EpiHidden2 e2{a.w, s.P, s.ob2, s.oW3, H2, n, a.z2g, a.outp};
-  if ((rc = launch_gemm<kBN, false, true>(m_z1, m_w2, C, n, H2, H1, a.status, e2, st))) return rc;
+  if ((rc = launch_gemm<kBN, false, true>(m_z1, m_w2, C, n, H2, H1, a.status, e2, st, rows_h2)))
+    return rc;
 
   mlp_out_kernel<<<dim3(n / kTile, C), 256, 0, st>>>(a);
   if ((rc = check_launch("mlp_out_kernel")) != GBSGMC_OK) return rc;
@@ -721,16 +788,17 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     // 6: dW2 [H1, H2] = Z1^T G2 (both operands MN-major), before step 7
     //    overwrites Z1.
     const EpiGradRows e6{a.grad, s.P, s.oW2, H2};
-    if ((rc = launch_gemm<kBN, true, true>(m_z1mn, m_g2mn, C, H1, H2, n, a.status, e6, st)))
+    if ((rc = launch_gemm<kBN, true, true>(m_z1mn, m_g2mn, C, H1, H2, n, a.status, e6, st, ksl)))
       return rc;
     // 7: G1 = (G2 W2^T) * (1 - Z1^2); W2 [H1, H2] is the K-major B operand.
     const EpiAdjoint1 e7{a.z1, a.pb1, H1, n};
-    if ((rc = launch_gemm<kBN, false, false>(m_g2, m_w2k, C, n, H1, H2, a.status, e7, st)))
+    if ((rc = launch_gemm<kBN, false, false>(m_g2, m_w2k, C, n, H1, H2, a.status, e7, st,
+                                             rows_h1)))
       return rc;
     // 8: dW1^T [H1, D] = G1^T Xb: GEMM row i (hidden unit), column f
     //    (feature) lands at dW1[f, i].
     const EpiGradCols e8{a.grad, s.P, s.oW1, H1};
-    if ((rc = launch_gemm<64, true, true>(m_z1mn, m_xbmn, C, H1, D, n, a.status, e8, st)))
+    if ((rc = launch_gemm<64, true, true>(m_z1mn, m_xbmn, C, H1, D, n, a.status, e8, st, ksl)))
       return rc;
     if (pf != 0.f) {
       mlp_prior_kernel<<<dim3(nprep - 1, C), 256, 0, st>>>(a, pf);
@@ -759,12 +827,13 @@ extern "C" size_t gbsgmc_mlp_workspace_bytes(const gbsgmc_mlp* model, int chains
   return mlp_layout(mlp_shape(model->d_in, model->h1, model->h2), chains, n).total;
 }
 
-extern "C" int gbsgmc_mlp_value_and_grad(
-    const gbsgmc_mlp* model, int chains, int n, const int32_t* idx_dev,
-    int64_t idx_stride, const float* mask_dev, const float* w_dev,
-    double* U_dev, float* grad_dev, float* lk_dev, double* lk_var_dev,
-    void* workspace_dev, size_t workspace_bytes, int* status_dev,
-    gbsgmc_stream_t stream) {
+namespace {
+
+int mlp_call(const gbsgmc_mlp* model, int chains, int n, const int32_t* n_dev,
+             const int32_t* idx_dev, int64_t idx_stride, const float* mask_dev,
+             const float* w_dev, double* U_dev, float* grad_dev, float* lk_dev,
+             double* lk_var_dev, void* workspace_dev, size_t workspace_bytes,
+             int* status_dev, gbsgmc_stream_t stream) {
   int rc = check_model(model, "mlp_value_and_grad");
   if (rc != GBSGMC_OK) return rc;
   if (chains < 0 || n < 0)
@@ -810,5 +879,32 @@ extern "C" int gbsgmc_mlp_value_and_grad(
   a.lk = lk_dev;
   a.lk_var = lk_var_dev;
   a.status = status_dev;
+  a.n_true = n_dev;
   return run_mlp(a, L, workspace_dev, static_cast<cudaStream_t>(stream));
+}
+
+}  // namespace
+
+extern "C" int gbsgmc_mlp_value_and_grad(
+    const gbsgmc_mlp* model, int chains, int n, const int32_t* idx_dev,
+    int64_t idx_stride, const float* mask_dev, const float* w_dev,
+    double* U_dev, float* grad_dev, float* lk_dev, double* lk_var_dev,
+    void* workspace_dev, size_t workspace_bytes, int* status_dev,
+    gbsgmc_stream_t stream) {
+  return mlp_call(model, chains, n, nullptr, idx_dev, idx_stride, mask_dev, w_dev, U_dev,
+                  grad_dev, lk_dev, lk_var_dev, workspace_dev, workspace_bytes, status_dev,
+                  stream);
+}
+
+extern "C" int gbsgmc_mlp_value_and_grad_ragged(
+    const gbsgmc_mlp* model, int chains, int n_max, const int32_t* n_dev,
+    const int32_t* idx_dev, int64_t idx_stride, const float* mask_dev,
+    const float* w_dev, double* U_dev, float* grad_dev, float* lk_dev,
+    double* lk_var_dev, void* workspace_dev, size_t workspace_bytes,
+    int* status_dev, gbsgmc_stream_t stream) {
+  if (n_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "mlp_value_and_grad_ragged: null row counts");
+  return mlp_call(model, chains, n_max, n_dev, idx_dev, idx_stride, mask_dev, w_dev, U_dev,
+                  grad_dev, lk_dev, lk_var_dev, workspace_dev, workspace_bytes, status_dev,
+                  stream);
 }

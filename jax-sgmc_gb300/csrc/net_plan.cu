@@ -123,6 +123,73 @@ struct NetPlan final : gbsgmc_plan {
   }
 };
 
+// reSGLD over R replicas with ragged minibatches and adjacent exchanges.
+struct ResgldPlan final : gbsgmc_plan {
+  GradFn grad_fn;
+  int replicas = 0, n_max = 0;
+  int64_t P = 0, rows = 0;
+  float* x = nullptr;
+  float* v = nullptr;
+  float alpha = 0.9f, lmbd = 1e-5f;
+  float* grad = nullptr;  // owned [R, P]
+  gbsgmc_sched sched{};
+  gbsgmc_noise noise{};
+  gbsgmc_index_src isrc{};
+  gbsgmc_tempering temp{};
+  double* U = nullptr;
+  double* lk_var = nullptr;
+  double* var_own = nullptr;  // owned when the caller passes no lk_var buffer
+  int* status = nullptr;
+  int32_t* idx = nullptr;  // owned [G, R, n_max]
+  void* ws = nullptr;      // owned
+  size_t ws_size = 0;
+
+  ~ResgldPlan() override {
+    if (stream != nullptr) cudaStreamSynchronize(stream);
+    cudaFree(grad);
+    cudaFree(idx);
+    cudaFree(ws);
+    cudaFree(var_own);
+  }
+
+  int step_multiple() const override { return temp.every; }
+
+  int64_t launches_per_block(int g) const override {
+    return 2 + 2 * static_cast<int64_t>(g) + 3 * (g / temp.every);
+  }
+
+  int enqueue(int g, cudaStream_t s) override {
+    const int64_t cn = static_cast<int64_t>(replicas) * n_max;
+    int rc;
+    if (isrc.pcg_dev != nullptr) {
+      rc = gbsgmc_index_draw_pcg64(isrc.pcg_dev, replicas, rows,
+                                   static_cast<int64_t>(g) * n_max, n_max, idx, n_max, cn,
+                                   status, s);
+    } else {
+      rc = launch_philox_index(isrc.index_seed, isrc.chain_base, replicas, base, 0, g, n_max,
+                               rows, idx, n_max, cn, s);
+    }
+    if (rc != GBSGMC_OK) return rc;
+    for (int j = 0; j < g; ++j) {
+      gbsgmc_sched sj = sched;
+      sj.base_dev = base;
+      sj.offset = j;
+      if ((rc = grad_fn(idx + j * cn, n_max, U, lk_var, s))) return rc;
+      if ((rc = gbsgmc_sgld_update(replicas, P, x, grad, v, alpha, lmbd, &sj, &noise, nullptr,
+                                   s)))
+        return rc;
+      if ((rc = gbsgmc_resgld_sa_update(replicas, lk_var, temp.ssq_dev, temp.k_dev, s)))
+        return rc;
+      if ((j + 1) % temp.every == 0 &&
+          (rc = gbsgmc_resgld_exchange_adjacent(replicas, P, x, v, U, lk_var, &sj, temp.every,
+                                                temp.ssq_dev, temp.F, temp.seed, nullptr,
+                                                temp.flags_dev, temp.counts_dev, nullptr, s)))
+        return rc;
+    }
+    return plan_advance(this, g, s);
+  }
+};
+
 int check_common(const gbsgmc_integrator* integ, int chains, int n, float* x, float* aux,
                  const gbsgmc_sched* sched, const gbsgmc_noise* noise,
                  const gbsgmc_index_src* isrc, double* U, int block_steps, int* status) {
@@ -202,6 +269,85 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
                      cudaStream_t s) {
       return gbsgmc_mlp_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
                                        nullptr, var, wsp, ws, status_dev, s);
+    };
+    rc = plan_capture(p);
+  } while (false);
+  if (rc != GBSGMC_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return GBSGMC_OK;
+}
+
+extern "C" int gbsgmc_mlp_resgld_plan_create(
+    gbsgmc_plan** out, const gbsgmc_mlp* model, int replicas, int n_max, const int32_t* n_dev,
+    float* x_dev, float* v_dev, float alpha, float lmbd, const gbsgmc_sched* sched,
+    const gbsgmc_noise* noise, const gbsgmc_index_src* isrc, const gbsgmc_tempering* temp,
+    double* U_dev, double* lk_var_dev, int block_steps, int* status_dev) {
+  if (out == nullptr) return set_error(GBSGMC_ERR_ARG, "mlp_resgld_plan_create: null plan");
+  *out = nullptr;
+  if (model == nullptr || n_dev == nullptr || x_dev == nullptr || sched == nullptr ||
+      noise == nullptr || isrc == nullptr || temp == nullptr || U_dev == nullptr ||
+      status_dev == nullptr || temp->ssq_dev == nullptr || temp->k_dev == nullptr ||
+      temp->flags_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "mlp_resgld_plan_create: null argument");
+  if (replicas < 2 || replicas > 65535 || n_max <= 0 || block_steps <= 0 ||
+      block_steps > 100000 || temp->every < 1 || block_steps % temp->every != 0 ||
+      !(temp->F > 0))
+    return set_error(GBSGMC_ERR_ARG,
+                     "mlp_resgld_plan_create: bad replicas, sizes or exchange period "
+                     "(block_steps must be a multiple of every)");
+  if (sched->keep_slot_dev != nullptr)
+    return set_error(GBSGMC_ERR_UNSUPPORTED,
+                     "mlp_resgld_plan_create: samples are collected by the caller");
+  const size_t ws = gbsgmc_mlp_workspace_bytes(model, replicas, n_max);
+  if (ws == 0)
+    return set_error(GBSGMC_ERR_SHAPE, "mlp_resgld_plan_create: unsupported shape (n_max %% 128)");
+  ResgldPlan* p = new (std::nothrow) ResgldPlan();
+  if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "mlp_resgld_plan_create: out of memory");
+  p->replicas = replicas;
+  p->n_max = n_max;
+  p->P = gbsgmc_mlp_param_count(model);
+  p->rows = model->n_rows > 0 ? model->n_rows : model->n_obs;
+  p->x = x_dev;
+  p->v = v_dev;
+  p->alpha = alpha;
+  p->lmbd = lmbd;
+  p->sched = *sched;
+  p->noise = *noise;
+  p->isrc = *isrc;
+  p->temp = *temp;
+  p->U = U_dev;
+  p->lk_var = lk_var_dev;
+  p->status = status_dev;
+  p->ws_size = ws;
+  int rc = GBSGMC_OK;
+  do {
+    if ((rc = plan_init(p, block_steps))) break;
+    if (p->lk_var == nullptr) {
+      if ((rc = cuda_err(cudaMalloc(&p->var_own, sizeof(double) * replicas),
+                         "mlp_resgld_plan_create: var")))
+        break;
+      p->lk_var = p->var_own;
+    }
+    const size_t gbytes = sizeof(float) * static_cast<size_t>(replicas) * p->P;
+    const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * replicas * n_max;
+    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "mlp_resgld_plan_create: gradient")))
+      break;
+    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "mlp_resgld_plan_create: index buffer")))
+      break;
+    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "mlp_resgld_plan_create: workspace"))) break;
+    const gbsgmc_mlp m = *model;
+    float* grad = p->grad;
+    void* wsp = p->ws;
+    const float* x = x_dev;
+    p->grad_fn = [m, replicas, n_max, n_dev, x, grad, wsp, ws, status_dev](
+                     const int32_t* idx, int64_t stride, double* U, double* var,
+                     cudaStream_t s) {
+      return gbsgmc_mlp_value_and_grad_ragged(&m, replicas, n_max, n_dev, idx, stride, nullptr,
+                                              x, U, grad, nullptr, var, wsp, ws, status_dev,
+                                              s);
     };
     rc = plan_capture(p);
   } while (false);

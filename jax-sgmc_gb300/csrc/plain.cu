@@ -144,7 +144,7 @@ __global__ void update_kernel(int d, float* w, float* v, const float* grad,
   if (j >= d) return;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
-  const float T = sched.temperature(k);
+  const float T = sched.temperature(k, 0);
   const float g = grad[j];
   const float sgrad = -h * g;
   const float snoise = sqrtf(2.0f * T * h) * xi[j];

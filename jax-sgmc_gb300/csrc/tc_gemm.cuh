@@ -65,6 +65,26 @@ int make_tmap_bf16_3d(CUtensorMap* map, const void* base, int64_t cols,
 
 size_t gemm_smem_bytes(int bn);
 
+// Ragged batches: chain b may use only the first m_b rows (row-ragged: its
+// output tiles are counted by tile_prefix[b + 1] - tile_prefix[b]) or only
+// the first kblocks[b] 64-wide K slices (K-ragged).  Null pointers mean the
+// uniform batch.  Both arrays live in device memory.
+struct GemmRagged {
+  const int* tile_prefix = nullptr;  // [batch + 1], tile_prefix[0] = 0
+  const int* kblocks = nullptr;      // [batch]
+};
+
+__device__ __forceinline__ int ragged_batch(const GemmRagged& rg, int t, int per_batch,
+                                            int batch) {
+  if (rg.tile_prefix == nullptr) return t / per_batch;
+  int lo = 0, hi = batch;  // largest b with tile_prefix[b] <= t
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(rg.tile_prefix + mid) <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // Persistent batched GEMM C[b] = A[b] * B[b]^T on the tcgen05 tensor cores.
 //
 // A is M x K and B is N x K, BF16; each is either K-major (rows of K
@@ -95,7 +115,7 @@ template <int BN, bool A_MN, bool B_MN, class Epi>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta,
                    const __grid_constant__ CUtensorMap tb, int M, int N, int K,
-                   int batch, int* status, Epi epi) {
+                   int batch, int* status, Epi epi, GemmRagged rg) {
   constexpr int BM = kGemmBM, BK = kGemmBK, STAGES = kGemmStages;
   constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
   constexpr uint32_t BLOCK_BYTES = 64 * BK * 2;  // one 64 x 64 MN-major box
@@ -117,8 +137,14 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles_n = N / BN, per_batch = (M / BM) * tiles_n;
-  const int tiles = per_batch * batch;
-  const int KB = K / BK;
+  const int tiles = rg.tile_prefix != nullptr ? __ldg(rg.tile_prefix + batch)
+                                              : per_batch * batch;
+  // Chain of tile t, its index within the chain, and its K slices.
+  auto decode = [&](int t, int& b, int& r, int& KB) {
+    b = ragged_batch(rg, t, per_batch, batch);
+    r = t - (rg.tile_prefix != nullptr ? __ldg(rg.tile_prefix + b) : b * per_batch);
+    KB = rg.kblocks != nullptr ? __ldg(rg.kblocks + b) : K / BK;
+  };
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < STAGES; ++i) {
@@ -147,7 +173,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       uint32_t it = 0;
       bool ok = true;
       for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x) {
-        const int b = t / per_batch, r = t - b * per_batch;
+        int b, r, KB;
+        decode(t, b, r, KB);
         const int m0 = (r / tiles_n) * BM, n0 = (r % tiles_n) * BN;
         for (int kb = 0; kb < KB; ++kb, ++it) {
           const int s = it % STAGES;
@@ -190,6 +217,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       uint32_t it = 0, acc = 0;
       bool ok = true;
       for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x, ++acc) {
+        int b, r, KB;
+        decode(t, b, r, KB);
         const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
         if (!mbar_wait_bounded(&tempty[buf], aph ^ 1u, abort_flag)) {
           raise_status(status, GBSGMC_ERR_TIMEOUT);
@@ -245,7 +274,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         break;
       }
       tc::fence_after_sync();
-      const int b = t / per_batch, r = t - b * per_batch;
+      int b, r, KB;
+      decode(t, b, r, KB);
       const int row0 = (r / tiles_n) * BM + q * 32;
       const uint32_t tbase =
           tmem + buf * BN + h * NC + (static_cast<uint32_t>(q * 32) << 16);
@@ -267,11 +297,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 }
 
 // Launches the persistent GEMM on `st`: one CTA per resident slot (at most
-// one per output tile).  ta / tb: tensor maps made by make_tmap_bf16_3d with
+// one per output tile of the uniform batch; with a ragged batch M and K are
+// the largest chain's).  ta / tb: tensor maps made by make_tmap_bf16_3d with
 // boxes of 64 x 128 (A, K-major), 64 x BN (B, K-major) or 64 x 64 (MN-major).
 template <int BN, bool A_MN, bool B_MN, class Epi>
 int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, int batch, int M,
-                int N, int K, int* status, const Epi& epi, cudaStream_t st) {
+                int N, int K, int* status, const Epi& epi, cudaStream_t st,
+                GemmRagged rg = GemmRagged{}) {
   auto kern = tc_gemm_kernel<BN, A_MN, B_MN, Epi>;
   const size_t smem = gemm_smem_bytes(BN);
   static int per_sm = 0;
@@ -290,7 +322,7 @@ int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, int batch, int M,
     return set_error(GBSGMC_ERR_CUDA, "gemm: cannot query the device");
   const int64_t tiles = static_cast<int64_t>(M / kGemmBM) * (N / BN) * batch;
   const int grid = static_cast<int>(tiles < int64_t(sms) * per_sm ? tiles : int64_t(sms) * per_sm);
-  kern<<<grid, kGemmThreads, smem, st>>>(ta, tb, M, N, K, batch, status, epi);
+  kern<<<grid, kGemmThreads, smem, st>>>(ta, tb, M, N, K, batch, status, epi, rg);
   return check_launch("tc_gemm_kernel");
 }
 

@@ -43,7 +43,7 @@ __global__ void sgld_update_kernel(int chains, int64_t P, float* x,
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
-  const float T = sched.temperature(k);
+  const float T = sched.temperature(k, c);
   const int slot = sched.keep_slot(k);
   const float noise_scale = sqrtf(2.0f * T * h);
   const int64_t groups = (P + 3) / 4;
@@ -88,7 +88,7 @@ __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
-  const float T = sched.temperature(k);
+  const float T = sched.temperature(k, c);
   const float permanence = expf(-friction * h);
   const float keep = sqrtf(permanence);
   const float inject = sqrtf((1.0f - permanence) * T);
@@ -122,7 +122,7 @@ __global__ void obabo_second_kernel(int chains, int64_t P, float* p,
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
-  const float T = sched.temperature(k);
+  const float T = sched.temperature(k, c);
   const float permanence = expf(-friction * h);
   const float keep = sqrtf(permanence);
   const float inject = sqrtf((1.0f - permanence) * T);
@@ -212,6 +212,16 @@ __global__ void sghmc_momentum_kernel(int chains, int64_t P, float* p,
   }
 }
 
+// Uniform in (0, 1) with 53 random bits from Philox (seed, counter (pair,
+// step, 0, GBSGMC_TAG_SWAP)).
+__device__ __forceinline__ double swap_uniform(uint64_t seed, uint32_t pair, uint32_t step) {
+  const U32x4 r = philox4x32_10(U32x4{pair, step, 0u, GBSGMC_TAG_SWAP},
+                                static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+  const uint64_t bits = ((static_cast<uint64_t>(r.x) >> 5) << 26) |
+                        (static_cast<uint64_t>(r.y) >> 6);
+  return (static_cast<double>(bits) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
 __global__ void resgld_swap_kernel(int pairs, const double* Un,
                                    const double* Uh, const double* var_n,
                                    const double* Tn, const double* Th,
@@ -229,18 +239,9 @@ __global__ void resgld_swap_kernel(int pairs, const double* Un,
   const double dbeta = 1.0 / Tn[i] - 1.0 / Th[i];
   const double correction = dbeta * s2 / F;
   const double log_s = dbeta * (Un[i] - Uh[i] - correction);
-  double u;
-  if (u_in != nullptr) {
-    u = u_in[i];
-  } else {
-    const U32x4 r = philox4x32_10(
-        U32x4{static_cast<uint32_t>(i), static_cast<uint32_t>(step), 0u,
-              GBSGMC_TAG_SWAP},
-        static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
-    const uint64_t bits = ((static_cast<uint64_t>(r.x) >> 5) << 26) |
-                          (static_cast<uint64_t>(r.y) >> 6);
-    u = (static_cast<double>(bits) + 0.5) * (1.0 / 9007199254740992.0);
-  }
+  const double u = u_in != nullptr
+                       ? u_in[i]
+                       : swap_uniform(seed, static_cast<uint32_t>(i), static_cast<uint32_t>(step));
   if (log_s_out != nullptr) log_s_out[i] = log_s;
   perm[i] = (log(u) < log_s) ? 0 : 1;
 }
@@ -255,6 +256,75 @@ __global__ void swap_rows_kernel(int pairs, int64_t width, float* a, float* b,
     const float t = a[off + j];
     a[off + j] = b[off + j];
     b[off + j] = t;
+  }
+}
+
+// Stochastic-approximation update of the adjacent-pair variance estimates
+// (one block): k += 1, ssq[r] = (1 - 1/k) ssq[r] + (1/k) var[r].
+__global__ void resgld_sa_kernel(int replicas, const double* var, double* ssq, int64_t* kc) {
+  const int64_t k = kc[0] + 1;
+  __syncthreads();
+  if (threadIdx.x == 0) kc[0] = k;
+  const double sa = 1.0 / static_cast<double>(k);
+  for (int r = threadIdx.x; r < replicas - 1; r += blockDim.x)
+    ssq[r] = (1.0 - sa) * ssq[r] + sa * var[r];
+}
+
+// Exchange decisions between adjacent replicas (r, r + 1) at step k, for the
+// pairs r = parity, parity + 2, ... with parity = round & 1, round =
+// (k + 1) / every.  Replica r runs at T(k, r) = t_k f_r (the schedule's
+// per-chain temperature).  The rule of solver.py:273-291 per pair, in FP64;
+// a pair that exchanges swaps its U and var here and its rows in
+// swap_adjacent_rows_kernel.
+__global__ void resgld_decide_kernel(int replicas, Sched sched, int every, double* U,
+                                     double* var, const double* ssq, double F, uint64_t seed,
+                                     const double* u_in, int32_t* flags, int32_t* counts,
+                                     double* log_s_out) {
+  const int64_t k = sched.step();
+  const int64_t round = (k + 1) / every;
+  const int parity = static_cast<int>(round & 1);
+  for (int r = threadIdx.x; r < replicas - 1; r += blockDim.x) {
+    int swapped = 0;
+    if ((r & 1) == parity) {
+      const double Tn = sched.temperature(k, r), Th = sched.temperature(k, r + 1);
+      const double dbeta = 1.0 / Tn - 1.0 / Th;
+      const double log_s = dbeta * (U[r] - U[r + 1] - dbeta * ssq[r] / F);
+      const double u = u_in != nullptr
+                           ? u_in[r]
+                           : swap_uniform(seed, static_cast<uint32_t>(r),
+                                          static_cast<uint32_t>(round));
+      // The reference keeps the pair when log u < log s (lax.cond true branch).
+      swapped = (log(u) < log_s) ? 0 : 1;
+      if (log_s_out != nullptr) log_s_out[r] = log_s;
+    }
+    flags[r] = swapped;
+  }
+  __syncthreads();
+  // Pairs of one parity are disjoint, so the swaps do not interfere.
+  for (int r = threadIdx.x; r < replicas - 1; r += blockDim.x) {
+    if (flags[r] == 0) continue;
+    double t = U[r];
+    U[r] = U[r + 1];
+    U[r + 1] = t;
+    if (var != nullptr) {
+      t = var[r];
+      var[r] = var[r + 1];
+      var[r + 1] = t;
+    }
+    if (counts != nullptr) counts[r] += 1;
+  }
+}
+
+__global__ void swap_adjacent_rows_kernel(int64_t width, float* a, const int32_t* flags) {
+  const int r = blockIdx.y;
+  if (flags[r] == 0) return;
+  float* x = a + static_cast<int64_t>(r) * width;
+  float* y = x + width;
+  for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < width;
+       j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const float t = x[j];
+    x[j] = y[j];
+    y[j] = t;
   }
 }
 
@@ -410,4 +480,35 @@ extern "C" int gbsgmc_swap_rows(int pairs, int64_t width, float* a_dev,
   swap_rows_kernel<<<grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
       pairs, width, a_dev, b_dev, perm_dev);
   return check_launch("swap_rows");
+}
+
+extern "C" int gbsgmc_resgld_sa_update(int replicas, const double* lk_var_dev, double* ssq_dev,
+                                       int64_t* k_dev, gbsgmc_stream_t stream) {
+  if (replicas < 2 || replicas > 65536 || lk_var_dev == nullptr || ssq_dev == nullptr ||
+      k_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "resgld_sa_update: bad arguments");
+  resgld_sa_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(replicas, lk_var_dev,
+                                                                     ssq_dev, k_dev);
+  return check_launch("resgld_sa_update");
+}
+
+extern "C" int gbsgmc_resgld_exchange_adjacent(
+    int replicas, int64_t P, float* x_dev, float* v_dev, double* U_dev, double* lk_var_dev,
+    const gbsgmc_sched* sched, int every, const double* ssq_dev, double F, uint64_t seed,
+    const double* u_dev, int32_t* flags_dev, int32_t* counts_dev, double* log_s_dev,
+    gbsgmc_stream_t stream) {
+  if (replicas < 2 || replicas > 65536 || P < 0 || x_dev == nullptr || U_dev == nullptr ||
+      sched == nullptr || ssq_dev == nullptr || flags_dev == nullptr || every < 1 || !(F > 0))
+    return set_error(GBSGMC_ERR_ARG, "resgld_exchange_adjacent: bad arguments");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  resgld_decide_kernel<<<1, 256, 0, st>>>(replicas, to_sched(sched), every, U_dev, lk_var_dev,
+                                         ssq_dev, F, seed, u_dev, flags_dev, counts_dev,
+                                         log_s_dev);
+  int rc = check_launch("resgld_exchange_adjacent: decide");
+  if (rc != GBSGMC_OK || P == 0) return rc;
+  const int chunks = static_cast<int>(std::min<int64_t>((P + 1023) / 1024, 64));
+  dim3 grid(chunks, replicas - 1);
+  swap_adjacent_rows_kernel<<<grid, 256, 0, st>>>(P, x_dev, flags_dev);
+  if (v_dev != nullptr) swap_adjacent_rows_kernel<<<grid, 256, 0, st>>>(P, v_dev, flags_dev);
+  return check_launch("resgld_exchange_adjacent: rows");
 }

@@ -75,11 +75,19 @@ class Integrator(C.Structure):
 INTEGRATOR_SGLD, INTEGRATOR_OBABO, INTEGRATOR_SGHMC = 0, 1, 2
 
 
+class Tempering(C.Structure):
+  _fields_ = [("every", C.c_int), ("_pad", C.c_int), ("F", C.c_double),
+              ("seed", C.c_uint64), ("ssq_dev", C.c_void_p),
+              ("k_dev", C.c_void_p), ("counts_dev", C.c_void_p),
+              ("flags_dev", C.c_void_p)]
+
+
 class Sched(C.Structure):
   _fields_ = [("step_size_dev", C.c_void_p), ("temperature_dev", C.c_void_p),
               ("base_dev", C.c_void_p), ("keep_slot_dev", C.c_void_p),
               ("offset", C.c_int64), ("step_size", C.c_float),
-              ("temperature", C.c_float)]
+              ("temperature", C.c_float),
+              ("chain_temperature_dev", C.c_void_p)]
 
 
 class Noise(C.Structure):
@@ -117,6 +125,9 @@ SIGNATURES = {
     "gbsgmc_mlp_value_and_grad": (_i, [_P(Mlp), _i, _i, _vp, _i64, _vp, _vp,
                                        _vp, _vp, _vp, _vp, _vp, _sz, _vp,
                                        _vp]),
+    "gbsgmc_mlp_value_and_grad_ragged": (_i, [_P(Mlp), _i, _i, _vp, _vp, _i64,
+                                              _vp, _vp, _vp, _vp, _vp, _vp,
+                                              _vp, _sz, _vp, _vp]),
     "gbsgmc_sgld_update": (_i, [_i, _i64, _vp, _vp, _vp, _f, _f, _P(Sched),
                                 _P(Noise), _vp, _vp]),
     "gbsgmc_obabo_first": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _f, _vp,
@@ -145,6 +156,14 @@ SIGNATURES = {
     "gbsgmc_mlp_plan_create": (_i, [_P(_vp), _P(Mlp), _i, _i, _P(Integrator),
                                     _vp, _vp, _P(Sched), _P(Noise),
                                     _P(IndexSrc), _vp, _vp, _vp, _i, _vp]),
+    "gbsgmc_resgld_sa_update": (_i, [_i, _vp, _vp, _vp, _vp]),
+    "gbsgmc_resgld_exchange_adjacent": (_i, [_i, _i64, _vp, _vp, _vp, _vp,
+                                             _P(Sched), _i, _vp, _d, _u64,
+                                             _vp, _vp, _vp, _vp, _vp]),
+    "gbsgmc_mlp_resgld_plan_create": (_i, [_P(_vp), _P(Mlp), _i, _i, _vp, _vp,
+                                           _vp, _f, _f, _P(Sched), _P(Noise),
+                                           _P(IndexSrc), _P(Tempering), _vp,
+                                           _vp, _i, _vp]),
     "gbsgmc_plan_run": (_i, [_vp, _i64, _i64, _vp]),
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
     "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i)]),
@@ -210,10 +229,10 @@ def stream_handle(stream=None) -> int | None:
 
 def sched(step_size=0.0, temperature=1.0, step_size_dev=None,
           temperature_dev=None, base_dev=None, keep_slot_dev=None,
-          offset=0) -> Sched:
+          offset=0, chain_temperature_dev=None) -> Sched:
   return Sched(ptr(step_size_dev), ptr(temperature_dev), ptr(base_dev),
                ptr(keep_slot_dev), int(offset), float(step_size),
-               float(temperature))
+               float(temperature), ptr(chain_temperature_dev))
 
 
 def noise(seed=0, chain_base=0, noise_dev=None, noise_stride=0) -> Noise:

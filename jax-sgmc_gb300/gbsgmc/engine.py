@@ -201,6 +201,75 @@ class NetPlan:
       pass
 
 
+class ResgldPlan:
+  """Owns a reSGLD network plan (``gbsgmc_mlp_resgld_plan_create``): R
+  replicas of SGLD(+RMSprop) on a dense-network potential at the temperature
+  ladder ``ladder`` [R] (coldest first), minibatch rows[r] <= n_max for
+  replica r, adjacent exchanges every ``every`` steps.  ``X`` [R, P] (and
+  ``V``) are updated in place; ``U``, ``lk_var``, ``ssq``, ``counts`` and
+  ``flags`` are readable device tensors."""
+
+  def __init__(self, potential, dataset, X, V, rows, n_max, ladder, h_tab,
+               t_tab, index_src, noise_seed, swap_seed, every=50, F=1.0,
+               alpha=0.9, lmbd=1e-5, chain_base=0, block_steps=None,
+               observation_count=None):
+    import torch
+    R, P = X.shape
+    self.R, self.P = R, P
+    self.model, self._keep_alive = potential.model(dataset, observation_count)
+    self.X, self.V = X, V
+    self.rows = torch.as_tensor(rows, dtype=torch.int32).cuda().contiguous()
+    self.ladder = torch.as_tensor(ladder, dtype=torch.float32).cuda().contiguous()
+    self.U = torch.zeros(R, dtype=torch.float64, device="cuda")
+    self.lk_var = torch.zeros(R, dtype=torch.float64, device="cuda")
+    self.ssq = torch.zeros(R - 1, dtype=torch.float64, device="cuda")
+    self.k = torch.zeros(1, dtype=torch.int64, device="cuda")
+    self.counts = torch.zeros(R - 1, dtype=torch.int32, device="cuda")
+    self.flags = torch.zeros(R - 1, dtype=torch.int32, device="cuda")
+    self.status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    self.h_tab, self.t_tab = h_tab, t_tab
+    self.index_src = index_src
+    self.sched = _lib.sched(step_size_dev=h_tab, temperature_dev=t_tab,
+                            chain_temperature_dev=self.ladder)
+    self.noise = _lib.noise(noise_seed, chain_base)
+    self.temp = _lib.Tempering(int(every), 0, float(F), int(swap_seed) & (2**64 - 1),
+                               _lib.ptr(self.ssq), _lib.ptr(self.k),
+                               _lib.ptr(self.counts), _lib.ptr(self.flags))
+    if block_steps is None:
+      block_steps = every * max(1, DEFAULT_BLOCK_STEPS // every)
+    handle = _lib.C.c_void_p()
+    _lib.call("gbsgmc_mlp_resgld_plan_create", _lib.C.byref(handle), self.model,
+              R, int(n_max), _lib.ptr(self.rows), _lib.ptr(X), _lib.ptr(V),
+              float(alpha), float(lmbd), self.sched, self.noise,
+              index_src.struct, self.temp, _lib.ptr(self.U),
+              _lib.ptr(self.lk_var), int(block_steps), _lib.ptr(self.status))
+    self.handle = handle
+
+  def run(self, first_step, steps):
+    _lib.call("gbsgmc_plan_run", self.handle, int(first_step), int(steps),
+              _lib.stream_handle())
+
+  def launches(self, steps) -> int:
+    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps))) + \
+        10 * int(steps)
+
+  def check_status(self):
+    code = int(self.status.item())
+    if code != 0:
+      raise _lib.GbsgmcError(code, "device status of the reSGLD plan")
+
+  def close(self):
+    if getattr(self, "handle", None):
+      _lib.load().gbsgmc_plan_destroy(self.handle)
+      self.handle = None
+
+  def __del__(self):
+    try:
+      self.close()
+    except Exception:  # pragma: no cover - interpreter shutdown
+      pass
+
+
 def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
   """Runs sgmc chains of langevin_diffusion / obabo / friction_leapfrog on a
   dense-network potential through one :class:`NetPlan`; returns None when

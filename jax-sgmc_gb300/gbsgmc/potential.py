@@ -142,8 +142,10 @@ class StochasticPotential:
 
   # -- batched evaluation --------------------------------------------------
   def evaluate(self, W, idx, dataset, mask=None, grad=True, lk=False,
-               observation_count=None, model=None):
-    """U, grad, lk, var for ``C`` chains: W [C, d], idx [C, n] int32."""
+               observation_count=None, model=None, rows=None):
+    """U, grad, lk, var for ``C`` chains: W [C, d], idx [C, n] int32.
+    ``rows`` (network likelihoods only): int32 device [C], chain c uses the
+    first rows[c] indices of its row of ``idx``."""
     import torch
     C, d = W.shape
     n = idx.shape[-1]
@@ -166,6 +168,17 @@ class StochasticPotential:
     idx = idx.to(torch.int32).contiguous()
     if mask is not None:
       mask = mask.to(device="cuda", dtype=torch.float32).reshape(C, n).contiguous()
+    if rows is not None:
+      if not self.is_mlp:
+        raise NotImplementedError("per-chain minibatch sizes are implemented "
+                                  "for the network likelihoods")
+      rows = rows.to(device="cuda", dtype=torch.int32).contiguous()
+      _lib.call("gbsgmc_mlp_value_and_grad_ragged", m, C, n, _lib.ptr(rows),
+                _lib.ptr(idx), idx.stride(0) if idx.dim() == 2 else n,
+                _lib.ptr(mask), _lib.ptr(W), _lib.ptr(U), _lib.ptr(g),
+                _lib.ptr(lko), _lib.ptr(var), _lib.ptr(ws), ws.numel(),
+                _lib.ptr(self.status()), _lib.stream_handle())
+      return GlmEval(U, g, lko, var)
     fn = "gbsgmc_mlp_value_and_grad" if self.is_mlp else \
         "gbsgmc_glm_value_and_grad"
     _lib.call(fn, m, C, n, _lib.ptr(idx),

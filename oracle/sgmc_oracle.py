@@ -394,6 +394,44 @@ def resgld_swap(U_n, U_h, var_n, T_n, T_h, ssq, k, u, F=1.0):
   return swapped, ssq, k, log_s
 
 
+def swap_uniform(seed: int, pair: int, step: int) -> float:
+  """The exchange uniform: Philox(counter=(pair, step, 0, 5), key=seed), 53
+  bits ((r0 >> 5) << 26 | r1 >> 6) + 0.5 over 2^53."""
+  r = philox4x32_10(np.array([[pair, step & 0xFFFFFFFF, 0, 5]], np.uint64),
+                    (seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF))[0]
+  bits = ((int(r[0]) >> 5) << 26) | (int(r[1]) >> 6)
+  return (bits + 0.5) / 9007199254740992.0
+
+
+def resgld_sa_update(var, ssq, k):
+  """Every step: k += 1, ssq[r] = (1 - 1/k) ssq[r] + (1/k) var[r] for the
+  adjacent pairs (r, r+1) -- solver.py:273-276 applied per pair, fed by the
+  colder replica's variance as the reference feeds the normal chain's."""
+  k = k + 1
+  sa = 1.0 / k
+  return (1 - sa) * np.asarray(ssq, np.float64) + sa * np.asarray(var, np.float64)[:-1], k
+
+
+def resgld_exchange_adjacent(U, var, ssq, T, F, round_, u):
+  """One exchange round over a temperature ladder T [R] (coldest first):
+  pairs r with r % 2 == round % 2 evaluate the rule of solver.py:278-291
+  (log_s = dbeta (U_r - U_{r+1} - dbeta ssq_r / F); exchange unless
+  log u_r < log_s).  Returns (flags [R-1], U', var', log_s)."""
+  U = np.array(U, np.float64)
+  var = np.array(var, np.float64)
+  R = U.size
+  flags = np.zeros(R - 1, np.int32)
+  log_s = np.zeros(R - 1)
+  for r in range(round_ % 2, R - 1, 2):
+    dbeta = 1.0 / T[r] - 1.0 / T[r + 1]
+    log_s[r] = dbeta * (U[r] - U[r + 1] - dbeta * ssq[r] / F)
+    flags[r] = 0 if math.log(u[r]) < log_s[r] else 1
+  for r in np.nonzero(flags)[0]:
+    U[[r, r + 1]] = U[[r + 1, r]]
+    var[[r, r + 1]] = var[[r + 1, r]]
+  return flags, U, var, log_s
+
+
 # ---------------------------------------------------------------------------
 # Scheduler
 # ---------------------------------------------------------------------------
