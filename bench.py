@@ -495,6 +495,100 @@ def run_mlp_reference(args):
               "d2h_bytes_per_step": 0}}), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# reSGLD workload: 32 replicas of SGLD on the same network, temperatures
+# 100^(r/31), minibatch sizes drawn uniformly from 64..4096, exchange
+# attempts between adjacent replicas every 50 steps.
+# ---------------------------------------------------------------------------
+RE_REPLICAS, RE_EVERY = 32, 50
+RE_WORKLOAD = ("reSGLD on the MLP regression model: 32 replicas at T_r = 100^(r/31), "
+               "minibatch n_r ~ U{64..4096} per replica, adjacent exchange every "
+               "50 steps (FP64 log-ratio), SGLD with RMSprop")
+
+
+def resgld_sizes():
+  return np.random.default_rng(20261203 + 4).integers(64, 4097, size=RE_REPLICAS)
+
+
+def run_resgld(args):
+  import torch
+  from gbsgmc import engine, likelihoods as L, potential, data
+  rank, world, local = dist_env()
+  torch.cuda.set_device(local)
+  lik, X, y, inits = mlp_data()
+  ds = data.NumpyDataLoader(x=X, y=y).device_dataset()
+  pot = potential.minibatch_potential(L.GaussianPrior(1.0), lik)
+  rows = resgld_sizes().astype(np.int32)
+  n_max = int((rows.max() + 127) // 128 * 128)
+  ladder = (100.0 ** (np.arange(RE_REPLICAS) / (RE_REPLICAS - 1))).astype(np.float32)
+  steps = max(RE_EVERY, args.steps // RE_EVERY * RE_EVERY)
+  warm = RE_EVERY
+  total = warm + steps
+  h = torch.full((total,), 1e-5, dtype=torch.float32, device="cuda")
+  t = torch.ones(total, dtype=torch.float32, device="cuda")
+  Xd = torch.from_numpy(inits[:RE_REPLICAS].copy()).cuda()
+  Vd = torch.ones_like(Xd)   # RMSprop preconditioner (alpha 0.9, lambda 1e-5)
+  words = np.array([pcg_words(RE_REPLICAS * rank + c) for c in range(RE_REPLICAS)],
+                   np.uint64).view(np.int64)
+  pcg = torch.from_numpy(words.copy()).cuda()
+  plan = engine.ResgldPlan(pot, ds, Xd, Vd, rows, n_max, ladder, h, t,
+                           engine.IndexSource(pcg=pcg, chain_base=RE_REPLICAS * rank),
+                           noise_seed=11, swap_seed=12, every=RE_EVERY)
+  plan.run(0, warm)
+  torch.cuda.synchronize()
+  clocks = Clocks(local)
+  clocks.start()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record()
+  plan.run(warm, steps)
+  e1.record()
+  torch.cuda.synchronize()
+  clk = clocks.stop()
+  ms = e0.elapsed_time(e1)
+  plan.check_status()
+  finite = bool(torch.isfinite(Xd).all().item())
+  exchanges = int(plan.counts.sum().item())
+  value = world * RE_REPLICAS * steps / (ms / 1e3)
+  launches = plan.launches(steps)
+  plan.close()
+  # The ragged batched gradient alone.
+  idx = torch.randint(0, MLP_N, (RE_REPLICAS, n_max), dtype=torch.int32, device="cuda")
+  rows_d = torch.from_numpy(rows).cuda()
+  for _ in range(3):
+    pot.evaluate(Xd, idx, ds, grad=True, rows=rows_d)
+  torch.cuda.synchronize()
+  g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  g0.record()
+  for _ in range(10):
+    pot.evaluate(Xd, idx, ds, grad=True, rows=rows_d)
+  g1.record()
+  torch.cuda.synchronize()
+  grad_ms = g0.elapsed_time(g1) / 10
+  flops = 6.0 * float(rows.sum()) * MLP_PMATMUL
+  peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+      if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+  peak = peaks.get("bf16_tflops_sustained", 1700.0)
+  achieved = flops / (grad_ms / 1e3) / 1e12
+  if rank == 0:
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 GEMMs, f32 state, f64 exchange",
+        "data": "synthetic (teacher MLP targets, numpy default_rng(20261206))",
+        "config": {"workload": RE_WORKLOAD, "replicas": RE_REPLICAS,
+                   "minibatch_sizes": rows.tolist(), "sum_minibatch": int(rows.sum()),
+                   "exchange_every": RE_EVERY, "exchanges_accepted": exchanges,
+                   "graph_block_steps": 50},
+        "gpu_launches": launches,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": "measured bf16_tflops_sustained",
+                     "kernel": "ragged batched value-and-gradient, 32 replicas",
+                     "kernel_ms": grad_ms, "algorithmic_flop_per_launch": flops},
+        "clocks": clk, "finite": finite}), flush=True)
+
+
 def mlp_kernel_only(args):
   """`--steps` batched value-and-gradient calls of the 64-chain workload and
   nothing else (a short run for profilers); no JSON line."""
@@ -670,15 +764,21 @@ def main():
   ap.add_argument("--steps", type=int, default=K_CONFIG)
   ap.add_argument("--warmup", type=int, default=5)
   ap.add_argument("--impl", default="gbsgmc", choices=["gbsgmc", "reference"])
-  ap.add_argument("--workload", default="logistic", choices=["logistic", "mlp"],
+  ap.add_argument("--workload", default="logistic",
+                  choices=["logistic", "mlp", "resgld"],
                   help="logistic: 256-chain SGLD headline; mlp: 64-chain OBABO "
-                       "on the tanh network")
+                       "on the tanh network; resgld: 32-replica exchange on it")
   ap.add_argument("--kernel-only", action="store_true",
                   help="short run of the fused kernel for profilers; no JSON line")
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error("--warmup must be at least 3")
-  if args.workload == "mlp":
+  if args.workload == "resgld":
+    if args.impl == "reference":
+      run_mlp_reference(args)
+    else:
+      run_resgld(args)
+  elif args.workload == "mlp":
     if args.impl == "reference":
       run_mlp_reference(args)
     elif args.kernel_only:
