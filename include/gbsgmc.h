@@ -375,6 +375,43 @@ int gbsgmc_mlp_value_and_grad_ragged(const gbsgmc_mlp* model, int chains,
                                      int* status_dev, gbsgmc_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Convolutional classifier with a softmax likelihood (CNN)                  */
+/* ------------------------------------------------------------------------ */
+
+/* x [32,32,3] -> conv3x3(32) ReLU maxpool2 -> conv3x3(64) ReLU maxpool2 ->
+ * conv3x3(128) ReLU maxpool2 -> flatten (h, w, c) -> dense(10), SAME padding;
+ * lk = logits[label] - logsumexp(logits).  Flat parameters (sorted ravel of
+ * {conv1: {b, w}, conv2: {b, w}, conv3: {b, w}, linear: {b, w}}, w in HWIO
+ * and [in, out]): b1 | W1 | b2 | W2 | b3 | W3 | bd | Wd, P = 113,738.
+ * Image of row r: X[r*ld .. r*ld + 3072) (NHWC floats); its label (a class
+ * index stored as a float) at labels[r*label_ld]. */
+typedef struct gbsgmc_cnn {
+  int64_t n_obs, n_rows, ld;
+  const float* X;
+  const float* labels;
+  int64_t label_ld;
+  float prior_scale, temperature;
+} gbsgmc_cnn;
+
+int64_t gbsgmc_cnn_param_count(void);
+/* n must be even. */
+size_t gbsgmc_cnn_workspace_bytes(int chains, int n);
+
+/* As gbsgmc_glm_value_and_grad for the CNN: U[c], grad[c] (may be NULL),
+ * lk[c, i] (may be NULL) and lk_var[c] for chains whose parameters are the
+ * rows of w [chains, P].  The convolutions run as BF16 GEMMs with fp32
+ * accumulation on the tensor cores.  Replaces minibatch_potential
+ * (jax_sgmc/potential.py:159-214) under jax.value_and_grad for a
+ * classifier likelihood such as examples/cifar.md:203-210. */
+int gbsgmc_cnn_value_and_grad(const gbsgmc_cnn* model, int chains, int n,
+                              const int32_t* idx_dev, int64_t idx_stride,
+                              const float* mask_dev, const float* w_dev,
+                              double* U_dev, float* grad_dev, float* lk_dev,
+                              double* lk_var_dev, void* workspace_dev,
+                              size_t workspace_bytes, int* status_dev,
+                              gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* Fused SGLD step for the generalised-linear families                       */
 /* ------------------------------------------------------------------------ */
 
@@ -489,6 +526,15 @@ typedef struct gbsgmc_integrator {
  * (jax_sgmc/solver.py:152-185) over alias.sgld / obabo / sghmc
  * (jax_sgmc/alias.py) for this likelihood. */
 int gbsgmc_mlp_plan_create(gbsgmc_plan** plan, const gbsgmc_mlp* model,
+                           int chains, int n, const gbsgmc_integrator* integrator,
+                           float* x_dev, float* aux_dev,
+                           const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                           const gbsgmc_index_src* index_src, double* U_dev,
+                           double* lk_var_dev, double* ke_dev, int block_steps,
+                           int* status_dev);
+
+/* As gbsgmc_mlp_plan_create for the CNN classifier (n even). */
+int gbsgmc_cnn_plan_create(gbsgmc_plan** plan, const gbsgmc_cnn* model,
                            int chains, int n, const gbsgmc_integrator* integrator,
                            float* x_dev, float* aux_dev,
                            const gbsgmc_sched* sched, const gbsgmc_noise* noise,

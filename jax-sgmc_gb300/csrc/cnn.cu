@@ -1,0 +1,770 @@
+// Convolutional classifier with a softmax likelihood: U, dU/dw, lk and
+// var(lk) for many chains at once, the convolutions as GEMMs on the tcgen05
+// tensor cores.
+//
+// Network (NHWC, SAME padding, stride 1):
+//   x [32,32,3] -> conv3x3 32 + b, ReLU, 2x2 max-pool -> [16,16,32]
+//               -> conv3x3 64 + b, ReLU, 2x2 max-pool -> [8,8,64]
+//               -> conv3x3 128 + b, ReLU, 2x2 max-pool -> [4,4,128]
+//               -> flatten (h, w, c) 2048 -> dense 10 -> logits
+//   lk = logits[label] - logsumexp(logits)   (the negative softmax cross
+//   entropy of the reference's classifier example, examples/cifar.md:203-210)
+// Flat parameters: the sorted ravel of {conv1: {b, w}, conv2: {b, w},
+// conv3: {b, w}, linear: {b, w}} with w in HWIO / [in, out] layout:
+//   b1 32 | W1 [3,3,3,32] | b2 64 | W2 [3,3,32,64] | b3 128 | W3 [3,3,64,128]
+//   | bd 10 | Wd [2048,10],   P = 113,738.
+//
+// Each convolution is a GEMM over an im2col matrix Col [pixels, K] with K
+// ordered (kh, kw, ci) and zero-padded to a multiple of 64:
+//   forward  Y = ReLU(Col W + b)          A = Col (K-major), B = W (HWIO rows
+//                                         = K, MN-major)
+//   weights  dW = dY^T Col                 both MN-major; written into the
+//                                         HWIO gradient directly
+//   inputs   dCol = dY W^T                 A = dY (K-major), B = W (K-major)
+// then col2im (the 9-tap sum), the pooling's argmax routing and the ReLU
+// mask in one pass.  The ReLU outputs are kept in fp32 so that the pooling
+// picks its maximum from unrounded values; everything a GEMM reads is BF16.  Channel and K padding come from the tensor maps'
+// out-of-bounds zero fill; epilogues drop rows and columns past the real
+// extents.  The dense layer, softmax and their adjoints are small and run on
+// the CUDA cores in fp32.
+#include <cuda_bf16.h>
+
+#include <cmath>
+
+#include "common.cuh"
+#include "internal.h"
+#include "tc_gemm.cuh"
+
+namespace gbsgmc {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kImg = 32, kInC = 3, kClasses = 10;
+constexpr int kC1 = 32, kC2 = 64, kC3 = 128;
+constexpr int kFlat = 4 * 4 * kC3;  // 2048
+constexpr int kK1 = 27, kK1p = 64;  // im2col widths (real, padded)
+constexpr int kK2 = 9 * kC1, kK2p = 320;
+constexpr int kK3 = 9 * kC2, kK3p = 576;
+constexpr int kA1ld = 64;  // conv1 output channels as stored (32 real)
+
+// Offsets of the leaves in a chain's flat parameter vector.
+constexpr int64_t ob1 = 0, oW1 = ob1 + kC1, ob2 = oW1 + kK1 * kC1, oW2 = ob2 + kC2,
+                  ob3 = oW2 + kK2 * kC2, oW3 = ob3 + kC3, obd = oW3 + kK3 * kC3,
+                  oWd = obd + kClasses, kP = oWd + kFlat * kClasses;
+static_assert(kP == 113738, "parameter count");
+
+struct CnnLayout {
+  size_t w1b, w2b, w3b;               // BF16 HWIO copies
+  size_t col1, p1, col2, p2, col3, p3;  // BF16 GEMM operands
+  size_t a1, a2, a3;                  // fp32 pre-pool activations (ReLU output)
+  size_t dy1, dy2, dy3;               // BF16 output gradients of the convs
+  size_t m1, m2, m3;                  // uint8 argmax of each pool window
+  size_t dcol3, dcol2;                // BF16 input-gradient columns
+  size_t labels;                      // int32
+  size_t dp3, gl;                     // fp32 dP3 [n, 2048], dlogits [n, 10]
+  size_t psq, plk;                    // fp64 partial sums
+  size_t total;
+};
+
+constexpr int kPrepBlocks = 64;  // Σw² partial sums per chain
+
+CnnLayout cnn_layout(int chains, int n) {
+  CnnLayout L;
+  size_t off = 0;
+  auto take = [&](size_t per_chain) {
+    const size_t at = off;
+    off += (per_chain * static_cast<size_t>(chains) + 255) & ~static_cast<size_t>(255);
+    return at;
+  };
+  const size_t N = n;
+  L.w1b = take(2 * kK1 * kC1);
+  L.w2b = take(2 * kK2 * kC2);
+  L.w3b = take(2 * kK3 * kC3);
+  L.col1 = take(2 * N * 1024 * kK1p);
+  L.a1 = take(4 * N * 1024 * kA1ld);
+  L.dy1 = take(2 * N * 1024 * kA1ld);
+  L.p1 = take(2 * N * 256 * kC1);
+  L.col2 = take(2 * N * 256 * kK2p);
+  L.a2 = take(4 * N * 256 * kC2);
+  L.dy2 = take(2 * N * 256 * kC2);
+  L.p2 = take(2 * N * 64 * kC2);
+  L.col3 = take(2 * N * 64 * kK3p);
+  L.a3 = take(4 * N * 64 * kC3);
+  L.dy3 = take(2 * N * 64 * kC3);
+  L.p3 = take(2 * N * 16 * kC3);
+  L.m1 = take(N * 256 * kC1);
+  L.m2 = take(N * 64 * kC2);
+  L.m3 = take(N * 16 * kC3);
+  L.dcol3 = take(2 * N * 64 * kK3p);
+  L.dcol2 = take(2 * N * 256 * kK2p);
+  L.labels = take(4 * N);
+  L.dp3 = take(4 * N * kFlat);
+  L.gl = take(4 * N * kClasses);
+  L.psq = take(8 * kPrepBlocks);
+  L.plk = take(8 * 4 * N);
+  L.total = off;
+  return L;
+}
+
+struct CnnArgs {
+  int chains, n, want_grad;
+  int64_t n_obs, n_rows, ld;
+  const float* X;       // image rows: 3072 floats (32x32x3 NHWC) at X + row*ld
+  const float* labels;  // label of row r at labels[r * label_ld]
+  int64_t label_ld;
+  const float* mask;
+  const int32_t* idx;
+  int64_t idx_stride;
+  const float* w;
+  float prior_scale, temperature;
+  double* U;
+  float* grad;
+  float* lk;
+  double* lk_var;
+  int* status;
+  bf16 *w1b, *w2b, *w3b, *col1, *p1, *col2, *p2, *col3, *p3, *dcol3, *dcol2;
+  float *a1, *a2, *a3;
+  bf16 *dy1, *dy2, *dy3;
+  uint8_t *m1, *m2, *m3;
+  int32_t* lab;
+  float *dp3, *gl;
+  double *psq, *plk;
+};
+
+__device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
+
+// ---------------------------------------------------------------------------
+// Weights to BF16 (HWIO layout unchanged) and partial sums of squares.
+// Grid (kPrepBlocks, chains).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) cnn_prep_kernel(const CnnArgs a) {
+  __shared__ double red[32];
+  const int c = blockIdx.y;
+  const float* w = a.w + static_cast<int64_t>(c) * kP;
+  float sq = 0.f;
+  for (int64_t i = blockIdx.x * 256 + threadIdx.x; i < kP; i += kPrepBlocks * 256) {
+    const float v = __ldg(w + i);
+    sq = fmaf(v, v, sq);
+    if (i >= oW1 && i < ob2)
+      a.w1b[static_cast<int64_t>(c) * kK1 * kC1 + (i - oW1)] = __float2bfloat16_rn(v);
+    else if (i >= oW2 && i < ob3)
+      a.w2b[static_cast<int64_t>(c) * kK2 * kC2 + (i - oW2)] = __float2bfloat16_rn(v);
+    else if (i >= oW3 && i < obd)
+      a.w3b[static_cast<int64_t>(c) * kK3 * kC3 + (i - oW3)] = __float2bfloat16_rn(v);
+  }
+  const double tot = block_sum(static_cast<double>(sq), red);
+  if (threadIdx.x == 0) a.psq[c * kPrepBlocks + blockIdx.x] = tot;
+}
+
+// ---------------------------------------------------------------------------
+// Gather of the minibatch images straight into conv1's im2col matrix
+// Col1 [n*1024, 64] (K = (kh, kw, ci), 27 real), plus labels.
+// Grid (n*1024/256, chains): one thread per output pixel.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
+  const int c = blockIdx.y;
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (p >= static_cast<int64_t>(a.n) * 1024) return;
+  const int i = static_cast<int>(p >> 10), hw = static_cast<int>(p & 1023);
+  const int h = hw >> 5, wq = hw & 31;
+  int64_t o = a.idx[static_cast<int64_t>(c) * a.idx_stride + i];
+  if (o < 0 || o >= a.n_rows) {
+    raise_status(a.status, GBSGMC_ERR_INDEX);
+    o = 0;
+  }
+  if (hw == 0) {
+    const float lf = __ldg(a.labels + o * a.label_ld);
+    int lab = static_cast<int>(lf);
+    if (!(lf >= 0.f) || lab >= kClasses) {
+      raise_status(a.status, GBSGMC_ERR_INDEX);
+      lab = 0;
+    }
+    a.lab[static_cast<int64_t>(c) * a.n + i] = lab;
+  }
+  const float* img = a.X + o * a.ld;
+  uint32_t out[kK1p / 2];
+  float v[kK1p];
+#pragma unroll
+  for (int k = 0; k < kK1p; ++k) v[k] = 0.f;
+#pragma unroll
+  for (int kh = 0; kh < 3; ++kh)
+#pragma unroll
+    for (int kw = 0; kw < 3; ++kw) {
+      const int y = h + kh - 1, x = wq + kw - 1;
+      if (y >= 0 && y < kImg && x >= 0 && x < kImg) {
+#pragma unroll
+        for (int ci = 0; ci < kInC; ++ci)
+          v[(kh * 3 + kw) * kInC + ci] = __ldg(img + (y * kImg + x) * kInC + ci);
+      }
+    }
+#pragma unroll
+  for (int k = 0; k < kK1p / 2; ++k) {
+    const __nv_bfloat162 pr = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    out[k] = *reinterpret_cast<const uint32_t*>(&pr);
+  }
+  uint4* dst = reinterpret_cast<uint4*>(a.col1 + (static_cast<int64_t>(c) * a.n * 1024 + p) * kK1p);
+#pragma unroll
+  for (int k = 0; k < kK1p / 8; ++k)
+    dst[k] = make_uint4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+}
+
+// ---------------------------------------------------------------------------
+// 2x2 max-pool: A [n, H, W, ld] (C real channels) -> P [n, H/2, W/2, C] and
+// the argmax (0..3, row-major in the window, first maximum) per output.
+// One thread per output element.  Grid (ceil(n*H*W*C/4 / 256), chains).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pout, uint8_t* M,
+                                                      int n, int H, int W, int C, int ld) {
+  const int c = blockIdx.y;
+  const int Ho = H / 2, Wo = W / 2;
+  const int64_t per = static_cast<int64_t>(n) * Ho * Wo * C;
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (e >= per) return;
+  const int ch = static_cast<int>(e % C);
+  const int64_t pix = e / C;
+  const int x = static_cast<int>(pix % Wo), y = static_cast<int>((pix / Wo) % Ho);
+  const int64_t i = pix / (static_cast<int64_t>(Wo) * Ho);
+  const float* src = A + (static_cast<int64_t>(c) * n * H * W + (i * H + 2 * y) * W + 2 * x) * ld + ch;
+  float best = src[0];
+  int arg = 0;
+  const float v1 = src[ld], v2 = src[static_cast<int64_t>(W) * ld],
+              v3 = src[static_cast<int64_t>(W) * ld + ld];
+  if (v1 > best) { best = v1; arg = 1; }
+  if (v2 > best) { best = v2; arg = 2; }
+  if (v3 > best) { best = v3; arg = 3; }
+  Pout[static_cast<int64_t>(c) * per + e] = __float2bfloat16_rn(best);
+  M[static_cast<int64_t>(c) * per + e] = static_cast<uint8_t>(arg);
+}
+
+// ---------------------------------------------------------------------------
+// im2col of a pooled map P [n, H, W, C] -> Col [n*H*W, Kp], K = (kh, kw, ci)
+// (9C real).  One thread per 8 consecutive K entries (C is a multiple of 8).
+// Grid (ceil(n*H*W*Kp/8 / 256), chains).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) cnn_im2col_kernel(const bf16* Pin, bf16* Col, int n,
+                                                        int H, int W, int C, int Kp) {
+  const int c = blockIdx.y;
+  const int64_t groups = static_cast<int64_t>(n) * H * W * (Kp / 8);
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (e >= groups) return;
+  const int k0 = static_cast<int>(e % (Kp / 8)) * 8;
+  const int64_t pix = e / (Kp / 8);
+  const int x = static_cast<int>(pix % W), y = static_cast<int>((pix / W) % H);
+  const int64_t i = pix / (static_cast<int64_t>(W) * H);
+  uint4 v = make_uint4(0, 0, 0, 0);
+  if (k0 < 9 * C) {
+    const int tap = k0 / C, ci = k0 % C;
+    const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+    if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+      v = *reinterpret_cast<const uint4*>(
+          Pin + (static_cast<int64_t>(c) * n * H * W + (i * H + yy) * W + xx) * C + ci);
+  }
+  reinterpret_cast<uint4*>(Col + static_cast<int64_t>(c) * n * H * W * Kp)[e] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Dense layer, softmax likelihood and its adjoint: one block of 128 threads
+// per (image, chain).  Writes lk, dlogits g = dU/dlogits (fp32), dP3 = g Wd^T
+// and the per-image likelihood terms.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) cnn_dense_kernel(const CnnArgs a) {
+  __shared__ float part[kClasses][4];
+  __shared__ float g_s[kClasses];
+  const int i = blockIdx.x, c = blockIdx.y, t = threadIdx.x;
+  const float* w = a.w + static_cast<int64_t>(c) * kP;
+  const bf16* x = a.p3 + (static_cast<int64_t>(c) * a.n + i) * kFlat;
+  float acc[kClasses];
+#pragma unroll
+  for (int k = 0; k < kClasses; ++k) acc[k] = 0.f;
+  for (int f = t; f < kFlat; f += 128) {
+    const float xv = bf(x[f]);
+    const float* wr = w + oWd + static_cast<int64_t>(f) * kClasses;
+#pragma unroll
+    for (int k = 0; k < kClasses; ++k) acc[k] = fmaf(xv, __ldg(wr + k), acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < kClasses; ++k) {
+    const float s = warp_sum(acc[k]);
+    if ((t & 31) == 0) part[k][t >> 5] = s;
+  }
+  __syncthreads();
+  if (t == 0) {
+    float logit[kClasses], mx = -INFINITY;
+    for (int k = 0; k < kClasses; ++k) {
+      logit[k] = part[k][0] + part[k][1] + part[k][2] + part[k][3] + __ldg(w + obd + k);
+      mx = fmaxf(mx, logit[k]);
+    }
+    float se = 0.f;
+    for (int k = 0; k < kClasses; ++k) se += expf(logit[k] - mx);
+    const float lse = mx + logf(se);
+    const int lab = a.lab[static_cast<int64_t>(c) * a.n + i];
+    const float lk = logit[lab] - lse;
+    const float m = a.mask != nullptr ? __ldg(a.mask + static_cast<int64_t>(c) * a.n + i) : 1.f;
+    const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n / a.temperature);
+    for (int k = 0; k < kClasses; ++k) {
+      const float pk = expf(logit[k] - lse);
+      const float g = -scale * m * ((k == lab ? 1.f : 0.f) - pk);
+      g_s[k] = g;
+      a.gl[(static_cast<int64_t>(c) * a.n + i) * kClasses + k] = g;
+    }
+    if (a.lk != nullptr) a.lk[static_cast<int64_t>(c) * a.n + i] = lk;
+    double* pl = a.plk + (static_cast<int64_t>(c) * a.n + i) * 4;
+    pl[0] = static_cast<double>(m) * lk;
+    pl[1] = lk;
+    pl[2] = static_cast<double>(lk) * lk;
+    pl[3] = 0.0;
+  }
+  if (!a.want_grad) return;
+  __syncthreads();
+  float* dx = a.dp3 + (static_cast<int64_t>(c) * a.n + i) * kFlat;
+  for (int f = t; f < kFlat; f += 128) {
+    const float* wr = w + oWd + static_cast<int64_t>(f) * kClasses;
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kClasses; ++k) s = fmaf(g_s[k], __ldg(wr + k), s);
+    dx[f] = s;
+  }
+}
+
+// dWd [2048, 10] = sum_i P3_i (x) g_i and dbd = sum_i g_i (likelihood part).
+// Grid (kFlat / 128 + 1, chains), 128 threads.
+__global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
+  const int c = blockIdx.y;
+  float* g = a.grad + static_cast<int64_t>(c) * kP;
+  const float* gl = a.gl + static_cast<int64_t>(c) * a.n * kClasses;
+  if (blockIdx.x == kFlat / 128) {
+    if (threadIdx.x < kClasses) {
+      float s = 0.f;
+      for (int i = 0; i < a.n; ++i) s += gl[i * kClasses + threadIdx.x];
+      g[obd + threadIdx.x] = s;
+    }
+    return;
+  }
+  const int f = blockIdx.x * 128 + threadIdx.x;
+  const bf16* x = a.p3 + static_cast<int64_t>(c) * a.n * kFlat + f;
+  float acc[kClasses];
+#pragma unroll
+  for (int k = 0; k < kClasses; ++k) acc[k] = 0.f;
+  for (int i = 0; i < a.n; ++i) {
+    const float xv = bf(x[static_cast<int64_t>(i) * kFlat]);
+#pragma unroll
+    for (int k = 0; k < kClasses; ++k) acc[k] = fmaf(xv, gl[i * kClasses + k], acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < kClasses; ++k) g[oWd + static_cast<int64_t>(f) * kClasses + k] = acc[k];
+}
+
+// ---------------------------------------------------------------------------
+// Pool-window routing + ReLU mask of the fp32 pre-pool activations A:
+// dY[i, y, x, ch] = (argmax of its window == this position) * dP * (A > 0).
+// dP is read either directly (fp32 dp, layer 3) or as the 9-tap col2im sum of
+// the next layer's dCol [n*Hn*Wn, Kp] (Hn = H/2).  One thread per element of
+// A [n, H, W, ld]; channels ch >= C are zeroed.  Grid (ceil(n*H*W*ld/256),
+// chains).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) cnn_unpool_kernel(const float* A, bf16* dY,
+                                                        const uint8_t* M, const float* dp,
+                                                        const bf16* dcol, int n, int H, int W,
+                                                        int C, int ld, int Kp) {
+  const int c = blockIdx.y;
+  const int64_t per = static_cast<int64_t>(n) * H * W * ld;
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (e >= per) return;
+  const int ch = static_cast<int>(e % ld);
+  const int64_t pix = e / ld;
+  const int x = static_cast<int>(pix % W), y = static_cast<int>((pix / W) % H);
+  const int64_t i = pix / (static_cast<int64_t>(W) * H);
+  const float act = A[static_cast<int64_t>(c) * per + e];
+  float out = 0.f;
+  if (ch < C) {
+    const int Ho = H / 2, Wo = W / 2, py = y >> 1, px = x >> 1;
+    const int64_t pe = ((i * Ho + py) * Wo + px) * C + ch;
+    const int64_t pper = static_cast<int64_t>(n) * Ho * Wo * C;
+    const int arg = (y & 1) * 2 + (x & 1);
+    if (M[static_cast<int64_t>(c) * pper + pe] == arg && act > 0.f) {
+      if (dp != nullptr) {
+        out = dp[static_cast<int64_t>(c) * pper + pe];
+      } else {
+        // dP[i, py, px, ch] = sum over taps of dCol at the output pixel
+        // (py - kh + 1, px - kw + 1), column (kh, kw, ch).
+        const bf16* dc = dcol + static_cast<int64_t>(c) * n * Ho * Wo * Kp;
+        float s = 0.f;
+#pragma unroll
+        for (int kh = 0; kh < 3; ++kh)
+#pragma unroll
+          for (int kw = 0; kw < 3; ++kw) {
+            const int oy = py - kh + 1, ox = px - kw + 1;
+            if (oy >= 0 && oy < Ho && ox >= 0 && ox < Wo)
+              s += bf(dc[((i * Ho + oy) * Wo + ox) * Kp + (kh * 3 + kw) * C + ch]);
+          }
+        out = s;
+      }
+    }
+  }
+  dY[static_cast<int64_t>(c) * per + e] = __float2bfloat16_rn(out);
+}
+
+// Column sums of dY [rows, ld] over a chain's rows (bias gradients), C real
+// channels.  Grid (C, chains), 256 threads.
+__global__ void __launch_bounds__(256) cnn_bias_grad_kernel(const bf16* dY, int64_t rows,
+                                                           int ld, float* grad, int64_t off) {
+  __shared__ double red[32];
+  const int ch = blockIdx.x, c = blockIdx.y;
+  const bf16* src = dY + static_cast<int64_t>(c) * rows * ld + ch;
+  float s = 0.f;
+  for (int64_t r = threadIdx.x; r < rows; r += 256) s += bf(src[r * ld]);
+  const double tot = block_sum(static_cast<double>(s), red);
+  if (threadIdx.x == 0) grad[static_cast<int64_t>(c) * kP + off + ch] = static_cast<float>(tot);
+}
+
+// grad += w / (s^2 T) over every parameter; U and var(lk).  Grid
+// (ceil(P/256), chains); block 0 of a chain also writes U, var.
+__global__ void __launch_bounds__(256) cnn_finalize_kernel(const CnnArgs a, float pf) {
+  __shared__ double red[32];
+  const int c = blockIdx.y, t = threadIdx.x;
+  const float* w = a.w + static_cast<int64_t>(c) * kP;
+  if (a.want_grad && pf != 0.f) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * 256 + t;
+    if (j < kP) {
+      float* g = a.grad + static_cast<int64_t>(c) * kP + j;
+      *g = fmaf(pf, __ldg(w + j), *g);
+    }
+  }
+  if (blockIdx.x != 0) return;
+  double sq = 0.0, lm = 0.0, l1 = 0.0, l2 = 0.0;
+  for (int i = t; i < kPrepBlocks; i += 256) sq += a.psq[c * kPrepBlocks + i];
+  for (int i = t; i < a.n; i += 256) {
+    const double* p = a.plk + (static_cast<int64_t>(c) * a.n + i) * 4;
+    lm += p[0];
+    l1 += p[1];
+    l2 += p[2];
+  }
+  sq = block_sum(sq, red);
+  lm = block_sum(lm, red);
+  l1 = block_sum(l1, red);
+  l2 = block_sum(l2, red);
+  if (t != 0) return;
+  double log_prior = 0.0;
+  if (a.prior_scale > 0.f) {
+    const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;
+    log_prior = -0.5 * sq / s2 -
+                static_cast<double>(kP) * (log(static_cast<double>(a.prior_scale)) +
+                                           0.91893853320467274178);
+  }
+  const double U = (-static_cast<double>(a.n_obs) * (lm / a.n) - log_prior) / a.temperature;
+  a.U[c] = U;
+  if (a.lk_var != nullptr) {
+    const double mean = l1 / a.n;
+    a.lk_var[c] = fmax(l2 / a.n - mean * mean, 0.0);
+  }
+  if (!isfinite(U)) raise_status(a.status, GBSGMC_ERR_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// GEMM epilogues.
+// ---------------------------------------------------------------------------
+
+// Stores 32 BF16 columns of the warp's 32 rows: lane l holds its row's 16
+// packed pairs w[16]; through the staging tile, each store instruction writes
+// 64 contiguous bytes of two rows.  dst points at (row0, first column) as
+// 32-bit words, rows ld_words apart.
+__device__ __forceinline__ void store_block32(uint32_t* dst, int64_t ld_words,
+                                              const uint32_t (&w)[16], uint32_t* st) {
+  const int lane = epi::lane_id(), h = lane >> 4, l = lane & 15;
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 16; ++j) st[lane * 33 + j] = w[j];
+  __syncwarp();
+#pragma unroll 4
+  for (int rr = 0; rr < 16; ++rr) {
+    const int r = 2 * rr + h;
+    dst[r * ld_words + l] = st[r * 33 + l];
+  }
+}
+
+// Forward: Y = ReLU(acc + b) in fp32 into [rows, ldo]; columns >= C get 0.
+// (fp32 so that the pooling's maximum is taken over unrounded values.)
+struct EpiConvRelu {
+  const float* w;
+  int64_t boff;
+  int C, ldo;
+  int64_t rows;  // rows per chain
+  float* y;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    const float* bias = w + b * kP + boff;
+    float* dst = y + (b * rows + row0) * ldo + col0 + epi::lane_id();
+#pragma unroll 1
+    for (int cb = 0; cb < NC / 32; ++cb) {
+      float v[32];
+      uint32_t u[32];
+      load(cb, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int k = col0 + 32 * cb + j;
+        u[j] = __float_as_uint(k < C ? fmaxf(v[j] + __ldg(bias + k), 0.f) : 0.f);
+      }
+      epi::put_rows(st, u);
+#pragma unroll 4
+      for (int r = 0; r < 32; ++r) dst[r * ldo + 32 * cb] = __uint_as_float(epi::get(st, r));
+    }
+  }
+};
+
+// Weights: element (row = output channel co, col = im2col column k) of dW
+// lands at grad[b*P + off + k*Cout + co] (HWIO), rows < Cout, cols < K.
+struct EpiConvGradW {
+  float* grad;
+  int64_t off;
+  int Cout, K;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t*) const {
+    const int co = row0 + epi::lane_id();
+    float* dst = grad + b * kP + off + co;
+#pragma unroll 1
+    for (int cb = 0; cb < NC / 32; ++cb) {
+      float v[32];
+      load(cb, v);
+      if (co < Cout) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int k = col0 + 32 * cb + j;
+          if (k < K) dst[static_cast<int64_t>(k) * Cout] = v[j];
+        }
+      }
+    }
+  }
+};
+
+// dCol as BF16 into [rows, ldo] (all columns < ldo).
+struct EpiStoreBf16 {
+  bf16* y;
+  int ldo;
+  int64_t rows;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    uint32_t* dst = reinterpret_cast<uint32_t*>(y + (b * rows + row0) * ldo + col0);
+#pragma unroll 1
+    for (int cb = 0; cb < NC / 32; ++cb) {
+      float v[32];
+      uint32_t pk[16];
+      load(cb, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        pk[j] = *reinterpret_cast<const uint32_t*>(&pr);
+      }
+      store_block32(dst + 16 * cb, ldo / 2, pk, st);
+    }
+  }
+};
+
+template <class T>
+T* view(void* ws, size_t off) {
+  return reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + off);
+}
+
+int grid1(int64_t work) { return static_cast<int>((work + 255) / 256); }
+
+int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
+  a.w1b = view<bf16>(ws, L.w1b);
+  a.w2b = view<bf16>(ws, L.w2b);
+  a.w3b = view<bf16>(ws, L.w3b);
+  a.col1 = view<bf16>(ws, L.col1);
+  a.a1 = view<float>(ws, L.a1);
+  a.dy1 = view<bf16>(ws, L.dy1);
+  a.p1 = view<bf16>(ws, L.p1);
+  a.col2 = view<bf16>(ws, L.col2);
+  a.a2 = view<float>(ws, L.a2);
+  a.dy2 = view<bf16>(ws, L.dy2);
+  a.p2 = view<bf16>(ws, L.p2);
+  a.col3 = view<bf16>(ws, L.col3);
+  a.a3 = view<float>(ws, L.a3);
+  a.dy3 = view<bf16>(ws, L.dy3);
+  a.p3 = view<bf16>(ws, L.p3);
+  a.m1 = view<uint8_t>(ws, L.m1);
+  a.m2 = view<uint8_t>(ws, L.m2);
+  a.m3 = view<uint8_t>(ws, L.m3);
+  a.dcol3 = view<bf16>(ws, L.dcol3);
+  a.dcol2 = view<bf16>(ws, L.dcol2);
+  a.lab = view<int32_t>(ws, L.labels);
+  a.dp3 = view<float>(ws, L.dp3);
+  a.gl = view<float>(ws, L.gl);
+  a.psq = view<double>(ws, L.psq);
+  a.plk = view<double>(ws, L.plk);
+  const int C = a.chains, n = a.n;
+  const int64_t r1 = int64_t(n) * 1024, r2 = int64_t(n) * 256, r3 = int64_t(n) * 64;
+  int rc;
+  auto launched = [&](const char* what) { return check_launch(what); };
+
+  cnn_prep_kernel<<<dim3(kPrepBlocks, C), 256, 0, st>>>(a);
+  if ((rc = launched("cnn_prep_kernel"))) return rc;
+  cnn_im2col1_kernel<<<dim3(grid1(r1), C), 256, 0, st>>>(a);
+  if ((rc = launched("cnn_im2col1_kernel"))) return rc;
+
+  // Tensor maps (columns, rows, chains).
+  CUtensorMap m_col1, m_w1, m_col2, m_w2, m_col3, m_w3;
+  if ((rc = make_tmap_bf16_3d(&m_col1, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, kGemmBK, kGemmBM)) ||
+      (rc = make_tmap_bf16_3d(&m_w1, a.w1b, kC1, kK1, C, kC1, kK1 * kC1, 64, 64)) ||
+      (rc = make_tmap_bf16_3d(&m_col2, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, kGemmBK, kGemmBM)) ||
+      (rc = make_tmap_bf16_3d(&m_w2, a.w2b, kC2, kK2, C, kC2, kK2 * kC2, 64, 64)) ||
+      (rc = make_tmap_bf16_3d(&m_col3, a.col3, kK3p, r3, C, kK3p, r3 * kK3p, kGemmBK, kGemmBM)) ||
+      (rc = make_tmap_bf16_3d(&m_w3, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, 64, 64)))
+    return rc;
+
+  // conv1 -> pool1 -> im2col2 -> conv2 -> pool2 -> im2col3 -> conv3 -> pool3.
+  const EpiConvRelu e1{a.w, ob1, kC1, kA1ld, r1, a.a1};
+  if ((rc = launch_gemm<64, false, true>(m_col1, m_w1, C, r1, 64, kK1p, a.status, e1, st)))
+    return rc;
+  cnn_pool_kernel<<<dim3(grid1(r2 * kC1 / 1), C), 256, 0, st>>>(a.a1, a.p1, a.m1, n, 32, 32, kC1,
+                                                                kA1ld);
+  if ((rc = launched("cnn_pool_kernel 1"))) return rc;
+  cnn_im2col_kernel<<<dim3(grid1(r2 * kK2p / 8), C), 256, 0, st>>>(a.p1, a.col2, n, 16, 16, kC1,
+                                                                   kK2p);
+  if ((rc = launched("cnn_im2col_kernel 2"))) return rc;
+  const EpiConvRelu e2{a.w, ob2, kC2, kC2, r2, a.a2};
+  if ((rc = launch_gemm<64, false, true>(m_col2, m_w2, C, r2, kC2, kK2p, a.status, e2, st)))
+    return rc;
+  cnn_pool_kernel<<<dim3(grid1(r3 * kC2), C), 256, 0, st>>>(a.a2, a.p2, a.m2, n, 16, 16, kC2, kC2);
+  if ((rc = launched("cnn_pool_kernel 2"))) return rc;
+  cnn_im2col_kernel<<<dim3(grid1(r3 * kK3p / 8), C), 256, 0, st>>>(a.p2, a.col3, n, 8, 8, kC2,
+                                                                   kK3p);
+  if ((rc = launched("cnn_im2col_kernel 3"))) return rc;
+  const EpiConvRelu e3{a.w, ob3, kC3, kC3, r3, a.a3};
+  if ((rc = launch_gemm<128, false, true>(m_col3, m_w3, C, r3, kC3, kK3p, a.status, e3, st)))
+    return rc;
+  cnn_pool_kernel<<<dim3(grid1(int64_t(n) * 16 * kC3), C), 256, 0, st>>>(a.a3, a.p3, a.m3, n, 8,
+                                                                         8, kC3, kC3);
+  if ((rc = launched("cnn_pool_kernel 3"))) return rc;
+  cnn_dense_kernel<<<dim3(n, C), 128, 0, st>>>(a);
+  if ((rc = launched("cnn_dense_kernel"))) return rc;
+
+  if (a.want_grad) {
+    cnn_dense_grad_kernel<<<dim3(kFlat / 128 + 1, C), 128, 0, st>>>(a);
+    if ((rc = launched("cnn_dense_grad_kernel"))) return rc;
+    // Layer 3: dY3 over A3, db3, dW3 = dY3^T Col3, dCol3 = dY3 W3^T.
+    cnn_unpool_kernel<<<dim3(grid1(r3 * kC3), C), 256, 0, st>>>(a.a3, a.dy3, a.m3, a.dp3, nullptr,
+                                                                n, 8, 8, kC3, kC3, 0);
+    if ((rc = launched("cnn_unpool_kernel 3"))) return rc;
+    cnn_bias_grad_kernel<<<dim3(kC3, C), 256, 0, st>>>(a.dy3, r3, kC3, a.grad, ob3);
+    if ((rc = launched("cnn_bias_grad_kernel 3"))) return rc;
+    CUtensorMap m_dy3t, m_col3t, m_dy3, m_w3k;
+    if ((rc = make_tmap_bf16_3d(&m_dy3t, a.dy3, kC3, r3, C, kC3, r3 * kC3, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_col3t, a.col3, kK3p, r3, C, kK3p, r3 * kK3p, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_dy3, a.dy3, kC3, r3, C, kC3, r3 * kC3, kGemmBK, kGemmBM)) ||
+        (rc = make_tmap_bf16_3d(&m_w3k, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, kGemmBK, 64)))
+      return rc;
+    const EpiConvGradW g3{a.grad, oW3, kC3, kK3};
+    if ((rc = launch_gemm<64, true, true>(m_dy3t, m_col3t, C, 128, kK3p, r3, a.status, g3, st)))
+      return rc;
+    const EpiStoreBf16 d3{a.dcol3, kK3p, r3};
+    if ((rc = launch_gemm<64, false, false>(m_dy3, m_w3k, C, r3, kK3p, kC3, a.status, d3, st)))
+      return rc;
+    // Layer 2.
+    cnn_unpool_kernel<<<dim3(grid1(r2 * kC2), C), 256, 0, st>>>(a.a2, a.dy2, a.m2, nullptr,
+                                                                a.dcol3, n, 16, 16, kC2, kC2,
+                                                                kK3p);
+    if ((rc = launched("cnn_unpool_kernel 2"))) return rc;
+    cnn_bias_grad_kernel<<<dim3(kC2, C), 256, 0, st>>>(a.dy2, r2, kC2, a.grad, ob2);
+    if ((rc = launched("cnn_bias_grad_kernel 2"))) return rc;
+    CUtensorMap m_dy2t, m_col2t, m_dy2, m_w2k;
+    if ((rc = make_tmap_bf16_3d(&m_dy2t, a.dy2, kC2, r2, C, kC2, r2 * kC2, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_col2t, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_dy2, a.dy2, kC2, r2, C, kC2, r2 * kC2, kGemmBK, kGemmBM)) ||
+        (rc = make_tmap_bf16_3d(&m_w2k, a.w2b, kC2, kK2, C, kC2, kK2 * kC2, kGemmBK, 64)))
+      return rc;
+    const EpiConvGradW g2{a.grad, oW2, kC2, kK2};
+    if ((rc = launch_gemm<64, true, true>(m_dy2t, m_col2t, C, 128, kK2p, r2, a.status, g2, st)))
+      return rc;
+    const EpiStoreBf16 d2{a.dcol2, kK2p, r2};
+    if ((rc = launch_gemm<64, false, false>(m_dy2, m_w2k, C, r2, kK2p, kC2, a.status, d2, st)))
+      return rc;
+    // Layer 1.
+    cnn_unpool_kernel<<<dim3(grid1(r1 * kA1ld), C), 256, 0, st>>>(a.a1, a.dy1, a.m1, nullptr,
+                                                                  a.dcol2, n, 32, 32, kC1, kA1ld,
+                                                                  kK2p);
+    if ((rc = launched("cnn_unpool_kernel 1"))) return rc;
+    cnn_bias_grad_kernel<<<dim3(kC1, C), 256, 0, st>>>(a.dy1, r1, kA1ld, a.grad, ob1);
+    if ((rc = launched("cnn_bias_grad_kernel 1"))) return rc;
+    CUtensorMap m_dy1t, m_col1t;
+    if ((rc = make_tmap_bf16_3d(&m_dy1t, a.dy1, kA1ld, r1, C, kA1ld, r1 * kA1ld, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_col1t, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, 64, 64)))
+      return rc;
+    const EpiConvGradW g1{a.grad, oW1, kC1, kK1};
+    if ((rc = launch_gemm<64, true, true>(m_dy1t, m_col1t, C, 128, kK1p, r1, a.status, g1, st)))
+      return rc;
+  }
+  const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;
+  const float pf = a.prior_scale > 0.f ? static_cast<float>(1.0 / (s2 * a.temperature)) : 0.f;
+  cnn_finalize_kernel<<<dim3(a.want_grad ? grid1(kP) : 1, C), 256, 0, st>>>(a, pf);
+  return launched("cnn_finalize_kernel");
+}
+
+}  // namespace
+}  // namespace gbsgmc
+
+using namespace gbsgmc;
+
+extern "C" int64_t gbsgmc_cnn_param_count(void) { return kP; }
+
+extern "C" size_t gbsgmc_cnn_workspace_bytes(int chains, int n) {
+  if (chains <= 0 || n <= 0 || n % 2 != 0) return 0;
+  return cnn_layout(chains, n).total;
+}
+
+extern "C" int gbsgmc_cnn_value_and_grad(const gbsgmc_cnn* model, int chains, int n,
+                                         const int32_t* idx_dev, int64_t idx_stride,
+                                         const float* mask_dev, const float* w_dev,
+                                         double* U_dev, float* grad_dev, float* lk_dev,
+                                         double* lk_var_dev, void* workspace_dev,
+                                         size_t workspace_bytes, int* status_dev,
+                                         gbsgmc_stream_t stream) {
+  if (model == nullptr || model->X == nullptr || model->labels == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: null model or data");
+  if (chains < 0 || n < 0) return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: negative size");
+  if (chains == 0) return GBSGMC_OK;
+  if (n == 0 || n % 2 != 0 || chains > 65535 || n > 65536)
+    return set_error(GBSGMC_ERR_SHAPE,
+                     "cnn_value_and_grad: n must be a positive even number (got %d)", n);
+  if (model->ld < kImg * kImg * kInC || model->label_ld < 1 || model->n_obs < 1 ||
+      model->n_rows < 0 || model->n_rows >= (1ll << 31))
+    return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: bad strides or sizes");
+  if (!(model->temperature > 0.f) || !(model->prior_scale >= 0.f))
+    return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: bad temperature or prior scale");
+  if (idx_dev == nullptr || w_dev == nullptr || U_dev == nullptr || workspace_dev == nullptr ||
+      status_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: null pointer");
+  if (idx_stride < n) return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: idx_stride < n");
+  if (reinterpret_cast<uintptr_t>(workspace_dev) % 256 != 0)
+    return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: workspace must be 256-byte aligned");
+  const CnnLayout L = cnn_layout(chains, n);
+  if (workspace_bytes < L.total)
+    return set_error(GBSGMC_ERR_ARG, "cnn_value_and_grad: workspace of %zu bytes, need %zu",
+                     workspace_bytes, L.total);
+  CnnArgs a{};
+  a.chains = chains;
+  a.n = n;
+  a.want_grad = grad_dev != nullptr;
+  a.n_obs = model->n_obs;
+  a.n_rows = model->n_rows > 0 ? model->n_rows : model->n_obs;
+  a.ld = model->ld;
+  a.X = model->X;
+  a.labels = model->labels;
+  a.label_ld = model->label_ld;
+  a.mask = mask_dev;
+  a.idx = idx_dev;
+  a.idx_stride = idx_stride;
+  a.w = w_dev;
+  a.prior_scale = model->prior_scale;
+  a.temperature = model->temperature;
+  a.U = U_dev;
+  a.grad = grad_dev;
+  a.lk = lk_dev;
+  a.lk_var = lk_var_dev;
+  a.status = status_dev;
+  return run_cnn(a, L, workspace_dev, static_cast<cudaStream_t>(stream));
+}

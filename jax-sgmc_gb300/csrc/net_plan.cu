@@ -280,6 +280,68 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
   return GBSGMC_OK;
 }
 
+extern "C" int gbsgmc_cnn_plan_create(gbsgmc_plan** out, const gbsgmc_cnn* model,
+                                      int chains, int n, const gbsgmc_integrator* integ,
+                                      float* x_dev, float* aux_dev,
+                                      const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                                      const gbsgmc_index_src* isrc, double* U_dev,
+                                      double* lk_var_dev, double* ke_dev, int block_steps,
+                                      int* status_dev) {
+  if (out == nullptr) return set_error(GBSGMC_ERR_ARG, "cnn_plan_create: null plan");
+  *out = nullptr;
+  int rc = check_common(integ, chains, n, x_dev, aux_dev, sched, noise, isrc, U_dev,
+                        block_steps, status_dev);
+  if (rc != GBSGMC_OK) return rc;
+  if (model == nullptr) return set_error(GBSGMC_ERR_ARG, "cnn_plan_create: null model");
+  const size_t ws = gbsgmc_cnn_workspace_bytes(chains, n);
+  if (ws == 0) return set_error(GBSGMC_ERR_SHAPE, "cnn_plan_create: n must be even");
+  NetPlan* p = new (std::nothrow) NetPlan();
+  if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "cnn_plan_create: out of memory");
+  p->chains = chains;
+  p->n = n;
+  p->P = gbsgmc_cnn_param_count();
+  p->rows = model->n_rows > 0 ? model->n_rows : model->n_obs;
+  p->integ = *integ;
+  p->x = x_dev;
+  p->aux = aux_dev;
+  p->sched = *sched;
+  p->noise = *noise;
+  p->isrc = *isrc;
+  p->U = U_dev;
+  p->lk_var = lk_var_dev;
+  p->ke = ke_dev;
+  p->status = status_dev;
+  p->ws_size = ws;
+  do {
+    if ((rc = plan_init(p, block_steps))) break;
+    const size_t gbytes = sizeof(float) * static_cast<size_t>(chains) * p->P;
+    const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
+                          p->draws() * n;
+    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "cnn_plan_create: gradient"))) break;
+    if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "cnn_plan_create: U")))
+      break;
+    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "cnn_plan_create: index buffer"))) break;
+    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "cnn_plan_create: workspace"))) break;
+    const gbsgmc_cnn m = *model;
+    float* grad = p->grad;
+    void* wsp = p->ws;
+    const float* x = x_dev;
+    p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
+                     const int32_t* idx, int64_t stride, double* U, double* var,
+                     cudaStream_t s) {
+      return gbsgmc_cnn_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
+                                       nullptr, var, wsp, ws, status_dev, s);
+    };
+    rc = plan_capture(p);
+  } while (false);
+  if (rc != GBSGMC_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return GBSGMC_OK;
+}
+
 extern "C" int gbsgmc_mlp_resgld_plan_create(
     gbsgmc_plan** out, const gbsgmc_mlp* model, int replicas, int n_max, const int32_t* n_dev,
     float* x_dev, float* v_dev, float alpha, float lmbd, const gbsgmc_sched* sched,

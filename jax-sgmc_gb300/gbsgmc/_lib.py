@@ -65,6 +65,13 @@ class Mlp(C.Structure):
               ("_reserved", C.c_int)]
 
 
+class Cnn(C.Structure):
+  _fields_ = [("n_obs", C.c_int64), ("n_rows", C.c_int64), ("ld", C.c_int64),
+              ("X", C.c_void_p), ("labels", C.c_void_p),
+              ("label_ld", C.c_int64), ("prior_scale", C.c_float),
+              ("temperature", C.c_float)]
+
+
 class Integrator(C.Structure):
   _fields_ = [("kind", C.c_int), ("leapfrog_steps", C.c_int),
               ("friction", C.c_float), ("alpha", C.c_float),
@@ -128,6 +135,11 @@ SIGNATURES = {
     "gbsgmc_mlp_value_and_grad_ragged": (_i, [_P(Mlp), _i, _i, _vp, _vp, _i64,
                                               _vp, _vp, _vp, _vp, _vp, _vp,
                                               _vp, _sz, _vp, _vp]),
+    "gbsgmc_cnn_param_count": (_i64, []),
+    "gbsgmc_cnn_workspace_bytes": (_sz, [_i, _i]),
+    "gbsgmc_cnn_value_and_grad": (_i, [_P(Cnn), _i, _i, _vp, _i64, _vp, _vp,
+                                       _vp, _vp, _vp, _vp, _vp, _sz, _vp,
+                                       _vp]),
     "gbsgmc_sgld_update": (_i, [_i, _i64, _vp, _vp, _vp, _f, _f, _P(Sched),
                                 _P(Noise), _vp, _vp]),
     "gbsgmc_obabo_first": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _f, _vp,
@@ -154,6 +166,9 @@ SIGNATURES = {
                                          _P(IndexSrc), _vp, _vp, _vp, _vp, _i,
                                          _vp]),
     "gbsgmc_mlp_plan_create": (_i, [_P(_vp), _P(Mlp), _i, _i, _P(Integrator),
+                                    _vp, _vp, _P(Sched), _P(Noise),
+                                    _P(IndexSrc), _vp, _vp, _vp, _i, _vp]),
+    "gbsgmc_cnn_plan_create": (_i, [_P(_vp), _P(Cnn), _i, _i, _P(Integrator),
                                     _vp, _vp, _P(Sched), _P(Noise),
                                     _P(IndexSrc), _vp, _vp, _vp, _i, _vp]),
     "gbsgmc_resgld_sa_update": (_i, [_i, _vp, _vp, _vp, _vp]),

@@ -134,9 +134,9 @@ def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
 
 
 class NetPlan:
-  """Owns a network plan (``gbsgmc_mlp_plan_create``): C chains of SGLD,
-  OBABO or SGHMC on a dense-network potential, one CUDA graph per block of
-  steps.  ``X`` [C, P] (positions) and ``AUX`` (rms_prop state, or momentum)
+  """Owns a network plan (``gbsgmc_mlp_plan_create`` or
+  ``gbsgmc_cnn_plan_create``): C chains of SGLD, OBABO or SGHMC on a network
+  potential, one CUDA graph per block of steps.  ``X`` [C, P] (positions) and ``AUX`` (rms_prop state, or momentum)
   are updated in place."""
 
   KINDS = {"langevin": _lib.INTEGRATOR_SGLD, "obabo": _lib.INTEGRATOR_OBABO,
@@ -166,7 +166,9 @@ class NetPlan:
     self.integ = _lib.Integrator(self.KINDS[kind], lf, float(friction),
                                  float(alpha), float(lmbd), 0, _lib.ptr(mass))
     handle = _lib.C.c_void_p()
-    _lib.call("gbsgmc_mlp_plan_create", _lib.C.byref(handle), self.model, C, n,
+    create = "gbsgmc_cnn_plan_create" if potential.is_cnn else \
+        "gbsgmc_mlp_plan_create"
+    _lib.call(create, _lib.C.byref(handle), self.model, C, n,
               self.integ, _lib.ptr(X), _lib.ptr(AUX), self.sched, self.noise,
               index_src.struct, _lib.ptr(self.U), _lib.ptr(self.lk_var),
               _lib.ptr(self.ke), int(block_steps), _lib.ptr(self.status))
@@ -286,7 +288,7 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
     return None
   pot = im.get("potential")
   bfn = im.get("batch_fn")
-  if not isinstance(pot, StochasticPotential) or not pot.is_mlp or not states:
+  if not isinstance(pot, StochasticPotential) or not pot.is_network or not states:
     return None
   if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn):
     return None
@@ -368,7 +370,7 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
     return None
   pot = im.get("potential")
   bfn = im.get("batch_fn")
-  if not isinstance(pot, StochasticPotential) or pot.is_mlp or not states:
+  if not isinstance(pot, StochasticPotential) or pot.is_network or not states:
     return None
   if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn):
     return None

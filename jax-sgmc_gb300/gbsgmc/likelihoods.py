@@ -20,6 +20,8 @@ Dense network (per observation, the parameters a pytree of matrices):
 * :class:`MLPGaussian` -- ``out = tanh(tanh(x W1 + b1) W2 + b2) W3 + b3``,
   ``lk = log N(y | out, sigma^2)``; BF16 tensor-core GEMMs with fp32
   accumulation.
+* :class:`CNNSoftmax` -- three conv3x3/ReLU/max-pool stages and a dense
+  layer, ``lk = log softmax(logits)[label]``; convolutions as BF16 GEMMs.
 
 Priors: :class:`GaussianPrior` (``sum norm.logpdf(w, 0, scale)``, constants
 included) and :class:`FlatPrior` (``log p = 0``).
@@ -161,13 +163,75 @@ class MLPGaussian:
                        f"(fields: {sorted(data)})")
 
 
+@dataclass(frozen=True)
+class CNNSoftmax:
+  """Convolutional classifier with the softmax (negative cross-entropy)
+  likelihood of the reference's classifier example (examples/cifar.md:
+  203-210): 32x32x3 images, conv3x3 32/64/128 each with ReLU and 2x2
+  max-pool (SAME padding), dense 10.
+
+  The sample is ``{"conv1": {"b", "w"}, "conv2": ..., "conv3": ...,
+  "linear": {"b", "w"}}`` (HWIO conv weights, [2048, 10] dense weights) or
+  its sorted-key ravel, P = 113,738.  Labels are class indices 0..9.
+  Minibatch sizes must be even.
+  """
+  image: str = "image"
+  label: str = "label"
+
+  CHANNELS = (3, 32, 64, 128)
+
+  def shapes(self):
+    c = self.CHANNELS
+    return {"conv1": {"b": (c[1],), "w": (3, 3, c[0], c[1])},
+            "conv2": {"b": (c[2],), "w": (3, 3, c[1], c[2])},
+            "conv3": {"b": (c[3],), "w": (3, 3, c[2], c[3])},
+            "linear": {"b": (10,), "w": (4 * 4 * c[3], 10)}}
+
+  @property
+  def param_count(self) -> int:
+    return sum(math.prod(s) for d in self.shapes().values() for s in d.values())
+
+  def init(self, rng):
+    """He-normal weights, zero biases, as the flat float32 vector."""
+    import numpy as np
+    parts = []
+    for layer in self.shapes().values():
+      for name, shp in layer.items():
+        if name == "w":
+          fan_in = math.prod(shp[:-1])
+          parts.append(rng.normal(0.0, math.sqrt(2.0 / fan_in), size=shp))
+        else:
+          parts.append(np.zeros(shp))
+    return np.concatenate([p.reshape(-1) for p in parts]).astype(np.float32)
+
+  def unravel(self, flat):
+    out, o = {}, 0
+    for lname, layer in self.shapes().items():
+      out[lname] = {}
+      for name, shp in layer.items():
+        k = math.prod(shp)
+        out[lname][name] = flat[..., o:o + k].reshape(tuple(flat.shape[:-1]) + shp)
+        o += k
+    return out
+
+  def check_data(self, data: dict) -> None:
+    for k in (self.image, self.label):
+      if k not in data:
+        raise KeyError(f"reference data has no field {k!r} "
+                       f"(fields: {sorted(data)})")
+
+
 def is_prior(p) -> bool:
   return isinstance(p, (GaussianPrior, FlatPrior))
 
 
 def is_likelihood(l) -> bool:
   return (isinstance(l, GLMLikelihood) and l.family >= 0) or \
-      isinstance(l, MLPGaussian)
+      isinstance(l, (MLPGaussian, CNNSoftmax))
+
+
+def is_cnn(l) -> bool:
+  return isinstance(l, CNNSoftmax)
 
 
 def is_mlp(l) -> bool:

@@ -78,11 +78,28 @@ class StochasticPotential:
   def is_mlp(self) -> bool:
     return lkmod.is_mlp(self.likelihood)
 
+  @property
+  def is_cnn(self) -> bool:
+    return lkmod.is_cnn(self.likelihood)
+
+  @property
+  def is_network(self) -> bool:
+    return self.is_mlp or self.is_cnn
+
   def model(self, dataset, observation_count=None):
     """``gbsgmc_glm`` (or ``gbsgmc_mlp``) for a device dataset, targets
     stored inline in the feature rows (DeviceDataset.glm_view)."""
     n_obs = dataset.observation_count if observation_count is None \
         else observation_count
+    if self.is_cnn:
+      lik = self.likelihood
+      X, d, ld = dataset.glm_view(lik.image, lik.label)
+      if d != 32 * 32 * 3:
+        raise ValueError(f"field {lik.image!r} holds {d} values per "
+                         "observation, the network takes 32x32x3 images")
+      return _lib.Cnn(int(n_obs), int(dataset.observation_count), ld,
+                      X.data_ptr(), X.data_ptr() + 4 * d, ld,
+                      float(self.prior.scale), float(self.temperature)), (X,)
     if self.is_mlp:
       lik = self.likelihood
       X, d, ld = dataset.glm_view(lik.x, lik.y)
@@ -105,7 +122,7 @@ class StochasticPotential:
                     int(dataset.observation_count)), (X,)
 
   def dim(self, dataset) -> int:
-    if self.is_mlp:
+    if self.is_network:
       return self.likelihood.param_count
     return dataset.feature_dim(self.likelihood.x)
 
@@ -128,7 +145,13 @@ class StochasticPotential:
     key = (chains, n, d)
     ws = self._ws.get(key)
     if ws is None:
-      if self.is_mlp:
+      if self.is_cnn:
+        nbytes = int(_lib.load().gbsgmc_cnn_workspace_bytes(chains, n))
+        if nbytes == 0:
+          raise _lib.GbsgmcError(_lib.ERR_SHAPE,
+                                 f"CNN minibatch of {n} images: needs an even "
+                                 "positive size")
+      elif self.is_mlp:
         nbytes = int(_lib.load().gbsgmc_mlp_workspace_bytes(model, chains, n))
         if nbytes == 0:
           raise _lib.GbsgmcError(_lib.ERR_SHAPE,
@@ -153,7 +176,7 @@ class StochasticPotential:
       m, keep = self.model(dataset, observation_count)
     else:
       m, keep = model
-    if self.is_mlp:
+    if self.is_network:
       if d != self.likelihood.param_count:
         raise ValueError(f"parameters per chain {d} != network parameters "
                          f"{self.likelihood.param_count}")
@@ -179,7 +202,8 @@ class StochasticPotential:
                 _lib.ptr(lko), _lib.ptr(var), _lib.ptr(ws), ws.numel(),
                 _lib.ptr(self.status()), _lib.stream_handle())
       return GlmEval(U, g, lko, var)
-    fn = "gbsgmc_mlp_value_and_grad" if self.is_mlp else \
+    fn = "gbsgmc_cnn_value_and_grad" if self.is_cnn else \
+        "gbsgmc_mlp_value_and_grad" if self.is_mlp else \
         "gbsgmc_glm_value_and_grad"
     _lib.call(fn, m, C, n, _lib.ptr(idx),
               idx.stride(0) if idx.dim() == 2 else n, _lib.ptr(mask),

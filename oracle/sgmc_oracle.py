@@ -295,6 +295,137 @@ def mlp_potential(W, X, y, idx, n_obs, d_in, h1, h2, sigma, prior_scale=0.0,
   return Potential(U, grad, lk, np.var(lk, axis=-1))
 
 
+# ---------------------------------------------------------------------------
+# Convolutional classifier (softmax likelihood)
+# ---------------------------------------------------------------------------
+# conv3x3(32) ReLU maxpool2 -> conv3x3(64) ReLU maxpool2 -> conv3x3(128)
+# ReLU maxpool2 -> dense(10), NHWC, SAME padding; lk = -softmax cross entropy
+# (examples/cifar.md:203-210).  Parameters: the sorted ravel of
+# {conv1: {b, w}, conv2: {b, w}, conv3: {b, w}, linear: {b, w}}, HWIO weights.
+
+CNN_CHANNELS = (3, 32, 64, 128)
+CNN_CLASSES = 10
+
+
+def cnn_offsets():
+  sizes, names = [], []
+  for l in range(3):
+    ci, co = CNN_CHANNELS[l], CNN_CHANNELS[l + 1]
+    names += [f"b{l + 1}", f"W{l + 1}"]
+    sizes += [co, 9 * ci * co]
+  names += ["bd", "Wd"]
+  sizes += [CNN_CLASSES, 4 * 4 * 128 * CNN_CLASSES]
+  off = np.concatenate([[0], np.cumsum(sizes)]).astype(int)
+  return dict(zip(names, zip(off[:-1], off[1:]))), int(off[-1])
+
+
+def _im2col(x):
+  """x [n, H, W, C] -> [n*H*W, 9C] with columns (kh, kw, ci), SAME padding."""
+  n, H, W, C = x.shape
+  xp = np.pad(x, ((0, 0), (1, 1), (1, 1), (0, 0)))
+  cols = [xp[:, kh:kh + H, kw:kw + W, :] for kh in range(3) for kw in range(3)]
+  return np.concatenate(cols, axis=-1).reshape(n * H * W, 9 * C)
+
+
+def _col2im(dcols, shape):
+  n, H, W, C = shape
+  d = dcols.reshape(n, H, W, 9, C)
+  out = np.zeros((n, H + 2, W + 2, C))
+  for t in range(9):
+    kh, kw = divmod(t, 3)
+    out[:, kh:kh + H, kw:kw + W, :] += d[:, :, :, t, :]
+  return out[:, 1:H + 1, 1:W + 1, :]
+
+
+def _pool(a):
+  """2x2 max-pool with the argmax (first maximum, row-major in the window)."""
+  n, H, W, C = a.shape
+  win = a.reshape(n, H // 2, 2, W // 2, 2, C).transpose(0, 1, 3, 2, 4, 5)
+  win = win.reshape(n, H // 2, W // 2, 4, C)
+  return win.max(axis=3), win.argmax(axis=3)
+
+
+def _unpool(dp, arg, shape):
+  n, H, W, C = shape
+  d = np.zeros((n, H // 2, W // 2, 4, C))
+  np.put_along_axis(d, arg[:, :, :, None, :], dp[:, :, :, None, :], axis=3)
+  d = d.reshape(n, H // 2, W // 2, 2, 2, C).transpose(0, 1, 3, 2, 4, 5)
+  return d.reshape(n, H, W, C)
+
+
+def round_bf16(x):
+  """Round-to-nearest-even to bfloat16 (the top 16 bits of float32), as
+  float64.  Used to give the oracle the activation precision of a BF16
+  pipeline."""
+  a = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+  r = ((a + 0x7FFF + ((a >> 16) & 1)) >> 16) << 16
+  return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def cnn_potential(w, images, labels, idx, n_obs, prior_scale=0.0,
+                  temperature=1.0, mask=None, activations=None,
+                  bf16_operands=False) -> Potential:
+  """Minibatch potential of the classifier for ONE chain, float64:
+  U = (-N/n sum_i m_i lk_i - log p(w)) / T, lk_i = log softmax(logits_i)[y_i].
+
+  ``activations`` (e.g. round_bf16) is applied to each ReLU output before
+  pooling: a 2x2 max over BF16-rounded values can pick a different window
+  element than the exact maximum, and that changes where the gradient flows.
+  ``bf16_operands`` rounds, to BF16, exactly the values a BF16 GEMM pipeline
+  feeds its tensor cores -- the images, the conv weights, the pooled maps,
+  the conv output gradients dY and the input-gradient columns dCol -- and
+  keeps everything else (accumulation, ReLU outputs, the dense layer, col2im
+  sums) in float64: the arithmetic of the GPU kernels up to summation order.
+  """
+  off, P = cnn_offsets()
+  w = np.asarray(w, np.float64)
+  rnd = round_bf16 if bf16_operands else (lambda v: v)
+  get = lambda k: w[off[k][0]:off[k][1]]
+  x = rnd(np.asarray(images, np.float64)[idx].reshape(-1, 32, 32, 3))
+  y = np.asarray(labels)[idx].astype(int)
+  n = x.shape[0]
+  acts = []
+  h = x
+  for l in range(3):
+    ci, co = CNN_CHANNELS[l], CNN_CHANNELS[l + 1]
+    cols = _im2col(h)
+    wl = rnd(get(f"W{l + 1}")).reshape(9 * ci, co)
+    z = cols @ wl + get(f"b{l + 1}")
+    a = np.maximum(z, 0).reshape(h.shape[0], h.shape[1], h.shape[2], co)
+    if activations is not None:
+      a = activations(a)
+    p, arg = _pool(a)
+    acts.append((h.shape, cols, a, arg, wl))
+    h = rnd(p)
+  flat = h.reshape(n, -1)
+  logits = flat @ get("Wd").reshape(-1, CNN_CLASSES) + get("bd")
+  mx = logits.max(1, keepdims=True)
+  lse = (mx + np.log(np.exp(logits - mx).sum(1, keepdims=True)))[:, 0]
+  lk = logits[np.arange(n), y] - lse
+  m = np.ones(n) if mask is None else np.asarray(mask, np.float64).reshape(n)
+  lp, dlp = log_prior(w[None], prior_scale)
+  U = (-(n_obs / n) * np.sum(m * lk) - lp[0]) / temperature
+  soft = np.exp(logits - lse[:, None])
+  onehot = np.zeros_like(soft)
+  onehot[np.arange(n), y] = 1
+  g = -(n_obs / n) * m[:, None] * (onehot - soft) / temperature
+  grad = np.zeros(P)
+  grad[off["Wd"][0]:off["Wd"][1]] = (flat.T @ g).reshape(-1)
+  grad[off["bd"][0]:off["bd"][1]] = g.sum(0)
+  dh = (g @ get("Wd").reshape(-1, CNN_CLASSES).T).reshape(h.shape)
+  for l in (2, 1, 0):
+    shape_in, cols, a, arg, wl = acts[l]
+    co = CNN_CHANNELS[l + 1]
+    da = rnd(_unpool(dh, arg, a.shape) * (a > 0))
+    dz = da.reshape(-1, co)
+    grad[off[f"W{l + 1}"][0]:off[f"W{l + 1}"][1]] = (cols.T @ dz).reshape(-1)
+    grad[off[f"b{l + 1}"][0]:off[f"b{l + 1}"][1]] = dz.sum(0)
+    if l > 0:
+      dh = _col2im(rnd(dz @ wl.T), shape_in)
+  grad = grad - dlp[0] / temperature
+  return Potential(np.array([U]), grad[None], lk[None], np.array([np.var(lk)]))
+
+
 def linear_posterior(X, y, sigma, prior_scale):
   """Closed-form posterior of Bayesian linear regression with known noise:
   Sigma = (X^T X / s^2 + I / p^2)^-1, mu = Sigma X^T y / s^2."""
