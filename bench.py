@@ -589,6 +589,195 @@ def run_resgld(args):
         "clocks": clk, "finite": finite}), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# CNN workload: 8 chains of OBABO on the conv classifier, minibatch 256 of
+# N = 50,000 synthetic 32x32x3 images.
+# ---------------------------------------------------------------------------
+CNN_N, CNN_CHAINS, CNN_MB = 50_000, 8, 256
+CNN_MAC_PER_IMAGE = (32 * 32 * 32 * 27 + 16 * 16 * 64 * 288 + 8 * 8 * 128 * 576
+                     + 2048 * 10)
+CNN_FLOP_PER_GRAD = 6 * CNN_MB * CNN_MAC_PER_IMAGE   # 2 flop per MAC, 3 passes
+CNN_WORKLOAD = ("Bayesian CNN classifier, OBABO: conv3x3 32/64/128 (ReLU, 2x2 "
+                "max-pool, SAME) + dense 10, P=113,738; N=50,000 synthetic "
+                "32x32x3 images, 10 classes; prior N(0,I); 8 chains, minibatch 256; "
+                "convolutions as BF16 GEMMs")
+
+
+def cnn_data():
+  from gbsgmc import likelihoods as L
+  rng = np.random.default_rng(20261203 + 5)
+  images = rng.standard_normal((CNN_N, 32, 32, 3), dtype=np.float32)
+  labels = rng.integers(0, 10, size=CNN_N).astype(np.float32)
+  lik = L.CNNSoftmax()
+  inits = np.stack([lik.init(np.random.default_rng(2000 + c)) for c in range(CNN_CHAINS)])
+  return lik, images, labels, inits
+
+
+def run_cnn(args):
+  import torch
+  from gbsgmc import alias, data, engine, likelihoods as L, potential
+  rank, world, local = dist_env()
+  torch.cuda.set_device(local)
+  lik, images, labels, inits = cnn_data()
+  loader = data.NumpyDataLoader(image=images, label=labels)
+  ds = loader.device_dataset()
+  pot = potential.minibatch_potential(L.GaussianPrior(1.0), lik)
+  total = args.warmup + args.steps
+  h = torch.full((total,), 1e-5, dtype=torch.float32, device="cuda")
+  t = torch.ones(total, dtype=torch.float32, device="cuda")
+  Xd = torch.from_numpy(inits).cuda()
+  Pd = torch.zeros_like(Xd)
+  words = np.array([pcg_words(CNN_CHAINS * rank + c) for c in range(CNN_CHAINS)],
+                   np.uint64).view(np.int64)
+  pcg = torch.from_numpy(words.copy()).cuda()
+  plan = engine.NetPlan(pot, ds, Xd, Pd, CNN_MB, "obabo", h, t,
+                        engine.IndexSource(pcg=pcg, chain_base=CNN_CHAINS * rank),
+                        noise_seed=13, chain_base=CNN_CHAINS * rank, friction=1.0)
+  plan.run(0, args.warmup)
+  torch.cuda.synchronize()
+  clocks = Clocks(local)
+  clocks.start()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record()
+  plan.run(args.warmup, args.steps)
+  e1.record()
+  torch.cuda.synchronize()
+  clk = clocks.stop()
+  ms = e0.elapsed_time(e1)
+  plan.check_status()
+  finite = bool(torch.isfinite(Xd).all().item())
+  value = world * CNN_CHAINS * args.steps / (ms / 1e3)
+  launches = plan.launches(args.steps)
+  plan.close()
+  idx = torch.randint(0, CNN_N, (CNN_CHAINS, CNN_MB), dtype=torch.int32, device="cuda")
+  for _ in range(3):
+    pot.evaluate(Xd, idx, ds, grad=True)
+  torch.cuda.synchronize()
+  g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  g0.record()
+  for _ in range(20):
+    pot.evaluate(Xd, idx, ds, grad=True)
+  g1.record()
+  torch.cuda.synchronize()
+  grad_ms = g0.elapsed_time(g1) / 20
+  flops = CNN_CHAINS * CNN_FLOP_PER_GRAD
+  peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+      if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+  peak = peaks.get("bf16_tflops_sustained", 1700.0)
+  achieved = flops / (grad_ms / 1e3) / 1e12
+  # Plain one-chain fp32 form: the same network in torch fp32 (cuDNN
+  # convolutions) with autograd, one OBABO step per chain-step.
+  F = torch.nn.functional
+  imgs = torch.from_numpy(images).cuda()
+  labs = torch.from_numpy(labels).cuda().long()
+  from oracle import sgmc_oracle as O
+  off, _ = O.cnn_offsets()
+
+  def plain_grad(w, rows):
+    w = w.detach().requires_grad_(True)
+    get = lambda k: w[off[k][0]:off[k][1]]
+    x = imgs[rows].permute(0, 3, 1, 2)
+    for l in range(3):
+      ci, co = O.CNN_CHANNELS[l], O.CNN_CHANNELS[l + 1]
+      k = get(f"W{l + 1}").reshape(3, 3, ci, co).permute(3, 2, 0, 1)
+      x = F.max_pool2d(F.relu(F.conv2d(x, k, get(f"b{l + 1}"), padding=1)), 2)
+    logits = x.permute(0, 2, 3, 1).reshape(CNN_MB, -1) @ get("Wd").reshape(-1, 10) + get("bd")
+    U = (CNN_N / CNN_MB) * F.cross_entropy(logits, labs[rows], reduction="sum") + \
+        0.5 * (w * w).sum()
+    U.backward()
+    return w.grad
+
+  w1 = Xd[0].clone()
+  p1 = torch.zeros_like(w1)
+
+  def plain_step():
+    nonlocal w1, p1
+    hh, keep = 1e-5, math.exp(-1e-5)
+    p1 = math.sqrt(keep) * p1 + math.sqrt(1 - keep) * torch.randn_like(p1)
+    p1 = p1 - 0.5 * hh * plain_grad(w1, torch.randint(0, CNN_N, (CNN_MB,), device="cuda"))
+    w1 = w1 + hh * p1
+    p1 = p1 - 0.5 * hh * plain_grad(w1, torch.randint(0, CNN_N, (CNN_MB,), device="cuda"))
+    p1 = math.sqrt(keep) * p1 + math.sqrt(1 - keep) * torch.randn_like(p1)
+
+  for _ in range(3):
+    plain_step()
+  torch.cuda.synchronize()
+  q0 = time.perf_counter()
+  for _ in range(20):
+    plain_step()
+  torch.cuda.synchronize()
+  plain_value = 20 / (time.perf_counter() - q0)
+  # End to end through alias.obabo.
+  kw = dict(cache_size=32, batch_size=CNN_MB, integration_steps=10, friction=1.0,
+            first_step_size=1e-5, last_step_size=1e-6)
+  trees = [lik.unravel(inits[c]) for c in range(CNN_CHAINS)]
+  alias.obabo(pot, loader, accepted_samples=1, **kw)(*trees[:2], iterations=2)
+  its = max(2, args.steps // 10)
+  torch.cuda.synchronize()
+  s0 = time.perf_counter()
+  res = alias.obabo(pot, loader, accepted_samples=1, **kw)(*trees, iterations=its)
+  torch.cuda.synchronize()
+  e2e_value = CNN_CHAINS * its * 10 / (time.perf_counter() - s0)
+  P = lik.param_count
+  cpu = None
+  if rank == 0:
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(5)
+    t0 = time.perf_counter()
+    for _ in range(2):
+      O.cnn_potential(inits[0], images.reshape(CNN_N, -1), labels,
+                      rng.integers(0, CNN_N, size=CNN_MB), CNN_N, prior_scale=1.0)
+    rate = 2 / (time.perf_counter() - t0) / 2.0
+    cpu = {"value": rate, "unit": "chain-steps/s", "cores": threads, "kind": "port",
+           "sample": f"2 float64 gradients of one chain (numpy oracle, {threads} threads); "
+                     "an OBABO step is two gradients"}
+  if rank == 0:
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 GEMMs, f32 state",
+        "data": "synthetic (images ~N(0,1), labels U{0..9}, numpy default_rng(20261208)); "
+                "614 MB resident in HBM",
+        "config": {"workload": CNN_WORKLOAD, "chains_per_gpu": CNN_CHAINS,
+                   "minibatch": CNN_MB, "integrator": "OBABO (2 gradients per step)",
+                   "index_stream": "numpy PCG64 per chain, bit-exact",
+                   "graph_block_steps": 50},
+        "gpu_launches": launches,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "peak_kind": "measured bf16_tflops_sustained",
+                     "kernel": "batched value-and-gradient (8 tcgen05 GEMMs + im2col, "
+                               "pooling, dense kernels), 8 chains",
+                     "kernel_ms": grad_ms, "algorithmic_flop_per_launch": flops},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "chain-steps/s",
+                "h2d_bytes_per_step": CNN_CHAINS * P * 4 / (its * 10),
+                "d2h_bytes_per_step": CNN_CHAINS * res[0]["sample_count"] * (P * 4 + 8)
+                / (its * 10),
+                "api": "gbsgmc.alias.obabo(...)(*8 samples, iterations=K/10)"},
+        "plain_gpu": {"value": plain_value, "unit": "chain-steps/s",
+                      "form": "one chain, torch fp32 ops (cuDNN convolutions) + autograd",
+                      "fused_over_plain": value / world / plain_value},
+        "clocks": clk, "finite": finite}), flush=True)
+
+
+def cnn_kernel_only(args):
+  """`--steps` batched value-and-gradient calls of the 8-chain CNN workload
+  and nothing else (for profilers); no JSON line."""
+  import torch
+  from gbsgmc import data, likelihoods as L, potential
+  lik, images, labels, inits = cnn_data()
+  ds = data.NumpyDataLoader(image=images, label=labels).device_dataset()
+  pot = potential.minibatch_potential(L.GaussianPrior(1.0), lik)
+  W = torch.from_numpy(inits).cuda()
+  idx = torch.randint(0, CNN_N, (CNN_CHAINS, CNN_MB), dtype=torch.int32, device="cuda")
+  for _ in range(args.steps):
+    pot.evaluate(W, idx, ds, grad=True)
+  torch.cuda.synchronize()
+  pot.check_status()
+
+
 def mlp_kernel_only(args):
   """`--steps` batched value-and-gradient calls of the 64-chain workload and
   nothing else (a short run for profilers); no JSON line."""
@@ -765,15 +954,23 @@ def main():
   ap.add_argument("--warmup", type=int, default=5)
   ap.add_argument("--impl", default="gbsgmc", choices=["gbsgmc", "reference"])
   ap.add_argument("--workload", default="logistic",
-                  choices=["logistic", "mlp", "resgld"],
+                  choices=["logistic", "mlp", "resgld", "cnn"],
                   help="logistic: 256-chain SGLD headline; mlp: 64-chain OBABO "
-                       "on the tanh network; resgld: 32-replica exchange on it")
+                       "on the tanh network; resgld: 32-replica exchange on it; "
+                       "cnn: 8-chain OBABO on the conv classifier")
   ap.add_argument("--kernel-only", action="store_true",
                   help="short run of the fused kernel for profilers; no JSON line")
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error("--warmup must be at least 3")
-  if args.workload == "resgld":
+  if args.workload == "cnn":
+    if args.impl == "reference":
+      run_mlp_reference(args)
+    elif args.kernel_only:
+      cnn_kernel_only(args)
+    else:
+      run_cnn(args)
+  elif args.workload == "resgld":
     if args.impl == "reference":
       run_mlp_reference(args)
     else:

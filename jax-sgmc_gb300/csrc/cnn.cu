@@ -29,6 +29,7 @@
 // the CUDA cores in fp32.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -64,10 +65,18 @@ struct CnnLayout {
   size_t labels;                      // int32
   size_t dp3, gl;                     // fp32 dP3 [n, 2048], dlogits [n, 10]
   size_t psq, plk;                    // fp64 partial sums
+  size_t part, bpart;                 // split-K weight partials, bias partials
   size_t total;
 };
 
 constexpr int kPrepBlocks = 64;  // Σw² partial sums per chain
+constexpr int kBiasChunks = 64;  // row chunks of the bias-gradient sums
+
+// Split-K factors of the weight-gradient GEMMs (K = pixels of n images:
+// 16n, 4n and n slices of 64 for the three layers; n is even).
+inline int wsplit(int layer, int n) {
+  return layer == 1 ? 32 : layer == 2 ? 8 : (n % 4 == 0 ? 4 : 2);
+}
 
 CnnLayout cnn_layout(int chains, int n) {
   CnnLayout L;
@@ -103,6 +112,12 @@ CnnLayout cnn_layout(int chains, int n) {
   L.gl = take(4 * N * kClasses);
   L.psq = take(8 * kPrepBlocks);
   L.plk = take(8 * 4 * N);
+  size_t part = 0;
+  part = std::max<size_t>(part, size_t(wsplit(1, n)) * kC1 * kK1);
+  part = std::max<size_t>(part, size_t(wsplit(2, n)) * kC2 * kK2);
+  part = std::max<size_t>(part, size_t(wsplit(3, n)) * kC3 * kK3);
+  L.part = take(4 * part);
+  L.bpart = take(4 * kBiasChunks * kC3);
   L.total = off;
   return L;
 }
@@ -130,6 +145,7 @@ struct CnnArgs {
   int32_t* lab;
   float *dp3, *gl;
   double *psq, *plk;
+  float *part, *bpart;
 };
 
 __device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
@@ -164,9 +180,9 @@ __global__ void __launch_bounds__(256) cnn_prep_kernel(const CnnArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
   const int c = blockIdx.y;
-  const int64_t p = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
-  if (p >= static_cast<int64_t>(a.n) * 1024) return;
-  const int i = static_cast<int>(p >> 10), hw = static_cast<int>(p & 1023);
+  const int p = blockIdx.x * 256 + threadIdx.x;
+  if (p >= a.n * 1024) return;
+  const int i = p >> 10, hw = p & 1023;
   const int h = hw >> 5, wq = hw & 31;
   int64_t o = a.idx[static_cast<int64_t>(c) * a.idx_stride + i];
   if (o < 0 || o >= a.n_rows) {
@@ -216,16 +232,18 @@ __global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pout, uint8_t* M,
                                                       int n, int H, int W, int C, int ld) {
+  // Per-chain element counts stay below 2^31: 32-bit index arithmetic.
   const int c = blockIdx.y;
   const int Ho = H / 2, Wo = W / 2;
-  const int64_t per = static_cast<int64_t>(n) * Ho * Wo * C;
-  const int64_t e = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  const int per = n * Ho * Wo * C;
+  const int e = blockIdx.x * 256 + threadIdx.x;
   if (e >= per) return;
-  const int ch = static_cast<int>(e % C);
-  const int64_t pix = e / C;
-  const int x = static_cast<int>(pix % Wo), y = static_cast<int>((pix / Wo) % Ho);
-  const int64_t i = pix / (static_cast<int64_t>(Wo) * Ho);
-  const float* src = A + (static_cast<int64_t>(c) * n * H * W + (i * H + 2 * y) * W + 2 * x) * ld + ch;
+  const int ch = e % C;
+  const int pix = e / C;
+  const int x = pix % Wo, y = (pix / Wo) % Ho;
+  const int i = pix / (Wo * Ho);
+  const float* src = A + static_cast<int64_t>(c) * n * H * W * ld +
+                     ((i * H + 2 * y) * W + 2 * x) * ld + ch;
   float best = src[0];
   int arg = 0;
   const float v1 = src[ld], v2 = src[static_cast<int64_t>(W) * ld],
@@ -245,20 +263,20 @@ __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pou
 __global__ void __launch_bounds__(256) cnn_im2col_kernel(const bf16* Pin, bf16* Col, int n,
                                                         int H, int W, int C, int Kp) {
   const int c = blockIdx.y;
-  const int64_t groups = static_cast<int64_t>(n) * H * W * (Kp / 8);
-  const int64_t e = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  const int groups = n * H * W * (Kp / 8);
+  const int e = blockIdx.x * 256 + threadIdx.x;
   if (e >= groups) return;
-  const int k0 = static_cast<int>(e % (Kp / 8)) * 8;
-  const int64_t pix = e / (Kp / 8);
-  const int x = static_cast<int>(pix % W), y = static_cast<int>((pix / W) % H);
-  const int64_t i = pix / (static_cast<int64_t>(W) * H);
+  const int k0 = (e % (Kp / 8)) * 8;
+  const int pix = e / (Kp / 8);
+  const int x = pix % W, y = (pix / W) % H;
+  const int i = pix / (W * H);
   uint4 v = make_uint4(0, 0, 0, 0);
   if (k0 < 9 * C) {
     const int tap = k0 / C, ci = k0 % C;
     const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
     if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-      v = *reinterpret_cast<const uint4*>(
-          Pin + (static_cast<int64_t>(c) * n * H * W + (i * H + yy) * W + xx) * C + ci);
+      v = *reinterpret_cast<const uint4*>(Pin + static_cast<int64_t>(c) * n * H * W * C +
+                                          ((i * H + yy) * W + xx) * C + ci);
   }
   reinterpret_cast<uint4*>(Col + static_cast<int64_t>(c) * n * H * W * Kp)[e] = v;
 }
@@ -328,94 +346,144 @@ __global__ void __launch_bounds__(128) cnn_dense_kernel(const CnnArgs a) {
 }
 
 // dWd [2048, 10] = sum_i P3_i (x) g_i and dbd = sum_i g_i (likelihood part).
-// Grid (kFlat / 128 + 1, chains), 128 threads.
+// Grid (kFlat / 128 + 1, chains), 128 threads; dlogits staged in shared
+// memory (n <= 1024 images per pass).
 __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
-  const int c = blockIdx.y;
+  __shared__ float gs[1024 * kClasses];
+  const int c = blockIdx.y, t = threadIdx.x;
   float* g = a.grad + static_cast<int64_t>(c) * kP;
   const float* gl = a.gl + static_cast<int64_t>(c) * a.n * kClasses;
   if (blockIdx.x == kFlat / 128) {
-    if (threadIdx.x < kClasses) {
+    if (t < kClasses) {
       float s = 0.f;
-      for (int i = 0; i < a.n; ++i) s += gl[i * kClasses + threadIdx.x];
-      g[obd + threadIdx.x] = s;
+      for (int i = 0; i < a.n; ++i) s += gl[i * kClasses + t];
+      g[obd + t] = s;
     }
     return;
   }
-  const int f = blockIdx.x * 128 + threadIdx.x;
+  const int f = blockIdx.x * 128 + t;
   const bf16* x = a.p3 + static_cast<int64_t>(c) * a.n * kFlat + f;
   float acc[kClasses];
 #pragma unroll
   for (int k = 0; k < kClasses; ++k) acc[k] = 0.f;
-  for (int i = 0; i < a.n; ++i) {
-    const float xv = bf(x[static_cast<int64_t>(i) * kFlat]);
+  for (int i0 = 0; i0 < a.n; i0 += 1024) {
+    const int cnt = min(1024, a.n - i0);
+    __syncthreads();
+    for (int j = t; j < cnt * kClasses; j += 128) gs[j] = gl[i0 * kClasses + j];
+    __syncthreads();
+    int i = 0;
+    for (; i + 8 <= cnt; i += 8) {
+      float xv[8];
 #pragma unroll
-    for (int k = 0; k < kClasses; ++k) acc[k] = fmaf(xv, gl[i * kClasses + k], acc[k]);
+      for (int u = 0; u < 8; ++u) xv[u] = bf(x[static_cast<int64_t>(i0 + i + u) * kFlat]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int k = 0; k < kClasses; ++k)
+          acc[k] = fmaf(xv[u], gs[(i + u) * kClasses + k], acc[k]);
+    }
+    for (; i < cnt; ++i) {
+      const float xv = bf(x[static_cast<int64_t>(i0 + i) * kFlat]);
+#pragma unroll
+      for (int k = 0; k < kClasses; ++k) acc[k] = fmaf(xv, gs[i * kClasses + k], acc[k]);
+    }
   }
 #pragma unroll
   for (int k = 0; k < kClasses; ++k) g[oWd + static_cast<int64_t>(f) * kClasses + k] = acc[k];
 }
 
 // ---------------------------------------------------------------------------
-// Pool-window routing + ReLU mask of the fp32 pre-pool activations A:
-// dY[i, y, x, ch] = (argmax of its window == this position) * dP * (A > 0).
-// dP is read either directly (fp32 dp, layer 3) or as the 9-tap col2im sum of
-// the next layer's dCol [n*Hn*Wn, Kp] (Hn = H/2).  One thread per element of
-// A [n, H, W, ld]; channels ch >= C are zeroed.  Grid (ceil(n*H*W*ld/256),
-// chains).
+// Pool-window routing + ReLU mask: for each pooled element (i, py, px, ch)
+// of a layer with pre-pool activations A [n, H, W, ld] (C real channels),
+//   dP = dp[i, py, px, ch]                       (layer 3: fp32 dP3), or
+//   dP = sum over taps (kh, kw) of dCol[(i, py - kh + 1, px - kw + 1),
+//                                      (kh, kw, ch)]  (col2im of the next
+//        layer's input-gradient columns dCol [n*Ho*Wo, Kp])
+// goes to the window element its argmax chose, masked by A > 0; the three
+// others (and channels C..ld-1) get 0:  dY [n, H, W, ld] BF16.  One thread
+// per pooled element, 32-bit index arithmetic (per-chain counts < 2^31).
+// Grid (ceil(n*Ho*Wo*C / 256), chains).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) cnn_unpool_kernel(const float* A, bf16* dY,
                                                         const uint8_t* M, const float* dp,
                                                         const bf16* dcol, int n, int H, int W,
                                                         int C, int ld, int Kp) {
   const int c = blockIdx.y;
-  const int64_t per = static_cast<int64_t>(n) * H * W * ld;
-  const int64_t e = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
-  if (e >= per) return;
-  const int ch = static_cast<int>(e % ld);
-  const int64_t pix = e / ld;
-  const int x = static_cast<int>(pix % W), y = static_cast<int>((pix / W) % H);
-  const int64_t i = pix / (static_cast<int64_t>(W) * H);
-  const float act = A[static_cast<int64_t>(c) * per + e];
-  float out = 0.f;
-  if (ch < C) {
-    const int Ho = H / 2, Wo = W / 2, py = y >> 1, px = x >> 1;
-    const int64_t pe = ((i * Ho + py) * Wo + px) * C + ch;
-    const int64_t pper = static_cast<int64_t>(n) * Ho * Wo * C;
-    const int arg = (y & 1) * 2 + (x & 1);
-    if (M[static_cast<int64_t>(c) * pper + pe] == arg && act > 0.f) {
-      if (dp != nullptr) {
-        out = dp[static_cast<int64_t>(c) * pper + pe];
-      } else {
-        // dP[i, py, px, ch] = sum over taps of dCol at the output pixel
-        // (py - kh + 1, px - kw + 1), column (kh, kw, ch).
-        const bf16* dc = dcol + static_cast<int64_t>(c) * n * Ho * Wo * Kp;
-        float s = 0.f;
+  const int Ho = H / 2, Wo = W / 2;
+  const int pper = n * Ho * Wo * C;
+  const int e = blockIdx.x * 256 + threadIdx.x;
+  if (e >= pper) return;
+  const int ch = e % C;
+  const int pix = e / C;
+  const int px = pix % Wo, py = (pix / Wo) % Ho, i = pix / (Wo * Ho);
+  float g;
+  if (dp != nullptr) {
+    g = dp[static_cast<int64_t>(c) * pper + e];
+  } else {
+    const bf16* dc = dcol + static_cast<int64_t>(c) * n * Ho * Wo * Kp;
+    g = 0.f;
 #pragma unroll
-        for (int kh = 0; kh < 3; ++kh)
+    for (int kh = 0; kh < 3; ++kh)
 #pragma unroll
-          for (int kw = 0; kw < 3; ++kw) {
-            const int oy = py - kh + 1, ox = px - kw + 1;
-            if (oy >= 0 && oy < Ho && ox >= 0 && ox < Wo)
-              s += bf(dc[((i * Ho + oy) * Wo + ox) * Kp + (kh * 3 + kw) * C + ch]);
-          }
-        out = s;
+      for (int kw = 0; kw < 3; ++kw) {
+        const int oy = py - kh + 1, ox = px - kw + 1;
+        if (oy >= 0 && oy < Ho && ox >= 0 && ox < Wo)
+          g += bf(dc[((i * Ho + oy) * Wo + ox) * Kp + (kh * 3 + kw) * C + ch]);
       }
-    }
   }
-  dY[static_cast<int64_t>(c) * per + e] = __float2bfloat16_rn(out);
+  const int arg = M[static_cast<int64_t>(c) * pper + e];
+  const int64_t base = static_cast<int64_t>(c) * n * H * W * ld;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int y = 2 * py + (q >> 1), x = 2 * px + (q & 1);
+    const int off = ((i * H + y) * W + x) * ld;
+    const float v = (q == arg && A[base + off + ch] > 0.f) ? g : 0.f;
+    dY[base + off + ch] = __float2bfloat16_rn(v);
+    for (int extra = C + ch; extra < ld; extra += C) dY[base + off + extra] = __float2bfloat16_rn(0.f);
+  }
 }
 
-// Column sums of dY [rows, ld] over a chain's rows (bias gradients), C real
-// channels.  Grid (C, chains), 256 threads.
-__global__ void __launch_bounds__(256) cnn_bias_grad_kernel(const bf16* dY, int64_t rows,
-                                                           int ld, float* grad, int64_t off) {
-  __shared__ double red[32];
-  const int ch = blockIdx.x, c = blockIdx.y;
-  const bf16* src = dY + static_cast<int64_t>(c) * rows * ld + ch;
+// Bias gradients, pass 1: partial column sums of dY [rows, ld] (C real
+// channels) over kBiasChunks row chunks: thread t adds channel t % C of rows
+// t / C, t / C + 256 / C, ... of its chunk (coalesced along channels).
+// Grid (kBiasChunks, chains), 256 threads; C divides 256.
+__global__ void __launch_bounds__(256) cnn_bias_part_kernel(const bf16* dY, int rows, int ld,
+                                                           int C, float* bpart) {
+  __shared__ float acc[256];
+  const int c = blockIdx.y, t = threadIdx.x, ch = t % C, r0 = t / C, step = 256 / C;
+  const int per = (rows + kBiasChunks - 1) / kBiasChunks;
+  const int lo = blockIdx.x * per, hi = min(rows, lo + per);
+  const bf16* src = dY + static_cast<int64_t>(c) * rows * ld;
   float s = 0.f;
-  for (int64_t r = threadIdx.x; r < rows; r += 256) s += bf(src[r * ld]);
-  const double tot = block_sum(static_cast<double>(s), red);
-  if (threadIdx.x == 0) grad[static_cast<int64_t>(c) * kP + off + ch] = static_cast<float>(tot);
+  for (int r = lo + r0; r < hi; r += step) s += bf(src[r * ld + ch]);
+  acc[t] = s;
+  __syncthreads();
+  if (t < C) {
+    float tot = 0.f;
+    for (int q = 0; q < step; ++q) tot += acc[q * C + t];
+    bpart[(static_cast<int64_t>(c) * kBiasChunks + blockIdx.x) * kC3 + t] = tot;
+  }
+}
+
+// Pass 2: grad[off + ch] = sum over chunks.  Grid (chains), C threads.
+__global__ void cnn_bias_sum_kernel(const float* bpart, float* grad, int64_t off) {
+  const int c = blockIdx.x, ch = threadIdx.x;
+  float s = 0.f;
+  for (int q = 0; q < kBiasChunks; ++q)
+    s += bpart[(static_cast<int64_t>(c) * kBiasChunks + q) * kC3 + ch];
+  grad[static_cast<int64_t>(c) * kP + off + ch] = s;
+}
+
+// Split-K reduction of a weight gradient: grad[off + e] = sum_s part[c, s, e]
+// over e < K * Cout (HWIO order).  Grid (ceil(K*Cout/256), chains).
+__global__ void __launch_bounds__(256) cnn_wsum_kernel(const float* part, int splits, int count,
+                                                      float* grad, int64_t off) {
+  const int c = blockIdx.y, e = blockIdx.x * 256 + threadIdx.x;
+  if (e >= count) return;
+  const float* p = part + static_cast<int64_t>(c) * splits * count + e;
+  float s = 0.f;
+  for (int q = 0; q < splits; ++q) s += p[static_cast<int64_t>(q) * count];
+  grad[static_cast<int64_t>(c) * kP + off + e] = s;
 }
 
 // grad += w / (s^2 T) over every parameter; U and var(lk).  Grid
@@ -513,17 +581,17 @@ struct EpiConvRelu {
   }
 };
 
-// Weights: element (row = output channel co, col = im2col column k) of dW
-// lands at grad[b*P + off + k*Cout + co] (HWIO), rows < Cout, cols < K.
+// Weights: element (row = output channel co, col = im2col column k) of the
+// split-K partial product of (virtual) batch bv = chain * splits + split
+// lands at part[bv][k][co] (HWIO order), rows < Cout, cols < K.
 struct EpiConvGradW {
-  float* grad;
-  int64_t off;
+  float* part;
   int Cout, K;
   template <int NC, class Load>
-  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+  __device__ __forceinline__ void tile(int bv, int row0, int col0, const Load& load,
                                        uint32_t*) const {
     const int co = row0 + epi::lane_id();
-    float* dst = grad + b * kP + off + co;
+    float* dst = part + static_cast<int64_t>(bv) * K * Cout + co;
 #pragma unroll 1
     for (int cb = 0; cb < NC / 32; ++cb) {
       float v[32];
@@ -596,10 +664,34 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   a.gl = view<float>(ws, L.gl);
   a.psq = view<double>(ws, L.psq);
   a.plk = view<double>(ws, L.plk);
+  a.part = view<float>(ws, L.part);
+  a.bpart = view<float>(ws, L.bpart);
   const int C = a.chains, n = a.n;
   const int64_t r1 = int64_t(n) * 1024, r2 = int64_t(n) * 256, r3 = int64_t(n) * 64;
   int rc;
   auto launched = [&](const char* what) { return check_launch(what); };
+  // Bias gradient of a layer from its dY [rows, ld] (C real channels).
+  auto bias_grad = [&](const bf16* dY, int64_t rows, int ld, int Cr, int64_t off) {
+    cnn_bias_part_kernel<<<dim3(kBiasChunks, C), 256, 0, st>>>(dY, static_cast<int>(rows), ld,
+                                                               Cr, a.bpart);
+    int r = launched("cnn_bias_part_kernel");
+    if (r) return r;
+    cnn_bias_sum_kernel<<<C, Cr, 0, st>>>(a.bpart, a.grad, off);
+    return launched("cnn_bias_sum_kernel");
+  };
+  // Weight gradient of a layer: split-K GEMM into partials, then their sum.
+  auto weight_grad = [&](const CUtensorMap& mdy, const CUtensorMap& mcol, int layer, int Cout,
+                         int K, int Kp, int64_t rows, int64_t off) {
+    GemmRagged rg;
+    rg.ksplit = wsplit(layer, n);
+    const EpiConvGradW e{a.part, Cout, K};
+    int r = launch_gemm<64, true, true>(mdy, mcol, C, 128, Kp, static_cast<int>(rows), a.status,
+                                        e, st, rg);
+    if (r) return r;
+    cnn_wsum_kernel<<<dim3(grid1(int64_t(K) * Cout), C), 256, 0, st>>>(a.part, rg.ksplit,
+                                                                       K * Cout, a.grad, off);
+    return launched("cnn_wsum_kernel");
+  };
 
   cnn_prep_kernel<<<dim3(kPrepBlocks, C), 256, 0, st>>>(a);
   if ((rc = launched("cnn_prep_kernel"))) return rc;
@@ -647,56 +739,47 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     cnn_dense_grad_kernel<<<dim3(kFlat / 128 + 1, C), 128, 0, st>>>(a);
     if ((rc = launched("cnn_dense_grad_kernel"))) return rc;
     // Layer 3: dY3 over A3, db3, dW3 = dY3^T Col3, dCol3 = dY3 W3^T.
-    cnn_unpool_kernel<<<dim3(grid1(r3 * kC3), C), 256, 0, st>>>(a.a3, a.dy3, a.m3, a.dp3, nullptr,
-                                                                n, 8, 8, kC3, kC3, 0);
+    cnn_unpool_kernel<<<dim3(grid1(int64_t(n) * 16 * kC3), C), 256, 0, st>>>(
+        a.a3, a.dy3, a.m3, a.dp3, nullptr, n, 8, 8, kC3, kC3, 0);
     if ((rc = launched("cnn_unpool_kernel 3"))) return rc;
-    cnn_bias_grad_kernel<<<dim3(kC3, C), 256, 0, st>>>(a.dy3, r3, kC3, a.grad, ob3);
-    if ((rc = launched("cnn_bias_grad_kernel 3"))) return rc;
+    if ((rc = bias_grad(a.dy3, r3, kC3, kC3, ob3))) return rc;
     CUtensorMap m_dy3t, m_col3t, m_dy3, m_w3k;
     if ((rc = make_tmap_bf16_3d(&m_dy3t, a.dy3, kC3, r3, C, kC3, r3 * kC3, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col3t, a.col3, kK3p, r3, C, kK3p, r3 * kK3p, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_dy3, a.dy3, kC3, r3, C, kC3, r3 * kC3, kGemmBK, kGemmBM)) ||
         (rc = make_tmap_bf16_3d(&m_w3k, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, kGemmBK, 64)))
       return rc;
-    const EpiConvGradW g3{a.grad, oW3, kC3, kK3};
-    if ((rc = launch_gemm<64, true, true>(m_dy3t, m_col3t, C, 128, kK3p, r3, a.status, g3, st)))
-      return rc;
+    if ((rc = weight_grad(m_dy3t, m_col3t, 3, kC3, kK3, kK3p, r3, oW3))) return rc;
     const EpiStoreBf16 d3{a.dcol3, kK3p, r3};
     if ((rc = launch_gemm<64, false, false>(m_dy3, m_w3k, C, r3, kK3p, kC3, a.status, d3, st)))
       return rc;
     // Layer 2.
-    cnn_unpool_kernel<<<dim3(grid1(r2 * kC2), C), 256, 0, st>>>(a.a2, a.dy2, a.m2, nullptr,
+    cnn_unpool_kernel<<<dim3(grid1(r3 * kC2), C), 256, 0, st>>>(a.a2, a.dy2, a.m2, nullptr,
                                                                 a.dcol3, n, 16, 16, kC2, kC2,
                                                                 kK3p);
     if ((rc = launched("cnn_unpool_kernel 2"))) return rc;
-    cnn_bias_grad_kernel<<<dim3(kC2, C), 256, 0, st>>>(a.dy2, r2, kC2, a.grad, ob2);
-    if ((rc = launched("cnn_bias_grad_kernel 2"))) return rc;
+    if ((rc = bias_grad(a.dy2, r2, kC2, kC2, ob2))) return rc;
     CUtensorMap m_dy2t, m_col2t, m_dy2, m_w2k;
     if ((rc = make_tmap_bf16_3d(&m_dy2t, a.dy2, kC2, r2, C, kC2, r2 * kC2, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col2t, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_dy2, a.dy2, kC2, r2, C, kC2, r2 * kC2, kGemmBK, kGemmBM)) ||
         (rc = make_tmap_bf16_3d(&m_w2k, a.w2b, kC2, kK2, C, kC2, kK2 * kC2, kGemmBK, 64)))
       return rc;
-    const EpiConvGradW g2{a.grad, oW2, kC2, kK2};
-    if ((rc = launch_gemm<64, true, true>(m_dy2t, m_col2t, C, 128, kK2p, r2, a.status, g2, st)))
-      return rc;
+    if ((rc = weight_grad(m_dy2t, m_col2t, 2, kC2, kK2, kK2p, r2, oW2))) return rc;
     const EpiStoreBf16 d2{a.dcol2, kK2p, r2};
     if ((rc = launch_gemm<64, false, false>(m_dy2, m_w2k, C, r2, kK2p, kC2, a.status, d2, st)))
       return rc;
     // Layer 1.
-    cnn_unpool_kernel<<<dim3(grid1(r1 * kA1ld), C), 256, 0, st>>>(a.a1, a.dy1, a.m1, nullptr,
-                                                                  a.dcol2, n, 32, 32, kC1, kA1ld,
-                                                                  kK2p);
+    cnn_unpool_kernel<<<dim3(grid1(r2 * kC1), C), 256, 0, st>>>(a.a1, a.dy1, a.m1, nullptr,
+                                                                a.dcol2, n, 32, 32, kC1, kA1ld,
+                                                                kK2p);
     if ((rc = launched("cnn_unpool_kernel 1"))) return rc;
-    cnn_bias_grad_kernel<<<dim3(kC1, C), 256, 0, st>>>(a.dy1, r1, kA1ld, a.grad, ob1);
-    if ((rc = launched("cnn_bias_grad_kernel 1"))) return rc;
+    if ((rc = bias_grad(a.dy1, r1, kA1ld, kC1, ob1))) return rc;
     CUtensorMap m_dy1t, m_col1t;
     if ((rc = make_tmap_bf16_3d(&m_dy1t, a.dy1, kA1ld, r1, C, kA1ld, r1 * kA1ld, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col1t, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, 64, 64)))
       return rc;
-    const EpiConvGradW g1{a.grad, oW1, kC1, kK1};
-    if ((rc = launch_gemm<64, true, true>(m_dy1t, m_col1t, C, 128, kK1p, r1, a.status, g1, st)))
-      return rc;
+    if ((rc = weight_grad(m_dy1t, m_col1t, 1, kC1, kK1, kK1p, r1, oW1))) return rc;
   }
   const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;
   const float pf = a.prior_scale > 0.f ? static_cast<float>(1.0 / (s2 * a.temperature)) : 0.f;

@@ -72,6 +72,10 @@ size_t gemm_smem_bytes(int bn);
 struct GemmRagged {
   const int* tile_prefix = nullptr;  // [batch + 1], tile_prefix[0] = 0
   const int* kblocks = nullptr;      // [batch]
+  // Split-K (uniform batches only): each output tile is computed as ksplit
+  // partial products over consecutive K ranges by different CTAs; the
+  // epilogue sees batch index b * ksplit + s for split s.
+  int ksplit = 1;
 };
 
 __device__ __forceinline__ int ragged_batch(const GemmRagged& rg, int t, int per_batch,
@@ -137,13 +141,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles_n = N / BN, per_batch = (M / BM) * tiles_n;
+  const int vbatch = batch * rg.ksplit;
   const int tiles = rg.tile_prefix != nullptr ? __ldg(rg.tile_prefix + batch)
-                                              : per_batch * batch;
-  // Chain of tile t, its index within the chain, and its K slices.
-  auto decode = [&](int t, int& b, int& r, int& KB) {
-    b = ragged_batch(rg, t, per_batch, batch);
+                                              : per_batch * vbatch;
+  // (Virtual) batch of tile t, its index within the batch, its K slices and
+  // the first of them.
+  auto decode = [&](int t, int& b, int& r, int& KB, int& kb0) {
+    b = ragged_batch(rg, t, per_batch, vbatch);
     r = t - (rg.tile_prefix != nullptr ? __ldg(rg.tile_prefix + b) : b * per_batch);
-    KB = rg.kblocks != nullptr ? __ldg(rg.kblocks + b) : K / BK;
+    KB = rg.kblocks != nullptr ? __ldg(rg.kblocks + b) : K / BK / rg.ksplit;
+    kb0 = (b % rg.ksplit) * KB;
   };
 
   if (threadIdx.x == 0) {
@@ -173,8 +180,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       uint32_t it = 0;
       bool ok = true;
       for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x) {
-        int b, r, KB;
-        decode(t, b, r, KB);
+        int bv, r, KB, kb0;
+        decode(t, bv, r, KB, kb0);
+        const int b = bv / rg.ksplit;
         const int m0 = (r / tiles_n) * BM, n0 = (r % tiles_n) * BN;
         for (int kb = 0; kb < KB; ++kb, ++it) {
           const int s = it % STAGES;
@@ -186,7 +194,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             break;
           }
           mbar_arrive_expect_tx(&full[s], A_BYTES + B_BYTES);
-          const int k0 = kb * BK;
+          const int k0 = (kb0 + kb) * BK;
           if constexpr (A_MN) {
 #pragma unroll
             for (int j = 0; j < BM / 64; ++j)
@@ -217,8 +225,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       uint32_t it = 0, acc = 0;
       bool ok = true;
       for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x, ++acc) {
-        int b, r, KB;
-        decode(t, b, r, KB);
+        int b, r, KB, kb0;
+        decode(t, b, r, KB, kb0);
         const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
         if (!mbar_wait_bounded(&tempty[buf], aph ^ 1u, abort_flag)) {
           raise_status(status, GBSGMC_ERR_TIMEOUT);
@@ -274,8 +282,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         break;
       }
       tc::fence_after_sync();
-      int b, r, KB;
-      decode(t, b, r, KB);
+      int b, r, KB, kb0;
+      decode(t, b, r, KB, kb0);
       const int row0 = (r / tiles_n) * BM + q * 32;
       const uint32_t tbase =
           tmem + buf * BN + h * NC + (static_cast<uint32_t>(q * 32) << 16);
@@ -320,7 +328,7 @@ int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, int batch, int M,
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return set_error(GBSGMC_ERR_CUDA, "gemm: cannot query the device");
-  const int64_t tiles = static_cast<int64_t>(M / kGemmBM) * (N / BN) * batch;
+  const int64_t tiles = static_cast<int64_t>(M / kGemmBM) * (N / BN) * batch * rg.ksplit;
   const int grid = static_cast<int>(tiles < int64_t(sms) * per_sm ? tiles : int64_t(sms) * per_sm);
   kern<<<grid, kGemmThreads, smem, st>>>(ta, tb, M, N, K, batch, status, epi, rg);
   return check_launch("tc_gemm_kernel");
