@@ -407,6 +407,7 @@ def run_gbsgmc(args):
                    "launch_shape": {"ctas_per_chain": shape[0],
                                     "rows_per_warp": shape[1],
                                     "warps_per_cta": shape[2],
+                                    "prefetch_tiles": shape[3],
                                     "chosen_by": "autotuner"}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,

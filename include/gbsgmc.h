@@ -586,13 +586,14 @@ int gbsgmc_plan_run(gbsgmc_plan* plan, int64_t first_step, int64_t steps,
                     gbsgmc_stream_t stream);
 
 /* The launch shape the plan's autotuner chose for the fused step: CTAs per
- * chain, rows per warp and warps per CTA (0 = the library default).  The autotuner times a
- * few candidate shapes on scratch copies of the chain state when the plan is
+ * chain, rows per warp, warps per CTA and whether each warp keeps two row
+ * tiles in flight (0 = the library default).  The autotuner times a few
+ * candidate shapes on scratch copies of the chain state when the plan is
  * created (GBSGMC_AUTOTUNE=0 disables it) and caches the choice per problem
- * shape for the process.  No reference counterpart: launch configuration
- * only. */
+ * shape for the process.  Network plans report zeros.  No reference
+ * counterpart: launch configuration only. */
 int gbsgmc_plan_launch_shape(const gbsgmc_plan* plan, int* slices,
-                             int* rows_per_warp, int* warps);
+                             int* rows_per_warp, int* warps, int* prefetch);
 
 /* Kernel launches one plan_run of `steps` steps performs (for accounting). */
 int64_t gbsgmc_plan_launches(const gbsgmc_plan* plan, int64_t steps);

@@ -79,6 +79,7 @@ struct GlmArgs {
   int slices_fixed;   // > 0: slices per chain chosen by the caller
   int rw_fixed;       // > 0: rows per warp chosen by the caller
   int warps_fixed;    // > 0: warps per CTA chosen by the caller
+  int pf_fixed;       // 1: prefetching variant, -1: not, 0: library choice
   int* status;
   int vec4;   // rows are 16-byte aligned: 128-bit loads
 };
@@ -690,6 +691,7 @@ struct Variant {
 // GBSGMC_GLM_SLICES (CTAs per chain).
 int rows_override() { return env_int("GBSGMC_GLM_RW", 0); }
 int warps_override() { return env_int("GBSGMC_GLM_WARPS", 0); }
+int prefetch_override() { return env_int("GBSGMC_GLM_PF", -1); }
 
 // Dispatch over the tuned shape: rows per warp (RW) and warps per CTA.  The
 // register budget (MINB) is 3 CTAs/SM for 8-warp CTAs with RW = 4, otherwise
@@ -703,8 +705,18 @@ int launch_q(const GlmArgs& a, size_t smem, cudaStream_t st) {
     const int rw = a.rw_fixed > 0 ? a.rw_fixed
                    : (rows_override() > 0 ? rows_override()
                                           : default_rows_per_warp(QPL));
-    if (rw == 4) return big ? Variant<QPL, 4, false, 1, 16>::launch(a, smem, st)
-                            : Variant<QPL, 4, false, 3, 8>::launch(a, smem, st);
+    const int pfo = prefetch_override();
+    const bool pf = a.pf_fixed > 0 || (a.pf_fixed == 0 && pfo > 0);
+    // Prefetching variants hold two tiles in registers, so they get the
+    // register budget of fewer resident CTAs.
+    if (rw == 8) return Variant<QPL, 8, false, 2, 8>::launch(a, smem, st);
+    if (rw == 4) {
+      if (pf) return big ? Variant<QPL, 4, true, 1, 16>::launch(a, smem, st)
+                         : Variant<QPL, 4, true, 2, 8>::launch(a, smem, st);
+      return big ? Variant<QPL, 4, false, 1, 16>::launch(a, smem, st)
+                 : Variant<QPL, 4, false, 3, 8>::launch(a, smem, st);
+    }
+    if (pf) return Variant<QPL, 2, true, 3, 8>::launch(a, smem, st);
     return big ? Variant<QPL, 2, false, 2, 16>::launch(a, smem, st)
                : Variant<QPL, 2, false, 4, 8>::launch(a, smem, st);
   } else if constexpr (QPL == 4) {
@@ -783,6 +795,7 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.slices_fixed = tune.slices;
   a.rw_fixed = tune.rows_per_warp;
   a.warps_fixed = tune.warps;
+  a.pf_fixed = tune.prefetch > 0 ? 1 : (tune.rows_per_warp > 0 ? -1 : 0);
   a.ws_base = ws;
   a.ws_size = ws_size;
   a.ws_part = nullptr;
@@ -840,6 +853,14 @@ int glm_prepare() {
   // Sets the shared-memory attribute of every variant before any stream
   // capture.
   int rc = Variant<1, 4, false, 3, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<1, 8, false, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<1, 4, true, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<1, 4, true, 1, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<1, 2, true, 3, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 8, false, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 4, true, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 4, true, 1, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = Variant<2, 2, true, 3, 8>::prepare();
   if (rc == GBSGMC_OK) rc = Variant<1, 4, false, 1, 16>::prepare();
   if (rc == GBSGMC_OK) rc = Variant<1, 2, false, 4, 8>::prepare();
   if (rc == GBSGMC_OK) rc = Variant<1, 2, false, 2, 16>::prepare();

@@ -16,8 +16,9 @@ int check_launch(const char* what);
 // Launch shape of the GLM kernel; 0 lets the library choose.
 struct GlmTune {
   int slices = 0;         // CTAs per chain
-  int rows_per_warp = 0;  // 2 or 4 (d <= 256 only)
+  int rows_per_warp = 0;  // 2, 4 or 8 (d <= 256 only)
   int warps = 0;          // warps per CTA: 8 or 16
+  int prefetch = 0;       // 1: two register tiles in flight per warp
 };
 
 size_t glm_ws_bytes(int chains, int n, int d);

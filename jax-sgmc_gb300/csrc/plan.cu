@@ -176,16 +176,18 @@ int autotune(GlmPlan* p) {
     const double rows_per_cta = (384.0 * 1024.0) / (4.0 * std::max<int64_t>(p->model.ld, 1));
     const int base = std::max(1, static_cast<int>(std::ceil(n / rows_per_cta)));
     const int ss[] = {1, base / 2, base, base + 1, 2 * base};
-    const int rws[] = {2, 4};
-    const int wps[] = {8, 16};
     for (int s : ss) {
       if (s < 1 || s > 64 || (s > 1 && n / s < 32)) continue;
-      for (int w : wps) {
-        if (d <= 256) {
-          for (int r : rws) cands.push_back(GlmTune{s, r, w});
-        } else {
-          cands.push_back(GlmTune{s, 0, w});
-        }
+      bool dup = false;
+      for (const GlmTune& t : cands) dup = dup || t.slices == s;
+      if (dup) continue;
+      if (d <= 256) {
+        // (rows per warp, warps, prefetch)
+        const int shapes[][3] = {{2, 8, 0}, {4, 8, 0}, {4, 8, 1}, {8, 8, 0},
+                                 {2, 8, 1}, {2, 16, 0}, {4, 16, 0}, {4, 16, 1}};
+        for (const auto& sh : shapes) cands.push_back(GlmTune{s, sh[0], sh[1], sh[2]});
+      } else {
+        for (int w : {8, 16}) cands.push_back(GlmTune{s, 0, w, 0});
       }
     }
   }
@@ -238,8 +240,9 @@ int autotune(GlmPlan* p) {
       float ms = 0.0f;
       cudaEventElapsedTime(&ms, e0, e1);
       if (verbose)
-        std::fprintf(stderr, "gbsgmc autotune: slices %d rows/warp %d warps %d: %.4f ms\n",
-                     t.slices, t.rows_per_warp, t.warps, ms / 6.0f);
+        std::fprintf(stderr,
+                     "gbsgmc autotune: slices %d rows/warp %d warps %d prefetch %d: %.4f ms\n",
+                     t.slices, t.rows_per_warp, t.warps, t.prefetch, ms / 6.0f);
       if (ms < best_ms) {
         best_ms = ms;
         best = t;
@@ -355,15 +358,16 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
 }
 
 extern "C" int gbsgmc_plan_launch_shape(const gbsgmc_plan* p, int* slices,
-                                        int* rows_per_warp, int* warps) {
+                                        int* rows_per_warp, int* warps, int* prefetch) {
   if (p == nullptr || slices == nullptr || rows_per_warp == nullptr ||
-      warps == nullptr)
+      warps == nullptr || prefetch == nullptr)
     return set_error(GBSGMC_ERR_ARG, "plan_launch_shape: null argument");
-  *slices = *rows_per_warp = *warps = 0;
+  *slices = *rows_per_warp = *warps = *prefetch = 0;
   if (const GlmPlan* g = dynamic_cast<const GlmPlan*>(p)) {
     *slices = g->tune.slices;
     *rows_per_warp = g->tune.rows_per_warp;
     *warps = g->tune.warps;
+    *prefetch = g->tune.prefetch;
   }
   return GBSGMC_OK;
 }

@@ -181,7 +181,7 @@ SIGNATURES = {
                                            _vp, _i, _vp]),
     "gbsgmc_plan_run": (_i, [_vp, _i64, _i64, _vp]),
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
-    "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i)]),
+    "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i), _P(_i)]),
     "gbsgmc_plan_destroy": (_i, [_vp]),
     "gbsgmc_gemm_bf16": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64, _vp,
                               _i64, _i64, _i, _i, _i, _i, _vp, _vp]),

@@ -75,11 +75,12 @@ class SgldGlmPlan:
               _lib.stream_handle())
 
   def launch_shape(self):
-    """(CTAs per chain, rows per warp, warps per CTA) from the autotuner."""
-    s, r, w = _lib.C.c_int(), _lib.C.c_int(), _lib.C.c_int()
+    """(CTAs per chain, rows per warp, warps per CTA, prefetch) from the
+    autotuner."""
+    s, r, w, f = _lib.C.c_int(), _lib.C.c_int(), _lib.C.c_int(), _lib.C.c_int()
     _lib.call("gbsgmc_plan_launch_shape", self.handle, _lib.C.byref(s),
-              _lib.C.byref(r), _lib.C.byref(w))
-    return s.value, r.value, w.value
+              _lib.C.byref(r), _lib.C.byref(w), _lib.C.byref(f))
+    return s.value, r.value, w.value, f.value
 
   def launches(self, steps) -> int:
     return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps)))
