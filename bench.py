@@ -780,8 +780,9 @@ def cnn_kernel_only(args):
 
 
 def mlp_kernel_only(args):
-  """`--steps` batched value-and-gradient calls of the 64-chain workload and
-  nothing else (a short run for profilers); no JSON line."""
+  """`--steps` batched value-and-gradient calls of the 64-chain workload,
+  then `--steps` OBABO steps of the network plan (a short run for
+  profilers); no JSON line."""
   import torch
   from gbsgmc import data, likelihoods as L, potential
   rng = np.random.default_rng(20261203 + 3)
@@ -796,6 +797,19 @@ def mlp_kernel_only(args):
     pot.evaluate(W, idx, ds, grad=True)
   torch.cuda.synchronize()
   pot.check_status()
+  # Then `--steps` OBABO steps of the graph-captured plan (one block).
+  from gbsgmc import engine
+  words = np.array([pcg_words(c) for c in range(MLP_CHAINS)], np.uint64).view(np.int64)
+  pcg = torch.from_numpy(words.copy()).cuda()
+  h = torch.full((args.steps,), 1e-7, dtype=torch.float32, device="cuda")
+  t = torch.ones(args.steps, dtype=torch.float32, device="cuda")
+  plan = engine.NetPlan(pot, ds, W, torch.zeros_like(W), MLP_MB, "obabo", h, t,
+                        engine.IndexSource(pcg=pcg), noise_seed=7, friction=1.0,
+                        block_steps=args.steps)
+  plan.run(0, args.steps)
+  torch.cuda.synchronize()
+  plan.check_status()
+  plan.close()
 
 
 def run_mlp(args):

@@ -72,6 +72,58 @@ def test_mlp_abi_shapes_and_validation_without_a_gpu():
     L.MLPGaussian(d_in=60)
 
 
+def test_cnn_and_plan_abi_validation_without_a_gpu():
+  import ctypes as C
+  from gbsgmc import _lib, likelihoods as L
+  lib = _lib.load()
+  assert lib.gbsgmc_cnn_param_count() == 113_738 == L.CNNSoftmax().param_count
+  assert lib.gbsgmc_cnn_workspace_bytes(8, 255) == 0
+  assert lib.gbsgmc_cnn_workspace_bytes(8, 256) > 8 * 256 * 1024 * 64 * 2
+  m = _lib.Cnn(1000, 1000, 3080, 16, 16 + 4 * 3072, 3080, 1.0, 1.0)
+  assert lib.gbsgmc_cnn_value_and_grad(C.byref(m), 2, 7, 16, 7, None, 16, 16,
+                                       None, None, None, 256, 1 << 40, 16,
+                                       None) == _lib.ERR_SHAPE
+  short = _lib.Cnn(1000, 1000, 1000, 16, 16, 3080, 1.0, 1.0)
+  assert lib.gbsgmc_cnn_value_and_grad(C.byref(short), 2, 8, 16, 8, None, 16,
+                                       16, None, None, None, 256, 1 << 40, 16,
+                                       None) == _lib.ERR_ARG
+  # Plans reject inconsistent integrator settings before touching the GPU.
+  mlp = _lib.Mlp(64, 256, 256, 1, 100, 100, 72, 16, None, 0.1, 1.0, 1.0, 0)
+  h = C.c_void_p()
+  bad = _lib.Integrator(_lib.INTEGRATOR_SGHMC, 3, 0.5, 0.9, 1e-5, 0, None)
+  rc = lib.gbsgmc_mlp_plan_create(C.byref(h), C.byref(mlp), 2, 128, C.byref(bad),
+                                  16, 16, _lib.sched(), _lib.noise(),
+                                  _lib.IndexSrc(None, 0, 0, 0), 16, None, None,
+                                  50, 16)
+  assert rc == _lib.ERR_ARG and b"leapfrog" in lib.gbsgmc_last_error()
+  nomom = _lib.Integrator(_lib.INTEGRATOR_OBABO, 1, 0.5, 0.9, 1e-5, 0, None)
+  rc = lib.gbsgmc_mlp_plan_create(C.byref(h), C.byref(mlp), 2, 128, C.byref(nomom),
+                                  16, None, _lib.sched(), _lib.noise(),
+                                  _lib.IndexSrc(None, 0, 0, 0), 16, None, None,
+                                  50, 16)
+  assert rc == _lib.ERR_ARG
+  tp = _lib.Tempering(50, 0, 1.0, 7, 16, 16, 16, 16)
+  rc = lib.gbsgmc_mlp_resgld_plan_create(C.byref(h), C.byref(mlp), 4, 128, 16,
+                                         16, None, 0.9, 1e-5, _lib.sched(),
+                                         _lib.noise(), _lib.IndexSrc(None, 0, 0, 0),
+                                         C.byref(tp), 16, None, 60, 16)
+  assert rc == _lib.ERR_ARG  # 60 steps per block is not a multiple of 50
+  assert lib.gbsgmc_resgld_exchange_adjacent(1, 10, 16, None, 16, None,
+                                             _lib.sched(), 50, 16, 1.0, 0, None,
+                                             16, None, None, None) == _lib.ERR_ARG
+
+
+def test_cnn_unravel_follows_sorted_keys():
+  from gbsgmc import likelihoods as L, util
+  lik = L.CNNSoftmax()
+  flat = lik.init(np.random.default_rng(0))
+  tree = lik.unravel(flat)
+  again, _ = util.ravel(tree)
+  np.testing.assert_array_equal(again, flat)
+  assert tree["conv2"]["w"].shape == (3, 3, 32, 64)
+  assert tree["linear"]["w"].shape == (2048, 10)
+
+
 def test_mlp_unravel_follows_sorted_keys():
   from gbsgmc import likelihoods as L, util
   lik = L.MLPGaussian(d_in=64, h1=256, h2=512)
