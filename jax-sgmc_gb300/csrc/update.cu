@@ -19,11 +19,16 @@ struct Grid4 {
   int64_t groups;
 };
 
+// Blocks per chain: enough to fill the GPU about eight times over with all
+// chains together, and no more -- the threads then stride over their chain's
+// parameters, so per-chain reductions (kinetic energies) take one atomic
+// per block rather than one per warp.
 Grid4 grid4(int chains, int64_t P) {
   Grid4 g;
   g.groups = (P + 3) / 4;
   int64_t bx = (g.groups + kThreads - 1) / kThreads;
-  bx = std::min<int64_t>(bx, 65535);
+  const int64_t fill = std::max<int64_t>(4, (152 * 8 + chains - 1) / std::max(chains, 1));
+  bx = std::min<int64_t>(std::min<int64_t>(bx, fill), 65535);
   g.grid = dim3(static_cast<unsigned>(std::max<int64_t>(bx, 1)),
                 static_cast<unsigned>(chains));
   return g;
@@ -74,11 +79,13 @@ __global__ void sgld_update_kernel(int chains, int64_t P, float* x,
   }
 }
 
-// Per-thread kinetic-energy partials are fp32 (a thread sees few
-// parameters); the warp sum and the accumulation across warps are fp64.
+// Per-thread kinetic-energy partials are fp32; the block sum and the
+// accumulation across blocks are fp64, one atomic per block.
 __device__ __forceinline__ void add_ke(double* ke, int c, float part) {
-  const double w = warp_sum(static_cast<double>(part));
-  if ((threadIdx.x & 31) == 0 && ke != nullptr) atomicAdd(ke + c, w);
+  if (ke == nullptr) return;
+  __shared__ double red[32];
+  const double tot = block_sum(static_cast<double>(part), red);
+  if (threadIdx.x == 0) atomicAdd(ke + c, tot);
 }
 
 __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
