@@ -34,6 +34,51 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   double* sample_lik_dev, void* ws, size_t ws_size,
                   int* status_dev, cudaStream_t stream, GlmTune tune);
 
+// update.cu: fusions of the integrator updates used by the network plans.
+struct UpdateFusion {
+  float prior_pf = 0.f;       // adds pf * x to the gradient (the prior term)
+  void* mirror = nullptr;     // BF16 copy of the new x[0, mirror_count) of
+  int64_t mirror_count = 0;   //   each chain, chain stride mirror_stride
+  int64_t mirror_stride = 0;  //   (elements; both multiples of 4)
+  double* sq_parts = nullptr; // per-block sums of squares of the new x,
+                              //   [chains, update_blocks(chains, P)]
+};
+int update_blocks(int chains, int64_t P);
+int sgld_update_fused(int chains, int64_t P, float* x, const float* g, float* v,
+                      float alpha, float lmbd, const gbsgmc_sched* sched,
+                      const gbsgmc_noise* noise, const UpdateFusion& f,
+                      cudaStream_t st);
+int obabo_first_fused(int chains, int64_t P, float* x, float* p, const float* g1,
+                      const float* mass, float friction, double* ke_start,
+                      const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                      const UpdateFusion& f, cudaStream_t st);
+int obabo_second_fused(int chains, int64_t P, const float* x, float* p,
+                       const float* g2, const float* mass, float friction,
+                       double* ke_end, const gbsgmc_sched* sched,
+                       const gbsgmc_noise* noise, const UpdateFusion& f,
+                       cudaStream_t st);
+int sghmc_position_fused(int chains, int64_t P, float* x, float* p, const float* mass,
+                         float friction, const gbsgmc_sched* sched,
+                         const UpdateFusion& f, cudaStream_t st);
+int sghmc_momentum_fused(int chains, int64_t P, const float* x, float* p,
+                         const float* g, float friction, const gbsgmc_sched* sched,
+                         const gbsgmc_noise* noise, const UpdateFusion& f,
+                         cudaStream_t st);
+// The mirror and squares of x itself (before the first fused update).
+int mirror_fused(int chains, int64_t P, const float* x, const UpdateFusion& f,
+                 cudaStream_t st);
+
+// mlp.cu: the value and likelihood gradient with the weights' BF16 copy and
+// sums of squares supplied by the integrator (UpdateFusion), the prior's
+// gradient left to the update.
+int mlp_mirror_region(const gbsgmc_mlp* model, int chains, int n, void* ws,
+                      void** mirror, int64_t* count, int64_t* stride);
+int mlp_value_and_grad_fused(const gbsgmc_mlp* model, int chains, int n,
+                             const int32_t* idx, int64_t idx_stride, const float* w,
+                             double* U, float* grad, double* lk_var, void* ws,
+                             size_t ws_bytes, int* status, cudaStream_t st,
+                             const double* sq_parts, int sq_count);
+
 // rng.cu
 int launch_philox_index(uint64_t seed, int chain_base, int chains,
                         const int64_t* base, int64_t first_step, int steps,

@@ -178,6 +178,10 @@ struct MlpArgs {
   int* status;
   // Ragged batch: rows of chain c are n_true[c] <= n (null: all n).
   const int32_t* n_true;
+  // Fused with the integrator: the BF16 weights and the sums of squares
+  // (sq_count per chain in psq) are supplied, the prior's gradient is the
+  // update's.
+  int fused, sq_count;
   int *prefix1, *prefix2, *kblocks;
   // workspace views
   bf16 *wb, *xb, *z1, *z2g;
@@ -624,7 +628,7 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
   const int c = blockIdx.y, t = threadIdx.x;
   const float* w = a.w + static_cast<int64_t>(c) * s.P;
   const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;
-  const float pf = a.prior_scale > 0.f
+  const float pf = a.prior_scale > 0.f && !a.fused
                        ? static_cast<float>(1.0 / (s2 * a.temperature))
                        : 0.f;
   const int nc = chain_rows(a, c), npad = chain_rows_padded(a, c);
@@ -727,7 +731,7 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   a.pw3 = view<float>(ws, L.pw3);
   a.pb2 = view<float>(ws, L.pb2);
   a.pb1 = view<float>(ws, L.pb1);
-  a.psq = view<double>(ws, L.psq);
+  if (!a.fused) a.psq = view<double>(ws, L.psq);
   a.plk = view<double>(ws, L.plk);
   a.prefix1 = view<int>(ws, L.rag);
   a.prefix2 = a.prefix1 + (a.chains + 1);
@@ -744,13 +748,15 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     ksl.kblocks = a.kblocks;
   }
   const int64_t pw = matrix_params(s);
-  const int nprep = prep_blocks(s);
+  const int nprep = a.fused ? a.sq_count : prep_blocks(s);
   const bf16* w1b = a.wb;
   const bf16* w2b = a.wb + s.oW2;
   int rc;
 
-  mlp_prep_kernel<<<dim3(nprep, C), 256, 0, st>>>(a);
-  if ((rc = check_launch("mlp_prep_kernel")) != GBSGMC_OK) return rc;
+  if (!a.fused) {
+    mlp_prep_kernel<<<dim3(nprep, C), 256, 0, st>>>(a);
+    if ((rc = check_launch("mlp_prep_kernel")) != GBSGMC_OK) return rc;
+  }
   mlp_gather_kernel<<<dim3(n / kTile, D / kTile, C), 256, 0, st>>>(a);
   if ((rc = check_launch("mlp_gather_kernel")) != GBSGMC_OK) return rc;
 
@@ -800,8 +806,8 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     const EpiGradCols e8{a.grad, s.P, s.oW1, H1};
     if ((rc = launch_gemm<64, true, true>(m_z1mn, m_xbmn, C, H1, D, n, a.status, e8, st, ksl)))
       return rc;
-    if (pf != 0.f) {
-      mlp_prior_kernel<<<dim3(nprep - 1, C), 256, 0, st>>>(a, pf);
+    if (pf != 0.f && !a.fused) {
+      mlp_prior_kernel<<<dim3(prep_blocks(s) - 1, C), 256, 0, st>>>(a, pf);
       if ((rc = check_launch("mlp_prior_kernel")) != GBSGMC_OK) return rc;
     }
   }
@@ -833,7 +839,8 @@ int mlp_call(const gbsgmc_mlp* model, int chains, int n, const int32_t* n_dev,
              const int32_t* idx_dev, int64_t idx_stride, const float* mask_dev,
              const float* w_dev, double* U_dev, float* grad_dev, float* lk_dev,
              double* lk_var_dev, void* workspace_dev, size_t workspace_bytes,
-             int* status_dev, gbsgmc_stream_t stream) {
+             int* status_dev, gbsgmc_stream_t stream, const double* sq_parts = nullptr,
+             int sq_count = 0) {
   int rc = check_model(model, "mlp_value_and_grad");
   if (rc != GBSGMC_OK) return rc;
   if (chains < 0 || n < 0)
@@ -880,10 +887,37 @@ int mlp_call(const gbsgmc_mlp* model, int chains, int n, const int32_t* n_dev,
   a.lk_var = lk_var_dev;
   a.status = status_dev;
   a.n_true = n_dev;
+  a.fused = sq_parts != nullptr ? 1 : 0;
+  a.sq_count = sq_count;
+  a.psq = const_cast<double*>(sq_parts);
   return run_mlp(a, L, workspace_dev, static_cast<cudaStream_t>(stream));
 }
 
 }  // namespace
+
+namespace gbsgmc {
+
+int mlp_mirror_region(const gbsgmc_mlp* model, int chains, int n, void* ws, void** mirror,
+                      int64_t* count, int64_t* stride) {
+  const MlpShape s = mlp_shape(model->d_in, model->h1, model->h2);
+  const MlpLayout L = mlp_layout(s, chains, n);
+  *mirror = static_cast<unsigned char*>(ws) + L.wb;
+  *count = matrix_params(s);
+  *stride = matrix_params(s);
+  return GBSGMC_OK;
+}
+
+int mlp_value_and_grad_fused(const gbsgmc_mlp* model, int chains, int n, const int32_t* idx,
+                             int64_t idx_stride, const float* w, double* U, float* grad,
+                             double* lk_var, void* ws, size_t ws_bytes, int* status,
+                             cudaStream_t st, const double* sq_parts, int sq_count) {
+  if (sq_parts == nullptr || sq_count < 1)
+    return set_error(GBSGMC_ERR_ARG, "mlp (fused): missing sums of squares");
+  return mlp_call(model, chains, n, nullptr, idx, idx_stride, nullptr, w, U, grad, nullptr,
+                  lk_var, ws, ws_bytes, status, st, sq_parts, sq_count);
+}
+
+}  // namespace gbsgmc
 
 extern "C" int gbsgmc_mlp_value_and_grad(
     const gbsgmc_mlp* model, int chains, int n, const int32_t* idx_dev,

@@ -6,6 +6,7 @@
 // and the integrator's elementwise kernels over [chains, P].  The integrator
 // kernels read their step index from the plan's device counter, so the Philox
 // noise of step k is the same whether the step runs inside a graph or alone.
+#include <cstdlib>
 #include <functional>
 #include <new>
 
@@ -43,6 +44,13 @@ struct NetPlan final : gbsgmc_plan {
   int32_t* idx = nullptr;  // owned [G, chains, draws * n]
   void* ws = nullptr;      // owned
   size_t ws_size = 0;
+  // Fused with the updates (network likelihoods that support it): the
+  // updates add the prior's gradient, keep the BF16 weight mirror in the
+  // workspace current and write the sums of squares the value needs.
+  bool fused = false;
+  UpdateFusion fz;          // the mirror and squares of the new positions
+  float pf = 0.f;           // 1 / (s^2 T) of the prior, 0 for a flat prior
+  double* sq = nullptr;     // owned [chains, update_blocks]
 
   int draws() const { return integ.kind == GBSGMC_INTEGRATOR_OBABO ? 2 : 1; }
 
@@ -52,7 +60,10 @@ struct NetPlan final : gbsgmc_plan {
     cudaFree(U2);
     cudaFree(idx);
     cudaFree(ws);
+    cudaFree(sq);
   }
+
+  int enqueue_fused(int g, cudaStream_t s);
 
   int step_multiple() const override {
     return integ.kind == GBSGMC_INTEGRATOR_SGHMC ? integ.leapfrog_steps : 1;
@@ -69,6 +80,7 @@ struct NetPlan final : gbsgmc_plan {
   }
 
   int enqueue(int g, cudaStream_t s) override {
+    if (fused) return enqueue_fused(g, s);
     const int per = draws() * n;
     const int64_t cn = static_cast<int64_t>(chains) * per;
     int rc;
@@ -122,6 +134,67 @@ struct NetPlan final : gbsgmc_plan {
     return plan_advance(this, g, s);
   }
 };
+
+int NetPlan::enqueue_fused(int g, cudaStream_t s) {
+  const int per = draws() * n;
+  const int64_t cn = static_cast<int64_t>(chains) * per;
+  int rc;
+  if (isrc.pcg_dev != nullptr) {
+    rc = gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows, static_cast<int64_t>(g) * per,
+                                 per, idx, per, cn, status, s);
+  } else {
+    rc = launch_philox_index(isrc.index_seed, isrc.chain_base, chains, base, 0, g, per, rows,
+                             idx, per, cn, s);
+  }
+  if (rc != GBSGMC_OK) return rc;
+  // The positions may have changed since the last block: refresh the mirror
+  // and the squares once per block; the updates keep them current after.
+  if ((rc = mirror_fused(chains, P, x, fz, s))) return rc;
+  UpdateFusion prior_only;
+  prior_only.prior_pf = pf;
+  UpdateFusion with_prior = fz;
+  with_prior.prior_pf = pf;
+  double* ke_start = ke;
+  double* ke_end = ke != nullptr ? ke + chains : nullptr;
+  for (int j = 0; j < g; ++j) {
+    gbsgmc_sched sj = sched;
+    sj.base_dev = base;
+    sj.offset = j;
+    const int32_t* ij = idx + j * cn;
+    switch (integ.kind) {
+      case GBSGMC_INTEGRATOR_SGLD:
+        if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+        rc = sgld_update_fused(chains, P, x, grad, aux, integ.alpha, integ.lmbd, &sj, &noise,
+                               with_prior, s);
+        break;
+      case GBSGMC_INTEGRATOR_OBABO:
+        if ((rc = grad_fn(ij, per, U, nullptr, s))) return rc;
+        if ((rc = obabo_first_fused(chains, P, x, aux, grad, integ.mass_dev, integ.friction,
+                                    ke_start, &sj, &noise, with_prior, s)))
+          return rc;
+        if ((rc = grad_fn(ij + n, per, U2, lk_var, s))) return rc;
+        if ((rc = obabo_second_fused(chains, P, x, aux, grad, integ.mass_dev, integ.friction,
+                                     ke_end, &sj, &noise, prior_only, s)))
+          return rc;
+        mean_pair_kernel<<<(chains + 127) / 128, 128, 0, s>>>(chains, U, U2);
+        rc = check_launch("plan: potential mean");
+        break;
+      default:  // SGHMC
+        if (j % integ.leapfrog_steps == 0 &&
+            (rc = gbsgmc_sghmc_resample(chains, P, aux, integ.mass_dev, &sj, &noise, s)))
+          return rc;
+        if ((rc = sghmc_position_fused(chains, P, x, aux, integ.mass_dev, integ.friction, &sj,
+                                       fz, s)))
+          return rc;
+        if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+        rc = sghmc_momentum_fused(chains, P, x, aux, grad, integ.friction, &sj, &noise,
+                                  prior_only, s);
+        break;
+    }
+    if (rc != GBSGMC_OK) return rc;
+  }
+  return plan_advance(this, g, s);
+}
 
 // reSGLD over R replicas with ragged minibatches and adjacent exchanges.
 struct ResgldPlan final : gbsgmc_plan {
@@ -264,12 +337,34 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
     float* grad = p->grad;
     void* wsp = p->ws;
     const float* x = x_dev;
-    p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
-                     const int32_t* idx, int64_t stride, double* U, double* var,
-                     cudaStream_t s) {
-      return gbsgmc_mlp_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
-                                       nullptr, var, wsp, ws, status_dev, s);
-    };
+    const char* env = std::getenv("GBSGMC_NO_STEP_FUSION");
+    p->fused = !(env != nullptr && env[0] == '1') && integ->mass_dev == nullptr;
+    if (p->fused) {
+      const int nb = update_blocks(chains, p->P);
+      if ((rc = cuda_err(cudaMalloc(&p->sq, sizeof(double) * chains * nb),
+                         "mlp_plan_create: squares")))
+        break;
+      mlp_mirror_region(&m, chains, n, wsp, &p->fz.mirror, &p->fz.mirror_count,
+                        &p->fz.mirror_stride);
+      p->fz.sq_parts = p->sq;
+      if (m.prior_scale > 0.f)
+        p->pf = static_cast<float>(1.0 / (static_cast<double>(m.prior_scale) *
+                                          m.prior_scale * m.temperature));
+      const double* sqp = p->sq;
+      p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev, sqp, nb](
+                       const int32_t* idx, int64_t stride, double* U, double* var,
+                       cudaStream_t s) {
+        return mlp_value_and_grad_fused(&m, chains, n, idx, stride, x, U, grad, var, wsp, ws,
+                                        status_dev, s, sqp, nb);
+      };
+    } else {
+      p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
+                       const int32_t* idx, int64_t stride, double* U, double* var,
+                       cudaStream_t s) {
+        return gbsgmc_mlp_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
+                                         nullptr, var, wsp, ws, status_dev, s);
+      };
+    }
     rc = plan_capture(p);
   } while (false);
   if (rc != GBSGMC_OK) {

@@ -7,7 +7,10 @@
 // parameters per thread so that one Philox call feeds one thread.
 #include <algorithm>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
+#include "internal.h"
 
 namespace gbsgmc {
 namespace {
@@ -41,10 +44,70 @@ __device__ __forceinline__ float mass_sqrt(const float* m, int64_t j) {
   return m != nullptr ? sqrtf(__ldg(m + j)) : 1.0f;
 }
 
+// Optional fusions of an update (see UpdateFusion): the prior term added to
+// the gradient, a BF16 mirror of the new positions and per-block sums of
+// their squares.
+struct Fuse {
+  float pf;
+  uint32_t* mirror;  // BF16 pairs
+  int64_t mcount, mstride;
+  double* sq;
+};
+
+Fuse to_fuse(const UpdateFusion* f) {
+  Fuse r{0.f, nullptr, 0, 0, nullptr};
+  if (f != nullptr) {
+    r.pf = f->prior_pf;
+    r.mirror = static_cast<uint32_t*>(f->mirror);
+    r.mcount = f->mirror_count;
+    r.mstride = f->mirror_stride;
+    r.sq = f->sq_parts;
+  }
+  return r;
+}
+
+// New positions xn[0..3] of parameters j0..j0+3 of chain c (j < P valid).
+__device__ __forceinline__ void fuse_store(const Fuse& f, int c, int64_t j0, int64_t P,
+                                           const float (&xn)[4], float& sq) {
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+    if (j0 + e < P) sq = fmaf(xn[e], xn[e], sq);
+  if (f.mirror != nullptr && j0 < f.mcount) {  // mcount % 4 == 0: whole groups
+    const __nv_bfloat162 a = __floats2bfloat162_rn(xn[0], xn[1]);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(xn[2], xn[3]);
+    uint2 w;
+    w.x = *reinterpret_cast<const uint32_t*>(&a);
+    w.y = *reinterpret_cast<const uint32_t*>(&b);
+    *reinterpret_cast<uint2*>(f.mirror + (static_cast<int64_t>(c) * f.mstride + j0) / 2) = w;
+  }
+}
+
+__device__ __forceinline__ void fuse_finish(const Fuse& f, int c, float sq) {
+  if (f.sq == nullptr) return;
+  __shared__ double red[32];
+  const double tot = block_sum(static_cast<double>(sq), red);
+  if (threadIdx.x == 0) f.sq[static_cast<int64_t>(c) * gridDim.x + blockIdx.x] = tot;
+}
+
+__global__ void mirror_kernel(int64_t P, const float* x, Fuse f) {
+  const int c = blockIdx.y;
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  float sq = 0.f;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xn[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) xn[e] = 4 * q + e < P ? x[off + 4 * q + e] : 0.f;
+    fuse_store(f, c, 4 * q, P, xn, sq);
+  }
+  fuse_finish(f, c, sq);
+}
+
 __global__ void sgld_update_kernel(int chains, int64_t P, float* x,
                                    const float* g, float* v, float alpha,
                                    float lmbd, Sched sched, Noise noise,
-                                   float* samples) {
+                                   float* samples, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
@@ -53,15 +116,16 @@ __global__ void sgld_update_kernel(int chains, int64_t P, float* x,
   const float noise_scale = sqrtf(2.0f * T * h);
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
+  float sq = 0.f;
   for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    float xi[4];
+    float xi[4], xs[4] = {0.f, 0.f, 0.f, 0.f};
     noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_SGLD, xi);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int64_t j = 4 * q + e;
       if (j >= P) break;
-      const float gj = g[off + j];
+      const float gj = fz.pf != 0.f ? fmaf(fz.pf, x[off + j], g[off + j]) : g[off + j];
       const float scaled_gradient = -h * gj;
       const float scaled_noise = noise_scale * xi[e];
       float xn;
@@ -74,9 +138,12 @@ __global__ void sgld_update_kernel(int chains, int64_t P, float* x,
         xn = x[off + j] + (scaled_gradient + scaled_noise);
       }
       x[off + j] = xn;
+      xs[e] = xn;
       if (slot >= 0) samples[(static_cast<int64_t>(slot) * chains + c) * P + j] = xn;
     }
+    fuse_store(fz, c, 4 * q, P, xs, sq);
   }
+  fuse_finish(fz, c, sq);
 }
 
 // Per-thread kinetic-energy partials are fp32; the block sum and the
@@ -91,7 +158,7 @@ __device__ __forceinline__ void add_ke(double* ke, int c, float part) {
 __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
                                    const float* g1, const float* mass,
                                    float friction, double* ke_start,
-                                   Sched sched, Noise noise) {
+                                   Sched sched, Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
@@ -102,30 +169,35 @@ __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
   const float half = 0.5f * h;
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
-  float ke = 0.0f;
+  float ke = 0.0f, sq = 0.0f;
   for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    float xi[4];
+    float xi[4], xs[4] = {0.f, 0.f, 0.f, 0.f};
     noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_OBABO_1, xi);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int64_t j = 4 * q + e;
       if (j >= P) break;
       const float mi = mass_inv(mass, j);
+      const float xj = x[off + j];
+      const float gj = fz.pf != 0.f ? fmaf(fz.pf, xj, g1[off + j]) : g1[off + j];
       float pj = keep * p[off + j] + inject * (mass_sqrt(mass, j) * xi[e]);
       ke = fmaf(0.5f * pj, mi * pj, ke);
-      pj = -half * g1[off + j] + pj;
+      pj = -half * gj + pj;
       p[off + j] = pj;
-      x[off + j] = x[off + j] + h * (mi * pj);
+      xs[e] = xj + h * (mi * pj);
+      x[off + j] = xs[e];
     }
+    fuse_store(fz, c, 4 * q, P, xs, sq);
   }
   add_ke(ke_start, c, ke);
+  fuse_finish(fz, c, sq);
 }
 
-__global__ void obabo_second_kernel(int chains, int64_t P, float* p,
+__global__ void obabo_second_kernel(int chains, int64_t P, const float* x, float* p,
                                     const float* g2, const float* mass,
                                     float friction, double* ke_end,
-                                    Sched sched, Noise noise) {
+                                    Sched sched, Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
@@ -146,7 +218,8 @@ __global__ void obabo_second_kernel(int chains, int64_t P, float* p,
       const int64_t j = 4 * q + e;
       if (j >= P) break;
       const float mi = mass_inv(mass, j);
-      float pj = -half * g2[off + j] + p[off + j];
+      const float gj = fz.pf != 0.f ? fmaf(fz.pf, x[off + j], g2[off + j]) : g2[off + j];
+      float pj = -half * gj + p[off + j];
       ke = fmaf(0.5f * pj, mi * pj, ke);
       pj = keep * pj + inject * (mass_sqrt(mass, j) * xi[e]);
       p[off + j] = pj;
@@ -178,25 +251,36 @@ __global__ void sghmc_resample_kernel(int chains, int64_t P, float* p,
 __global__ void sghmc_position_kernel(int chains, int64_t P, float* x,
                                       float* p, const float* mass,
                                       const float* fric, float friction,
-                                      Sched sched) {
+                                      Sched sched, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
+  const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
-  for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-       j < P; j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const float f = fric != nullptr ? __ldg(fric + j) : friction;
-    const float pj = p[off + j];
-    const float sm = mass_inv(mass, j) * pj;
-    x[off + j] = x[off + j] + h * sm;
-    p[off + j] = pj + (-h * f) * sm;
+  float sq = 0.f;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xs[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      const float f = fric != nullptr ? __ldg(fric + j) : friction;
+      const float pj = p[off + j];
+      const float sm = mass_inv(mass, j) * pj;
+      xs[e] = x[off + j] + h * sm;
+      x[off + j] = xs[e];
+      p[off + j] = pj + (-h * f) * sm;
+    }
+    fuse_store(fz, c, 4 * q, P, xs, sq);
   }
+  fuse_finish(fz, c, sq);
 }
 
-__global__ void sghmc_momentum_kernel(int chains, int64_t P, float* p,
+__global__ void sghmc_momentum_kernel(int chains, int64_t P, const float* x, float* p,
                                       const float* g, const float* fric,
                                       float friction, Sched sched,
-                                      Noise noise) {
+                                      Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
@@ -212,7 +296,8 @@ __global__ void sghmc_momentum_kernel(int chains, int64_t P, float* p,
       const int64_t j = 4 * q + e;
       if (j >= P) break;
       const float f = fric != nullptr ? __ldg(fric + j) : friction;
-      float pj = p[off + j] + (-h) * g[off + j];
+      const float gj = fz.pf != 0.f ? fmaf(fz.pf, x[off + j], g[off + j]) : g[off + j];
+      float pj = p[off + j] + (-h) * gj;
       pj = pj + f * (noise_scale * xi[e]);
       p[off + j] = pj;
     }
@@ -362,7 +447,7 @@ extern "C" int gbsgmc_sgld_update(int chains, int64_t P, float* x_dev,
   const Grid4 g = grid4(chains, P);
   sgld_update_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
       chains, P, x_dev, g_dev, v_dev, alpha, lmbd, to_sched(sched),
-      to_noise(noise), samples_dev);
+      to_noise(noise), samples_dev, to_fuse(nullptr));
   return check_launch("sgld_update");
 }
 
@@ -381,7 +466,7 @@ extern "C" int gbsgmc_obabo_first(int chains, int64_t P, float* x_dev,
   const Grid4 g = grid4(chains, P);
   obabo_first_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
       chains, P, x_dev, p_dev, g1_dev, mass_dev, friction, ke_start_dev,
-      to_sched(sched), to_noise(noise));
+      to_sched(sched), to_noise(noise), to_fuse(nullptr));
   return check_launch("obabo_first");
 }
 
@@ -398,8 +483,8 @@ extern "C" int gbsgmc_obabo_second(int chains, int64_t P, float* p_dev,
   if (chains == 0 || P == 0) return GBSGMC_OK;
   const Grid4 g = grid4(chains, P);
   obabo_second_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-      chains, P, p_dev, g2_dev, mass_dev, friction, ke_end_dev,
-      to_sched(sched), to_noise(noise));
+      chains, P, nullptr, p_dev, g2_dev, mass_dev, friction, ke_end_dev,
+      to_sched(sched), to_noise(noise), to_fuse(nullptr));
   return check_launch("obabo_second");
 }
 
@@ -429,11 +514,10 @@ extern "C" int gbsgmc_sghmc_position(int chains, int64_t P, float* x_dev,
   if (!x_dev || !p_dev || !sched)
     return set_error(GBSGMC_ERR_ARG, "sghmc_position: null pointer");
   if (chains == 0 || P == 0) return GBSGMC_OK;
-  int64_t bx = std::min<int64_t>((P + kThreads - 1) / kThreads, 65535);
-  dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(chains));
-  sghmc_position_kernel<<<grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+  const Grid4 g = grid4(chains, P);
+  sghmc_position_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
       chains, P, x_dev, p_dev, mass_dev, friction_dev, friction,
-      to_sched(sched));
+      to_sched(sched), to_fuse(nullptr));
   return check_launch("sghmc_position");
 }
 
@@ -450,8 +534,8 @@ extern "C" int gbsgmc_sghmc_momentum(int chains, int64_t P, float* p_dev,
   if (chains == 0 || P == 0) return GBSGMC_OK;
   const Grid4 g = grid4(chains, P);
   sghmc_momentum_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-      chains, P, p_dev, g_dev, friction_dev, friction, to_sched(sched),
-      to_noise(noise));
+      chains, P, nullptr, p_dev, g_dev, friction_dev, friction, to_sched(sched),
+      to_noise(noise), to_fuse(nullptr));
   return check_launch("sghmc_momentum");
 }
 
@@ -519,3 +603,67 @@ extern "C" int gbsgmc_resgld_exchange_adjacent(
   if (v_dev != nullptr) swap_adjacent_rows_kernel<<<grid, 256, 0, st>>>(P, v_dev, flags_dev);
   return check_launch("resgld_exchange_adjacent: rows");
 }
+
+namespace gbsgmc {
+
+int update_blocks(int chains, int64_t P) { return static_cast<int>(grid4(chains, P).grid.x); }
+
+int sgld_update_fused(int chains, int64_t P, float* x, const float* g, float* v,
+                      float alpha, float lmbd, const gbsgmc_sched* sched,
+                      const gbsgmc_noise* noise, const UpdateFusion& f, cudaStream_t st) {
+  const Grid4 gr = grid4(chains, P);
+  sgld_update_kernel<<<gr.grid, kThreads, 0, st>>>(chains, P, x, g, v, alpha, lmbd,
+                                                   to_sched(sched), to_noise(noise), nullptr,
+                                                   to_fuse(&f));
+  return check_launch("sgld_update (fused)");
+}
+
+int obabo_first_fused(int chains, int64_t P, float* x, float* p, const float* g1,
+                      const float* mass, float friction, double* ke_start,
+                      const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                      const UpdateFusion& f, cudaStream_t st) {
+  const Grid4 gr = grid4(chains, P);
+  obabo_first_kernel<<<gr.grid, kThreads, 0, st>>>(chains, P, x, p, g1, mass, friction,
+                                                   ke_start, to_sched(sched), to_noise(noise),
+                                                   to_fuse(&f));
+  return check_launch("obabo_first (fused)");
+}
+
+int obabo_second_fused(int chains, int64_t P, const float* x, float* p, const float* g2,
+                       const float* mass, float friction, double* ke_end,
+                       const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                       const UpdateFusion& f, cudaStream_t st) {
+  const Grid4 gr = grid4(chains, P);
+  obabo_second_kernel<<<gr.grid, kThreads, 0, st>>>(chains, P, x, p, g2, mass, friction,
+                                                    ke_end, to_sched(sched), to_noise(noise),
+                                                    to_fuse(&f));
+  return check_launch("obabo_second (fused)");
+}
+
+int sghmc_position_fused(int chains, int64_t P, float* x, float* p, const float* mass,
+                         float friction, const gbsgmc_sched* sched, const UpdateFusion& f,
+                         cudaStream_t st) {
+  const Grid4 gr = grid4(chains, P);
+  sghmc_position_kernel<<<gr.grid, kThreads, 0, st>>>(chains, P, x, p, mass, nullptr,
+                                                      friction, to_sched(sched), to_fuse(&f));
+  return check_launch("sghmc_position (fused)");
+}
+
+int sghmc_momentum_fused(int chains, int64_t P, const float* x, float* p, const float* g,
+                         float friction, const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                         const UpdateFusion& f, cudaStream_t st) {
+  const Grid4 gr = grid4(chains, P);
+  sghmc_momentum_kernel<<<gr.grid, kThreads, 0, st>>>(chains, P, x, p, g, nullptr, friction,
+                                                      to_sched(sched), to_noise(noise),
+                                                      to_fuse(&f));
+  return check_launch("sghmc_momentum (fused)");
+}
+
+int mirror_fused(int chains, int64_t P, const float* x, const UpdateFusion& f,
+                 cudaStream_t st) {
+  const Grid4 gr = grid4(chains, P);
+  mirror_kernel<<<gr.grid, kThreads, 0, st>>>(P, x, to_fuse(&f));
+  return check_launch("mirror (fused)");
+}
+
+}  // namespace gbsgmc
