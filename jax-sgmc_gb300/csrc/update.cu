@@ -89,6 +89,20 @@ __device__ __forceinline__ void fuse_finish(const Fuse& f, int c, float sq) {
   if (threadIdx.x == 0) f.sq[static_cast<int64_t>(c) * gridDim.x + blockIdx.x] = tot;
 }
 
+// The 4 parameters j0..j0+3 of a chain row (those below P): all loads of a
+// group are issued before any store, so they overlap.
+__device__ __forceinline__ void load4(const float* __restrict__ a, int64_t j0, int64_t P,
+                                      float (&v)[4]) {
+#pragma unroll
+  for (int e = 0; e < 4; ++e) v[e] = j0 + e < P ? a[j0 + e] : 0.f;
+}
+__device__ __forceinline__ void store4(float* __restrict__ a, int64_t j0, int64_t P,
+                                       const float (&v)[4]) {
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+    if (j0 + e < P) a[j0 + e] = v[e];
+}
+
 __global__ void mirror_kernel(int64_t P, const float* x, Fuse f) {
   const int c = blockIdx.y;
   const int64_t groups = (P + 3) / 4;
@@ -117,31 +131,36 @@ __global__ void sgld_update_kernel(int chains, int64_t P, float* x,
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
   float sq = 0.f;
+  float* __restrict__ xc = x + off;
+  const float* __restrict__ gc = g + off;
+  float* __restrict__ vc = v != nullptr ? v + off : nullptr;
   for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    float xi[4], xs[4] = {0.f, 0.f, 0.f, 0.f};
-    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_SGLD, xi);
+    const int64_t j0 = 4 * q;
+    float xv[4], gv[4], vv[4] = {0.f, 0.f, 0.f, 0.f}, xi[4];
+    load4(xc, j0, P, xv);
+    load4(gc, j0, P, gv);
+    if (vc != nullptr) load4(vc, j0, P, vv);
+    noise4(noise, c, j0, P, k, GBSGMC_TAG_SGLD, xi);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int64_t j = 4 * q + e;
-      if (j >= P) break;
-      const float gj = fz.pf != 0.f ? fmaf(fz.pf, x[off + j], g[off + j]) : g[off + j];
+      const float gj = fz.pf != 0.f ? fmaf(fz.pf, xv[e], gv[e]) : gv[e];
       const float scaled_gradient = -h * gj;
       const float scaled_noise = noise_scale * xi[e];
-      float xn;
-      if (v != nullptr) {
-        const float vn = alpha * v[off + j] + (1.0f - alpha) * (gj * gj);
+      if (vc != nullptr) {
+        const float vn = alpha * vv[e] + (1.0f - alpha) * (gj * gj);
         const float G = 1.0f / (lmbd + sqrtf(vn));
-        v[off + j] = vn;
-        xn = x[off + j] + ((0.0f + G * scaled_gradient) + sqrtf(G) * scaled_noise);
+        vv[e] = vn;
+        xv[e] = xv[e] + ((0.0f + G * scaled_gradient) + sqrtf(G) * scaled_noise);
       } else {
-        xn = x[off + j] + (scaled_gradient + scaled_noise);
+        xv[e] = xv[e] + (scaled_gradient + scaled_noise);
       }
-      x[off + j] = xn;
-      xs[e] = xn;
-      if (slot >= 0) samples[(static_cast<int64_t>(slot) * chains + c) * P + j] = xn;
     }
-    fuse_store(fz, c, 4 * q, P, xs, sq);
+    if (vc != nullptr) store4(vc, j0, P, vv);
+    store4(xc, j0, P, xv);
+    if (slot >= 0)
+      store4(samples + (static_cast<int64_t>(slot) * chains + c) * P, j0, P, xv);
+    fuse_store(fz, c, j0, P, xv, sq);
   }
   fuse_finish(fz, c, sq);
 }
@@ -170,25 +189,31 @@ __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
   float ke = 0.0f, sq = 0.0f;
+  float* __restrict__ xc = x + off;
+  float* __restrict__ pc = p + off;
+  const float* __restrict__ gc = g1 + off;
   for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    float xi[4], xs[4] = {0.f, 0.f, 0.f, 0.f};
-    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_OBABO_1, xi);
+    const int64_t j0 = 4 * q;
+    float xv[4], pv[4], gv[4], xi[4];
+    load4(xc, j0, P, xv);
+    load4(pc, j0, P, pv);
+    load4(gc, j0, P, gv);
+    noise4(noise, c, j0, P, k, GBSGMC_TAG_OBABO_1, xi);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int64_t j = 4 * q + e;
-      if (j >= P) break;
-      const float mi = mass_inv(mass, j);
-      const float xj = x[off + j];
-      const float gj = fz.pf != 0.f ? fmaf(fz.pf, xj, g1[off + j]) : g1[off + j];
-      float pj = keep * p[off + j] + inject * (mass_sqrt(mass, j) * xi[e]);
+      if (j0 + e >= P) break;
+      const float mi = mass_inv(mass, j0 + e);
+      const float gj = fz.pf != 0.f ? fmaf(fz.pf, xv[e], gv[e]) : gv[e];
+      float pj = keep * pv[e] + inject * (mass_sqrt(mass, j0 + e) * xi[e]);
       ke = fmaf(0.5f * pj, mi * pj, ke);
       pj = -half * gj + pj;
-      p[off + j] = pj;
-      xs[e] = xj + h * (mi * pj);
-      x[off + j] = xs[e];
+      pv[e] = pj;
+      xv[e] = xv[e] + h * (mi * pj);
     }
-    fuse_store(fz, c, 4 * q, P, xs, sq);
+    store4(pc, j0, P, pv);
+    store4(xc, j0, P, xv);
+    fuse_store(fz, c, j0, P, xv, sq);
   }
   add_ke(ke_start, c, ke);
   fuse_finish(fz, c, sq);
@@ -209,21 +234,27 @@ __global__ void obabo_second_kernel(int chains, int64_t P, const float* x, float
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
   float ke = 0.0f;
+  float* __restrict__ pc = p + off;
+  const float* __restrict__ gc = g2 + off;
+  const float* __restrict__ xc = fz.pf != 0.f ? x + off : nullptr;
   for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    float xi[4];
-    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_OBABO_2, xi);
+    const int64_t j0 = 4 * q;
+    float pv[4], gv[4], xv[4] = {0.f, 0.f, 0.f, 0.f}, xi[4];
+    load4(pc, j0, P, pv);
+    load4(gc, j0, P, gv);
+    if (xc != nullptr) load4(xc, j0, P, xv);
+    noise4(noise, c, j0, P, k, GBSGMC_TAG_OBABO_2, xi);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int64_t j = 4 * q + e;
-      if (j >= P) break;
-      const float mi = mass_inv(mass, j);
-      const float gj = fz.pf != 0.f ? fmaf(fz.pf, x[off + j], g2[off + j]) : g2[off + j];
-      float pj = -half * gj + p[off + j];
+      if (j0 + e >= P) break;
+      const float mi = mass_inv(mass, j0 + e);
+      const float gj = xc != nullptr ? fmaf(fz.pf, xv[e], gv[e]) : gv[e];
+      float pj = -half * gj + pv[e];
       ke = fmaf(0.5f * pj, mi * pj, ke);
-      pj = keep * pj + inject * (mass_sqrt(mass, j) * xi[e]);
-      p[off + j] = pj;
+      pv[e] = keep * pj + inject * (mass_sqrt(mass, j0 + e) * xi[e]);
     }
+    store4(pc, j0, P, pv);
   }
   add_ke(ke_end, c, ke);
 }
