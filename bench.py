@@ -136,12 +136,13 @@ def measured_peak_hbm():
 
 
 def profiled_traffic():
-  """DRAM bytes per launch of the fused step from the committed ncu summary."""
+  """DRAM bytes of one fused SGLD step of all chains, from the committed ncu
+  summary (dram__bytes_read.sum + dram__bytes_write.sum)."""
   p = ROOT / "profiles" / "glm_sgld_step_logistic_256x1024x256.md"
   if not p.exists():
     return None
   for line in p.read_text().splitlines():
-    if line.startswith("traffic_bytes_per_launch:"):
+    if line.startswith("traffic_bytes_per_step:"):
       try:
         return float(line.split(":", 1)[1].strip().split()[0])
       except ValueError:
@@ -233,9 +234,11 @@ class Setup:
 
 
 class FusedLauncher:
-  """Direct launches of the fused step kernel on torch's current stream."""
+  """Direct launches of the fused step kernel on torch's current stream:
+  one step per launch, or (multi=True, the plan's choice when its blocks run
+  in one launch) eight steps per launch over the eight index sets."""
 
-  def __init__(self, s):
+  def __init__(self, s, multi=False):
     import torch
     from gbsgmc import _lib
     self._lib = _lib
@@ -249,9 +252,17 @@ class FusedLauncher:
     self.W, self.V = s.W.clone(), s.V.clone()
     self.sched = _lib.sched(step_size=1e-5, temperature=1.0, offset=0)
     self.noise = _lib.noise(seed=5)
+    self.steps_per_launch = 8 if multi else 1
 
   def __call__(self, i):
     L = self._lib
+    if self.steps_per_launch > 1:
+      L.call("gbsgmc_sgld_glm_steps", self.model, CHAINS, MB, L.ptr(self.idx),
+             MB, CHAINS * MB, self.steps_per_launch, L.ptr(self.W),
+             L.ptr(self.V), 0.9, 1e-5, self.sched, self.noise, None, None, None,
+             None, L.ptr(self.ws), self.ws.numel(), L.ptr(self.status),
+             self.stream)
+      return
     L.call("gbsgmc_sgld_glm_step", self.model, CHAINS, MB, L.ptr(self.idx[i % 8]),
            MB, L.ptr(self.W), L.ptr(self.V), 0.9, 1e-5, self.sched, self.noise,
            None, None, None, None, L.ptr(self.ws), self.ws.numel(),
@@ -260,7 +271,8 @@ class FusedLauncher:
 
 def kernel_only(args):
   """A short run for profilers: three plan steps, ten more, then five direct
-  launches of the fused step kernel."""
+  launches of the fused step kernel (eight steps each when the plan runs a
+  block of steps per launch)."""
   import torch
   rank, _, local = dist_env()
   torch.cuda.set_device(local)
@@ -270,8 +282,9 @@ def kernel_only(args):
   plan.run(args.warmup, 10)
   torch.cuda.synchronize()
   plan.check_status()
+  multi = plan.launch_shape()[5] > 1
   plan.close()
-  f = FusedLauncher(s)
+  f = FusedLauncher(s, multi=multi)
   for i in range(5):
     f(i)
   torch.cuda.synchronize()
@@ -321,10 +334,10 @@ def run_gbsgmc(args):
   plan.close()
 
   # The fused step kernel alone: average launch time on its stream.
-  f = FusedLauncher(s)
+  f = FusedLauncher(s, multi=shape[5] > 1)
   for i in range(5):
     f(i)
-  reps = 200
+  reps = 200 if f.steps_per_launch == 1 else 25
   torch.cuda.synchronize()
   k0 = torch.cuda.Event(enable_timing=True)
   k1 = torch.cuda.Event(enable_timing=True)
@@ -334,7 +347,7 @@ def run_gbsgmc(args):
   k1.record()
   torch.cuda.synchronize()
   kernel_ms = k0.elapsed_time(k1) / reps
-  bytes_per_launch = CHAINS * BYTES_PER_CHAIN_STEP
+  bytes_per_launch = CHAINS * BYTES_PER_CHAIN_STEP * f.steps_per_launch
   achieved = bytes_per_launch / (kernel_ms / 1e3) / 1e9
   peak, peak_kind = measured_peak_hbm()
 
@@ -404,15 +417,19 @@ def run_gbsgmc(args):
                    "l2": "inputs larger than L2 (X 1.02 GB, random rows)",
                    "parallelism": f"chains sharded, {world} replica(s)",
                    "graph_block_steps": 50,
-                   "launch_shape": {"ctas_per_chain": shape[0],
+                   "launch_shape": {"ctas_or_items_per_chain": shape[0],
                                     "rows_per_warp": shape[1],
                                     "warps_per_cta": shape[2],
                                     "prefetch_tiles": shape[3],
+                                    "dynamic_items": shape[4],
+                                    "steps_per_launch": shape[5],
                                     "chosen_by": "autotuner"}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": profiled_traffic(),
+                     "traffic": (None if profiled_traffic() is None else
+                                 profiled_traffic() * f.steps_per_launch),
+                     "steps_per_launch": f.steps_per_launch,
                      "peak_kind": f"{peak_kind} hbm_gbs",
                      "kernel": "glm_kernel (fused SGLD step)",
                      "kernel_ms": kernel_ms,

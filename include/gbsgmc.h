@@ -415,8 +415,8 @@ int gbsgmc_cnn_value_and_grad(const gbsgmc_cnn* model, int chains, int n,
 /* Fused SGLD step for the generalised-linear families                       */
 /* ------------------------------------------------------------------------ */
 
-/* One fused launch: gather of the minibatch rows (TMA bulk copies into shared
- * memory), likelihood, adjoint, N/n-scaled reduction, Gaussian prior,
+/* One fused launch: gather of the minibatch rows (128-bit loads straight
+ * into registers), likelihood, adjoint, N/n-scaled reduction, Gaussian prior,
  * RMSprop, noise and the SGLD update of every chain, plus on-device sample
  * collection (samples_dev[slot, c, :] = new w, sample_lik_dev[slot, c] =
  * -U(old w)).  U_dev / lk_var_dev receive the potential at the pre-update
@@ -434,6 +434,26 @@ int gbsgmc_sgld_glm_step(const gbsgmc_glm* model, int chains, int n,
                          double* sample_lik_dev, void* workspace_dev,
                          size_t workspace_bytes, int* status_dev,
                          gbsgmc_stream_t stream);
+
+/* `steps` consecutive fused SGLD steps in one launch, step j drawing chain
+ * c's rows from idx_dev[j * idx_step_stride + c * idx_stride + i] and using
+ * schedule step (counter + offset + j).  With one CTA per chain (n <= 1024
+ * and the launch shape a plan's autotuner may choose) every CTA runs its
+ * chain's steps back to back, so the steps pay no launch gap or grid tail;
+ * other shapes issue one launch per step.  Results equal `steps` calls of
+ * gbsgmc_sgld_glm_step with the same shape.  Injected noise (noise_dev) is
+ * one draw and is rejected when steps > 1.  samples_dev / sample_lik_dev
+ * receive the steps whose keep slot is set.  Replaces `steps` iterations of
+ * the lax.scan in solver.mcmc (jax_sgmc/solver.py:152-160). */
+int gbsgmc_sgld_glm_steps(const gbsgmc_glm* model, int chains, int n,
+                          const int32_t* idx_dev, int64_t idx_stride,
+                          int64_t idx_step_stride, int steps, float* w_dev,
+                          float* v_dev, float alpha, float lmbd,
+                          const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                          double* U_dev, double* lk_var_dev, float* samples_dev,
+                          double* sample_lik_dev, void* workspace_dev,
+                          size_t workspace_bytes, int* status_dev,
+                          gbsgmc_stream_t stream);
 
 /* Size of the scratch array compiled into the library for
  * gbsgmc_sgld_glm_step_noalloc (8 MiB per GPU that loads the library). */
@@ -586,14 +606,17 @@ int gbsgmc_plan_run(gbsgmc_plan* plan, int64_t first_step, int64_t steps,
                     gbsgmc_stream_t stream);
 
 /* The launch shape the plan's autotuner chose for the fused step: CTAs per
- * chain, rows per warp, warps per CTA and whether each warp keeps two row
- * tiles in flight (0 = the library default).  The autotuner times a few
+ * chain, rows per warp, warps per CTA, whether each warp keeps two row tiles
+ * in flight, whether the dynamically scheduled kernel runs (then `slices`
+ * is the number of row items per chain that warps claim), and the steps one
+ * launch runs (1, or the plan's block of steps); 0 = the library default.  The autotuner times a few
  * candidate shapes on scratch copies of the chain state when the plan is
  * created (GBSGMC_AUTOTUNE=0 disables it) and caches the choice per problem
  * shape for the process.  Network plans report zeros.  No reference
  * counterpart: launch configuration only. */
 int gbsgmc_plan_launch_shape(const gbsgmc_plan* plan, int* slices,
-                             int* rows_per_warp, int* warps, int* prefetch);
+                             int* rows_per_warp, int* warps, int* prefetch,
+                             int* dynamic, int* steps_per_launch);
 
 /* Kernel launches one plan_run of `steps` steps performs (for accounting). */
 int64_t gbsgmc_plan_launches(const gbsgmc_plan* plan, int64_t steps);

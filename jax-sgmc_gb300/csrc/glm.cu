@@ -25,6 +25,9 @@
 //   U = (-N/n sum_i m_i lk_i - log p(w)) / T_pot
 //   g = (-N/n sum_i m_i dlk_i/dw + w / s^2) / T_pot
 // then either stores (U, g) or applies the SGLD(+RMSprop) update in place.
+// With one CTA per chain, one launch can run several SGLD steps back to back
+// (glm_kernel's step loop).  glm_dyn_kernel is a dynamically scheduled form
+// of the same step (warps claim row items of any chain).
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -58,6 +61,8 @@ struct GlmArgs {
   int chains, n, slices, rows_per_slice;
   const int32_t* idx;
   int64_t idx_stride;
+  int steps;                // SGLD steps per launch (> 1: one CTA per chain)
+  int64_t idx_step_stride;  // elements between the index sets of two steps
   const float* mask;
   int mode;
   float* w;
@@ -80,6 +85,7 @@ struct GlmArgs {
   int rw_fixed;       // > 0: rows per warp chosen by the caller
   int warps_fixed;    // > 0: warps per CTA chosen by the caller
   int pf_fixed;       // 1: prefetching variant, -1: not, 0: library choice
+  int dyn_fixed;      // 1: dynamically scheduled kernel, -1: not, 0: library choice
   int* status;
   int vec4;   // rows are 16-byte aligned: 128-bit loads
 };
@@ -289,10 +295,10 @@ __device__ __forceinline__ void consume_tile(const GlmArgs& a, const float* m_s,
   }
 }
 
-template <int QPL, int RW, bool PF, int MINB, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, MINB)
-    glm_kernel(const GlmArgs a) {
-  extern __shared__ __align__(128) unsigned char smem[];
+// Step j of a launch (see glm_kernel): indices at idx + j * idx_step_stride,
+// schedule step counter + offset + j.
+template <int QPL, int RW, bool PF, int WARPS>
+__device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char* smem) {
   constexpr int LOG = Log2<RW>::v;
   constexpr int GROUP = 32 >> LOG;  // lanes per row in the link phase
   const int dq = a.dq;
@@ -310,8 +316,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
 
   if (tid == 0) *is_last = 0;
   // Observation indices (and mask weights) of this slice.
+  const int32_t* idx_j = a.idx + j * a.idx_step_stride;
   for (int r = tid; r < R; r += (WARPS * 32)) {
-    int32_t o = __ldg(a.idx + c * a.idx_stride + row0 + r);
+    int32_t o = __ldg(idx_j + c * a.idx_stride + row0 + r);
     if (o < 0 || o >= a.n_rows) {
       raise_status(a.status, GBSGMC_ERR_INDEX);
       o = -1;
@@ -500,7 +507,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   }
 
   // SGLD (+RMSprop) update of chain c, four parameters per thread.
-  const int64_t k = a.sched.step();
+  const int64_t k = a.sched.step() + j;
   const float h = a.sched.step_size(k);
   const float T = a.sched.temperature(k, c);
   const int slot = a.sched.keep_slot(k);
@@ -544,6 +551,274 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   }
 }
 
+// One launch runs a.steps consecutive SGLD steps (a.steps > 1 only with one
+// CTA per chain: a chain's step depends on nothing but its own previous
+// step, so the CTA that owns the chain runs them back to back).  Chains drift
+// out of phase, so one CTA's index loads and update overlap the row streams
+// of the others, and the steps pay no launch gap or grid tail.
+template <int QPL, int RW, bool PF, int MINB, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, MINB)
+    glm_kernel(const GlmArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  for (int j = 0; j < a.steps; ++j) {
+    if (j > 0) __syncthreads();  // step j-1's update of w is visible
+    glm_step<QPL, RW, PF, WARPS>(a, j, smem);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dynamically scheduled form.  The rows of one launch are cut into items of
+// rows_per_slice rows of one chain (item u = chain * items + item), and every
+// warp of a persistent grid claims items from a counter in the workspace
+// until none are left: all SMs stay busy until the last item, whatever the
+// ratio of chains to SMs (256 chains on 152 SMs leave a static grid with one
+// or two CTAs per SM).  A warp loads the chain's w into registers, streams
+// the item's rows through the same tile loads and link as glm_kernel, and
+// writes the item's partial gradient and sums to the workspace.  The warp
+// that completes a chain's last item (per-chain ticket) adds the chain's
+// partials in item order -- the order does not depend on scheduling -- and
+// runs the epilogue and update of that chain alone.  The last warp to leave
+// the grid resets the claim counter for the next launch.
+// ---------------------------------------------------------------------------
+
+// Epilogue of chain c run by one warp: gq gets the chain's summed partial
+// gradient; wq holds the chain's w (lane's float4 columns q = lane + 32 k).
+template <int QPL>
+__device__ __forceinline__ void dyn_epilogue(const GlmArgs& a, int c, int lane,
+                                             const float4 (&wq)[QPL]) {
+  const int dq = a.dq, ipc = a.slices;
+  const float4* part = a.ws_part + static_cast<int64_t>(c) * ipc * dq;
+  float gl[QPL][4];
+  double ww = 0.0;
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    const int q = lane + 32 * k;
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (q < dq) {
+      t = __ldcg(part + q);
+      for (int s = 1; s < ipc; ++s) {
+        const float4 u = __ldcg(part + static_cast<int64_t>(s) * dq + q);
+        t.x += u.x;
+        t.y += u.y;
+        t.z += u.z;
+        t.w += u.w;
+      }
+    }
+    gl[k][0] = t.x;
+    gl[k][1] = t.y;
+    gl[k][2] = t.z;
+    gl[k][3] = t.w;
+    if (a.inv_p2 > 0.0f) {
+      const float wv[4] = {wq[k].x, wq[k].y, wq[k].z, wq[k].w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const double wj = wv[e];  // zero past d
+        ww += wj * wj;
+      }
+    }
+  }
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+  const double* ps = a.ws_sums + static_cast<int64_t>(c) * ipc * 4;
+  for (int s = lane; s < ipc; s += 32) {
+    t0 += __ldcg(ps + s * 4 + 0);
+    t1 += __ldcg(ps + s * 4 + 1);
+    t2 += __ldcg(ps + s * 4 + 2);
+  }
+  const double sum_mlk = warp_sum(t0);
+  const double sum_lk = warp_sum(t1);
+  const double sum_lk2 = warp_sum(t2);
+  ww = warp_sum(ww);
+
+  float* wc = a.w + static_cast<int64_t>(c) * a.d;
+  const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n);
+  const double log_prior = -0.5 * ww * a.inv_p2 - a.prior_const;
+  const double lik = a.mask == nullptr
+                         ? -static_cast<double>(a.n_obs) * (sum_mlk / a.n)
+                         : -(static_cast<double>(a.n_obs) / a.n) * sum_mlk;
+  const double U = (lik - log_prior) * a.inv_temp;
+  const double mean_lk = sum_lk / a.n;
+  const double var_lk = fmax(sum_lk2 / a.n - mean_lk * mean_lk, 0.0);
+  if (lane == 0 && !isfinite(U)) raise_status(a.status, GBSGMC_ERR_NONFINITE);
+
+  if (a.mode == kValueGrad) {
+    if (a.grad != nullptr) {
+      float* gc = a.grad + static_cast<int64_t>(c) * a.d;
+#pragma unroll
+      for (int k = 0; k < QPL; ++k) {
+        const float wv[4] = {wq[k].x, wq[k].y, wq[k].z, wq[k].w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int j = 4 * (lane + 32 * k) + e;
+          if (j < a.d) gc[j] = (-scale * gl[k][e] + wv[e] * a.inv_p2) * a.inv_temp;
+        }
+      }
+    }
+    if (lane == 0) {
+      a.U[c] = U;
+      if (a.lk_var != nullptr) a.lk_var[c] = var_lk;
+    }
+    return;
+  }
+
+  const int64_t k_step = a.sched.step();
+  const float h = a.sched.step_size(k_step);
+  const float T = a.sched.temperature(k_step, c);
+  const int slot = a.sched.keep_slot(k_step);
+  const float noise_scale = sqrtf(2.0f * T * h);
+  float* vc = a.v != nullptr ? a.v + static_cast<int64_t>(c) * a.d : nullptr;
+  float* smp = slot >= 0 ? a.samples + (static_cast<int64_t>(slot) * a.chains + c) * a.d
+                         : nullptr;
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    const int q = lane + 32 * k;
+    if (q >= dq) continue;
+    float xi[4];
+    noise4(a.noise, c, 4 * q, a.d, k_step, GBSGMC_TAG_SGLD, xi);
+    const float wv[4] = {wq[k].x, wq[k].y, wq[k].z, wq[k].w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int j = 4 * q + e;
+      if (j >= a.d) break;
+      const float x = wv[e];
+      const float g = (-scale * gl[k][e] + x * a.inv_p2) * a.inv_temp;
+      bad |= !isfinite(g);
+      const float scaled_gradient = -h * g;
+      const float scaled_noise = noise_scale * xi[e];
+      float x_new;
+      if (vc != nullptr) {
+        const float vn = a.alpha * vc[j] + (1.0f - a.alpha) * (g * g);
+        const float G = 1.0f / (a.lmbd + sqrtf(vn));
+        const float sG = sqrtf(G);
+        vc[j] = vn;
+        x_new = x + ((0.0f + G * scaled_gradient) + sG * scaled_noise);
+      } else {
+        x_new = x + (scaled_gradient + scaled_noise);
+      }
+      wc[j] = x_new;
+      if (smp != nullptr) smp[j] = x_new;
+    }
+  }
+  if (bad) raise_status(a.status, GBSGMC_ERR_NONFINITE);
+  if (lane == 0) {
+    if (a.U != nullptr) a.U[c] = U;
+    if (a.lk_var != nullptr) a.lk_var[c] = var_lk;
+    if (slot >= 0 && a.sample_lik != nullptr)
+      a.sample_lik[static_cast<int64_t>(slot) * a.chains + c] = -U;
+  }
+}
+
+// Shared memory of the dynamic kernel: per warp, the indices and mask
+// weights of its current item.
+__host__ __device__ inline size_t dyn_smem_bytes(int item_rows, int warps) {
+  return static_cast<size_t>(warps) * item_rows * (sizeof(int32_t) + sizeof(float));
+}
+
+template <int QPL, int RW, int MINB, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, MINB)
+    glm_dyn_kernel(const GlmArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int LOG = Log2<RW>::v;
+  constexpr int GROUP = 32 >> LOG;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int IR = a.rows_per_slice;
+  int32_t* idx_s = reinterpret_cast<int32_t*>(smem) + static_cast<size_t>(warp) * IR;
+  float* m_s = reinterpret_cast<float*>(smem) + static_cast<size_t>(WARPS + warp) * IR;
+  const int ipc = a.slices;
+  const int total = a.chains * ipc;
+  unsigned* claim = a.ws_ticket + a.chains;
+  unsigned* exits = claim + 1;
+  const int g = lane >> (5 - LOG);
+  const bool leader = (lane & (GROUP - 1)) == 0;
+
+  int u = 0;
+  if (lane == 0) u = static_cast<int>(atomicAdd(claim, 1u));
+  u = __shfl_sync(0xffffffffu, u, 0);
+  while (u < total) {
+    // The next item is claimed now; its number is needed only at the end.
+    int un = 0;
+    if (lane == 0) un = static_cast<int>(atomicAdd(claim, 1u));
+    const int c = u / ipc, s = u - c * ipc;
+    const int row0 = s * IR;
+    const int R = max(0, min(IR, a.n - row0));
+    __syncwarp();  // the previous item's reads of idx_s / m_s are done
+    for (int r = lane; r < R; r += 32) {
+      int32_t o = __ldg(a.idx + c * a.idx_stride + row0 + r);
+      if (o < 0 || o >= a.n_rows) {
+        raise_status(a.status, GBSGMC_ERR_INDEX);
+        o = -1;
+      }
+      idx_s[r] = o;
+      if (a.mask != nullptr)
+        m_s[r] = __ldg(a.mask + static_cast<int64_t>(c) * a.n + row0 + r);
+    }
+    float4 wq[QPL];
+    Accum<QPL> A;
+    const float* w_in = a.w + static_cast<int64_t>(c) * a.d;
+#pragma unroll
+    for (int k = 0; k < QPL; ++k) {
+      const int j = 4 * (lane + 32 * k);
+      wq[k].x = j + 0 < a.d ? w_in[j + 0] : 0.0f;
+      wq[k].y = j + 1 < a.d ? w_in[j + 1] : 0.0f;
+      wq[k].z = j + 2 < a.d ? w_in[j + 2] : 0.0f;
+      wq[k].w = j + 3 < a.d ? w_in[j + 3] : 0.0f;
+      A.acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    A.mlk = A.K = A.s1 = A.s2 = 0.0f;
+    A.cnt = 0;
+    __syncwarp();
+    float* lk_out = a.lk != nullptr ? a.lk + static_cast<int64_t>(c) * a.n + row0
+                                    : nullptr;
+    for (int r0 = 0; r0 < R; r0 += RW) {
+      float4 xv[RW][QPL];
+      float yv;
+      int og;
+      load_tile<QPL, RW>(a, idx_s, R, r0, lane, g, xv, yv, og);
+      consume_tile<QPL, RW>(a, m_s, lk_out, r0, lane, g, leader, wq, xv, yv, og, A);
+    }
+    const double K = A.K, n_l = A.cnt;
+    const double my_mlk = warp_sum(static_cast<double>(A.mlk));
+    const double my_lk = warp_sum(static_cast<double>(A.s1) + n_l * K);
+    const double my_lk2 =
+        warp_sum(static_cast<double>(A.s2) + 2.0 * K * A.s1 + n_l * K * K);
+    const int64_t pc = static_cast<int64_t>(c) * ipc + s;
+#pragma unroll
+    for (int k = 0; k < QPL; ++k) {
+      const int q = lane + 32 * k;
+      if (q < a.dq) a.ws_part[pc * a.dq + q] = A.acc[k];
+    }
+    if (lane == 0) {
+      a.ws_sums[pc * 4 + 0] = my_mlk;
+      a.ws_sums[pc * 4 + 1] = my_lk;
+      a.ws_sums[pc * 4 + 2] = my_lk2;
+    }
+    __threadfence();
+    __syncwarp();
+    int last = 0;
+    if (lane == 0) {
+      const unsigned ticket = atomicAdd(a.ws_ticket + c, 1u);
+      last = ticket == static_cast<unsigned>(ipc - 1);
+      if (last) a.ws_ticket[c] = 0u;  // ready for the next launch
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (last) {
+      __threadfence();
+      dyn_epilogue<QPL>(a, c, lane, wq);
+    }
+    u = __shfl_sync(0xffffffffu, un, 0);
+  }
+  // Every claim of this warp precedes its exit; the last warp to leave sees
+  // all claims done and resets both counters.
+  __threadfence();
+  if (lane == 0) {
+    const unsigned e = atomicAdd(exits, 1u);
+    if (e == gridDim.x * static_cast<unsigned>(WARPS) - 1u) {
+      atomicExch(claim, 0u);
+      atomicExch(exits, 0u);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host side: argument checks, slice choice, launch.
 // ---------------------------------------------------------------------------
@@ -563,7 +838,8 @@ size_t ws_bytes(int chains, int n, int d) {
   const size_t S = static_cast<size_t>(slices_alloc(n));
   size_t b = align_up(static_cast<size_t>(chains) * S * dq * 16, 256);
   b += align_up(static_cast<size_t>(chains) * S * 4 * sizeof(double), 256);
-  b += align_up(static_cast<size_t>(chains) * sizeof(unsigned), 256);
+  // Per-chain tickets, then the claim and exit counters of glm_dyn_kernel.
+  b += align_up((static_cast<size_t>(chains) + 2) * sizeof(unsigned), 256);
   return b;
 }
 
@@ -681,17 +957,97 @@ struct Variant {
       a.ws_ticket = v.ticket;
     }
     dim3 grid(a.slices, a.chains);
+    if (a.steps > 1 && a.slices > 1) {
+      // Several CTAs per chain: one launch per step.
+      GlmArgs b = a;
+      b.steps = 1;
+      for (int j = 0; j < a.steps; ++j) {
+        b.idx = a.idx + j * a.idx_step_stride;
+        b.sched.offset = a.sched.offset + j;
+        glm_kernel<QPL, RW, PF, MINB, WARPS><<<grid, WARPS * 32, smem, st>>>(b);
+        const int rc2 = check_launch("glm_kernel");
+        if (rc2 != GBSGMC_OK) return rc2;
+      }
+      return GBSGMC_OK;
+    }
     glm_kernel<QPL, RW, PF, MINB, WARPS><<<grid, WARPS * 32, smem, st>>>(a);
     return check_launch("glm_kernel");
   }
 };
 
+// The dynamically scheduled kernel: `slices` is the number of items per
+// chain, the grid is as many CTAs as fit on the SMs at once (no more than the
+// items need).
+template <int QPL, int RW, int MINB, int WARPS>
+struct DynVariant {
+  static int prepare() {
+    static int done = 0;
+    if (done) return GBSGMC_OK;
+    const cudaError_t e = cudaFuncSetAttribute(
+        glm_dyn_kernel<QPL, RW, MINB, WARPS>,
+        cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+    if (e != cudaSuccess)
+      return set_error(GBSGMC_ERR_CUDA, "glm: cudaFuncSetAttribute: %s",
+                       cudaGetErrorString(e));
+    done = 1;
+    return GBSGMC_OK;
+  }
+  static int occupancy(size_t smem) {
+    static size_t last_smem = 0;
+    static int last = 0;
+    if (last > 0 && last_smem == smem) return last;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, glm_dyn_kernel<QPL, RW, MINB, WARPS>, WARPS * 32, smem) != cudaSuccess ||
+        nb < 1)
+      nb = 1;
+    last_smem = smem;
+    last = nb;
+    return nb;
+  }
+  static int launch(GlmArgs a, cudaStream_t st) {
+    const int rc = prepare();
+    if (rc != GBSGMC_OK) return rc;
+    const int want = a.slices_fixed > 0 ? a.slices_fixed : kMinSlicesAlloc;
+    const int ipc0 = clamp_slices(want, a.n);
+    a.rows_per_slice = ceil_div(a.n, ipc0);
+    a.slices = ceil_div(a.n, a.rows_per_slice);  // no empty items
+    if (a.ws_base == nullptr || a.ws_size < ws_bytes(a.chains, a.n, a.d))
+      return set_error(GBSGMC_ERR_ARG,
+                       "glm: workspace missing or too small (need %zu bytes)",
+                       ws_bytes(a.chains, a.n, a.d));
+    const WsView v = ws_view(a.ws_base, a.chains, a.n, a.d);
+    a.ws_part = v.part;
+    a.ws_sums = v.sums;
+    a.ws_ticket = v.ticket;
+    const size_t smem = dyn_smem_bytes(a.rows_per_slice, WARPS);
+    const int64_t items = static_cast<int64_t>(a.chains) * a.slices;
+    const int64_t need = (items + WARPS - 1) / WARPS;
+    const int grid = static_cast<int>(
+        std::max<int64_t>(1, std::min<int64_t>(need,
+                                               static_cast<int64_t>(sm_count()) *
+                                                   occupancy(smem))));
+    GlmArgs b = a;
+    b.steps = 1;
+    for (int j = 0; j < a.steps; ++j) {
+      b.idx = a.idx + j * a.idx_step_stride;
+      b.sched.offset = a.sched.offset + j;
+      glm_dyn_kernel<QPL, RW, MINB, WARPS><<<grid, WARPS * 32, smem, st>>>(b);
+      const int rc2 = check_launch("glm_dyn_kernel");
+      if (rc2 != GBSGMC_OK) return rc2;
+    }
+    return GBSGMC_OK;
+  }
+};
+
 // Launch-shape overrides for experiments: GBSGMC_GLM_RW (2 or 4 rows per
 // warp, d <= 256), GBSGMC_GLM_WARPS (8 or 16 warps per CTA),
-// GBSGMC_GLM_SLICES (CTAs per chain).
+// GBSGMC_GLM_SLICES (CTAs per chain, or items per chain with
+// GBSGMC_GLM_DYN=1: the dynamically scheduled kernel).
 int rows_override() { return env_int("GBSGMC_GLM_RW", 0); }
 int warps_override() { return env_int("GBSGMC_GLM_WARPS", 0); }
 int prefetch_override() { return env_int("GBSGMC_GLM_PF", -1); }
+int dynamic_override() { return env_int("GBSGMC_GLM_DYN", -1); }
 
 // Dispatch over the tuned shape: rows per warp (RW) and warps per CTA.  The
 // register budget (MINB) is 3 CTAs/SM for 8-warp CTAs with RW = 4, otherwise
@@ -705,6 +1061,12 @@ int launch_q(const GlmArgs& a, size_t smem, cudaStream_t st) {
     const int rw = a.rw_fixed > 0 ? a.rw_fixed
                    : (rows_override() > 0 ? rows_override()
                                           : default_rows_per_warp(QPL));
+    const bool dyn = a.dyn_fixed > 0 || (a.dyn_fixed == 0 && dynamic_override() > 0);
+    if (dyn) {
+      if (rw == 8) return DynVariant<QPL, 8, 2, 8>::launch(a, st);
+      if (rw == 4) return DynVariant<QPL, 4, 3, 8>::launch(a, st);
+      return DynVariant<QPL, 2, 4, 8>::launch(a, st);
+    }
     const int pfo = prefetch_override();
     const bool pf = a.pf_fixed > 0 || (a.pf_fixed == 0 && pfo > 0);
     // Prefetching variants hold two tiles in registers, so they get the
@@ -796,6 +1158,7 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.rw_fixed = tune.rows_per_warp;
   a.warps_fixed = tune.warps;
   a.pf_fixed = tune.prefetch > 0 ? 1 : (tune.rows_per_warp > 0 ? -1 : 0);
+  a.dyn_fixed = tune.dynamic > 0 ? 1 : (tune.rows_per_warp > 0 ? -1 : 0);
   a.ws_base = ws;
   a.ws_size = ws_size;
   a.ws_part = nullptr;
@@ -803,6 +1166,8 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.ws_ticket = nullptr;
   a.idx = idx;
   a.idx_stride = idx_stride;
+  a.steps = 1;
+  a.idx_step_stride = 0;
   a.mask = mask;
   a.status = status;
   // 128-bit row loads need every row 16-byte aligned.
@@ -872,6 +1237,12 @@ int glm_prepare() {
   if (rc == GBSGMC_OK) rc = Variant<4, 2, false, 1, 16>::prepare();
   if (rc == GBSGMC_OK) rc = Variant<8, 1, false, 2, 8>::prepare();
   if (rc == GBSGMC_OK) rc = Variant<8, 1, false, 1, 16>::prepare();
+  if (rc == GBSGMC_OK) rc = DynVariant<1, 8, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = DynVariant<1, 4, 3, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = DynVariant<1, 2, 4, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = DynVariant<2, 8, 2, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = DynVariant<2, 4, 3, 8>::prepare();
+  if (rc == GBSGMC_OK) rc = DynVariant<2, 2, 4, 8>::prepare();
   return rc;
 }
 
@@ -881,7 +1252,8 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   const gbsgmc_sched* sched, const gbsgmc_noise* noise,
                   double* U_dev, double* lk_var_dev, float* samples_dev,
                   double* sample_lik_dev, void* ws, size_t ws_size,
-                  int* status_dev, cudaStream_t stream, GlmTune tune) {
+                  int* status_dev, cudaStream_t stream, GlmTune tune, int steps,
+                  int64_t idx_step_stride) {
   GlmArgs a;
   int rc = fill_common(a, model, chains, n, idx_dev, idx_stride, nullptr, ws,
                        ws_size, status_dev, tune);
@@ -893,6 +1265,13 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                      "sgld_glm_step: keep table given without sample buffer");
   if (noise->noise_dev != nullptr && noise->noise_stride < model->d)
     return set_error(GBSGMC_ERR_ARG, "sgld_glm_step: noise_stride < d");
+  if (steps < 1 || idx_step_stride < 0 || (steps > 1 && noise->noise_dev != nullptr))
+    return set_error(GBSGMC_ERR_ARG,
+                     "sgld_glm_steps: steps < 1, negative index step stride, or "
+                     "injected noise with several steps");
+  if (steps > 1 && chains == 0) return GBSGMC_OK;
+  a.steps = steps;
+  a.idx_step_stride = steps > 1 ? idx_step_stride : 0;
   a.mode = kSgldStep;
   a.w = w_dev;
   a.v = v_dev;
@@ -948,5 +1327,20 @@ extern "C" int gbsgmc_sgld_glm_step(
                        alpha, lmbd, sched, noise, U_dev, lk_var_dev,
                        samples_dev, sample_lik_dev, workspace_dev,
                        workspace_bytes, status_dev,
-                       static_cast<cudaStream_t>(stream), GlmTune{});
+                       static_cast<cudaStream_t>(stream), GlmTune{}, 1, 0);
+}
+
+extern "C" int gbsgmc_sgld_glm_steps(
+    const gbsgmc_glm* model, int chains, int n, const int32_t* idx_dev,
+    int64_t idx_stride, int64_t idx_step_stride, int steps, float* w_dev,
+    float* v_dev, float alpha, float lmbd, const gbsgmc_sched* sched,
+    const gbsgmc_noise* noise, double* U_dev, double* lk_var_dev,
+    float* samples_dev, double* sample_lik_dev, void* workspace_dev,
+    size_t workspace_bytes, int* status_dev, gbsgmc_stream_t stream) {
+  return glm_sgld_step(model, chains, n, idx_dev, idx_stride, w_dev, v_dev,
+                       alpha, lmbd, sched, noise, U_dev, lk_var_dev,
+                       samples_dev, sample_lik_dev, workspace_dev,
+                       workspace_bytes, status_dev,
+                       static_cast<cudaStream_t>(stream), GlmTune{}, steps,
+                       idx_step_stride);
 }

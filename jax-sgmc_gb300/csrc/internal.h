@@ -19,6 +19,8 @@ struct GlmTune {
   int rows_per_warp = 0;  // 2, 4 or 8 (d <= 256 only)
   int warps = 0;          // warps per CTA: 8 or 16
   int prefetch = 0;       // 1: two register tiles in flight per warp
+  int dynamic = 0;        // 1: warps claim items of `slices` per chain
+  int multistep = 0;      // 1: plans run a block of steps in one launch
 };
 
 size_t glm_ws_bytes(int chains, int n, int d);
@@ -32,7 +34,8 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   const gbsgmc_sched* sched, const gbsgmc_noise* noise,
                   double* U_dev, double* lk_var_dev, float* samples_dev,
                   double* sample_lik_dev, void* ws, size_t ws_size,
-                  int* status_dev, cudaStream_t stream, GlmTune tune);
+                  int* status_dev, cudaStream_t stream, GlmTune tune,
+                  int steps = 1, int64_t idx_step_stride = 0);
 
 // update.cu: fusions of the integrator updates used by the network plans.
 struct UpdateFusion {

@@ -57,7 +57,9 @@ struct GlmPlan final : gbsgmc_plan {
     if (idx != nullptr) cudaFree(idx);
   }
   int enqueue(int g, cudaStream_t s) override;
-  int64_t launches_per_block(int g) const override { return g + 2; }
+  int64_t launches_per_block(int g) const override {
+    return tune.multistep ? 3 : g + 2;
+  }
 };
 
 }  // namespace
@@ -139,6 +141,18 @@ int GlmPlan::enqueue(int g, cudaStream_t s) {
                              cn, s);
   }
   if (rc != GBSGMC_OK) return rc;
+  if (p->tune.multistep) {
+    // One launch for the g steps: each CTA runs its chain's steps in turn.
+    gbsgmc_sched s0 = p->sched;
+    s0.base_dev = p->base;
+    s0.offset = 0;
+    rc = glm_sgld_step(&p->model, p->chains, p->n, p->idx, p->n, p->w, p->v,
+                       p->alpha, p->lmbd, &s0, &p->noise, p->U, p->lk_var,
+                       p->samples, p->sample_lik, p->ws, p->ws_size, p->status,
+                       s, p->tune, g, cn);
+    if (rc != GBSGMC_OK) return rc;
+    return plan_advance(p, g, s);
+  }
   for (int j = 0; j < g; ++j) {
     gbsgmc_sched sj = p->sched;
     sj.base_dev = p->base;
@@ -185,9 +199,26 @@ int autotune(GlmPlan* p) {
         // (rows per warp, warps, prefetch)
         const int shapes[][3] = {{2, 8, 0}, {4, 8, 0}, {4, 8, 1}, {8, 8, 0},
                                  {2, 8, 1}, {2, 16, 0}, {4, 16, 0}, {4, 16, 1}};
-        for (const auto& sh : shapes) cands.push_back(GlmTune{s, sh[0], sh[1], sh[2]});
+        for (const auto& sh : shapes) cands.push_back(GlmTune{s, sh[0], sh[1], sh[2], 0});
       } else {
-        for (int w : {8, 16}) cands.push_back(GlmTune{s, 0, w, 0});
+        for (int w : {8, 16}) cands.push_back(GlmTune{s, 0, w, 0, 0});
+      }
+    }
+    // Dynamically scheduled kernel: items of n / ipc rows claimed by warps.
+    if (d <= 256) {
+      for (int ipc : {4, 8, 16}) {
+        if (n / ipc < 32) continue;
+        for (int rw : {4, 8}) cands.push_back(GlmTune{ipc, rw, 8, 0, 1, 0});
+      }
+    }
+    // One CTA per chain running a block of steps per launch.
+    if (n <= 1024 && p->G >= 6) {
+      const size_t m = cands.size();
+      for (size_t i = 0; i < m; ++i) {
+        if (cands[i].slices != 1 || cands[i].dynamic) continue;
+        GlmTune t = cands[i];
+        t.multistep = 1;
+        cands.push_back(t);
       }
     }
   }
@@ -226,13 +257,30 @@ int autotune(GlmPlan* p) {
     const char* vb = std::getenv("GBSGMC_AUTOTUNE_VERBOSE");
     const bool verbose = vb != nullptr && vb[0] == '1';
     for (const GlmTune& t : cands) {
-      for (int rep = 0; rep < 2 + 6 && rc == GBSGMC_OK; ++rep) {
-        if (rep == 2) cudaEventRecord(e0, p->stream);
-        const int j = rep % trials;
-        rc = glm_sgld_step(&p->model, C, n, p->idx + static_cast<int64_t>(j) * C * n,
-                           n, w, p->v != nullptr ? v : nullptr, p->alpha, p->lmbd,
-                           &sch, &p->noise, p->U, p->lk_var, nullptr, nullptr,
-                           p->ws, p->ws_size, status, p->stream, t);
+      if (t.multistep) {
+        // Two warm-up steps, then six steps in one launch.
+        for (int rep = 0; rep < 2 && rc == GBSGMC_OK; ++rep)
+          rc = glm_sgld_step(&p->model, C, n, p->idx, n, w,
+                             p->v != nullptr ? v : nullptr, p->alpha, p->lmbd,
+                             &sch, &p->noise, p->U, p->lk_var, nullptr, nullptr,
+                             p->ws, p->ws_size, status, p->stream, t);
+        if (rc == GBSGMC_OK) {
+          cudaEventRecord(e0, p->stream);
+          rc = glm_sgld_step(&p->model, C, n, p->idx, n, w,
+                             p->v != nullptr ? v : nullptr, p->alpha, p->lmbd,
+                             &sch, &p->noise, p->U, p->lk_var, nullptr, nullptr,
+                             p->ws, p->ws_size, status, p->stream, t, 6,
+                             static_cast<int64_t>(C) * n);
+        }
+      } else {
+        for (int rep = 0; rep < 2 + 6 && rc == GBSGMC_OK; ++rep) {
+          if (rep == 2) cudaEventRecord(e0, p->stream);
+          const int j = rep % trials;
+          rc = glm_sgld_step(&p->model, C, n, p->idx + static_cast<int64_t>(j) * C * n,
+                             n, w, p->v != nullptr ? v : nullptr, p->alpha, p->lmbd,
+                             &sch, &p->noise, p->U, p->lk_var, nullptr, nullptr,
+                             p->ws, p->ws_size, status, p->stream, t);
+        }
       }
       if (rc != GBSGMC_OK) break;
       cudaEventRecord(e1, p->stream);
@@ -241,8 +289,10 @@ int autotune(GlmPlan* p) {
       cudaEventElapsedTime(&ms, e0, e1);
       if (verbose)
         std::fprintf(stderr,
-                     "gbsgmc autotune: slices %d rows/warp %d warps %d prefetch %d: %.4f ms\n",
-                     t.slices, t.rows_per_warp, t.warps, t.prefetch, ms / 6.0f);
+                     "gbsgmc autotune: slices %d rows/warp %d warps %d prefetch %d "
+                     "dynamic %d multistep %d: %.4f ms\n",
+                     t.slices, t.rows_per_warp, t.warps, t.prefetch, t.dynamic,
+                     t.multistep, ms / 6.0f);
       if (ms < best_ms) {
         best_ms = ms;
         best = t;
@@ -314,6 +364,10 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
       break;
     if ((rc = glm_prepare())) break;
     if ((rc = autotune(p))) break;
+    // GBSGMC_GLM_MULTISTEP=1/0 forces one launch per block of steps or one
+    // launch per step, whatever the autotuner chose.
+    if (const char* ms = std::getenv("GBSGMC_GLM_MULTISTEP"))
+      if (ms[0] == '0' || ms[0] == '1') p->tune.multistep = ms[0] == '1';
     rc = plan_capture(p);
   } while (false);
   if (rc != GBSGMC_OK) {
@@ -358,16 +412,21 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
 }
 
 extern "C" int gbsgmc_plan_launch_shape(const gbsgmc_plan* p, int* slices,
-                                        int* rows_per_warp, int* warps, int* prefetch) {
+                                        int* rows_per_warp, int* warps, int* prefetch,
+                                        int* dynamic, int* steps_per_launch) {
   if (p == nullptr || slices == nullptr || rows_per_warp == nullptr ||
-      warps == nullptr || prefetch == nullptr)
+      warps == nullptr || prefetch == nullptr || dynamic == nullptr ||
+      steps_per_launch == nullptr)
     return set_error(GBSGMC_ERR_ARG, "plan_launch_shape: null argument");
-  *slices = *rows_per_warp = *warps = *prefetch = 0;
+  *slices = *rows_per_warp = *warps = *prefetch = *dynamic = 0;
+  *steps_per_launch = 1;
   if (const GlmPlan* g = dynamic_cast<const GlmPlan*>(p)) {
     *slices = g->tune.slices;
     *rows_per_warp = g->tune.rows_per_warp;
     *warps = g->tune.warps;
     *prefetch = g->tune.prefetch;
+    *dynamic = g->tune.dynamic;
+    if (g->tune.multistep) *steps_per_launch = g->G;
   }
   return GBSGMC_OK;
 }

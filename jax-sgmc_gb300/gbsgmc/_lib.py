@@ -158,6 +158,9 @@ SIGNATURES = {
     "gbsgmc_sgld_glm_step": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp, _f, _f,
                                   _P(Sched), _P(Noise), _vp, _vp, _vp, _vp,
                                   _vp, _sz, _vp, _vp]),
+    "gbsgmc_sgld_glm_steps": (_i, [_P(Glm), _i, _i, _vp, _i64, _i64, _i, _vp, _vp,
+                                   _f, _f, _P(Sched), _P(Noise), _vp, _vp, _vp,
+                                   _vp, _vp, _sz, _vp, _vp]),
     "gbsgmc_sgld_glm_step_noalloc": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp,
                                           _f, _f, _P(Sched), _P(Noise), _vp,
                                           _vp, _vp, _vp, _vp, _vp]),
@@ -181,7 +184,8 @@ SIGNATURES = {
                                            _vp, _i, _vp]),
     "gbsgmc_plan_run": (_i, [_vp, _i64, _i64, _vp]),
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
-    "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i), _P(_i)]),
+    "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i), _P(_i), _P(_i),
+                                      _P(_i)]),
     "gbsgmc_plan_destroy": (_i, [_vp]),
     "gbsgmc_gemm_bf16": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64, _vp,
                               _i64, _i64, _i, _i, _i, _i, _vp, _vp]),

@@ -75,12 +75,13 @@ class SgldGlmPlan:
               _lib.stream_handle())
 
   def launch_shape(self):
-    """(CTAs per chain, rows per warp, warps per CTA, prefetch) from the
-    autotuner."""
-    s, r, w, f = _lib.C.c_int(), _lib.C.c_int(), _lib.C.c_int(), _lib.C.c_int()
+    """(CTAs or row items per chain, rows per warp, warps per CTA,
+    prefetch, dynamic scheduling, steps per launch) from the autotuner."""
+    s, r, w, f, y, k = (_lib.C.c_int() for _ in range(6))
     _lib.call("gbsgmc_plan_launch_shape", self.handle, _lib.C.byref(s),
-              _lib.C.byref(r), _lib.C.byref(w), _lib.C.byref(f))
-    return s.value, r.value, w.value, f.value
+              _lib.C.byref(r), _lib.C.byref(w), _lib.C.byref(f),
+              _lib.C.byref(y), _lib.C.byref(k))
+    return s.value, r.value, w.value, f.value, y.value, k.value
 
   def launches(self, steps) -> int:
     return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps)))

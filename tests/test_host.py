@@ -43,6 +43,32 @@ def test_argument_validation_without_a_gpu():
   assert lib.gbsgmc_glm_workspace_bytes(256, 1024, 256) > 256 * 1024
 
 
+def test_multi_step_abi_validation_without_a_gpu():
+  """gbsgmc_sgld_glm_steps rejects a step count below one, a negative
+  index step stride and injected noise over several steps before touching
+  the device (the pointers below are never dereferenced)."""
+  import ctypes as C
+  from gbsgmc import _lib
+  lib = _lib.load()
+  fake = C.c_void_p(4096)
+  m = _lib.Glm(family=1, d=8, n_obs=100, ld=9, X=4096, y=None, sigma=1.0,
+               prior_scale=1.0, temperature=1.0, y_inline=1, n_rows=100)
+  sch = _lib.sched(step_size=1e-3)
+  gen = _lib.noise(seed=1)
+  injected = _lib.Noise(4096, 8, 0, 0, 0)
+
+  def call(steps, stride, nz):
+    return lib.gbsgmc_sgld_glm_steps(C.byref(m), 2, 16, fake, 16, stride, steps,
+                                     fake, None, 0.9, 1e-5, C.byref(sch),
+                                     C.byref(nz), None, None, None, None, fake,
+                                     1 << 20, None, None)
+
+  assert call(0, 32, gen) == _lib.ERR_ARG
+  assert call(3, -1, gen) == _lib.ERR_ARG
+  assert call(3, 32, injected) == _lib.ERR_ARG
+  assert b"injected noise" in lib.gbsgmc_last_error()
+
+
 def test_mlp_abi_shapes_and_validation_without_a_gpu():
   import ctypes as C
   from gbsgmc import _lib, likelihoods as L
