@@ -31,7 +31,7 @@ class MassMatrix(NamedTuple):
 
 
 class RmsPropState(NamedTuple):
-  v: Any        # fp32 device [P]
+  v: Any        # fp32 [P], on the device once the chain has stepped
   alpha: float
   lmbd: float
 
@@ -49,7 +49,8 @@ def rms_prop() -> AdaptionStrategy:
   def init(sample, alpha=0.9, lmbd=1e-5):
     import torch
     n = sample.numel() if hasattr(sample, "numel") else len(sample)
-    return RmsPropState(torch.ones(n, dtype=torch.float32, device="cuda"),
+    dev = sample.device if hasattr(sample, "device") else "cuda"
+    return RmsPropState(torch.ones(n, dtype=torch.float32, device=dev),
                         float(alpha), float(lmbd))
 
   def update(state: RmsPropState, sample, sample_grad, *args, **kwargs):

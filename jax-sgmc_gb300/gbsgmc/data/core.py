@@ -268,8 +268,9 @@ class IndexedBatch:
 # Random access
 # ---------------------------------------------------------------------------
 
-def _pcg_to_device(bitgen_state: dict):
-  """numpy PCG64 state dict -> device ``gbsgmc_pcg64`` (as int64 words)."""
+def _pcg_words(bitgen_state: dict):
+  """numpy PCG64 state dict -> host ``gbsgmc_pcg64`` words (int64); the
+  first refill moves them to the device."""
   import torch
   st = bitgen_state["state"]["state"]
   inc = bitgen_state["state"]["inc"]
@@ -280,7 +281,7 @@ def _pcg_to_device(bitgen_state: dict):
   words[2] = (inc >> 64) & m64
   words[3] = inc & m64
   words[4] = (int(bitgen_state["uinteger"]) << 32) | int(bitgen_state["has_uint32"])
-  return torch.from_numpy(words.view(np.int64).copy()).cuda()
+  return torch.from_numpy(words.view(np.int64).copy())
 
 
 def pcg_from_device(t) -> dict:
@@ -375,7 +376,7 @@ def _random_reference_data_host(loader, cache, mb_size):
                         valid=valid)
     # The first cache is drawn by the first batch_fn call (the stream order is
     # the reference's: consecutive draws, whatever the cache size).
-    pcg = _pcg_to_device(chain["rng"].bit_generator.state)
+    pcg = _pcg_words(chain["rng"].bit_generator.state)
     return CacheState(cached_batches=None, cached_batches_count=cache,
                       current_line=cache, chain_id=chain_id, state=pcg,
                       valid=None)
@@ -387,6 +388,9 @@ def _random_reference_data_host(loader, cache, mb_size):
         cached = torch.from_numpy(idx.astype(np.int32)).cuda()
         valid = torch.from_numpy(mask.astype(np.float32)).cuda()
       else:
+        # The draw kernel advances the stream in place on the device.
+        if not data_state.state.is_cuda:
+          data_state = data_state._replace(state=data_state.state.cuda())
         cached = refill(data_state.state)
         valid = None
       data_state = data_state._replace(cached_batches=cached, valid=valid,

@@ -310,8 +310,8 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
     adapt = [s.adapt_state for s in states]
     if any(a is None for a in adapt) and not all(a is None for a in adapt):
       return None
-    X = torch.stack([s.latent_variables for s in states]).contiguous()
-    AUX = torch.stack([a.v for a in adapt]).contiguous() \
+    X = torch.stack([s.latent_variables for s in states]).contiguous().cuda()
+    AUX = torch.stack([a.v for a in adapt]).contiguous().cuda() \
         if adapt[0] is not None else None
     kw = dict(alpha=adapt[0].alpha, lmbd=adapt[0].lmbd) \
         if adapt[0] is not None else {}
@@ -325,7 +325,7 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
     kw = dict(friction=float(im["friction"]), leapfrog_steps=steps)
     if any(int(s.step) != 0 for s in states):
       return None
-  pcg = torch.stack([d.state for d in ds_list]).contiguous()
+  pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
   index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
   dataset = rbf.loader.device_dataset()
   h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
@@ -350,12 +350,15 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
     plan.check_status()
   finally:
     plan.close()
-  for c, s in enumerate(states):   # the streams advanced on the device
-    s.data_state.state.copy_(pcg[c])
+  host = pcg.cpu()   # the streams advanced on the device
+  for c, s in enumerate(states):
+    dst = s.data_state.state
+    dst.copy_(pcg[c] if dst.is_cuda else host[c])
   key = "likelihood" if kind == "langevin" else "energy"
-  return [io.postprocess(saving or io.no_save(), n_kept, samples[:n_kept, c],
-                         s.treedef, {key: extra[:n_kept, c]}, s.model_state)
-          for c, s in enumerate(states)]
+  return io.postprocess_chains(saving or io.no_save(), n_kept,
+                               samples[:n_kept], [s.treedef for s in states],
+                               {key: extra[:n_kept]},
+                               [s.model_state for s in states])
 
 
 def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
@@ -390,7 +393,7 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
     ds_list = [s.data_state for s in states]
     if any(d.state is None or d.cached_batches is not None for d in ds_list):
       return None   # shuffled streams, or draws already consumed
-    pcg = torch.stack([d.state for d in ds_list]).contiguous()
+    pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
     index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
   else:
     seeds = {s.data_state.state[0] for s in states}
@@ -398,11 +401,11 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
       return None
     index_src = IndexSource(seed=seeds.pop(), chain_base=chain_ids[0])
   dataset = rbf.loader.device_dataset()
-  W = torch.stack([s.latent_variables for s in states]).contiguous()
+  W = torch.stack([s.latent_variables for s in states]).contiguous().cuda()
   if W.shape[1] != pot.dim(dataset):
     return None
   if adapt[0] is not None:
-    V = torch.stack([a.v for a in adapt]).contiguous()
+    V = torch.stack([a.v for a in adapt]).contiguous().cuda()
     alpha, lmbd = adapt[0].alpha, adapt[0].lmbd
   else:
     V, alpha, lmbd = None, 0.9, 1e-5
@@ -413,12 +416,13 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
                      chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,
                      block_steps=block)
   if rbf.kind == "host":
-    for c, s in enumerate(states):   # the streams advanced on the device
-      s.data_state.state.copy_(index_src.pcg[c])
-  out = []
-  for c, s in enumerate(states):
-    out.append(io.postprocess(saving or io.no_save(), n_kept,
-                              res.samples[:, c], s.treedef,
-                              {"likelihood": res.sample_lik[:, c]},
-                              s.model_state))
-  return out
+    # The streams advanced on the device; states still holding their
+    # initial host words get them back in one copy.
+    host = index_src.pcg.cpu()
+    for c, s in enumerate(states):
+      dst = s.data_state.state
+      dst.copy_(index_src.pcg[c] if dst.is_cuda else host[c])
+  return io.postprocess_chains(saving or io.no_save(), n_kept, res.samples,
+                               [s.treedef for s in states],
+                               {"likelihood": res.sample_lik},
+                               [s.model_state for s in states])

@@ -93,6 +93,18 @@ def _flat(sample):
   return torch.from_numpy(flat).cuda(), tdef
 
 
+def _flat_host(sample):
+  """Flat fp32 host tensor of a sample (a copy).  The first step moves it to
+  the device; fused runs of many chains move all chains' in one copy."""
+  import torch
+  flat, tdef = util.ravel(sample)
+  return torch.from_numpy(flat), tdef
+
+
+def _dev(t):
+  return t if t is None or t.is_cuda else t.cuda()
+
+
 def _flat_tree_like(tree, P, fill=None):
   """Mass / friction pytree (or scalar) -> fp32 device [P] or None."""
   import torch
@@ -139,15 +151,16 @@ def langevin_diffusion(potential_fn, batch_fn, adaption: AdaptionStrategy = None
     import torch
     adaption_kwargs = adaption_kwargs or {}
     batch_kwargs = batch_kwargs or {}
-    w, tdef = _flat(init_sample)
+    # The state starts on the host; update_fn (or a fused run) moves it.
+    w, tdef = _flat_host(init_sample)
     adapt_state = None if adaption is None else adaption.init(w, **adaption_kwargs)
     data_state = batch_init(**batch_kwargs)
     chain = int(data_state.chain_id or 0)
     return LangevinState(
         latent_variables=w, model_state=init_model_state,
         key=key_to_seed(key), adapt_state=adapt_state, data_state=data_state,
-        potential=torch.zeros((), dtype=torch.float64, device="cuda"),
-        variance=torch.ones((), dtype=torch.float64, device="cuda"),
+        potential=torch.zeros((), dtype=torch.float64),
+        variance=torch.ones((), dtype=torch.float64),
         step=0, chain=chain, treedef=tdef)
 
   def get_fn(state: LangevinState):
@@ -157,9 +170,12 @@ def langevin_diffusion(potential_fn, batch_fn, adaption: AdaptionStrategy = None
 
   def update_fn(state: LangevinState, parameters):
     data_state, (batch, info) = batch_get(state.data_state, information=True)
-    r = _eval(potential_fn, state.latent_variables, batch, info)
-    w = state.latent_variables
-    v = None if state.adapt_state is None else state.adapt_state.v
+    w = _dev(state.latent_variables)
+    r = _eval(potential_fn, w, batch, info)
+    adapt_state = state.adapt_state
+    if adapt_state is not None and not adapt_state.v.is_cuda:
+      adapt_state = adapt_state._replace(v=adapt_state.v.cuda())
+    v = None if adapt_state is None else adapt_state.v
     alpha = 0.9 if state.adapt_state is None else state.adapt_state.alpha
     lmbd = 1e-5 if state.adapt_state is None else state.adapt_state.lmbd
     buf = _injected(noise_source, state.step, state.chain, _lib.TAG_SGLD)
@@ -169,7 +185,8 @@ def langevin_diffusion(potential_fn, batch_fn, adaption: AdaptionStrategy = None
     _lib.call("gbsgmc_sgld_update", 1, w.numel(), _lib.ptr(w),
               _lib.ptr(r.grad), _lib.ptr(v), alpha, lmbd, sch,
               _noise(state.key, state.chain, buf), None, _lib.stream_handle())
-    return state._replace(data_state=data_state, potential=r.U[0],
+    return state._replace(latent_variables=w, adapt_state=adapt_state,
+                          data_state=data_state, potential=r.U[0],
                           variance=r.lk_var[0], step=state.step + 1)
 
   return IntegratorTriplet(init_fn, update_fn, get_fn, kind="langevin",

@@ -79,10 +79,29 @@ def postprocess(saving: Saving, count: int, variables, treedef, extras: dict,
     var_tree = util.tree_unflatten(treedef, leaves)
     samples = {"variables": var_tree, **extras, "model_state": model_state}
     return {"sample_count": count, "samples": samples}
-  host = variables.detach().cpu().numpy()
+  host = variables if isinstance(variables, np.ndarray) else \
+      variables.detach().cpu().numpy()
   samples = {"variables": util.unravel(treedef, host)}
   for k, v in extras.items():
     samples[k] = v.detach().cpu().numpy() if hasattr(v, "detach") else v
   samples["model_state"] = model_state
   samples = saving.collector.finalize(samples)
   return {"sample_count": count, "samples": samples}
+
+
+def postprocess_chains(saving: Saving, count: int, variables, treedefs,
+                       extras: dict, model_states) -> list:
+  """Result dicts of C chains from a ``[count, C, P]`` device buffer (extras
+  ``[count, C]``).  With host saving, the buffers of all chains are
+  transposed chain-major on the device and copied to the host at once, and
+  each chain's arrays are views of that copy."""
+  C = variables.shape[1]
+  if saving is None or saving.kind == "device":
+    return [postprocess(saving, count, variables[:, c], treedefs[c],
+                        {k: v[:, c] for k, v in extras.items()},
+                        model_states[c]) for c in range(C)]
+  host = variables.permute(1, 0, 2).contiguous().cpu().numpy()
+  hext = {k: v.t().contiguous().cpu().numpy() for k, v in extras.items()}
+  return [postprocess(saving, count, host[c], treedefs[c],
+                      {k: v[c] for k, v in hext.items()}, model_states[c])
+          for c in range(C)]
