@@ -88,10 +88,11 @@ struct GlmArgs {
   int dyn_fixed;      // 1: dynamically scheduled kernel, -1: not, 0: library choice
   int* status;
   int vec4;   // rows are 16-byte aligned: 128-bit loads
+  int l2_hints;  // rows evict-first, separate targets evict-last in L2
 };
 
 struct SmemLayout {
-  size_t flags, idx, m, red, sums, total;
+  size_t flags, idx, idx2, m, red, sums, wbuf, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t x, size_t a) {
@@ -107,6 +108,9 @@ __host__ __device__ inline SmemLayout smem_layout(int rows_per_slice, int dq,
   L.idx = o;
   o += sizeof(int32_t) * rows_per_slice;
   o = align_up(o, 16);
+  L.idx2 = o;  // the next step's indices (multi-step launches)
+  o += sizeof(int32_t) * rows_per_slice;
+  o = align_up(o, 16);
   L.m = o;
   o += sizeof(float) * rows_per_slice;
   o = align_up(o, 16);
@@ -115,6 +119,9 @@ __host__ __device__ inline SmemLayout smem_layout(int rows_per_slice, int dq,
   o = align_up(o, 16);
   L.sums = o;
   o += sizeof(double) * 4 * (warps + 1);
+  o = align_up(o, 16);
+  L.wbuf = o;  // w between the steps of a multi-step launch
+  o += static_cast<size_t>(dq) * 16;
   L.total = o;
   return L;
 }
@@ -142,6 +149,45 @@ __device__ __forceinline__ float4 ld_row4(const float* p) {
 __device__ __forceinline__ float ld_row1(const float* p) {
   float v;
   asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
+// 4-byte asynchronous copy global -> shared (completes in the background;
+// cp_async_wait_all waits for the calling thread's copies).
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gmem_src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// The same loads with an L2 eviction-priority policy (createpolicy): rows
+// are streamed once and should leave L2 first; a separate target array is
+// small and gathered by every chain, so it should stay.
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float4 ld_row4_hint(const float* p, uint64_t pol) {
+  float4 v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ld_row1_hint(const float* p, uint64_t pol) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;"
+      : "=f"(v)
+      : "l"(p), "l"(pol));
   return v;
 }
 
@@ -196,7 +242,8 @@ __device__ __forceinline__ void load_tile(const GlmArgs& a, const int32_t* idx_s
       const int q = lane + 32 * k;
       if (o >= 0 && q < a.dq) {
         if (a.vec4) {
-          xv[r][k] = ld_row4(row + 4 * q);
+          xv[r][k] = a.l2_hints ? ld_row4_hint(row + 4 * q, l2_policy_evict_first())
+                                : ld_row4(row + 4 * q);
         } else {
           const int j = 4 * q;
           xv[r][k].x = ld_row1(row + j);
@@ -215,7 +262,8 @@ __device__ __forceinline__ void load_tile(const GlmArgs& a, const int32_t* idx_s
     if (a.y_inline) {
       yv = ld_row1(a.X + static_cast<int64_t>(og) * a.ld + a.d);
     } else if (a.y != nullptr) {
-      yv = ld_row1(a.y + og);
+      yv = a.l2_hints ? ld_row1_hint(a.y + og, l2_policy_evict_last())
+                      : ld_row1(a.y + og);
     }
   }
 }
@@ -304,10 +352,15 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
   const int dq = a.dq;
   const SmemLayout L = smem_layout(a.rows_per_slice, dq, WARPS);
   int* is_last = reinterpret_cast<int*>(smem + L.flags);
-  int32_t* idx_s = reinterpret_cast<int32_t*>(smem + L.idx);
+  // Multi-step launches alternate two index buffers: step j reads buffer
+  // j & 1 while the copies of step j + 1 fill the other.
+  const bool multi = a.steps > 1;
+  int32_t* idx_s = reinterpret_cast<int32_t*>(smem + ((multi && (j & 1)) ? L.idx2 : L.idx));
+  int32_t* idx_next = reinterpret_cast<int32_t*>(smem + ((j & 1) ? L.idx : L.idx2));
   float* m_s = reinterpret_cast<float*>(smem + L.m);
   float4* red = reinterpret_cast<float4*>(smem + L.red);
   double* sums = reinterpret_cast<double*>(smem + L.sums);
+  float4* w_s = reinterpret_cast<float4*>(smem + L.wbuf);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int s = blockIdx.x, c = blockIdx.y;
@@ -315,34 +368,93 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
   const int R = max(0, min(a.rows_per_slice, a.n - row0));
 
   if (tid == 0) *is_last = 0;
-  // Observation indices (and mask weights) of this slice.
+  // Observation indices (and mask weights) of this slice.  In a multi-step
+  // launch the indices of step j > 0 were copied asynchronously during step
+  // j - 1 (each thread the same entries r), so they are only checked here.
   const int32_t* idx_j = a.idx + j * a.idx_step_stride;
-  for (int r = tid; r < R; r += (WARPS * 32)) {
-    int32_t o = __ldg(idx_j + c * a.idx_stride + row0 + r);
-    if (o < 0 || o >= a.n_rows) {
-      raise_status(a.status, GBSGMC_ERR_INDEX);
-      o = -1;
+  if (multi && j > 0) {
+    cp_async_wait_all();
+    for (int r = tid; r < R; r += (WARPS * 32)) {
+      const int32_t o = idx_s[r];
+      if (o < 0 || o >= a.n_rows) {
+        raise_status(a.status, GBSGMC_ERR_INDEX);
+        idx_s[r] = -1;
+      }
     }
-    idx_s[r] = o;
-    if (a.mask != nullptr)
-      m_s[r] = __ldg(a.mask + static_cast<int64_t>(c) * a.n + row0 + r);
+  } else {
+    for (int r = tid; r < R; r += (WARPS * 32)) {
+      int32_t o = __ldg(idx_j + c * a.idx_stride + row0 + r);
+      if (o < 0 || o >= a.n_rows) {
+        raise_status(a.status, GBSGMC_ERR_INDEX);
+        o = -1;
+      }
+      idx_s[r] = o;
+      if (a.mask != nullptr)
+        m_s[r] = __ldg(a.mask + static_cast<int64_t>(c) * a.n + row0 + r);
+    }
   }
   __syncthreads();
+  if (multi && j + 1 < a.steps) {
+    const int32_t* src = idx_j + a.idx_step_stride + c * a.idx_stride + row0;
+    for (int r = tid; r < R; r += (WARPS * 32)) cp_async4(idx_next + r, src + r);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
 
+  // w of the chain: from global memory at the first step of a launch, then
+  // from the copy the previous step's update left in shared memory.
   float4 wq[QPL];
   Accum<QPL> A;
   const float* w_in = a.w + static_cast<int64_t>(c) * a.d;
 #pragma unroll
   for (int k = 0; k < QPL; ++k) {
-    const int j = 4 * (lane + 32 * k);
-    wq[k].x = j + 0 < a.d ? w_in[j + 0] : 0.0f;
-    wq[k].y = j + 1 < a.d ? w_in[j + 1] : 0.0f;
-    wq[k].z = j + 2 < a.d ? w_in[j + 2] : 0.0f;
-    wq[k].w = j + 3 < a.d ? w_in[j + 3] : 0.0f;
+    const int q = lane + 32 * k;
+    const int e0 = 4 * q;
+    if (multi && j > 0) {
+      wq[k] = q < dq ? w_s[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+      wq[k].x = e0 + 0 < a.d ? w_in[e0 + 0] : 0.0f;
+      wq[k].y = e0 + 1 < a.d ? w_in[e0 + 1] : 0.0f;
+      wq[k].z = e0 + 2 < a.d ? w_in[e0 + 2] : 0.0f;
+      wq[k].w = e0 + 3 < a.d ? w_in[e0 + 3] : 0.0f;
+    }
     A.acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   A.mlk = A.K = A.s1 = A.s2 = 0.0f;
   A.cnt = 0;
+  // What the epilogue needs, loaded now so that the latency overlaps the row
+  // stream instead of stalling the step after it: the schedule at this step
+  // (counter, then table entries), the chain's RMSprop state for this
+  // thread's parameters (q = tid), and sum(w^2) for the prior (warp 0, from
+  // the w just loaded; zero past d).
+  int64_t k_step = 0;
+  float h_step = 0.0f, t_step = 1.0f;
+  int slot = -1;
+  float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (a.mode == kSgldStep) {
+    k_step = a.sched.step() + j;
+    h_step = a.sched.step_size(k_step);
+    t_step = a.sched.temperature(k_step, c);
+    slot = a.sched.keep_slot(k_step);
+    if (a.v != nullptr && tid < dq) {
+      const float* vc = a.v + static_cast<int64_t>(c) * a.d + 4 * tid;
+      const int e0 = 4 * tid;
+      vq.x = vc[0];
+      vq.y = e0 + 1 < a.d ? vc[1] : 0.0f;
+      vq.z = e0 + 2 < a.d ? vc[2] : 0.0f;
+      vq.w = e0 + 3 < a.d ? vc[3] : 0.0f;
+    }
+  }
+  if (a.inv_p2 > 0.0f && warp == 0) {
+    double ww = 0.0;
+#pragma unroll
+    for (int k = 0; k < QPL; ++k) {
+      const double e[4] = {wq[k].x, wq[k].y, wq[k].z, wq[k].w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) ww += e[i] * e[i];
+    }
+    ww = warp_sum(ww);
+    if (lane == 0) sums[WARPS * 4 + 3] = ww;
+  }
   const int g = lane >> (5 - LOG);           // my row in the link phase
   const bool leader = (lane & (GROUP - 1)) == 0;
   float* lk_out = a.lk != nullptr ? a.lk + static_cast<int64_t>(c) * a.n + row0
@@ -472,15 +584,7 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
   float* wc = a.w + static_cast<int64_t>(c) * a.d;
   const float scale = static_cast<float>(static_cast<double>(a.n_obs) / a.n);
 
-  double ww = 0.0;
-  if (a.inv_p2 > 0.0f) {
-    for (int j = tid; j < a.d; j += (WARPS * 32)) {
-      const double wj = wc[j];
-      ww += wj * wj;
-    }
-  }
-  // Reuse the per-warp sums area as block-reduction scratch (9 warps).
-  ww = block_sum(ww, sums);
+  const double ww = a.inv_p2 > 0.0f ? sums[WARPS * 4 + 3] : 0.0;
   const double log_prior = -0.5 * ww * a.inv_p2 - a.prior_const;
   // -N * mean(lk) without a mask, -N/n * (lk . mask) with one, as written in
   // potential.py:183-185 (the unmasked form is exact for integer sums).
@@ -506,41 +610,49 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
     return;
   }
 
-  // SGLD (+RMSprop) update of chain c, four parameters per thread.
-  const int64_t k = a.sched.step() + j;
-  const float h = a.sched.step_size(k);
-  const float T = a.sched.temperature(k, c);
-  const int slot = a.sched.keep_slot(k);
-  const float noise_scale = sqrtf(2.0f * T * h);
+  // SGLD (+RMSprop) update of chain c: thread tid < dq owns the four
+  // parameters 4 tid .. 4 tid + 3, whose w is in its warp's wq[tid / 32]
+  // (dq <= 32 QPL <= WARPS * 32).
+  const float noise_scale = sqrtf(2.0f * t_step * h_step);
   float* vc = a.v != nullptr ? a.v + static_cast<int64_t>(c) * a.d : nullptr;
   float* smp = slot >= 0 ? a.samples + (static_cast<int64_t>(slot) * a.chains + c) * a.d
                          : nullptr;
   bool bad = false;
-  for (int q = tid; q < dq; q += (WARPS * 32)) {
+  if (tid < dq) {
+    const int q = tid;
+    float4 xq = wq[0];
+#pragma unroll
+    for (int k = 1; k < QPL; ++k)
+      if (warp == k) xq = wq[k];
+    const float xs[4] = {xq.x, xq.y, xq.z, xq.w};
+    const float vs[4] = {vq.x, vq.y, vq.z, vq.w};
     float xi[4];
-    noise4(a.noise, c, 4 * q, a.d, k, GBSGMC_TAG_SGLD, xi);
+    noise4(a.noise, c, 4 * q, a.d, k_step, GBSGMC_TAG_SGLD, xi);
+    float xn[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const int j = 4 * q + e;
-      if (j >= a.d) break;
-      const float x = wc[j];
-      const float g = (-scale * gl[j] + x * a.inv_p2) * a.inv_temp;
+      const int jj = 4 * q + e;
+      if (jj >= a.d) break;
+      const float x = xs[e];
+      const float g = (-scale * gl[jj] + x * a.inv_p2) * a.inv_temp;
       bad |= !isfinite(g);
-      const float scaled_gradient = -h * g;
+      const float scaled_gradient = -h_step * g;
       const float scaled_noise = noise_scale * xi[e];
       float x_new;
       if (vc != nullptr) {
-        const float vn = a.alpha * vc[j] + (1.0f - a.alpha) * (g * g);
+        const float vn = a.alpha * vs[e] + (1.0f - a.alpha) * (g * g);
         const float G = 1.0f / (a.lmbd + sqrtf(vn));
         const float sG = sqrtf(G);
-        vc[j] = vn;
+        vc[jj] = vn;
         x_new = x + ((0.0f + G * scaled_gradient) + sG * scaled_noise);
       } else {
         x_new = x + (scaled_gradient + scaled_noise);
       }
-      wc[j] = x_new;
-      if (smp != nullptr) smp[j] = x_new;
+      wc[jj] = x_new;
+      xn[e] = x_new;
+      if (smp != nullptr) smp[jj] = x_new;
     }
+    if (multi) w_s[q] = make_float4(xn[0], xn[1], xn[2], xn[3]);
   }
   if (bad) raise_status(a.status, GBSGMC_ERR_NONFINITE);
   if (tid == 0) {
@@ -1172,6 +1284,7 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.status = status;
   // 128-bit row loads need every row 16-byte aligned.
   a.vec4 = (reinterpret_cast<uintptr_t>(m->X) % 16 == 0) && (m->ld % 4 == 0) ? 1 : 0;
+  a.l2_hints = env_int("GBSGMC_GLM_L2HINT", 0) > 0 ? 1 : 0;
   a.lk = nullptr;
   a.lk_var = nullptr;
   a.grad = nullptr;

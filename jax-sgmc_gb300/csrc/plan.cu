@@ -7,10 +7,14 @@
 // counter by G.  The block is captured once into a CUDA graph and replayed,
 // so a run of K steps costs K/G graph launches on the host.  The schedule
 // tables (step size, temperature, keep slots) are read on the device at
-// step k.
+// step k.  When the autotuner chooses one launch per block (one CTA per
+// chain looping over the block's steps) and the indices come from PCG64
+// streams, blocks are pipelined: the index draws of block b+1 run on a side
+// stream into a second buffer while block b's launch runs.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <new>
@@ -20,6 +24,20 @@
 #include "common.cuh"
 #include "internal.h"
 #include "plan.cuh"
+
+int gbsgmc_plan::run_blocks(int64_t full, int rem) {
+  using namespace gbsgmc;
+  int rc;
+  for (int64_t b = 0; b < full; ++b) {
+    if (use_graph) {
+      if ((rc = cuda_err(cudaGraphLaunch(exec, stream), "plan_run: graph"))) return rc;
+    } else if ((rc = enqueue(G, stream))) {
+      return rc;
+    }
+  }
+  if (rem > 0 && (rc = enqueue(rem, stream))) return rc;
+  return GBSGMC_OK;
+}
 
 gbsgmc_plan::~gbsgmc_plan() {
   if (stream != nullptr) cudaStreamSynchronize(stream);
@@ -50,13 +68,36 @@ struct GlmPlan final : gbsgmc_plan {
   void* ws = nullptr;
   size_t ws_size = 0;
   int32_t* idx = nullptr;
+  // Pipelined blocks (one launch per block, numpy PCG64 index streams): the
+  // indices of block b+1 are drawn into the other buffer on a side stream
+  // while block b runs.  g_pref[p] / g_last[p]: the block reading buffer p,
+  // with and without the draw of the next block.
+  bool pipelined = false;
+  int32_t* idx2 = nullptr;
+  cudaStream_t side = nullptr;
+  cudaEvent_t e_fork = nullptr, e_join = nullptr;
+  cudaGraphExec_t g_pref[2] = {nullptr, nullptr}, g_last[2] = {nullptr, nullptr};
 
   ~GlmPlan() override {
     if (stream != nullptr) cudaStreamSynchronize(stream);
+    if (side != nullptr) cudaStreamSynchronize(side);
+    for (int i = 0; i < 2; ++i) {
+      if (g_pref[i] != nullptr) cudaGraphExecDestroy(g_pref[i]);
+      if (g_last[i] != nullptr) cudaGraphExecDestroy(g_last[i]);
+    }
+    if (e_fork != nullptr) cudaEventDestroy(e_fork);
+    if (e_join != nullptr) cudaEventDestroy(e_join);
+    if (side != nullptr) cudaStreamDestroy(side);
     if (ws != nullptr) cudaFree(ws);
     if (idx != nullptr) cudaFree(idx);
+    if (idx2 != nullptr) cudaFree(idx2);
   }
   int enqueue(int g, cudaStream_t s) override;
+  int run_blocks(int64_t full, int rem) override;
+  int draw(int g, int32_t* buf, cudaStream_t s);
+  int steps_launch(int g, int32_t* buf, cudaStream_t s);
+  int pipelined_block(int parity, bool prefetch, cudaStream_t s);
+  int setup_pipeline();
   int64_t launches_per_block(int g) const override {
     return tune.multistep ? 3 : g + 2;
   }
@@ -97,19 +138,8 @@ int plan_init(gbsgmc_plan* p, int G) {
 int plan_capture(gbsgmc_plan* p) {
   int rc = GBSGMC_OK;
   if (p->use_graph) {
-    if ((rc = cuda_err(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal),
-                       "plan: begin capture")))
-      return rc;
-    rc = p->enqueue(p->G, p->stream);
-    cudaGraph_t graph = nullptr;
-    const cudaError_t e = cudaStreamEndCapture(p->stream, &graph);
-    if (rc != GBSGMC_OK) {
-      if (graph != nullptr) cudaGraphDestroy(graph);
-      return rc;
-    }
-    if ((rc = cuda_err(e, "plan: end capture"))) return rc;
-    rc = cuda_err(cudaGraphInstantiate(&p->exec, graph, 0), "plan: instantiate");
-    cudaGraphDestroy(graph);
+    rc = capture_graph(p->stream, [p]() { return p->enqueue(p->G, p->stream); },
+                       &p->exec);
     if (rc) return rc;
   }
   return cuda_err(cudaStreamSynchronize(p->stream), "plan: sync");
@@ -120,39 +150,148 @@ int plan_advance(gbsgmc_plan* p, int g, cudaStream_t s) {
   return check_launch("plan: advance counter");
 }
 
+int capture_graph(cudaStream_t s, const std::function<int()>& body,
+                  cudaGraphExec_t* out, bool node_priority) {
+  int rc;
+  if ((rc = cuda_err(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                     "plan: begin capture")))
+    return rc;
+  rc = body();
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc != GBSGMC_OK) {
+    if (graph != nullptr) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if ((rc = cuda_err(e, "plan: end capture"))) return rc;
+  rc = cuda_err(cudaGraphInstantiate(
+                    out, graph,
+                    node_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
+                "plan: instantiate");
+  cudaGraphDestroy(graph);
+  return rc;
+}
+
 namespace {
 
 }  // namespace
 }  // namespace gbsgmc
+
+// Index draws of the next g steps into buf ([g, chains, n]).
+int GlmPlan::draw(int g, int32_t* buf, cudaStream_t s) {
+  using namespace gbsgmc;
+  const int64_t cn = static_cast<int64_t>(chains) * n;
+  const int64_t rows = model.n_rows > 0 ? model.n_rows : model.n_obs;
+  if (isrc.pcg_dev != nullptr)
+    return gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows,
+                                   static_cast<int64_t>(g) * n, n, buf, n, cn,
+                                   status, s);
+  return launch_philox_index(isrc.index_seed, isrc.chain_base, chains, base, 0,
+                             g, n, rows, buf, n, cn, s);
+}
+
+// One launch running g steps from the index sets in buf, then the counter
+// advance.
+int GlmPlan::steps_launch(int g, int32_t* buf, cudaStream_t s) {
+  using namespace gbsgmc;
+  const int64_t cn = static_cast<int64_t>(chains) * n;
+  gbsgmc_sched s0 = sched;
+  s0.base_dev = base;
+  s0.offset = 0;
+  const int rc = glm_sgld_step(&model, chains, n, buf, n, w, v, alpha, lmbd, &s0,
+                               &noise, U, lk_var, samples, sample_lik, ws,
+                               ws_size, status, s, tune, g, cn);
+  if (rc != GBSGMC_OK) return rc;
+  return plan_advance(this, g, s);
+}
+
+int GlmPlan::pipelined_block(int parity, bool prefetch, cudaStream_t s) {
+  using namespace gbsgmc;
+  int32_t* cur = parity ? idx2 : idx;
+  int32_t* nxt = parity ? idx : idx2;
+  int rc;
+  if (prefetch) {
+    if ((rc = cuda_err(cudaEventRecord(e_fork, s), "plan: fork"))) return rc;
+    if ((rc = cuda_err(cudaStreamWaitEvent(side, e_fork, 0), "plan: fork"))) return rc;
+    if ((rc = draw(G, nxt, side))) return rc;
+    if ((rc = cuda_err(cudaEventRecord(e_join, side), "plan: join"))) return rc;
+  }
+  if ((rc = steps_launch(G, cur, s))) return rc;
+  if (prefetch && (rc = cuda_err(cudaStreamWaitEvent(s, e_join, 0), "plan: join")))
+    return rc;
+  return GBSGMC_OK;
+}
+
+int GlmPlan::setup_pipeline() {
+  using namespace gbsgmc;
+  int rc;
+  const size_t bytes = sizeof(int32_t) * static_cast<size_t>(G) * chains * n;
+  if ((rc = cuda_err(cudaMalloc(&idx2, bytes), "plan_create: index buffer"))) return rc;
+  // The block's launch runs at the greatest stream priority and the draws at
+  // the least, so that the launch gets its CTAs onto the SMs first and the
+  // draws fill the room it leaves.
+  int least = 0, greatest = 0;
+  if ((rc = cuda_err(cudaDeviceGetStreamPriorityRange(&least, &greatest),
+                     "plan: priorities")))
+    return rc;
+  if ((rc = cuda_err(cudaStreamSynchronize(stream), "plan: sync"))) return rc;
+  if ((rc = cuda_err(cudaStreamDestroy(stream), "plan: stream"))) return rc;
+  stream = nullptr;
+  if ((rc = cuda_err(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking,
+                                                  greatest),
+                     "plan: stream")))
+    return rc;
+  if ((rc = cuda_err(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, least),
+                     "plan: stream")))
+    return rc;
+  if ((rc = cuda_err(cudaEventCreateWithFlags(&e_fork, cudaEventDisableTiming),
+                     "plan: event")))
+    return rc;
+  if ((rc = cuda_err(cudaEventCreateWithFlags(&e_join, cudaEventDisableTiming),
+                     "plan: event")))
+    return rc;
+  if (use_graph) {
+    for (int par = 0; par < 2; ++par) {
+      rc = capture_graph(stream, [this, par]() { return pipelined_block(par, true, stream); },
+                         &g_pref[par], true);
+      if (rc) return rc;
+      rc = capture_graph(stream, [this, par]() { return pipelined_block(par, false, stream); },
+                         &g_last[par], true);
+      if (rc) return rc;
+    }
+  }
+  pipelined = true;
+  return GBSGMC_OK;
+}
+
+int GlmPlan::run_blocks(int64_t full, int rem) {
+  using namespace gbsgmc;
+  if (!pipelined) return gbsgmc_plan::run_blocks(full, rem);
+  int rc;
+  if (full > 0 && (rc = draw(G, idx, stream))) return rc;
+  for (int64_t b = 0; b < full; ++b) {
+    const int par = static_cast<int>(b & 1);
+    const bool pref = b + 1 < full;
+    if (use_graph) {
+      if ((rc = cuda_err(cudaGraphLaunch(pref ? g_pref[par] : g_last[par], stream),
+                         "plan_run: graph")))
+        return rc;
+    } else if ((rc = pipelined_block(par, pref, stream))) {
+      return rc;
+    }
+  }
+  if (rem > 0 && (rc = enqueue(rem, stream))) return rc;
+  return GBSGMC_OK;
+}
 
 int GlmPlan::enqueue(int g, cudaStream_t s) {
   using namespace gbsgmc;
   int rc;
   GlmPlan* p = this;
   const int64_t cn = static_cast<int64_t>(p->chains) * p->n;
-  const int64_t rows = p->model.n_rows > 0 ? p->model.n_rows : p->model.n_obs;
-  if (p->isrc.pcg_dev != nullptr) {
-    rc = gbsgmc_index_draw_pcg64(p->isrc.pcg_dev, p->chains, rows,
-                                 static_cast<int64_t>(g) * p->n, p->n, p->idx,
-                                 p->n, cn, p->status, s);
-  } else {
-    rc = launch_philox_index(p->isrc.index_seed, p->isrc.chain_base, p->chains,
-                             p->base, 0, g, p->n, rows, p->idx, p->n,
-                             cn, s);
-  }
-  if (rc != GBSGMC_OK) return rc;
-  if (p->tune.multistep) {
-    // One launch for the g steps: each CTA runs its chain's steps in turn.
-    gbsgmc_sched s0 = p->sched;
-    s0.base_dev = p->base;
-    s0.offset = 0;
-    rc = glm_sgld_step(&p->model, p->chains, p->n, p->idx, p->n, p->w, p->v,
-                       p->alpha, p->lmbd, &s0, &p->noise, p->U, p->lk_var,
-                       p->samples, p->sample_lik, p->ws, p->ws_size, p->status,
-                       s, p->tune, g, cn);
-    if (rc != GBSGMC_OK) return rc;
-    return plan_advance(p, g, s);
-  }
+  if ((rc = draw(g, p->idx, s))) return rc;
+  // One launch for the g steps: each CTA runs its chain's steps in turn.
+  if (p->tune.multistep) return steps_launch(g, p->idx, s);
   for (int j = 0; j < g; ++j) {
     gbsgmc_sched sj = p->sched;
     sj.base_dev = p->base;
@@ -368,7 +507,15 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
     // launch per step, whatever the autotuner chose.
     if (const char* ms = std::getenv("GBSGMC_GLM_MULTISTEP"))
       if (ms[0] == '0' || ms[0] == '1') p->tune.multistep = ms[0] == '1';
-    rc = plan_capture(p);
+    if ((rc = plan_capture(p))) break;
+    // GBSGMC_PLAN_PIPELINE=1 overlaps the next block's index draws with this
+    // block's launch when the block is one launch and the draws carry state
+    // (PCG64 streams).  Off by default: on the 256-chain logistic workload
+    // the overlapped draws slowed the block more than they saved.
+    const char* pe = std::getenv("GBSGMC_PLAN_PIPELINE");
+    const bool pipe_ok = pe != nullptr && pe[0] == '1';
+    if (pipe_ok && p->tune.multistep && p->isrc.pcg_dev != nullptr)
+      rc = p->setup_pipeline();
   } while (false);
   if (rc != GBSGMC_OK) {
     delete p;
@@ -397,15 +544,7 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
   if ((rc = check_launch("plan_run: set counter"))) return rc;
   const int64_t full = steps / p->G;
   const int rem = static_cast<int>(steps % p->G);
-  for (int64_t b = 0; b < full; ++b) {
-    if (p->use_graph) {
-      if ((rc = cuda_err(cudaGraphLaunch(p->exec, p->stream), "plan_run: graph")))
-        return rc;
-    } else if ((rc = p->enqueue(p->G, p->stream))) {
-      return rc;
-    }
-  }
-  if (rem > 0 && (rc = p->enqueue(rem, p->stream))) return rc;
+  if ((rc = p->run_blocks(full, rem))) return rc;
   if ((rc = cuda_err(cudaEventRecord(p->ev_out, p->stream), "plan_run: record")))
     return rc;
   return cuda_err(cudaStreamWaitEvent(us, p->ev_out, 0), "plan_run: wait");

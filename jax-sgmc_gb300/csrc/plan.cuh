@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
+
 #include "internal.h"
 
 struct gbsgmc_plan {
@@ -21,6 +23,10 @@ struct gbsgmc_plan {
   virtual int64_t launches_per_block(int g) const = 0;
   // plan_run's first step and step count must be multiples of this.
   virtual int step_multiple() const { return 1; }
+  // Runs `full` blocks of G steps, then `rem` steps, on the plan's stream
+  // (after plan_run has set the counter).  The default replays the captured
+  // block and enqueues the remainder directly.
+  virtual int run_blocks(int64_t full, int rem);
 
   int G = 0;
   bool use_graph = true;
@@ -40,5 +46,10 @@ int plan_init(gbsgmc_plan* p, int G);
 int plan_capture(gbsgmc_plan* p);
 // Enqueues the one-thread launch that advances the counter by g.
 int plan_advance(gbsgmc_plan* p, int g, cudaStream_t s);
+// Captures what body() enqueues on s (and on streams it forks from s) into
+// an executable graph; node_priority keeps the capturing streams' priorities
+// on the kernel nodes.
+int capture_graph(cudaStream_t s, const std::function<int()>& body,
+                  cudaGraphExec_t* out, bool node_priority = false);
 
 }  // namespace gbsgmc

@@ -6,10 +6,11 @@
 //   interval"): x = next_uint32(); m = x * N; accept when (m mod 2^32) >=
 //   2^32 mod N, the index being m >> 32.  next_uint32 hands out the low half
 //   of a fresh PCG64 output and keeps the high half for the next call.  The
-//   accept test depends only on the 32-bit value, so a CTA expands 256 PCG64
-//   outputs at once by LCG jump-ahead (Brown 1994, "Random number generation
-//   with arbitrary strides"), tests the 512 halves, and compacts the accepted
-//   ones with a block scan.  The chain's stream state (128-bit LCG state,
+//   accept test depends only on the 32-bit value, so a CTA expands 2048 PCG64
+//   outputs at once (each thread jumps ahead to its own 8 consecutive steps
+//   by LCG jump-ahead, Brown 1994, "Random number generation with arbitrary
+//   strides"), tests the 4096 halves, and compacts the accepted ones with a
+//   block scan.  The chain's stream state (128-bit LCG state,
 //   buffered half) is advanced exactly as numpy advances it.
 // * gbsgmc_index_draw_philox and gbsgmc_philox_normal use Philox4x32-10.
 #include "common.cuh"
@@ -18,6 +19,8 @@ namespace gbsgmc {
 namespace {
 
 constexpr int kDrawThreads = 256;
+constexpr int kDrawPerThread = 8;   // consecutive LCG outputs per thread per round
+constexpr int kDrawLog2Round = 11;  // log2(kDrawThreads * kDrawPerThread)
 
 // Block-wide exclusive scan of small non-negative ints; returns the exclusive
 // prefix and sets *total.  Contains __syncthreads.
@@ -48,7 +51,8 @@ __global__ void __launch_bounds__(kDrawThreads)
     pcg64_draw_kernel(gbsgmc_pcg64* states, int64_t n_obs, int64_t draws,
                       int per_step, int32_t* idx, int64_t chain_stride,
                       int64_t step_stride) {
-  __shared__ Affine pow2[9];  // the LCG map applied 1, 2, 4, ..., 256 times
+  // The LCG map applied 1, 2, 4, ..., 2^kDrawLog2Round times.
+  __shared__ Affine pow2[kDrawLog2Round + 1];
   __shared__ int warp_tot[kDrawThreads / 32];
 
   const int c = blockIdx.x;
@@ -75,17 +79,20 @@ __global__ void __launch_bounds__(kDrawThreads)
   if (t == 0) {
     pow2[0].a = pcg_multiplier();
     pow2[0].c = inc;
-    for (int i = 1; i < 9; ++i) pow2[i] = compose(pow2[i - 1], pow2[i - 1]);
+    for (int i = 1; i <= kDrawLog2Round; ++i) pow2[i] = compose(pow2[i - 1], pow2[i - 1]);
   }
   __syncthreads();
-  // This thread's output is the (t+1)-th LCG step of the round.
+  // A round is kDrawThreads * kDrawPerThread LCG steps; this thread's
+  // outputs are steps t*K + 1 .. t*K + K of the round (K = kDrawPerThread),
+  // so the thread order of the scan is the stream order.
   Affine jump{U128{0, 1}, U128{0, 0}};
   {
-    const int k = t + 1;
-    for (int i = 0; i < 9; ++i)
+    const int k = t * kDrawPerThread + 1;
+    for (int i = 0; i <= kDrawLog2Round; ++i)
       if ((k >> i) & 1) jump = compose(jump, pow2[i]);
   }
-  const Affine round_jump = pow2[8];
+  const Affine step1 = pow2[0];
+  const Affine round_jump = pow2[kDrawLog2Round];
 
   int64_t produced = 0;
   if (has) {  // the half buffered by the previous call comes first
@@ -103,27 +110,70 @@ __global__ void __launch_bounds__(kDrawThreads)
   }
 
   for (;;) {
-    const U128 sj = apply(jump, s);
-    const uint64_t o = pcg_output(sj);
-    const uint32_t lo = static_cast<uint32_t>(o);
-    const uint32_t hi = static_cast<uint32_t>(o >> 32);
-    const int a0 = static_cast<uint32_t>(lo * N) >= threshold ? 1 : 0;
-    const int a1 = static_cast<uint32_t>(hi * N) >= threshold ? 1 : 0;
-    const int cnt = a0 + a1;
+    U128 sj[kDrawPerThread];
+    uint32_t lo[kDrawPerThread], hi[kDrawPerThread];
+    unsigned acc = 0;  // bit 2i: low half i accepted, bit 2i+1: high half i
+    int cnt = 0;
+#pragma unroll
+    for (int i = 0; i < kDrawPerThread; ++i) {
+      sj[i] = i == 0 ? apply(jump, s) : apply(step1, sj[i - 1]);
+      const uint64_t o = pcg_output(sj[i]);
+      lo[i] = static_cast<uint32_t>(o);
+      hi[i] = static_cast<uint32_t>(o >> 32);
+      const unsigned a0 = static_cast<uint32_t>(lo[i] * N) >= threshold ? 1u : 0u;
+      const unsigned a1 = static_cast<uint32_t>(hi[i] * N) >= threshold ? 1u : 0u;
+      acc |= (a0 << (2 * i)) | (a1 << (2 * i + 1));
+      cnt += static_cast<int>(a0 + a1);
+    }
     int total;
     const int excl = block_excl_scan(cnt, warp_tot, &total);
-    const int64_t base = produced + excl;
-    if (a0 && base < draws) put(base, static_cast<int32_t>((lo * N) >> 32));
-    if (a1 && base + a0 < draws)
-      put(base + a0, static_cast<int32_t>((hi * N) >> 32));
+    // Output position pos = q * per_step + r, advanced without divisions.
+    int64_t pos = produced + excl;
+    int64_t q = pos / per_step;
+    int r = static_cast<int>(pos - q * per_step);
+    int32_t* dst = out + q * step_stride;
+#pragma unroll
+    for (int i = 0; i < kDrawPerThread; ++i) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if ((acc >> (2 * i + h)) & 1u) {
+          const uint32_t v = h ? hi[i] : lo[i];
+          if (pos < draws) dst[r] = static_cast<int32_t>((v * N) >> 32);
+          ++pos;
+          if (++r == per_step) {
+            r = 0;
+            dst += step_stride;
+          }
+        }
+      }
+    }
     if (produced + total >= draws) {
-      const int64_t r = draws - 1 - produced;  // rank of the last value used
-      if (cnt > 0 && r >= excl && r < excl + cnt) {
-        const bool last_is_low = a0 && r == excl;
-        st->state_hi = sj.hi;
-        st->state_lo = sj.lo;
-        st->has_uint32 = last_is_low ? 1u : 0u;
-        st->uinteger = hi;
+      // The thread holding the last value used stores the stream state after
+      // its output, and buffers the high half if the low half was the last.
+      const int64_t last = draws - 1 - produced;  // rank of the last value used
+      if (cnt > 0 && last >= excl && last < excl + cnt) {
+        int64_t rank = excl;
+#pragma unroll
+        for (int i = 0; i < kDrawPerThread; ++i) {
+          if ((acc >> (2 * i)) & 1u) {
+            if (rank == last) {
+              st->state_hi = sj[i].hi;
+              st->state_lo = sj[i].lo;
+              st->has_uint32 = 1u;
+              st->uinteger = hi[i];
+            }
+            ++rank;
+          }
+          if ((acc >> (2 * i + 1)) & 1u) {
+            if (rank == last) {
+              st->state_hi = sj[i].hi;
+              st->state_lo = sj[i].lo;
+              st->has_uint32 = 0u;
+              st->uinteger = hi[i];
+            }
+            ++rank;
+          }
+        }
       }
       return;
     }

@@ -411,6 +411,10 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
     V, alpha, lmbd = None, 0.9, 1e-5
   h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
   block = min(rbf.cached_batches_count, DEFAULT_BLOCK_STEPS, max(iterations, 1))
+  outbuf = None
+  if saving is not None and saving.kind != "device":
+    outbuf = io.HostBuffers([((len(states), n_kept, W.shape[1]), np.float32),
+                           ((len(states), n_kept), np.float64)])
   res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,
                      n_kept, index_src, noise_seed=states[0].key,
                      chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,
@@ -425,4 +429,5 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
   return io.postprocess_chains(saving or io.no_save(), n_kept, res.samples,
                                [s.treedef for s in states],
                                {"likelihood": res.sample_lik},
-                               [s.model_state for s in states])
+                               [s.model_state for s in states],
+                               host=None if outbuf is None else outbuf.get())

@@ -13,6 +13,7 @@ returns device tensors.
 
 from __future__ import annotations
 
+import threading
 from pathlib import Path
 from typing import Any, NamedTuple
 
@@ -89,19 +90,54 @@ def postprocess(saving: Saving, count: int, variables, treedef, extras: dict,
   return {"sample_count": count, "samples": samples}
 
 
+class HostBuffers:
+  """Host arrays whose pages a background thread touches while the GPU
+  runs, so that the final device-to-host copy does not pay the page faults
+  of fresh memory (most of its cost for a few hundred MB)."""
+
+  def __init__(self, specs):
+    self._specs = list(specs)
+    self._arrays = None
+    self._thread = threading.Thread(target=self._fill, daemon=True)
+    self._thread.start()
+
+  def _fill(self):
+    out = []
+    for shape, dtype in self._specs:
+      a = np.empty(shape, dtype)
+      if a.size:
+        a.reshape(-1).view(np.uint8)[::4096] = 0
+      out.append(a)
+    self._arrays = out
+
+  def get(self):
+    self._thread.join()
+    return self._arrays
+
+
 def postprocess_chains(saving: Saving, count: int, variables, treedefs,
-                       extras: dict, model_states) -> list:
+                       extras: dict, model_states, host=None) -> list:
   """Result dicts of C chains from a ``[count, C, P]`` device buffer (extras
   ``[count, C]``).  With host saving, the buffers of all chains are
   transposed chain-major on the device and copied to the host at once, and
-  each chain's arrays are views of that copy."""
+  each chain's arrays are views of that copy.  ``host`` optionally gives the
+  destination arrays (``[C, count, P]``, then one ``[C, count]`` per extra,
+  e.g. from :class:`HostBuffers`)."""
+  import torch
   C = variables.shape[1]
   if saving is None or saving.kind == "device":
     return [postprocess(saving, count, variables[:, c], treedefs[c],
                         {k: v[:, c] for k, v in extras.items()},
                         model_states[c]) for c in range(C)]
-  host = variables.permute(1, 0, 2).contiguous().cpu().numpy()
-  hext = {k: v.t().contiguous().cpu().numpy() for k, v in extras.items()}
+  if host is None:
+    host = [np.empty((C, count, variables.shape[2]), np.float32)]
+    host += [np.empty((C, count), np.float64) for _ in extras]
+  torch.from_numpy(host[0]).copy_(variables.permute(1, 0, 2).contiguous())
+  hext = {}
+  for (k, v), h in zip(extras.items(), host[1:]):
+    torch.from_numpy(h).copy_(v.t().contiguous())
+    hext[k] = h
+  host = host[0]
   return [postprocess(saving, count, host[c], treedefs[c],
                       {k: v[c] for k, v in hext.items()}, model_states[c])
           for c in range(C)]

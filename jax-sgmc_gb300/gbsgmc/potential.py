@@ -87,8 +87,11 @@ class StochasticPotential:
     return self.is_mlp or self.is_cnn
 
   def model(self, dataset, observation_count=None):
-    """``gbsgmc_glm`` (or ``gbsgmc_mlp``) for a device dataset, targets
-    stored inline in the feature rows (DeviceDataset.glm_view)."""
+    """``gbsgmc_glm`` (or ``gbsgmc_mlp`` / ``gbsgmc_cnn``) for a device
+    dataset.  The GLM families read feature rows padded to 16 bytes and the
+    targets from their own vector (4 bytes per observation, small enough to
+    stay in L2 while the rows stream past); the networks read targets stored
+    inline in the feature rows (DeviceDataset.glm_view)."""
     n_obs = dataset.observation_count if observation_count is None \
         else observation_count
     if self.is_cnn:
@@ -110,16 +113,13 @@ class StochasticPotential:
                       int(dataset.observation_count), ld, X.data_ptr(), None,
                       float(lik.sigma), float(self.prior.scale),
                       float(self.temperature), 0), (X,)
-    if self.likelihood.y is None:
-      X, d, ld = dataset.matrix(self.likelihood.x)
-      inline = 0
-    else:
-      X, d, ld = dataset.glm_view(self.likelihood.x, self.likelihood.y)
-      inline = 1
+    X, d, ld = dataset.matrix(self.likelihood.x)
+    y = None if self.likelihood.y is None else dataset.vector(self.likelihood.y)
     return _lib.Glm(self.likelihood.family, d, int(n_obs), ld, X.data_ptr(),
-                    None, float(self.likelihood.sigma),
-                    float(self.prior.scale), float(self.temperature), inline,
-                    int(dataset.observation_count)), (X,)
+                    None if y is None else y.data_ptr(),
+                    float(self.likelihood.sigma), float(self.prior.scale),
+                    float(self.temperature), 0,
+                    int(dataset.observation_count)), (X, y)
 
   def dim(self, dataset) -> int:
     if self.is_network:

@@ -237,8 +237,10 @@ def test_multi_step_launch_equals_single_steps(lib, monkeypatch, slices, dyn):
 
 
 def test_multi_step_plan_matches_per_step_plan_and_oracle(lib, monkeypatch):
-  """A plan whose blocks run in one launch against the same plan with one
-  launch per step (bit for bit) and against the oracle trajectory."""
+  """A plan whose blocks run in one launch (with the next block's index
+  draws overlapped, or not) against the same plan with one launch per step
+  -- bit for bit, including the PCG64 stream states left behind -- and
+  against the oracle trajectory."""
   import torch
   from gbsgmc import data, engine
   monkeypatch.setenv("GBSGMC_AUTOTUNE", "0")
@@ -262,18 +264,30 @@ def test_multi_step_plan_matches_per_step_plan_and_oracle(lib, monkeypatch):
     return np.array([(s >> 64) & mk, s & mk, (inc >> 64) & mk, inc & mk, 0],
                     np.uint64).view(np.int64)
 
-  runs = []
-  for multi, block in (("1", 10), ("1", 45), ("0", 10)):
+  runs, streams = [], []
+  for multi, pipe, block in (("1", "1", 10), ("1", "0", 10), ("1", "1", 45),
+                             ("1", "1", 20), ("0", "1", 10)):
     monkeypatch.setenv("GBSGMC_GLM_MULTISTEP", multi)
+    monkeypatch.setenv("GBSGMC_PLAN_PIPELINE", pipe)
     pcg = cuda(np.stack([words(c) for c in range(C)]))
     runs.append(engine.run_sgld_glm(pot, loader.device_dataset(), cuda(W0),
                                     cuda(V0), n, K, h, T, keep,
                                     int((keep >= 0).sum()),
                                     engine.IndexSource(pcg=pcg), noise_seed=11,
                                     block_steps=block))
-  for r in runs[1:]:
+    streams.append(pcg)
+  for r, pcg in zip(runs[1:], streams[1:]):
     assert torch.equal(r.w, runs[0].w) and torch.equal(r.U, runs[0].U)
     assert torch.equal(r.samples, runs[0].samples)
+    assert torch.equal(pcg, streams[0])
+  # The streams advanced by exactly K steps of draws, as numpy's would.
+  for c in range(C):
+    rng = O.loader_rng(c)
+    O.loader_draws(rng, N, n, K)
+    st = rng.bit_generator.state
+    mk = (1 << 64) - 1
+    got = streams[0][c].cpu().numpy().view(np.uint64)
+    assert (int(got[0]) << 64) | int(got[1]) == st["state"]["state"]
   idx = np.stack([O.loader_draws(O.loader_rng(c), N, n, K) for c in range(C)], 1)
   xi = np.stack([[O.philox_normals(11, c, k, 0, d) for c in range(C)]
                  for k in range(K)]).astype(np.float32)

@@ -66,8 +66,11 @@ def test_pcg64_draws_match_golden(lib):
         np.testing.assert_array_equal(st[0], want, err_msg=key)
 
 
-@pytest.mark.parametrize("N", [1, 2, 3, 7, 1000, 999_983, 2**31 - 1])
-@pytest.mark.parametrize("draws", [1, 2, 3, 511, 512, 513, 5000])
+# Draw counts around the kernel's rounds of 2048 halves; N = 1,431,655,766
+# rejects a third of all 32-bit values (2^32 mod N = 1,431,655,764).
+@pytest.mark.parametrize("N", [1, 2, 3, 7, 1000, 999_983, 1_431_655_766, 2**31 - 1])
+@pytest.mark.parametrize("draws", [1, 2, 3, 511, 512, 513, 2047, 2048, 2049, 5000,
+                                   20_000])
 def test_pcg64_many_chains_edge_sizes(lib, N, draws):
   C = 5
   rngs = [O.loader_rng(100 + c) for c in range(C)]
