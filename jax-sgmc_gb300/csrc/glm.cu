@@ -13,10 +13,11 @@
 //     so the link function runs once per row, not 32 times;
 //   * the RW coefficients are broadcast back and acc += coef * x accumulates
 //     the gradient from the rows still held in registers.
-// The dataset stores the target at column d of each feature row (y_inline),
-// in the same sectors as the row, so no separate scattered gather of y is
-// needed.  (Staging rows through shared memory with one cp.async.bulk per
-// 1 KB row was measured slower: per-request cost held it near 13 GB/s per SM.)
+// The target comes either from its own vector (the layout the Python
+// package uploads: 4 bytes per observation, small enough to stay in L2 while
+// the rows stream past) or from column d of the feature row (y_inline).
+// (Staging rows through shared memory with one cp.async.bulk per 1 KB row
+// was measured slower: per-request cost held it near 13 GB/s per SM.)
 // The warp partials are reduced through shared memory in a fixed order.  With
 // several slices per chain, each CTA writes its partial gradient and partial
 // sums to the workspace and the last CTA of the chain to finish (ticket
@@ -88,7 +89,6 @@ struct GlmArgs {
   int dyn_fixed;      // 1: dynamically scheduled kernel, -1: not, 0: library choice
   int* status;
   int vec4;   // rows are 16-byte aligned: 128-bit loads
-  int l2_hints;  // rows evict-first, separate targets evict-last in L2
 };
 
 struct SmemLayout {
@@ -163,34 +163,6 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
-// The same loads with an L2 eviction-priority policy (createpolicy): rows
-// are streamed once and should leave L2 first; a separate target array is
-// small and gathered by every chain, so it should stay.
-__device__ __forceinline__ uint64_t l2_policy_evict_first() {
-  uint64_t p;
-  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_evict_last() {
-  uint64_t p;
-  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ float4 ld_row4_hint(const float* p, uint64_t pol) {
-  float4 v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-      : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ float ld_row1_hint(const float* p, uint64_t pol) {
-  float v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;"
-      : "=f"(v)
-      : "l"(p), "l"(pol));
-  return v;
-}
-
 template <int RW>
 struct Log2;
 template <>
@@ -242,8 +214,7 @@ __device__ __forceinline__ void load_tile(const GlmArgs& a, const int32_t* idx_s
       const int q = lane + 32 * k;
       if (o >= 0 && q < a.dq) {
         if (a.vec4) {
-          xv[r][k] = a.l2_hints ? ld_row4_hint(row + 4 * q, l2_policy_evict_first())
-                                : ld_row4(row + 4 * q);
+          xv[r][k] = ld_row4(row + 4 * q);
         } else {
           const int j = 4 * q;
           xv[r][k].x = ld_row1(row + j);
@@ -262,8 +233,7 @@ __device__ __forceinline__ void load_tile(const GlmArgs& a, const int32_t* idx_s
     if (a.y_inline) {
       yv = ld_row1(a.X + static_cast<int64_t>(og) * a.ld + a.d);
     } else if (a.y != nullptr) {
-      yv = a.l2_hints ? ld_row1_hint(a.y + og, l2_policy_evict_last())
-                      : ld_row1(a.y + og);
+      yv = ld_row1(a.y + og);
     }
   }
 }
@@ -1284,7 +1254,6 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.status = status;
   // 128-bit row loads need every row 16-byte aligned.
   a.vec4 = (reinterpret_cast<uintptr_t>(m->X) % 16 == 0) && (m->ld % 4 == 0) ? 1 : 0;
-  a.l2_hints = env_int("GBSGMC_GLM_L2HINT", 0) > 0 ? 1 : 0;
   a.lk = nullptr;
   a.lk_var = nullptr;
   a.grad = nullptr;
