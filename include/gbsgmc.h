@@ -562,6 +562,19 @@ int gbsgmc_cnn_plan_create(gbsgmc_plan** plan, const gbsgmc_cnn* model,
                            double* lk_var_dev, double* ke_dev, int block_steps,
                            int* status_dev);
 
+/* As gbsgmc_mlp_plan_create for the generalised-linear families (P = d):
+ * per step gbsgmc_glm_value_and_grad over all chains and the integrator's
+ * updates.  Meant for OBABO and SGHMC; SGLD on these families has its own
+ * fused step (gbsgmc_sgld_glm_plan_create), in which the update runs inside
+ * the likelihood kernel. */
+int gbsgmc_glm_plan_create(gbsgmc_plan** plan, const gbsgmc_glm* model,
+                           int chains, int n, const gbsgmc_integrator* integrator,
+                           float* x_dev, float* aux_dev,
+                           const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                           const gbsgmc_index_src* index_src, double* U_dev,
+                           double* lk_var_dev, double* ke_dev, int block_steps,
+                           int* status_dev);
+
 /* Tempering of a network plan: replica r of R runs at the schedule's
  * temperature times chain_temperature_dev[r] (set in the plan's sched), and
  * every `every` steps adjacent replicas attempt an exchange

@@ -1,5 +1,6 @@
-// Plans over the network likelihoods: many chains of SGLD(+RMSprop), OBABO
-// or SGHMC stepped together, one CUDA graph per block of steps.
+// Plans over the network likelihoods (and the GLM families for OBABO and
+// SGHMC): many chains of SGLD(+RMSprop), OBABO or SGHMC stepped together, one
+// CUDA graph per block of steps.
 //
 // Per step: index draw(s) for all chains (one per minibatch the integrator
 // consumes), the batched value-and-gradient of the network over all chains,
@@ -505,6 +506,72 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
       return gbsgmc_mlp_value_and_grad_ragged(&m, replicas, n_max, n_dev, idx, stride, nullptr,
                                               x, U, grad, nullptr, var, wsp, ws, status_dev,
                                               s);
+    };
+    rc = plan_capture(p);
+  } while (false);
+  if (rc != GBSGMC_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return GBSGMC_OK;
+}
+
+extern "C" int gbsgmc_glm_plan_create(gbsgmc_plan** out, const gbsgmc_glm* model,
+                                      int chains, int n, const gbsgmc_integrator* integ,
+                                      float* x_dev, float* aux_dev,
+                                      const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                                      const gbsgmc_index_src* isrc, double* U_dev,
+                                      double* lk_var_dev, double* ke_dev, int block_steps,
+                                      int* status_dev) {
+  if (out == nullptr) return set_error(GBSGMC_ERR_ARG, "glm_plan_create: null plan");
+  *out = nullptr;
+  int rc = check_common(integ, chains, n, x_dev, aux_dev, sched, noise, isrc, U_dev,
+                        block_steps, status_dev);
+  if (rc != GBSGMC_OK) return rc;
+  if (model == nullptr) return set_error(GBSGMC_ERR_ARG, "glm_plan_create: null model");
+  const size_t ws = gbsgmc_glm_workspace_bytes(chains, n, model->d);
+  if (ws == 0) return set_error(GBSGMC_ERR_SHAPE, "glm_plan_create: bad shape");
+  NetPlan* p = new (std::nothrow) NetPlan();
+  if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "glm_plan_create: out of memory");
+  p->chains = chains;
+  p->n = n;
+  p->P = model->d;
+  p->rows = model->n_rows > 0 ? model->n_rows : model->n_obs;
+  p->integ = *integ;
+  p->x = x_dev;
+  p->aux = aux_dev;
+  p->sched = *sched;
+  p->noise = *noise;
+  p->isrc = *isrc;
+  p->U = U_dev;
+  p->lk_var = lk_var_dev;
+  p->ke = ke_dev;
+  p->status = status_dev;
+  p->ws_size = ws;
+  do {
+    if ((rc = plan_init(p, block_steps))) break;
+    const size_t gbytes = sizeof(float) * static_cast<size_t>(chains) * p->P;
+    const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
+                          p->draws() * n;
+    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "glm_plan_create: gradient"))) break;
+    if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "glm_plan_create: U")))
+      break;
+    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "glm_plan_create: index buffer"))) break;
+    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "glm_plan_create: workspace"))) break;
+    // The GLM workspace's tickets start at zero and are left at zero.
+    if ((rc = cuda_err(cudaMemsetAsync(p->ws, 0, ws, p->stream), "glm_plan_create: memset")))
+      break;
+    if ((rc = glm_prepare())) break;
+    const gbsgmc_glm m = *model;
+    float* grad = p->grad;
+    void* wsp = p->ws;
+    const float* x = x_dev;
+    p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
+                     const int32_t* idx, int64_t stride, double* U, double* var,
+                     cudaStream_t s) {
+      return gbsgmc_glm_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
+                                       nullptr, var, wsp, ws, status_dev, s);
     };
     rc = plan_capture(p);
   } while (false);

@@ -174,6 +174,9 @@ SIGNATURES = {
     "gbsgmc_cnn_plan_create": (_i, [_P(_vp), _P(Cnn), _i, _i, _P(Integrator),
                                     _vp, _vp, _P(Sched), _P(Noise),
                                     _P(IndexSrc), _vp, _vp, _vp, _i, _vp]),
+    "gbsgmc_glm_plan_create": (_i, [_P(_vp), _P(Glm), _i, _i, _P(Integrator),
+                                    _vp, _vp, _P(Sched), _P(Noise),
+                                    _P(IndexSrc), _vp, _vp, _vp, _i, _vp]),
     "gbsgmc_resgld_sa_update": (_i, [_i, _vp, _vp, _vp, _vp]),
     "gbsgmc_resgld_exchange_adjacent": (_i, [_i, _i64, _vp, _vp, _vp, _vp,
                                              _P(Sched), _i, _vp, _d, _u64,

@@ -136,9 +136,10 @@ def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
 
 
 class NetPlan:
-  """Owns a network plan (``gbsgmc_mlp_plan_create`` or
-  ``gbsgmc_cnn_plan_create``): C chains of SGLD, OBABO or SGHMC on a network
-  potential, one CUDA graph per block of steps.  ``X`` [C, P] (positions) and ``AUX`` (rms_prop state, or momentum)
+  """Owns a network plan (``gbsgmc_mlp_plan_create``,
+  ``gbsgmc_cnn_plan_create``, or ``gbsgmc_glm_plan_create`` for the GLM
+  families): C chains of SGLD, OBABO or SGHMC, one CUDA graph per block of
+  steps.  ``X`` [C, P] (positions) and ``AUX`` (rms_prop state, or momentum)
   are updated in place."""
 
   KINDS = {"langevin": _lib.INTEGRATOR_SGLD, "obabo": _lib.INTEGRATOR_OBABO,
@@ -168,8 +169,12 @@ class NetPlan:
     self.integ = _lib.Integrator(self.KINDS[kind], lf, float(friction),
                                  float(alpha), float(lmbd), 0, _lib.ptr(mass))
     handle = _lib.C.c_void_p()
+    # Kernel launches of one value-and-gradient call.
+    self.launches_per_gradient = 30 if potential.is_cnn else \
+        10 if potential.is_mlp else 1
     create = "gbsgmc_cnn_plan_create" if potential.is_cnn else \
-        "gbsgmc_mlp_plan_create"
+        "gbsgmc_mlp_plan_create" if potential.is_mlp else \
+        "gbsgmc_glm_plan_create"
     _lib.call(create, _lib.C.byref(handle), self.model, C, n,
               self.integ, _lib.ptr(X), _lib.ptr(AUX), self.sched, self.noise,
               index_src.struct, _lib.ptr(self.U), _lib.ptr(self.lk_var),
@@ -183,7 +188,7 @@ class NetPlan:
   def launches(self, steps) -> int:
     """Kernel launches of ``steps`` steps (value-and-gradient kernels
     included)."""
-    per_grad = 10 if self.kind != "langevin" else 10
+    per_grad = self.launches_per_gradient
     grads = {"obabo": 2}.get(self.kind, 1) * int(steps)
     return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps))) + \
         per_grad * grads
@@ -275,9 +280,10 @@ class ResgldPlan:
 
 
 def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
-  """Runs sgmc chains of langevin_diffusion / obabo / friction_leapfrog on a
-  dense-network potential through one :class:`NetPlan`; returns None when
-  the chains do not qualify (the caller steps them one by one)."""
+  """Runs sgmc chains of langevin_diffusion / obabo / friction_leapfrog
+  through one :class:`NetPlan` (network potentials, and OBABO / SGHMC on the
+  GLM families, whose SGLD has its own fused step); returns None when the
+  chains do not qualify (the caller steps them one by one)."""
   import torch
   from .potential import StochasticPotential
   meta = getattr(solver, "meta", {})
@@ -290,7 +296,7 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
     return None
   pot = im.get("potential")
   bfn = im.get("batch_fn")
-  if not isinstance(pot, StochasticPotential) or not pot.is_network or not states:
+  if not isinstance(pot, StochasticPotential) or not states:
     return None
   if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn):
     return None

@@ -297,3 +297,51 @@ def test_multi_step_plan_matches_per_step_plan_and_oracle(lib, monkeypatch):
   kept = np.nonzero(keep >= 0)[0]
   np.testing.assert_allclose(runs[0].samples.cpu().numpy(), Ws[kept + 1],
                              rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.parametrize("kind", ["obabo", "sghmc"])
+def test_glm_obabo_sghmc_plan_equals_per_chain_steps(lib, monkeypatch, kind):
+  """OBABO and SGHMC chains on the logistic potential through one plan
+  (gbsgmc_glm_plan_create) against the per-chain step path.  With one CTA
+  per chain the GLM kernel's arithmetic for a chain does not depend on the
+  other chains, and both paths draw the same PCG64 indices and Philox
+  noise, so the samples agree bit for bit."""
+  from gbsgmc import alias, data, engine, likelihoods as L, potential
+  monkeypatch.setenv("GBSGMC_GLM_SLICES", "1")
+  monkeypatch.setenv("GBSGMC_GLM_RW", "4")
+  N, d, n, C = 3000, 24, 96, 3
+  X, y = _problem(N, d, O.LOGISTIC, seed=41)
+  pot = potential.minibatch_potential(L.GaussianPrior(2.0), L.Logistic())
+  common = dict(cache_size=32, batch_size=n, first_step_size=1e-3,
+                last_step_size=1e-4, burn_in=0, accepted_samples=4)
+  rng = np.random.default_rng(5)
+  inits = [{"w": (0.1 * rng.normal(size=d)).astype(np.float32)} for _ in range(C)]
+  made = []
+  real_init = engine.NetPlan.__init__
+
+  def spy(self, *args, **kwargs):
+    made.append(kind)
+    return real_init(self, *args, **kwargs)
+
+  monkeypatch.setattr(engine.NetPlan, "__init__", spy)
+  outs = []
+  for fused in (True, False):
+    # A fresh loader each time: its chains (index seeds, noise keys) are
+    # numbered in registration order.
+    loader = data.NumpyDataLoader(x=X, y=y)
+    if kind == "obabo":
+      r = alias.obabo(pot, loader, integration_steps=3, friction=5.0, **common)
+    else:
+      r = alias.sghmc(pot, loader, integration_steps=2, friction=0.5, **common)
+    engine.FUSED_ENABLED = fused
+    try:
+      outs.append(r(*inits, iterations=8))
+    finally:
+      engine.FUSED_ENABLED = True
+  assert made == [kind]   # the fused run went through one plan
+  for ra, rb in zip(*outs):
+    assert ra["sample_count"] == rb["sample_count"] == 4
+    va = np.asarray(ra["samples"]["variables"]["w"])
+    vb = np.asarray(rb["samples"]["variables"]["w"])
+    assert np.isfinite(va).all() and not np.array_equal(va[0], va[-1])
+    np.testing.assert_array_equal(va, vb)
