@@ -47,7 +47,7 @@ constexpr int kFlat = 4 * 4 * kC3;  // 2048
 constexpr int kK1 = 27, kK1p = 64;  // im2col widths (real, padded)
 constexpr int kK2 = 9 * kC1, kK2p = 320;
 constexpr int kK3 = 9 * kC2, kK3p = 576;
-constexpr int kA1ld = 64;  // conv1 output channels as stored (32 real)
+constexpr int kA1ld = 64;  // conv1 output-gradient channels as stored (32 real)
 
 // Offsets of the leaves in a chain's flat parameter vector.
 constexpr int64_t ob1 = 0, oW1 = ob1 + kC1, ob2 = oW1 + kK1 * kC1, oW2 = ob2 + kC2,
@@ -70,7 +70,6 @@ struct CnnLayout {
 };
 
 constexpr int kPrepBlocks = 64;  // Σw² partial sums per chain
-constexpr int kBiasChunks = 64;  // row chunks of the bias-gradient sums
 
 // Split-K factors of the weight-gradient GEMMs (K = pixels of n images:
 // 16n, 4n and n slices of 64 for the three layers; n is even).
@@ -91,7 +90,7 @@ CnnLayout cnn_layout(int chains, int n) {
   L.w2b = take(2 * kK2 * kC2);
   L.w3b = take(2 * kK3 * kC3);
   L.col1 = take(2 * N * 1024 * kK1p);
-  L.a1 = take(4 * N * 1024 * kA1ld);
+  L.a1 = take(4 * N * 1024 * kC1);
   L.dy1 = take(2 * N * 1024 * kA1ld);
   L.p1 = take(2 * N * 256 * kC1);
   L.col2 = take(2 * N * 256 * kK2p);
@@ -117,7 +116,10 @@ CnnLayout cnn_layout(int chains, int n) {
   part = std::max<size_t>(part, size_t(wsplit(2, n)) * kC2 * kK2);
   part = std::max<size_t>(part, size_t(wsplit(3, n)) * kC3 * kK3);
   L.part = take(4 * part);
-  L.bpart = take(4 * kBiasChunks * kC3);
+  // Bias partials: one per unpool block and channel, 8 pooled elements per
+  // thread and 256 threads per block: n*Ho*Wo*C / 2048 * C = 128 n floats
+  // for each of the three layers.
+  L.bpart = take(4 * 128 * N);
   L.total = off;
   return L;
 }
@@ -226,9 +228,12 @@ __global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// 2x2 max-pool: A [n, H, W, ld] (C real channels) -> P [n, H/2, W/2, C] and
-// the argmax (0..3, row-major in the window, first maximum) per output.
-// One thread per output element.  Grid (ceil(n*H*W*C/4 / 256), chains).
+// 2x2 max-pool: A [n, H, W, ld] (C real channels) -> P [n, H/2, W/2, C], and
+// per output the argmax (bits 0-1: 0..3, row-major in the window, first
+// maximum) and bit 2 = (maximum > 0), the ReLU mask of the element the
+// backward pass routes the gradient to.  One thread per output pixel and four
+// channels (128-bit loads of A, 64-bit stores of P, 32-bit of M); C and ld
+// are multiples of 4.  Grid (ceil(n*H*W*C/16 / 256), chains).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pout, uint8_t* M,
                                                       int n, int H, int W, int C, int ld) {
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pou
   const int c = blockIdx.y;
   const int Ho = H / 2, Wo = W / 2;
   const int per = n * Ho * Wo * C;
-  const int e = blockIdx.x * 256 + threadIdx.x;
+  const int e = (blockIdx.x * 256 + threadIdx.x) * 4;
   if (e >= per) return;
   const int ch = e % C;
   const int pix = e / C;
@@ -244,15 +249,28 @@ __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pou
   const int i = pix / (Wo * Ho);
   const float* src = A + static_cast<int64_t>(c) * n * H * W * ld +
                      ((i * H + 2 * y) * W + 2 * x) * ld + ch;
-  float best = src[0];
-  int arg = 0;
-  const float v1 = src[ld], v2 = src[static_cast<int64_t>(W) * ld],
-              v3 = src[static_cast<int64_t>(W) * ld + ld];
-  if (v1 > best) { best = v1; arg = 1; }
-  if (v2 > best) { best = v2; arg = 2; }
-  if (v3 > best) { best = v3; arg = 3; }
-  Pout[static_cast<int64_t>(c) * per + e] = __float2bfloat16_rn(best);
-  M[static_cast<int64_t>(c) * per + e] = static_cast<uint8_t>(arg);
+  const float4 w0 = *reinterpret_cast<const float4*>(src);
+  const float4 w1 = *reinterpret_cast<const float4*>(src + ld);
+  const float4 w2 = *reinterpret_cast<const float4*>(src + static_cast<int64_t>(W) * ld);
+  const float4 w3 = *reinterpret_cast<const float4*>(src + static_cast<int64_t>(W) * ld + ld);
+  const float a0[4] = {w0.x, w0.y, w0.z, w0.w}, a1[4] = {w1.x, w1.y, w1.z, w1.w};
+  const float a2[4] = {w2.x, w2.y, w2.z, w2.w}, a3[4] = {w3.x, w3.y, w3.z, w3.w};
+  __nv_bfloat162 out[2];
+  uint32_t marks = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float best = a0[k];
+    int arg = 0;
+    if (a1[k] > best) { best = a1[k]; arg = 1; }
+    if (a2[k] > best) { best = a2[k]; arg = 2; }
+    if (a3[k] > best) { best = a3[k]; arg = 3; }
+    marks |= static_cast<uint32_t>(arg | (best > 0.f ? 4 : 0)) << (8 * k);
+    const bf16 b = __float2bfloat16_rn(best);
+    if (k & 1) out[k >> 1].y = b; else out[k >> 1].x = b;
+  }
+  *reinterpret_cast<uint2*>(Pout + static_cast<int64_t>(c) * per + e) =
+      *reinterpret_cast<const uint2*>(out);
+  *reinterpret_cast<uint32_t*>(M + static_cast<int64_t>(c) * per + e) = marks;
 }
 
 // ---------------------------------------------------------------------------
@@ -393,85 +411,120 @@ __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Pool-window routing + ReLU mask: for each pooled element (i, py, px, ch)
-// of a layer with pre-pool activations A [n, H, W, ld] (C real channels),
+// Pool-window routing + ReLU mask: for each pooled element (i, py, px, ch),
 //   dP = dp[i, py, px, ch]                       (layer 3: fp32 dP3), or
 //   dP = sum over taps (kh, kw) of dCol[(i, py - kh + 1, px - kw + 1),
 //                                      (kh, kw, ch)]  (col2im of the next
 //        layer's input-gradient columns dCol [n*Ho*Wo, Kp])
-// goes to the window element its argmax chose, masked by A > 0; the three
-// others (and channels C..ld-1) get 0:  dY [n, H, W, ld] BF16.  One thread
-// per pooled element, 32-bit index arithmetic (per-chain counts < 2^31).
-// Grid (ceil(n*Ho*Wo*C / 256), chains).
+// goes to the window element its argmax chose if that element was positive
+// (the pool's mark byte, bits 0-1 and 2); the three others (and channels
+// C..ld-1) get 0:  dY [n, H, W, ld] BF16.  One thread per pooled pixel and
+// eight channels: 128-bit loads of dCol / dp, 64-bit of the marks, 128-bit
+// stores of dY; C, ld and Kp are multiples of 8.  32-bit index arithmetic
+// (per-chain counts < 2^31).  Grid (ceil(n*Ho*Wo*C/8 / 256), chains).
+// The bias gradient is the column sum of dY, i.e. the sum over pooled
+// elements of the routed (BF16-rounded) values: each block adds its threads'
+// values per channel in a fixed order and writes
+// bpart[(chain * gridDim.x + block) * C + ch]; cnn_bias_sum_kernel adds the
+// blocks.  2048 / C threads of a block share a channel group (256 * 8 is a
+// multiple of C, so the channel of thread t is 8 t mod C).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) cnn_unpool_kernel(const float* A, bf16* dY,
-                                                        const uint8_t* M, const float* dp,
-                                                        const bf16* dcol, int n, int H, int W,
-                                                        int C, int ld, int Kp) {
+__global__ void __launch_bounds__(256) cnn_unpool_kernel(bf16* dY, const uint8_t* M,
+                                                        const float* dp, const bf16* dcol,
+                                                        int n, int H, int W, int C, int ld,
+                                                        int Kp, float* bpart) {
+  __shared__ float red[256 * 8];
   const int c = blockIdx.y;
   const int Ho = H / 2, Wo = W / 2;
   const int pper = n * Ho * Wo * C;
-  const int e = blockIdx.x * 256 + threadIdx.x;
-  if (e >= pper) return;
+  const int e = (blockIdx.x * 256 + threadIdx.x) * 8;
+  const bool active = e < pper;
+  float bsum[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (active) {
   const int ch = e % C;
   const int pix = e / C;
   const int px = pix % Wo, py = (pix / Wo) % Ho, i = pix / (Wo * Ho);
-  float g;
+  float g[8];
   if (dp != nullptr) {
-    g = dp[static_cast<int64_t>(c) * pper + e];
+    const float4* d4 = reinterpret_cast<const float4*>(dp + static_cast<int64_t>(c) * pper + e);
+    const float4 u = d4[0], v = d4[1];
+    g[0] = u.x; g[1] = u.y; g[2] = u.z; g[3] = u.w;
+    g[4] = v.x; g[5] = v.y; g[6] = v.z; g[7] = v.w;
   } else {
     const bf16* dc = dcol + static_cast<int64_t>(c) * n * Ho * Wo * Kp;
-    g = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) g[k] = 0.f;
 #pragma unroll
     for (int kh = 0; kh < 3; ++kh)
 #pragma unroll
       for (int kw = 0; kw < 3; ++kw) {
         const int oy = py - kh + 1, ox = px - kw + 1;
-        if (oy >= 0 && oy < Ho && ox >= 0 && ox < Wo)
-          g += bf(dc[((i * Ho + oy) * Wo + ox) * Kp + (kh * 3 + kw) * C + ch]);
+        if (oy >= 0 && oy < Ho && ox >= 0 && ox < Wo) {
+          const uint4 t = *reinterpret_cast<const uint4*>(
+              dc + ((i * Ho + oy) * Wo + ox) * Kp + (kh * 3 + kw) * C + ch);
+          const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&t);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            g[2 * k] += __low2float(h[k]);
+            g[2 * k + 1] += __high2float(h[k]);
+          }
+        }
       }
   }
-  const int arg = M[static_cast<int64_t>(c) * pper + e];
+  const uint2 mk = *reinterpret_cast<const uint2*>(M + static_cast<int64_t>(c) * pper + e);
+  const uint32_t marks[2] = {mk.x, mk.y};
   const int64_t base = static_cast<int64_t>(c) * n * H * W * ld;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int y = 2 * py + (q >> 1), x = 2 * px + (q & 1);
     const int off = ((i * H + y) * W + x) * ld;
-    const float v = (q == arg && A[base + off + ch] > 0.f) ? g : 0.f;
-    dY[base + off + ch] = __float2bfloat16_rn(v);
-    for (int extra = C + ch; extra < ld; extra += C) dY[base + off + extra] = __float2bfloat16_rn(0.f);
+    __nv_bfloat162 o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t m0 = (marks[k >> 1] >> (16 * (k & 1))) & 0xffu;
+      const uint32_t m1 = (marks[k >> 1] >> (16 * (k & 1) + 8)) & 0xffu;
+      const float v0 = ((m0 & 3u) == static_cast<uint32_t>(q) && (m0 & 4u)) ? g[2 * k] : 0.f;
+      const float v1 = ((m1 & 3u) == static_cast<uint32_t>(q) && (m1 & 4u)) ? g[2 * k + 1] : 0.f;
+      o[k] = __floats2bfloat162_rn(v0, v1);
+      bsum[2 * k] += __low2float(o[k]);
+      bsum[2 * k + 1] += __high2float(o[k]);
+    }
+    *reinterpret_cast<uint4*>(dY + base + off + ch) = *reinterpret_cast<const uint4*>(o);
+    for (int extra = C + ch; extra < ld; extra += C)
+      *reinterpret_cast<uint4*>(dY + base + off + extra) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  }  // active
+#pragma unroll
+  for (int k = 0; k < 8; ++k) red[threadIdx.x * 8 + k] = bsum[k];
+  __syncthreads();
+  if (static_cast<int>(threadIdx.x) < C) {
+    const int t = threadIdx.x, group = t / 8, k = t % 8, groups = C / 8;
+    float s = 0.f;
+    for (int u = group; u < 256; u += groups) s += red[u * 8 + k];
+    bpart[(static_cast<int64_t>(c) * gridDim.x + blockIdx.x) * C + t] = s;
   }
 }
 
-// Bias gradients, pass 1: partial column sums of dY [rows, ld] (C real
-// channels) over kBiasChunks row chunks: thread t adds channel t % C of rows
-// t / C, t / C + 256 / C, ... of its chunk (coalesced along channels).
-// Grid (kBiasChunks, chains), 256 threads; C divides 256.
-__global__ void __launch_bounds__(256) cnn_bias_part_kernel(const bf16* dY, int rows, int ld,
-                                                           int C, float* bpart) {
+// Bias gradient: grad[off + ch] = sum over the unpool blocks' partials in a
+// fixed order: thread t adds channel t % C of blocks t / C, t / C + 256 / C,
+// ... (coalesced along channels, eight loads in flight), then the 256 / C
+// partial sums of a channel are added in order.  Grid (chains), 256 threads;
+// C divides 256.
+__global__ void __launch_bounds__(256) cnn_bias_sum_kernel(const float* bpart, int blocks,
+                                                           int C, float* grad, int64_t off) {
   __shared__ float acc[256];
-  const int c = blockIdx.y, t = threadIdx.x, ch = t % C, r0 = t / C, step = 256 / C;
-  const int per = (rows + kBiasChunks - 1) / kBiasChunks;
-  const int lo = blockIdx.x * per, hi = min(rows, lo + per);
-  const bf16* src = dY + static_cast<int64_t>(c) * rows * ld;
+  const int c = blockIdx.x, t = threadIdx.x, ch = t % C, g0 = t / C, step = 256 / C;
+  const float* p = bpart + static_cast<int64_t>(c) * blocks * C + ch;
   float s = 0.f;
-  for (int r = lo + r0; r < hi; r += step) s += bf(src[r * ld + ch]);
+#pragma unroll 8
+  for (int q = g0; q < blocks; q += step) s += p[static_cast<int64_t>(q) * C];
   acc[t] = s;
   __syncthreads();
   if (t < C) {
     float tot = 0.f;
-    for (int q = 0; q < step; ++q) tot += acc[q * C + t];
-    bpart[(static_cast<int64_t>(c) * kBiasChunks + blockIdx.x) * kC3 + t] = tot;
+    for (int u = 0; u < step; ++u) tot += acc[u * C + t];
+    grad[static_cast<int64_t>(c) * kP + off + t] = tot;
   }
-}
-
-// Pass 2: grad[off + ch] = sum over chunks.  Grid (chains), C threads.
-__global__ void cnn_bias_sum_kernel(const float* bpart, float* grad, int64_t off) {
-  const int c = blockIdx.x, ch = threadIdx.x;
-  float s = 0.f;
-  for (int q = 0; q < kBiasChunks; ++q)
-    s += bpart[(static_cast<int64_t>(c) * kBiasChunks + q) * kC3 + ch];
-  grad[static_cast<int64_t>(c) * kP + off + ch] = s;
 }
 
 // Split-K reduction of a weight gradient: grad[off + e] = sum_s part[c, s, e]
@@ -562,6 +615,7 @@ struct EpiConvRelu {
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
+    if (col0 >= ldo) return;  // columns past the stored width (warp-uniform)
     const float* bias = w + b * kP + boff;
     float* dst = y + (b * rows + row0) * ldo + col0 + epi::lane_id();
 #pragma unroll 1
@@ -671,12 +725,16 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   int rc;
   auto launched = [&](const char* what) { return check_launch(what); };
   // Bias gradient of a layer from its dY [rows, ld] (C real channels).
-  auto bias_grad = [&](const bf16* dY, int64_t rows, int ld, int Cr, int64_t off) {
-    cnn_bias_part_kernel<<<dim3(kBiasChunks, C), 256, 0, st>>>(dY, static_cast<int>(rows), ld,
-                                                               Cr, a.bpart);
-    int r = launched("cnn_bias_part_kernel");
+  // Unpool of a layer (pooled grid Ho x Wo, Cr channels) and its bias
+  // gradient from the unpool blocks' partials.
+  auto unpool = [&](bf16* dY, const uint8_t* M, const float* dp, const bf16* dcol, int H,
+                    int Cr, int ld, int Kp, int64_t off) {
+    const int blocks = grid1(int64_t(n) * (H / 2) * (H / 2) * Cr / 8);
+    cnn_unpool_kernel<<<dim3(blocks, C), 256, 0, st>>>(dY, M, dp, dcol, n, H, H, Cr, ld, Kp,
+                                                       a.bpart);
+    int r = launched("cnn_unpool_kernel");
     if (r) return r;
-    cnn_bias_sum_kernel<<<C, Cr, 0, st>>>(a.bpart, a.grad, off);
+    cnn_bias_sum_kernel<<<C, 256, 0, st>>>(a.bpart, blocks, Cr, a.grad, off);
     return launched("cnn_bias_sum_kernel");
   };
   // Weight gradient of a layer: split-K GEMM into partials, then their sum.
@@ -709,11 +767,13 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     return rc;
 
   // conv1 -> pool1 -> im2col2 -> conv2 -> pool2 -> im2col3 -> conv3 -> pool3.
-  const EpiConvRelu e1{a.w, ob1, kC1, kA1ld, r1, a.a1};
+  // conv1 runs as N = 64 (the weight map's zero fill beyond 32 channels);
+  // the epilogue stores the 32 real columns.
+  const EpiConvRelu e1{a.w, ob1, kC1, kC1, r1, a.a1};
   if ((rc = launch_gemm<64, false, true>(m_col1, m_w1, C, r1, 64, kK1p, a.status, e1, st)))
     return rc;
-  cnn_pool_kernel<<<dim3(grid1(r2 * kC1 / 1), C), 256, 0, st>>>(a.a1, a.p1, a.m1, n, 32, 32, kC1,
-                                                                kA1ld);
+  cnn_pool_kernel<<<dim3(grid1(r2 * kC1 / 4), C), 256, 0, st>>>(a.a1, a.p1, a.m1, n, 32, 32, kC1,
+                                                                kC1);
   if ((rc = launched("cnn_pool_kernel 1"))) return rc;
   cnn_im2col_kernel<<<dim3(grid1(r2 * kK2p / 8), C), 256, 0, st>>>(a.p1, a.col2, n, 16, 16, kC1,
                                                                    kK2p);
@@ -721,7 +781,8 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   const EpiConvRelu e2{a.w, ob2, kC2, kC2, r2, a.a2};
   if ((rc = launch_gemm<64, false, true>(m_col2, m_w2, C, r2, kC2, kK2p, a.status, e2, st)))
     return rc;
-  cnn_pool_kernel<<<dim3(grid1(r3 * kC2), C), 256, 0, st>>>(a.a2, a.p2, a.m2, n, 16, 16, kC2, kC2);
+  cnn_pool_kernel<<<dim3(grid1(r3 * kC2 / 4), C), 256, 0, st>>>(a.a2, a.p2, a.m2, n, 16, 16, kC2,
+                                                                kC2);
   if ((rc = launched("cnn_pool_kernel 2"))) return rc;
   cnn_im2col_kernel<<<dim3(grid1(r3 * kK3p / 8), C), 256, 0, st>>>(a.p2, a.col3, n, 8, 8, kC2,
                                                                    kK3p);
@@ -729,8 +790,8 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   const EpiConvRelu e3{a.w, ob3, kC3, kC3, r3, a.a3};
   if ((rc = launch_gemm<128, false, true>(m_col3, m_w3, C, r3, kC3, kK3p, a.status, e3, st)))
     return rc;
-  cnn_pool_kernel<<<dim3(grid1(int64_t(n) * 16 * kC3), C), 256, 0, st>>>(a.a3, a.p3, a.m3, n, 8,
-                                                                         8, kC3, kC3);
+  cnn_pool_kernel<<<dim3(grid1(int64_t(n) * 16 * kC3 / 4), C), 256, 0, st>>>(a.a3, a.p3, a.m3,
+                                                                             n, 8, 8, kC3, kC3);
   if ((rc = launched("cnn_pool_kernel 3"))) return rc;
   cnn_dense_kernel<<<dim3(n, C), 128, 0, st>>>(a);
   if ((rc = launched("cnn_dense_kernel"))) return rc;
@@ -739,10 +800,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     cnn_dense_grad_kernel<<<dim3(kFlat / 128 + 1, C), 128, 0, st>>>(a);
     if ((rc = launched("cnn_dense_grad_kernel"))) return rc;
     // Layer 3: dY3 over A3, db3, dW3 = dY3^T Col3, dCol3 = dY3 W3^T.
-    cnn_unpool_kernel<<<dim3(grid1(int64_t(n) * 16 * kC3), C), 256, 0, st>>>(
-        a.a3, a.dy3, a.m3, a.dp3, nullptr, n, 8, 8, kC3, kC3, 0);
-    if ((rc = launched("cnn_unpool_kernel 3"))) return rc;
-    if ((rc = bias_grad(a.dy3, r3, kC3, kC3, ob3))) return rc;
+    if ((rc = unpool(a.dy3, a.m3, a.dp3, nullptr, 8, kC3, kC3, 0, ob3))) return rc;
     CUtensorMap m_dy3t, m_col3t, m_dy3, m_w3k;
     if ((rc = make_tmap_bf16_3d(&m_dy3t, a.dy3, kC3, r3, C, kC3, r3 * kC3, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col3t, a.col3, kK3p, r3, C, kK3p, r3 * kK3p, 64, 64)) ||
@@ -754,11 +812,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     if ((rc = launch_gemm<64, false, false>(m_dy3, m_w3k, C, r3, kK3p, kC3, a.status, d3, st)))
       return rc;
     // Layer 2.
-    cnn_unpool_kernel<<<dim3(grid1(r3 * kC2), C), 256, 0, st>>>(a.a2, a.dy2, a.m2, nullptr,
-                                                                a.dcol3, n, 16, 16, kC2, kC2,
-                                                                kK3p);
-    if ((rc = launched("cnn_unpool_kernel 2"))) return rc;
-    if ((rc = bias_grad(a.dy2, r2, kC2, kC2, ob2))) return rc;
+    if ((rc = unpool(a.dy2, a.m2, nullptr, a.dcol3, 16, kC2, kC2, kK3p, ob2))) return rc;
     CUtensorMap m_dy2t, m_col2t, m_dy2, m_w2k;
     if ((rc = make_tmap_bf16_3d(&m_dy2t, a.dy2, kC2, r2, C, kC2, r2 * kC2, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col2t, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, 64, 64)) ||
@@ -770,11 +824,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     if ((rc = launch_gemm<64, false, false>(m_dy2, m_w2k, C, r2, kK2p, kC2, a.status, d2, st)))
       return rc;
     // Layer 1.
-    cnn_unpool_kernel<<<dim3(grid1(r2 * kC1), C), 256, 0, st>>>(a.a1, a.dy1, a.m1, nullptr,
-                                                                a.dcol2, n, 32, 32, kC1, kA1ld,
-                                                                kK2p);
-    if ((rc = launched("cnn_unpool_kernel 1"))) return rc;
-    if ((rc = bias_grad(a.dy1, r1, kA1ld, kC1, ob1))) return rc;
+    if ((rc = unpool(a.dy1, a.m1, nullptr, a.dcol2, 32, kC1, kA1ld, kK2p, ob1))) return rc;
     CUtensorMap m_dy1t, m_col1t;
     if ((rc = make_tmap_bf16_3d(&m_dy1t, a.dy1, kA1ld, r1, C, kA1ld, r1 * kA1ld, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col1t, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, 64, 64)))
