@@ -178,7 +178,8 @@ __global__ void __launch_bounds__(256) cnn_prep_kernel(const CnnArgs a) {
 // ---------------------------------------------------------------------------
 // Gather of the minibatch images straight into conv1's im2col matrix
 // Col1 [n*1024, 64] (K = (kh, kw, ci), 27 real), plus labels.
-// Grid (n*1024/256, chains): one thread per output pixel.
+// Grid (n*1024/256, chains): one thread per output pixel.  (Eight threads
+// per row, each storing one 16-byte group, measured twice as slow.)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
   const int c = blockIdx.y;
@@ -235,8 +236,9 @@ __global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
 // channels (128-bit loads of A, 64-bit stores of P, 32-bit of M); C and ld
 // are multiples of 4.  Grid (ceil(n*H*W*C/16 / 256), chains).
 // ---------------------------------------------------------------------------
+template <int H, int W, int C, int ld>
 __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pout, uint8_t* M,
-                                                      int n, int H, int W, int C, int ld) {
+                                                      int n) {
   // Per-chain element counts stay below 2^31: 32-bit index arithmetic.
   const int c = blockIdx.y;
   const int Ho = H / 2, Wo = W / 2;
@@ -251,8 +253,8 @@ __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pou
                      ((i * H + 2 * y) * W + 2 * x) * ld + ch;
   const float4 w0 = *reinterpret_cast<const float4*>(src);
   const float4 w1 = *reinterpret_cast<const float4*>(src + ld);
-  const float4 w2 = *reinterpret_cast<const float4*>(src + static_cast<int64_t>(W) * ld);
-  const float4 w3 = *reinterpret_cast<const float4*>(src + static_cast<int64_t>(W) * ld + ld);
+  const float4 w2 = *reinterpret_cast<const float4*>(src + W * ld);
+  const float4 w3 = *reinterpret_cast<const float4*>(src + W * ld + ld);
   const float a0[4] = {w0.x, w0.y, w0.z, w0.w}, a1[4] = {w1.x, w1.y, w1.z, w1.w};
   const float a2[4] = {w2.x, w2.y, w2.z, w2.w}, a3[4] = {w3.x, w3.y, w3.z, w3.w};
   __nv_bfloat162 out[2];
@@ -278,8 +280,8 @@ __global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pou
 // (9C real).  One thread per 8 consecutive K entries (C is a multiple of 8).
 // Grid (ceil(n*H*W*Kp/8 / 256), chains).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) cnn_im2col_kernel(const bf16* Pin, bf16* Col, int n,
-                                                        int H, int W, int C, int Kp) {
+template <int H, int W, int C, int Kp>
+__global__ void __launch_bounds__(256) cnn_im2col_kernel(const bf16* Pin, bf16* Col, int n) {
   const int c = blockIdx.y;
   const int groups = n * H * W * (Kp / 8);
   const int e = blockIdx.x * 256 + threadIdx.x;
@@ -429,10 +431,10 @@ __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
 // blocks.  2048 / C threads of a block share a channel group (256 * 8 is a
 // multiple of C, so the channel of thread t is 8 t mod C).
 // ---------------------------------------------------------------------------
+template <int H, int W, int C, int ld, int Kp>
 __global__ void __launch_bounds__(256) cnn_unpool_kernel(bf16* dY, const uint8_t* M,
                                                         const float* dp, const bf16* dcol,
-                                                        int n, int H, int W, int C, int ld,
-                                                        int Kp, float* bpart) {
+                                                        int n, float* bpart) {
   __shared__ float red[256 * 8];
   const int c = blockIdx.y;
   const int Ho = H / 2, Wo = W / 2;
@@ -725,17 +727,15 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   int rc;
   auto launched = [&](const char* what) { return check_launch(what); };
   // Bias gradient of a layer from its dY [rows, ld] (C real channels).
-  // Unpool of a layer (pooled grid Ho x Wo, Cr channels) and its bias
+  // Unpool of a layer (H x H before pooling, Cr channels) and its bias
   // gradient from the unpool blocks' partials.
-  auto unpool = [&](bf16* dY, const uint8_t* M, const float* dp, const bf16* dcol, int H,
-                    int Cr, int ld, int Kp, int64_t off) {
+  auto bias_sum = [&](int H, int Cr, int64_t off) {
     const int blocks = grid1(int64_t(n) * (H / 2) * (H / 2) * Cr / 8);
-    cnn_unpool_kernel<<<dim3(blocks, C), 256, 0, st>>>(dY, M, dp, dcol, n, H, H, Cr, ld, Kp,
-                                                       a.bpart);
-    int r = launched("cnn_unpool_kernel");
-    if (r) return r;
     cnn_bias_sum_kernel<<<C, 256, 0, st>>>(a.bpart, blocks, Cr, a.grad, off);
     return launched("cnn_bias_sum_kernel");
+  };
+  auto unpool_grid = [&](int H, int Cr) {
+    return dim3(grid1(int64_t(n) * (H / 2) * (H / 2) * Cr / 8), C);
   };
   // Weight gradient of a layer: split-K GEMM into partials, then their sum.
   auto weight_grad = [&](const CUtensorMap& mdy, const CUtensorMap& mcol, int layer, int Cout,
@@ -772,26 +772,26 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   const EpiConvRelu e1{a.w, ob1, kC1, kC1, r1, a.a1};
   if ((rc = launch_gemm<64, false, true>(m_col1, m_w1, C, r1, 64, kK1p, a.status, e1, st)))
     return rc;
-  cnn_pool_kernel<<<dim3(grid1(r2 * kC1 / 4), C), 256, 0, st>>>(a.a1, a.p1, a.m1, n, 32, 32, kC1,
-                                                                kC1);
+  cnn_pool_kernel<32, 32, kC1, kC1><<<dim3(grid1(r2 * kC1 / 4), C), 256, 0, st>>>(a.a1, a.p1,
+                                                                                 a.m1, n);
   if ((rc = launched("cnn_pool_kernel 1"))) return rc;
-  cnn_im2col_kernel<<<dim3(grid1(r2 * kK2p / 8), C), 256, 0, st>>>(a.p1, a.col2, n, 16, 16, kC1,
-                                                                   kK2p);
+  cnn_im2col_kernel<16, 16, kC1, kK2p><<<dim3(grid1(r2 * kK2p / 8), C), 256, 0, st>>>(
+      a.p1, a.col2, n);
   if ((rc = launched("cnn_im2col_kernel 2"))) return rc;
   const EpiConvRelu e2{a.w, ob2, kC2, kC2, r2, a.a2};
   if ((rc = launch_gemm<64, false, true>(m_col2, m_w2, C, r2, kC2, kK2p, a.status, e2, st)))
     return rc;
-  cnn_pool_kernel<<<dim3(grid1(r3 * kC2 / 4), C), 256, 0, st>>>(a.a2, a.p2, a.m2, n, 16, 16, kC2,
-                                                                kC2);
+  cnn_pool_kernel<16, 16, kC2, kC2><<<dim3(grid1(r3 * kC2 / 4), C), 256, 0, st>>>(a.a2, a.p2,
+                                                                                 a.m2, n);
   if ((rc = launched("cnn_pool_kernel 2"))) return rc;
-  cnn_im2col_kernel<<<dim3(grid1(r3 * kK3p / 8), C), 256, 0, st>>>(a.p2, a.col3, n, 8, 8, kC2,
-                                                                   kK3p);
+  cnn_im2col_kernel<8, 8, kC2, kK3p><<<dim3(grid1(r3 * kK3p / 8), C), 256, 0, st>>>(
+      a.p2, a.col3, n);
   if ((rc = launched("cnn_im2col_kernel 3"))) return rc;
   const EpiConvRelu e3{a.w, ob3, kC3, kC3, r3, a.a3};
   if ((rc = launch_gemm<128, false, true>(m_col3, m_w3, C, r3, kC3, kK3p, a.status, e3, st)))
     return rc;
-  cnn_pool_kernel<<<dim3(grid1(int64_t(n) * 16 * kC3 / 4), C), 256, 0, st>>>(a.a3, a.p3, a.m3,
-                                                                             n, 8, 8, kC3, kC3);
+  cnn_pool_kernel<8, 8, kC3, kC3><<<dim3(grid1(int64_t(n) * 16 * kC3 / 4), C), 256, 0, st>>>(
+      a.a3, a.p3, a.m3, n);
   if ((rc = launched("cnn_pool_kernel 3"))) return rc;
   cnn_dense_kernel<<<dim3(n, C), 128, 0, st>>>(a);
   if ((rc = launched("cnn_dense_kernel"))) return rc;
@@ -800,7 +800,9 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     cnn_dense_grad_kernel<<<dim3(kFlat / 128 + 1, C), 128, 0, st>>>(a);
     if ((rc = launched("cnn_dense_grad_kernel"))) return rc;
     // Layer 3: dY3 over A3, db3, dW3 = dY3^T Col3, dCol3 = dY3 W3^T.
-    if ((rc = unpool(a.dy3, a.m3, a.dp3, nullptr, 8, kC3, kC3, 0, ob3))) return rc;
+    cnn_unpool_kernel<8, 8, kC3, kC3, 0><<<unpool_grid(8, kC3), 256, 0, st>>>(
+        a.dy3, a.m3, a.dp3, nullptr, n, a.bpart);
+    if ((rc = launched("cnn_unpool_kernel 3")) || (rc = bias_sum(8, kC3, ob3))) return rc;
     CUtensorMap m_dy3t, m_col3t, m_dy3, m_w3k;
     if ((rc = make_tmap_bf16_3d(&m_dy3t, a.dy3, kC3, r3, C, kC3, r3 * kC3, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col3t, a.col3, kK3p, r3, C, kK3p, r3 * kK3p, 64, 64)) ||
@@ -812,7 +814,9 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     if ((rc = launch_gemm<64, false, false>(m_dy3, m_w3k, C, r3, kK3p, kC3, a.status, d3, st)))
       return rc;
     // Layer 2.
-    if ((rc = unpool(a.dy2, a.m2, nullptr, a.dcol3, 16, kC2, kC2, kK3p, ob2))) return rc;
+    cnn_unpool_kernel<16, 16, kC2, kC2, kK3p><<<unpool_grid(16, kC2), 256, 0, st>>>(
+        a.dy2, a.m2, nullptr, a.dcol3, n, a.bpart);
+    if ((rc = launched("cnn_unpool_kernel 2")) || (rc = bias_sum(16, kC2, ob2))) return rc;
     CUtensorMap m_dy2t, m_col2t, m_dy2, m_w2k;
     if ((rc = make_tmap_bf16_3d(&m_dy2t, a.dy2, kC2, r2, C, kC2, r2 * kC2, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col2t, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, 64, 64)) ||
@@ -824,7 +828,9 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     if ((rc = launch_gemm<64, false, false>(m_dy2, m_w2k, C, r2, kK2p, kC2, a.status, d2, st)))
       return rc;
     // Layer 1.
-    if ((rc = unpool(a.dy1, a.m1, nullptr, a.dcol2, 32, kC1, kA1ld, kK2p, ob1))) return rc;
+    cnn_unpool_kernel<32, 32, kC1, kA1ld, kK2p><<<unpool_grid(32, kC1), 256, 0, st>>>(
+        a.dy1, a.m1, nullptr, a.dcol2, n, a.bpart);
+    if ((rc = launched("cnn_unpool_kernel 1")) || (rc = bias_sum(32, kC1, ob1))) return rc;
     CUtensorMap m_dy1t, m_col1t;
     if ((rc = make_tmap_bf16_3d(&m_dy1t, a.dy1, kA1ld, r1, C, kA1ld, r1 * kA1ld, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col1t, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, 64, 64)))
