@@ -419,8 +419,8 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
   block = min(rbf.cached_batches_count, DEFAULT_BLOCK_STEPS, max(iterations, 1))
   outbuf = None
   if saving is not None and saving.kind != "device":
-    outbuf = io.HostBuffers([((len(states), n_kept, W.shape[1]), np.float32),
-                           ((len(states), n_kept), np.float64)])
+    outbuf = io.HostBuffers([((n_kept, len(states), W.shape[1]), np.float32),
+                             ((n_kept, len(states)), np.float64)])
   res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,
                      n_kept, index_src, noise_seed=states[0].key,
                      chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,

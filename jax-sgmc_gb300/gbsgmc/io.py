@@ -117,12 +117,12 @@ class HostBuffers:
 
 def postprocess_chains(saving: Saving, count: int, variables, treedefs,
                        extras: dict, model_states, host=None) -> list:
-  """Result dicts of C chains from a ``[count, C, P]`` device buffer (extras
-  ``[count, C]``).  With host saving, the buffers of all chains are
-  transposed chain-major on the device and copied to the host at once, and
-  each chain's arrays are views of that copy.  ``host`` optionally gives the
-  destination arrays (``[C, count, P]``, then one ``[C, count]`` per extra,
-  e.g. from :class:`HostBuffers`)."""
+  """Result dicts of C chains from a contiguous ``[count, C, P]`` device
+  buffer (extras ``[count, C]``).  With host saving, the buffers of all
+  chains are copied to the host at once (one plain device-to-host copy each,
+  no kernel), and each chain's arrays are strided views of that copy.
+  ``host`` optionally gives the destination arrays (``[count, C, P]``, then
+  one ``[count, C]`` per extra, e.g. from :class:`HostBuffers`)."""
   import torch
   C = variables.shape[1]
   if saving is None or saving.kind == "device":
@@ -130,14 +130,14 @@ def postprocess_chains(saving: Saving, count: int, variables, treedefs,
                         {k: v[:, c] for k, v in extras.items()},
                         model_states[c]) for c in range(C)]
   if host is None:
-    host = [np.empty((C, count, variables.shape[2]), np.float32)]
-    host += [np.empty((C, count), np.float64) for _ in extras]
-  torch.from_numpy(host[0]).copy_(variables.permute(1, 0, 2).contiguous())
+    host = [np.empty(tuple(variables.shape), np.float32)]
+    host += [np.empty(tuple(v.shape), np.float64) for v in extras.values()]
+  torch.from_numpy(host[0]).copy_(variables.contiguous())
   hext = {}
   for (k, v), h in zip(extras.items(), host[1:]):
-    torch.from_numpy(h).copy_(v.t().contiguous())
+    torch.from_numpy(h).copy_(v.contiguous())
     hext[k] = h
   host = host[0]
-  return [postprocess(saving, count, host[c], treedefs[c],
-                      {k: v[c] for k, v in hext.items()}, model_states[c])
+  return [postprocess(saving, count, host[:, c], treedefs[c],
+                      {k: v[:, c] for k, v in hext.items()}, model_states[c])
           for c in range(C)]
