@@ -51,6 +51,9 @@ typedef void* gbsgmc_stream_t;
 #define GBSGMC_TAG_SGHMC_STEP 4u
 #define GBSGMC_TAG_SWAP 5u
 #define GBSGMC_TAG_INDEX 6u
+#define GBSGMC_TAG_AMAGOLD 7u
+#define GBSGMC_TAG_AMAGOLD_INIT 8u
+#define GBSGMC_TAG_MH 9u
 
 /* Thread-local message for the last non-zero status returned on this thread. */
 const char* gbsgmc_last_error(void);
@@ -228,6 +231,54 @@ int gbsgmc_sghmc_momentum(int chains, int64_t P, float* p_dev,
                           const float* g_dev, const float* friction_dev,
                           float friction, const gbsgmc_sched* sched,
                           const gbsgmc_noise* noise, gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Reversible leapfrog (AMAGOLD) and Metropolis-Hastings corrections         */
+/* ------------------------------------------------------------------------ */
+
+/* x <- x + (scale h_k) p / m: the half (scale 0.5) and full (scale 1) position
+ * steps of reversible_leapfrog (jax_sgmc/integrator.py:383-388). */
+int gbsgmc_leapfrog_position(int chains, int64_t P, float* x_dev,
+                             const float* p_dev, const float* mass_dev,
+                             float scale, const gbsgmc_sched* sched,
+                             gbsgmc_stream_t stream);
+
+/* One momentum step of reversible_leapfrog (jax_sgmc/integrator.py:402-458):
+ *   p' = ((1 - h f) p - h g + sqrt(4 f h) sqrt(m) xi) / (1 + h f)
+ * with xi the Philox normals of tag GBSGMC_TAG_AMAGOLD at step k, and
+ * energy_dev[c] += 0.5 h sum (p + p') g / m (may be NULL). */
+int gbsgmc_amagold_momentum(int chains, int64_t P, float* p_dev,
+                            const float* g_dev, const float* mass_dev,
+                            float friction, double* energy_dev,
+                            const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                            gbsgmc_stream_t stream);
+
+#define GBSGMC_MH_AMAGOLD 0
+#define GBSGMC_MH_SGGMC 1
+
+/* FP64 Metropolis-Hastings decision per chain of solver.amagold
+ * (jax_sgmc/solver.py:368-395: log a = U_old - U_new + energy) or
+ * solver.sggmc (jax_sgmc/solver.py:508-528: log a = -(U_new - U_old +
+ * ke_end - ke_start) / T_k), capped at 0; accept when log u < log a with
+ * u = u_dev[c] or the 53-bit Philox uniform (seed, counter (chain_base + c,
+ * k, 0, GBSGMC_TAG_MH)).  Writes accept_dev[c] (0/1), ratio_dev[c] =
+ * exp(log a) and U_keep_dev[c] (U_new if accepted, else U_old); the last two
+ * may be NULL. */
+int gbsgmc_mh_accept(int chains, int kind, const double* U_old_dev,
+                     const double* U_new_dev, const double* energy_dev,
+                     const double* ke_start_dev, const double* ke_end_dev,
+                     const gbsgmc_sched* sched, const double* u_dev,
+                     uint64_t seed, int chain_base, int32_t* accept_dev,
+                     double* ratio_dev, double* U_keep_dev,
+                     gbsgmc_stream_t stream);
+
+/* After gbsgmc_mh_accept: rejected chains return to x_old and
+ * reject_momentum_sign * p_old (AMAGOLD flips the momentum: -1; SGGMC: +1;
+ * p_dev NULL leaves momenta alone); accepted chains keep the proposal. */
+int gbsgmc_mh_select(int chains, int64_t P, const int32_t* accept_dev,
+                     float* x_dev, const float* x_old_dev, float* p_dev,
+                     const float* p_old_dev, float reject_momentum_sign,
+                     gbsgmc_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
 /* Replica exchange                                                          */

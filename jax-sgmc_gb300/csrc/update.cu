@@ -451,6 +451,121 @@ __global__ void swap_adjacent_rows_kernel(int64_t width, float* a, const int32_t
   }
 }
 
+// ---------------------------------------------------------------------------
+// Reversible leapfrog (AMAGOLD) and Metropolis-Hastings corrections.
+// ---------------------------------------------------------------------------
+
+// x <- x + (scale h) p / m at the schedule's step.
+__global__ void leapfrog_position_kernel(int chains, int64_t P, float* x, const float* p,
+                                         const float* mass, float scale, Sched sched) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const float s = scale * sched.step_size(k);
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      const float sm = mass_inv(mass, j) * p[off + j];
+      x[off + j] = x[off + j] + s * sm;
+    }
+  }
+}
+
+// One momentum step of the reversible leapfrog, with the noise of tag
+// GBSGMC_TAG_AMAGOLD at the schedule's step:
+//   p' = ((1 - h f) p - h g + sqrt(4 f h) sqrt(m) xi) / (1 + h f)
+// and energy[c] += 0.5 h sum_j (p_j + p'_j) g_j / m_j.
+__global__ void amagold_momentum_kernel(int chains, int64_t P, float* p, const float* g,
+                                        const float* mass, float friction, double* energy,
+                                        Sched sched, Noise noise) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const float h = sched.step_size(k);
+  const float decay = 1.0f - h * friction;
+  const float inv = 1.0f / (1.0f + h * friction);
+  const float ns = sqrtf(4.0f * friction * h);
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  float part = 0.f;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float xi[4];
+    noise4(noise, c, 4 * q, P, k, GBSGMC_TAG_AMAGOLD, xi);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t j = 4 * q + e;
+      if (j >= P) break;
+      const float pj = p[off + j], gj = g[off + j];
+      const float noise_j = ns * (mass_sqrt(mass, j) * xi[e]);
+      const float pn = inv * ((decay * pj + (-h) * gj) + noise_j);
+      p[off + j] = pn;
+      part += (pj + pn) * (mass_inv(mass, j) * gj);
+    }
+  }
+  add_ke(energy, c, 0.5f * h * part);
+}
+
+// The MH decision of chain c in FP64:
+//   AMAGOLD (kind 0): log a = U_old - U_new + energy
+//   SGGMC   (kind 1): log a = -(U_new - U_old + ke_end - ke_start) / T_k
+// capped at 0 as the reference caps it (AMAGOLD keeps a NaN, SGGMC maps it
+// to 0); the proposal is accepted when log u < log a, u from Philox (seed,
+// counter (chain_base + c, step, 0, GBSGMC_TAG_MH)) or u_dev[c].  Writes
+// accept[c], ratio[c] = exp(log a) and the potential the chain keeps.
+__global__ void mh_accept_kernel(int chains, int kind, const double* U_old,
+                                 const double* U_new, const double* energy,
+                                 const double* ke_start, const double* ke_end, Sched sched,
+                                 const double* u_in, uint64_t seed, int chain_base,
+                                 int32_t* accept, double* ratio, double* U_keep) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= chains) return;
+  const int64_t k = sched.step();
+  double la;
+  if (kind == 0) {
+    la = U_old[c] - U_new[c] + energy[c];
+    la = la > 0.0 ? 0.0 : la;
+  } else {
+    const double T = static_cast<double>(sched.temperature(k, c));
+    la = -1.0 / T * (U_new[c] - U_old[c] + ke_end[c] - ke_start[c]);
+    la = la <= 0.0 ? la : 0.0;
+  }
+  double u;
+  if (u_in != nullptr) {
+    u = u_in[c];
+  } else {
+    const U32x4 r = philox4x32_10(
+        U32x4{static_cast<uint32_t>(chain_base + c), static_cast<uint32_t>(k), 0u,
+              GBSGMC_TAG_MH},
+        static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    const uint64_t bits = ((static_cast<uint64_t>(r.x) >> 5) << 26) |
+                          (static_cast<uint64_t>(r.y) >> 6);
+    u = (static_cast<double>(bits) + 0.5) * (1.0 / 9007199254740992.0);
+  }
+  const int acc = log(u) < la ? 1 : 0;
+  accept[c] = acc;
+  if (ratio != nullptr) ratio[c] = exp(la);
+  if (U_keep != nullptr) U_keep[c] = acc ? U_new[c] : U_old[c];
+}
+
+// Rejected chains go back to (x_old, sign * p_old); accepted ones keep the
+// proposal in x, p.
+__global__ void mh_select_kernel(int chains, int64_t P, const int32_t* accept, float* x,
+                                 const float* x_old, float* p, const float* p_old,
+                                 float sign) {
+  const int c = blockIdx.y;
+  if (accept[c]) return;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < P;
+       j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    x[off + j] = x_old[off + j];
+    if (p != nullptr) p[off + j] = sign * p_old[off + j];
+  }
+}
+
 int check_ec(int chains, int64_t P, const char* what) {
   if (chains < 0 || P < 0 || chains > 65535)
     return set_error(GBSGMC_ERR_ARG, "%s: bad chains/P", what);
@@ -568,6 +683,74 @@ extern "C" int gbsgmc_sghmc_momentum(int chains, int64_t P, float* p_dev,
       chains, P, nullptr, p_dev, g_dev, friction_dev, friction, to_sched(sched),
       to_noise(noise), to_fuse(nullptr));
   return check_launch("sghmc_momentum");
+}
+
+extern "C" int gbsgmc_leapfrog_position(int chains, int64_t P, float* x_dev,
+                                        const float* p_dev, const float* mass_dev,
+                                        float scale, const gbsgmc_sched* sched,
+                                        gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "leapfrog_position");
+  if (rc) return rc;
+  if (!x_dev || !p_dev || !sched)
+    return set_error(GBSGMC_ERR_ARG, "leapfrog_position: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, P);
+  leapfrog_position_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, x_dev, p_dev, mass_dev, scale, to_sched(sched));
+  return check_launch("leapfrog_position");
+}
+
+extern "C" int gbsgmc_amagold_momentum(int chains, int64_t P, float* p_dev,
+                                       const float* g_dev, const float* mass_dev,
+                                       float friction, double* energy_dev,
+                                       const gbsgmc_sched* sched,
+                                       const gbsgmc_noise* noise,
+                                       gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "amagold_momentum");
+  if (rc) return rc;
+  if (!p_dev || !g_dev || !sched || !noise)
+    return set_error(GBSGMC_ERR_ARG, "amagold_momentum: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, P);
+  amagold_momentum_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, p_dev, g_dev, mass_dev, friction, energy_dev, to_sched(sched),
+      to_noise(noise));
+  return check_launch("amagold_momentum");
+}
+
+extern "C" int gbsgmc_mh_accept(int chains, int kind, const double* U_old_dev,
+                                const double* U_new_dev, const double* energy_dev,
+                                const double* ke_start_dev, const double* ke_end_dev,
+                                const gbsgmc_sched* sched, const double* u_dev,
+                                uint64_t seed, int chain_base, int32_t* accept_dev,
+                                double* ratio_dev, double* U_keep_dev,
+                                gbsgmc_stream_t stream) {
+  if (chains < 0 || (kind != GBSGMC_MH_AMAGOLD && kind != GBSGMC_MH_SGGMC))
+    return set_error(GBSGMC_ERR_ARG, "mh_accept: bad chains or kind");
+  if (!U_old_dev || !U_new_dev || !sched || !accept_dev ||
+      (kind == GBSGMC_MH_AMAGOLD && !energy_dev) ||
+      (kind == GBSGMC_MH_SGGMC && (!ke_start_dev || !ke_end_dev)))
+    return set_error(GBSGMC_ERR_ARG, "mh_accept: null pointer");
+  if (chains == 0) return GBSGMC_OK;
+  mh_accept_kernel<<<(chains + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, kind, U_old_dev, U_new_dev, energy_dev, ke_start_dev, ke_end_dev,
+      to_sched(sched), u_dev, seed, chain_base, accept_dev, ratio_dev, U_keep_dev);
+  return check_launch("mh_accept");
+}
+
+extern "C" int gbsgmc_mh_select(int chains, int64_t P, const int32_t* accept_dev,
+                                float* x_dev, const float* x_old_dev, float* p_dev,
+                                const float* p_old_dev, float reject_momentum_sign,
+                                gbsgmc_stream_t stream) {
+  int rc = check_ec(chains, P, "mh_select");
+  if (rc) return rc;
+  if (!accept_dev || !x_dev || !x_old_dev || (p_dev != nullptr && p_old_dev == nullptr))
+    return set_error(GBSGMC_ERR_ARG, "mh_select: null pointer");
+  if (chains == 0 || P == 0) return GBSGMC_OK;
+  const Grid4 g = grid4(chains, (P + 3) / 4 * 4);
+  mh_select_kernel<<<g.grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      chains, P, accept_dev, x_dev, x_old_dev, p_dev, p_old_dev, reject_momentum_sign);
+  return check_launch("mh_select");
 }
 
 extern "C" int gbsgmc_resgld_swap_f64(

@@ -31,7 +31,8 @@ GLM_LINEAR = 2
 STATIC_SCRATCH_BYTES = 8 << 20
 
 TAG_SGLD, TAG_OBABO_1, TAG_OBABO_2, TAG_SGHMC_RESAMPLE, TAG_SGHMC_STEP, \
-  TAG_SWAP, TAG_INDEX = range(7)
+  TAG_SWAP, TAG_INDEX, TAG_AMAGOLD, TAG_AMAGOLD_INIT, TAG_MH = range(10)
+MH_AMAGOLD, MH_SGGMC = 0, 1
 
 
 class GbsgmcError(RuntimeError):
@@ -152,6 +153,13 @@ SIGNATURES = {
                                    _P(Sched), _vp]),
     "gbsgmc_sghmc_momentum": (_i, [_i, _i64, _vp, _vp, _vp, _f, _P(Sched),
                                    _P(Noise), _vp]),
+    "gbsgmc_leapfrog_position": (_i, [_i, _i64, _vp, _vp, _vp, _f, _P(Sched),
+                                      _vp]),
+    "gbsgmc_amagold_momentum": (_i, [_i, _i64, _vp, _vp, _vp, _f, _vp,
+                                     _P(Sched), _P(Noise), _vp]),
+    "gbsgmc_mh_accept": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _P(Sched), _vp,
+                              _u64, _i, _vp, _vp, _vp, _vp]),
+    "gbsgmc_mh_select": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _f, _vp]),
     "gbsgmc_resgld_swap_f64": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _vp, _vp,
                                     _vp, _u64, _i64, _vp, _vp, _vp]),
     "gbsgmc_swap_rows": (_i, [_i, _i64, _vp, _vp, _vp, _vp]),

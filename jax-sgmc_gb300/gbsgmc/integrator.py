@@ -317,6 +317,90 @@ def friction_leapfrog(potential_fn, batch_fn, steps=10, friction=0.25,
                            const_mass=const_mass, noise_source=noise_source)
 
 
-def reversible_leapfrog(*args, **kwargs):
-  raise NotImplementedError("the AMAGOLD reversible leapfrog is not part of "
-                            "the GPU hot path yet")
+def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,
+                        friction: float = 0.25, const_mass=None,
+                        noise_source: Callable = None):
+  """Time-reversible leapfrog of AMAGOLD (integrator.py:349-560): a half
+  position step, ``steps`` momentum steps (each but the first after a full
+  position step) with the friction-implicit update
+  ``p' = ((1 - h f) p - h g + sqrt(4 f h) sqrt(M) xi) / (1 + h f)``, and a
+  final half position step.  The state's ``potential`` is the energy the
+  MH test needs, ``sum 0.5 h (p + p') . M^-1 g`` over the steps (fp64,
+  accumulated on the device).  The initial momentum is ``sqrt(M) xi``
+  (Philox tag GBSGMC_TAG_AMAGOLD_INIT).  ``noise_source(step, chain, tag)``
+  injects the normals (tests)."""
+  if not np.isscalar(friction):
+    raise NotImplementedError("per-parameter friction is not supported by the "
+                              "reversible leapfrog kernels")
+  init_data, get_data, _ = batch_fn
+  f = float(friction)
+
+  def init_fn(init_sample, key=None, batch_kwargs=None, init_model_state=None,
+              mass=None):
+    import torch
+    if mass is not None:
+      raise NotImplementedError("mass adaption is not supported; use "
+                                "const_mass")
+    batch_kwargs = batch_kwargs or {}
+    data_state = init_data(**batch_kwargs)
+    w, tdef = _flat(init_sample)
+    P = w.numel()
+    chain = int(data_state.chain_id or 0)
+    seed = key_to_seed(key)
+    buf = _injected(noise_source, 0, chain, _lib.TAG_AMAGOLD_INIT)
+    if buf is not None:
+      p = buf.clone()
+    else:
+      p = torch.empty(P, dtype=torch.float32, device="cuda")
+      _lib.call("gbsgmc_philox_normal", seed, chain, 1, 0,
+                _lib.TAG_AMAGOLD_INIT, P, _lib.ptr(p), P, _lib.stream_handle())
+    m = _flat_tree_like(const_mass, P)
+    if m is not None:
+      p = p * m.sqrt()
+    return LeapfrogState(
+        positions=w, momentum=p,
+        potential=torch.zeros(1, dtype=torch.float64, device="cuda"),
+        model_state=init_model_state, data_state=data_state, key=seed,
+        step=0, chain=chain, treedef=tdef)
+
+  def integrate(state: LeapfrogState, parameters, mass=None):
+    import torch
+    if mass is not None:
+      raise NotImplementedError("mass adaption is not supported; use "
+                                "const_mass")
+    x, p = state.positions, state.momentum
+    P = x.numel()
+    m = _flat_tree_like(const_mass, P)
+    step = state.step
+    energy = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def sch(k):
+      return _lib.sched(step_size=float(parameters.step_size),
+                        temperature=float(parameters.temperature), offset=k)
+
+    _lib.call("gbsgmc_leapfrog_position", 1, P, _lib.ptr(x), _lib.ptr(p),
+              _lib.ptr(m), 0.5, sch(step), _lib.stream_handle())
+    data_state = state.data_state
+    for j in range(steps):
+      if j > 0:
+        _lib.call("gbsgmc_leapfrog_position", 1, P, _lib.ptr(x), _lib.ptr(p),
+                  _lib.ptr(m), 1.0, sch(step), _lib.stream_handle())
+      data_state, (b, i) = get_data(data_state, information=True)
+      r = _eval(potential_fn, x, b, i)
+      buf = _injected(noise_source, step, state.chain, _lib.TAG_AMAGOLD)
+      _lib.call("gbsgmc_amagold_momentum", 1, P, _lib.ptr(p), _lib.ptr(r.grad),
+                _lib.ptr(m), f, _lib.ptr(energy), sch(step),
+                _noise(state.key, state.chain, buf), _lib.stream_handle())
+      step += 1
+    _lib.call("gbsgmc_leapfrog_position", 1, P, _lib.ptr(x), _lib.ptr(p),
+              _lib.ptr(m), 0.5, sch(step), _lib.stream_handle())
+    return state._replace(potential=energy, data_state=data_state, step=step)
+
+  def get_fn(state):
+    return {"variables": state.positions, "energy": state.potential,
+            "model_state": state.model_state}
+
+  return IntegratorTriplet(init_fn, integrate, get_fn, kind="reversible_leapfrog",
+                           potential=potential_fn, batch_fn=batch_fn,
+                           steps=steps, friction=friction,
+                           const_mass=const_mass, noise_source=noise_source)

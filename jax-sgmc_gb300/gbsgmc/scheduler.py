@@ -202,6 +202,7 @@ def adaptive_step_size(burn_in=0, initial_step_size=0.05,
 
   def update(state, iteration, acceptance_ratio=0.0, **kwargs):
     burn_in, x_bar, h_bar, alpha, t0, kappa, gamma, mu = state
+    acceptance_ratio = float(acceptance_ratio)  # a device scalar from the MH step
     m = iteration + 1
     h_bar *= (1 - 1 / (m + t0))
     h_bar += 1 / (m + t0) * (alpha - acceptance_ratio)

@@ -107,12 +107,125 @@ def parallel_tempering(integrator, sa_schedule=None):
                        integrator=integrator)
 
 
-def amagold(*args, **kwargs):
-  raise NotImplementedError("AMAGOLD is not part of the GPU hot path yet")
+class MHState(NamedTuple):
+  """State of a solver with a full-data MH correction (AMAGOLD, SGGMC)."""
+  integrator_state: Any
+  potential: Any          # fp64 device [1]: full potential of the current sample
+  full_data_state: Any
+  key: int
+  acceptance_ratio: Any   # fp64 device [1]
+  step_size: float
+  mh_step: int            # MH corrections done (the Philox counter of u)
+  mass_state: Any = None
 
 
-def sggmc(*args, **kwargs):
-  raise NotImplementedError("SGGMC is not part of the GPU hot path yet")
+def _mh_solver(kind, integrator, full_potential_fn, full_data_map,
+               mass_adaption, reject_sign):
+  init_integrator, update_integrator, get_integrator = integrator
+  init_full_data, full_data_map_fn, _ = full_data_map
+  if mass_adaption is not None:
+    raise NotImplementedError("mass adaption is not supported; pass a "
+                              "constant mass to the integrator")
+
+  def init(init_sample, key=0, initial_mass=None, full_data_kwargs=None,
+           **kwargs):
+    import torch
+    if initial_mass is not None:
+      raise NotImplementedError("mass adaption is not supported")
+    full_data_state = init_full_data(**(full_data_kwargs or {}))
+    U, (full_data_state, model_state) = full_potential_fn(
+        init_sample, full_data_state, full_data_map_fn,
+        state=kwargs.get("init_model_state"))
+    kwargs["init_model_state"] = model_state
+    seed = int(np.asarray(key).ravel()[-1]) if key is not None else 0
+    integrator_state = init_integrator(init_sample, key=(seed, 1), **kwargs)
+    return MHState(integrator_state=integrator_state,
+                   potential=U.reshape(1).to(torch.float64).clone(),
+                   full_data_state=full_data_state, key=seed,
+                   acceptance_ratio=torch.zeros(1, dtype=torch.float64,
+                                                device="cuda"),
+                   step_size=0.0, mh_step=0)
+
+  def update(state: MHState, schedule):
+    import torch
+    ist = state.integrator_state
+    x_old = ist.positions.clone()
+    p_old = ist.momentum.clone()
+    proposal = update_integrator(ist, schedule)
+    U_new, (full_data_state, model_state) = full_potential_fn(
+        proposal.positions, state.full_data_state, full_data_map_fn,
+        state=proposal.model_state)
+    U_new = U_new.reshape(1).to(torch.float64)
+    accept = torch.empty(1, dtype=torch.int32, device="cuda")
+    ratio = torch.empty(1, dtype=torch.float64, device="cuda")
+    U_keep = torch.empty(1, dtype=torch.float64, device="cuda")
+    sch = _lib.sched(step_size=float(schedule.step_size),
+                     temperature=float(schedule.temperature),
+                     offset=state.mh_step)
+    if kind == _lib.MH_AMAGOLD:
+      energy, ke0, ke1 = proposal.potential, None, None
+    else:
+      energy, ke0, ke1 = None, proposal.kinetic_energy_start, \
+          proposal.kinetic_energy_end
+    _lib.call("gbsgmc_mh_accept", 1, kind, _lib.ptr(state.potential),
+              _lib.ptr(U_new), _lib.ptr(energy), _lib.ptr(ke0), _lib.ptr(ke1),
+              sch, None, state.key, int(ist.chain), _lib.ptr(accept),
+              _lib.ptr(ratio), _lib.ptr(U_keep), _lib.stream_handle())
+    P = proposal.positions.numel()
+    _lib.call("gbsgmc_mh_select", 1, P, _lib.ptr(accept),
+              _lib.ptr(proposal.positions), _lib.ptr(x_old),
+              _lib.ptr(proposal.momentum), _lib.ptr(p_old), float(reject_sign),
+              _lib.stream_handle())
+    new_ist = proposal
+    if kind == _lib.MH_SGGMC:
+      # The kinetic energies restart at 0 after each correction
+      # (solver.py:536-537).
+      new_ist = proposal._replace(
+          kinetic_energy_start=torch.zeros(1, dtype=torch.float64, device="cuda"),
+          kinetic_energy_end=torch.zeros(1, dtype=torch.float64, device="cuda"))
+    new_state = state._replace(integrator_state=new_ist, potential=U_keep,
+                               full_data_state=full_data_state,
+                               acceptance_ratio=ratio,
+                               step_size=float(schedule.step_size),
+                               mh_step=state.mh_step + 1)
+    return new_state, {"acceptance_ratio": ratio}
+
+  def get(state: MHState):
+    out = dict(get_integrator(state.integrator_state))
+    out["acceptance_ratio"] = state.acceptance_ratio
+    out["step_size"] = state.step_size
+    if kind == _lib.MH_SGGMC:
+      out["potential"] = state.potential
+    return out
+
+  return init, update, get
+
+
+def amagold(integrator_fn, full_potential_fn, full_data_map,
+            mass_adaption=None):
+  """AMAGOLD (solver.py:301-432): reversible-leapfrog proposals with an
+  amortised full-data MH correction, log a = U_old - U_new + E (E the
+  proposal's accumulated energy); a rejected proposal returns to the old
+  sample with the momentum flipped.  The decision runs in FP64 on the device
+  (``gbsgmc_mh_accept``); u comes from Philox (tag GBSGMC_TAG_MH) where the
+  reference splits a JAX key."""
+  init, update, get = _mh_solver(_lib.MH_AMAGOLD, integrator_fn,
+                                 full_potential_fn, full_data_map,
+                                 mass_adaption, -1.0)
+  return SolverTriplet(init, update, get, kind="amagold",
+                       integrator=integrator_fn)
+
+
+def sggmc(integrator_fn, full_potential_fn, full_data_map, mass_adaption=None):
+  """SGGMC (solver.py:434-577): OBABO proposals with a full-data MH
+  correction, log a = -(U_new - U_old + KE_end - KE_start) / T; a rejected
+  proposal returns to the old sample and momentum.  FP64 decision on the
+  device as for :func:`amagold`."""
+  init, update, get = _mh_solver(_lib.MH_SGGMC, integrator_fn,
+                                 full_potential_fn, full_data_map,
+                                 mass_adaption, 1.0)
+  return SolverTriplet(init, update, get, kind="sggmc",
+                       integrator=integrator_fn)
 
 
 def _flat_of(sample_dict):
@@ -142,12 +255,14 @@ def mcmc(solver, scheduler, strategy="map", saving=None, loading=None):
     extra = torch.empty((n_kept,), dtype=torch.float64, device="cuda")
     for k in range(iterations):
       schedules = [get_fn(s) for s in states]
-      state, _ = solver_update(state, *schedules)
+      state, stats = solver_update(state, *schedules)
       if keep[k] >= 0:
         got = solver_get(state)
         samples[keep[k]] = _flat_of(got)
         extra[keep[k]] = got[extra_key].reshape(())
-      states = [update_fn(s) for s in states]
+      # The solver's statistics (the MH acceptance ratio) feed the schedule,
+      # as in solver.py:113-121.
+      states = [update_fn(s, **(stats or {})) for s in states]
     treedef = _treedef_of(state)
     return io.postprocess(saving or io.no_save(), n_kept, samples, treedef,
                           {extra_key: extra})
@@ -176,4 +291,6 @@ def _treedef_of(state):
       return getattr(state, name)
   if hasattr(state, "normal"):
     return _treedef_of(state.normal)
+  if hasattr(state, "integrator_state"):
+    return _treedef_of(state.integrator_state)
   raise ValueError("state carries no sample tree definition")

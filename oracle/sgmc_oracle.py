@@ -512,6 +512,72 @@ def sghmc_momentum(p, g, xi, h, friction):
   return (p + f * (np.sqrt(f32(2.0) * h, dtype=f32) * xi)).astype(f32)
 
 
+def leapfrog_position(x, p, h, scale, mass=None):
+  """x + (scale h) M^-1 p: the half / full position steps of
+  reversible_leapfrog (integrator.py:383-388), fp32."""
+  x, p = np.asarray(x, f32), np.asarray(p, f32)
+  mi = f32(1.0) if mass is None else (f32(1.0) / np.asarray(mass, f32))
+  s = f32(scale) * f32(h)
+  return (x + s * (mi * p)).astype(f32)
+
+
+def amagold_momentum(p, g, xi, h, friction, mass=None):
+  """One momentum step of reversible_leapfrog (integrator.py:402-458):
+  p' = ((1 - h f) p - h g + sqrt(4 f h) sqrt(M) xi) / (1 + h f), and the
+  energy 0.5 h (p + p') . M^-1 g (fp64 sum of fp32 products).  Returns
+  (p', energy)."""
+  p, g, xi = (np.asarray(a, f32) for a in (p, g, xi))
+  h, f = f32(h), f32(friction)
+  mi = f32(1.0) if mass is None else (f32(1.0) / np.asarray(mass, f32))
+  ms = f32(1.0) if mass is None else np.sqrt(np.asarray(mass, f32))
+  decay = f32(1.0) - h * f
+  inv = f32(1.0) / (f32(1.0) + h * f)
+  ns = np.sqrt(f32(4.0) * f * h, dtype=f32)
+  pn = (inv * ((decay * p + (-h) * g) + ns * (ms * xi))).astype(f32)
+  energy = 0.5 * float(h) * float(np.sum((p + pn).astype(np.float64) *
+                                         (mi * g).astype(np.float64)))
+  return pn, energy
+
+
+def reversible_leapfrog(x, p, grad_fn, xis, h, friction, mass=None):
+  """integrate of reversible_leapfrog (integrator.py:510-553): half position
+  step, len(xis) momentum steps (a full position step before each but the
+  first; grad_fn(x, j) gives the stochastic gradient of step j), half
+  position step.  Returns (x, p, accumulated energy)."""
+  x = leapfrog_position(x, p, h, 0.5, mass)
+  energy = 0.0
+  for j, xi in enumerate(xis):
+    if j > 0:
+      x = leapfrog_position(x, p, h, 1.0, mass)
+    p, e = amagold_momentum(p, grad_fn(x, j), xi, h, friction, mass)
+    energy += e
+  x = leapfrog_position(x, p, h, 0.5, mass)
+  return x, p, energy
+
+
+def mh_log_alpha(kind, U_old, U_new, energy=0.0, ke_start=0.0, ke_end=0.0,
+                 T=1.0):
+  """The capped log acceptance of solver.amagold (kind 'amagold',
+  solver.py:381-383: U_old - U_new + E, NaN kept) or solver.sggmc (kind
+  'sggmc', solver.py:518-524: -(U_new - U_old + KE_end - KE_start) / T, NaN
+  capped to 0), FP64."""
+  if kind == "amagold":
+    la = U_old - U_new + energy
+    return 0.0 if la > 0.0 else la
+  la = -1.0 / T * (U_new - U_old + ke_end - ke_start)
+  return la if la <= 0.0 else 0.0
+
+
+def mh_uniform(seed: int, chain: int, step: int) -> float:
+  """The MH uniform: Philox(counter=(chain, step, 0, 9), key=seed), 53 bits
+  as in swap_uniform."""
+  r = philox4x32_10(np.array([[chain & 0xFFFFFFFF, step & 0xFFFFFFFF, 0, 9]],
+                             np.uint64),
+                    (seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF))[0]
+  bits = ((int(r[0]) >> 5) << 26) | (int(r[1]) >> 6)
+  return (bits + 0.5) / 9007199254740992.0
+
+
 def resgld_swap(U_n, U_h, var_n, T_n, T_h, ssq, k, u, F=1.0):
   """solver.parallel_tempering.update exchange step (solver.py:273-291), FP64.
   Returns (swapped, ssq', k', log_s); swapped is True when NOT log u < log s

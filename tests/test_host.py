@@ -292,8 +292,8 @@ def test_potential_rejects_arbitrary_callables():
 
 
 def test_unported_presets_raise():
-  from gbsgmc import alias, adaption
-  with pytest.raises(NotImplementedError):
-    alias.amagold()
+  from gbsgmc import adaption, integrator
   with pytest.raises(NotImplementedError):
     adaption.fisher_information()
+  with pytest.raises(NotImplementedError):   # per-parameter friction
+    integrator.reversible_leapfrog(None, (None, None, None), friction=[0.1, 0.2])

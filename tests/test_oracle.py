@@ -189,3 +189,29 @@ def test_linear_posterior_is_the_normal_equations():
   mu, cov = O.linear_posterior(X, y, 0.1, 1e6)
   np.testing.assert_allclose(mu, np.linalg.lstsq(X, y, rcond=None)[0], rtol=1e-6)
   assert np.all(np.linalg.eigvalsh(cov) > 0)
+
+
+def test_reversible_leapfrog_oracle_is_time_reversible():
+  """With friction 0 (no noise) and a deterministic gradient, running the
+  leapfrog back from (x', -p') returns to (x, -p) -- the property AMAGOLD's
+  MH correction rests on (integrator.py:349-360) -- and the capped MH
+  log-acceptances follow solver.py:381-383 / 518-524."""
+  rng = np.random.default_rng(0)
+  d, steps, h = 7, 12, 0.05
+  A = rng.normal(size=(d, d))
+  A = (A @ A.T / d + np.eye(d)).astype(np.float32)
+  grad = lambda x, j: (A @ x).astype(np.float32)
+  x0 = rng.normal(size=d).astype(np.float32)
+  p0 = rng.normal(size=d).astype(np.float32)
+  xis = [np.zeros(d, np.float32)] * steps
+  x1, p1, _ = O.reversible_leapfrog(x0, p0, grad, xis, h, 0.0)
+  x2, p2, _ = O.reversible_leapfrog(x1, -p1, grad, xis, h, 0.0)
+  np.testing.assert_allclose(x2, x0, rtol=1e-4, atol=1e-5)
+  np.testing.assert_allclose(-p2, p0, rtol=1e-4, atol=1e-5)
+  assert O.mh_log_alpha("amagold", 1.0, 0.5, 0.1) == 0.0
+  assert O.mh_log_alpha("amagold", 1.0, 2.0, 0.25) == -0.75
+  assert np.isnan(O.mh_log_alpha("amagold", 1.0, np.nan, 0.0))
+  assert O.mh_log_alpha("sggmc", 1.0, np.nan) == 0.0
+  assert O.mh_log_alpha("sggmc", 1.0, 3.0, 0.0, 0.5, 1.0, 2.0) == -1.25
+  u = O.mh_uniform(7, 3, 11)
+  assert 0.0 < u < 1.0 and u != O.mh_uniform(7, 3, 12)
