@@ -63,11 +63,30 @@ def step_tables(total):
 
 
 def pcg_words(seed):
-  from oracle import sgmc_oracle as O
-  st = O.loader_rng(seed).bit_generator.state
-  s, inc = st["state"]["state"], st["state"]["inc"]
-  m = (1 << 64) - 1
-  return [(s >> 64) & m, s & m, (inc >> 64) & m, inc & m, 0]
+  """Device PCG64 words of the index stream of chain `seed`, as the
+  NumpyDataLoader registers it."""
+  from gbsgmc.data.numpy_loader import pcg64_words
+  return pcg64_words(seed)
+
+
+def shard_chains(rank, per_rank):
+  """Weak scaling: rank r runs its own `per_rank` chains, ids
+  [r * per_rank, (r + 1) * per_rank).  A chain's index stream is seeded with
+  its id and its noise keyed by it, so a chain's samples do not depend on
+  how chains are spread over ranks.  Returns (first id, ids)."""
+  base = rank * per_rank
+  return base, list(range(base, base + per_rank))
+
+
+def max_over_ranks(value, world, device):
+  """The slowest rank's time (all-reduce MAX); `value` itself for one rank."""
+  if world <= 1:
+    return value
+  import torch
+  import torch.distributed as dist
+  t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+  dist.all_reduce(t, op=dist.ReduceOp.MAX)
+  return float(t.item())
 
 
 def dist_env():
@@ -215,7 +234,7 @@ class Setup:
     self.ds = self.loader.device_dataset()
     self.pot = potential.minibatch_potential(L.GaussianPrior(1.0), L.Logistic(),
                                              strategy="vmap")
-    self.chain_base = rank * CHAINS
+    self.chain_base, _ = shard_chains(rank, CHAINS)
     self.W = torch.zeros((CHAINS, D), dtype=torch.float32, device="cuda")
     self.V = torch.ones((CHAINS, D), dtype=torch.float32, device="cuda")
 
@@ -323,10 +342,7 @@ def run_gbsgmc(args):
   clk = clocks.stop()
   ms = start.elapsed_time(end)
   plan.check_status()
-  if world > 1:
-    t = torch.tensor([ms], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
+  ms = max_over_ranks(ms, world, "cuda")
   value = world * CHAINS * args.steps / (ms / 1e3)
   launches = plan.launches(args.steps)
   shape = plan.launch_shape()
@@ -465,16 +481,17 @@ MLP_WORKLOAD = ("Bayesian MLP regression, OBABO: 64-1024-1024-1 tanh "
 def mlp_data():
   """X ~ N(0,1) [N, 64], targets from a random teacher network + N(0, 0.1^2)."""
   from gbsgmc import likelihoods as L
-  from oracle import sgmc_oracle as O
   rng = np.random.default_rng(20261203 + 3)
   lik = L.MLPGaussian(d_in=MLP_D, h1=MLP_H, h2=MLP_H, sigma=0.1)
   X = rng.standard_normal((MLP_N, MLP_D), dtype=np.float32)
-  teacher = lik.init(rng).astype(np.float64)
+  teacher = lik.unravel(lik.init(rng).astype(np.float64))
   y = np.empty(MLP_N, np.float32)
   for a in range(0, MLP_N, 50_000):
-    f, _, _ = O.mlp_forward(teacher[None], X[None, a:a + 50_000].astype(np.float64),
-                            MLP_D, MLP_H, MLP_H)
-    y[a:a + 50_000] = f[0] + 0.1 * rng.standard_normal(min(50_000, MLP_N - a))
+    xb = X[a:a + 50_000].astype(np.float64)
+    z1 = np.tanh(xb @ teacher["W1"] + teacher["b1"])
+    z2 = np.tanh(z1 @ teacher["W2"] + teacher["b2"])
+    f = (z2 @ teacher["W3"])[:, 0] + teacher["b3"][0]
+    y[a:a + 50_000] = f + 0.1 * rng.standard_normal(min(50_000, MLP_N - a))
   inits = np.stack([lik.init(np.random.default_rng(1000 + c))
                     for c in range(MLP_CHAINS)])
   return lik, X, y, inits
@@ -688,18 +705,19 @@ def run_cnn(args):
   F = torch.nn.functional
   imgs = torch.from_numpy(images).cuda()
   labs = torch.from_numpy(labels).cuda().long()
-  from oracle import sgmc_oracle as O
-  off, _ = O.cnn_offsets()
+  from gbsgmc import likelihoods as L
+  cnn_lik = L.CNNSoftmax()
 
   def plain_grad(w, rows):
     w = w.detach().requires_grad_(True)
-    get = lambda k: w[off[k][0]:off[k][1]]
+    prm = cnn_lik.unravel(w)   # views of w in the sorted-key ravel order
     x = imgs[rows].permute(0, 3, 1, 2)
     for l in range(3):
-      ci, co = O.CNN_CHANNELS[l], O.CNN_CHANNELS[l + 1]
-      k = get(f"W{l + 1}").reshape(3, 3, ci, co).permute(3, 2, 0, 1)
-      x = F.max_pool2d(F.relu(F.conv2d(x, k, get(f"b{l + 1}"), padding=1)), 2)
-    logits = x.permute(0, 2, 3, 1).reshape(CNN_MB, -1) @ get("Wd").reshape(-1, 10) + get("bd")
+      layer = prm[f"conv{l + 1}"]
+      k = layer["w"].permute(3, 2, 0, 1)   # HWIO -> OIHW
+      x = F.max_pool2d(F.relu(F.conv2d(x, k, layer["b"], padding=1)), 2)
+    logits = x.permute(0, 2, 3, 1).reshape(CNN_MB, -1) @ prm["linear"]["w"] + \
+        prm["linear"]["b"]
     U = (CNN_N / CNN_MB) * F.cross_entropy(logits, labs[rows], reduction="sum") + \
         0.5 * (w * w).sum()
     U.backward()
@@ -739,6 +757,7 @@ def run_cnn(args):
   P = lik.param_count
   cpu = None
   if rank == 0:
+    from oracle import sgmc_oracle as O   # the CPU baseline leg
     threads = os.cpu_count() or 1
     rng = np.random.default_rng(5)
     t0 = time.perf_counter()

@@ -28,6 +28,22 @@ from .core import (DeviceDataLoader, HostDataLoader, DataLoader,
 PyTree = Any
 
 
+def chain_rng(seed: int) -> onp.random.Generator:
+  """The index stream of a chain registered with ``seed``: numpy's PCG64
+  seeded with ``SeedSequence(seed).spawn(1)[0]`` (numpy_loader.py:261-265)."""
+  return onp.random.default_rng(onp.random.SeedSequence(seed).spawn(1)[0])
+
+
+def pcg64_words(seed: int) -> List[int]:
+  """The five 64-bit words of ``gbsgmc_pcg64`` (state high/low, increment
+  high/low, buffered half) of :func:`chain_rng`'s fresh generator."""
+  st = chain_rng(seed).bit_generator.state
+  s, inc = st["state"]["state"], st["state"]["inc"]
+  m = (1 << 64) - 1
+  return [(s >> 64) & m, s & m, (inc >> 64) & m, inc & m,
+          (int(st["uinteger"]) << 32) | int(st["has_uint32"])]
+
+
 class NumpyBase(DataLoader):
 
   def __init__(self, on_device: bool = True, copy=True, **reference_data):
@@ -124,7 +140,7 @@ class NumpyDataLoader(NumpyBase, HostDataLoader):
       raise ValueError("in_epochs = True can only be used for shuffle = True.")
     chain_id = len(self._chains)
     seed = kwargs.get("seed", chain_id)
-    rng = onp.random.default_rng(onp.random.SeedSequence(seed).spawn(1)[0])
+    rng = chain_rng(seed)
     self._chains.append({'type': 'random', 'rng': rng, 'idx_offset': None,
                          'in_epochs': in_epochs, 'shuffle': shuffle,
                          'remaining_samples': 0,

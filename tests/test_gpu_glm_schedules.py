@@ -345,3 +345,44 @@ def test_glm_obabo_sghmc_plan_equals_per_chain_steps(lib, monkeypatch, kind):
     vb = np.asarray(rb["samples"]["variables"]["w"])
     assert np.isfinite(va).all() and not np.array_equal(va[0], va[-1])
     np.testing.assert_array_equal(va, vb)
+
+
+def test_sharded_plans_equal_one_plan(lib, monkeypatch):
+  """Replicas on one GPU: two plans over chain ids [0, C) and [C, 2C) --
+  bench.py's shard_chains, index streams seeded and noise keyed by the chain
+  id -- equal one plan over all 2C chains bit for bit (one CTA per chain,
+  so a chain's arithmetic does not depend on the others)."""
+  import torch
+  from gbsgmc import data, engine
+  from gbsgmc.data.numpy_loader import pcg64_words
+  monkeypatch.setenv("GBSGMC_AUTOTUNE", "0")
+  monkeypatch.setenv("GBSGMC_GLM_SLICES", "1")
+  monkeypatch.setenv("GBSGMC_GLM_RW", "8")
+  monkeypatch.setenv("GBSGMC_GLM_MULTISTEP", "1")
+  N, d, C, n, K = 4000, 64, 4, 256, 30
+  X, y = _problem(N, d, O.LOGISTIC, seed=51)
+  loader = data.NumpyDataLoader(x=X, y=y)
+  pot = _pot(O.LOGISTIC, prior=5.0)
+  h = np.full(K, 1e-4, np.float32)
+  T = np.ones(K, np.float32)
+  keep = np.full(K, -1, np.int32)
+  keep[::6] = np.arange(len(keep[::6]))
+  words = np.array([pcg64_words(c) for c in range(2 * C)], np.uint64).view(np.int64)
+
+  def run(lo, hi):
+    pcg = cuda(words[lo:hi])
+    r = engine.run_sgld_glm(pot, loader.device_dataset(),
+                            cuda(np.zeros((hi - lo, d), np.float32)),
+                            cuda(np.ones((hi - lo, d), np.float32)), n, K, h, T,
+                            keep, int((keep >= 0).sum()),
+                            engine.IndexSource(pcg=pcg, chain_base=lo),
+                            noise_seed=11, chain_base=lo, block_steps=10)
+    return r, pcg
+
+  whole, pw = run(0, 2 * C)
+  a, pa = run(0, C)
+  b, pb = run(C, 2 * C)
+  assert torch.equal(whole.w, torch.cat([a.w, b.w]))
+  assert torch.equal(whole.U, torch.cat([a.U, b.U]))
+  assert torch.equal(whole.samples, torch.cat([a.samples, b.samples], 1))
+  assert torch.equal(pw, torch.cat([pa, pb]))
