@@ -36,7 +36,7 @@ typedef void* gbsgmc_stream_t;
 #define GBSGMC_ERR_NONFINITE 4   /* potential or gradient is NaN / Inf        */
 #define GBSGMC_ERR_TIMEOUT 5     /* a bounded device wait gave up             */
 #define GBSGMC_ERR_CUDA 6        /* CUDA runtime error (message in last_error) */
-#define GBSGMC_ERR_UNSUPPORTED 7 /* feature not available in this build        */
+#define GBSGMC_ERR_UNSUPPORTED 7 /* feature not available in this library      */
 
 /* Likelihood families of the generalised-linear kernels. */
 #define GBSGMC_GLM_LINEAR_GAUSSIAN 0 /* lk = log N(y | x.w, sigma^2)          */

@@ -69,8 +69,9 @@ def test_fused_plan_equals_per_step_path(lib):
 
 
 def test_plan_reproduces_oracle_over_many_steps(lib):
-  """1000 steps of config 1 with the reference loader's index stream (seed =
-  chain id 0) and the production Philox noise, against the oracle."""
+  """1000 steps of the linear-regression workload (N = 10,000, d = 32,
+  minibatch 128) with the reference loader's index stream (seed = chain id
+  0) and the production Philox noise, against the oracle."""
   from gbsgmc import engine, likelihoods as L, potential, data
   X, y = linreg()
   N, d, n, K = 10_000, 32, 128, 1000
