@@ -604,6 +604,35 @@ def run_resgld(args):
       if (ROOT / "MEASURED_PEAKS.json").exists() else {}
   peak = peaks.get("bf16_tflops_sustained", 1700.0)
   achieved = flops / (grad_ms / 1e3) / 1e12
+  # End to end through the package: host replicas in, plan built, the steps
+  # run, replicas and exchange counts back on the host.
+  torch.cuda.synchronize()
+  s0 = time.perf_counter()
+  Xh = inits[:RE_REPLICAS].copy()
+  X2 = torch.from_numpy(Xh).cuda()
+  V2 = torch.ones_like(X2)
+  pcg2 = torch.from_numpy(words.copy()).cuda()
+  plan2 = engine.ResgldPlan(pot, ds, X2, V2, rows, n_max, ladder, h, t,
+                            engine.IndexSource(pcg=pcg2, chain_base=RE_REPLICAS * rank),
+                            noise_seed=11, swap_seed=12, every=RE_EVERY)
+  plan2.run(0, steps)
+  X_out = X2.cpu().numpy()
+  counts_out = plan2.counts.cpu().numpy()
+  plan2.check_status()
+  plan2.close()
+  e2e_s = time.perf_counter() - s0
+  e2e_value = world * RE_REPLICAS * steps / e2e_s
+  h2d = 2 * Xh.nbytes + words.nbytes
+  d2h = X_out.nbytes + counts_out.nbytes
+  cpu = None
+  if rank == 0:
+    threads = os.cpu_count() or 1
+    grad_rate = mlp_cpu_grad_rate(lik, X, y, inits, 3, threads)
+    # One replica-step is one gradient at n_r rows; the sample is at 2048.
+    cpu_rate = grad_rate * MLP_MB / float(rows.mean())
+    cpu = {"value": cpu_rate, "unit": "chain-steps/s", "cores": threads, "kind": "port",
+           "sample": f"3 float64 gradients of one replica at n = {MLP_MB} (numpy oracle, "
+                     f"{threads} threads), scaled to the mean minibatch {rows.mean():.0f}"}
   if rank == 0:
     print(json.dumps({
         "metric": METRIC, "value": value, "unit": "chain-steps/s", "n_gpus": world,
@@ -621,6 +650,10 @@ def run_resgld(args):
                      "peak_kind": "measured bf16_tflops_sustained",
                      "kernel": "ragged batched value-and-gradient, 32 replicas",
                      "kernel_ms": grad_ms, "algorithmic_flop_per_launch": flops},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "chain-steps/s",
+                "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+                "api": "gbsgmc.engine.ResgldPlan from host replicas, results to host"},
         "clocks": clk, "finite": finite}), flush=True)
 
 

@@ -60,6 +60,14 @@ int obabo_second_fused(int chains, int64_t P, const float* x, float* p,
                        double* ke_end, const gbsgmc_sched* sched,
                        const gbsgmc_noise* noise, const UpdateFusion& f,
                        cudaStream_t st);
+// Step k's second OBABO half (gradient g2) then step k + 1's first half
+// (gradient g1, taken at the same positions) in one pass: the same values as
+// obabo_second_fused at step k followed by obabo_first_fused at step k + 1.
+int obabo_second_first_fused(int chains, int64_t P, float* x, float* p, const float* g2,
+                             const float* g1, const float* mass, float friction,
+                             double* ke_end, double* ke_start, const gbsgmc_sched* sched,
+                             const gbsgmc_noise* noise, const UpdateFusion& f,
+                             cudaStream_t st);
 int sghmc_position_fused(int chains, int64_t P, float* x, float* p, const float* mass,
                          float friction, const gbsgmc_sched* sched,
                          const UpdateFusion& f, cudaStream_t st);

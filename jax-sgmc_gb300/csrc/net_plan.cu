@@ -23,8 +23,10 @@ __global__ void mean_pair_kernel(int chains, double* a, const double* b) {
   if (c < chains) a[c] = 0.5 * (a[c] + b[c]);
 }
 
-// Value and gradient over all chains: (idx, idx_stride, U, lk_var, stream).
-using GradFn = std::function<int(const int32_t*, int64_t, double*, double*, cudaStream_t)>;
+// Value and gradient over all chains:
+// (idx, idx_stride, U, lk_var, gradient out [chains, P], stream).
+using GradFn =
+    std::function<int(const int32_t*, int64_t, double*, double*, float*, cudaStream_t)>;
 
 struct NetPlan final : gbsgmc_plan {
   GradFn grad_fn;
@@ -34,6 +36,7 @@ struct NetPlan final : gbsgmc_plan {
   float* x = nullptr;
   float* aux = nullptr;
   float* grad = nullptr;  // owned [chains, P]
+  float* grad2 = nullptr; // owned [chains, P] (OBABO: the second gradient)
   gbsgmc_sched sched{};
   gbsgmc_noise noise{};
   gbsgmc_index_src isrc{};
@@ -58,6 +61,7 @@ struct NetPlan final : gbsgmc_plan {
   ~NetPlan() override {
     if (stream != nullptr) cudaStreamSynchronize(stream);
     cudaFree(grad);
+    cudaFree(grad2);
     cudaFree(U2);
     cudaFree(idx);
     cudaFree(ws);
@@ -65,6 +69,18 @@ struct NetPlan final : gbsgmc_plan {
   }
 
   int enqueue_fused(int g, cudaStream_t s);
+  int enqueue_obabo(int g, const UpdateFusion& moving, const UpdateFusion& last,
+                    cudaStream_t s);
+
+  // The gradient buffers: OBABO keeps two, because its second gradient of
+  // step j and its first gradient of step j + 1 feed one update pass.
+  int alloc_grads(const char* what) {
+    const size_t bytes = sizeof(float) * static_cast<size_t>(chains) * P;
+    int rc = cuda_err(cudaMalloc(&grad, bytes), what);
+    if (rc == GBSGMC_OK && integ.kind == GBSGMC_INTEGRATOR_OBABO)
+      rc = cuda_err(cudaMalloc(&grad2, bytes), what);
+    return rc;
+  }
 
   int step_multiple() const override {
     return integ.kind == GBSGMC_INTEGRATOR_SGHMC ? integ.leapfrog_steps : 1;
@@ -72,11 +88,13 @@ struct NetPlan final : gbsgmc_plan {
 
   int64_t launches_per_block(int g) const override {
     // Kernels of one value-and-gradient call are counted by the caller.
+    // Every block: the index draw, the step counter and, fused, the mirror.
+    const int64_t fixed = fused ? 3 : 2;
     switch (integ.kind) {
-      case GBSGMC_INTEGRATOR_OBABO: return 2 + 3 * static_cast<int64_t>(g);
+      case GBSGMC_INTEGRATOR_OBABO: return fixed + 2 + static_cast<int64_t>(g);
       case GBSGMC_INTEGRATOR_SGHMC:
-        return 2 + 2 * static_cast<int64_t>(g) + g / integ.leapfrog_steps;
-      default: return 2 + static_cast<int64_t>(g);
+        return fixed + 2 * static_cast<int64_t>(g) + g / integ.leapfrog_steps;
+      default: return fixed + static_cast<int64_t>(g);
     }
   }
 
@@ -93,8 +111,10 @@ struct NetPlan final : gbsgmc_plan {
                                rows, idx, per, cn, s);
     }
     if (rc != GBSGMC_OK) return rc;
-    double* ke_start = ke;
-    double* ke_end = ke != nullptr ? ke + chains : nullptr;
+    if (integ.kind == GBSGMC_INTEGRATOR_OBABO) {
+      if ((rc = enqueue_obabo(g, UpdateFusion{}, UpdateFusion{}, s))) return rc;
+      return plan_advance(this, g, s);
+    }
     for (int j = 0; j < g; ++j) {
       gbsgmc_sched sj = sched;
       sj.base_dev = base;
@@ -102,21 +122,9 @@ struct NetPlan final : gbsgmc_plan {
       const int32_t* ij = idx + j * cn;
       switch (integ.kind) {
         case GBSGMC_INTEGRATOR_SGLD:
-          if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+          if ((rc = grad_fn(ij, per, U, lk_var, grad, s))) return rc;
           rc = gbsgmc_sgld_update(chains, P, x, grad, aux, integ.alpha, integ.lmbd, &sj,
                                   &noise, nullptr, s);
-          break;
-        case GBSGMC_INTEGRATOR_OBABO:
-          if ((rc = grad_fn(ij, per, U, nullptr, s))) return rc;
-          if ((rc = gbsgmc_obabo_first(chains, P, x, aux, grad, integ.mass_dev, integ.friction,
-                                       ke_start, &sj, &noise, s)))
-            return rc;
-          if ((rc = grad_fn(ij + n, per, U2, lk_var, s))) return rc;
-          if ((rc = gbsgmc_obabo_second(chains, P, aux, grad, integ.mass_dev, integ.friction,
-                                        ke_end, &sj, &noise, s)))
-            return rc;
-          mean_pair_kernel<<<(chains + 127) / 128, 128, 0, s>>>(chains, U, U2);
-          rc = check_launch("plan: potential mean");
           break;
         default:  // SGHMC
           if (j % integ.leapfrog_steps == 0 &&
@@ -125,7 +133,7 @@ struct NetPlan final : gbsgmc_plan {
           if ((rc = gbsgmc_sghmc_position(chains, P, x, aux, integ.mass_dev, nullptr,
                                           integ.friction, &sj, s)))
             return rc;
-          if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+          if ((rc = grad_fn(ij, per, U, lk_var, grad, s))) return rc;
           rc = gbsgmc_sghmc_momentum(chains, P, aux, grad, nullptr, integ.friction, &sj,
                                      &noise, s);
           break;
@@ -155,8 +163,10 @@ int NetPlan::enqueue_fused(int g, cudaStream_t s) {
   prior_only.prior_pf = pf;
   UpdateFusion with_prior = fz;
   with_prior.prior_pf = pf;
-  double* ke_start = ke;
-  double* ke_end = ke != nullptr ? ke + chains : nullptr;
+  if (integ.kind == GBSGMC_INTEGRATOR_OBABO) {
+    if ((rc = enqueue_obabo(g, with_prior, prior_only, s))) return rc;
+    return plan_advance(this, g, s);
+  }
   for (int j = 0; j < g; ++j) {
     gbsgmc_sched sj = sched;
     sj.base_dev = base;
@@ -164,21 +174,9 @@ int NetPlan::enqueue_fused(int g, cudaStream_t s) {
     const int32_t* ij = idx + j * cn;
     switch (integ.kind) {
       case GBSGMC_INTEGRATOR_SGLD:
-        if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+        if ((rc = grad_fn(ij, per, U, lk_var, grad, s))) return rc;
         rc = sgld_update_fused(chains, P, x, grad, aux, integ.alpha, integ.lmbd, &sj, &noise,
                                with_prior, s);
-        break;
-      case GBSGMC_INTEGRATOR_OBABO:
-        if ((rc = grad_fn(ij, per, U, nullptr, s))) return rc;
-        if ((rc = obabo_first_fused(chains, P, x, aux, grad, integ.mass_dev, integ.friction,
-                                    ke_start, &sj, &noise, with_prior, s)))
-          return rc;
-        if ((rc = grad_fn(ij + n, per, U2, lk_var, s))) return rc;
-        if ((rc = obabo_second_fused(chains, P, x, aux, grad, integ.mass_dev, integ.friction,
-                                     ke_end, &sj, &noise, prior_only, s)))
-          return rc;
-        mean_pair_kernel<<<(chains + 127) / 128, 128, 0, s>>>(chains, U, U2);
-        rc = check_launch("plan: potential mean");
         break;
       default:  // SGHMC
         if (j % integ.leapfrog_steps == 0 &&
@@ -187,7 +185,7 @@ int NetPlan::enqueue_fused(int g, cudaStream_t s) {
         if ((rc = sghmc_position_fused(chains, P, x, aux, integ.mass_dev, integ.friction, &sj,
                                        fz, s)))
           return rc;
-        if ((rc = grad_fn(ij, per, U, lk_var, s))) return rc;
+        if ((rc = grad_fn(ij, per, U, lk_var, grad, s))) return rc;
         rc = sghmc_momentum_fused(chains, P, x, aux, grad, integ.friction, &sj, &noise,
                                   prior_only, s);
         break;
@@ -195,6 +193,46 @@ int NetPlan::enqueue_fused(int g, cudaStream_t s) {
     if (rc != GBSGMC_OK) return rc;
   }
   return plan_advance(this, g, s);
+}
+
+// OBABO over the block's g steps (integrator.py:192-273), indices already
+// drawn.  Step j's first half moves the positions; its second gradient and
+// step j + 1's first gradient are both taken there, so step j's second half
+// and step j + 1's first half run as one pass over the parameters.  The
+// block's last step ends with its own second half, and the potential is the
+// mean of that step's two minibatch values.  `moving` is the fusion of the
+// passes that move x, `last` that of the final second half.
+int NetPlan::enqueue_obabo(int g, const UpdateFusion& moving, const UpdateFusion& last,
+                           cudaStream_t s) {
+  const int per = draws() * n;
+  const int64_t cn = static_cast<int64_t>(chains) * per;
+  double* ke_start = ke;
+  double* ke_end = ke != nullptr ? ke + chains : nullptr;
+  gbsgmc_sched sj = sched;
+  sj.base_dev = base;
+  sj.offset = 0;
+  int rc;
+  if ((rc = grad_fn(idx, per, U, nullptr, grad, s))) return rc;
+  if ((rc = obabo_first_fused(chains, P, x, aux, grad, integ.mass_dev, integ.friction,
+                              ke_start, &sj, &noise, moving, s)))
+    return rc;
+  for (int j = 0; j + 1 < g; ++j) {
+    const int32_t* ij = idx + j * cn;
+    if ((rc = grad_fn(ij + n, per, U2, nullptr, grad2, s))) return rc;
+    if ((rc = grad_fn(ij + cn, per, U, nullptr, grad, s))) return rc;
+    sj.offset = j;
+    if ((rc = obabo_second_first_fused(chains, P, x, aux, grad2, grad, integ.mass_dev,
+                                       integ.friction, ke_end, ke_start, &sj, &noise, moving,
+                                       s)))
+      return rc;
+  }
+  sj.offset = g - 1;
+  if ((rc = grad_fn(idx + (g - 1) * cn + n, per, U2, lk_var, grad2, s))) return rc;
+  if ((rc = obabo_second_fused(chains, P, x, aux, grad2, integ.mass_dev, integ.friction,
+                               ke_end, &sj, &noise, last, s)))
+    return rc;
+  mean_pair_kernel<<<(chains + 127) / 128, 128, 0, s>>>(chains, U, U2);
+  return check_launch("plan: potential mean");
 }
 
 // reSGLD over R replicas with ragged minibatches and adjacent exchanges.
@@ -248,7 +286,7 @@ struct ResgldPlan final : gbsgmc_plan {
       gbsgmc_sched sj = sched;
       sj.base_dev = base;
       sj.offset = j;
-      if ((rc = grad_fn(idx + j * cn, n_max, U, lk_var, s))) return rc;
+      if ((rc = grad_fn(idx + j * cn, n_max, U, lk_var, grad, s))) return rc;
       if ((rc = gbsgmc_sgld_update(replicas, P, x, grad, v, alpha, lmbd, &sj, &noise, nullptr,
                                    s)))
         return rc;
@@ -326,16 +364,14 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
   p->ws_size = ws;
   do {
     if ((rc = plan_init(p, block_steps))) break;
-    const size_t gbytes = sizeof(float) * static_cast<size_t>(chains) * p->P;
     const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
                           p->draws() * n;
-    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "mlp_plan_create: gradient"))) break;
+    if ((rc = p->alloc_grads("mlp_plan_create: gradient"))) break;
     if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "mlp_plan_create: U")))
       break;
     if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "mlp_plan_create: index buffer"))) break;
     if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "mlp_plan_create: workspace"))) break;
     const gbsgmc_mlp m = *model;
-    float* grad = p->grad;
     void* wsp = p->ws;
     const float* x = x_dev;
     const char* env = std::getenv("GBSGMC_NO_STEP_FUSION");
@@ -352,15 +388,15 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
         p->pf = static_cast<float>(1.0 / (static_cast<double>(m.prior_scale) *
                                           m.prior_scale * m.temperature));
       const double* sqp = p->sq;
-      p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev, sqp, nb](
-                       const int32_t* idx, int64_t stride, double* U, double* var,
+      p->grad_fn = [m, chains, n, x, wsp, ws, status_dev, sqp, nb](
+                       const int32_t* idx, int64_t stride, double* U, double* var, float* grad,
                        cudaStream_t s) {
         return mlp_value_and_grad_fused(&m, chains, n, idx, stride, x, U, grad, var, wsp, ws,
                                         status_dev, s, sqp, nb);
       };
     } else {
-      p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
-                       const int32_t* idx, int64_t stride, double* U, double* var,
+      p->grad_fn = [m, chains, n, x, wsp, ws, status_dev](
+                       const int32_t* idx, int64_t stride, double* U, double* var, float* grad,
                        cudaStream_t s) {
         return gbsgmc_mlp_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
                                          nullptr, var, wsp, ws, status_dev, s);
@@ -410,20 +446,18 @@ extern "C" int gbsgmc_cnn_plan_create(gbsgmc_plan** out, const gbsgmc_cnn* model
   p->ws_size = ws;
   do {
     if ((rc = plan_init(p, block_steps))) break;
-    const size_t gbytes = sizeof(float) * static_cast<size_t>(chains) * p->P;
     const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
                           p->draws() * n;
-    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "cnn_plan_create: gradient"))) break;
+    if ((rc = p->alloc_grads("cnn_plan_create: gradient"))) break;
     if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "cnn_plan_create: U")))
       break;
     if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "cnn_plan_create: index buffer"))) break;
     if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "cnn_plan_create: workspace"))) break;
     const gbsgmc_cnn m = *model;
-    float* grad = p->grad;
     void* wsp = p->ws;
     const float* x = x_dev;
-    p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
-                     const int32_t* idx, int64_t stride, double* U, double* var,
+    p->grad_fn = [m, chains, n, x, wsp, ws, status_dev](
+                     const int32_t* idx, int64_t stride, double* U, double* var, float* grad,
                      cudaStream_t s) {
       return gbsgmc_cnn_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
                                        nullptr, var, wsp, ws, status_dev, s);
@@ -497,11 +531,10 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
       break;
     if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "mlp_resgld_plan_create: workspace"))) break;
     const gbsgmc_mlp m = *model;
-    float* grad = p->grad;
     void* wsp = p->ws;
     const float* x = x_dev;
-    p->grad_fn = [m, replicas, n_max, n_dev, x, grad, wsp, ws, status_dev](
-                     const int32_t* idx, int64_t stride, double* U, double* var,
+    p->grad_fn = [m, replicas, n_max, n_dev, x, wsp, ws, status_dev](
+                     const int32_t* idx, int64_t stride, double* U, double* var, float* grad,
                      cudaStream_t s) {
       return gbsgmc_mlp_value_and_grad_ragged(&m, replicas, n_max, n_dev, idx, stride, nullptr,
                                               x, U, grad, nullptr, var, wsp, ws, status_dev,
@@ -551,10 +584,9 @@ extern "C" int gbsgmc_glm_plan_create(gbsgmc_plan** out, const gbsgmc_glm* model
   p->ws_size = ws;
   do {
     if ((rc = plan_init(p, block_steps))) break;
-    const size_t gbytes = sizeof(float) * static_cast<size_t>(chains) * p->P;
     const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
                           p->draws() * n;
-    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "glm_plan_create: gradient"))) break;
+    if ((rc = p->alloc_grads("glm_plan_create: gradient"))) break;
     if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "glm_plan_create: U")))
       break;
     if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "glm_plan_create: index buffer"))) break;
@@ -564,11 +596,10 @@ extern "C" int gbsgmc_glm_plan_create(gbsgmc_plan** out, const gbsgmc_glm* model
       break;
     if ((rc = glm_prepare())) break;
     const gbsgmc_glm m = *model;
-    float* grad = p->grad;
     void* wsp = p->ws;
     const float* x = x_dev;
-    p->grad_fn = [m, chains, n, x, grad, wsp, ws, status_dev](
-                     const int32_t* idx, int64_t stride, double* U, double* var,
+    p->grad_fn = [m, chains, n, x, wsp, ws, status_dev](
+                     const int32_t* idx, int64_t stride, double* U, double* var, float* grad,
                      cudaStream_t s) {
       return gbsgmc_glm_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
                                        nullptr, var, wsp, ws, status_dev, s);

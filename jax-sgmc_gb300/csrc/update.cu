@@ -174,18 +174,48 @@ __device__ __forceinline__ void add_ke(double* ke, int c, float part) {
   if (threadIdx.x == 0) atomicAdd(ke + c, tot);
 }
 
+// The OBABO halves of one parameter (integrator.py:192-273), with every
+// rounding spelled out (__fmaf_rn / __fmul_rn) so that the separate kernels
+// and the fused second-then-first kernel compute the same bits.
+struct ObaboCoef {
+  float h, keep, inject, half;
+};
+__device__ __forceinline__ ObaboCoef obabo_coef(const Sched& sched, int64_t k, int c,
+                                                float friction) {
+  ObaboCoef q;
+  q.h = sched.step_size(k);
+  const float T = sched.temperature(k, c);
+  const float permanence = expf(-friction * q.h);
+  q.keep = sqrtf(permanence);
+  q.inject = sqrtf((1.0f - permanence) * T);
+  q.half = 0.5f * q.h;
+  return q;
+}
+// O, kinetic energy, B, A: p, x updated, ke accumulates.
+__device__ __forceinline__ void obabo_first_elem(const ObaboCoef& q, float mi, float ms,
+                                                 float g, float xi, float& p, float& x,
+                                                 float& ke) {
+  float pj = __fmaf_rn(q.keep, p, __fmul_rn(q.inject, __fmul_rn(ms, xi)));
+  ke = __fmaf_rn(__fmul_rn(0.5f, pj), __fmul_rn(mi, pj), ke);
+  pj = __fmaf_rn(-q.half, g, pj);
+  p = pj;
+  x = __fmaf_rn(q.h, __fmul_rn(mi, pj), x);
+}
+// B, kinetic energy, O: p updated, ke accumulates.
+__device__ __forceinline__ void obabo_second_elem(const ObaboCoef& q, float mi, float ms,
+                                                  float g, float xi, float& p, float& ke) {
+  const float pj = __fmaf_rn(-q.half, g, p);
+  ke = __fmaf_rn(__fmul_rn(0.5f, pj), __fmul_rn(mi, pj), ke);
+  p = __fmaf_rn(q.keep, pj, __fmul_rn(q.inject, __fmul_rn(ms, xi)));
+}
+
 __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
                                    const float* g1, const float* mass,
                                    float friction, double* ke_start,
                                    Sched sched, Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
-  const float h = sched.step_size(k);
-  const float T = sched.temperature(k, c);
-  const float permanence = expf(-friction * h);
-  const float keep = sqrtf(permanence);
-  const float inject = sqrtf((1.0f - permanence) * T);
-  const float half = 0.5f * h;
+  const ObaboCoef qc = obabo_coef(sched, k, c, friction);
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
   float ke = 0.0f, sq = 0.0f;
@@ -203,13 +233,9 @@ __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       if (j0 + e >= P) break;
-      const float mi = mass_inv(mass, j0 + e);
-      const float gj = fz.pf != 0.f ? fmaf(fz.pf, xv[e], gv[e]) : gv[e];
-      float pj = keep * pv[e] + inject * (mass_sqrt(mass, j0 + e) * xi[e]);
-      ke = fmaf(0.5f * pj, mi * pj, ke);
-      pj = -half * gj + pj;
-      pv[e] = pj;
-      xv[e] = xv[e] + h * (mi * pj);
+      const float gj = fz.pf != 0.f ? __fmaf_rn(fz.pf, xv[e], gv[e]) : gv[e];
+      obabo_first_elem(qc, mass_inv(mass, j0 + e), mass_sqrt(mass, j0 + e), gj, xi[e],
+                       pv[e], xv[e], ke);
     }
     store4(pc, j0, P, pv);
     store4(xc, j0, P, xv);
@@ -225,12 +251,7 @@ __global__ void obabo_second_kernel(int chains, int64_t P, const float* x, float
                                     Sched sched, Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
-  const float h = sched.step_size(k);
-  const float T = sched.temperature(k, c);
-  const float permanence = expf(-friction * h);
-  const float keep = sqrtf(permanence);
-  const float inject = sqrtf((1.0f - permanence) * T);
-  const float half = 0.5f * h;
+  const ObaboCoef qc = obabo_coef(sched, k, c, friction);
   const int64_t groups = (P + 3) / 4;
   const int64_t off = static_cast<int64_t>(c) * P;
   float ke = 0.0f;
@@ -248,15 +269,61 @@ __global__ void obabo_second_kernel(int chains, int64_t P, const float* x, float
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       if (j0 + e >= P) break;
-      const float mi = mass_inv(mass, j0 + e);
-      const float gj = xc != nullptr ? fmaf(fz.pf, xv[e], gv[e]) : gv[e];
-      float pj = -half * gj + pv[e];
-      ke = fmaf(0.5f * pj, mi * pj, ke);
-      pv[e] = keep * pj + inject * (mass_sqrt(mass, j0 + e) * xi[e]);
+      const float gj = xc != nullptr ? __fmaf_rn(fz.pf, xv[e], gv[e]) : gv[e];
+      obabo_second_elem(qc, mass_inv(mass, j0 + e), mass_sqrt(mass, j0 + e), gj, xi[e],
+                        pv[e], ke);
     }
     store4(pc, j0, P, pv);
   }
   add_ke(ke_end, c, ke);
+}
+
+// The second half of step k and the first half of step k + 1 in one pass
+// (their gradients g2 of step k and g1 of step k + 1 are both taken at the
+// same positions): per parameter exactly the operations of
+// obabo_second_kernel (step k) then obabo_first_kernel (step k + 1).
+__global__ void obabo_second_first_kernel(int chains, int64_t P, float* x, float* p,
+                                          const float* g2, const float* g1,
+                                          const float* mass, float friction,
+                                          double* ke_end, double* ke_start, Sched sched,
+                                          Noise noise, Fuse fz) {
+  const int c = blockIdx.y;
+  const int64_t k = sched.step();
+  const ObaboCoef q2 = obabo_coef(sched, k, c, friction);
+  const ObaboCoef q1 = obabo_coef(sched, k + 1, c, friction);
+  const int64_t groups = (P + 3) / 4;
+  const int64_t off = static_cast<int64_t>(c) * P;
+  float ke2 = 0.0f, ke1 = 0.0f, sq = 0.0f;
+  float* __restrict__ xc = x + off;
+  float* __restrict__ pc = p + off;
+  const float* __restrict__ g2c = g2 + off;
+  const float* __restrict__ g1c = g1 + off;
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       q < groups; q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t j0 = 4 * q;
+    float xv[4], pv[4], gv2[4], gv1[4], xi2[4], xi1[4];
+    load4(xc, j0, P, xv);
+    load4(pc, j0, P, pv);
+    load4(g2c, j0, P, gv2);
+    load4(g1c, j0, P, gv1);
+    noise4(noise, c, j0, P, k, GBSGMC_TAG_OBABO_2, xi2);
+    noise4(noise, c, j0, P, k + 1, GBSGMC_TAG_OBABO_1, xi1);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      if (j0 + e >= P) break;
+      const float mi = mass_inv(mass, j0 + e), ms = mass_sqrt(mass, j0 + e);
+      const float ga = fz.pf != 0.f ? __fmaf_rn(fz.pf, xv[e], gv2[e]) : gv2[e];
+      obabo_second_elem(q2, mi, ms, ga, xi2[e], pv[e], ke2);
+      const float gb = fz.pf != 0.f ? __fmaf_rn(fz.pf, xv[e], gv1[e]) : gv1[e];
+      obabo_first_elem(q1, mi, ms, gb, xi1[e], pv[e], xv[e], ke1);
+    }
+    store4(pc, j0, P, pv);
+    store4(xc, j0, P, xv);
+    fuse_store(fz, c, j0, P, xv, sq);
+  }
+  add_ke(ke_end, c, ke2);
+  add_ke(ke_start, c, ke1);
+  fuse_finish(fz, c, sq);
 }
 
 __global__ void sghmc_resample_kernel(int chains, int64_t P, float* p,
@@ -852,6 +919,18 @@ int obabo_second_fused(int chains, int64_t P, const float* x, float* p, const fl
                                                     ke_end, to_sched(sched), to_noise(noise),
                                                     to_fuse(&f));
   return check_launch("obabo_second (fused)");
+}
+
+int obabo_second_first_fused(int chains, int64_t P, float* x, float* p, const float* g2,
+                             const float* g1, const float* mass, float friction,
+                             double* ke_end, double* ke_start, const gbsgmc_sched* sched,
+                             const gbsgmc_noise* noise, const UpdateFusion& f,
+                             cudaStream_t st) {
+  const Grid4 gr = grid4(chains, P);
+  obabo_second_first_kernel<<<gr.grid, kThreads, 0, st>>>(
+      chains, P, x, p, g2, g1, mass, friction, ke_end, ke_start, to_sched(sched),
+      to_noise(noise), to_fuse(&f));
+  return check_launch("obabo_second_first (fused)");
 }
 
 int sghmc_position_fused(int chains, int64_t P, float* x, float* p, const float* mass,
