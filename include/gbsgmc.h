@@ -281,6 +281,38 @@ int gbsgmc_mh_select(int chains, int64_t P, const int32_t* accept_dev,
                      gbsgmc_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Sample statistics                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* FP64 posterior moments of kept samples (replaces collecting every sample
+ * on the host through io.py:626-771 to take moments there).  Adds `count`
+ * samples of each chain -- sample k of chain c at
+ * samples_dev[k * slot_stride + c * chain_stride + j] -- to the shifted sums
+ * of [chains, P]: shift (fp32, the first sample, written when seen == 0),
+ * s1 = sum (x - shift), s2 = sum (x - shift)^2 (fp64).  `seen` is the number
+ * of samples already in the sums. */
+int gbsgmc_moments_accumulate(int chains, int64_t P, int count, const float* samples_dev,
+                              int64_t slot_stride, int64_t chain_stride, int64_t seen,
+                              float* shift_dev, double* s1_dev, double* s2_dev,
+                              gbsgmc_stream_t stream);
+
+/* Mean and population variance (ddof 0) of n samples from the sums above:
+ * mean = shift + s1 / n, var = max((s2 - s1 (s1 / n)) / n, 0). */
+int gbsgmc_moments_finalize(int chains, int64_t P, int64_t n, const float* shift_dev,
+                            const double* s1_dev, const double* s2_dev, double* mean_dev,
+                            double* var_dev, gbsgmc_stream_t stream);
+
+/* Diagonal mass adaption (adaption.py:296-368, mass_matrix(diagonal=True)),
+ * one update with the `iteration`-th sample x (1-based), fp32:
+ *   mean' = (i-1)/i mean + 1/i x;  ssq += (x - mean)(x - mean')
+ * and when iteration == burn_in: inv = ssq / i, sqrt = sqrt(i / ssq) and,
+ * when mass_dev is not NULL, the mass i / ssq that the integrator kernels
+ * take as `mass_dev`. */
+int gbsgmc_mass_adapt(int64_t P, int iteration, int burn_in, const float* x_dev,
+                      float* mean_dev, float* ssq_dev, float* inv_dev, float* sqrt_dev,
+                      float* mass_dev, gbsgmc_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* Replica exchange                                                          */
 /* ------------------------------------------------------------------------ */
 

@@ -160,6 +160,11 @@ SIGNATURES = {
     "gbsgmc_mh_accept": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _P(Sched), _vp,
                               _u64, _i, _vp, _vp, _vp, _vp]),
     "gbsgmc_mh_select": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _f, _vp]),
+    "gbsgmc_moments_accumulate": (_i, [_i, _i64, _i, _vp, _i64, _i64, _i64, _vp,
+                                       _vp, _vp, _vp]),
+    "gbsgmc_moments_finalize": (_i, [_i, _i64, _i64, _vp, _vp, _vp, _vp, _vp,
+                                     _vp]),
+    "gbsgmc_mass_adapt": (_i, [_i64, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbsgmc_resgld_swap_f64": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _vp, _vp,
                                     _vp, _u64, _i64, _vp, _vp, _vp]),
     "gbsgmc_swap_rows": (_i, [_i, _i64, _vp, _vp, _vp, _vp]),

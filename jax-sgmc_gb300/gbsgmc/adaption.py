@@ -10,8 +10,12 @@ adaption.py:120-222; here parameters are flat already):
 
 The integrators do not call update/get separately: the SGLD kernels fuse
 them into the parameter update (``gbsgmc_sgld_update``,
-``gbsgmc_sgld_glm_step``).  ``mass_matrix`` and ``fisher_information`` are
-not provided.
+``gbsgmc_sgld_glm_step``).
+
+``mass_matrix(diagonal=True)`` adapts the diagonal mass of the MH samplers
+(AMAGOLD, SGGMC) on the device with ``gbsgmc_mass_adapt``
+(adaption.py:296-368).  The dense variant and ``fisher_information`` are not
+provided.
 """
 
 from __future__ import annotations
@@ -64,9 +68,67 @@ def rms_prop() -> AdaptionStrategy:
   return AdaptionStrategy(init, update, get, "rms_prop")
 
 
-def mass_matrix(diagonal=True, burn_in=1000):
-  raise NotImplementedError("mass_matrix adaption is not part of the GPU "
-                            "hot path")
+class MassState(NamedTuple):
+  """Diagonal mass adaption state (adaption.py:321-340), fp32 device [P]
+  vectors.  ``mass`` is the mass the integrator kernels take (they use 1/M
+  and sqrt(M)); the adaption writes it with ``inv`` and ``sqrt``."""
+  iteration: int
+  mean: Any
+  ssq: Any
+  inv: Any
+  sqrt: Any
+  mass: Any
+  burn_in: int
+
+
+def _flat_device(tree):
+  import torch
+  if hasattr(tree, "is_cuda"):
+    t = tree.reshape(-1).to(torch.float32)
+    return t if t.is_cuda else t.cuda()
+  from . import util
+  flat, _ = util.ravel(tree)
+  return torch.from_numpy(flat).cuda()
+
+
+def mass_matrix(diagonal=True, burn_in=1000) -> AdaptionStrategy:
+  """Adapts the mass for the MH samplers from the accepted samples during
+  the first ``burn_in`` updates (adaption.py:296-368): a running mean and
+  sum of squared deviations, and at update ``burn_in`` the inverse mass
+  ssq / burn_in (the sample variance) and sqrt(burn_in / ssq).  Before then
+  the mass is the initial one: inverse ``init_cov`` (ones by default).
+  Only the diagonal form is provided."""
+  if not diagonal:
+    raise NotImplementedError("only the diagonal mass is adapted (the dense "
+                              "form needs an eigendecomposition of a P x P "
+                              "matrix and dense-mass integrator kernels)")
+
+  def init(sample, init_cov=None) -> MassState:
+    import torch
+    x = _flat_device(sample)
+    cov = torch.ones_like(x) if init_cov is None else _flat_device(init_cov)
+    if cov.numel() != x.numel():
+      raise ValueError(f"init_cov has {cov.numel()} entries, the sample "
+                       f"{x.numel()}")
+    return MassState(iteration=0, mean=torch.zeros_like(x),
+                     ssq=torch.zeros_like(x), inv=cov.clone(),
+                     sqrt=1.0 / cov.sqrt(), mass=1.0 / cov,
+                     burn_in=int(burn_in))
+
+  def update(state: MassState, sample, *args, **kwargs) -> MassState:
+    from . import _lib
+    del args, kwargs
+    x = _flat_device(sample)
+    it = state.iteration + 1
+    _lib.call("gbsgmc_mass_adapt", x.numel(), it, state.burn_in, _lib.ptr(x),
+              _lib.ptr(state.mean), _lib.ptr(state.ssq), _lib.ptr(state.inv),
+              _lib.ptr(state.sqrt), _lib.ptr(state.mass), _lib.stream_handle())
+    return state._replace(iteration=it)
+
+  def get(state: MassState) -> MassMatrix:
+    return MassMatrix(inv=state.inv, sqrt=state.sqrt)
+
+  return AdaptionStrategy(init, update, get, "mass_matrix")
 
 
 def fisher_information(minibatch_potential=None, diagonal=True):

@@ -418,7 +418,7 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
   h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
   block = min(rbf.cached_batches_count, DEFAULT_BLOCK_STEPS, max(iterations, 1))
   outbuf = None
-  if saving is not None and saving.kind != "device":
+  if saving is not None and saving.kind == "memory":
     outbuf = io.HostBuffers([((n_kept, len(states), W.shape[1]), np.float32),
                              ((n_kept, len(states)), np.float64)])
   res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,

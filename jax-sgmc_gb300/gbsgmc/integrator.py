@@ -118,6 +118,24 @@ def _flat_tree_like(tree, P, fill=None):
   return torch.from_numpy(flat).cuda()
 
 
+def _mass_vector(mass, const_mass, P):
+  """The diagonal mass M [P] the update kernels take (they use 1/M and
+  sqrt(M)): an adapted mass -- a flat device vector M, or a ``MassMatrix``
+  whose inverse is inverted -- else ``const_mass``, else None (unit mass)."""
+  import torch
+  if mass is None:
+    return _flat_tree_like(const_mass, P)
+  if isinstance(mass, MassMatrix):
+    inv = mass.inv
+    inv = inv.reshape(-1) if hasattr(inv, "is_cuda") else _flat_tree_like(inv, P)
+    return torch.reciprocal(_dev(inv).to(torch.float32))
+  m = _dev(mass.reshape(-1).to(torch.float32)) if hasattr(mass, "is_cuda") else \
+      _flat_tree_like(mass, P)
+  if m.numel() != P:
+    raise ValueError(f"mass has {m.numel()} entries, sample has {P}")
+  return m
+
+
 def _noise(seed, chain, buf=None):
   if buf is not None:
     return _lib.noise(seed, chain, noise_dev=buf, noise_stride=buf.numel())
@@ -144,6 +162,9 @@ def _eval(potential_fn, w, batch, info, want_grad=True):
 def langevin_diffusion(potential_fn, batch_fn, adaption: AdaptionStrategy = None,
                        noise_source: Callable = None):
   """SGLD with optional RMSprop (integrator.py:767-924)."""
+  if adaption is not None and getattr(adaption, "kind", "rms_prop") != "rms_prop":
+    raise NotImplementedError("langevin_diffusion adapts its manifold with "
+                              "rms_prop only")
   batch_init, batch_get, _ = batch_fn
 
   def init_fn(init_sample, key=0, adaption_kwargs=None, batch_kwargs=None,
@@ -221,7 +242,7 @@ def obabo(potential_fn, batch_fn, steps=10, friction=1.0, const_mass=None,
   def integrate(state: ObaboState, parameters, mass=None):
     x, p = state.positions, state.momentum
     P = x.numel()
-    m = _flat_tree_like(const_mass, P)
+    m = _mass_vector(mass, const_mass, P)
     data_state = state.data_state
     step = state.step
     pot = state.potential
@@ -338,9 +359,6 @@ def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,
   def init_fn(init_sample, key=None, batch_kwargs=None, init_model_state=None,
               mass=None):
     import torch
-    if mass is not None:
-      raise NotImplementedError("mass adaption is not supported; use "
-                                "const_mass")
     batch_kwargs = batch_kwargs or {}
     data_state = init_data(**batch_kwargs)
     w, tdef = _flat(init_sample)
@@ -354,7 +372,7 @@ def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,
       p = torch.empty(P, dtype=torch.float32, device="cuda")
       _lib.call("gbsgmc_philox_normal", seed, chain, 1, 0,
                 _lib.TAG_AMAGOLD_INIT, P, _lib.ptr(p), P, _lib.stream_handle())
-    m = _flat_tree_like(const_mass, P)
+    m = _mass_vector(mass, const_mass, P)
     if m is not None:
       p = p * m.sqrt()
     return LeapfrogState(
@@ -365,12 +383,9 @@ def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,
 
   def integrate(state: LeapfrogState, parameters, mass=None):
     import torch
-    if mass is not None:
-      raise NotImplementedError("mass adaption is not supported; use "
-                                "const_mass")
     x, p = state.positions, state.momentum
     P = x.numel()
-    m = _flat_tree_like(const_mass, P)
+    m = _mass_vector(mass, const_mass, P)
     step = state.step
     energy = torch.zeros(1, dtype=torch.float64, device="cuda")
 

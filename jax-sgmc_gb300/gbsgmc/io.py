@@ -8,7 +8,10 @@ host once at the end.  The result format is the reference's
 ``{'sample_count': S, 'samples': {'variables': pytree of [S, ...], ...}}``
 (io.py:768-769).  ``save(MemoryCollector())`` returns numpy arrays (written
 to ``save_dir/chain_{i}.npz`` when a directory is given); ``no_save()``
-returns device tensors.
+returns device tensors.  ``moments()`` keeps only the FP64 posterior mean
+and variance of each chain's samples, taken on the device
+(:class:`DeviceMoments`), and copies those to the host instead of the
+samples.
 """
 
 from __future__ import annotations
@@ -67,9 +70,94 @@ def no_save() -> Saving:
   return Saving("device", None)
 
 
+def moments() -> Saving:
+  """Returns, per chain, only the FP64 mean and (population) variance of the
+  accepted samples: ``{'sample_count': S, 'moments': {'mean': pytree,
+  'variance': pytree}, 'samples': {extras of [S]}}`` (numpy float64)."""
+  return Saving("moments", None)
+
+
+class DeviceMoments:
+  """Streaming FP64 moments of [chains, P] samples on the device
+  (``gbsgmc_moments_accumulate`` / ``gbsgmc_moments_finalize``): shifted
+  sums, with each parameter's first sample as the shift.  ``add`` takes
+  ``[K, chains, P]`` or ``[chains, P]`` fp32 device tensors whose last axis
+  is contiguous."""
+
+  def __init__(self, chains: int, P: int):
+    import torch
+    self.chains, self.P, self.count = int(chains), int(P), 0
+    self.shift = torch.empty((chains, P), dtype=torch.float32, device="cuda")
+    self.s1 = torch.zeros((chains, P), dtype=torch.float64, device="cuda")
+    self.s2 = torch.zeros((chains, P), dtype=torch.float64, device="cuda")
+
+  def add(self, samples) -> "DeviceMoments":
+    from . import _lib
+    import torch
+    if samples.dim() == 2:
+      samples = samples.unsqueeze(0)
+    K, C, P = samples.shape
+    if (C, P) != (self.chains, self.P):
+      raise ValueError(f"samples [{K}, {C}, {P}] do not match moments of "
+                       f"[{self.chains}, {self.P}]")
+    if samples.dtype != torch.float32 or not samples.is_cuda:
+      samples = samples.to(device="cuda", dtype=torch.float32)
+    if P > 1 and samples.stride(2) != 1:
+      samples = samples.contiguous()
+    if K == 0:
+      return self
+    _lib.call("gbsgmc_moments_accumulate", C, P, K, _lib.ptr(samples),
+              samples.stride(0), samples.stride(1), self.count,
+              _lib.ptr(self.shift), _lib.ptr(self.s1), _lib.ptr(self.s2),
+              _lib.stream_handle())
+    self.count += K
+    return self
+
+  def finalize(self):
+    """(mean, variance): fp64 device tensors [chains, P]."""
+    from . import _lib
+    import torch
+    if self.count == 0:
+      raise ValueError("no samples")
+    mean = torch.empty_like(self.s1)
+    var = torch.empty_like(self.s1)
+    _lib.call("gbsgmc_moments_finalize", self.chains, self.P, self.count,
+              _lib.ptr(self.shift), _lib.ptr(self.s1), _lib.ptr(self.s2),
+              _lib.ptr(mean), _lib.ptr(var), _lib.stream_handle())
+    return mean, var
+
+
+def _moment_results(count, variables, treedefs, extras, model_states):
+  """Per-chain moment results from a ``[count, C, P]`` device buffer."""
+  C, P = variables.shape[1], variables.shape[2]
+  if count == 0:
+    mean = var = np.full((C, P), np.nan)
+  else:
+    mean_d, var_d = DeviceMoments(C, P).add(variables[:count]).finalize()
+    mean, var = mean_d.cpu().numpy(), var_d.cpu().numpy()
+  out = []
+  for c in range(C):
+    samples = {k: (v[:, c].detach().cpu().numpy() if hasattr(v, "detach")
+                   else np.asarray(v)[:, c]) for k, v in extras.items()}
+    samples["model_state"] = model_states[c]
+    out.append({"sample_count": count,
+                "moments": {"mean": util.unravel(treedefs[c], mean[c]),
+                            "variance": util.unravel(treedefs[c], var[c])},
+                "samples": samples})
+  return out
+
+
 def postprocess(saving: Saving, count: int, variables, treedef, extras: dict,
                 model_state=None) -> dict:
   """Builds one chain's result dict from its device sample buffers."""
+  if saving is not None and saving.kind == "moments":
+    import torch
+    v = variables if hasattr(variables, "is_cuda") else torch.from_numpy(
+        np.ascontiguousarray(variables))
+    ext = {k: (x.reshape(-1, 1) if hasattr(x, "reshape") else
+               np.asarray(x).reshape(-1, 1)) for k, x in extras.items()}
+    return _moment_results(count, v[:, None, :], [treedef], ext,
+                           [model_state])[0]
   if saving is None or saving.kind == "device":
     # Device results: one torch view per leaf of the [count, P] buffer.
     leaves, o = [], 0
@@ -125,6 +213,8 @@ def postprocess_chains(saving: Saving, count: int, variables, treedefs,
   one ``[count, C]`` per extra, e.g. from :class:`HostBuffers`)."""
   import torch
   C = variables.shape[1]
+  if saving is not None and saving.kind == "moments":
+    return _moment_results(count, variables, treedefs, extras, model_states)
   if saving is None or saving.kind == "device":
     return [postprocess(saving, count, variables[:, c], treedefs[c],
                         {k: v[:, c] for k, v in extras.items()},

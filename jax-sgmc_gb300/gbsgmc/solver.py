@@ -124,34 +124,50 @@ def _mh_solver(kind, integrator, full_potential_fn, full_data_map,
   init_integrator, update_integrator, get_integrator = integrator
   init_full_data, full_data_map_fn, _ = full_data_map
   if mass_adaption is not None:
-    raise NotImplementedError("mass adaption is not supported; pass a "
-                              "constant mass to the integrator")
+    init_mass, update_mass, get_mass = tuple(mass_adaption)[:3]
+
+  def current_mass(mass_state):
+    # The device adaption keeps the kernels' mass vector itself; any other
+    # adaption triplet gives a MassMatrix.
+    m = getattr(mass_state, "mass", None)
+    return m if m is not None else get_mass(mass_state)
 
   def init(init_sample, key=0, initial_mass=None, full_data_kwargs=None,
            **kwargs):
     import torch
-    if initial_mass is not None:
-      raise NotImplementedError("mass adaption is not supported")
+    mass_state = mass = None
+    if mass_adaption is not None:
+      mass_state = init_mass(init_sample, initial_mass)
+      mass = current_mass(mass_state)
+    elif initial_mass is not None:
+      raise ValueError("initial_mass needs a mass_adaption")
     full_data_state = init_full_data(**(full_data_kwargs or {}))
     U, (full_data_state, model_state) = full_potential_fn(
         init_sample, full_data_state, full_data_map_fn,
         state=kwargs.get("init_model_state"))
     kwargs["init_model_state"] = model_state
     seed = int(np.asarray(key).ravel()[-1]) if key is not None else 0
+    if kind == _lib.MH_AMAGOLD and mass is not None:
+      # The initial momentum is drawn with the initial mass (solver.py:352).
+      kwargs["mass"] = mass
     integrator_state = init_integrator(init_sample, key=(seed, 1), **kwargs)
     return MHState(integrator_state=integrator_state,
                    potential=U.reshape(1).to(torch.float64).clone(),
                    full_data_state=full_data_state, key=seed,
                    acceptance_ratio=torch.zeros(1, dtype=torch.float64,
                                                 device="cuda"),
-                   step_size=0.0, mh_step=0)
+                   step_size=0.0, mh_step=0, mass_state=mass_state)
 
   def update(state: MHState, schedule):
     import torch
     ist = state.integrator_state
     x_old = ist.positions.clone()
     p_old = ist.momentum.clone()
-    proposal = update_integrator(ist, schedule)
+    if mass_adaption is not None:
+      proposal = update_integrator(ist, schedule,
+                                   mass=current_mass(state.mass_state))
+    else:
+      proposal = update_integrator(ist, schedule)
     U_new, (full_data_state, model_state) = full_potential_fn(
         proposal.positions, state.full_data_state, full_data_map_fn,
         state=proposal.model_state)
@@ -183,11 +199,16 @@ def _mh_solver(kind, integrator, full_potential_fn, full_data_map,
       new_ist = proposal._replace(
           kinetic_energy_start=torch.zeros(1, dtype=torch.float64, device="cuda"),
           kinetic_energy_end=torch.zeros(1, dtype=torch.float64, device="cuda"))
+    mass_state = state.mass_state
+    if mass_adaption is not None:
+      # Adapted on the sample the correction kept (solver.py:409-412).
+      mass_state = update_mass(mass_state, new_ist.positions)
     new_state = state._replace(integrator_state=new_ist, potential=U_keep,
                                full_data_state=full_data_state,
                                acceptance_ratio=ratio,
                                step_size=float(schedule.step_size),
-                               mh_step=state.mh_step + 1)
+                               mh_step=state.mh_step + 1,
+                               mass_state=mass_state)
     return new_state, {"acceptance_ratio": ratio}
 
   def get(state: MHState):

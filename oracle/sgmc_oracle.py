@@ -630,6 +630,53 @@ def resgld_exchange_adjacent(U, var, ssq, T, F, round_, u):
 
 
 # ---------------------------------------------------------------------------
+# Sample statistics
+# ---------------------------------------------------------------------------
+
+
+class MassAdaption(NamedTuple):
+  iteration: int
+  mean: np.ndarray
+  ssq: np.ndarray
+  inv: np.ndarray
+  sqrt: np.ndarray
+
+
+def mass_adapt_init(sample, init_cov=None) -> MassAdaption:
+  """mass_matrix(diagonal=True) init (jax_sgmc/adaption.py:321-340), fp32."""
+  x = np.asarray(sample, np.float32)
+  cov = np.ones_like(x) if init_cov is None else np.asarray(init_cov, np.float32)
+  return MassAdaption(0, np.zeros_like(x), np.zeros_like(x), cov.copy(),
+                      (np.float32(1) / np.sqrt(cov)).astype(np.float32))
+
+
+def mass_adapt_update(state: MassAdaption, sample, burn_in) -> MassAdaption:
+  """One update (jax_sgmc/adaption.py:342-362) with the matrix computed at
+  iteration == burn_in (:309-319), fp32 in the reference's operation order:
+  the int32 iteration divides as float32 ((i - 1) / i, 1 / i), products and
+  sums unfused."""
+  x = np.asarray(sample, np.float32)
+  it = state.iteration + 1
+  fi = np.float32(it)
+  a = np.float32(it - 1) / fi
+  b = np.float32(1) / fi
+  mean = (a * state.mean + b * x).astype(np.float32)
+  ssq = (state.ssq + (x - state.mean) * (x - mean)).astype(np.float32)
+  inv, sq = state.inv, state.sqrt
+  if it == burn_in:
+    inv = (ssq / fi).astype(np.float32)
+    sq = np.sqrt(fi / ssq).astype(np.float32)
+  return MassAdaption(it, mean, ssq, inv, sq)
+
+
+def sample_moments(samples):
+  """FP64 mean and population variance over the first axis (the posterior
+  moments of kept samples)."""
+  a = np.asarray(samples, np.float64)
+  return a.mean(axis=0), a.var(axis=0)
+
+
+# ---------------------------------------------------------------------------
 # Scheduler
 # ---------------------------------------------------------------------------
 

@@ -295,5 +295,17 @@ def test_unported_presets_raise():
   from gbsgmc import adaption, integrator
   with pytest.raises(NotImplementedError):
     adaption.fisher_information()
+  with pytest.raises(NotImplementedError):   # dense mass adaption
+    adaption.mass_matrix(diagonal=False)
+  with pytest.raises(NotImplementedError):   # langevin adapts with rms_prop only
+    integrator.langevin_diffusion(None, (None, None, None),
+                                  adaption=adaption.mass_matrix())
   with pytest.raises(NotImplementedError):   # per-parameter friction
     integrator.reversible_leapfrog(None, (None, None, None), friction=[0.1, 0.2])
+
+
+def test_moments_saving_and_mass_adaption_strategy_shapes():
+  from gbsgmc import adaption, io
+  assert io.moments().kind == "moments"
+  strat = adaption.mass_matrix(burn_in=7)
+  assert strat.kind == "mass_matrix" and len(tuple(strat)[:3]) == 3

@@ -215,3 +215,34 @@ def test_reversible_leapfrog_oracle_is_time_reversible():
   assert O.mh_log_alpha("sggmc", 1.0, 3.0, 0.0, 0.5, 1.0, 2.0) == -1.25
   u = O.mh_uniform(7, 3, 11)
   assert 0.0 < u < 1.0 and u != O.mh_uniform(7, 3, 12)
+
+
+def test_mass_adaption_oracle_is_the_sample_variance():
+  """mass_matrix(diagonal=True) (adaption.py:296-368): after burn_in
+  updates the inverse mass is the population variance of the samples seen
+  and its root's reciprocal sqrt(burn_in / ssq); before burn-in and after it
+  the matrix does not move."""
+  rng = np.random.default_rng(2)
+  B, P = 40, 9
+  xs = (rng.normal(size=(B + 5, P)) * rng.uniform(0.2, 4.0, size=P) + 3.0).astype(
+      np.float32)
+  st = O.mass_adapt_init(xs[0])
+  for k in range(B + 5):
+    st = O.mass_adapt_update(st, xs[k], B)
+    if k + 1 < B:
+      np.testing.assert_array_equal(st.inv, np.ones(P, np.float32))
+    if k + 1 == B:
+      at_burn_in = st
+  assert st.iteration == B + 5
+  np.testing.assert_array_equal(st.inv, at_burn_in.inv)
+  np.testing.assert_allclose(at_burn_in.inv, xs[:B].astype(np.float64).var(axis=0),
+                             rtol=1e-4)
+  np.testing.assert_allclose(at_burn_in.sqrt, 1.0 / np.sqrt(at_burn_in.inv), rtol=1e-6)
+  np.testing.assert_allclose(st.mean, xs.astype(np.float64).mean(axis=0), rtol=1e-5)
+
+
+def test_sample_moments_oracle():
+  a = np.arange(12, dtype=np.float32).reshape(4, 3)
+  m, v = O.sample_moments(a)
+  np.testing.assert_array_equal(m, [4.5, 5.5, 6.5])
+  np.testing.assert_array_equal(v, [11.25, 11.25, 11.25])
