@@ -118,10 +118,12 @@ __global__ void mirror_kernel(int64_t P, const float* x, Fuse f) {
   fuse_finish(f, c, sq);
 }
 
-__global__ void sgld_update_kernel(int chains, int64_t P, float* x,
-                                   const float* g, float* v, float alpha,
-                                   float lmbd, Sched sched, Noise noise,
-                                   float* samples, Fuse fz) {
+// Four resident blocks per SM (64 registers instead of 72): more loads in
+// flight for this memory-bound stream (measured 1 % faster in the reSGLD
+// plan; the OBABO kernels measured no gain from the same bound).
+__global__ void __launch_bounds__(kThreads, 4)
+sgld_update_kernel(int chains, int64_t P, float* x, const float* g, float* v, float alpha,
+                   float lmbd, Sched sched, Noise noise, float* samples, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const float h = sched.step_size(k);
@@ -209,10 +211,9 @@ __device__ __forceinline__ void obabo_second_elem(const ObaboCoef& q, float mi, 
   p = __fmaf_rn(q.keep, pj, __fmul_rn(q.inject, __fmul_rn(ms, xi)));
 }
 
-__global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
-                                   const float* g1, const float* mass,
-                                   float friction, double* ke_start,
-                                   Sched sched, Noise noise, Fuse fz) {
+__global__ void obabo_first_kernel(
+    int chains, int64_t P, float* x, float* p, const float* g1, const float* mass,
+    float friction, double* ke_start, Sched sched, Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const ObaboCoef qc = obabo_coef(sched, k, c, friction);
@@ -245,10 +246,9 @@ __global__ void obabo_first_kernel(int chains, int64_t P, float* x, float* p,
   fuse_finish(fz, c, sq);
 }
 
-__global__ void obabo_second_kernel(int chains, int64_t P, const float* x, float* p,
-                                    const float* g2, const float* mass,
-                                    float friction, double* ke_end,
-                                    Sched sched, Noise noise, Fuse fz) {
+__global__ void obabo_second_kernel(
+    int chains, int64_t P, const float* x, float* p, const float* g2, const float* mass,
+    float friction, double* ke_end, Sched sched, Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const ObaboCoef qc = obabo_coef(sched, k, c, friction);
@@ -282,11 +282,10 @@ __global__ void obabo_second_kernel(int chains, int64_t P, const float* x, float
 // (their gradients g2 of step k and g1 of step k + 1 are both taken at the
 // same positions): per parameter exactly the operations of
 // obabo_second_kernel (step k) then obabo_first_kernel (step k + 1).
-__global__ void obabo_second_first_kernel(int chains, int64_t P, float* x, float* p,
-                                          const float* g2, const float* g1,
-                                          const float* mass, float friction,
-                                          double* ke_end, double* ke_start, Sched sched,
-                                          Noise noise, Fuse fz) {
+__global__ void obabo_second_first_kernel(
+    int chains, int64_t P, float* x, float* p, const float* g2, const float* g1,
+    const float* mass, float friction, double* ke_end, double* ke_start, Sched sched,
+    Noise noise, Fuse fz) {
   const int c = blockIdx.y;
   const int64_t k = sched.step();
   const ObaboCoef q2 = obabo_coef(sched, k, c, friction);
