@@ -575,12 +575,15 @@ int gbsgmc_sgld_glm_step_noalloc(const gbsgmc_glm* model, int chains, int n,
 typedef struct gbsgmc_plan gbsgmc_plan;
 
 /* Index source of a plan: numpy-identical PCG64 streams (pcg_dev != NULL,
- * advanced in place) or Philox indices from index_seed. */
+ * advanced in place), Philox indices from index_seed, or, with external != 0,
+ * indices the caller supplies before each run of at most one block
+ * (gbsgmc_plan_set_indices; e.g. the shuffled streams of
+ * jax_sgmc/data/numpy_loader.py:391-460, drawn by the host loader). */
 typedef struct gbsgmc_index_src {
   gbsgmc_pcg64* pcg_dev;
   uint64_t index_seed;
   int chain_base;
-  int _pad;
+  int external;
 } gbsgmc_index_src;
 
 /* Builds a plan that runs SGLD(+RMSprop) on a GLM for `chains` chains: per
@@ -716,6 +719,16 @@ int gbsgmc_plan_launch_shape(const gbsgmc_plan* plan, int* slices,
 
 /* Kernel launches one plan_run of `steps` steps performs (for accounting). */
 int64_t gbsgmc_plan_launches(const gbsgmc_plan* plan, int64_t steps);
+
+/* Plans with an external index source (GLM SGLD, network and GLM OBABO /
+ * SGHMC / SGLD plans): copies the indices of the next `steps` steps
+ * (1 <= steps <= block_steps) into the plan, stream-ordered on `stream`.
+ * src (host, pinned or pageable, or device) is [steps, chains, k * n]
+ * int32, k the minibatches of one step (2 for OBABO, else 1), in the order
+ * the chain's loader hands them out.  The next gbsgmc_plan_run on `stream`
+ * must cover at most `steps` steps. */
+int gbsgmc_plan_set_indices(gbsgmc_plan* plan, const int32_t* src, int steps,
+                            gbsgmc_stream_t stream);
 
 /* Releases the plan's graphs, stream and workspace (synchronises the plan's
  * internal stream first). */

@@ -72,6 +72,16 @@ struct NetPlan final : gbsgmc_plan {
   int enqueue_obabo(int g, const UpdateFusion& moving, const UpdateFusion& last,
                     cudaStream_t s);
 
+  // With an external index source the caller writes the block's indices
+  // (gbsgmc_plan_set_indices); until then the buffer holds index 0.
+  int setup_external(const char* what) {
+    if (!isrc.external) return GBSGMC_OK;
+    ext_idx = idx;
+    ext_per_step = static_cast<int64_t>(chains) * draws() * n;
+    return cuda_err(cudaMemsetAsync(idx, 0, sizeof(int32_t) * G * ext_per_step, stream),
+                    what);
+  }
+
   // The gradient buffers: OBABO keeps two, because its second gradient of
   // step j and its first gradient of step j + 1 feed one update pass.
   int alloc_grads(const char* what) {
@@ -88,8 +98,9 @@ struct NetPlan final : gbsgmc_plan {
 
   int64_t launches_per_block(int g) const override {
     // Kernels of one value-and-gradient call are counted by the caller.
-    // Every block: the index draw, the step counter and, fused, the mirror.
-    const int64_t fixed = fused ? 3 : 2;
+    // Every block: the index draw (unless external), the step counter and,
+    // fused, the mirror.
+    const int64_t fixed = (fused ? 3 : 2) - (isrc.external ? 1 : 0);
     switch (integ.kind) {
       case GBSGMC_INTEGRATOR_OBABO: return fixed + 2 + static_cast<int64_t>(g);
       case GBSGMC_INTEGRATOR_SGHMC:
@@ -103,7 +114,9 @@ struct NetPlan final : gbsgmc_plan {
     const int per = draws() * n;
     const int64_t cn = static_cast<int64_t>(chains) * per;
     int rc;
-    if (isrc.pcg_dev != nullptr) {
+    if (isrc.external) {
+      rc = GBSGMC_OK;  // written by gbsgmc_plan_set_indices
+    } else if (isrc.pcg_dev != nullptr) {
       rc = gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows, static_cast<int64_t>(g) * per,
                                    per, idx, per, cn, status, s);
     } else {
@@ -148,7 +161,9 @@ int NetPlan::enqueue_fused(int g, cudaStream_t s) {
   const int per = draws() * n;
   const int64_t cn = static_cast<int64_t>(chains) * per;
   int rc;
-  if (isrc.pcg_dev != nullptr) {
+  if (isrc.external) {
+    rc = GBSGMC_OK;  // written by gbsgmc_plan_set_indices
+  } else if (isrc.pcg_dev != nullptr) {
     rc = gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows, static_cast<int64_t>(g) * per,
                                  per, idx, per, cn, status, s);
   } else {
@@ -402,6 +417,7 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
                                          nullptr, var, wsp, ws, status_dev, s);
       };
     }
+    if ((rc = p->setup_external("mlp_plan_create: index memset"))) break;
     rc = plan_capture(p);
   } while (false);
   if (rc != GBSGMC_OK) {
@@ -462,6 +478,7 @@ extern "C" int gbsgmc_cnn_plan_create(gbsgmc_plan** out, const gbsgmc_cnn* model
       return gbsgmc_cnn_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
                                        nullptr, var, wsp, ws, status_dev, s);
     };
+    if ((rc = p->setup_external("cnn_plan_create: index memset"))) break;
     rc = plan_capture(p);
   } while (false);
   if (rc != GBSGMC_OK) {
@@ -493,6 +510,9 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
   if (sched->keep_slot_dev != nullptr)
     return set_error(GBSGMC_ERR_UNSUPPORTED,
                      "mlp_resgld_plan_create: samples are collected by the caller");
+  if (isrc->external)
+    return set_error(GBSGMC_ERR_UNSUPPORTED,
+                     "mlp_resgld_plan_create: external index sources");
   const size_t ws = gbsgmc_mlp_workspace_bytes(model, replicas, n_max);
   if (ws == 0)
     return set_error(GBSGMC_ERR_SHAPE, "mlp_resgld_plan_create: unsupported shape (n_max %% 128)");
@@ -604,6 +624,7 @@ extern "C" int gbsgmc_glm_plan_create(gbsgmc_plan** out, const gbsgmc_glm* model
       return gbsgmc_glm_value_and_grad(&m, chains, n, idx, stride, nullptr, x, U, grad,
                                        nullptr, var, wsp, ws, status_dev, s);
     };
+    if ((rc = p->setup_external("glm_plan_create: index memset"))) break;
     rc = plan_capture(p);
   } while (false);
   if (rc != GBSGMC_OK) {

@@ -99,7 +99,7 @@ struct GlmPlan final : gbsgmc_plan {
   int pipelined_block(int parity, bool prefetch, cudaStream_t s);
   int setup_pipeline();
   int64_t launches_per_block(int g) const override {
-    return tune.multistep ? 3 : g + 2;
+    return (tune.multistep ? 3 : g + 2) - (isrc.external ? 1 : 0);
   }
 };
 
@@ -182,6 +182,7 @@ int GlmPlan::draw(int g, int32_t* buf, cudaStream_t s) {
   using namespace gbsgmc;
   const int64_t cn = static_cast<int64_t>(chains) * n;
   const int64_t rows = model.n_rows > 0 ? model.n_rows : model.n_obs;
+  if (isrc.external) return GBSGMC_OK;  // written by gbsgmc_plan_set_indices
   if (isrc.pcg_dev != nullptr)
     return gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows,
                                    static_cast<int64_t>(g) * n, n, buf, n, cn,
@@ -501,6 +502,14 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
     if ((rc = cuda_err(cudaMemsetAsync(p->ws, 0, p->ws_size, p->stream),
                        "plan_create: memset")))
       break;
+    if (p->isrc.external) {
+      p->ext_idx = p->idx;
+      p->ext_per_step = static_cast<int64_t>(chains) * n;
+      if ((rc = cuda_err(cudaMemsetAsync(p->idx, 0, sizeof(int32_t) * block_steps *
+                                                        p->ext_per_step, p->stream),
+                         "plan_create: memset")))
+        break;
+    }
     if ((rc = glm_prepare())) break;
     if ((rc = autotune(p))) break;
     // GBSGMC_GLM_MULTISTEP=1/0 forces one launch per block of steps or one
@@ -548,6 +557,21 @@ extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
   if ((rc = cuda_err(cudaEventRecord(p->ev_out, p->stream), "plan_run: record")))
     return rc;
   return cuda_err(cudaStreamWaitEvent(us, p->ev_out, 0), "plan_run: wait");
+}
+
+extern "C" int gbsgmc_plan_set_indices(gbsgmc_plan* p, const int32_t* src, int steps,
+                                       gbsgmc_stream_t stream) {
+  if (p == nullptr || src == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "plan_set_indices: null argument");
+  if (p->ext_idx == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "plan_set_indices: the plan draws its own indices");
+  if (steps < 1 || steps > p->G)
+    return set_error(GBSGMC_ERR_ARG, "plan_set_indices: steps %d outside [1, %d]", steps,
+                     p->G);
+  const size_t bytes = sizeof(int32_t) * static_cast<size_t>(steps) * p->ext_per_step;
+  return cuda_err(cudaMemcpyAsync(p->ext_idx, src, bytes, cudaMemcpyDefault,
+                                  static_cast<cudaStream_t>(stream)),
+                  "plan_set_indices: copy");
 }
 
 extern "C" int gbsgmc_plan_launch_shape(const gbsgmc_plan* p, int* slices,

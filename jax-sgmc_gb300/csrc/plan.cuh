@@ -30,6 +30,10 @@ struct gbsgmc_plan {
 
   int G = 0;
   bool use_graph = true;
+  // External index source: the plan's index buffer [G, ext_per_step] int32
+  // that gbsgmc_plan_set_indices fills (null when the plan draws its own).
+  int32_t* ext_idx = nullptr;
+  int64_t ext_per_step = 0;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;

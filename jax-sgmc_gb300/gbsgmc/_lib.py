@@ -106,7 +106,7 @@ class Noise(C.Structure):
 
 class IndexSrc(C.Structure):
   _fields_ = [("pcg_dev", C.c_void_p), ("index_seed", C.c_uint64),
-              ("chain_base", C.c_int), ("_pad", C.c_int)]
+              ("chain_base", C.c_int), ("external", C.c_int)]
 
 
 _vp, _i, _i64, _u64, _f, _d, _sz = (C.c_void_p, C.c_int, C.c_int64,
@@ -200,6 +200,7 @@ SIGNATURES = {
                                            _vp, _i, _vp]),
     "gbsgmc_plan_run": (_i, [_vp, _i64, _i64, _vp]),
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
+    "gbsgmc_plan_set_indices": (_i, [_vp, _vp, _i, _vp]),
     "gbsgmc_plan_launch_shape": (_i, [_vp, _P(_i), _P(_i), _P(_i), _P(_i), _P(_i),
                                       _P(_i)]),
     "gbsgmc_plan_destroy": (_i, [_vp]),

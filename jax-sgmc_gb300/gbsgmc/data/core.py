@@ -353,6 +353,70 @@ class RandomBatchFn:
     return self._fn(data_state, information, device_count)
 
 
+class ShuffledFeed:
+  """Minibatch indices of C shuffled host pipelines (shuffle=True,
+  in_epochs=False), step by step, for a plan with an external index source.
+
+  Chain c's batches come in the order its own batch function would hand
+  them out: the rest of its device cache, then cache-sized chunks from the
+  loader (``take_shuffled``: one chunk when the previous one is used up,
+  as the batch function refills).  :meth:`next` returns ``[steps, C,
+  k * mb]`` int32 (k minibatches per step).  The loader's chain states
+  advance exactly as under the per-chain path.  The chains' chunks are
+  drawn on a thread pool: numpy releases the GIL while it shuffles."""
+
+  def __init__(self, loader, data_states, per_step=1):
+    import concurrent.futures as cf
+    import os
+    self.loader = loader
+    self.states = list(data_states)
+    self.k = int(per_step)
+    self.cache = int(self.states[0].cached_batches_count)
+    self.chunk = [ds.cached_batches.cpu().numpy() for ds in self.states]
+    self.pos = [int(ds.current_line) for ds in self.states]
+    self.mb = self.chunk[0].shape[1]
+    self._pool = cf.ThreadPoolExecutor(max(1, min(len(self.states),
+                                                   os.cpu_count() or 1)))
+
+  @staticmethod
+  def qualifies(loader, data_states) -> bool:
+    chains = getattr(loader, "_chains", None)
+    if chains is None or not data_states:
+      return False
+    for ds in data_states:
+      ch = chains[ds.chain_id]
+      if (ds.state is not None or ds.cached_batches is None
+          or not ch.get("shuffle") or ch.get("in_epochs")):
+        return False
+    return len({int(ds.cached_batches_count) for ds in data_states}) == 1
+
+  def _take(self, c, count):
+    out = []
+    while count > 0:
+      if self.pos[c] == self.cache:
+        self.chunk[c] = self.loader.take_shuffled(self.states[c].chain_id,
+                                                  self.cache)
+        self.pos[c] = 0
+      m = min(count, self.cache - self.pos[c])
+      out.append(self.chunk[c][self.pos[c]:self.pos[c] + m])
+      self.pos[c] += m
+      count -= m
+    return np.concatenate(out).reshape(-1, self.k * self.mb)
+
+  def next(self, steps, out=None):
+    """Indices of the next ``steps`` steps of every chain, written into
+    ``out`` ([>= steps, C, k * mb] int32) when given."""
+    parts = list(self._pool.map(lambda c: self._take(c, steps * self.k),
+                                range(len(self.states))))
+    if out is None:
+      out = np.empty((steps, len(parts), self.k * self.mb), np.int32)
+    np.stack(parts, axis=1, out=out[:steps])
+    return out[:steps]
+
+  def close(self):
+    self._pool.shutdown(wait=True)
+
+
 def _random_reference_data_host(loader, cache, mb_size):
   import torch
   N = loader.static_information["observation_count"]

@@ -221,6 +221,50 @@ class NumpyDataLoader(NumpyBase, HostDataLoader):
     chain['remaining_samples'] -= chain['mb_size']
     return selections, mask
 
+  def take_shuffled(self, chain_id: int, count: int) -> onp.ndarray:
+    """``count`` consecutive minibatches ``[count, mb_size]`` of a shuffled
+    pipeline (shuffle=True, in_epochs=False), leaving the chain's state --
+    generator, ring, draws, remaining -- exactly as ``count`` calls of
+    ``_shuffle_indices`` would.
+
+    Those calls hand out the concatenation of successive permutations
+    ``rng.choice(arange(N), N, replace=False)`` in pieces of mb: the ring of
+    (floor(N/mb) + 2) mb >= N + mb entries never overwrites an unread entry,
+    a permutation is appended at the write head whenever fewer than mb
+    entries are unread, and after `count` calls ceil((count mb - r0) / N)
+    permutations have been appended (r0 the unread entries before).  So the
+    batches are the unread entries followed by those permutations, cut into
+    pieces of mb, and the ring receives each permutation at the position
+    the per-call code would write it to."""
+    chain = self._chains[chain_id]
+    if not chain['shuffle'] or chain['in_epochs'] or chain['type'] != 'random':
+      raise ValueError("take_shuffled needs a shuffle=True, in_epochs=False "
+                       "random pipeline")
+    N, mb = self._observation_count, chain['mb_size']
+    ceil_draws = N // mb + 2
+    R = ceil_draws * mb
+    count = int(count)
+    if count <= 0:
+      return onp.empty((0, mb), dtype=onp.int_)
+    r0 = chain['remaining_samples']
+    ring = chain['random_indices']
+    d0 = chain['draws'] if ring is not None else 0
+    need = count * mb
+    k = max(0, -((r0 - need) // N))   # ceil((need - r0) / N), at least 0
+    if ring is None:
+      ring = onp.zeros(R, dtype=onp.int_)
+      chain['random_indices'] = ring
+    parts = [ring[(d0 * mb + onp.arange(r0)) % R]]
+    head = d0 * mb + r0
+    for t in range(k):
+      perm = chain['rng'].choice(onp.arange(0, N), size=N, replace=False)
+      ring[(head + t * N + onp.arange(N)) % R] = perm
+      parts.append(perm)
+    stream = onp.concatenate(parts)[:need]
+    chain['draws'] = (d0 + count) % ceil_draws
+    chain['remaining_samples'] = r0 + k * N - need
+    return stream.reshape(count, mb)
+
   def _shuffle_in_epochs(self, chain):
     ceil_draws = math.ceil(self._observation_count / chain['mb_size'])
     if chain['draws'] == ceil_draws:

@@ -16,7 +16,7 @@ from typing import List, NamedTuple
 import numpy as np
 
 from . import _lib, io, scheduler as sched_mod
-from .data.core import RandomBatchFn
+from .data.core import RandomBatchFn, ShuffledFeed
 
 DEFAULT_BLOCK_STEPS = 50
 
@@ -35,15 +35,63 @@ class SgldRun(NamedTuple):
   launches: int
 
 
+class _ExternalIndices:
+  """Feeds a plan with an external index source: before each run of at
+  most one block, the next steps' indices from a :class:`ShuffledFeed` go
+  through one of two pinned host buffers into the plan
+  (``gbsgmc_plan_set_indices``), so that the host prepares block b + 1
+  while the GPU runs block b."""
+
+  def __init__(self, feed, G, C, per_chain_step):
+    import torch
+    self.feed, self.G = feed, int(G)
+    self.bufs = [torch.empty((self.G, C, per_chain_step), dtype=torch.int32,
+                             pin_memory=True) for _ in range(2)]
+    self.events = [None, None]
+    self.turn = 0
+
+  def run(self, handle, first_step, steps, step_multiple=1):
+    import torch
+    done = 0
+    while done < steps:
+      g = min(self.G, steps - done)
+      i = self.turn
+      self.turn ^= 1
+      if self.events[i] is not None:
+        self.events[i].synchronize()   # its previous copy has left the buffer
+      idx = self.feed.next(g, out=self.bufs[i].numpy())
+      _lib.call("gbsgmc_plan_set_indices", handle, _lib.ptr(self.bufs[i]), g,
+                _lib.stream_handle())
+      ev = torch.cuda.Event()
+      ev.record()
+      self.events[i] = ev
+      _lib.call("gbsgmc_plan_run", handle, int(first_step + done), g,
+                _lib.stream_handle())
+      done += g
+      del idx
+
+
+def _plan_launches(handle, steps, external=None) -> int:
+  """Launches of ``steps`` steps run by one plan_run, or, with external
+  indices, by one plan_run per block."""
+  f = _lib.load().gbsgmc_plan_launches
+  if external is None:
+    return int(f(handle, int(steps)))
+  full, rem = divmod(int(steps), external.G)
+  return full * int(f(handle, external.G)) + (int(f(handle, rem)) if rem else 0)
+
+
 class SgldGlmPlan:
   """Owns a ``gbsgmc_plan`` and the device buffers baked into it."""
 
   def __init__(self, potential, dataset, W, V, alpha, lmbd, n, h_tab, t_tab,
                keep_tab, n_kept, index_src, noise_seed, chain_base=0,
-               block_steps=DEFAULT_BLOCK_STEPS, noise_dev=None):
+               block_steps=DEFAULT_BLOCK_STEPS, noise_dev=None, feed=None):
     import torch
     self.potential = potential
     C, d = W.shape
+    self.external = _ExternalIndices(feed, block_steps, C, n) \
+        if index_src.external else None
     self.C, self.d, self.n = C, d, n
     self.model, self._keep_alive = potential.model(dataset)
     self.W = W
@@ -71,6 +119,9 @@ class SgldGlmPlan:
     self.handle = handle
 
   def run(self, first_step, steps):
+    if self.external is not None:
+      self.external.run(self.handle, int(first_step), int(steps))
+      return
     _lib.call("gbsgmc_plan_run", self.handle, int(first_step), int(steps),
               _lib.stream_handle())
 
@@ -84,7 +135,7 @@ class SgldGlmPlan:
     return s.value, r.value, w.value, f.value, y.value, k.value
 
   def launches(self, steps) -> int:
-    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps)))
+    return _plan_launches(self.handle, steps, self.external)
 
   def check_status(self):
     code = int(self.status.item())
@@ -104,17 +155,20 @@ class SgldGlmPlan:
 
 
 class IndexSource:
-  """PCG64 streams (device [C] gbsgmc_pcg64, advanced in place) or Philox."""
+  """PCG64 streams (device [C] gbsgmc_pcg64, advanced in place), Philox, or
+  ``external``: indices the host supplies block by block
+  (:class:`ShuffledFeed`)."""
 
-  def __init__(self, pcg=None, seed=0, chain_base=0):
+  def __init__(self, pcg=None, seed=0, chain_base=0, external=False):
     self.pcg = pcg
+    self.external = bool(external)
     self.struct = _lib.IndexSrc(_lib.ptr(pcg), int(seed) & (2**64 - 1),
-                                int(chain_base), 0)
+                                int(chain_base), int(self.external))
 
 
 def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
                  index_src, noise_seed=0, chain_base=0, alpha=0.9, lmbd=1e-5,
-                 block_steps=None) -> SgldRun:
+                 block_steps=None, feed=None) -> SgldRun:
   """Runs ``iterations`` fused SGLD steps for all chains (W, V updated in
   place) and returns the final state and the kept samples."""
   import torch
@@ -125,7 +179,7 @@ def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
   k_tab = torch.from_numpy(np.asarray(keep, np.int32)).cuda()
   plan = SgldGlmPlan(potential, dataset, W, V, alpha, lmbd, n, h_tab, t_tab,
                      k_tab, n_kept, index_src, noise_seed, chain_base,
-                     block_steps)
+                     block_steps, feed=feed)
   try:
     plan.run(0, iterations)
     plan.check_status()
@@ -148,7 +202,7 @@ class NetPlan:
   def __init__(self, potential, dataset, X, AUX, n, kind, h_tab, t_tab,
                index_src, noise_seed, chain_base=0, block_steps=None,
                friction=0.0, leapfrog_steps=1, alpha=0.9, lmbd=1e-5,
-               mass=None, observation_count=None):
+               mass=None, observation_count=None, feed=None):
     import torch
     C, P = X.shape
     self.C, self.P, self.n, self.kind = C, P, n, kind
@@ -166,6 +220,9 @@ class NetPlan:
     if block_steps is None:
       block_steps = DEFAULT_BLOCK_STEPS
     block_steps = max(lf, block_steps // lf * lf)
+    draws = 2 if kind == "obabo" else 1
+    self.external = _ExternalIndices(feed, block_steps, C, draws * n) \
+        if index_src.external else None
     self.integ = _lib.Integrator(self.KINDS[kind], lf, float(friction),
                                  float(alpha), float(lmbd), 0, _lib.ptr(mass))
     handle = _lib.C.c_void_p()
@@ -182,6 +239,9 @@ class NetPlan:
     self.handle = handle
 
   def run(self, first_step, steps):
+    if self.external is not None:
+      self.external.run(self.handle, int(first_step), int(steps))
+      return
     _lib.call("gbsgmc_plan_run", self.handle, int(first_step), int(steps),
               _lib.stream_handle())
 
@@ -190,8 +250,7 @@ class NetPlan:
     included)."""
     per_grad = self.launches_per_gradient
     grads = {"obabo": 2}.get(self.kind, 1) * int(steps)
-    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps))) + \
-        per_grad * grads
+    return _plan_launches(self.handle, steps, self.external) + per_grad * grads
 
   def check_status(self):
     code = int(self.status.item())
@@ -309,7 +368,9 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
   if rbf.kind != "host":
     return None
   ds_list = [s.data_state for s in states]
-  if any(d.state is None or d.cached_batches is not None for d in ds_list):
+  shuffled = ShuffledFeed.qualifies(rbf.loader, ds_list)
+  if not shuffled and any(d.state is None or d.cached_batches is not None
+                          for d in ds_list):
     return None
   steps = int(im.get("steps", 1)) if kind != "langevin" else 1
   if kind == "langevin":
@@ -331,15 +392,21 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
     kw = dict(friction=float(im["friction"]), leapfrog_steps=steps)
     if any(int(s.step) != 0 for s in states):
       return None
-  pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
-  index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
+  feed = pcg = None
+  if shuffled:
+    # Shuffled streams: the host loader draws them, the plan reads them.
+    feed = ShuffledFeed(rbf.loader, ds_list, 2 if kind == "obabo" else 1)
+    index_src = IndexSource(chain_base=chain_ids[0], external=True)
+  else:
+    pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
+    index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
   dataset = rbf.loader.device_dataset()
   h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
   # One solver iteration is `steps` integrator steps with the same schedule.
   h_tab = torch.from_numpy(np.repeat(np.asarray(h, np.float32), steps)).cuda()
   t_tab = torch.from_numpy(np.repeat(np.asarray(t, np.float32), steps)).cuda()
   plan = NetPlan(pot, dataset, X, AUX, rbf.mb_size, kind, h_tab, t_tab,
-                 index_src, states[0].key, chain_ids[0], **kw)
+                 index_src, states[0].key, chain_ids[0], feed=feed, **kw)
   C = len(states)
   samples = torch.empty((max(n_kept, 1), C, X.shape[1]), dtype=torch.float32,
                         device="cuda")
@@ -356,10 +423,13 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
     plan.check_status()
   finally:
     plan.close()
-  host = pcg.cpu()   # the streams advanced on the device
-  for c, s in enumerate(states):
-    dst = s.data_state.state
-    dst.copy_(pcg[c] if dst.is_cuda else host[c])
+    if feed is not None:
+      feed.close()
+  if pcg is not None:
+    host = pcg.cpu()   # the streams advanced on the device
+    for c, s in enumerate(states):
+      dst = s.data_state.state
+      dst.copy_(pcg[c] if dst.is_cuda else host[c])
   key = "likelihood" if kind == "langevin" else "energy"
   return io.postprocess_chains(saving or io.no_save(), n_kept,
                                samples[:n_kept], [s.treedef for s in states],
@@ -395,12 +465,18 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
   chain_ids = [int(s.chain) for s in states]
   if chain_ids != list(range(chain_ids[0], chain_ids[0] + len(states))):
     return None
+  feed = None
   if rbf.kind == "host":
     ds_list = [s.data_state for s in states]
-    if any(d.state is None or d.cached_batches is not None for d in ds_list):
-      return None   # shuffled streams, or draws already consumed
-    pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
-    index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
+    if ShuffledFeed.qualifies(rbf.loader, ds_list):
+      # Shuffled streams: the host loader draws them, the plan reads them.
+      feed = ShuffledFeed(rbf.loader, ds_list, 1)
+      index_src = IndexSource(chain_base=chain_ids[0], external=True)
+    elif any(d.state is None or d.cached_batches is not None for d in ds_list):
+      return None   # in-epoch streams, or draws already consumed
+    else:
+      pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
+      index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
   else:
     seeds = {s.data_state.state[0] for s in states}
     if len(seeds) != 1 or any(s.data_state.state[1] != 0 for s in states):
@@ -421,11 +497,15 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
   if saving is not None and saving.kind == "memory":
     outbuf = io.HostBuffers([((n_kept, len(states), W.shape[1]), np.float32),
                              ((n_kept, len(states)), np.float64)])
-  res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,
-                     n_kept, index_src, noise_seed=states[0].key,
-                     chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,
-                     block_steps=block)
-  if rbf.kind == "host":
+  try:
+    res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,
+                       n_kept, index_src, noise_seed=states[0].key,
+                       chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,
+                       block_steps=block, feed=feed)
+  finally:
+    if feed is not None:
+      feed.close()
+  if rbf.kind == "host" and feed is None:
     # The streams advanced on the device; states still holding their
     # initial host words get them back in one copy.
     host = index_src.pcg.cpu()

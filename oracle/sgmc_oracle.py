@@ -629,6 +629,33 @@ def resgld_exchange_adjacent(U, var, ssq, T, F, round_, u):
   return flags, U, var, log_s
 
 
+class ShuffledBatches:
+  """Minibatches of a shuffled random pipeline, one call at a time, as
+  NumpyDataLoader._shuffle_indices hands them out
+  (jax_sgmc/data/numpy_loader.py:391-431): a ring of (floor(N/mb) + 2) mb
+  entries; when fewer than mb are unread, a permutation
+  rng.choice(arange(N), N, replace=False) is written after the unread ones;
+  each call reads the next mb entries."""
+
+  def __init__(self, rng: np.random.Generator, n_obs: int, mb: int):
+    self.rng, self.N, self.mb = rng, n_obs, mb
+    self.R = (n_obs // mb + 2) * mb
+    self.ring = np.zeros(self.R, dtype=np.int64)
+    self.read = 0       # next ring position to read (mod R)
+    self.unread = 0
+
+  def next(self) -> np.ndarray:
+    if self.unread < self.mb:
+      perm = self.rng.choice(np.arange(self.N), size=self.N, replace=False)
+      write = (self.read + self.unread + np.arange(self.N)) % self.R
+      self.ring[write] = perm
+      self.unread += self.N
+    out = self.ring[(self.read + np.arange(self.mb)) % self.R].copy()
+    self.read = (self.read + self.mb) % self.R
+    self.unread -= self.mb
+    return out
+
+
 # ---------------------------------------------------------------------------
 # Sample statistics
 # ---------------------------------------------------------------------------

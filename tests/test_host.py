@@ -309,3 +309,50 @@ def test_moments_saving_and_mass_adaption_strategy_shapes():
   assert io.moments().kind == "moments"
   strat = adaption.mass_matrix(burn_in=7)
   assert strat.kind == "mass_matrix" and len(tuple(strat)[:3]) == 3
+
+
+@pytest.mark.parametrize("N,mb,cache,counts", [
+    (1000, 100, 3, [1, 2, 7, 15, 3, 40]),
+    (1037, 64, 5, [5, 33, 1, 70]),
+    (500, 500, 1, [1, 1, 3, 2]),
+    (10, 3, 2, [1, 4, 9, 2]),
+])
+def test_take_shuffled_equals_the_per_batch_ring(N, mb, cache, counts):
+  """NumpyDataLoader.take_shuffled (the bulk draw the fused plans read
+  shuffled streams from) hands out the batches of
+  numpy_loader.py:391-431 one call at a time would, and leaves the chain's
+  generator, ring and counters where those calls would."""
+  from gbsgmc import data
+  from gbsgmc.data.numpy_loader import chain_rng
+  from oracle import sgmc_oracle as O
+  X = np.zeros((N, 2), np.float32)
+  bulk, single = data.NumpyDataLoader(x=X), data.NumpyDataLoader(x=X)
+  cb = bulk.register_random_pipeline(cache, mb_size=mb, shuffle=True)
+  cs = single.register_random_pipeline(cache, mb_size=mb, shuffle=True)
+  oracle = O.ShuffledBatches(chain_rng(cb), N, mb)
+  for count in counts:
+    got = bulk.take_shuffled(cb, count)
+    want = np.stack([oracle.next() for _ in range(count)])
+    np.testing.assert_array_equal(got, want)
+    per = np.stack([single._shuffle_indices(single._chains[cs])[0]
+                    for _ in range(count)])
+    np.testing.assert_array_equal(got, per)
+    a, b = bulk._chains[cb], single._chains[cs]
+    assert (a["draws"], a["remaining_samples"]) == (b["draws"], b["remaining_samples"])
+    np.testing.assert_array_equal(a["random_indices"], b["random_indices"])
+    assert a["rng"].bit_generator.state == b["rng"].bit_generator.state
+  # Every permutation is one: each index appears once per N entries.
+  stream = O.ShuffledBatches(chain_rng(0), N, mb)
+  first = np.concatenate([stream.next() for _ in range(N // mb)])
+  assert len(np.unique(first)) == len(first)
+
+
+def test_take_shuffled_rejects_other_pipelines():
+  from gbsgmc import data
+  loader = data.NumpyDataLoader(x=np.zeros((20, 1), np.float32))
+  c = loader.register_random_pipeline(2, mb_size=4)
+  with pytest.raises(ValueError):
+    loader.take_shuffled(c, 1)
+  e = loader.register_random_pipeline(2, mb_size=4, shuffle=True, in_epochs=True)
+  with pytest.raises(ValueError):
+    loader.take_shuffled(e, 1)
