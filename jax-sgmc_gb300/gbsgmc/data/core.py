@@ -353,6 +353,21 @@ class RandomBatchFn:
     return self._fn(data_state, information, device_count)
 
 
+class _BatchRows:
+  """[steps, k * mb] seen as the [steps * k, mb] batch rows it holds, for
+  slice assignment (a strided view that reshape cannot give)."""
+
+  def __init__(self, a, mb):
+    self.a, self.mb = a, mb
+    self.k = a.shape[1] // mb
+
+  def __setitem__(self, sl, value):
+    start, stop = sl.start, sl.stop
+    for r in range(start, stop):
+      s, j = divmod(r, self.k)
+      self.a[s, j * self.mb:(j + 1) * self.mb] = value[r - start]
+
+
 class ShuffledFeed:
   """Minibatch indices of C shuffled host pipelines (shuffle=True,
   in_epochs=False), step by step, for a plan with an external index source.
@@ -390,28 +405,33 @@ class ShuffledFeed:
         return False
     return len({int(ds.cached_batches_count) for ds in data_states}) == 1
 
-  def _take(self, c, count):
-    out = []
-    while count > 0:
+  def _take(self, c, count, dst):
+    """The next ``count`` batches of chain c into dst ([count, mb])."""
+    done = 0
+    while done < count:
       if self.pos[c] == self.cache:
         self.chunk[c] = self.loader.take_shuffled(self.states[c].chain_id,
                                                   self.cache)
         self.pos[c] = 0
-      m = min(count, self.cache - self.pos[c])
-      out.append(self.chunk[c][self.pos[c]:self.pos[c] + m])
+      m = min(count - done, self.cache - self.pos[c])
+      dst[done:done + m] = self.chunk[c][self.pos[c]:self.pos[c] + m]
       self.pos[c] += m
-      count -= m
-    return np.concatenate(out).reshape(-1, self.k * self.mb)
+      done += m
 
   def next(self, steps, out=None):
     """Indices of the next ``steps`` steps of every chain, written into
     ``out`` ([>= steps, C, k * mb] int32) when given."""
-    parts = list(self._pool.map(lambda c: self._take(c, steps * self.k),
-                                range(len(self.states))))
+    C = len(self.states)
     if out is None:
-      out = np.empty((steps, len(parts), self.k * self.mb), np.int32)
-    np.stack(parts, axis=1, out=out[:steps])
-    return out[:steps]
+      out = np.empty((steps, C, self.k * self.mb), np.int32)
+    view = out[:steps]
+    # Chain c's batches are view[:, c, :] read as [steps * k, mb].
+    list(self._pool.map(
+        lambda c: self._take(c, steps * self.k,
+                             view[:, c, :].reshape(steps * self.k, self.mb)
+                             if self.k == 1 else _BatchRows(view[:, c, :], self.mb)),
+        range(C)))
+    return view
 
   def close(self):
     self._pool.shutdown(wait=True)

@@ -99,6 +99,26 @@ class DeviceNumpyDataLoader(NumpyBase, DeviceDataLoader):
     return self._reference_data
 
 
+def _ring_read(ring, start, length):
+  """ring[(start + arange(length)) % len(ring)] as at most two slices."""
+  R = len(ring)
+  start %= R
+  first = min(length, R - start)
+  if first == length:
+    return ring[start:start + length].copy()
+  return onp.concatenate([ring[start:], ring[:length - first]])
+
+
+def _ring_write(ring, start, values):
+  """ring[(start + arange(len(values))) % len(ring)] = values, as slices
+  (values no longer than the ring)."""
+  R = len(ring)
+  start %= R
+  first = min(len(values), R - start)
+  ring[start:start + first] = values[:first]
+  ring[:len(values) - first] = values[first:]
+
+
 class NumpyDataLoader(NumpyBase, HostDataLoader):
   """Load complete dataset into memory from multiple numpy arrays."""
 
@@ -254,11 +274,11 @@ class NumpyDataLoader(NumpyBase, HostDataLoader):
     if ring is None:
       ring = onp.zeros(R, dtype=onp.int_)
       chain['random_indices'] = ring
-    parts = [ring[(d0 * mb + onp.arange(r0)) % R]]
+    parts = [_ring_read(ring, d0 * mb, r0)]
     head = d0 * mb + r0
     for t in range(k):
       perm = chain['rng'].choice(onp.arange(0, N), size=N, replace=False)
-      ring[(head + t * N + onp.arange(N)) % R] = perm
+      _ring_write(ring, head + t * N, perm)
       parts.append(perm)
     stream = onp.concatenate(parts)[:need]
     chain['draws'] = (d0 + count) % ceil_draws
