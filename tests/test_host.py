@@ -356,3 +356,38 @@ def test_take_shuffled_rejects_other_pipelines():
   e = loader.register_random_pipeline(2, mb_size=4, shuffle=True, in_epochs=True)
   with pytest.raises(ValueError):
     loader.take_shuffled(e, 1)
+
+
+@pytest.mark.parametrize("k", [1, 2])
+def test_shuffled_feed_hands_out_each_chains_batches_in_order(k):
+  """ShuffledFeed (the host side of a plan's external index source): per
+  step and chain, the next k batches the chain's own batch function would
+  use -- its cached batches, then cache-sized refills -- whatever the block
+  sizes asked for."""
+  import torch
+  from gbsgmc import data
+  from gbsgmc.data.core import CacheState, ShuffledFeed
+  N, mb, C, cache = 1000, 16, 3, 5
+  X = np.zeros((N, 1), np.float32)
+  fed, ref = data.NumpyDataLoader(x=X), data.NumpyDataLoader(x=X)
+  states, ref_states = [], []
+  for _ in range(C):
+    for loader, out in ((fed, states), (ref, ref_states)):
+      cid = loader.register_random_pipeline(cache, mb_size=mb, shuffle=True)
+      idx, _ = loader._get_indices(cid)
+      out.append(CacheState(cached_batches=torch.from_numpy(idx.astype(np.int32)),
+                            cached_batches_count=cache, current_line=0,
+                            chain_id=cid))
+  assert ShuffledFeed.qualifies(fed, states)
+  feed = ShuffledFeed(fed, states, k)
+  try:
+    got = np.concatenate([feed.next(s).copy() for s in (3, 7, 1, 12)])
+  finally:
+    feed.close()
+  for c in range(C):
+    batches = list(ref_states[c].cached_batches.numpy())
+    while len(batches) < got.shape[0] * k:
+      idx, _ = ref._get_indices(ref_states[c].chain_id)
+      batches += list(idx)
+    want = np.array(batches[:got.shape[0] * k]).reshape(got.shape[0], k * mb)
+    np.testing.assert_array_equal(got[:, c, :], want)
