@@ -50,7 +50,7 @@ class _ExternalIndices:
     self.events = [None, None]
     self.turn = 0
 
-  def run(self, handle, first_step, steps, step_multiple=1):
+  def run(self, handle, first_step, steps):
     import torch
     done = 0
     while done < steps:
@@ -59,7 +59,7 @@ class _ExternalIndices:
       self.turn ^= 1
       if self.events[i] is not None:
         self.events[i].synchronize()   # its previous copy has left the buffer
-      idx = self.feed.next(g, out=self.bufs[i].numpy())
+      self.feed.next(g, out=self.bufs[i].numpy())
       _lib.call("gbsgmc_plan_set_indices", handle, _lib.ptr(self.bufs[i]), g,
                 _lib.stream_handle())
       ev = torch.cuda.Event()
@@ -68,7 +68,6 @@ class _ExternalIndices:
       _lib.call("gbsgmc_plan_run", handle, int(first_step + done), g,
                 _lib.stream_handle())
       done += g
-      del idx
 
 
 def _plan_launches(handle, steps, external=None) -> int:
