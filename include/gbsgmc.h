@@ -232,6 +232,29 @@ int gbsgmc_sghmc_momentum(int chains, int64_t P, float* p_dev,
                           float friction, const gbsgmc_sched* sched,
                           const gbsgmc_noise* noise, gbsgmc_stream_t stream);
 
+/* SGHMC force and noise under a noise model (integrator.py:630-647):
+ * p <- p - h g + sqrt(2h) (cb_diff_sqrt * xi), cb_diff_sqrt [chains, P]
+ * from gbsgmc_glm_fisher_noise, xi of tag GBSGMC_TAG_SGHMC_STEP. */
+int gbsgmc_sghmc_momentum_noise_model(int chains, int64_t P, float* p_dev,
+                                      const float* g_dev, const float* cb_diff_sqrt_dev,
+                                      const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                                      gbsgmc_stream_t stream);
+
+/* The empirical-Fisher noise model of fisher_information(diagonal=True)
+ * (jax_sgmc/adaption.py:371-457) on a generalised-linear likelihood, per
+ * chain: with G = grad_dev (dU/dw of the minibatch potential at w) and the
+ * per-observation likelihood gradients lk'(z_i) x_i of the n rows idx,
+ *   ssq = sum_i (lk'(z_i) x_i - G / N)^2,  b = 0.5 step_size ssq / (n - 1),
+ *   corr = friction - b, corr <= 0 replaced by the chain's smallest positive
+ *   corr;  cb_diff_sqrt = sqrt(corr),  b_sqrt = sqrt(friction - corr)
+ * (b_sqrt_dev may be NULL).  friction_dev [d] or NULL (scalar friction).
+ * 2 <= n <= 4096; fp32 like the reference. */
+int gbsgmc_glm_fisher_noise(const gbsgmc_glm* model, int chains, int n,
+                            const int32_t* idx_dev, int64_t idx_stride, const float* w_dev,
+                            const float* grad_dev, const float* friction_dev, float friction,
+                            float step_size, float* cb_diff_sqrt_dev, float* b_sqrt_dev,
+                            int* status_dev, gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Reversible leapfrog (AMAGOLD) and Metropolis-Hastings corrections         */
 /* ------------------------------------------------------------------------ */

@@ -165,6 +165,10 @@ SIGNATURES = {
     "gbsgmc_moments_finalize": (_i, [_i, _i64, _i64, _vp, _vp, _vp, _vp, _vp,
                                      _vp]),
     "gbsgmc_mass_adapt": (_i, [_i64, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbsgmc_glm_fisher_noise": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp, _vp,
+                                     _f, _f, _vp, _vp, _vp, _vp]),
+    "gbsgmc_sghmc_momentum_noise_model": (_i, [_i, _i64, _vp, _vp, _vp, _P(Sched),
+                                               _P(Noise), _vp]),
     "gbsgmc_resgld_swap_f64": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _vp, _vp,
                                     _vp, _u64, _i64, _vp, _vp, _vp]),
     "gbsgmc_swap_rows": (_i, [_i, _i64, _vp, _vp, _vp, _vp]),

@@ -14,7 +14,9 @@ them into the parameter update (``gbsgmc_sgld_update``,
 
 ``mass_matrix(diagonal=True)`` adapts the diagonal mass of the MH samplers
 (AMAGOLD, SGGMC) on the device with ``gbsgmc_mass_adapt``
-(adaption.py:296-368).  The dense variant and ``fisher_information`` are not
+(adaption.py:296-368).  ``fisher_information(diagonal=True)`` is SGHMC's
+empirical-Fisher noise model (adaption.py:371-457) on the generalised-linear
+likelihoods (``gbsgmc_glm_fisher_noise``).  The dense variants are not
 provided.
 """
 
@@ -32,6 +34,12 @@ class Manifold(NamedTuple):
 class MassMatrix(NamedTuple):
   inv: Any
   sqrt: Any
+
+
+class NoiseModel(NamedTuple):
+  """SGHMC noise model (adaption.py:79-90): sqrt(friction - B) and sqrt(B)."""
+  cb_diff_sqrt: Any
+  b_sqrt: Any
 
 
 class RmsPropState(NamedTuple):
@@ -131,6 +139,54 @@ def mass_matrix(diagonal=True, burn_in=1000) -> AdaptionStrategy:
   return AdaptionStrategy(init, update, get, "mass_matrix")
 
 
-def fisher_information(minibatch_potential=None, diagonal=True):
-  raise NotImplementedError("fisher_information is not part of the GPU "
-                            "hot path")
+def fisher_information(minibatch_potential=None, diagonal=True) -> AdaptionStrategy:
+  """Empirical Fisher information of the minibatch as SGHMC's noise model
+  (adaption.py:371-457, after https://arxiv.org/abs/1206.6380).  Stateless:
+  ``get(state, sample, sample_grad, friction, mini_batch=..., step_size=...)``
+  returns the :class:`NoiseModel` of the current minibatch, computed on the
+  device from the per-observation likelihood gradients (the
+  generalised-linear families)."""
+  assert minibatch_potential, "Fisher information requires potential function."
+  if not diagonal:
+    raise NotImplementedError("only the diagonal noise model is provided (the "
+                              "dense one needs two SVDs of P x P matrices)")
+  if getattr(minibatch_potential, "is_network", False):
+    raise NotImplementedError("per-observation gradients are provided for the "
+                              "generalised-linear likelihoods")
+  pot = minibatch_potential
+
+  def init(*args, **kwargs):
+    del args, kwargs
+
+  def update(*args, **kwargs):
+    del args, kwargs
+
+  def get(state, sample, sample_grad, friction, *args, mini_batch=None,
+          step_size=1.0, **kwargs) -> NoiseModel:
+    import numpy as np
+    import torch
+    from . import _lib
+    del state, args, kwargs
+    assert mini_batch, "Adaption strategy requires mini-batch"
+    batch, info = mini_batch
+    ds = batch.dataset
+    n_obs = info.observation_count if info is not None else ds.observation_count
+    m, keep = pot.model(ds, n_obs)
+    x = _flat_device(sample)
+    P = x.numel()
+    g = _flat_device(sample_grad)
+    idx = batch.indices.reshape(-1).to(device="cuda", dtype=torch.int32).contiguous()
+    if np.isscalar(friction):
+      fric, f = None, float(friction)
+    else:
+      fric, f = _flat_device(friction), 0.0
+    cb = torch.empty(P, dtype=torch.float32, device="cuda")
+    bs = torch.empty(P, dtype=torch.float32, device="cuda")
+    _lib.call("gbsgmc_glm_fisher_noise", m, 1, idx.numel(), _lib.ptr(idx),
+              idx.numel(), _lib.ptr(x), _lib.ptr(g), _lib.ptr(fric), f,
+              float(step_size), _lib.ptr(cb), _lib.ptr(bs),
+              _lib.ptr(pot.status()), _lib.stream_handle())
+    del keep
+    return NoiseModel(cb_diff_sqrt=cb, b_sqrt=bs)
+
+  return AdaptionStrategy(init, update, get, "fisher_information")

@@ -91,12 +91,15 @@ def sghmc(potential_fn, data_loader, cache_size: int = 512,
           save_to_numpy: bool = True, progress_bar: bool = True):
   """Stochastic Gradient Hamiltonian Monte Carlo (alias.py:451-540)."""
   if adapt_noise_model:
-    raise NotImplementedError("adapt_noise_model needs fisher_information, "
-                              "which is not part of the GPU hot path")
+    noise_model = adaption.fisher_information(minibatch_potential=potential_fn,
+                                              diagonal=diagonal_noise)
+  else:
+    noise_model = None
   random_data = data.random_reference_data(data_loader, cache_size, batch_size)
   leapfrog = integrator.friction_leapfrog(potential_fn, random_data,
                                           friction=friction, const_mass=mass,
-                                          steps=integration_steps)
+                                          steps=integration_steps,
+                                          noise_model=noise_model)
   schedule = _schedule(first_step_size, last_step_size, burn_in,
                        accepted_samples, progress_bar)
   saving = io.save(io.MemoryCollector()) if save_to_numpy else None

@@ -350,7 +350,8 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
   integ = meta.get("integrator")
   im = getattr(integ, "meta", {})
   kind = im.get("kind")
-  if kind not in NetPlan.KINDS or im.get("noise_source") is not None:
+  if kind not in NetPlan.KINDS or im.get("noise_source") is not None \
+      or im.get("noise_model") is not None:
     return None
   pot = im.get("potential")
   bfn = im.get("batch_fn")

@@ -280,10 +280,13 @@ def obabo(potential_fn, batch_fn, steps=10, friction=1.0, const_mass=None,
 def friction_leapfrog(potential_fn, batch_fn, steps=10, friction=0.25,
                       const_mass=None, noise_model=None,
                       noise_source: Callable = None):
-  """Original SGHMC leapfrog (integrator.py:563-765), no noise model."""
-  if noise_model is not None:
-    raise NotImplementedError("noise models (fisher_information) are not part "
-                              "of the GPU hot path")
+  """Original SGHMC leapfrog (integrator.py:563-765).  With a noise model
+  (``adaption.fisher_information``) the injected noise of each step is
+  sqrt(2h) cb_diff_sqrt xi, cb_diff_sqrt from the step's minibatch at the
+  new positions (integrator.py:630-647), instead of friction sqrt(2h) xi."""
+  if noise_model is not None and getattr(noise_model, "kind", None) != \
+      "fisher_information":
+    raise NotImplementedError("the SGHMC noise model is fisher_information")
   init_data, get_data, _ = batch_fn
 
   def init_fn(init_sample, key=None, batch_kwargs=None, init_model_state=None):
@@ -321,9 +324,17 @@ def friction_leapfrog(potential_fn, batch_fn, steps=10, friction=0.25,
       data_state, (b, i) = get_data(data_state, information=True)
       r = _eval(potential_fn, x, b, i)
       buf = _injected(noise_source, step, state.chain, _lib.TAG_SGHMC_STEP)
-      _lib.call("gbsgmc_sghmc_momentum", 1, P, _lib.ptr(p), _lib.ptr(r.grad),
-                _lib.ptr(fric), f, sch, _noise(state.key, state.chain, buf),
-                _lib.stream_handle())
+      if noise_model is not None:
+        nm = noise_model.get(None, x, r.grad, friction if scalar_friction else fric,
+                             mini_batch=(b, i),
+                             step_size=float(parameters.step_size))
+        _lib.call("gbsgmc_sghmc_momentum_noise_model", 1, P, _lib.ptr(p),
+                  _lib.ptr(r.grad), _lib.ptr(nm.cb_diff_sqrt), sch,
+                  _noise(state.key, state.chain, buf), _lib.stream_handle())
+      else:
+        _lib.call("gbsgmc_sghmc_momentum", 1, P, _lib.ptr(p), _lib.ptr(r.grad),
+                  _lib.ptr(fric), f, sch, _noise(state.key, state.chain, buf),
+                  _lib.stream_handle())
       pot = r.U[0]
       step += 1
     return state._replace(potential=pot, data_state=data_state, step=step)
@@ -335,7 +346,8 @@ def friction_leapfrog(potential_fn, batch_fn, steps=10, friction=0.25,
   return IntegratorTriplet(init_fn, integrate, get_fn, kind="sghmc",
                            potential=potential_fn, batch_fn=batch_fn,
                            steps=steps, friction=friction,
-                           const_mass=const_mass, noise_source=noise_source)
+                           const_mass=const_mass, noise_source=noise_source,
+                           noise_model=noise_model)
 
 
 def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,

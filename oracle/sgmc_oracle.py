@@ -223,6 +223,33 @@ def full_potential(w, X, y, family, sigma=1.0, prior_scale=0.0,
   return U, g
 
 
+def fisher_variance(w, X, y, idx, grad, n_obs, family, sigma):
+  """v = ssq / (n - 1) of fisher_information's get (jax_sgmc/adaption.py
+  403-437), float64, one chain: the per-observation gradients of the
+  likelihoods lk_i (not the potential) against grad / N."""
+  w = np.asarray(w, np.float64)
+  Xb = np.asarray(X, np.float64)[np.asarray(idx)]
+  yb = np.asarray(y, np.float64)[np.asarray(idx)]
+  _, dz = glm_lk(family, Xb @ w, yb, sigma)
+  gbar = np.asarray(grad, np.float64) / n_obs
+  ssq = np.sum((dz[:, None] * Xb - gbar) ** 2, axis=0)
+  return 1.0 / (len(idx) - 1) * ssq
+
+
+def fisher_noise(w, X, y, idx, grad, n_obs, family, sigma, friction, step_size):
+  """fisher_information(diagonal=True).get (jax_sgmc/adaption.py:403-455),
+  float64, one chain: b = 0.5 h v (v from :func:`fisher_variance`),
+  corr = friction - b with corr <= 0 replaced by the smallest positive corr;
+  returns (sqrt(corr), sqrt(friction - corr))."""
+  v = fisher_variance(w, X, y, idx, grad, n_obs, family, sigma)
+  b = 0.5 * step_size * v
+  f = np.broadcast_to(np.asarray(friction, np.float64), b.shape)
+  corr = f - b
+  smallest = np.min(np.where(corr <= 0, np.inf, corr))
+  pc = np.where(corr <= 0, smallest, corr)
+  return np.sqrt(pc), np.sqrt(f - pc)
+
+
 # ---------------------------------------------------------------------------
 # Dense tanh network with a Gaussian likelihood
 # ---------------------------------------------------------------------------

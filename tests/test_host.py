@@ -293,8 +293,10 @@ def test_potential_rejects_arbitrary_callables():
 
 def test_unported_presets_raise():
   from gbsgmc import adaption, integrator
-  with pytest.raises(NotImplementedError):
+  with pytest.raises(AssertionError):        # needs the potential
     adaption.fisher_information()
+  with pytest.raises(NotImplementedError):   # dense noise model
+    adaption.fisher_information(minibatch_potential=object(), diagonal=False)
   with pytest.raises(NotImplementedError):   # dense mass adaption
     adaption.mass_matrix(diagonal=False)
   with pytest.raises(NotImplementedError):   # langevin adapts with rms_prop only
