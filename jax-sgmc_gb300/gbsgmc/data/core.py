@@ -369,8 +369,11 @@ class _BatchRows:
 
 
 class ShuffledFeed:
-  """Minibatch indices of C shuffled host pipelines (shuffle=True,
-  in_epochs=False), step by step, for a plan with an external index source.
+  """Minibatch indices of C shuffled host pipelines (shuffle=True, with or
+  without in_epochs), step by step, for a plan with an external index
+  source.  The integrators use an in-epoch batch's masked tail like any
+  other rows (the reference applies a mask only when the caller passes
+  one), so the plans need the indices alone.
 
   Chain c's batches come in the order its own batch function would hand
   them out: the rest of its device cache, then cache-sized chunks from the
@@ -390,6 +393,8 @@ class ShuffledFeed:
     self.chunk = [ds.cached_batches.cpu().numpy() for ds in self.states]
     self.pos = [int(ds.current_line) for ds in self.states]
     self.mb = self.chunk[0].shape[1]
+    in_epochs = loader._chains[self.states[0].chain_id].get("in_epochs")
+    self._draw = loader.take_in_epochs if in_epochs else loader.take_shuffled
     self._pool = cf.ThreadPoolExecutor(max(1, min(len(self.states),
                                                    os.cpu_count() or 1)))
 
@@ -399,19 +404,20 @@ class ShuffledFeed:
     if chains is None or not data_states:
       return False
     for ds in data_states:
-      ch = chains[ds.chain_id]
-      if (ds.state is not None or ds.cached_batches is None
-          or not ch.get("shuffle") or ch.get("in_epochs")):
+      if ds.state is not None or ds.cached_batches is None or ds.chain_id is None:
         return False
-    return len({int(ds.cached_batches_count) for ds in data_states}) == 1
+      if not chains[ds.chain_id].get("shuffle"):
+        return False
+    modes = {bool(chains[ds.chain_id].get("in_epochs")) for ds in data_states}
+    return len(modes) == 1 and \
+        len({int(ds.cached_batches_count) for ds in data_states}) == 1
 
   def _take(self, c, count, dst):
     """The next ``count`` batches of chain c into dst ([count, mb])."""
     done = 0
     while done < count:
       if self.pos[c] == self.cache:
-        self.chunk[c] = self.loader.take_shuffled(self.states[c].chain_id,
-                                                  self.cache)
+        self.chunk[c] = self._draw(self.states[c].chain_id, self.cache)
         self.pos[c] = 0
       m = min(count - done, self.cache - self.pos[c])
       dst[done:done + m] = self.chunk[c][self.pos[c]:self.pos[c] + m]

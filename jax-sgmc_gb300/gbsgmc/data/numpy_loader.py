@@ -241,6 +241,34 @@ class NumpyDataLoader(NumpyBase, HostDataLoader):
     chain['remaining_samples'] -= chain['mb_size']
     return selections, mask
 
+  def take_in_epochs(self, chain_id: int, count: int) -> onp.ndarray:
+    """``count`` consecutive minibatches ``[count, mb_size]`` of an in-epoch
+    pipeline (shuffle=True, in_epochs=True), leaving the chain's state as
+    ``count`` calls of ``_shuffle_in_epochs`` (numpy_loader.py:433-460)
+    would: a new permutation at the start of each epoch of ceil(N / mb)
+    batches, the batches read in order from the ring (whose entries past N
+    are never written, so the last batch of an epoch ends with them)."""
+    chain = self._chains[chain_id]
+    if not chain['in_epochs'] or chain['type'] != 'random':
+      raise ValueError("take_in_epochs needs an in_epochs=True pipeline")
+    N, mb = self._observation_count, chain['mb_size']
+    epoch = math.ceil(N / mb)
+    out = onp.empty((int(count), mb), dtype=onp.int_)
+    done = 0
+    while done < count:
+      if chain['draws'] == epoch:
+        perm = chain['rng'].choice(onp.arange(0, N), size=N, replace=False)
+        if chain['random_indices'] is None:
+          chain['random_indices'] = onp.zeros(epoch * mb, dtype=onp.int_)
+        chain['random_indices'][0:N] = perm
+        chain['draws'] = 0
+      d = chain['draws']
+      m = min(count - done, epoch - d)
+      out[done:done + m] = chain['random_indices'][mb * d:mb * (d + m)].reshape(m, mb)
+      chain['draws'] = d + m
+      done += m
+    return out
+
   def take_shuffled(self, chain_id: int, count: int) -> onp.ndarray:
     """``count`` consecutive minibatches ``[count, mb_size]`` of a shuffled
     pipeline (shuffle=True, in_epochs=False), leaving the chain's state --

@@ -473,7 +473,7 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
       feed = ShuffledFeed(rbf.loader, ds_list, 1)
       index_src = IndexSource(chain_base=chain_ids[0], external=True)
     elif any(d.state is None or d.cached_batches is not None for d in ds_list):
-      return None   # in-epoch streams, or draws already consumed
+      return None   # draws already consumed
     else:
       pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
       index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])

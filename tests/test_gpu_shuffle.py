@@ -1,8 +1,8 @@
-"""Shuffled index streams (NumpyDataLoader shuffle=True,
-jax_sgmc/data/numpy_loader.py:391-431) in the fused many-chain plans: the
-host loader draws each chain's permutations (numpy itself, so the streams
-are numpy's), ``ShuffledFeed`` hands them to a plan with an external index
-source block by block (``gbsgmc_plan_set_indices``), and the samples equal
+"""Shuffled index streams (NumpyDataLoader shuffle=True, with and without
+in_epochs, jax_sgmc/data/numpy_loader.py:391-460) in the fused many-chain
+plans: the host loader draws each chain's permutations (numpy itself, so
+the streams are numpy's), ``ShuffledFeed`` hands them to a plan with an
+external index source block by block (``gbsgmc_plan_set_indices``), and the samples equal
 the per-chain path's, which takes the same batches one call at a time: bit
 for bit for OBABO and SGHMC (the same kernels run), and within 1e-4
 relative for SGLD on a GLM (the fused step kernel rounds its update
@@ -18,7 +18,8 @@ pytestmark = pytest.mark.gpu
 N, D, n, CHAINS = 900, 10, 32, 3
 
 
-def _run(kind, fused, iterations=60, accepted=20, cache=7, shuffle=True):
+def _run(kind, fused, iterations=60, accepted=20, cache=7, shuffle=True,
+         in_epochs=False):
   from gbsgmc import adaption, alias, data, engine, integrator, io, solver
   from gbsgmc import likelihoods as L, potential
   rng = np.random.default_rng(3)
@@ -36,7 +37,8 @@ def _run(kind, fused, iterations=60, accepted=20, cache=7, shuffle=True):
   s = solver.sgmc(integ)
   sched = alias._schedule(1e-3, 1e-4, 10, accepted, False)
   run = solver.mcmc(s, sched, saving=io.save())
-  states = [s[0]({"w": np.zeros(D, np.float32)}, batch_kwargs={"shuffle": shuffle})
+  kw = {"shuffle": shuffle, "in_epochs": in_epochs} if in_epochs else {"shuffle": shuffle}
+  states = [s[0]({"w": np.zeros(D, np.float32)}, batch_kwargs=kw)
             for _ in range(CHAINS)]
   engine.FUSED_ENABLED = fused
   try:
@@ -45,8 +47,9 @@ def _run(kind, fused, iterations=60, accepted=20, cache=7, shuffle=True):
     engine.FUSED_ENABLED = True
 
 
+@pytest.mark.parametrize("in_epochs", [False, True])
 @pytest.mark.parametrize("kind", ["sgld", "obabo", "sghmc"])
-def test_fused_shuffled_streams_equal_per_chain_path(lib, kind, monkeypatch):
+def test_fused_shuffled_streams_equal_per_chain_path(lib, kind, in_epochs, monkeypatch):
   from gbsgmc.data import core
   # One CTA per chain, a fixed row tiling and no autotuned shape (a plan's
   # autotuner stores its choice for later calls of the same shape): a
@@ -63,9 +66,9 @@ def test_fused_shuffled_streams_equal_per_chain_path(lib, kind, monkeypatch):
     return orig(self, steps, out)
 
   monkeypatch.setattr(core.ShuffledFeed, "next", spy)
-  a, la = _run(kind, fused=True)
+  a, la = _run(kind, fused=True, in_epochs=in_epochs)
   fused_calls = len(calls)
-  b, lb = _run(kind, fused=False)
+  b, lb = _run(kind, fused=False, in_epochs=in_epochs)
   assert fused_calls > 1 and len(calls) == fused_calls   # only the fused run
   assert len(a) == len(b) == CHAINS
   for ra, rb in zip(a, b):
@@ -80,6 +83,7 @@ def test_fused_shuffled_streams_equal_per_chain_path(lib, kind, monkeypatch):
   # The loaders' chains end where the per-chain calls leave them.
   for ca, cb in zip(la._chains, lb._chains):
     assert (ca["draws"], ca["remaining_samples"]) == (cb["draws"], cb["remaining_samples"])
+    assert ca["in_epochs"] == in_epochs
     assert ca["rng"].bit_generator.state == cb["rng"].bit_generator.state
     np.testing.assert_array_equal(ca["random_indices"], cb["random_indices"])
 

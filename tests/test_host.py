@@ -393,3 +393,28 @@ def test_shuffled_feed_hands_out_each_chains_batches_in_order(k):
       batches += list(idx)
     want = np.array(batches[:got.shape[0] * k]).reshape(got.shape[0], k * mb)
     np.testing.assert_array_equal(got[:, c, :], want)
+
+
+@pytest.mark.parametrize("N,mb,counts", [(1000, 64, [1, 5, 16, 40, 3]),
+                                         (96, 32, [2, 3, 7]), (50, 50, [1, 4])])
+def test_take_in_epochs_equals_the_per_batch_epochs(N, mb, counts):
+  """NumpyDataLoader.take_in_epochs hands out what _shuffle_in_epochs
+  (numpy_loader.py:433-460) does one call at a time -- a permutation per
+  epoch of ceil(N / mb) batches, the last batch ending with ring entries
+  past N -- and leaves the same chain state."""
+  from gbsgmc import data
+  X = np.zeros((N, 1), np.float32)
+  bulk, single = data.NumpyDataLoader(x=X), data.NumpyDataLoader(x=X)
+  cb = bulk.register_random_pipeline(2, mb_size=mb, shuffle=True, in_epochs=True)
+  cs = single.register_random_pipeline(2, mb_size=mb, shuffle=True, in_epochs=True)
+  for count in counts:
+    got = bulk.take_in_epochs(cb, count)
+    want = np.stack([single._shuffle_in_epochs(single._chains[cs])[0]
+                     for _ in range(count)])
+    np.testing.assert_array_equal(got, want)
+    a, b = bulk._chains[cb], single._chains[cs]
+    assert a["draws"] == b["draws"]
+    np.testing.assert_array_equal(a["random_indices"], b["random_indices"])
+    assert a["rng"].bit_generator.state == b["rng"].bit_generator.state
+  with pytest.raises(ValueError):
+    bulk.take_in_epochs(bulk.register_random_pipeline(2, mb_size=mb, shuffle=True), 1)
