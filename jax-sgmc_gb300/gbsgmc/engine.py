@@ -33,6 +33,7 @@ class SgldRun(NamedTuple):
   samples: object      # fp32 [S, C, d]
   sample_lik: object   # fp64 [S, C]
   launches: int
+  host: object = None  # [samples, likelihoods] host arrays, when copied
 
 
 class _ExternalIndices:
@@ -167,9 +168,12 @@ class IndexSource:
 
 def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
                  index_src, noise_seed=0, chain_base=0, alpha=0.9, lmbd=1e-5,
-                 block_steps=None, feed=None) -> SgldRun:
+                 block_steps=None, feed=None, host=None) -> SgldRun:
   """Runs ``iterations`` fused SGLD steps for all chains (W, V updated in
-  place) and returns the final state and the kept samples."""
+  place) and returns the final state and the kept samples.  With ``host``
+  (the kept samples' and likelihoods' host arrays, or a HostBuffers), the
+  samples each block keeps are copied there while the next blocks run, and
+  ``SgldRun.host`` holds the filled arrays."""
   import torch
   if block_steps is None:
     block_steps = min(DEFAULT_BLOCK_STEPS, max(1, iterations))
@@ -180,10 +184,30 @@ def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
                      k_tab, n_kept, index_src, noise_seed, chain_base,
                      block_steps, feed=feed)
   try:
-    plan.run(0, iterations)
+    filled = None
+    if host is not None and n_kept > 0:
+      # One run per block, so that each block's kept samples can leave
+      # while the next block runs.
+      drain = io.SampleDrain([plan.samples, plan.sample_lik], host)
+      keep_np = np.asarray(keep)
+      launches = 0
+      try:
+        for k0 in range(0, iterations, block_steps):
+          g = min(block_steps, iterations - k0)
+          plan.run(k0, g)
+          launches += plan.launches(g)
+          kept = keep_np[k0:k0 + g]
+          kept = kept[kept >= 0]
+          if kept.size:
+            drain.filled(kept.min(), kept.max() + 1)
+      finally:
+        filled = drain.finish()
+    else:
+      plan.run(0, iterations)
+      launches = plan.launches(iterations)
     plan.check_status()
     return SgldRun(W, V, plan.U, plan.lk_var, plan.samples[:n_kept],
-                   plan.sample_lik[:n_kept], plan.launches(iterations))
+                   plan.sample_lik[:n_kept], launches, filled)
   finally:
     plan.close()
 
@@ -501,7 +525,7 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
     res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,
                        n_kept, index_src, noise_seed=states[0].key,
                        chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,
-                       block_steps=block, feed=feed)
+                       block_steps=block, feed=feed, host=outbuf)
   finally:
     if feed is not None:
       feed.close()
@@ -516,4 +540,4 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
                                [s.treedef for s in states],
                                {"likelihood": res.sample_lik},
                                [s.model_state for s in states],
-                               host=None if outbuf is None else outbuf.get())
+                               host=res.host, host_filled=res.host is not None)

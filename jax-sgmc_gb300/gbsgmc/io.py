@@ -203,14 +203,76 @@ class HostBuffers:
     return self._arrays
 
 
+class SampleDrain:
+  """Copies kept samples to host arrays while later steps run: after each
+  block of steps the caller reports the slots the block filled
+  (:meth:`filled`), and a thread waits for that block on the device and
+  copies those rows of every buffer ([slots, ...] device tensors) into the
+  matching host arrays on its own stream.  ``host`` is a list of arrays or a
+  :class:`HostBuffers`, fetched by the thread (it may still be faulting in
+  its pages)."""
+
+  def __init__(self, buffers, host):
+    import queue
+    import torch
+    self._buffers = list(buffers)
+    self._host = host
+    self._arrays = None
+    self._queue = queue.Queue()
+    self._device = self._buffers[0].device
+    self._stream = torch.cuda.Stream(device=self._device)
+    self._error = None
+    self._thread = threading.Thread(target=self._work, daemon=True)
+    self._thread.start()
+
+  def filled(self, s0: int, s1: int):
+    import torch
+    if s1 <= s0:
+      return
+    ev = torch.cuda.Event()
+    ev.record()
+    self._queue.put((ev, int(s0), int(s1)))
+
+  def _work(self):
+    import torch
+    try:
+      arrays = self._host.get() if hasattr(self._host, "get") else self._host
+      self._arrays = arrays
+      with torch.cuda.device(self._device), torch.cuda.stream(self._stream):
+        while True:
+          item = self._queue.get()
+          if item is None:
+            break
+          ev, s0, s1 = item
+          self._stream.wait_event(ev)
+          for buf, arr in zip(self._buffers, arrays):
+            torch.from_numpy(arr[s0:s1]).copy_(buf[s0:s1])
+        self._stream.synchronize()
+    except Exception as e:  # reported by finish()
+      self._error = e
+      while self._queue.get() is not None:
+        pass
+
+  def finish(self) -> list:
+    """Waits for every copy; returns the host arrays."""
+    self._queue.put(None)
+    self._thread.join()
+    if self._error is not None:
+      raise self._error
+    return self._arrays
+
+
 def postprocess_chains(saving: Saving, count: int, variables, treedefs,
-                       extras: dict, model_states, host=None) -> list:
+                       extras: dict, model_states, host=None,
+                       host_filled=False) -> list:
   """Result dicts of C chains from a contiguous ``[count, C, P]`` device
   buffer (extras ``[count, C]``).  With host saving, the buffers of all
   chains are copied to the host at once (one plain device-to-host copy each,
   no kernel), and each chain's arrays are strided views of that copy.
   ``host`` optionally gives the destination arrays (``[count, C, P]``, then
-  one ``[count, C]`` per extra, e.g. from :class:`HostBuffers`)."""
+  one ``[count, C]`` per extra, e.g. from :class:`HostBuffers`);
+  ``host_filled`` says they already hold the data (a :class:`SampleDrain`
+  copied it during the run)."""
   import torch
   C = variables.shape[1]
   if saving is not None and saving.kind == "moments":
@@ -222,10 +284,12 @@ def postprocess_chains(saving: Saving, count: int, variables, treedefs,
   if host is None:
     host = [np.empty(tuple(variables.shape), np.float32)]
     host += [np.empty(tuple(v.shape), np.float64) for v in extras.values()]
-  torch.from_numpy(host[0]).copy_(variables.contiguous())
+  if not host_filled:
+    torch.from_numpy(host[0]).copy_(variables.contiguous())
   hext = {}
   for (k, v), h in zip(extras.items(), host[1:]):
-    torch.from_numpy(h).copy_(v.contiguous())
+    if not host_filled:
+      torch.from_numpy(h).copy_(v.contiguous())
     hext[k] = h
   host = host[0]
   return [postprocess(saving, count, host[:, c], treedefs[c],
