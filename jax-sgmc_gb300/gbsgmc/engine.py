@@ -541,3 +541,150 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
                                {"likelihood": res.sample_lik},
                                [s.model_state for s in states],
                                host=res.host, host_filled=res.host is not None)
+
+
+def try_fused_mh(solver, scheduler, states, schedulers, iterations, saving):
+  """Runs AMAGOLD / SGGMC chains batched (solver.py:301-577): each MH
+  iteration proposes for all chains at once with the [C, P] kernels (the
+  batched value and gradient, the leapfrog or OBABO updates), evaluates the
+  full-data potential of all proposals in one pass over the ordered chunks
+  and decides all chains in one MH launch.  The per-chain streams are the
+  per-chain path's (numpy PCG64 index draws, Philox noise and MH uniforms
+  keyed by chain id), so the samples are the same.  Returns None when the
+  chains do not qualify: a static schedule (no adaptive step size), one key,
+  consecutive chain ids, fresh numpy PCG64 pipelines, no mass adaption, no
+  constant mass or per-parameter friction, no injected noise."""
+  import torch
+  from .potential import StochasticPotential
+  meta = getattr(solver, "meta", {})
+  kind = meta.get("kind")
+  if not FUSED_ENABLED or kind not in ("amagold", "sggmc") or schedulers:
+    return None
+  if meta.get("mass_adaption") is not None:
+    return None
+  integ = meta.get("integrator")
+  im = getattr(integ, "meta", {})
+  if im.get("noise_source") is not None or im.get("const_mass") is not None:
+    return None
+  if not np.isscalar(im.get("friction")):
+    return None
+  want = "reversible_leapfrog" if kind == "amagold" else "obabo"
+  if im.get("kind") != want:
+    return None
+  pot, bfn, full = im.get("potential"), im.get("batch_fn"), meta.get("full_potential")
+  fmap = meta.get("full_data_map")
+  if not isinstance(pot, StochasticPotential) or full is None or not states:
+    return None
+  if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn) \
+      or bfn[1].kind != "host":
+    return None
+  comps = getattr(scheduler, "components", None)
+  if comps is None or any(getattr(comps[k], "table", None) is None
+                          for k in ("step_size", "temperature", "burn_in", "thinning")):
+    return None
+  if len({int(s.key) for s in states}) != 1 or any(s.mh_step != 0 for s in states):
+    return None
+  ists = [s.integrator_state for s in states]
+  chain_ids = [int(i.chain) for i in ists]
+  if chain_ids != list(range(chain_ids[0], chain_ids[0] + len(states))):
+    return None
+  if any(int(i.step) != 0 for i in ists) or len({int(i.key) for i in ists}) != 1:
+    return None
+  ds_list = [i.data_state for i in ists]
+  if any(d.state is None or d.cached_batches is not None for d in ds_list):
+    return None
+  loader = getattr(fmap[1], "loader", None) if isinstance(fmap, tuple) else None
+  if loader is None or loader is not bfn[1].loader:
+    return None
+  rbf = bfn[1]
+  C, n = len(states), rbf.mb_size
+  ds = loader.device_dataset()
+  N = ds.observation_count
+  steps, f = int(im["steps"]), float(im["friction"])
+  X = torch.stack([i.positions for i in ists]).contiguous()
+  Pm = torch.stack([i.momentum for i in ists]).contiguous()
+  P = X.shape[1]
+  U_old = torch.cat([s.potential.reshape(1) for s in states]).to(torch.float64)
+  pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
+  status = torch.zeros(1, dtype=torch.int32, device="cuda")
+  seed, noise_key = int(states[0].key), int(ists[0].key)
+  noise = _lib.noise(noise_key, chain_ids[0])
+  h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
+  per = steps * (2 if kind == "sggmc" else 1)
+  idx = torch.empty((per, C, n), dtype=torch.int32, device="cuda")
+  samples = torch.empty((max(n_kept, 1), C, P), dtype=torch.float32, device="cuda")
+  extra = torch.empty((max(n_kept, 1), C), dtype=torch.float64, device="cuda")
+  accept = torch.empty(C, dtype=torch.int32, device="cuda")
+  ratio = torch.empty(C, dtype=torch.float64, device="cuda")
+  U_keep = torch.empty(C, dtype=torch.float64, device="cuda")
+  rows = loader.static_information["observation_count"]
+  s = _lib.stream_handle()
+  step = 0
+  for k in range(iterations):
+    hk, tk = float(h[k]), float(t[k])
+
+    def sch(kk):
+      return _lib.sched(step_size=hk, temperature=tk, offset=kk)
+
+    x_old, p_old = X.clone(), Pm.clone()
+    _lib.call("gbsgmc_index_draw_pcg64", _lib.ptr(pcg), C, rows, per * n, n,
+              _lib.ptr(idx), n, C * n, _lib.ptr(status), s)
+    if kind == "amagold":
+      # Reversible leapfrog (integrator.py:349-560), as integrator.reversible_leapfrog.
+      energy = torch.zeros(C, dtype=torch.float64, device="cuda")
+      _lib.call("gbsgmc_leapfrog_position", C, P, _lib.ptr(X), _lib.ptr(Pm), None,
+                0.5, sch(step), s)
+      for j in range(steps):
+        if j > 0:
+          _lib.call("gbsgmc_leapfrog_position", C, P, _lib.ptr(X), _lib.ptr(Pm),
+                    None, 1.0, sch(step), s)
+        r = pot.evaluate(X, idx[j], ds, grad=True, observation_count=N)
+        _lib.call("gbsgmc_amagold_momentum", C, P, _lib.ptr(Pm), _lib.ptr(r.grad),
+                  None, f, _lib.ptr(energy), sch(step), noise, s)
+        step += 1
+      _lib.call("gbsgmc_leapfrog_position", C, P, _lib.ptr(X), _lib.ptr(Pm), None,
+                0.5, sch(step), s)
+      stat = energy
+      ke0 = ke1 = None
+    else:
+      # OBABO (integrator.py:138-346); the kinetic energies restart at 0
+      # after each correction (solver.py:536-537).
+      ke0 = torch.zeros(C, dtype=torch.float64, device="cuda")
+      ke1 = torch.zeros(C, dtype=torch.float64, device="cuda")
+      energy = None
+      for j in range(steps):
+        r1 = pot.evaluate(X, idx[2 * j], ds, grad=True, observation_count=N)
+        _lib.call("gbsgmc_obabo_first", C, P, _lib.ptr(X), _lib.ptr(Pm),
+                  _lib.ptr(r1.grad), None, f, _lib.ptr(ke0), sch(step), noise, s)
+        r2 = pot.evaluate(X, idx[2 * j + 1], ds, grad=True, observation_count=N)
+        _lib.call("gbsgmc_obabo_second", C, P, _lib.ptr(Pm), _lib.ptr(r2.grad), None,
+                  f, _lib.ptr(ke1), sch(step), noise, s)
+        step += 1
+      stat = 0.5 * (r1.U + r2.U)
+    U_new, _ = full.value_and_grad_all(X, ds)
+    U_new = U_new.to(torch.float64).contiguous()
+    _lib.call("gbsgmc_mh_accept", C,
+              _lib.MH_AMAGOLD if kind == "amagold" else _lib.MH_SGGMC,
+              _lib.ptr(U_old), _lib.ptr(U_new), _lib.ptr(energy), _lib.ptr(ke0),
+              _lib.ptr(ke1), _lib.sched(step_size=hk, temperature=tk, offset=k),
+              None, seed, chain_ids[0], _lib.ptr(accept), _lib.ptr(ratio),
+              _lib.ptr(U_keep), s)
+    _lib.call("gbsgmc_mh_select", C, P, _lib.ptr(accept), _lib.ptr(X),
+              _lib.ptr(x_old), _lib.ptr(Pm), _lib.ptr(p_old),
+              -1.0 if kind == "amagold" else 1.0, s)
+    U_old = U_keep.clone()
+    if keep[k] >= 0:
+      samples[keep[k]] = X
+      extra[keep[k]] = stat
+  code = int(status.item())
+  if code != 0:
+    raise _lib.GbsgmcError(code, "device status of the batched MH chains")
+  pot.check_status()
+  full._unit.check_status()
+  full._flat.check_status()
+  host = pcg.cpu()   # the streams advanced on the device
+  for c, d in enumerate(ds_list):
+    d.state.copy_(pcg[c] if d.state.is_cuda else host[c])
+  return io.postprocess_chains(saving or io.no_save(), n_kept, samples[:n_kept],
+                               [i.treedef for i in ists], {"energy": extra[:n_kept]},
+                               [i.model_state for i in ists])

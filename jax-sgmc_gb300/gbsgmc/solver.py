@@ -234,7 +234,8 @@ def amagold(integrator_fn, full_potential_fn, full_data_map,
                                  full_potential_fn, full_data_map,
                                  mass_adaption, -1.0)
   return SolverTriplet(init, update, get, kind="amagold",
-                       integrator=integrator_fn)
+                       integrator=integrator_fn, full_potential=full_potential_fn,
+                       full_data_map=full_data_map, mass_adaption=mass_adaption)
 
 
 def sggmc(integrator_fn, full_potential_fn, full_data_map, mass_adaption=None):
@@ -246,7 +247,8 @@ def sggmc(integrator_fn, full_potential_fn, full_data_map, mass_adaption=None):
                                  full_potential_fn, full_data_map,
                                  mass_adaption, 1.0)
   return SolverTriplet(init, update, get, kind="sggmc",
-                       integrator=integrator_fn)
+                       integrator=integrator_fn, full_potential=full_potential_fn,
+                       full_data_map=full_data_map, mass_adaption=mass_adaption)
 
 
 def _flat_of(sample_dict):
@@ -299,6 +301,9 @@ def mcmc(solver, scheduler, strategy="map", saving=None, loading=None):
     if fused is None:
       fused = engine.try_fused_net(solver, scheduler, states, schedulers,
                                    iterations, saving)
+    if fused is None:
+      fused = engine.try_fused_mh(solver, scheduler, states, schedulers,
+                                  iterations, saving)
     if fused is not None:
       return fused
     return [run_single(s, iterations, schedulers) for s in states]
