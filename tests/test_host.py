@@ -360,8 +360,9 @@ def test_take_shuffled_rejects_other_pipelines():
     loader.take_shuffled(e, 1)
 
 
+@pytest.mark.parametrize("in_epochs", [False, True])
 @pytest.mark.parametrize("k", [1, 2])
-def test_shuffled_feed_hands_out_each_chains_batches_in_order(k):
+def test_shuffled_feed_hands_out_each_chains_batches_in_order(k, in_epochs):
   """ShuffledFeed (the host side of a plan's external index source): per
   step and chain, the next k batches the chain's own batch function would
   use -- its cached batches, then cache-sized refills -- whatever the block
@@ -375,7 +376,8 @@ def test_shuffled_feed_hands_out_each_chains_batches_in_order(k):
   states, ref_states = [], []
   for _ in range(C):
     for loader, out in ((fed, states), (ref, ref_states)):
-      cid = loader.register_random_pipeline(cache, mb_size=mb, shuffle=True)
+      cid = loader.register_random_pipeline(cache, mb_size=mb, shuffle=True,
+                                            in_epochs=in_epochs)
       idx, _ = loader._get_indices(cid)
       out.append(CacheState(cached_batches=torch.from_numpy(idx.astype(np.int32)),
                             cached_batches_count=cache, current_line=0,
