@@ -36,6 +36,12 @@ class SgldRun(NamedTuple):
   host: object = None  # [samples, likelihoods] host arrays, when copied
 
 
+# Device bytes the kept samples of a network plan may occupy with host
+# saving; beyond that they pass through a ring of rows emptied to the host
+# during the run.
+RING_BYTES = 4 << 30
+
+
 class _ExternalIndices:
   """Feeds a plan with an external index source: before each run of at
   most one block, the next steps' indices from a :class:`ShuffledFeed` go
@@ -431,19 +437,46 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
   t_tab = torch.from_numpy(np.repeat(np.asarray(t, np.float32), steps)).cuda()
   plan = NetPlan(pot, dataset, X, AUX, rbf.mb_size, kind, h_tab, t_tab,
                  index_src, states[0].key, chain_ids[0], feed=feed, **kw)
-  C = len(states)
-  samples = torch.empty((max(n_kept, 1), C, X.shape[1]), dtype=torch.float32,
-                        device="cuda")
+  C, P = len(states), X.shape[1]
   extra = torch.empty((max(n_kept, 1), C), dtype=torch.float64, device="cuda")
+  # Kept samples: all on the device (device saving), streamed into FP64
+  # moments (moments saving), or through a ring of device rows that a
+  # SampleDrain empties to the host while the chains run (host saving).
+  mom = drain = None
+  kind_saving = saving.kind if saving is not None else "device"
+  ring = max(n_kept, 1)
+  if kind_saving == "moments":
+    mom = io.DeviceMoments(C, P)
+    samples = None
+  else:
+    if kind_saving == "memory":
+      ring = max(1, min(ring, RING_BYTES // max(1, 4 * C * P)))
+    samples = torch.empty((ring, C, P), dtype=torch.float32, device="cuda")
+    if kind_saving == "memory" and ring < n_kept:
+      drain = io.SampleDrain([samples], io.HostBuffers(
+          [((n_kept, C, P), np.float32)]), ring=ring)
+  drained = None
   try:
     done = 0
-    for k in np.nonzero(np.asarray(keep) >= 0)[0]:
-      plan.run(done * steps, (k + 1 - done) * steps)
-      done = k + 1
-      samples[keep[k]] = X
-      extra[keep[k]] = -plan.U if kind == "langevin" else plan.U
-    if done < iterations:
-      plan.run(done * steps, (iterations - done) * steps)
+    try:
+      for k in np.nonzero(np.asarray(keep) >= 0)[0]:
+        plan.run(done * steps, (k + 1 - done) * steps)
+        done = k + 1
+        slot = int(keep[k])
+        if mom is not None:
+          mom.add(X)
+        else:
+          if drain is not None and slot >= ring:
+            drain.wait_copied(slot - ring)   # the row's last sample has left
+          samples[slot % ring] = X
+          if drain is not None:
+            drain.filled(slot, slot + 1)
+        extra[slot] = -plan.U if kind == "langevin" else plan.U
+      if done < iterations:
+        plan.run(done * steps, (iterations - done) * steps)
+    finally:
+      if drain is not None:
+        drained = drain.finish()
     plan.check_status()
   finally:
     plan.close()
@@ -455,10 +488,19 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
       dst = s.data_state.state
       dst.copy_(pcg[c] if dst.is_cuda else host[c])
   key = "likelihood" if kind == "langevin" else "energy"
+  treedefs = [s.treedef for s in states]
+  model_states = [s.model_state for s in states]
+  if mom is not None:
+    return io.moment_results(n_kept, mom, treedefs, {key: extra[:n_kept]},
+                             model_states)
+  if drained is not None:
+    return io.postprocess_chains(saving, n_kept, samples, treedefs,
+                                 {key: extra[:n_kept]}, model_states,
+                                 host=[drained[0], extra[:n_kept].cpu().numpy()],
+                                 host_filled=True)
   return io.postprocess_chains(saving or io.no_save(), n_kept,
-                               samples[:n_kept], [s.treedef for s in states],
-                               {key: extra[:n_kept]},
-                               [s.model_state for s in states])
+                               samples[:n_kept], treedefs,
+                               {key: extra[:n_kept]}, model_states)
 
 
 def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):

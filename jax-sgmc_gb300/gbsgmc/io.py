@@ -127,13 +127,20 @@ class DeviceMoments:
     return mean, var
 
 
-def _moment_results(count, variables, treedefs, extras, model_states):
-  """Per-chain moment results from a ``[count, C, P]`` device buffer."""
-  C, P = variables.shape[1], variables.shape[2]
+def _moment_results(count, variables, treedefs, extras, model_states,
+                    moments=None):
+  """Per-chain moment results from a ``[count, C, P]`` device buffer, or
+  from the :class:`DeviceMoments` ``moments`` the samples went into."""
+  if moments is not None:
+    C, P = moments.chains, moments.P
+  else:
+    C, P = variables.shape[1], variables.shape[2]
   if count == 0:
     mean = var = np.full((C, P), np.nan)
   else:
-    mean_d, var_d = DeviceMoments(C, P).add(variables[:count]).finalize()
+    if moments is None:
+      moments = DeviceMoments(C, P).add(variables[:count])
+    mean_d, var_d = moments.finalize()
     mean, var = mean_d.cpu().numpy(), var_d.cpu().numpy()
   out = []
   for c in range(C):
@@ -210,20 +217,30 @@ class SampleDrain:
   copies those rows of every buffer ([slots, ...] device tensors) into the
   matching host arrays on its own stream.  ``host`` is a list of arrays or a
   :class:`HostBuffers`, fetched by the thread (it may still be faulting in
-  its pages)."""
+  its pages).  With ``ring`` the device buffers hold only ``ring`` rows and
+  slot s lives in row s % ring; :meth:`wait_copied` tells the caller when a
+  row may be written again."""
 
-  def __init__(self, buffers, host):
+  def __init__(self, buffers, host, ring=None):
     import queue
     import torch
     self._buffers = list(buffers)
     self._host = host
+    self._ring = ring
     self._arrays = None
     self._queue = queue.Queue()
     self._device = self._buffers[0].device
     self._stream = torch.cuda.Stream(device=self._device)
     self._error = None
+    self._done = 0                   # slots [0, done) are on the host
+    self._cond = threading.Condition()
     self._thread = threading.Thread(target=self._work, daemon=True)
     self._thread.start()
+
+  def wait_copied(self, slot: int):
+    """Blocks until slot ``slot`` has reached the host."""
+    with self._cond:
+      self._cond.wait_for(lambda: self._done > slot or self._error is not None)
 
   def filled(self, s0: int, s1: int):
     import torch
@@ -246,10 +263,20 @@ class SampleDrain:
           ev, s0, s1 = item
           self._stream.wait_event(ev)
           for buf, arr in zip(self._buffers, arrays):
-            torch.from_numpy(arr[s0:s1]).copy_(buf[s0:s1])
+            if self._ring is None:
+              torch.from_numpy(arr[s0:s1]).copy_(buf[s0:s1])
+            else:
+              for slot in range(s0, s1):
+                torch.from_numpy(arr[slot]).copy_(buf[slot % self._ring])
+          # Copies into pageable memory have completed when copy_ returns.
+          with self._cond:
+            self._done = s1
+            self._cond.notify_all()
         self._stream.synchronize()
     except Exception as e:  # reported by finish()
-      self._error = e
+      with self._cond:
+        self._error = e
+        self._cond.notify_all()
       while self._queue.get() is not None:
         pass
 
@@ -260,6 +287,12 @@ class SampleDrain:
     if self._error is not None:
       raise self._error
     return self._arrays
+
+
+def moment_results(count, moments, treedefs, extras, model_states) -> list:
+  """Result dicts of ``io.moments()`` saving from samples that were streamed
+  into ``moments`` (a :class:`DeviceMoments`) during the run."""
+  return _moment_results(count, None, treedefs, extras, model_states, moments)
 
 
 def postprocess_chains(saving: Saving, count: int, variables, treedefs,

@@ -70,3 +70,39 @@ def test_network_plan_moves_chains_and_keeps_them_distinct(lib):
     start = lik.unravel(inits[c])["W2"]
     assert not np.array_equal(w0[c], start)
   assert not np.array_equal(w0[0], w0[1])
+
+
+def test_kept_samples_through_a_device_ring_equal_the_full_buffer(lib, monkeypatch):
+  """With host saving and more kept samples than the ring holds, the
+  network plan keeps two device rows and a SampleDrain empties them to the
+  host during the run; the samples equal those kept in a full buffer."""
+  from gbsgmc import engine
+  from gbsgmc.likelihoods import MLPGaussian
+  full = run("obabo", fused=True, iterations=8, accepted=5)
+  P = MLPGaussian(d_in=D, h1=H1, h2=H2, sigma=0.1).param_count
+  monkeypatch.setattr(engine, "RING_BYTES", 2 * 3 * P * 4)
+  ringed = run("obabo", fused=True, iterations=8, accepted=5)
+  for a, b in zip(full, ringed):
+    assert a["sample_count"] == b["sample_count"] == 5
+    for leaf in ("W1", "W2", "b3"):
+      np.testing.assert_array_equal(np.asarray(a["samples"]["variables"][leaf]),
+                                    np.asarray(b["samples"]["variables"][leaf]))
+    np.testing.assert_array_equal(a["samples"]["energy"], b["samples"]["energy"])
+
+
+def test_moments_saving_streams_from_the_network_plan(lib, monkeypatch):
+  """io.moments() on the network plan: each kept sample goes into the FP64
+  sums as it is taken; the moments equal those of the saved samples."""
+  from gbsgmc import io
+  from oracle import sgmc_oracle as O
+  saved = run("obabo", fused=True, iterations=8, accepted=5)
+  monkeypatch.setattr(io, "save", lambda *args, **kwargs: io.moments())
+  mom = run("obabo", fused=True, iterations=8, accepted=5)
+  for a, b in zip(saved, mom):
+    assert b["sample_count"] == 5
+    for leaf in ("W2", "b1"):
+      mean, var = O.sample_moments(np.asarray(a["samples"]["variables"][leaf]))
+      np.testing.assert_allclose(b["moments"]["mean"][leaf], mean, rtol=1e-12,
+                                 atol=1e-14)
+      np.testing.assert_allclose(b["moments"]["variance"][leaf], var, rtol=1e-9,
+                                 atol=1e-14)
