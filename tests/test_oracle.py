@@ -246,3 +246,38 @@ def test_sample_moments_oracle():
   m, v = O.sample_moments(a)
   np.testing.assert_array_equal(m, [4.5, 5.5, 6.5])
   np.testing.assert_array_equal(v, [11.25, 11.25, 11.25])
+
+
+@pytest.mark.parametrize("family", [O.LOGISTIC, O.LINEAR_GAUSSIAN, O.LINEAR])
+def test_fisher_oracle_matches_finite_differences(family):
+  """fisher_variance's per-observation gradients (lk'(z_i) x_i) against
+  central differences of the per-observation log-likelihoods, and
+  fisher_noise's replacement rule: corrections <= 0 take the smallest
+  positive one (adaption.py:437-448)."""
+  rng = np.random.default_rng(4)
+  N, d, n = 50, 6, 12
+  X = rng.normal(size=(N, d))
+  y = (rng.random(N) < 0.5).astype(float) if family == O.LOGISTIC else rng.normal(size=N)
+  w = 0.3 * rng.normal(size=d)
+  idx = rng.integers(0, N, size=n)
+  grad = rng.normal(size=d)
+  sigma = 0.7
+  eps = 1e-6
+  per_obs = np.empty((n, d))
+  for j in range(d):
+    e = np.zeros(d)
+    e[j] = eps
+    lp, _ = O.glm_lk(family, X[idx] @ (w + e), y[idx], sigma)
+    lm, _ = O.glm_lk(family, X[idx] @ (w - e), y[idx], sigma)
+    per_obs[:, j] = (lp - lm) / (2 * eps)
+  want = np.sum((per_obs - grad / N) ** 2, axis=0) / (n - 1)
+  np.testing.assert_allclose(O.fisher_variance(w, X, y, idx, grad, N, family, sigma),
+                             want, rtol=1e-6, atol=1e-9)
+  v = O.fisher_variance(w, X, y, idx, grad, N, family, sigma)
+  f = 1.0
+  h = 2.0 * f / np.median(v)
+  cb, bs = O.fisher_noise(w, X, y, idx, grad, N, family, sigma, f, h)
+  corr = f - 0.5 * h * v
+  smallest = corr[corr > 0].min()
+  np.testing.assert_allclose(cb ** 2, np.where(corr <= 0, smallest, corr), rtol=1e-12)
+  np.testing.assert_allclose(bs ** 2 + cb ** 2, f, rtol=1e-12)
