@@ -2,7 +2,7 @@
 
 This package restates the reference (jax_sgmc 0.1.5) arithmetic on the CPU
 with numpy, function by function, each citing the reference file:line it
-follows.  It is the checker of the CUDA path: only ``tests/``,
+follows.  The CUDA path is checked against it: only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py`` (its ``cpu_baseline`` leg and
 ``--impl reference`` arm) may import it.  The product (the ``gbsgmc``
 package and ``libgbsgmc.so``) never calls it.

@@ -1,7 +1,7 @@
 """CPU restatement of jax_sgmc's sampling hot path -- TEST INFRASTRUCTURE ONLY.
 
-Used as the checker by tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline; never by the product path.  numpy only.  Each function cites the
+The CUDA path is checked against it by tests/, __graft_entry__.smoke() and
+bench.py's CPU baseline; the product path never calls it.  numpy only.  Each function cites the
 reference (jax_sgmc 0.1.5) file:line it follows; float32 variants follow the
 reference's operation order so that results agree with the fp32 kernels to
 rounding, float64 variants serve as the accuracy oracle.
