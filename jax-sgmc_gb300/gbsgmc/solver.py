@@ -119,6 +119,12 @@ class MHState(NamedTuple):
   mass_state: Any = None
 
 
+# The reference's state names for the two MH solvers (solver.py:27-64);
+# both share one layout here.
+AMAGOLDState = MHState
+SGGMCState = MHState
+
+
 def _mh_solver(kind, integrator, full_potential_fn, full_data_map,
                mass_adaption, reject_sign):
   init_integrator, update_integrator, get_integrator = integrator
