@@ -420,3 +420,44 @@ def test_take_in_epochs_equals_the_per_batch_epochs(N, mb, counts):
     assert a["rng"].bit_generator.state == b["rng"].bit_generator.state
   with pytest.raises(ValueError):
     bulk.take_in_epochs(bulk.register_random_pipeline(2, mb_size=mb, shuffle=True), 1)
+
+
+def test_statistics_fisher_and_external_index_abi_validation_without_a_gpu():
+  """The sample-statistics, Fisher and external-index entry points reject
+  bad arguments on the host, before any device work."""
+  import ctypes as C
+  from gbsgmc import _lib
+  lib = _lib.load()
+  # Moments: negative chains, a chain stride below P, n < 1.
+  assert lib.gbsgmc_moments_accumulate(-1, 10, 1, 16, 10, 10, 0, 16, 16, 16,
+                                       None) == _lib.ERR_ARG
+  assert lib.gbsgmc_moments_accumulate(2, 10, 1, 16, 20, 5, 0, 16, 16, 16,
+                                       None) == _lib.ERR_ARG
+  assert lib.gbsgmc_moments_accumulate(2, 10, 0, None, 0, 0, 0, None, None, None,
+                                       None) == _lib.OK   # nothing to add
+  assert lib.gbsgmc_moments_finalize(2, 10, 0, 16, 16, 16, 16, 16, None) == _lib.ERR_ARG
+  # Mass adaption counts updates from 1.
+  assert lib.gbsgmc_mass_adapt(10, 0, 5, 16, 16, 16, 16, 16, None, None) == _lib.ERR_ARG
+  # Fisher noise: null model, a minibatch of one row, an unknown family.
+  assert lib.gbsgmc_glm_fisher_noise(None, 1, 8, 16, 8, 16, 16, None, 1.0, 0.1, 16,
+                                     None, 16, None) == _lib.ERR_ARG
+  glm = _lib.Glm()
+  glm.family, glm.d, glm.n_obs, glm.ld, glm.X, glm.y = _lib.GLM_LOGISTIC, 4, 100, 4, 16, 16
+  assert lib.gbsgmc_glm_fisher_noise(C.byref(glm), 1, 1, 16, 1, 16, 16, None, 1.0,
+                                     0.1, 16, None, 16, None) == _lib.ERR_SHAPE
+  glm.family = 9
+  assert lib.gbsgmc_glm_fisher_noise(C.byref(glm), 1, 8, 16, 8, 16, 16, None, 1.0,
+                                     0.1, 16, None, 16, None) == _lib.ERR_ARG
+  assert lib.gbsgmc_sghmc_momentum_noise_model(1, 10, None, 16, 16, _lib.sched(),
+                                               _lib.noise(), None) == _lib.ERR_ARG
+  # External indices need a plan created with an external source.
+  assert lib.gbsgmc_plan_set_indices(None, 16, 1, None) == _lib.ERR_ARG
+  # A replica-exchange plan does not take an external source.
+  mlp = _lib.Mlp(64, 256, 256, 1, 100, 100, 72, 16, None, 0.1, 1.0, 1.0, 0)
+  tp = _lib.Tempering(50, 0, 1.0, 7, 16, 16, 16, 16)
+  h = C.c_void_p()
+  rc = lib.gbsgmc_mlp_resgld_plan_create(C.byref(h), C.byref(mlp), 4, 128, 16,
+                                         16, None, 0.9, 1e-5, _lib.sched(),
+                                         _lib.noise(), _lib.IndexSrc(None, 0, 0, 1),
+                                         C.byref(tp), 16, None, 50, 16)
+  assert rc == _lib.ERR_UNSUPPORTED
