@@ -566,8 +566,9 @@ int gbsgmc_sgld_glm_steps(const gbsgmc_glm* model, int chains, int n,
 #define GBSGMC_STATIC_SCRATCH_BYTES (8u << 20)
 
 /* gbsgmc_sgld_glm_step for callers that cannot allocate device memory --
- * code running inside another runtime's memory pool, code issued during a
- * CUDA graph capture, or loops that must not pay for cudaMalloc/cudaFree.
+ * code running inside another runtime's memory pool (which has reserved the
+ * GPU's memory for itself), host code that receives device pointers but owns
+ * no allocator, or loops that must not pay for cudaMalloc/cudaFree.
  * It has no counterpart in the reference.  Same arguments and results as
  * gbsgmc_sgld_glm_step minus the workspace: the scratch is an array of
  * GBSGMC_STATIC_SCRATCH_BYTES inside the library, held by every GPU that loads
@@ -575,9 +576,10 @@ int gbsgmc_sgld_glm_steps(const gbsgmc_glm* model, int chains, int n,
  * (gbsgmc_glm_workspace_bytes(chains, n, d)) exceeds that size are rejected
  * with GBSGMC_ERR_SHAPE (256 chains with d <= 256 and n <= 16384 fit).  It
  * calls no cudaMalloc, cudaFree or other allocating routine.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress, with that device current); make that first call
- *     before any stream capture.
+ *   - The first call in each CUDA context (normally once per device, with
+ *     that device current) looks up the array's device address
+ *     (cudaGetSymbolAddress) and caches it; make that first call before any
+ *     stream capture.
  *   - Each call clears the part of the array it uses, on `stream`.
  *   - All calls share the one array: calls that may overlap on the GPU
  *     (different streams without an ordering between them) race and must be

@@ -4,13 +4,15 @@
 // partial sums and ticket counters, and expects the caller to allocate it.
 // Some callers cannot do that: code running inside another runtime's device
 // memory pool (an XLA FFI handler whose framework has already reserved most
-// of HBM, so a cudaMalloc beside it fails or fragments the pool), code issued
-// while a CUDA graph is being captured (cudaMalloc/cudaFree are not stream
-// work and cudaFree synchronises the device), and latency-bound loops that
-// must not pay for allocation.  This entry point takes the scratch from a
-// fixed-size array compiled into the library instead.  The array lives in
-// every GPU's memory from the moment the library's module is loaded on that
-// GPU until the process exits.
+// of HBM, so a cudaMalloc beside it fails or fragments the pool), host code
+// that only receives device pointers from its framework and has no allocator
+// of its own, and latency-bound loops that must not pay for cudaMalloc and
+// the device-wide synchronisation of cudaFree.  This entry point takes the
+// scratch from a fixed-size array compiled into the library instead.  The
+// array lives in every GPU's memory from the moment the library's module is
+// loaded on that GPU until the process exits.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -25,33 +27,98 @@ constexpr size_t kStaticScratchBytes = GBSGMC_STATIC_SCRATCH_BYTES;
 // symbol; its device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_sgld_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+// Driver calls that identify the current context, resolved at run time
+// through the runtime (the library links no libcuda).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-// Device address of the scratch on the current device, looked up once per
-// device (with that device current) and cached.
-int scratch_on_current_device(void** out) {
+struct CtxFns {
+  CtxGetCurrentFn current = nullptr;
+  CtxGetIdFn id = nullptr;
+};
+
+const CtxFns& ctx_fns() {
+  static CtxFns fns;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fns.current = reinterpret_cast<CtxGetCurrentFn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fns.id = reinterpret_cast<CtxGetIdFn>(p);
+  });
+  return fns;
+}
+
+// The scratch's device address belongs to the module instance of one CUDA
+// context: a cudaDeviceReset, or a context the caller made with the driver
+// API, loads the module again at another address.  Addresses are therefore
+// cached per context, keyed by the context's process-unique id (cuCtxGetId),
+// or by the device ordinal where the driver offers no context ids.
+struct ScratchEntry {
+  unsigned long long key;
+  void* addr;
+};
+constexpr int kMaxEntries = 64;
+std::mutex g_scratch_mutex;
+ScratchEntry g_scratch[kMaxEntries];
+int g_scratch_used = 0;
+int g_scratch_next = 0;   // entry replaced when the table is full
+
+int context_key(unsigned long long* key) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess)
     return set_error(GBSGMC_ERR_CUDA, "sgld_glm_step_noalloc: cudaGetDevice: %s",
                      cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices)
-    return set_error(GBSGMC_ERR_UNSUPPORTED,
-                     "sgld_glm_step_noalloc: device ordinal %d >= %d", dev,
-                     kMaxDevices);
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (g_scratch_addr[dev] == nullptr) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_sgld_scratch);
-    if (e != cudaSuccess || p == nullptr)
-      return set_error(GBSGMC_ERR_CUDA,
-                       "sgld_glm_step_noalloc: cudaGetSymbolAddress: %s",
-                       cudaGetErrorString(e));
-    g_scratch_addr[dev] = p;
+  // With no context current yet (the runtime makes the device's primary
+  // context current on its first call that needs one), the key is the
+  // device ordinal; the lookup is then repeated once the context exists.
+  const CtxFns& f = ctx_fns();
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (f.current != nullptr && f.id != nullptr && f.current(&ctx) == CUDA_SUCCESS &&
+      ctx != nullptr && f.id(ctx, &id) == CUDA_SUCCESS) {
+    *key = id << 1;   // even: a context id
+    return GBSGMC_OK;
   }
-  *out = g_scratch_addr[dev];
+  *key = (static_cast<unsigned long long>(dev) << 1) | 1ull;   // odd: an ordinal
+  return GBSGMC_OK;
+}
+
+// Device address of the scratch in the current context, looked up once per
+// context (with its device current) and cached.
+int scratch_in_current_context(void** out) {
+  unsigned long long key = 0;
+  int rc = context_key(&key);
+  if (rc != GBSGMC_OK) return rc;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  for (int i = 0; i < g_scratch_used; ++i)
+    if (g_scratch[i].key == key) {
+      *out = g_scratch[i].addr;
+      return GBSGMC_OK;
+    }
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_sgld_scratch);
+  if (e != cudaSuccess || p == nullptr)
+    return set_error(GBSGMC_ERR_CUDA,
+                     "sgld_glm_step_noalloc: cudaGetSymbolAddress: %s",
+                     cudaGetErrorString(e));
+  int slot = g_scratch_used;
+  if (slot < kMaxEntries) {
+    ++g_scratch_used;
+  } else {
+    slot = g_scratch_next;
+    g_scratch_next = (g_scratch_next + 1) % kMaxEntries;
+  }
+  g_scratch[slot] = ScratchEntry{key, p};
+  *out = p;
   return GBSGMC_OK;
 }
 
@@ -78,7 +145,7 @@ extern "C" int gbsgmc_sgld_glm_step_noalloc(
                      "%zu bytes of scratch; the static scratch holds %zu",
                      chains, n, model->d, need, kStaticScratchBytes);
   void* scratch = nullptr;
-  int rc = scratch_on_current_device(&scratch);
+  int rc = scratch_in_current_context(&scratch);
   if (rc != GBSGMC_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // The array keeps whatever the previous call left: clear the part this
