@@ -5,9 +5,12 @@
 //
 // Moments use shifted sums: for each parameter the first kept sample is the
 // shift s (fp32), and the sums S1 = sum (x - s), S2 = sum (x - s)^2 run in
-// fp64.  x - s of two fp32 values is exact in fp64 whenever their exponents
-// differ by less than 29, and so is its square, so the only roundings are the
-// fp64 additions: mean = s + S1 / n, variance = (S2 - S1 (S1 / n)) / n.
+// fp64.  The difference d = x - s of two fp32 values is exact in fp64
+// whenever their exponents differ by less than 29; its square can need up to
+// twice d's significant bits, so S2 += d*d is one fma that rounds once (a
+// relative error of at most 2^-53 per added term).  The other roundings are
+// the fp64 additions of S1 and the final mean = s + S1 / n,
+// variance = (S2 - S1 (S1 / n)) / n.
 // Accumulating more samples later just continues the sums.
 #include <algorithm>
 
