@@ -60,12 +60,12 @@ struct NetPlan final : gbsgmc_plan {
 
   ~NetPlan() override {
     if (stream != nullptr) cudaStreamSynchronize(stream);
-    cudaFree(grad);
-    cudaFree(grad2);
-    cudaFree(U2);
-    cudaFree(idx);
-    cudaFree(ws);
-    cudaFree(sq);
+    plan_free(this, grad);
+    plan_free(this, grad2);
+    plan_free(this, U2);
+    plan_free(this, idx);
+    plan_free(this, ws);
+    plan_free(this, sq);
   }
 
   int enqueue_fused(int g, cudaStream_t s);
@@ -86,9 +86,9 @@ struct NetPlan final : gbsgmc_plan {
   // step j and its first gradient of step j + 1 feed one update pass.
   int alloc_grads(const char* what) {
     const size_t bytes = sizeof(float) * static_cast<size_t>(chains) * P;
-    int rc = cuda_err(cudaMalloc(&grad, bytes), what);
+    int rc = plan_alloc(this, &grad, bytes, what);
     if (rc == GBSGMC_OK && integ.kind == GBSGMC_INTEGRATOR_OBABO)
-      rc = cuda_err(cudaMalloc(&grad2, bytes), what);
+      rc = plan_alloc(this, &grad2, bytes, what);
     return rc;
   }
 
@@ -273,10 +273,10 @@ struct ResgldPlan final : gbsgmc_plan {
 
   ~ResgldPlan() override {
     if (stream != nullptr) cudaStreamSynchronize(stream);
-    cudaFree(grad);
-    cudaFree(idx);
-    cudaFree(ws);
-    cudaFree(var_own);
+    plan_free(this, grad);
+    plan_free(this, idx);
+    plan_free(this, ws);
+    plan_free(this, var_own);
   }
 
   int step_multiple() const override { return temp.every; }
@@ -382,10 +382,10 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
     const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
                           p->draws() * n;
     if ((rc = p->alloc_grads("mlp_plan_create: gradient"))) break;
-    if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "mlp_plan_create: U")))
+    if ((rc = plan_alloc(p, &p->U2, sizeof(double) * chains, "mlp_plan_create: U")))
       break;
-    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "mlp_plan_create: index buffer"))) break;
-    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "mlp_plan_create: workspace"))) break;
+    if ((rc = plan_alloc(p, &p->idx, ibytes, "mlp_plan_create: index buffer"))) break;
+    if ((rc = plan_alloc(p, &p->ws, ws, "mlp_plan_create: workspace"))) break;
     const gbsgmc_mlp m = *model;
     void* wsp = p->ws;
     const float* x = x_dev;
@@ -393,8 +393,7 @@ extern "C" int gbsgmc_mlp_plan_create(gbsgmc_plan** out, const gbsgmc_mlp* model
     p->fused = !(env != nullptr && env[0] == '1') && integ->mass_dev == nullptr;
     if (p->fused) {
       const int nb = update_blocks(chains, p->P);
-      if ((rc = cuda_err(cudaMalloc(&p->sq, sizeof(double) * chains * nb),
-                         "mlp_plan_create: squares")))
+      if ((rc = plan_alloc(p, &p->sq, sizeof(double) * chains * nb, "mlp_plan_create: squares")))
         break;
       mlp_mirror_region(&m, chains, n, wsp, &p->fz.mirror, &p->fz.mirror_count,
                         &p->fz.mirror_stride);
@@ -465,10 +464,10 @@ extern "C" int gbsgmc_cnn_plan_create(gbsgmc_plan** out, const gbsgmc_cnn* model
     const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
                           p->draws() * n;
     if ((rc = p->alloc_grads("cnn_plan_create: gradient"))) break;
-    if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "cnn_plan_create: U")))
+    if ((rc = plan_alloc(p, &p->U2, sizeof(double) * chains, "cnn_plan_create: U")))
       break;
-    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "cnn_plan_create: index buffer"))) break;
-    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "cnn_plan_create: workspace"))) break;
+    if ((rc = plan_alloc(p, &p->idx, ibytes, "cnn_plan_create: index buffer"))) break;
+    if ((rc = plan_alloc(p, &p->ws, ws, "cnn_plan_create: workspace"))) break;
     const gbsgmc_cnn m = *model;
     void* wsp = p->ws;
     const float* x = x_dev;
@@ -538,18 +537,17 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
   do {
     if ((rc = plan_init(p, block_steps))) break;
     if (p->lk_var == nullptr) {
-      if ((rc = cuda_err(cudaMalloc(&p->var_own, sizeof(double) * replicas),
-                         "mlp_resgld_plan_create: var")))
+      if ((rc = plan_alloc(p, &p->var_own, sizeof(double) * replicas, "mlp_resgld_plan_create: var")))
         break;
       p->lk_var = p->var_own;
     }
     const size_t gbytes = sizeof(float) * static_cast<size_t>(replicas) * p->P;
     const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * replicas * n_max;
-    if ((rc = cuda_err(cudaMalloc(&p->grad, gbytes), "mlp_resgld_plan_create: gradient")))
+    if ((rc = plan_alloc(p, &p->grad, gbytes, "mlp_resgld_plan_create: gradient")))
       break;
-    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "mlp_resgld_plan_create: index buffer")))
+    if ((rc = plan_alloc(p, &p->idx, ibytes, "mlp_resgld_plan_create: index buffer")))
       break;
-    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "mlp_resgld_plan_create: workspace"))) break;
+    if ((rc = plan_alloc(p, &p->ws, ws, "mlp_resgld_plan_create: workspace"))) break;
     const gbsgmc_mlp m = *model;
     void* wsp = p->ws;
     const float* x = x_dev;
@@ -607,10 +605,10 @@ extern "C" int gbsgmc_glm_plan_create(gbsgmc_plan** out, const gbsgmc_glm* model
     const size_t ibytes = sizeof(int32_t) * static_cast<size_t>(block_steps) * chains *
                           p->draws() * n;
     if ((rc = p->alloc_grads("glm_plan_create: gradient"))) break;
-    if ((rc = cuda_err(cudaMalloc(&p->U2, sizeof(double) * chains), "glm_plan_create: U")))
+    if ((rc = plan_alloc(p, &p->U2, sizeof(double) * chains, "glm_plan_create: U")))
       break;
-    if ((rc = cuda_err(cudaMalloc(&p->idx, ibytes), "glm_plan_create: index buffer"))) break;
-    if ((rc = cuda_err(cudaMalloc(&p->ws, ws), "glm_plan_create: workspace"))) break;
+    if ((rc = plan_alloc(p, &p->idx, ibytes, "glm_plan_create: index buffer"))) break;
+    if ((rc = plan_alloc(p, &p->ws, ws, "glm_plan_create: workspace"))) break;
     // The GLM workspace's tickets start at zero and are left at zero.
     if ((rc = cuda_err(cudaMemsetAsync(p->ws, 0, ws, p->stream), "glm_plan_create: memset")))
       break;

@@ -21,6 +21,8 @@
 #include <tuple>
 #include <vector>
 
+#include <cuda.h>
+
 #include "common.cuh"
 #include "internal.h"
 #include "plan.cuh"
@@ -28,8 +30,13 @@
 int gbsgmc_plan::run_blocks(int64_t full, int rem) {
   using namespace gbsgmc;
   int rc;
+  if (use_graph && exec == nullptr && blocks_run + full >= 2) {
+    rc = capture_graph(stream, [this]() { return enqueue(G, stream); }, &exec);
+    if (rc) return rc;
+  }
+  blocks_run += full;
   for (int64_t b = 0; b < full; ++b) {
-    if (use_graph) {
+    if (exec != nullptr) {
       if ((rc = cuda_err(cudaGraphLaunch(exec, stream), "plan_run: graph"))) return rc;
     } else if ((rc = enqueue(G, stream))) {
       return rc;
@@ -42,7 +49,7 @@ int gbsgmc_plan::run_blocks(int64_t full, int rem) {
 gbsgmc_plan::~gbsgmc_plan() {
   if (stream != nullptr) cudaStreamSynchronize(stream);
   if (exec != nullptr) cudaGraphExecDestroy(exec);
-  if (base != nullptr) cudaFree(base);
+  gbsgmc::plan_free(this, base);
   if (ev_in != nullptr) cudaEventDestroy(ev_in);
   if (ev_out != nullptr) cudaEventDestroy(ev_out);
   if (stream != nullptr) cudaStreamDestroy(stream);
@@ -88,9 +95,9 @@ struct GlmPlan final : gbsgmc_plan {
     if (e_fork != nullptr) cudaEventDestroy(e_fork);
     if (e_join != nullptr) cudaEventDestroy(e_join);
     if (side != nullptr) cudaStreamDestroy(side);
-    if (ws != nullptr) cudaFree(ws);
-    if (idx != nullptr) cudaFree(idx);
-    if (idx2 != nullptr) cudaFree(idx2);
+    gbsgmc::plan_free(this, ws);
+    gbsgmc::plan_free(this, idx);
+    gbsgmc::plan_free(this, idx2);
   }
   int enqueue(int g, cudaStream_t s) override;
   int run_blocks(int64_t full, int rem) override;
@@ -131,18 +138,98 @@ int plan_init(gbsgmc_plan* p, int G) {
   if ((rc = cuda_err(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming),
                      "plan: event")))
     return rc;
-  if ((rc = cuda_err(cudaMalloc(&p->base, sizeof(int64_t)), "plan: counter"))) return rc;
+  if ((rc = plan_alloc(p, &p->base, sizeof(int64_t), "plan: counter"))) return rc;
   return cuda_err(cudaMemsetAsync(p->base, 0, sizeof(int64_t), p->stream), "plan: memset");
 }
 
 int plan_capture(gbsgmc_plan* p) {
-  int rc = GBSGMC_OK;
-  if (p->use_graph) {
-    rc = capture_graph(p->stream, [p]() { return p->enqueue(p->G, p->stream); },
-                       &p->exec);
-    if (rc) return rc;
-  }
   return cuda_err(cudaStreamSynchronize(p->stream), "plan: sync");
+}
+
+namespace {
+
+// The library's memory pool of the current context, made on first use.
+// Contexts are told apart by their process-unique ids (cuCtxGetId, resolved
+// through the runtime), so a pool never outlives the context it belongs to
+// in this table's eyes.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* q = nullptr;
+    cudaDriverEntryPointQueryResult r;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &q, 4000, cudaEnableDefault,
+                                         &r) == cudaSuccess &&
+        r == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(q);
+    q = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault,
+                                         &r) == cudaSuccess &&
+        r == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(q);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current != nullptr && get_id != nullptr && get_current(&ctx) == CUDA_SUCCESS &&
+      ctx != nullptr && get_id(ctx, &id) == CUDA_SUCCESS)
+    return id << 1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return (static_cast<unsigned long long>(dev) << 1) | 1ull;
+}
+
+constexpr uint64_t kPoolKeepBytes = 2ull << 30;
+std::mutex g_pool_mutex;
+std::vector<std::pair<unsigned long long, cudaMemPool_t>> g_pools;
+
+int library_pool(cudaMemPool_t* out) {
+  const unsigned long long key = current_context_id();
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  for (const auto& e : g_pools)
+    if (e.first == key) {
+      *out = e.second;
+      return GBSGMC_OK;
+    }
+  int dev = 0;
+  int rc;
+  if ((rc = cuda_err(cudaGetDevice(&dev), "plan: device"))) return rc;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  if ((rc = cuda_err(cudaMemPoolCreate(&pool, &props), "plan: memory pool"))) return rc;
+  uint64_t keep = kPoolKeepBytes;
+  if ((rc = cuda_err(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep),
+                     "plan: memory pool"))) {
+    cudaMemPoolDestroy(pool);
+    return rc;
+  }
+  g_pools.emplace_back(key, pool);
+  *out = pool;
+  return GBSGMC_OK;
+}
+
+}  // namespace
+
+int plan_alloc(gbsgmc_plan* p, void** ptr, size_t bytes, const char* what) {
+  *ptr = nullptr;
+  cudaMemPool_t pool = nullptr;
+  int rc;
+  if ((rc = library_pool(&pool))) return rc;
+  if ((rc = cuda_err(cudaMallocFromPoolAsync(ptr, bytes, pool, p->stream), what)))
+    return rc;
+  // A pooled block may hold an earlier plan's data: start from zeros, as the
+  // kernels' counters and partial sums expect of a fresh workspace.
+  return cuda_err(cudaMemsetAsync(*ptr, 0, bytes, p->stream), what);
+}
+
+void plan_free(gbsgmc_plan* p, void* ptr) {
+  if (ptr != nullptr) cudaFreeAsync(ptr, p->stream);
 }
 
 int plan_advance(gbsgmc_plan* p, int g, cudaStream_t s) {
@@ -227,7 +314,7 @@ int GlmPlan::setup_pipeline() {
   using namespace gbsgmc;
   int rc;
   const size_t bytes = sizeof(int32_t) * static_cast<size_t>(G) * chains * n;
-  if ((rc = cuda_err(cudaMalloc(&idx2, bytes), "plan_create: index buffer"))) return rc;
+  if ((rc = plan_alloc(this, &idx2, bytes, "plan_create: index buffer"))) return rc;
   // The block's launch runs at the greatest stream priority and the draws at
   // the least, so that the launch gets its CTAs onto the SMs first and the
   // draws fill the room it leaves.
@@ -493,11 +580,10 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
   do {
     if ((rc = plan_init(p, block_steps))) break;
     p->ws_size = glm_ws_bytes(chains, n, model->d);
-    if ((rc = cuda_err(cudaMalloc(&p->ws, p->ws_size), "plan_create: workspace")))
-      break;
-    if ((rc = cuda_err(cudaMalloc(&p->idx, sizeof(int32_t) * static_cast<size_t>(
-                                                   block_steps) * chains * n),
-                       "plan_create: index buffer")))
+    if ((rc = plan_alloc(p, &p->ws, p->ws_size, "plan_create: workspace"))) break;
+    if ((rc = plan_alloc(p, &p->idx,
+                         sizeof(int32_t) * static_cast<size_t>(block_steps) * chains * n,
+                         "plan_create: index buffer")))
       break;
     if ((rc = cuda_err(cudaMemsetAsync(p->ws, 0, p->ws_size, p->stream),
                        "plan_create: memset")))

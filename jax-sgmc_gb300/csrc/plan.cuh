@@ -30,6 +30,9 @@ struct gbsgmc_plan {
 
   int G = 0;
   bool use_graph = true;
+  // Blocks run so far; the block graph is captured when the plan's second
+  // block is about to run (a plan that runs one block launches it directly).
+  int64_t blocks_run = 0;
   // External index source: the plan's index buffer [G, ext_per_step] int32
   // that gbsgmc_plan_set_indices fills (null when the plan draws its own).
   int32_t* ext_idx = nullptr;
@@ -45,9 +48,26 @@ namespace gbsgmc {
 int cuda_err(cudaError_t e, const char* what);
 // Stream, events and counter of a new plan with blocks of G steps.
 int plan_init(gbsgmc_plan* p, int G);
-// Captures enqueue(G) into p->exec (unless GBSGMC_NO_GRAPH=1) and waits for
-// the plan's stream.
+// Waits for the plan's set-up work.  The block graph (enqueue(G) captured
+// into p->exec, unless GBSGMC_NO_GRAPH=1) is captured later, when the
+// plan's second block is about to run.
 int plan_capture(gbsgmc_plan* p);
+// Device memory of plans comes from one memory pool of the library per
+// CUDA context: allocations and frees are ordered on the plan's stream, and
+// freed blocks (up to a release threshold of 2 GiB) stay in the pool for the
+// next plan instead of going back to the driver, so creating and destroying
+// plans neither synchronises the device nor maps fresh memory each time.
+// Every block handed out is zeroed on the plan's stream.
+int plan_alloc(gbsgmc_plan* p, void** ptr, size_t bytes, const char* what);
+template <class T>
+int plan_alloc(gbsgmc_plan* p, T** ptr, size_t bytes, const char* what) {
+  void* q = nullptr;
+  const int rc = plan_alloc(p, &q, bytes, what);
+  *ptr = static_cast<T*>(q);
+  return rc;
+}
+// Returns plan memory to the pool, ordered after the plan's stream work.
+void plan_free(gbsgmc_plan* p, void* ptr);
 // Enqueues the one-thread launch that advances the counter by g.
 int plan_advance(gbsgmc_plan* p, int g, cudaStream_t s);
 // Captures what body() enqueues on s (and on streams it forks from s) into
