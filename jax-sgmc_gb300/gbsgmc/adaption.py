@@ -65,6 +65,17 @@ def rms_prop() -> AdaptionStrategy:
     return RmsPropState(torch.ones(n, dtype=torch.float32, device=dev),
                         float(alpha), float(lmbd))
 
+  def init_many(samples, alpha=0.9, lmbd=1e-5):
+    """``init`` of the rows of ``samples`` ([C, P]) at once: returns
+    ``(v, alpha, lmbd)`` with ``v`` one [C, P] tensor of ones, whose row c
+    is chain c's state."""
+    import torch
+    V = torch.ones(tuple(samples.shape), dtype=torch.float32,
+                   device=samples.device)
+    return V, float(alpha), float(lmbd)
+
+  init.many = init_many
+
   def update(state: RmsPropState, sample, sample_grad, *args, **kwargs):
     v = state.alpha * state.v + (1 - state.alpha) * sample_grad * sample_grad
     return RmsPropState(v, state.alpha, state.lmbd)

@@ -30,6 +30,19 @@ def _schedule(first_step_size, last_step_size, burn_in, accepted_samples,
                                   progress_bar=progress_bar)
 
 
+def _init_states(solver_init, init, init_samples, **kwargs):
+  """``[init(s) for s in init_samples]``, or for several chains whose
+  samples have one structure the solver's bulk initialisation
+  (``solver_init.many``): a sequence of the same states."""
+  many = getattr(solver_init, "many", None)
+  if many is not None and len(init_samples) > 1:
+    try:
+      return many(list(init_samples), **kwargs)
+    except ValueError:
+      pass   # samples of different structures: one by one
+  return [init(s) for s in init_samples]
+
+
 def sgld(potential_fn, data_loader, cache_size: int = 512,
          batch_size: int = 32, first_step_size: float = 0.05,
          last_step_size: float = 0.001, burn_in: int = 0,
@@ -51,8 +64,10 @@ def sgld(potential_fn, data_loader, cache_size: int = 512,
     init = partial(sgld_solver[0],
                    adaption_kwargs={'alpha': alpha, 'lmbd': lmbd},
                    init_model_state=init_model_state)
-    states = [init(s) for s in init_samples]
-    return mcmc(*states, iterations=iterations)
+    states = _init_states(sgld_solver[0], init, init_samples,
+                          adaption_kwargs={'alpha': alpha, 'lmbd': lmbd},
+                          init_model_state=init_model_state)
+    return mcmc.run_chains(states, iterations=iterations)
 
   return run_fn
 

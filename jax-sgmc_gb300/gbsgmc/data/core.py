@@ -443,6 +443,24 @@ class ShuffledFeed:
     self._pool.shutdown(wait=True)
 
 
+class RandomPipelines(NamedTuple):
+  """C random pipelines of one host loader registered together: their chain
+  ids, their fresh numpy PCG64 stream words as one ``[C, 5]`` int64 host
+  tensor (row c is chain c's ``gbsgmc_pcg64``), and the cache size."""
+  loader: Any
+  chain_ids: Any
+  pcg: Any
+  cached_batches_count: int
+
+  def state(self, i) -> CacheState:
+    """Chain i's :class:`CacheState`, as ``init_fn`` would have returned it
+    (its stream words a row view of ``pcg``)."""
+    return CacheState(cached_batches=None,
+                      cached_batches_count=self.cached_batches_count,
+                      current_line=self.cached_batches_count,
+                      chain_id=self.chain_ids[i], state=self.pcg[i], valid=None)
+
+
 def _random_reference_data_host(loader, cache, mb_size):
   import torch
   N = loader.static_information["observation_count"]
@@ -470,6 +488,20 @@ def _random_reference_data_host(loader, cache, mb_size):
     return CacheState(cached_batches=None, cached_batches_count=cache,
                       current_line=cache, chain_id=chain_id, state=pcg,
                       valid=None)
+
+  def init_many(count, **kwargs):
+    """``count`` calls of ``init_fn(**kwargs)`` at once, as one
+    :class:`RandomPipelines`; None when the chains must register one by one
+    (shuffled pipelines, loaders without bulk registration)."""
+    if kwargs.get("shuffle") or kwargs.get("in_epochs") or \
+        not hasattr(loader, "register_random_pipelines"):
+      return None
+    ids, words = loader.register_random_pipelines(count, cache,
+                                                  mb_size=mb_size, **kwargs)
+    return RandomPipelines(loader, ids, torch.from_numpy(words.view(np.int64)),
+                           cache)
+
+  init_fn.many = init_many
 
   def batch_fn(data_state: CacheState, information=False, device_count=1):
     if data_state.current_line == data_state.cached_batches_count:

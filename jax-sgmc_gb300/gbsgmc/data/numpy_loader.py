@@ -44,6 +44,119 @@ def pcg64_words(seed: int) -> List[int]:
           (int(st["uinteger"]) << 32) | int(st["has_uint32"])]
 
 
+# numpy's SeedSequence is M. O'Neill's seed_seq_fe entropy mixer ("Developing
+# a seed_seq Alternative", 2015) over a pool of four 32-bit words; these are
+# its published hash and mix constants.
+_SS_INIT_A, _SS_MULT_A = 0x43B0D7E5, 0x931E8875
+_SS_INIT_B, _SS_MULT_B = 0x8B51F9DD, 0x58F38DED
+_SS_MIX_L, _SS_MIX_R = 0xCA01F9DD, 0x4973F715
+_PCG64_MULT = 0x2360ED051FC65DA44385DF649FCCF645   # PCG's 128-bit LCG multiplier
+_M32, _M64, _M128 = (1 << 32) - 1, (1 << 64) - 1, (1 << 128) - 1
+
+
+def pcg64_words_many(seeds) -> onp.ndarray:
+  """:func:`pcg64_words` of many chains at once, ``[C, 5]`` uint64.
+
+  The seed hashing runs vectorised over the chains: each chain's assembled
+  entropy is its seed as four little-endian 32-bit words followed by the
+  spawn key word 0 (``SeedSequence(seed).spawn(1)[0]``); the pool is mixed
+  as seed_seq_fe does and four 64-bit words are generated from it, which
+  seed PCG64 as numpy does (state = 0, inc = 2 initseq + 1, one step,
+  state += initstate, one step).  Seeds of 2**128 and above (more entropy
+  words than the pool) fall back to numpy per chain."""
+  seeds = [int(s) for s in seeds]
+  C = len(seeds)
+  if C == 0:
+    return onp.zeros((0, 5), onp.uint64)
+  if any(s < 0 or s >> 128 for s in seeds):
+    return onp.array([pcg64_words(s) for s in seeds], dtype=onp.uint64)
+  u32 = onp.uint32
+  if all(s >> 32 == 0 for s in seeds):
+    ent = [onp.array(seeds, u32)] + [onp.zeros(C, u32) for _ in range(3)]
+  else:
+    ent = [onp.array([(s >> (32 * k)) & _M32 for s in seeds], u32)
+           for k in range(4)]
+  ent.append(onp.zeros(C, u32))                      # the spawn key (0,)
+  with onp.errstate(over="ignore"):
+    h = [_SS_INIT_A]
+
+    def hashmix(v):
+      v = v ^ u32(h[0])
+      h[0] = (h[0] * _SS_MULT_A) & _M32
+      v = v * u32(h[0])
+      return v ^ (v >> u32(16))
+
+    def mix(x, y):
+      r = u32(_SS_MIX_L) * x - u32(_SS_MIX_R) * y
+      return r ^ (r >> u32(16))
+
+    pool = [hashmix(ent[i]) for i in range(4)]
+    for i_src in range(4):
+      for i_dst in range(4):
+        if i_src != i_dst:
+          pool[i_dst] = mix(pool[i_dst], hashmix(pool[i_src]))
+    for i_dst in range(4):
+      pool[i_dst] = mix(pool[i_dst], hashmix(ent[4]))
+    hb = _SS_INIT_B
+    words = []
+    for i in range(8):
+      v = pool[i % 4] ^ u32(hb)
+      hb = (hb * _SS_MULT_B) & _M32
+      v = v * u32(hb)
+      words.append((v ^ (v >> u32(16))).astype(onp.uint64))
+    # generate_state(4, uint64) pairs the words little-endian: 64-bit word k
+    # is words[2k] | words[2k+1] << 32; initstate = w0 << 64 | w1 and
+    # initseq = w2 << 64 | w3.  As 32-bit limbs, least significant first:
+    init = [words[2], words[3], words[0], words[1]]
+    seq = [words[6], words[7], words[4], words[5]]
+    m32 = onp.uint64(_M32)
+    one, s31, s32 = onp.uint64(1), onp.uint64(31), onp.uint64(32)
+    # inc = 2 initseq + 1 (mod 2**128)
+    inc = [((seq[0] << one) | one) & m32]
+    inc += [((seq[k] << one) | (seq[k - 1] >> s31)) & m32 for k in range(1, 4)]
+    # state = (inc + initstate) * MULT + inc (mod 2**128), limb by limb.
+    a, carry = [], onp.zeros(C, onp.uint64)
+    for k in range(4):
+      t = inc[k] + init[k] + carry
+      a.append(t & m32)
+      carry = t >> s32
+    mult = [onp.uint64((_PCG64_MULT >> (32 * k)) & _M32) for k in range(4)]
+    acc = [onp.zeros(C, onp.uint64) for _ in range(4)]
+    for i in range(4):
+      for j in range(4 - i):
+        prod = a[i] * mult[j]                 # < 2**64
+        acc[i + j] += prod & m32
+        if i + j + 1 < 4:
+          acc[i + j + 1] += prod >> s32       # each limb sums < 2**35
+    state, carry = [], onp.zeros(C, onp.uint64)
+    for k in range(4):
+      t = acc[k] + inc[k] + carry
+      state.append(t & m32)
+      carry = t >> s32
+  out = onp.zeros((C, 5), onp.uint64)
+  out[:, 0] = (state[3] << s32) | state[2]
+  out[:, 1] = (state[1] << s32) | state[0]
+  out[:, 2] = (inc[3] << s32) | inc[2]
+  out[:, 3] = (inc[1] << s32) | inc[0]
+  return out
+
+
+class _RandomChain(dict):
+  """A random chain's record whose numpy Generator (``'rng'``) is built
+  from its seed on first use.  Chains registered in bulk start with their
+  PCG64 words alone; the record's items are those of a chain registered
+  one by one."""
+
+  __slots__ = ("seed",)
+
+  def __missing__(self, key):
+    if key == "rng":
+      rng = chain_rng(self.seed)
+      self["rng"] = rng
+      return rng
+    raise KeyError(key)
+
+
 class NumpyBase(DataLoader):
 
   def __init__(self, on_device: bool = True, copy=True, **reference_data):
@@ -168,6 +281,34 @@ class NumpyDataLoader(NumpyBase, HostDataLoader):
                          'random_indices': None, 'mb_size': mb_size,
                          'cache_size': cache_size})
     return chain_id
+
+  def register_random_pipelines(self, count: int, cache_size: int = 1,
+                                mb_size: int = None, **kwargs: Any):
+    """Registers ``count`` random chains at once, as ``count`` calls of
+    :meth:`register_random_pipeline` with the same arguments would (the same
+    chain ids and seeds, so the same streams).  The chains' numpy Generators
+    are built only when first used; their fresh PCG64 states come back as
+    ``[count, 5]`` uint64 ``gbsgmc_pcg64`` words, computed for all chains at
+    once (:func:`pcg64_words_many`).  Returns ``(chain ids, words)``.
+    Shuffled pipelines register one by one."""
+    if kwargs.get("shuffle") or kwargs.get("in_epochs"):
+      raise ValueError("shuffled pipelines are registered one by one")
+    if mb_size > self._observation_count:
+      raise ValueError(f"The batch size cannot be bigger than the observation "
+                       f"count. Provided {mb_size} and "
+                       f"{self._observation_count}")
+    first = len(self._chains)
+    seeds = [kwargs.get("seed", first + i) for i in range(count)]
+    words = pcg64_words_many(seeds)
+    draws = math.ceil(self._observation_count / mb_size)
+    for seed in seeds:
+      rec = _RandomChain(type='random', idx_offset=None, in_epochs=False,
+                         shuffle=False, remaining_samples=0, draws=draws,
+                         random_indices=None, mb_size=mb_size,
+                         cache_size=cache_size)
+      rec.seed = seed
+      self._chains.append(rec)
+    return range(first, first + count), words
 
   def register_ordered_pipeline(self, cache_size: int = 1, mb_size: int = None,
                                 **kwargs) -> int:

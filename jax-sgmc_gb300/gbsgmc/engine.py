@@ -34,6 +34,7 @@ class SgldRun(NamedTuple):
   sample_lik: object   # fp64 [S, C]
   launches: int
   host: object = None  # [samples, likelihoods] host arrays, when copied
+  early: object = None # what on_enqueued returned
 
 
 # Device bytes the kept samples of a network plan may occupy with host
@@ -174,12 +175,17 @@ class IndexSource:
 
 def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
                  index_src, noise_seed=0, chain_base=0, alpha=0.9, lmbd=1e-5,
-                 block_steps=None, feed=None, host=None) -> SgldRun:
+                 block_steps=None, feed=None, host=None,
+                 on_enqueued=None) -> SgldRun:
   """Runs ``iterations`` fused SGLD steps for all chains (W, V updated in
   place) and returns the final state and the kept samples.  With ``host``
   (the kept samples' and likelihoods' host arrays, or a HostBuffers), the
-  samples each block keeps are copied there while the next blocks run, and
-  ``SgldRun.host`` holds the filled arrays."""
+  kept samples are copied there -- each block's while the next blocks run,
+  or, for a run of one block, all at once after it -- and ``SgldRun.host``
+  holds the filled arrays.  For a run of one block, ``on_enqueued(arrays)``
+  is called with the host arrays once the block is enqueued and before
+  they are filled (host work that overlaps the GPU's), and its value is
+  ``SgldRun.early``."""
   import torch
   if block_steps is None:
     block_steps = min(DEFAULT_BLOCK_STEPS, max(1, iterations))
@@ -190,8 +196,18 @@ def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
                      k_tab, n_kept, index_src, noise_seed, chain_base,
                      block_steps, feed=feed)
   try:
-    filled = None
-    if host is not None and n_kept > 0:
+    filled = early = None
+    if host is not None and n_kept > 0 and iterations <= block_steps \
+        and plan.external is None:
+      # One block: enqueue it, let the host work meanwhile, then copy.
+      plan.run(0, iterations)
+      launches = plan.launches(iterations)
+      filled = host.get() if hasattr(host, "get") else host
+      if on_enqueued is not None:
+        early = on_enqueued(filled)
+      torch.from_numpy(filled[0]).copy_(plan.samples[:n_kept])
+      torch.from_numpy(filled[1]).copy_(plan.sample_lik[:n_kept])
+    elif host is not None and n_kept > 0:
       # One run per block, so that each block's kept samples can leave
       # while the next block runs.
       drain = io.SampleDrain([plan.samples, plan.sample_lik], host)
@@ -213,7 +229,7 @@ def run_sgld_glm(potential, dataset, W, V, n, iterations, h, t, keep, n_kept,
       launches = plan.launches(iterations)
     plan.check_status()
     return SgldRun(W, V, plan.U, plan.lk_var, plan.samples[:n_kept],
-                   plan.sample_lik[:n_kept], launches, filled)
+                   plan.sample_lik[:n_kept], launches, filled, early)
   finally:
     plan.close()
 
@@ -505,8 +521,12 @@ def try_fused_net(solver, scheduler, states, schedulers, iterations, saving):
 
 def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
   """Runs the chains through :func:`run_sgld_glm` when they qualify;
-  returns None otherwise (the caller then steps chain by chain)."""
+  returns None otherwise (the caller then steps chain by chain).  Chains
+  made together (:class:`~gbsgmc.integrator.LangevinChains`) move as whole
+  [C, ...] tensors, and their result dicts are assembled while the GPU
+  runs."""
   import torch
+  from .integrator import LangevinChains
   from .potential import StochasticPotential
   meta = getattr(solver, "meta", {})
   if not FUSED_ENABLED or meta.get("kind") != "sgmc" or schedulers:
@@ -517,72 +537,104 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
     return None
   pot = im.get("potential")
   bfn = im.get("batch_fn")
-  if not isinstance(pot, StochasticPotential) or pot.is_network or not states:
+  if not isinstance(pot, StochasticPotential) or pot.is_network or not len(states):
     return None
   if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn):
     return None
   rbf = bfn[1]
-  keys = {s.key for s in states}
-  if len(keys) != 1:
-    return None
-  adapt = [s.adapt_state for s in states]
-  if any(a is None for a in adapt) and not all(a is None for a in adapt):
-    return None
-  chain_ids = [int(s.chain) for s in states]
-  if chain_ids != list(range(chain_ids[0], chain_ids[0] + len(states))):
-    return None
+  C = len(states)
   feed = None
-  if rbf.kind == "host":
-    ds_list = [s.data_state for s in states]
-    if ShuffledFeed.qualifies(rbf.loader, ds_list):
-      # Shuffled streams: the host loader draws them, the plan reads them.
-      feed = ShuffledFeed(rbf.loader, ds_list, 1)
-      index_src = IndexSource(chain_base=chain_ids[0], external=True)
-    elif any(d.state is None or d.cached_batches is not None for d in ds_list):
-      return None   # draws already consumed
-    else:
-      pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
-      index_src = IndexSource(pcg=pcg, chain_base=chain_ids[0])
-  else:
-    seeds = {s.data_state.state[0] for s in states}
-    if len(seeds) != 1 or any(s.data_state.state[1] != 0 for s in states):
+  if isinstance(states, LangevinChains):
+    # Fresh chains made together: consecutive ids, one key, step 0.
+    if rbf.kind != "host" or states.pipelines.loader is not rbf.loader:
       return None
-    index_src = IndexSource(seed=seeds.pop(), chain_base=chain_ids[0])
-  dataset = rbf.loader.device_dataset()
-  W = torch.stack([s.latent_variables for s in states]).contiguous().cuda()
-  if W.shape[1] != pot.dim(dataset):
-    return None
-  if adapt[0] is not None:
-    V = torch.stack([a.v for a in adapt]).contiguous().cuda()
-    alpha, lmbd = adapt[0].alpha, adapt[0].lmbd
+    chain_base, key = int(states.chain_ids[0]), states.key
+    W = states.positions.cuda()
+    V = None if states.rms_v is None else states.rms_v.cuda()
+    alpha, lmbd = states.alpha, states.lmbd
+    index_src = IndexSource(pcg=states.pipelines.pcg.cuda(), chain_base=chain_base)
+    treedefs = [states.treedef] * C
+    model_states = [states.model_state] * C
   else:
-    V, alpha, lmbd = None, 0.9, 1e-5
+    keys = {s.key for s in states}
+    if len(keys) != 1:
+      return None
+    key = states[0].key
+    adapt = [s.adapt_state for s in states]
+    if any(a is None for a in adapt) and not all(a is None for a in adapt):
+      return None
+    chain_ids = [int(s.chain) for s in states]
+    if chain_ids != list(range(chain_ids[0], chain_ids[0] + C)):
+      return None
+    chain_base = chain_ids[0]
+    if rbf.kind == "host":
+      ds_list = [s.data_state for s in states]
+      if ShuffledFeed.qualifies(rbf.loader, ds_list):
+        # Shuffled streams: the host loader draws them, the plan reads them.
+        feed = ShuffledFeed(rbf.loader, ds_list, 1)
+        index_src = IndexSource(chain_base=chain_base, external=True)
+      elif any(d.state is None or d.cached_batches is not None for d in ds_list):
+        return None   # draws already consumed
+      else:
+        pcg = torch.stack([d.state for d in ds_list]).contiguous().cuda()
+        index_src = IndexSource(pcg=pcg, chain_base=chain_base)
+    else:
+      seeds = {s.data_state.state[0] for s in states}
+      if len(seeds) != 1 or any(s.data_state.state[1] != 0 for s in states):
+        return None
+      index_src = IndexSource(seed=seeds.pop(), chain_base=chain_base)
+    W = torch.stack([s.latent_variables for s in states]).contiguous().cuda()
+    if adapt[0] is not None:
+      V = torch.stack([a.v for a in adapt]).contiguous().cuda()
+      alpha, lmbd = adapt[0].alpha, adapt[0].lmbd
+    else:
+      V, alpha, lmbd = None, 0.9, 1e-5
+    treedefs = [s.treedef for s in states]
+    model_states = [s.model_state for s in states]
+  dataset = rbf.loader.device_dataset()
+  if W.shape[1] != pot.dim(dataset):
+    if feed is not None:
+      feed.close()
+    return None
   h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
   block = min(rbf.cached_batches_count, DEFAULT_BLOCK_STEPS, max(iterations, 1))
   outbuf = None
+  early = None
   if saving is not None and saving.kind == "memory":
-    outbuf = io.HostBuffers([((n_kept, len(states), W.shape[1]), np.float32),
-                             ((n_kept, len(states)), np.float64)])
+    outbuf = io.HostBuffers([((n_kept, C, W.shape[1]), np.float32),
+                             ((n_kept, C), np.float64)])
+    if getattr(saving.collector, "_dir", None) is None:
+      # Collectors that write nothing take views of the host arrays, so the
+      # result dicts can be built before the samples arrive.
+      def early(arrays):
+        return io.postprocess_chains(saving, n_kept, arrays[0], treedefs,
+                                     {"likelihood": arrays[1]}, model_states,
+                                     host=arrays, host_filled=True)
   try:
     res = run_sgld_glm(pot, dataset, W, V, rbf.mb_size, iterations, h, t, keep,
-                       n_kept, index_src, noise_seed=states[0].key,
-                       chain_base=chain_ids[0], alpha=alpha, lmbd=lmbd,
-                       block_steps=block, feed=feed, host=outbuf)
+                       n_kept, index_src, noise_seed=key, chain_base=chain_base,
+                       alpha=alpha, lmbd=lmbd, block_steps=block, feed=feed,
+                       host=outbuf, on_enqueued=early)
   finally:
     if feed is not None:
       feed.close()
-  if rbf.kind == "host" and feed is None:
+  if isinstance(states, LangevinChains):
+    # The streams advanced on the device: every chain's stream words are a
+    # row of the pipelines' host tensor.
+    states.pipelines.pcg.copy_(index_src.pcg)
+  elif rbf.kind == "host" and feed is None:
     # The streams advanced on the device; states still holding their
     # initial host words get them back in one copy.
     host = index_src.pcg.cpu()
     for c, s in enumerate(states):
       dst = s.data_state.state
       dst.copy_(index_src.pcg[c] if dst.is_cuda else host[c])
+  if res.early is not None:
+    return res.early
   return io.postprocess_chains(saving or io.no_save(), n_kept, res.samples,
-                               [s.treedef for s in states],
-                               {"likelihood": res.sample_lik},
-                               [s.model_state for s in states],
-                               host=res.host, host_filled=res.host is not None)
+                               treedefs, {"likelihood": res.sample_lik},
+                               model_states, host=res.host,
+                               host_filled=res.host is not None)
 
 
 def try_fused_mh(solver, scheduler, states, schedulers, iterations, saving):

@@ -17,6 +17,7 @@ oracle on identical noise).
 
 from __future__ import annotations
 
+from collections.abc import Sequence
 from typing import Any, Callable, NamedTuple
 
 import numpy as np
@@ -159,6 +160,54 @@ def _eval(potential_fn, w, batch, info, want_grad=True):
                                observation_count=n_obs)
 
 
+class LangevinChains(Sequence):
+  """The initial states of C chains of :func:`langevin_diffusion` made
+  together (``init_fn.many``), held as whole host tensors: positions
+  [C, P], RMSprop ``v`` [C, P] (or None) and the chains' data pipelines
+  (:class:`gbsgmc.data.core.RandomPipelines`, whose stream words are one
+  [C, 5] tensor).  Indexing gives chain i's :class:`LangevinState`, whose
+  tensors are row views of these (made on first access and kept), so the
+  sequence stands for the list of states; the fused driver moves each
+  whole tensor in one copy instead."""
+
+  def __init__(self, positions, rms_v, alpha, lmbd, pipelines, key,
+               model_state, treedef):
+    self.positions, self.rms_v = positions, rms_v
+    self.alpha, self.lmbd = float(alpha), float(lmbd)
+    self.pipelines = pipelines
+    self.key = key
+    self.model_state = model_state
+    self.treedef = treedef
+    self._states = [None] * int(positions.shape[0])
+
+  @property
+  def chain_ids(self):
+    return self.pipelines.chain_ids
+
+  def __len__(self):
+    return len(self._states)
+
+  def __getitem__(self, i):
+    if isinstance(i, slice):
+      return [self[j] for j in range(*i.indices(len(self)))]
+    if i < 0:
+      i += len(self)
+    st = self._states[i]   # raises IndexError past the end
+    if st is None:
+      import torch
+      from .adaption import RmsPropState
+      adapt = None if self.rms_v is None else \
+          RmsPropState(self.rms_v[i], self.alpha, self.lmbd)
+      st = LangevinState(
+          latent_variables=self.positions[i], model_state=self.model_state,
+          key=self.key, adapt_state=adapt, data_state=self.pipelines.state(i),
+          potential=torch.zeros((), dtype=torch.float64),
+          variance=torch.ones((), dtype=torch.float64), step=0,
+          chain=int(self.pipelines.chain_ids[i]), treedef=self.treedef)
+      self._states[i] = st
+    return st
+
+
 def langevin_diffusion(potential_fn, batch_fn, adaption: AdaptionStrategy = None,
                        noise_source: Callable = None):
   """SGLD with optional RMSprop (integrator.py:767-924)."""
@@ -183,6 +232,36 @@ def langevin_diffusion(potential_fn, batch_fn, adaption: AdaptionStrategy = None
         potential=torch.zeros((), dtype=torch.float64),
         variance=torch.ones((), dtype=torch.float64),
         step=0, chain=chain, treedef=tdef)
+
+  def init_many(init_samples, key=0, adaption_kwargs=None, batch_kwargs=None,
+                init_model_state=None):
+    """``[init_fn(s, key, ...) for s in init_samples]`` in bulk.  With host
+    random pipelines that register in bulk, the chains come back as one
+    :class:`LangevinChains` (the samples raveled into one [C, P] tensor, the
+    RMSprop states and the pipelines' stream words made for all chains at
+    once); otherwise as a list of states made one by one."""
+    import torch
+    adaption_kwargs = adaption_kwargs or {}
+    batch_kwargs = batch_kwargs or {}
+    many = getattr(batch_init, "many", None)
+    if adaption is not None and getattr(adaption.init, "many", None) is None:
+      many = None
+    if many is None:
+      return [init_fn(s, key, adaption_kwargs, batch_kwargs, init_model_state)
+              for s in init_samples]
+    flat, tdef = util.ravel_many(init_samples)
+    pipelines = many(len(init_samples), **batch_kwargs)
+    if pipelines is None:
+      return [init_fn(s, key, adaption_kwargs, batch_kwargs, init_model_state)
+              for s in init_samples]
+    W = torch.from_numpy(flat)
+    V, alpha, lmbd = None, 0.9, 1e-5
+    if adaption is not None:
+      V, alpha, lmbd = adaption.init.many(W, **adaption_kwargs)
+    return LangevinChains(W, V, alpha, lmbd, pipelines, key_to_seed(key),
+                          init_model_state, tdef)
+
+  init_fn.many = init_many
 
   def get_fn(state: LangevinState):
     return {"variables": state.latent_variables,

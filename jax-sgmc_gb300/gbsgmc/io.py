@@ -190,9 +190,19 @@ class HostBuffers:
   runs, so that the final device-to-host copy does not pay the page faults
   of fresh memory (most of its cost for a few hundred MB)."""
 
+  # Below this total the arrays are made in the caller's thread (starting
+  # a thread would cost more than the page faults it hides).
+  SMALL_BYTES = 32 << 20
+
   def __init__(self, specs):
     self._specs = list(specs)
     self._arrays = None
+    self._thread = None
+    total = sum(int(np.prod(shape, dtype=np.int64)) * np.dtype(dt).itemsize
+                for shape, dt in self._specs)
+    if total < self.SMALL_BYTES:
+      self._arrays = [np.empty(shape, dt) for shape, dt in self._specs]
+      return
     self._thread = threading.Thread(target=self._fill, daemon=True)
     self._thread.start()
 
@@ -206,7 +216,8 @@ class HostBuffers:
     self._arrays = out
 
   def get(self):
-    self._thread.join()
+    if self._thread is not None:
+      self._thread.join()
     return self._arrays
 
 
@@ -325,6 +336,19 @@ def postprocess_chains(saving: Saving, count: int, variables, treedefs,
       torch.from_numpy(h).copy_(v.contiguous())
     hext[k] = h
   host = host[0]
-  return [postprocess(saving, count, host[:, c], treedefs[c],
-                      {k: v[:, c] for k, v in hext.items()}, model_states[c])
-          for c in range(C)]
+  # What postprocess() does for host saving, with each tree definition's
+  # leaf layout worked out once for all chains that share it.
+  unravelers = {}
+  out = []
+  for c in range(C):
+    td = treedefs[c]
+    f = unravelers.get(id(td))
+    if f is None:
+      f = unravelers[id(td)] = util.unraveler(td)
+    samples = {"variables": f(host[:, c])}
+    for k, v in hext.items():
+      samples[k] = v[:, c]
+    samples["model_state"] = model_states[c]
+    out.append({"sample_count": count,
+                "samples": saving.collector.finalize(samples)})
+  return out

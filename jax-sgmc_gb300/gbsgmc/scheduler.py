@@ -141,6 +141,13 @@ def tables(scheduler, iterations: int, **scheduler_kwargs):
   ``keep = burn_in and accept`` rule of solver.mcmc (solver.py:103-104).
   """
   init_fn, update_fn, get_fn = scheduler
+  # Tables of the component schedulers' own (vectorised) tables depend on
+  # the iteration count alone: a scheduler keeps the last few it made.
+  cache = getattr(scheduler, "__dict__", {}).setdefault("_tables", {}) \
+      if not scheduler_kwargs else None
+  if cache is not None and iterations in cache:
+    h, t, keep, n, static = cache[iterations]
+    return h.copy(), t.copy(), keep.copy(), n, static
   state, static = init_fn(iterations, **scheduler_kwargs)
   vec = _vector_tables(scheduler, state, iterations)
   if vec is not None:
@@ -149,6 +156,10 @@ def tables(scheduler, iterations: int, **scheduler_kwargs):
     kept = (vec["burn_in"] > 0) & vec["thinning"].astype(bool)
     keep = np.full(iterations, -1, np.int32)
     keep[kept] = np.arange(int(kept.sum()), dtype=np.int32)
+    if cache is not None:
+      if len(cache) >= 8:
+        cache.pop(next(iter(cache)))
+      cache[iterations] = (h.copy(), t.copy(), keep.copy(), int(kept.sum()), static)
     return h, t, keep, int(kept.sum()), static
   h = np.empty(iterations, np.float32)
   t = np.empty(iterations, np.float32)

@@ -33,6 +33,10 @@ def sgmc(integrator):
   def init(*args, **kwargs):
     return init_integrator(*args, **kwargs)
 
+  many = getattr(init_integrator, "many", None)
+  if many is not None:
+    init.many = many
+
   def update(state, schedule):
     return update_integrator(state, schedule), None
 
@@ -296,12 +300,14 @@ def mcmc(solver, scheduler, strategy="map", saving=None, loading=None):
     return io.postprocess(saving or io.no_save(), n_kept, samples, treedef,
                           {extra_key: extra})
 
-  def run(*states, schedulers=None, iterations=100000):
+  def run_chains(states, schedulers=None, iterations=100000):
+    """``run(*states)`` over a sequence of chain states, such as the
+    :class:`~gbsgmc.integrator.LangevinChains` of a bulk initialisation
+    (which the fused driver moves as whole tensors)."""
     iterations = int(iterations)
     if loading is not None:
       raise NotImplementedError("Loading of checkpoints is currently not "
                                 "supported.")
-    states = list(states)
     fused = engine.try_fused_sgld(solver, scheduler, states, schedulers,
                                   iterations, saving)
     if fused is None:
@@ -314,6 +320,10 @@ def mcmc(solver, scheduler, strategy="map", saving=None, loading=None):
       return fused
     return [run_single(s, iterations, schedulers) for s in states]
 
+  def run(*states, schedulers=None, iterations=100000):
+    return run_chains(list(states), schedulers, iterations)
+
+  run.run_chains = run_chains
   return run
 
 

@@ -99,6 +99,59 @@ def ravel(tree: PyTree) -> Tuple[np.ndarray, TreeDef]:
   return flat, tdef
 
 
+def ravel_many(trees) -> Tuple[np.ndarray, TreeDef]:
+  """:func:`ravel` of each tree of one structure, as the rows of one
+  ``[len(trees), P]`` float32 array, with the first tree's definition.
+  Dicts of array leaves are stacked key by key; other trees are raveled one
+  by one.  Raises ValueError when the trees differ in structure."""
+  trees = list(trees)
+  if not trees:
+    raise ValueError("no trees")
+  _, tdef = tree_flatten(trees[0])
+  C = len(trees)
+  if tdef.kind == "dict" and tdef.children and \
+      all(c.kind == "leaf" for c in tdef.children) and \
+      all(type(t) is dict and len(t) == len(tdef.keys) for t in trees):
+    try:
+      cols = []
+      for k, child in zip(tdef.keys, tdef.children):
+        a = np.stack([np.asarray(t[k]) for t in trees])
+        if a.shape[1:] != tuple(child.shape):
+          raise ValueError("leaf shapes differ")
+        cols.append(a.reshape(C, -1).astype(np.float32, copy=False))
+      flat = cols[0] if len(cols) == 1 else np.concatenate(cols, axis=1)
+      return np.ascontiguousarray(flat, np.float32), tdef
+    except (KeyError, TypeError, ValueError, RuntimeError):
+      pass
+  rows = []
+  for t in trees:
+    flat, d = ravel(t)
+    if d.kind != tdef.kind or d.keys != tdef.keys or \
+        leaf_shapes(d) != leaf_shapes(tdef):
+      raise ValueError("the samples differ in structure")
+    rows.append(flat)
+  return np.stack(rows).astype(np.float32, copy=False), tdef
+
+
+def unraveler(tdef: TreeDef):
+  """:func:`unravel` for one tree definition, with its leaf layout worked
+  out once: returns ``f(flat) -> tree`` for numpy or torch ``flat``."""
+  if tdef.kind == "dict" and all(c.kind == "leaf" for c in tdef.children):
+    spec, o = [], 0
+    for k, c in zip(tdef.keys, tdef.children):
+      n = int(np.prod(c.shape, dtype=np.int64))
+      spec.append((k, o, o + n, tuple(c.shape)))
+      o += n
+
+    def f(flat):
+      flat = _to_numpy(flat)
+      lead = flat.shape[:-1]
+      return {k: flat[..., a:b].reshape(lead + shape) for k, a, b, shape in spec}
+
+    return f
+  return lambda flat: unravel(tdef, flat)
+
+
 def unravel(tdef: TreeDef, flat) -> PyTree:
   """Inverse of :func:`ravel`; ``flat`` may carry leading batch axes."""
   flat = _to_numpy(flat)

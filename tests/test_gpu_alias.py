@@ -125,3 +125,22 @@ def test_other_presets_return_reference_format(lib):
   res = run((sample, sample), iterations=40)
   assert res[0]["sample_count"] == 10
   assert np.all(np.isfinite(res[0]["samples"]["variables"]["w"]))
+
+
+def test_bulk_initialisation_equals_one_by_one(lib, monkeypatch):
+  """alias.sgld initialises many chains in bulk (one ChainGroup: stacked
+  samples, RMSprop states and PCG64 words computed for all chains at once);
+  its samples and advanced index streams must equal those of chains
+  initialised one by one, bit for bit."""
+  from gbsgmc import alias
+  X, y = linreg(N=4000, d=16, seed=9)
+  bulk = sgld_run(X, y, 120, chains=7, accepted=30, batch=64)
+  monkeypatch.setattr(alias, "_init_states",
+                      lambda solver_init, init, samples, **kw:
+                      [init(s) for s in samples])
+  single = sgld_run(X, y, 120, chains=7, accepted=30, batch=64)
+  for a, b in zip(bulk, single):
+    np.testing.assert_array_equal(a["samples"]["variables"]["w"],
+                                  b["samples"]["variables"]["w"])
+    np.testing.assert_array_equal(a["samples"]["likelihood"],
+                                  b["samples"]["likelihood"])

@@ -461,3 +461,63 @@ def test_statistics_fisher_and_external_index_abi_validation_without_a_gpu():
                                          _lib.noise(), _lib.IndexSrc(None, 0, 0, 1),
                                          C.byref(tp), 16, None, 50, 16)
   assert rc == _lib.ERR_UNSUPPORTED
+
+
+def test_bulk_pcg64_seeding_equals_numpy():
+  """pcg64_words_many restates SeedSequence(seed).spawn(1)[0] -> PCG64 for
+  many seeds at once; it must give numpy's own states bit for bit."""
+  from gbsgmc.data.numpy_loader import pcg64_words, pcg64_words_many
+  seeds = list(range(600)) + [2**31 - 1, 2**32 - 1, 2**32, 2**40 + 7,
+                              2**63 + 11, 2**64 + 3, 2**100 + 12345,
+                              2**128 - 1, 2**128, 2**130 + 5]
+  got = pcg64_words_many(seeds)
+  want = np.array([pcg64_words(s) for s in seeds], np.uint64)
+  np.testing.assert_array_equal(got, want)
+  assert pcg64_words_many([]).shape == (0, 5)
+
+
+def test_bulk_pipeline_registration_equals_one_by_one():
+  from gbsgmc import data
+  X = np.random.default_rng(0).normal(size=(500, 3)).astype(np.float32)
+  a = data.NumpyDataLoader(x=X)
+  b = data.NumpyDataLoader(x=X)
+  a.register_random_pipeline(4, mb_size=7)          # chains before the bulk
+  b.register_random_pipeline(4, mb_size=7)
+  ids = [a.register_random_pipeline(4, mb_size=7) for _ in range(5)]
+  got_ids, words = b.register_random_pipelines(5, 4, mb_size=7)
+  assert list(got_ids) == ids
+  for c in ids:
+    st = a._chains[c]["rng"].bit_generator.state
+    s, inc = st["state"]["state"], st["state"]["inc"]
+    w = words[c - 1]
+    assert (int(w[0]) << 64 | int(w[1])) == s and (int(w[2]) << 64 | int(w[3])) == inc
+    # The lazily built generator and the checkpoint are the one-by-one ones.
+    assert a.save_state(c) == b.save_state(c)
+    np.testing.assert_array_equal(a.get_batches(c)[0]["x"], b.get_batches(c)[0]["x"])
+  with pytest.raises(ValueError):
+    b.register_random_pipelines(2, 4, mb_size=7, shuffle=True)
+  with pytest.raises(ValueError):
+    b.register_random_pipelines(2, 4, mb_size=501)
+
+
+def test_ravel_many_and_unraveler_match_ravel_and_unravel():
+  from gbsgmc import util
+  rng = np.random.default_rng(1)
+  trees = [{"w": rng.normal(size=(3, 2)), "b": rng.normal(size=4).astype(np.float32)}
+           for _ in range(6)]
+  flat, tdef = util.ravel_many(trees)
+  assert flat.dtype == np.float32 and flat.shape == (6, 10)
+  for c, t in enumerate(trees):
+    one, d = util.ravel(t)
+    np.testing.assert_array_equal(flat[c], one)
+  f = util.unraveler(tdef)
+  stacked = np.stack([flat, 2 * flat])          # leading axes as in [S, P]
+  for k, v in util.unravel(tdef, stacked).items():
+    np.testing.assert_array_equal(f(stacked)[k], v)
+  nested = [{"a": [np.ones(2), np.zeros(1)]} for _ in range(3)]
+  flat2, _ = util.ravel_many(nested)
+  np.testing.assert_array_equal(flat2, np.tile([1, 1, 0], (3, 1)))
+  with pytest.raises(ValueError):
+    util.ravel_many([{"w": np.ones(2)}, {"v": np.ones(2)}])
+  with pytest.raises(ValueError):
+    util.ravel_many([{"w": np.ones(2)}, {"w": np.ones(3)}])
