@@ -774,9 +774,11 @@ def sgld_glm_cpu_steps(X, y, W, V, rngs, steps, h, T, family, sigma=1.0,
                        lmbd=1e-5, noise_rng=None, threads=1):
   """The reference's SGLD(+RMSprop) hot loop on the CPU in float32 for C
   chains: per chain and step the loader's index draw (numpy_loader.py:
-  382-389), the host gather (numpy_loader.py:330-340), the GLM potential and
-  gradient, RMSprop and the update.  Used as the timed CPU baseline.  Chains
-  are split over ``threads`` worker threads."""
+  382-389), the host gather (numpy_loader.py:330-340), the per-observation
+  likelihoods, the potential U and var(lk) that update_fn stores every step
+  (integrator.py:875-880), the gradient, RMSprop and the update.  Used as
+  the timed CPU baseline.  Chains are split over ``threads`` worker threads.
+  Returns (W, V, U [C], var [C]) after the last step."""
   import concurrent.futures as cf
   C, d = W.shape
   n_obs = X.shape[0]
@@ -784,6 +786,10 @@ def sgld_glm_cpu_steps(X, y, W, V, rngs, steps, h, T, family, sigma=1.0,
   Xf = np.asarray(X, f32)
   yf = np.asarray(y, f32)
   inv_p2 = f32(0.0) if not prior_scale else f32(1.0 / prior_scale ** 2)
+  lp_const = 0.0 if not prior_scale else \
+      d * (math.log(prior_scale) + 0.5 * math.log(2 * math.pi))
+  U = np.zeros(C)
+  var = np.zeros(C)
 
   def chain_block(cs, k, xi):
     for c in cs:
@@ -791,9 +797,16 @@ def sgld_glm_cpu_steps(X, y, W, V, rngs, steps, h, T, family, sigma=1.0,
       xb, yb = Xf[idx], yf[idx]
       z = xb @ W[c]
       if family == LOGISTIC:
+        lk = yb * z - (np.maximum(z, f32(0.0)) + np.log1p(np.exp(-np.abs(z))))
         dz = yb - f32(1.0) / (f32(1.0) + np.exp(-z))
       else:
-        dz = (yb - z) / f32(sigma ** 2)
+        r = yb - z
+        lk = (f32(-0.5 / sigma ** 2) * (r * r)
+              - f32(math.log(sigma) + 0.5 * math.log(2 * math.pi)))
+        dz = r / f32(sigma ** 2)
+      lp = -0.5 * float(inv_p2) * float(W[c] @ W[c]) - lp_const
+      U[c] = (-(n_obs / steps_n) * float(lk.sum(dtype=np.float64)) - lp) / temperature
+      var[c] = float(np.var(lk, dtype=np.float64))
       g = (-(f32(n_obs / steps_n)) * (dz @ xb) + W[c] * inv_p2) / f32(temperature)
       W[c], V[c] = sgld_step(W[c], g, V[c], xi[c], h[k], T[k], alpha, lmbd, True)
 
@@ -804,4 +817,74 @@ def sgld_glm_cpu_steps(X, y, W, V, rngs, steps, h, T, family, sigma=1.0,
     for k in range(K):
       xi = noise_rng.standard_normal((C, d), dtype=f32)
       list(ex.map(lambda cs: chain_block(cs, k, xi), blocks))
-  return W, V
+  return W, V, U, var
+
+
+def alias_chains_1d(kind, curvature, h, C, rng, x0=0.0, **kw):
+  """C independent chains of one of the reference's alias samplers on the
+  1-D potential U(w) = curvature w^2 / 2 with exact gradients (a batch that
+  every draw makes the same), vectorised over chains with numpy normals.
+  Returns the position after each iteration, [len(h), C] (what
+  solver.mcmc keeps, solver.py:95-121, after update).
+
+  kind:
+    'sgld_rms'  alias.sgld(rms_prop=True): langevin_diffusion with rms_prop
+                (integrator.py:860-922, adaption.py:254-291), one step per
+                iteration;
+    're_sgld'   alias.re_sgld: a normal (T = 1) and a hot (T = kw['T_hot'])
+                plain SGLD chain, then solver.parallel_tempering's exchange
+                (solver.py:264-293) on the potentials at the pre-update
+                positions with var(lk) = 0 (one observation per batch), F = 1;
+                the normal chain is kept;
+    'obabo'     alias.obabo: obabo._leapfrog_steps kw['steps'] times per
+                iteration (integrator.py:192-273), momentum from zero and
+                kept across iterations, friction kw['friction'];
+    'sghmc'     alias.sghmc: momentum resampled, then kw['steps'] friction
+                leapfrog steps (integrator.py:603-666, 735-738), friction
+                kw['friction'].
+  """
+  A = f32(curvature)
+  x = np.full(C, x0, f32)
+  out = np.empty((len(h), C), f32)
+  if kind == "sgld_rms":
+    v = np.ones(C, f32)
+    for k, hk in enumerate(h):
+      x, v = sgld_step(x, A * x, v, rng.normal(size=C), hk, 1.0)
+      out[k] = x
+  elif kind == "re_sgld":
+    xh = x.copy()
+    T_h = float(kw["T_hot"])
+    ssq, it = np.zeros(C), 0
+    for k, hk in enumerate(h):
+      Un = 0.5 * float(A) * x.astype(np.float64) ** 2
+      Uh = 0.5 * float(A) * xh.astype(np.float64) ** 2
+      x, _ = sgld_step(x, A * x, None, rng.normal(size=C), hk, 1.0, rms_prop=False)
+      xh, _ = sgld_step(xh, A * xh, None, rng.normal(size=C), hk, T_h,
+                        rms_prop=False)
+      it += 1
+      ssq = (1 - 1.0 / it) * ssq          # + (1/k) var(lk), var(lk) = 0
+      dbeta = 1.0 - 1.0 / T_h
+      log_s = dbeta * (Un - Uh - dbeta * ssq)
+      swap = ~(np.log(rng.random(C)) < log_s)
+      x, xh = np.where(swap, xh, x), np.where(swap, x, xh)
+      out[k] = x
+  elif kind == "obabo":
+    p = np.zeros((C, 1), f32)
+    xc = x[:, None]
+    for k, hk in enumerate(h):
+      for _ in range(int(kw["steps"])):
+        xc, p, _ = obabo_first(xc, p, A * xc, rng.normal(size=(C, 1)), hk, 1.0,
+                               kw["friction"])
+        p, _ = obabo_second(p, A * xc, rng.normal(size=(C, 1)), hk, 1.0,
+                            kw["friction"])
+      out[k] = xc[:, 0]
+  elif kind == "sghmc":
+    for k, hk in enumerate(h):
+      p = sghmc_resample(rng.normal(size=C))
+      for _ in range(int(kw["steps"])):
+        x, p = sghmc_position(x, p, hk, kw["friction"])
+        p = sghmc_momentum(p, A * x, rng.normal(size=C), hk, kw["friction"])
+      out[k] = x
+  else:
+    raise ValueError(kind)
+  return out

@@ -281,3 +281,49 @@ def test_fisher_oracle_matches_finite_differences(family):
   smallest = corr[corr > 0].min()
   np.testing.assert_allclose(cb ** 2, np.where(corr <= 0, smallest, corr), rtol=1e-12)
   np.testing.assert_allclose(bs ** 2 + cb ** 2, f, rtol=1e-12)
+
+
+@pytest.mark.parametrize("alpha,low,high", [(0.9, 0.07, 0.16), (0.999, -0.02, 0.03)])
+def test_rms_prop_sgld_variance_excess_is_set_by_alpha(alpha, low, high):
+  """The restated SGLD + rms_prop update (integrator.py:882-912 with
+  adaption.py:254-291: v is updated with the current gradient before
+  G = 1 / (lmbd + sqrt v) scales it) on a Gaussian potential whose
+  stochastic gradient is g = A x + eps (A = 4e4, Var eps = 3.125e6: the
+  config-1 linear regression at minibatch 128).  The larger a gradient,
+  the more it raises v and the less of it moves x: the restoring drift is
+  weaker than the noise scale assumes, and the stationary variance exceeds
+  1 / A by about 11 % at alpha 0.9, whatever the step size, but by about
+  1 % at alpha 0.999 -- the setting of the config-1 moment check."""
+  A, S, h, C = 4e4, 3.125e6, 1e-5, 4000
+  rng = np.random.default_rng(3)
+  x = (rng.normal(size=C) / np.sqrt(A)).astype(np.float32)
+  v = np.full(C, S, np.float32)
+  acc = []
+  for k in range(16000):
+    g = (A * x + np.sqrt(S) * rng.normal(size=C)).astype(np.float32)
+    x, v = O.sgld_step(x, g, v, rng.normal(size=C).astype(np.float32), 1e-5, 1.0,
+                       alpha=alpha)
+    if k >= 8000 and k % 50 == 0:
+      acc.append(float(np.var(x.astype(np.float64))))
+  excess = np.mean(acc) * A - 1.0
+  assert low < excess < high, excess
+
+
+def test_cpu_baseline_steps_compute_the_potential_and_variance():
+  """The timed CPU loop computes, like update_fn every step
+  (integrator.py:875-880), U and var(lk) at the pre-update position: they
+  equal the FP64 restatement on the same draws (float32 likelihoods)."""
+  rng = np.random.default_rng(4)
+  N, d, C, n = 500, 6, 3, 16
+  X = rng.normal(size=(N, d)).astype(np.float32)
+  y = (rng.random(N) < 0.5).astype(np.float32)
+  W = (0.1 * rng.normal(size=(C, d))).astype(np.float32)
+  W0 = W.copy()
+  V = np.ones_like(W)
+  _, _, U, var = O.sgld_glm_cpu_steps(X, y, W, V, [O.loader_rng(c) for c in range(C)],
+                                      (1, n), np.full(1, 1e-4), np.ones(1), O.LOGISTIC,
+                                      prior_scale=1.0)
+  idx = np.stack([O.loader_draws(O.loader_rng(c), N, n, 1)[0] for c in range(C)])
+  ref = O.glm_potential(W0, X, y, idx, N, O.LOGISTIC, 1.0, 1.0)
+  np.testing.assert_allclose(U, ref.U, rtol=1e-5)
+  np.testing.assert_allclose(var, ref.var, rtol=1e-4)
