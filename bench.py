@@ -213,6 +213,75 @@ def profiled_traffic():
 
 
 # ---------------------------------------------------------------------------
+# Posterior-moment error: Bayesian linear regression with a closed-form
+# posterior (N = 10,000, d = 32, sigma 0.5, prior N(0, 10^2 I), minibatch
+# 128, SGLD with RMSprop through alias.sgld).
+# ---------------------------------------------------------------------------
+CFG1_N, CFG1_D, CFG1_MB = 10_000, 32, 128
+# Three alias.sgld calls, each starting from the previous call's last
+# sample: (first step size, last step size, iterations, burn-in, kept).  The
+# first call travels from w = 0 to the posterior (RMSprop moves each weight
+# about one step size per step far from it), the second brings the chains'
+# spread close to the posterior's, the third samples.  RMSprop alpha 0.999:
+# the rms_prop adaption updates v with the current gradient before scaling
+# that gradient by 1 / sqrt(v) (adaption.py:254-291), which widens the
+# stationary distribution by about (1 - alpha) relative in variance, 11 %
+# at the default alpha 0.9.
+CFG1_PHASES = ((2e-3, 1e-3, 10_000, 9_999, 1),
+               (1e-4, 5e-5, 10_000, 9_999, 1),
+               (5e-6, 4e-6, 60_000, 36_000, 50))
+CFG1_ALPHA = 0.999
+
+
+def config1_data():
+  rng = np.random.default_rng(20261203 + 1)
+  X = rng.standard_normal((CFG1_N, CFG1_D), dtype=np.float32)
+  w_star = rng.normal(size=CFG1_D)
+  y = (X @ w_star + 0.5 * rng.normal(size=CFG1_N)).astype(np.float32)
+  return X, y
+
+
+def linear_posterior(X, y, sigma=0.5, prior_scale=10.0):
+  """Closed-form Gaussian posterior (FP64): mean and covariance."""
+  Xd = X.astype(np.float64)
+  prec = Xd.T @ Xd / sigma ** 2 + np.eye(X.shape[1]) / prior_scale ** 2
+  cov = np.linalg.inv(prec)
+  return cov @ (Xd.T @ y.astype(np.float64)) / sigma ** 2, cov
+
+
+def config1_moment_error(chains=16384):
+  """Runs the config-1 chains through alias.sgld (CFG1_PHASES) and returns
+  the relative errors of the kept samples' mean and per-weight variance
+  against the closed-form posterior, with the chain-steps and seconds of
+  the three calls."""
+  import torch
+  from gbsgmc import alias, data, likelihoods as L, potential
+  X, y = config1_data()
+  mu, cov = linear_posterior(X, y)
+  loader = data.NumpyDataLoader(x=X, y=y)
+  pot = potential.minibatch_potential(L.GaussianPrior(10.0),
+                                      L.LinearGaussian(sigma=0.5), strategy="vmap")
+  starts = [{"w": np.zeros(CFG1_D, np.float32)} for _ in range(chains)]
+  steps = 0
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
+  for first, last, its, burn, kept in CFG1_PHASES:
+    run = alias.sgld(pot, loader, cache_size=512, batch_size=CFG1_MB,
+                     first_step_size=first, last_step_size=last, burn_in=burn,
+                     accepted_samples=kept, rms_prop=True, alpha=CFG1_ALPHA)
+    res = run(*starts, iterations=its)
+    steps += chains * its
+    W = np.stack([r["samples"]["variables"]["w"] for r in res], 1)  # [S, C, d]
+    starts = [{"w": W[-1, c]} for c in range(chains)]
+  seconds = time.perf_counter() - t0
+  flat = W.reshape(-1, CFG1_D).astype(np.float64)
+  var = np.diag(cov)
+  return {"mean": float(np.linalg.norm(flat.mean(0) - mu) / np.linalg.norm(mu)),
+          "var": float(np.linalg.norm(flat.var(0) - var) / np.linalg.norm(var)),
+          "chains": chains, "chain_steps": steps, "seconds": seconds}
+
+
+# ---------------------------------------------------------------------------
 # CPU arms (oracle)
 # ---------------------------------------------------------------------------
 
@@ -467,6 +536,22 @@ def run_gbsgmc(args):
   d2h = CHAINS * kept * (D * 4 + 8)
   e2e_value = world * CHAINS * args.steps / e2e_s
 
+  # Posterior-moment error of the same fused SGLD path on the workload
+  # with a closed-form posterior (rank 0 only).
+  moment = None
+  if rank == 0:
+    m = config1_moment_error()
+    moment = {"mean": m["mean"], "var": m["var"], "bar": 0.02,
+              "workload": ("Bayesian linear regression N=10,000, d=32, sigma 0.5, "
+                           "prior N(0,10^2 I), minibatch 128, SGLD+RMSprop "
+                           f"(alpha {CFG1_ALPHA}) via alias.sgld, "
+                           f"{m['chains']} chains; steps/burn-in/kept per call "
+                           + ", ".join(f"{i}/{b}/{k} at h {f:g}->{l:g}"
+                                       for f, l, i, b, k in CFG1_PHASES)),
+              "against": "closed-form Gaussian posterior (FP64): relative L2 "
+                         "error of the mean and of the per-weight variances",
+              "chain_steps_per_s": m["chain_steps"] / m["seconds"]}
+
   # CPU oracle on a bounded sample (rank 0 only).
   cpu = None
   if rank == 0:
@@ -519,6 +604,7 @@ def run_gbsgmc(args):
         "plain_gpu": {"value": plain_value, "unit": "chain-steps/s",
                       "form": "one chain, 8 unfused launches per step",
                       "fused_over_plain": value / world / plain_value},
+        "moment_error": moment,
         "clocks": clk, "finite": finite,
         "device_status": int(f.status.item()),
     }

@@ -1,8 +1,8 @@
 """End-to-end runs through the reference-shaped API (gbsgmc.alias).
 
 * Config-1 problem (Bayesian linear regression, N=10,000, d=32, n=128):
-  alias.sgld with RMSprop reaches the closed-form posterior mean within 2 %
-  relative error (alias defaults h: 0.05 -> 0.001).
+  alias.sgld with RMSprop reaches the closed-form posterior mean and the
+  per-weight variances within 2 % relative error (bench.CFG1_PHASES).
 * The fused many-chain plan and the per-step path give the same samples
   (1e-4 relative), and the plan reproduces the oracle trajectory driven by
   the same index stream and Philox normals.
@@ -39,16 +39,20 @@ def sgld_run(X, y, iterations, chains=1, burn_in=0, accepted=100, first=0.05,
              iterations=iterations)
 
 
-def test_sgld_reaches_closed_form_posterior_mean(lib):
-  X, y = linreg()
-  mu, cov = O.linear_posterior(X, y, 0.5, 10.0)
-  res = sgld_run(X, y, 10_000, burn_in=5000, accepted=1000)
-  assert len(res) == 1 and res[0]["sample_count"] == 1000
-  w = res[0]["samples"]["variables"]["w"]
-  assert w.shape == (1000, 32)
-  err = np.linalg.norm(w.mean(0) - mu) / np.linalg.norm(mu)
-  assert err < 0.02, err
-  assert res[0]["samples"]["likelihood"].shape == (1000,)
+def test_config1_posterior_moments_within_2_percent(lib):
+  """Bayesian linear regression with a closed-form posterior (N = 10,000,
+  d = 32, sigma 0.5, prior N(0, 10^2 I), minibatch 128): alias.sgld with
+  RMSprop (alpha 0.999), 16,384 chains run as the bench's three calls (travel
+  from w = 0, shrink the spread, sample), reaches the posterior mean AND the
+  per-weight posterior variances within 2 % relative L2 error.  At the
+  default alpha 0.9 the reference's rms_prop (v updated with the current
+  gradient before scaling it) widens the variance by about 11 %, whatever
+  the step size; that is checked on the restated algorithm in
+  tests/test_oracle.py."""
+  import bench
+  m = bench.config1_moment_error(chains=16384)
+  assert m["mean"] < 0.02, m
+  assert m["var"] < 0.02, m
 
 
 def test_fused_plan_equals_per_step_path(lib):
