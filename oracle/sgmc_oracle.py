@@ -749,15 +749,17 @@ def polynomial_first_last(first, last, gamma, iterations):
 
 def sgld_glm_trajectory(X, y, w0, idx, xi, h, T, family, sigma=1.0,
                         prior_scale=0.0, temperature=1.0, rms_prop=True,
-                        alpha=0.9, lmbd=1e-5):
+                        alpha=0.9, lmbd=1e-5, n_obs=None):
   """K SGLD steps of C chains with given minibatch indices idx [K, C, n] and
   injected normals xi [K, C, d]; gradients in float64, updates in float32.
+  ``n_obs`` (default: the rows of X) is the N of the N/n scaling, so that X
+  may hold only the rows the indices reach.
   Returns (W [K+1, C, d], U [K, C], var [K, C])."""
   W = np.atleast_2d(np.asarray(w0, f32)).copy()
   V = np.ones_like(W)
   K = idx.shape[0]
   Ws, Us, Vs = [W.copy()], [], []
-  n_obs = X.shape[0]
+  n_obs = X.shape[0] if n_obs is None else n_obs
   for k in range(K):
     pot = glm_potential(W, X, y, idx[k], n_obs, family, sigma, prior_scale,
                         temperature)
