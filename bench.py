@@ -552,6 +552,9 @@ def run_gbsgmc(args):
                          "error of the mean and of the per-weight variances",
               "chain_steps_per_s": m["chain_steps"] / m["seconds"]}
 
+  # The tensor-core workload in brief: OBABO on the tanh network (rank 0).
+  mlp = mlp_record() if rank == 0 else None
+
   # CPU oracle on a bounded sample (rank 0 only).
   cpu = None
   if rank == 0:
@@ -605,6 +608,7 @@ def run_gbsgmc(args):
                       "form": "one chain, 8 unfused launches per step",
                       "fused_over_plain": value / world / plain_value},
         "moment_error": moment,
+        "mlp_obabo": mlp,
         "clocks": clk, "finite": finite,
         "device_status": int(f.status.item()),
     }
@@ -633,11 +637,25 @@ def mlp_data():
   X = rng.standard_normal((MLP_N, MLP_D), dtype=np.float32)
   teacher = lik.unravel(lik.init(rng).astype(np.float64))
   y = np.empty(MLP_N, np.float32)
+  try:
+    import torch
+    gpu = torch.cuda.is_available()
+  except ImportError:
+    gpu = False
+  if gpu:
+    # The teacher's forward pass in FP64 on the GPU (about 1e12 flop).
+    tw = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in teacher.items()}
   for a in range(0, MLP_N, 50_000):
-    xb = X[a:a + 50_000].astype(np.float64)
-    z1 = np.tanh(xb @ teacher["W1"] + teacher["b1"])
-    z2 = np.tanh(z1 @ teacher["W2"] + teacher["b2"])
-    f = (z2 @ teacher["W3"])[:, 0] + teacher["b3"][0]
+    if gpu:
+      xb = torch.from_numpy(X[a:a + 50_000]).cuda().double()
+      z1 = torch.tanh(xb @ tw["W1"] + tw["b1"])
+      z2 = torch.tanh(z1 @ tw["W2"] + tw["b2"])
+      f = ((z2 @ tw["W3"])[:, 0] + tw["b3"][0]).cpu().numpy()
+    else:
+      xb = X[a:a + 50_000].astype(np.float64)
+      z1 = np.tanh(xb @ teacher["W1"] + teacher["b1"])
+      z2 = np.tanh(z1 @ teacher["W2"] + teacher["b2"])
+      f = (z2 @ teacher["W3"])[:, 0] + teacher["b3"][0]
     y[a:a + 50_000] = f + 0.1 * rng.standard_normal(min(50_000, MLP_N - a))
   inits = np.stack([lik.init(np.random.default_rng(1000 + c))
                     for c in range(MLP_CHAINS)])
@@ -1026,6 +1044,67 @@ def mlp_kernel_only(args):
   torch.cuda.synchronize()
   plan.check_status()
   plan.close()
+
+
+def mlp_record(steps=20, warmup=3):
+  """A compact record of the tanh-network workload for the default line:
+  `steps` OBABO steps of its 64 chains (minibatch 2048, graph-captured
+  network plan; two value-and-gradient calls per step) timed with CUDA
+  events after `warmup` steps, and the batched value and gradient alone
+  against the sustained BF16 peak."""
+  import torch
+  from gbsgmc import data, engine, likelihoods as L, potential
+  lik, X, y, inits = mlp_data()
+  ds = data.NumpyDataLoader(copy=False, x=X, y=y).device_dataset()
+  pot = potential.minibatch_potential(L.GaussianPrior(1.0), lik)
+  total = warmup + steps
+  h = torch.full((total,), 1e-7, dtype=torch.float32, device="cuda")
+  t = torch.ones(total, dtype=torch.float32, device="cuda")
+  Xd = torch.from_numpy(inits).cuda()
+  from gbsgmc.data.numpy_loader import pcg64_words_many
+  pcg = torch.from_numpy(pcg64_words_many(range(MLP_CHAINS)).view(np.int64)).cuda()
+  plan = engine.NetPlan(pot, ds, Xd, torch.zeros_like(Xd), MLP_MB, "obabo", h, t,
+                        engine.IndexSource(pcg=pcg), noise_seed=7, friction=1.0)
+  plan.run(0, warmup)
+  torch.cuda.synchronize()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record()
+  plan.run(warmup, steps)
+  e1.record()
+  torch.cuda.synchronize()
+  ms = e0.elapsed_time(e1) / steps
+  plan.check_status()
+  launches = plan.launches(steps)
+  plan.close()
+  idx = torch.randint(0, MLP_N, (MLP_CHAINS, MLP_MB), dtype=torch.int32, device="cuda")
+  for _ in range(3):
+    pot.evaluate(Xd, idx, ds, grad=True)
+  torch.cuda.synchronize()
+  g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  g0.record()
+  for _ in range(10):
+    pot.evaluate(Xd, idx, ds, grad=True)
+  g1.record()
+  torch.cuda.synchronize()
+  pot.check_status()
+  grad_ms = g0.elapsed_time(g1) / 10
+  peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+      if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+  peak = peaks.get("bf16_tflops_sustained", 1700.0)
+  kind = "measured bf16_tflops_sustained" if "bf16_tflops_sustained" in peaks else \
+      "fallback"
+  achieved = MLP_CHAINS * MLP_FLOP_PER_GRAD / (grad_ms / 1e3) / 1e12
+  return {"workload": MLP_WORKLOAD, "value": MLP_CHAINS / (ms / 1e3),
+          "unit": "chain-steps/s", "ms_per_step": ms, "steps": steps,
+          "gpu_launches": launches, "dtype": "bf16 GEMMs, fp32 accumulation",
+          "finite": bool(torch.isfinite(Xd).all().item()),
+          "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                       "unit": "TFLOP/s", "frac": achieved / peak,
+                       "peak_kind": kind,
+                       "kernel": "batched value and gradient (5 tcgen05 GEMMs + "
+                                 "epilogue kernels)",
+                       "kernel_ms": grad_ms,
+                       "algorithmic_flop_per_launch": MLP_CHAINS * MLP_FLOP_PER_GRAD}}
 
 
 def run_mlp(args):
