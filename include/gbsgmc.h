@@ -421,6 +421,21 @@ int gbsgmc_gemm_bf16(int a_mn, int b_mn, const void* A_dev, int64_t lda,
                      int64_t c_batch_stride, int batch, int M, int N, int K,
                      int* status_dev, gbsgmc_stream_t stream);
 
+/* As gbsgmc_gemm_bf16 with the bound of each wait for pipeline progress (the
+ * TMA operands of a stage, a free stage, a finished or drained TMEM
+ * accumulator) given in nanoseconds instead of the default 1 s.  A CTA whose
+ * wait runs out writes GBSGMC_ERR_TIMEOUT to *status_dev, stops issuing
+ * copies and MMAs, waits (up to 1 s) for those it issued, frees its TMEM and
+ * returns; C is then incomplete, and the device stays usable.  No reference
+ * counterpart: the bounded waits are this library's failure detection. */
+int gbsgmc_gemm_bf16_wait_limit(int a_mn, int b_mn, const void* A_dev,
+                                int64_t lda, int64_t a_batch_stride,
+                                const void* B_dev, int64_t ldb,
+                                int64_t b_batch_stride, float* C_dev,
+                                int64_t ldc, int64_t c_batch_stride, int batch,
+                                int M, int N, int K, uint64_t wait_limit_ns,
+                                int* status_dev, gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Dense tanh network (MLP) with a Gaussian likelihood                       */
 /* ------------------------------------------------------------------------ */

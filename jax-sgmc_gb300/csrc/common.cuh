@@ -259,18 +259,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase with the given parity.  Returns false after
-// kWaitLimitNs or when *abort becomes non-zero.
+// limit_ns (kWaitLimitNs unless given) or when *abort becomes non-zero.
+// try_wait may itself suspend the thread for a while, so the clock and the
+// abort flag are checked after every unsuccessful try.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar,
                                                   uint32_t parity,
-                                                  volatile int* abort) {
+                                                  volatile int* abort,
+                                                  uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
-  for (uint32_t it = 1;; ++it) {
+  for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 63u) == 0u) {
-      if (abort != nullptr && *abort) return false;
-      if (global_ns() - t0 > kWaitLimitNs) return false;
-    }
+    if (abort != nullptr && *abort) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 

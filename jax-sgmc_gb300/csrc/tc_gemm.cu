@@ -112,12 +112,12 @@ namespace {
 template <int BN>
 int dispatch_layout(bool a_mn, bool b_mn, const CUtensorMap& ta, const CUtensorMap& tb,
                     int batch, int M, int N, int K, int* status, const StoreF32& epi,
-                    cudaStream_t st) {
+                    cudaStream_t st, const GemmRagged& rg) {
   if (a_mn)
-    return b_mn ? launch_gemm<BN, true, true>(ta, tb, batch, M, N, K, status, epi, st)
-                : launch_gemm<BN, true, false>(ta, tb, batch, M, N, K, status, epi, st);
-  return b_mn ? launch_gemm<BN, false, true>(ta, tb, batch, M, N, K, status, epi, st)
-              : launch_gemm<BN, false, false>(ta, tb, batch, M, N, K, status, epi, st);
+    return b_mn ? launch_gemm<BN, true, true>(ta, tb, batch, M, N, K, status, epi, st, rg)
+                : launch_gemm<BN, true, false>(ta, tb, batch, M, N, K, status, epi, st, rg);
+  return b_mn ? launch_gemm<BN, false, true>(ta, tb, batch, M, N, K, status, epi, st, rg)
+              : launch_gemm<BN, false, false>(ta, tb, batch, M, N, K, status, epi, st, rg);
 }
 
 }  // namespace
@@ -127,6 +127,16 @@ extern "C" int gbsgmc_gemm_bf16(int a_mn, int b_mn, const void* A_dev, int64_t l
                                 int64_t b_batch_stride, float* C_dev, int64_t ldc,
                                 int64_t c_batch_stride, int batch, int M, int N, int K,
                                 int* status_dev, gbsgmc_stream_t stream) {
+  return gbsgmc_gemm_bf16_wait_limit(a_mn, b_mn, A_dev, lda, a_batch_stride, B_dev, ldb,
+                                     b_batch_stride, C_dev, ldc, c_batch_stride, batch, M,
+                                     N, K, kWaitLimitNs, status_dev, stream);
+}
+
+extern "C" int gbsgmc_gemm_bf16_wait_limit(
+    int a_mn, int b_mn, const void* A_dev, int64_t lda, int64_t a_batch_stride,
+    const void* B_dev, int64_t ldb, int64_t b_batch_stride, float* C_dev, int64_t ldc,
+    int64_t c_batch_stride, int batch, int M, int N, int K, uint64_t wait_limit_ns,
+    int* status_dev, gbsgmc_stream_t stream) {
   if (A_dev == nullptr || B_dev == nullptr || C_dev == nullptr || status_dev == nullptr)
     return set_error(GBSGMC_ERR_ARG, "gemm_bf16: null pointer");
   if (batch <= 0 || M <= 0 || N <= 0 || K <= 0 || batch > (1 << 20))
@@ -149,8 +159,11 @@ extern "C" int gbsgmc_gemm_bf16(int a_mn, int b_mn, const void* A_dev, int64_t l
   if (rc != GBSGMC_OK) return rc;
   const StoreF32 epi{C_dev, ldc, c_batch_stride};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  return bn == 256 ? dispatch_layout<256>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st)
-                   : dispatch_layout<128>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st);
+  GemmRagged rg;
+  rg.wait_ns = wait_limit_ns;
+  return bn == 256
+             ? dispatch_layout<256>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st, rg)
+             : dispatch_layout<128>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st, rg);
 }
 
 extern "C" int gbsgmc_gemm_bf16_nt(const void* A_dev, int64_t lda,

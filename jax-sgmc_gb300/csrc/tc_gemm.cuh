@@ -76,6 +76,10 @@ struct GemmRagged {
   // partial products over consecutive K ranges by different CTAs; the
   // epilogue sees batch index b * ksplit + s for split s.
   int ksplit = 1;
+  // Bound of each wait for pipeline progress (a stage's operands, a free
+  // stage or accumulator, a finished accumulator).  The waits of the clean-up
+  // after a timeout (copies and MMAs already issued) keep kWaitLimitNs.
+  uint64_t wait_ns = kWaitLimitNs;
 };
 
 __device__ __forceinline__ int ragged_batch(const GemmRagged& rg, int t, int per_batch,
@@ -112,9 +116,10 @@ __device__ __forceinline__ int ragged_batch(const GemmRagged& rg, int t, int per
 // [32c, 32c + 32) of the lane's row (warp-collective), and stage a private
 // 32 x 33-word shared-memory tile for the epi:: helpers.
 //
-// Every wait is bounded (kWaitLimitNs): on a timeout the CTA records
-// GBSGMC_ERR_TIMEOUT, stops issuing work, waits for what it issued, frees
-// its TMEM and returns.
+// Every wait is bounded (rg.wait_ns, kWaitLimitNs by default): on a timeout
+// the CTA records GBSGMC_ERR_TIMEOUT, stops issuing work, waits (bounded by
+// kWaitLimitNs) for the copies and MMAs it issued, frees its TMEM and
+// returns.
 template <int BN, bool A_MN, bool B_MN, class Epi>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta,
@@ -187,7 +192,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         for (int kb = 0; kb < KB; ++kb, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1u;
-          if (!mbar_wait_bounded(&empty[s], ph ^ 1u, abort_flag)) {
+          if (!mbar_wait_bounded(&empty[s], ph ^ 1u, abort_flag, rg.wait_ns)) {
             raise_status(status, GBSGMC_ERR_TIMEOUT);
             *abort_flag = 1;
             ok = false;
@@ -228,7 +233,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         int b, r, KB, kb0;
         decode(t, b, r, KB, kb0);
         const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
-        if (!mbar_wait_bounded(&tempty[buf], aph ^ 1u, abort_flag)) {
+        if (!mbar_wait_bounded(&tempty[buf], aph ^ 1u, abort_flag, rg.wait_ns)) {
           raise_status(status, GBSGMC_ERR_TIMEOUT);
           *abort_flag = 1;
           break;
@@ -238,7 +243,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         for (int kb = 0; kb < KB; ++kb, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1u;
-          if (!mbar_wait_bounded(&full[s], ph, abort_flag)) {
+          if (!mbar_wait_bounded(&full[s], ph, abort_flag, rg.wait_ns)) {
             raise_status(status, GBSGMC_ERR_TIMEOUT);
             *abort_flag = 1;
             ok = false;
@@ -273,7 +278,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     uint32_t acc = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++acc) {
       const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
-      const bool ok = mbar_wait_bounded(&tfull[buf], aph, abort_flag);
+      const bool ok = mbar_wait_bounded(&tfull[buf], aph, abort_flag, rg.wait_ns);
       if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0 && !*abort_flag) {
           raise_status(status, GBSGMC_ERR_TIMEOUT);

@@ -210,6 +210,9 @@ SIGNATURES = {
     "gbsgmc_plan_destroy": (_i, [_vp]),
     "gbsgmc_gemm_bf16": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64, _vp,
                               _i64, _i64, _i, _i, _i, _i, _vp, _vp]),
+    "gbsgmc_gemm_bf16_wait_limit": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64,
+                                         _vp, _i64, _i64, _i, _i, _i, _i,
+                                         C.c_uint64, _vp, _vp]),
     "gbsgmc_gemm_bf16_nt": (_i, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64,
                                  _i64, _i, _i, _i, _i, _vp, _vp]),
     "gbsgmc_plain_buffer_bytes": (_sz, [_i, _i]),

@@ -68,3 +68,37 @@ def test_gemm_rejects_unsupported_shapes(lib):
   rc = lib.gbsgmc_gemm_bf16(1, 0, 16, 64, 0, 16, 64, 0, 16, 128, 0, 1, 128, 128,
                             64, None, None)
   assert rc == _lib.ERR_ARG
+
+
+def test_gemm_progress_wait_bound_runs_out_cleanly(lib):
+  """The bounded waits are the GEMM's failure detection.  With a 1 us bound
+  on the waits for pipeline progress, the epilogue warps (whose first
+  accumulator needs 32 K slices of MMAs, several microseconds) give up:
+  each CTA records GBSGMC_ERR_TIMEOUT, stops issuing copies and MMAs, waits
+  for those in flight, frees its TMEM and returns.  The device stays usable:
+  the same GEMM with the default bound then completes and is correct, twice
+  in a row."""
+  import torch
+  from gbsgmc import _lib
+  batch, M, N, K = 2, 1024, 1024, 2048
+  g = torch.Generator(device="cuda").manual_seed(99)
+  A = torch.randn((batch, M, K), generator=g, device="cuda").to(torch.bfloat16)
+  B = torch.randn((batch, N, K), generator=g, device="cuda").to(torch.bfloat16)
+  ref = torch.bmm(A.float(), B.float().transpose(1, 2))
+  bound = torch.bmm(A.float().abs(), B.float().abs().transpose(1, 2))
+  for _ in range(2):
+    C = torch.zeros((batch, M, N), device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("gbsgmc_gemm_bf16_wait_limit", 0, 0, A.data_ptr(), K, M * K,
+              B.data_ptr(), K, N * K, C.data_ptr(), N, M * N, batch, M, N, K,
+              1000, status.data_ptr(), _lib.stream_handle())
+    torch.cuda.synchronize()
+    assert int(status.item()) == _lib.ERR_TIMEOUT
+    status.zero_()
+    C.fill_(float("nan"))
+    _lib.call("gbsgmc_gemm_bf16", 0, 0, A.data_ptr(), K, M * K, B.data_ptr(), K,
+              N * K, C.data_ptr(), N, M * N, batch, M, N, K, status.data_ptr(),
+              _lib.stream_handle())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert bool(((C - ref).abs() <= 1e-3 * bound + 1e-4).all())
