@@ -243,15 +243,29 @@ __device__ __forceinline__ void load_tile(const GlmArgs& a, const int32_t* idx_s
 // the warp and block reductions.  GB300's fp64 pipe runs at a small fraction
 // of the fp32 rate, so per-row fp64 arithmetic would throttle the kernel.
 //
+// The sum of the (masked) likelihoods that makes U is compensated: each
+// addition's rounding error is carried in mlk_c (Neumaier's variant of
+// Kahan summation, A. Neumaier 1974), so a lane's sum is good to about one
+// rounding of its total whatever its row count.  Once the sum overflows the
+// correction is dropped, so an infinite likelihood sum stays infinite (the
+// MH tests reject such a proposal) instead of turning into inf - inf.
+//
 // The variance needs E[lk^2] - E[lk]^2, which cancels badly when |lk| is
 // large, so each lane sums around its first value K: s1 = sum(lk - K),
 // s2 = sum((lk - K)^2); the widening to fp64 restores sum(lk) and sum(lk^2).
 template <int QPL>
 struct Accum {
   float4 acc[QPL];
-  float mlk, K, s1, s2;
+  float mlk, mlk_c, K, s1, s2;
   int cnt;
 };
+
+__device__ __forceinline__ void neumaier_add(float& sum, float& comp, float x) {
+  const float t = sum + x;
+  const float e = fabsf(sum) >= fabsf(x) ? (sum - t) + x : (x - t) + sum;
+  comp += isfinite(t) ? e : 0.0f;
+  sum = t;
+}
 
 // Likelihood, adjoint and accumulation for a loaded tile (see load_tile).
 template <int QPL, int RW>
@@ -292,7 +306,7 @@ __device__ __forceinline__ void consume_tile(const GlmArgs& a, const float* m_s,
   }
   const float coef = ok ? mw * dz : 0.0f;
   if (ok && leader) {
-    A.mlk = fmaf(mw, lkv, A.mlk);
+    neumaier_add(A.mlk, A.mlk_c, mw * lkv);
     if (A.cnt == 0) A.K = lkv;
     const float dk = lkv - A.K;
     A.s1 += dk;
@@ -389,7 +403,7 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
     }
     A.acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  A.mlk = A.K = A.s1 = A.s2 = 0.0f;
+  A.mlk = A.mlk_c = A.K = A.s1 = A.s2 = 0.0f;
   A.cnt = 0;
   // What the epilogue needs, loaded now so that the latency overlaps the row
   // stream instead of stalling the step after it: the schedule at this step
@@ -458,7 +472,7 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
   }
   // Widen once: sum(lk) = s1 + n K, sum(lk^2) = s2 + 2 K s1 + n K^2.
   const double K = A.K, n_l = A.cnt;
-  double my_mlk = A.mlk;
+  double my_mlk = static_cast<double>(A.mlk) + A.mlk_c;
   double my_lk = static_cast<double>(A.s1) + n_l * K;
   double my_lk2 = static_cast<double>(A.s2) + 2.0 * K * A.s1 + n_l * K * K;
   my_mlk = warp_sum(my_mlk);
@@ -846,7 +860,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       wq[k].w = j + 3 < a.d ? w_in[j + 3] : 0.0f;
       A.acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    A.mlk = A.K = A.s1 = A.s2 = 0.0f;
+    A.mlk = A.mlk_c = A.K = A.s1 = A.s2 = 0.0f;
     A.cnt = 0;
     __syncwarp();
     float* lk_out = a.lk != nullptr ? a.lk + static_cast<int64_t>(c) * a.n + row0
@@ -859,7 +873,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       consume_tile<QPL, RW>(a, m_s, lk_out, r0, lane, g, leader, wq, xv, yv, og, A);
     }
     const double K = A.K, n_l = A.cnt;
-    const double my_mlk = warp_sum(static_cast<double>(A.mlk));
+    const double my_mlk = warp_sum(static_cast<double>(A.mlk) + A.mlk_c);
     const double my_lk = warp_sum(static_cast<double>(A.s1) + n_l * K);
     const double my_lk2 =
         warp_sum(static_cast<double>(A.s2) + 2.0 * K * A.s1 + n_l * K * K);
