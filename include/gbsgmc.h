@@ -738,6 +738,41 @@ int gbsgmc_mlp_resgld_plan_create(gbsgmc_plan** plan, const gbsgmc_mlp* model,
                                   double* U_dev, double* lk_var_dev,
                                   int block_steps, int* status_dev);
 
+/* reSGLD on a generalised-linear potential as alias.re_sgld runs it: `pairs`
+ * pairs of a normal and a hot chain, plain SGLD (rms_prop when v_dev is not
+ * NULL), and after every step each pair's exchange in FP64 with the rule of
+ * solver.parallel_tempering.update (jax_sgmc/solver.py:264-293, the SA
+ * schedule 1/k):  k_p += 1;  ssq_p <- (1 - 1/k_p) ssq_p + (1/k_p) var_normal;
+ * log s = dbeta (U_normal - U_hot - dbeta ssq_p / F); the pair exchanges its
+ * states unless log u < log s.  Chains are slots of [2 pairs, d] arrays
+ * (x_dev, v_dev, U_dev, lk_var_dev): normal chain p in slot p, its hot
+ * partner in slot pairs + p, each at the temperature T_k *
+ * sched->chain_temperature_dev[slot].  An exchange swaps the two slots' x, v,
+ * U, var(lk) and chain identities ident_dev[slot]: identity i (0 <= i <
+ * 2 pairs) is the chain with index stream index_src->pcg_dev[i] and noise
+ * chain id noise->chain_base + i, so streams travel with the states as the
+ * reference's whole-state exchange moves them.  Pair p's uniform is
+ * Philox(counter (0, k + 1, 0, GBSGMC_TAG_SWAP), key (tempering->seed << 32)
+ * | pair_chain_dev[p]).  At kept steps the normal slots' x and -U go to
+ * samples_dev [slot, pairs, d] and sample_lik_dev [slot, pairs]; swap counts
+ * are added to tempering->counts_dev [pairs] when it is not NULL
+ * (tempering->every and flags_dev are not used).  Per step: one fused SGLD
+ * launch for all 2 pairs chains and one exchange launch; per block one
+ * index-draw launch, replayed from a CUDA graph.
+ * Replaces alias.re_sgld (jax_sgmc/alias.py:122-208) through solver.mcmc. */
+int gbsgmc_glm_resgld_plan_create(gbsgmc_plan** plan, const gbsgmc_glm* model,
+                                  int pairs, int n, float* x_dev, float* v_dev,
+                                  float alpha, float lmbd,
+                                  const gbsgmc_sched* sched,
+                                  const gbsgmc_noise* noise,
+                                  const gbsgmc_index_src* index_src,
+                                  const gbsgmc_tempering* tempering,
+                                  const int32_t* pair_chain_dev,
+                                  int32_t* ident_dev, double* U_dev,
+                                  double* lk_var_dev, float* samples_dev,
+                                  double* sample_lik_dev, int block_steps,
+                                  int* status_dev);
+
 /* Runs steps [first_step, first_step + steps) of the plan, ordered after prior
  * work on `stream`; later work on `stream` waits for it.  Does not block the
  * host. */

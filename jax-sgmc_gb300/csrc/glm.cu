@@ -89,7 +89,15 @@ struct GlmArgs {
   int dyn_fixed;      // 1: dynamically scheduled kernel, -1: not, 0: library choice
   int* status;
   int vec4;   // rows are 16-byte aligned: 128-bit loads
+  // Replica exchange: chain c's index row and noise stream belong to chain
+  // ident[c] (the states that moved into c with an exchange); NULL: c itself.
+  const int32_t* ident;
 };
+
+// The chain whose index row and noise stream chain (slot) c uses.
+__device__ __forceinline__ int ident_of(const GlmArgs& a, int c) {
+  return a.ident != nullptr ? __ldg(a.ident + c) : c;
+}
 
 struct SmemLayout {
   size_t flags, idx, idx2, m, red, sums, wbuf, total;
@@ -367,7 +375,7 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
     }
   } else {
     for (int r = tid; r < R; r += (WARPS * 32)) {
-      int32_t o = __ldg(idx_j + c * a.idx_stride + row0 + r);
+      int32_t o = __ldg(idx_j + ident_of(a, c) * a.idx_stride + row0 + r);
       if (o < 0 || o >= a.n_rows) {
         raise_status(a.status, GBSGMC_ERR_INDEX);
         o = -1;
@@ -379,7 +387,7 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
   }
   __syncthreads();
   if (multi && j + 1 < a.steps) {
-    const int32_t* src = idx_j + a.idx_step_stride + c * a.idx_stride + row0;
+    const int32_t* src = idx_j + a.idx_step_stride + ident_of(a, c) * a.idx_stride + row0;
     for (int r = tid; r < R; r += (WARPS * 32)) cp_async4(idx_next + r, src + r);
     asm volatile("cp.async.commit_group;" ::: "memory");
   }
@@ -611,7 +619,7 @@ __device__ __forceinline__ void glm_step(const GlmArgs& a, int j, unsigned char*
     const float xs[4] = {xq.x, xq.y, xq.z, xq.w};
     const float vs[4] = {vq.x, vq.y, vq.z, vq.w};
     float xi[4];
-    noise4(a.noise, c, 4 * q, a.d, k_step, GBSGMC_TAG_SGLD, xi);
+    noise4(a.noise, ident_of(a, c), 4 * q, a.d, k_step, GBSGMC_TAG_SGLD, xi);
     float xn[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -770,7 +778,7 @@ __device__ __forceinline__ void dyn_epilogue(const GlmArgs& a, int c, int lane,
     const int q = lane + 32 * k;
     if (q >= dq) continue;
     float xi[4];
-    noise4(a.noise, c, 4 * q, a.d, k_step, GBSGMC_TAG_SGLD, xi);
+    noise4(a.noise, ident_of(a, c), 4 * q, a.d, k_step, GBSGMC_TAG_SGLD, xi);
     const float wv[4] = {wq[k].x, wq[k].y, wq[k].z, wq[k].w};
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -839,7 +847,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     const int R = max(0, min(IR, a.n - row0));
     __syncwarp();  // the previous item's reads of idx_s / m_s are done
     for (int r = lane; r < R; r += 32) {
-      int32_t o = __ldg(a.idx + c * a.idx_stride + row0 + r);
+      int32_t o = __ldg(a.idx + ident_of(a, c) * a.idx_stride + row0 + r);
       if (o < 0 || o >= a.n_rows) {
         raise_status(a.status, GBSGMC_ERR_INDEX);
         o = -1;
@@ -1279,6 +1287,7 @@ int fill_common(GlmArgs& a, const gbsgmc_glm* m, int chains, int n,
   a.lmbd = 1e-5f;
   a.sched = Sched{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0.0f, 1.0f};
   a.noise = Noise{nullptr, 0, 0, 0};
+  a.ident = nullptr;
   return GBSGMC_OK;
 }
 
@@ -1349,7 +1358,7 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   double* U_dev, double* lk_var_dev, float* samples_dev,
                   double* sample_lik_dev, void* ws, size_t ws_size,
                   int* status_dev, cudaStream_t stream, GlmTune tune, int steps,
-                  int64_t idx_step_stride) {
+                  int64_t idx_step_stride, const int32_t* ident_dev) {
   GlmArgs a;
   int rc = fill_common(a, model, chains, n, idx_dev, idx_stride, nullptr, ws,
                        ws_size, status_dev, tune);
@@ -1366,6 +1375,10 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                      "sgld_glm_steps: steps < 1, negative index step stride, or "
                      "injected noise with several steps");
   if (steps > 1 && chains == 0) return GBSGMC_OK;
+  if (ident_dev != nullptr && steps > 1)
+    return set_error(GBSGMC_ERR_ARG, "sgld_glm_steps: chain identities need one step "
+                                     "per launch");
+  a.ident = ident_dev;
   a.steps = steps;
   a.idx_step_stride = steps > 1 ? idx_step_stride : 0;
   a.mode = kSgldStep;

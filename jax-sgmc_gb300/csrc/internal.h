@@ -35,7 +35,20 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
                   double* U_dev, double* lk_var_dev, float* samples_dev,
                   double* sample_lik_dev, void* ws, size_t ws_size,
                   int* status_dev, cudaStream_t stream, GlmTune tune,
-                  int steps = 1, int64_t idx_step_stride = 0);
+                  int steps = 1, int64_t idx_step_stride = 0,
+                  const int32_t* ident_dev = nullptr);
+// The exchange of reSGLD (normal, hot) pairs on the device after a step of
+// all 2 * pairs chains (normal chain p in slot p, its hot partner in slot
+// pairs + p): solver.parallel_tempering's rule per pair in FP64, and for a
+// pair that exchanges, its rows of x (and v), U, var and chain identities
+// swapped; then, at kept steps, the normal slots' rows and -U stored as the
+// step's samples.  Pair p's uniform is Philox(counter (0, k + 1), key
+// (seed << 32) | pair_chain[p]).
+int resgld_pairs_exchange(int pairs, int d, float* x, float* v, double* U,
+                          double* var, int32_t* ident, const gbsgmc_sched* sched,
+                          double F, uint64_t seed, const int32_t* pair_chain,
+                          double* ssq, int64_t* k, int32_t* counts, float* samples,
+                          double* sample_lik, cudaStream_t stream);
 
 // update.cu: fusions of the integrator updates used by the network plans.
 struct UpdateFusion {

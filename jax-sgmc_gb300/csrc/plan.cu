@@ -620,6 +620,145 @@ extern "C" int gbsgmc_sgld_glm_plan_create(
   return GBSGMC_OK;
 }
 
+namespace {
+
+// reSGLD pairs on a GLM potential (alias.re_sgld through solver.mcmc): 2P
+// chains, normal chain p in slot p and its hot partner in slot P + p, plain
+// SGLD (or SGLD + rms_prop) at the slot's temperature, and after every step
+// the pairs' exchange on the device.  The chains' index streams and noise
+// belong to chain identities that travel with exchanged states: identity i
+// draws its own indices (buffer [G, 2P, n] by identity) and its own noise
+// (chain id chain_base + i), and slot s runs identity ident[s].
+struct GlmPairsPlan final : gbsgmc_plan {
+  gbsgmc_glm model;
+  int pairs = 0, n = 0;
+  float* w = nullptr;
+  float* v = nullptr;
+  float alpha = 0.9f, lmbd = 1e-5f;
+  gbsgmc_sched sched{};
+  gbsgmc_noise noise{};
+  gbsgmc_index_src isrc{};
+  gbsgmc_tempering temp{};
+  const int32_t* pair_chain = nullptr;
+  int32_t* ident = nullptr;
+  double* U = nullptr;
+  double* lk_var = nullptr;
+  float* samples = nullptr;
+  double* sample_lik = nullptr;
+  int* status = nullptr;
+  gbsgmc::GlmTune tune;
+  void* ws = nullptr;
+  size_t ws_size = 0;
+  int32_t* idx = nullptr;
+
+  ~GlmPairsPlan() override {
+    if (stream != nullptr) cudaStreamSynchronize(stream);
+    gbsgmc::plan_free(this, ws);
+    gbsgmc::plan_free(this, idx);
+  }
+  int64_t launches_per_block(int g) const override { return 2 + 2 * static_cast<int64_t>(g); }
+  int enqueue(int g, cudaStream_t s) override {
+    using namespace gbsgmc;
+    const int chains = 2 * pairs;
+    const int64_t cn = static_cast<int64_t>(chains) * n;
+    const int64_t rows = model.n_rows > 0 ? model.n_rows : model.n_obs;
+    int rc = gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows, static_cast<int64_t>(g) * n,
+                                     n, idx, n, cn, status, s);
+    if (rc != GBSGMC_OK) return rc;
+    for (int j = 0; j < g; ++j) {
+      gbsgmc_sched sj = sched;
+      sj.base_dev = base;
+      sj.offset = j;
+      gbsgmc_sched step_sched = sj;
+      step_sched.keep_slot_dev = nullptr;  // the exchange stores the samples
+      rc = glm_sgld_step(&model, chains, n, idx + j * cn, n, w, v, alpha, lmbd, &step_sched,
+                         &noise, U, lk_var, nullptr, nullptr, ws, ws_size, status, s, tune,
+                         1, 0, ident);
+      if (rc != GBSGMC_OK) return rc;
+      rc = resgld_pairs_exchange(pairs, model.d, w, v, U, lk_var, ident, &sj, temp.F,
+                                 temp.seed, pair_chain, temp.ssq_dev, temp.k_dev,
+                                 temp.counts_dev, samples, sample_lik, s);
+      if (rc != GBSGMC_OK) return rc;
+    }
+    return plan_advance(this, g, s);
+  }
+};
+
+}  // namespace
+
+extern "C" int gbsgmc_glm_resgld_plan_create(
+    gbsgmc_plan** out, const gbsgmc_glm* model, int pairs, int n, float* x_dev,
+    float* v_dev, float alpha, float lmbd, const gbsgmc_sched* sched,
+    const gbsgmc_noise* noise, const gbsgmc_index_src* index_src,
+    const gbsgmc_tempering* tempering, const int32_t* pair_chain_dev, int32_t* ident_dev,
+    double* U_dev, double* lk_var_dev, float* samples_dev, double* sample_lik_dev,
+    int block_steps, int* status_dev) {
+  if (out == nullptr || model == nullptr || sched == nullptr || noise == nullptr ||
+      index_src == nullptr || tempering == nullptr || x_dev == nullptr ||
+      pair_chain_dev == nullptr || ident_dev == nullptr || U_dev == nullptr ||
+      lk_var_dev == nullptr || status_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "glm_resgld_plan_create: null argument");
+  *out = nullptr;
+  if (pairs <= 0 || n <= 0 || block_steps <= 0 || block_steps > 100000 ||
+      pairs > (1 << 20))
+    return set_error(GBSGMC_ERR_ARG, "glm_resgld_plan_create: bad pairs/n/block_steps");
+  if (index_src->pcg_dev == nullptr || index_src->external)
+    return set_error(GBSGMC_ERR_ARG,
+                     "glm_resgld_plan_create: needs PCG64 index streams (one per chain)");
+  if (sched->chain_temperature_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG,
+                     "glm_resgld_plan_create: needs the per-chain temperatures");
+  if (tempering->ssq_dev == nullptr || tempering->k_dev == nullptr ||
+      !(tempering->F != 0.0))
+    return set_error(GBSGMC_ERR_ARG, "glm_resgld_plan_create: bad tempering state");
+  if (sched->keep_slot_dev != nullptr && samples_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG,
+                     "glm_resgld_plan_create: keep table given without sample buffer");
+  GlmPairsPlan* p = new (std::nothrow) GlmPairsPlan();
+  if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "glm_resgld_plan_create: out of memory");
+  p->model = *model;
+  p->pairs = pairs;
+  p->n = n;
+  p->w = x_dev;
+  p->v = v_dev;
+  p->alpha = alpha;
+  p->lmbd = lmbd;
+  p->sched = *sched;
+  p->noise = *noise;
+  p->isrc = *index_src;
+  p->temp = *tempering;
+  p->pair_chain = pair_chain_dev;
+  p->ident = ident_dev;
+  p->U = U_dev;
+  p->lk_var = lk_var_dev;
+  p->samples = samples_dev;
+  p->sample_lik = sample_lik_dev;
+  p->status = status_dev;
+  int rc = GBSGMC_OK;
+  do {
+    if ((rc = plan_init(p, block_steps))) break;
+    const int chains = 2 * pairs;
+    p->ws_size = glm_ws_bytes(chains, n, model->d);
+    if ((rc = plan_alloc(p, &p->ws, p->ws_size, "glm_resgld_plan_create: workspace"))) break;
+    if ((rc = plan_alloc(p, &p->idx,
+                         sizeof(int32_t) * static_cast<size_t>(block_steps) * chains * n,
+                         "glm_resgld_plan_create: index buffer")))
+      break;
+    if ((rc = glm_prepare())) break;
+    // One launch per step (the exchange sits between steps): the cached
+    // launch shape of this problem, or the library's default.
+    glm_tune_lookup(chains, n, model->d, model->ld, &p->tune);
+    p->tune.multistep = 0;
+    rc = plan_capture(p);
+  } while (false);
+  if (rc != GBSGMC_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return GBSGMC_OK;
+}
+
 extern "C" int gbsgmc_plan_run(gbsgmc_plan* p, int64_t first_step,
                                int64_t steps, gbsgmc_stream_t stream) {
   if (p == nullptr) return set_error(GBSGMC_ERR_ARG, "plan_run: null plan");

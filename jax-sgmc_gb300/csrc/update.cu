@@ -435,6 +435,71 @@ __global__ void resgld_swap_kernel(int pairs, const double* Un,
   perm[i] = (log(u) < log_s) ? 0 : 1;
 }
 
+// One CTA per (normal, hot) pair: the decision of resgld_swap_kernel at the
+// pair's own counter k, the swap of the pair's slots, then the kept sample
+// of the normal slot.
+__global__ void resgld_pairs_kernel(int pairs, int d, float* x, float* v, double* U,
+                                    double* var, int32_t* ident, Sched sched, double F,
+                                    uint64_t seed, const int32_t* pair_chain, double* ssq,
+                                    int64_t* kc, int32_t* counts, float* samples,
+                                    double* sample_lik) {
+  const int p = blockIdx.x;
+  const int sn = p, sh = pairs + p;
+  const int64_t k = sched.step();
+  __shared__ int swapped;
+  if (threadIdx.x == 0) {
+    const int64_t kk = kc[p] + 1;
+    kc[p] = kk;
+    const double sa = 1.0 / static_cast<double>(kk);
+    const double s2 = (1.0 - sa) * ssq[p] + sa * var[sn];
+    ssq[p] = s2;
+    const double Tn = sched.temperature(k, sn), Th = sched.temperature(k, sh);
+    const double dbeta = 1.0 / Tn - 1.0 / Th;
+    const double log_s = dbeta * (U[sn] - U[sh] - dbeta * s2 / F);
+    const uint64_t key = (seed << 32) | static_cast<uint32_t>(__ldg(pair_chain + p));
+    const double u = swap_uniform(key, 0u, static_cast<uint32_t>(k + 1));
+    // The reference keeps the pair when log u < log s (lax.cond true branch).
+    const int sw = (log(u) < log_s) ? 0 : 1;
+    swapped = sw;
+    if (sw) {
+      double t = U[sn];
+      U[sn] = U[sh];
+      U[sh] = t;
+      t = var[sn];
+      var[sn] = var[sh];
+      var[sh] = t;
+      const int32_t i = ident[sn];
+      ident[sn] = ident[sh];
+      ident[sh] = i;
+      if (counts != nullptr) counts[p] += 1;
+    }
+  }
+  __syncthreads();
+  float* xn = x + static_cast<int64_t>(sn) * d;
+  float* xh = x + static_cast<int64_t>(sh) * d;
+  if (swapped) {
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      const float t = xn[j];
+      xn[j] = xh[j];
+      xh[j] = t;
+      if (v != nullptr) {
+        float* vn = v + static_cast<int64_t>(sn) * d;
+        float* vh = v + static_cast<int64_t>(sh) * d;
+        const float tv = vn[j];
+        vn[j] = vh[j];
+        vh[j] = tv;
+      }
+    }
+  }
+  const int slot = sched.keep_slot(k);
+  if (slot >= 0) {
+    float* dst = samples + (static_cast<int64_t>(slot) * pairs + p) * d;
+    for (int j = threadIdx.x; j < d; j += blockDim.x) dst[j] = xn[j];
+    if (threadIdx.x == 0 && sample_lik != nullptr)
+      sample_lik[static_cast<int64_t>(slot) * pairs + p] = -U[sn];
+  }
+}
+
 __global__ void swap_rows_kernel(int pairs, int64_t width, float* a, float* b,
                                  const int32_t* perm) {
   const int i = blockIdx.y;
@@ -837,6 +902,24 @@ extern "C" int gbsgmc_resgld_swap_f64(
       F, ssq_dev, k_dev, u_dev, seed, step, log_s_dev, perm_dev);
   return check_launch("resgld_swap");
 }
+
+namespace gbsgmc {
+
+int resgld_pairs_exchange(int pairs, int d, float* x, float* v, double* U,
+                          double* var, int32_t* ident, const gbsgmc_sched* sched,
+                          double F, uint64_t seed, const int32_t* pair_chain,
+                          double* ssq, int64_t* k, int32_t* counts, float* samples,
+                          double* sample_lik, cudaStream_t stream) {
+  if (pairs <= 0 || d <= 0) return GBSGMC_OK;
+  if (sched->keep_slot_dev != nullptr && samples == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "resgld pairs: keep table without sample buffer");
+  resgld_pairs_kernel<<<pairs, 128, 0, stream>>>(pairs, d, x, v, U, var, ident,
+                                                 to_sched(sched), F, seed, pair_chain, ssq,
+                                                 k, counts, samples, sample_lik);
+  return check_launch("resgld_pairs");
+}
+
+}  // namespace gbsgmc
 
 extern "C" int gbsgmc_swap_rows(int pairs, int64_t width, float* a_dev,
                                 float* b_dev, const int32_t* perm_dev,

@@ -202,6 +202,10 @@ SIGNATURES = {
                                            _vp, _f, _f, _P(Sched), _P(Noise),
                                            _P(IndexSrc), _P(Tempering), _vp,
                                            _vp, _i, _vp]),
+    "gbsgmc_glm_resgld_plan_create": (_i, [_P(_vp), _P(Glm), _i, _i, _vp, _vp,
+                                           _f, _f, _P(Sched), _P(Noise),
+                                           _P(IndexSrc), _P(Tempering), _vp, _vp,
+                                           _vp, _vp, _vp, _vp, _i, _vp]),
     "gbsgmc_plan_run": (_i, [_vp, _i64, _i64, _vp]),
     "gbsgmc_plan_launches": (_i64, [_vp, _i64]),
     "gbsgmc_plan_set_indices": (_i, [_vp, _vp, _i, _vp]),

@@ -42,6 +42,10 @@ class SgldRun(NamedTuple):
 # during the run.
 RING_BYTES = 4 << 30
 
+# Per-pair exchange counts ([P] int32, host) of the last reSGLD pairs run
+# through try_fused_resgld, for inspection.
+LAST_EXCHANGES = None
+
 
 class _ExternalIndices:
   """Feeds a plan with an external index source: before each run of at
@@ -635,6 +639,174 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
                                treedefs, {"likelihood": res.sample_lik},
                                model_states, host=res.host,
                                host_filled=res.host is not None)
+
+
+class ResgldPairsPlan:
+  """Owns a ``gbsgmc_glm_resgld_plan``: P (normal, hot) pairs of SGLD chains
+  on a GLM potential with the pairs' exchange after every step on the
+  device (alias.re_sgld).  X [2P, d] holds the normal chains in rows [0, P)
+  and their hot partners in rows [P, 2P); ``ident`` [2P] maps each row to
+  the chain identity (index stream ``pcg[i]``, noise chain id chain_base + i)
+  it holds after the exchanges so far."""
+
+  def __init__(self, potential, dataset, X, V, alpha, lmbd, n, h_tab, t_tab,
+               keep_tab, ladder, n_kept, pcg, ident, pair_chain, ssq, k, F,
+               swap_seed, noise_seed, chain_base, block_steps):
+    import torch
+    P2, d = X.shape
+    self.pairs = P2 // 2
+    self.model, self._keep_alive = potential.model(dataset)
+    self.X, self.V, self.pcg, self.ident = X, V, pcg, ident
+    self.pair_chain, self.ssq, self.k = pair_chain, ssq, k
+    self.U = torch.zeros(P2, dtype=torch.float64, device="cuda")
+    self.lk_var = torch.zeros(P2, dtype=torch.float64, device="cuda")
+    self.counts = torch.zeros(self.pairs, dtype=torch.int32, device="cuda")
+    self.samples = torch.empty((max(n_kept, 1), self.pairs, d), dtype=torch.float32,
+                               device="cuda")
+    self.sample_lik = torch.empty((max(n_kept, 1), self.pairs), dtype=torch.float64,
+                                  device="cuda")
+    self.status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    self.tabs = (h_tab, t_tab, keep_tab, ladder)
+    self.sched = _lib.sched(step_size_dev=h_tab, temperature_dev=t_tab,
+                            keep_slot_dev=keep_tab, chain_temperature_dev=ladder)
+    self.noise = _lib.noise(noise_seed, chain_base)
+    self.isrc = _lib.IndexSrc(_lib.ptr(pcg), 0, int(chain_base), 0)
+    self.temp = _lib.Tempering(1, 0, float(F), int(swap_seed) & (2**64 - 1),
+                               _lib.ptr(ssq), _lib.ptr(k), _lib.ptr(self.counts), None)
+    handle = _lib.C.c_void_p()
+    _lib.call("gbsgmc_glm_resgld_plan_create", _lib.C.byref(handle), self.model,
+              self.pairs, int(n), _lib.ptr(X), _lib.ptr(V), float(alpha), float(lmbd),
+              self.sched, self.noise, self.isrc, self.temp, _lib.ptr(pair_chain),
+              _lib.ptr(ident), _lib.ptr(self.U), _lib.ptr(self.lk_var),
+              _lib.ptr(self.samples), _lib.ptr(self.sample_lik), int(block_steps),
+              _lib.ptr(self.status))
+    self.handle = handle
+
+  def run(self, first_step, steps):
+    _lib.call("gbsgmc_plan_run", self.handle, int(first_step), int(steps),
+              _lib.stream_handle())
+
+  def launches(self, steps) -> int:
+    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps)))
+
+  def check_status(self):
+    code = int(self.status.item())
+    if code != 0:
+      raise _lib.GbsgmcError(code, "device status of the reSGLD pairs plan")
+
+  def close(self):
+    if getattr(self, "handle", None):
+      _lib.load().gbsgmc_plan_destroy(self.handle)
+      self.handle = None
+
+  def __del__(self):
+    try:
+      self.close()
+    except Exception:  # pragma: no cover - interpreter shutdown
+      pass
+
+
+def try_fused_resgld(solver, scheduler, states, schedulers, iterations, saving):
+  """Runs alias.re_sgld's pairs (solver.parallel_tempering over
+  langevin_diffusion, solver.py:220-299) on a GLM potential as one
+  :class:`ResgldPairsPlan`: every pair steps, exchanges and keeps its normal
+  chain's samples on the device, and the chains' index streams and noise
+  are the per-pair path's, so the samples are the same.  Returns None when
+  the pairs do not qualify: fresh pairs of one key and one F whose chains
+  have consecutive ids (normal, hot, normal, hot, ...), fresh numpy PCG64
+  pipelines, one hot schedule whose temperatures are the normal schedule's
+  times a constant factor and whose step sizes are the same, no injected
+  noise."""
+  import torch
+  from .integrator import LangevinState, key_to_seed
+  from .potential import StochasticPotential
+  meta = getattr(solver, "meta", {})
+  if not FUSED_ENABLED or meta.get("kind") != "parallel_tempering":
+    return None
+  if not schedulers or len(schedulers) != 1 or not len(states):
+    return None
+  im = getattr(meta.get("integrator"), "meta", {})
+  if im.get("kind") != "langevin" or im.get("noise_source") is not None:
+    return None
+  pot, bfn = im.get("potential"), im.get("batch_fn")
+  if not isinstance(pot, StochasticPotential) or pot.is_network:
+    return None
+  if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn) \
+      or bfn[1].kind != "host":
+    return None
+  rbf = bfn[1]
+  P = len(states)
+  chains = []
+  for s in states:
+    chains += [s.normal, s.hot]
+  if not all(isinstance(c, LangevinState) and c.step == 0 for c in chains):
+    return None
+  seeds = {int(s.seed) for s in states}
+  if len(seeds) != 1 or len({float(s.F) for s in states}) != 1:
+    return None
+  seed = seeds.pop()
+  if any(c.key != seed for c in chains):
+    return None
+  ids = [int(c.chain) for c in chains]
+  if ids != list(range(ids[0], ids[0] + 2 * P)):
+    return None
+  if any(int(s.pair_chain) != int(s.normal.chain) for s in states):
+    return None
+  ds = [c.data_state for c in chains]
+  if any(d.state is None or d.cached_batches is not None for d in ds):
+    return None
+  adapt = [c.adapt_state for c in chains]
+  if any(a is None for a in adapt) != all(a is None for a in adapt):
+    return None
+  h, t, keep, n_kept, _ = sched_mod.tables(scheduler, iterations)
+  h2, t2, _, _, _ = sched_mod.tables(scheduler, iterations, **schedulers[0])
+  if not np.array_equal(h, h2) or iterations == 0 or not (t[0] > 0):
+    return None
+  f = np.float32(t2[0] / t[0])
+  if not np.array_equal((t * f).astype(np.float32), t2):
+    return None
+  dataset = rbf.loader.device_dataset()
+  normals = [s.normal for s in states]
+  hots = [s.hot for s in states]
+  X = torch.stack([c.latent_variables for c in normals + hots]).contiguous().cuda()
+  if X.shape[1] != pot.dim(dataset):
+    return None
+  if adapt[0] is not None:
+    V = torch.stack([c.adapt_state.v for c in normals + hots]).contiguous().cuda()
+    alpha, lmbd = adapt[0].alpha, adapt[0].lmbd
+  else:
+    V, alpha, lmbd = None, 0.9, 1e-5
+  pcg = torch.stack([d.state for d in ds]).contiguous().cuda()   # by identity
+  ident = torch.from_numpy(np.concatenate([np.arange(0, 2 * P, 2),
+                                           np.arange(1, 2 * P, 2)]).astype(np.int32)).cuda()
+  pair_chain = torch.tensor([int(s.pair_chain) for s in states], dtype=torch.int32,
+                            device="cuda")
+  ssq = torch.cat([s.ssq.reshape(1).to(torch.float64) for s in states]).cuda()
+  k = torch.cat([s.step.reshape(1).to(torch.int64) for s in states]).cuda()
+  ladder = torch.from_numpy(np.concatenate([np.ones(P, np.float32),
+                                            np.full(P, f, np.float32)])).cuda()
+  tabs = [torch.from_numpy(np.ascontiguousarray(a)).cuda()
+          for a in (np.asarray(h, np.float32), np.asarray(t, np.float32),
+                    np.asarray(keep, np.int32))]
+  block = min(rbf.cached_batches_count, DEFAULT_BLOCK_STEPS, max(iterations, 1))
+  plan = ResgldPairsPlan(pot, dataset, X, V, alpha, lmbd, rbf.mb_size, *tabs, ladder,
+                         n_kept, pcg, ident, pair_chain, ssq, k, float(states[0].F),
+                         seed, seed, ids[0], block)
+  global LAST_EXCHANGES
+  try:
+    plan.run(0, iterations)
+    plan.check_status()
+    samples, lik = plan.samples[:n_kept], plan.sample_lik[:n_kept]
+    LAST_EXCHANGES = plan.counts.cpu().numpy()
+  finally:
+    plan.close()
+  host = pcg.cpu()   # the identities' streams advanced on the device
+  for i, d in enumerate(ds):
+    d.state.copy_(pcg[i] if d.state.is_cuda else host[i])
+  return io.postprocess_chains(saving or io.no_save(), n_kept, samples,
+                               [s.normal.treedef for s in states],
+                               {"likelihood": lik},
+                               [s.normal.model_state for s in states])
 
 
 def try_fused_mh(solver, scheduler, states, schedulers, iterations, saving):

@@ -52,7 +52,9 @@ class TemperingState(NamedTuple):
   ssq: Any        # fp64 device [1]
   F: float
   step: Any       # int64 device [1]
-  key: int
+  key: int        # the exchange uniforms' Philox key: (seed << 32) | pair chain
+  seed: int = 0   # the user's key
+  pair_chain: int = 0   # chain id of the pair's first normal chain
 
 
 def parallel_tempering(integrator, sa_schedule=None):
@@ -72,13 +74,22 @@ def parallel_tempering(integrator, sa_schedule=None):
   def init(normal_sample, tempered_sample, ssq_init=0.0, key=0, F=1.0,
            **kwargs):
     import torch
+    from .integrator import key_to_seed
     seed = int(np.asarray(key).ravel()[-1]) if key is not None else 0
-    normal = init_integrator(normal_sample, key=(seed, 1), **kwargs)
-    hot = init_integrator(tempered_sample, key=(seed, 2), **kwargs)
+    # Both chains draw their noise with the pair's key; their own chain ids
+    # (their data pipelines') keep the streams apart, and the streams move
+    # with the states when the pair exchanges them.  Chains without distinct
+    # ids (pipelines that carry none) get distinct keys instead.
+    normal = init_integrator(normal_sample, key=seed, **kwargs)
+    hot = init_integrator(tempered_sample, key=seed, **kwargs)
+    if normal.chain == hot.chain:
+      normal = normal._replace(key=key_to_seed((seed, 1)))
+      hot = hot._replace(key=key_to_seed((seed, 2)))
     return TemperingState(
         normal, hot,
         torch.full((1,), float(ssq_init), dtype=torch.float64, device="cuda"),
-        float(F), torch.zeros(1, dtype=torch.int64, device="cuda"), seed)
+        float(F), torch.zeros(1, dtype=torch.int64, device="cuda"),
+        key_to_seed((seed, normal.chain)), seed, int(normal.chain))
 
   def update(state: TemperingState, normal_schedule, hot_schedule,
              uniform=None):
@@ -308,8 +319,11 @@ def mcmc(solver, scheduler, strategy="map", saving=None, loading=None):
     if loading is not None:
       raise NotImplementedError("Loading of checkpoints is currently not "
                                 "supported.")
-    fused = engine.try_fused_sgld(solver, scheduler, states, schedulers,
-                                  iterations, saving)
+    fused = engine.try_fused_resgld(solver, scheduler, states, schedulers,
+                                    iterations, saving)
+    if fused is None:
+      fused = engine.try_fused_sgld(solver, scheduler, states, schedulers,
+                                    iterations, saving)
     if fused is None:
       fused = engine.try_fused_net(solver, scheduler, states, schedulers,
                                    iterations, saving)

@@ -244,3 +244,38 @@ def test_row_layouts_through_the_abi(lib, d, ld, inline):
   ref = O.glm_potential(W, X, y, idx, N, O.LOGISTIC, 1.0, 2.0, 1.0)
   from types import SimpleNamespace
   check(SimpleNamespace(U=U, grad=G, lk_var=var), ref)
+
+
+@pytest.mark.parametrize("family", ["logistic", "lingauss"])
+@pytest.mark.parametrize("n", [4096, 16384])
+def test_potential_sum_is_compensated(lib, family, n):
+  """U sums the minibatch's fp32 likelihoods with a compensated (Neumaier)
+  sum per lane and fp64 across lanes, so U differs from the exact sum of the
+  kernel's own per-row likelihoods by summation error alone: at most 1e-10
+  relative here, where uncompensated fp32 lane sums left about 5e-9.  The
+  remaining distance to the FP64 oracle (under 3e-8 relative) is the fp32
+  rounding of the per-row likelihoods themselves."""
+  import torch
+  from gbsgmc import data, likelihoods as L, potential
+  rng = np.random.default_rng(n)
+  N, d, C = 50_000, 64, 16
+  X = rng.normal(size=(N, d)).astype(np.float32)
+  w = rng.normal(size=d)
+  if family == "logistic":
+    y = (rng.random(N) < 1 / (1 + np.exp(-X @ w / 4))).astype(np.float32)
+    lik, fam = L.Logistic(), O.LOGISTIC
+  else:
+    y = (X @ w + 3.0 + 0.5 * rng.normal(size=N)).astype(np.float32)
+    lik, fam = L.LinearGaussian(sigma=0.5), O.LINEAR_GAUSSIAN
+  pot = potential.minibatch_potential(L.GaussianPrior(1.0), lik)
+  W = (rng.normal(size=(C, d)) * 0.2).astype(np.float32)
+  idx = rng.integers(0, N, (C, n)).astype(np.int32)
+  r = pot.evaluate(torch.from_numpy(W).cuda(), torch.from_numpy(idx).cuda(),
+                   data.NumpyDataLoader(x=X, y=y).device_dataset(), lk=True)
+  pot.check_status()
+  U = r.U.cpu().numpy()
+  lp, _ = O.log_prior(W, 1.0)
+  U_lk = -(N / n) * r.lk.cpu().numpy().astype(np.float64).sum(1) - lp
+  assert np.max(np.abs(U - U_lk) / np.abs(U_lk)) <= 1e-10
+  ref = O.glm_potential(W, X, y, idx, N, fam, 0.5, 1.0)
+  assert np.max(np.abs(U - ref.U) / np.abs(ref.U)) <= 3e-8
