@@ -255,6 +255,37 @@ int gbsgmc_glm_fisher_noise(const gbsgmc_glm* model, int chains, int n,
                             float step_size, float* cb_diff_sqrt_dev, float* b_sqrt_dev,
                             int* status_dev, gbsgmc_stream_t stream);
 
+/* The dense form, fisher_information(diagonal=False)
+ * (jax_sgmc/adaption.py:441-452): with d_i = lk'(z_i) x_i - G / N,
+ *   b = 0.5 step_size / (n - 1) sum_i d_i d_i^T       (d x d),
+ *   cb_diff_sqrt = u sqrt(s) for (u, s, .) = svd(diag(friction) - b),
+ *   b_sqrt = u sqrt(s) for (u, s, .) = svd(b),
+ * each a d-vector (the left singular vectors times the root singular
+ * values, which the integrator applies elementwise, as the reference does).
+ * The SVDs of these symmetric matrices come from their eigendecompositions
+ * (gbsgmc_sym_eig's method and sign convention; the signs of LAPACK's
+ * singular vectors are not specified, and these vectors depend on them).
+ * d <= 128, 2 <= n <= 4096 (n * 8 bytes + 8 d^2 bytes of shared memory
+ * within 227 KB); fp32. */
+int gbsgmc_glm_fisher_noise_dense(const gbsgmc_glm* model, int chains, int n,
+                                  const int32_t* idx_dev, int64_t idx_stride,
+                                  const float* w_dev, const float* grad_dev,
+                                  const float* friction_dev, float friction,
+                                  float step_size, float* cb_diff_sqrt_dev,
+                                  float* b_sqrt_dev, int* status_dev,
+                                  gbsgmc_stream_t stream);
+
+/* Eigendecomposition of `batch` symmetric P x P matrices (A_dev [batch, P,
+ * P], row-major; the symmetric part (A + A^T) / 2 is used): eigenvalues in
+ * ascending order to w_dev [batch, P] and the eigenvectors as the columns of
+ * V_dev [batch, P, P], each scaled so that its largest-magnitude component
+ * (the first of equal ones) is positive.  Cyclic Jacobi with the
+ * round-robin ordering, one CTA per matrix, fp32; P <= 128.
+ * Replaces jnp.linalg.eigh in mass_matrix(diagonal=False)
+ * (jax_sgmc/adaption.py:316). */
+int gbsgmc_sym_eig(int batch, int P, const float* A_dev, float* w_dev,
+                   float* V_dev, gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Reversible leapfrog (AMAGOLD) and Metropolis-Hastings corrections         */
 /* ------------------------------------------------------------------------ */

@@ -167,6 +167,9 @@ SIGNATURES = {
     "gbsgmc_mass_adapt": (_i, [_i64, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbsgmc_glm_fisher_noise": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp, _vp,
                                      _f, _f, _vp, _vp, _vp, _vp]),
+    "gbsgmc_glm_fisher_noise_dense": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp,
+                                           _vp, _f, _f, _vp, _vp, _vp, _vp]),
+    "gbsgmc_sym_eig": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
     "gbsgmc_sghmc_momentum_noise_model": (_i, [_i, _i64, _vp, _vp, _vp, _P(Sched),
                                                _P(Noise), _vp]),
     "gbsgmc_resgld_swap_f64": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _vp, _vp,

@@ -16,8 +16,9 @@ them into the parameter update (``gbsgmc_sgld_update``,
 (AMAGOLD, SGGMC) on the device with ``gbsgmc_mass_adapt``
 (adaption.py:296-368).  ``fisher_information(diagonal=True)`` is SGHMC's
 empirical-Fisher noise model (adaption.py:371-457) on the generalised-linear
-likelihoods (``gbsgmc_glm_fisher_noise``).  The dense variants are not
-provided.
+likelihoods (``gbsgmc_glm_fisher_noise``), and with ``diagonal=False`` its
+dense form for up to 128 parameters (``gbsgmc_glm_fisher_noise_dense``).
+The dense mass matrix is not provided.
 """
 
 from __future__ import annotations
@@ -156,11 +157,10 @@ def fisher_information(minibatch_potential=None, diagonal=True) -> AdaptionStrat
   ``get(state, sample, sample_grad, friction, mini_batch=..., step_size=...)``
   returns the :class:`NoiseModel` of the current minibatch, computed on the
   device from the per-observation likelihood gradients (the
-  generalised-linear families)."""
+  generalised-linear families): elementwise (``diagonal=True``), or from
+  the d x d matrices (``diagonal=False``, d <= 128) through their
+  eigendecompositions (``gbsgmc_glm_fisher_noise_dense``)."""
   assert minibatch_potential, "Fisher information requires potential function."
-  if not diagonal:
-    raise NotImplementedError("only the diagonal noise model is provided (the "
-                              "dense one needs two SVDs of P x P matrices)")
   if getattr(minibatch_potential, "is_network", False):
     raise NotImplementedError("per-observation gradients are provided for the "
                               "generalised-linear likelihoods")
@@ -193,7 +193,8 @@ def fisher_information(minibatch_potential=None, diagonal=True) -> AdaptionStrat
       fric, f = _flat_device(friction), 0.0
     cb = torch.empty(P, dtype=torch.float32, device="cuda")
     bs = torch.empty(P, dtype=torch.float32, device="cuda")
-    _lib.call("gbsgmc_glm_fisher_noise", m, 1, idx.numel(), _lib.ptr(idx),
+    _lib.call("gbsgmc_glm_fisher_noise" if diagonal else "gbsgmc_glm_fisher_noise_dense",
+              m, 1, idx.numel(), _lib.ptr(idx),
               idx.numel(), _lib.ptr(x), _lib.ptr(g), _lib.ptr(fric), f,
               float(step_size), _lib.ptr(cb), _lib.ptr(bs),
               _lib.ptr(pot.status()), _lib.stream_handle())

@@ -250,6 +250,39 @@ def fisher_noise(w, X, y, idx, grad, n_obs, family, sigma, friction, step_size):
   return np.sqrt(pc), np.sqrt(f - pc)
 
 
+def sym_eig(A):
+  """Symmetric eigendecomposition with the library's conventions (float64,
+  numpy.linalg.eigh): eigenvalues ascending, each eigenvector's
+  largest-magnitude component (the first of equal ones) positive."""
+  w, V = np.linalg.eigh(0.5 * (np.asarray(A, np.float64) + np.asarray(A, np.float64).T))
+  k = np.argmax(np.abs(V), axis=0)
+  return w, V * np.where(V[k, np.arange(V.shape[1])] < 0, -1.0, 1.0)
+
+
+def fisher_noise_dense(w, X, y, idx, grad, n_obs, family, sigma, friction,
+                       step_size):
+  """fisher_information(diagonal=False).get (jax_sgmc/adaption.py:403-452),
+  float64, one chain: b = 0.5 h / (n - 1) sum_i d_i d_i^T with d_i the
+  per-observation likelihood gradient minus grad / N;
+  cb_diff_sqrt = u sqrt(s) of svd(diag(friction) - b), b_sqrt = u sqrt(s)
+  of svd(b).  For these symmetric matrices the SVD is taken from
+  :func:`sym_eig` (s = |eigenvalue|, u = the eigenvectors), the sign
+  convention the library uses where LAPACK's is unspecified."""
+  w = np.asarray(w, np.float64)
+  Xb = np.asarray(X, np.float64)[np.asarray(idx)]
+  yb = np.asarray(y, np.float64)[np.asarray(idx)]
+  _, dz = glm_lk(family, Xb @ w, yb, sigma)
+  D = dz[:, None] * Xb - np.asarray(grad, np.float64) / n_obs
+  b = 0.5 * step_size / (len(idx) - 1) * (D.T @ D)
+  f = np.broadcast_to(np.asarray(friction, np.float64), (b.shape[0],))
+
+  def root(M):
+    lam, U = sym_eig(M)
+    return U @ np.sqrt(np.abs(lam))
+
+  return root(np.diag(f) - b), root(b)
+
+
 # ---------------------------------------------------------------------------
 # Dense tanh network with a Gaussian likelihood
 # ---------------------------------------------------------------------------

@@ -295,8 +295,8 @@ def test_unported_presets_raise():
   from gbsgmc import adaption, integrator
   with pytest.raises(AssertionError):        # needs the potential
     adaption.fisher_information()
-  with pytest.raises(NotImplementedError):   # dense noise model
-    adaption.fisher_information(minibatch_potential=object(), diagonal=False)
+  # The dense noise model exists (d <= 128, on the generalised-linear families).
+  adaption.fisher_information(minibatch_potential=object(), diagonal=False)
   with pytest.raises(NotImplementedError):   # dense mass adaption
     adaption.mass_matrix(diagonal=False)
   with pytest.raises(NotImplementedError):   # langevin adapts with rms_prop only

@@ -327,3 +327,34 @@ def test_cpu_baseline_steps_compute_the_potential_and_variance():
   ref = O.glm_potential(W0, X, y, idx, N, O.LOGISTIC, 1.0, 1.0)
   np.testing.assert_allclose(U, ref.U, rtol=1e-5)
   np.testing.assert_allclose(var, ref.var, rtol=1e-4)
+
+
+def test_sym_eig_convention_and_dense_fisher_restatement():
+  """The oracle's eigendecomposition reconstructs its input and follows the
+  library's sign convention; with a scalar friction the dense noise model's
+  two matrices share eigenvectors, and b_sqrt's singular values are b's
+  eigenvalues."""
+  rng = np.random.default_rng(8)
+  M = rng.normal(size=(7, 7))
+  A = M + M.T
+  w, V = O.sym_eig(A)
+  np.testing.assert_allclose(V @ np.diag(w) @ V.T, A, atol=1e-12)
+  assert np.all(np.diff(w) >= 0)
+  k = np.argmax(np.abs(V), axis=0)
+  assert np.all(V[k, np.arange(7)] > 0)
+  N, d, n = 400, 5, 32
+  X = rng.normal(size=(N, d)).astype(np.float32)
+  y = (rng.random(N) < 0.5).astype(np.float32)
+  wv = 0.3 * rng.normal(size=d)
+  idx = rng.integers(0, N, n)
+  g = O.glm_potential(wv[None], X, y, idx[None], N, O.LOGISTIC, 1.0, 1.0).grad[0]
+  cb, bs = O.fisher_noise_dense(wv, X, y, idx, g, N, O.LOGISTIC, 1.0, 2.0, 1e-2)
+  Xb = X[idx].astype(np.float64)
+  dz = y[idx] - 1 / (1 + np.exp(-(Xb @ wv)))
+  D = dz[:, None] * Xb - g / N
+  b = 0.5e-2 / (n - 1) * D.T @ D
+  lam, U = O.sym_eig(b)
+  np.testing.assert_allclose(bs, U @ np.sqrt(np.abs(lam)), rtol=1e-9)
+  lam2, U2 = O.sym_eig(2.0 * np.eye(d) - b)
+  np.testing.assert_allclose(np.sort(lam2), np.sort(2.0 - lam), rtol=1e-10)
+  np.testing.assert_allclose(cb, U2 @ np.sqrt(np.abs(lam2)), rtol=1e-9)
