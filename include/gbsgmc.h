@@ -334,6 +334,55 @@ int gbsgmc_mh_select(int chains, int64_t P, const int32_t* accept_dev,
                      const float* p_old_dev, float reject_momentum_sign,
                      gbsgmc_stream_t stream);
 
+/* Dense mass matrices.  The reference's integrators multiply by the inverse
+ * mass and the root mass as matrices when those are P x P (tensor_matmul of
+ * a Tensor with ndim 2, jax_sgmc/util/tree_util.py:38-56), which is what
+ * mass_matrix(diagonal=False) adapts.  These are the updates of
+ * gbsgmc_leapfrog_position, gbsgmc_amagold_momentum, gbsgmc_obabo_first and
+ * gbsgmc_obabo_second with m^-1 p, m^-1 g and sqrt(m) xi replaced by the
+ * products with minv_dev [P, P] and msqrt_dev [P, P] (row-major, shared by
+ * all chains), and the same noise streams.  One CTA per chain, P <= 8192
+ * (meant for small P: each update reads the matrices once per chain). */
+int gbsgmc_leapfrog_position_dense(int chains, int64_t P, float* x_dev,
+                                   const float* p_dev, const float* minv_dev,
+                                   float scale, const gbsgmc_sched* sched,
+                                   gbsgmc_stream_t stream);
+int gbsgmc_amagold_momentum_dense(int chains, int64_t P, float* p_dev,
+                                  const float* g_dev, const float* minv_dev,
+                                  const float* msqrt_dev, float friction,
+                                  double* energy_dev, const gbsgmc_sched* sched,
+                                  const gbsgmc_noise* noise,
+                                  gbsgmc_stream_t stream);
+int gbsgmc_obabo_first_dense(int chains, int64_t P, float* x_dev, float* p_dev,
+                             const float* g1_dev, const float* minv_dev,
+                             const float* msqrt_dev, float friction,
+                             double* ke_start_dev, const gbsgmc_sched* sched,
+                             const gbsgmc_noise* noise, gbsgmc_stream_t stream);
+int gbsgmc_obabo_second_dense(int chains, int64_t P, float* p_dev,
+                              const float* g2_dev, const float* minv_dev,
+                              const float* msqrt_dev, float friction,
+                              double* ke_end_dev, const gbsgmc_sched* sched,
+                              const gbsgmc_noise* noise, gbsgmc_stream_t stream);
+
+/* y[c] = M x[c] for c < chains (M [P, P] row-major, x and y [chains, P]);
+ * the initial AMAGOLD momentum sqrt(M) xi under a dense mass
+ * (jax_sgmc/solver.py:352).  P <= 8192. */
+int gbsgmc_dense_matvec(int chains, int64_t P, const float* m_dev,
+                        const float* x_dev, float* y_dev, gbsgmc_stream_t stream);
+
+/* One update of mass_matrix(diagonal=False) (jax_sgmc/adaption.py:296-368)
+ * with the `iteration`-th sample x (1-based), fp32 in the reference's
+ * operation order:  mean' = (i-1)/i mean + 1/i x;
+ * ssq += (x - mean)(x - mean')^T  (ssq_dev [P, P]).  When iteration ==
+ * burn_in: inv = ssq / i and, from the eigendecomposition (w, V) of inv
+ * (gbsgmc_sym_eig into eig_w_dev [P] and eig_v_dev [P, P]),
+ * sqrt = V^T diag(sqrt(max(w, 0))) V, the product adaption.py:317 forms.
+ * P <= 128. */
+int gbsgmc_mass_adapt_dense(int64_t P, int iteration, int burn_in,
+                            const float* x_dev, float* mean_dev, float* ssq_dev,
+                            float* inv_dev, float* sqrt_dev, float* eig_w_dev,
+                            float* eig_v_dev, gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Sample statistics                                                         */
 /* ------------------------------------------------------------------------ */

@@ -170,6 +170,17 @@ SIGNATURES = {
     "gbsgmc_glm_fisher_noise_dense": (_i, [_P(Glm), _i, _i, _vp, _i64, _vp, _vp,
                                            _vp, _f, _f, _vp, _vp, _vp, _vp]),
     "gbsgmc_sym_eig": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
+    "gbsgmc_leapfrog_position_dense": (_i, [_i, _i64, _vp, _vp, _vp, _f,
+                                            _P(Sched), _vp]),
+    "gbsgmc_amagold_momentum_dense": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _f,
+                                           _vp, _P(Sched), _P(Noise), _vp]),
+    "gbsgmc_obabo_first_dense": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _vp, _f,
+                                      _vp, _P(Sched), _P(Noise), _vp]),
+    "gbsgmc_obabo_second_dense": (_i, [_i, _i64, _vp, _vp, _vp, _vp, _f, _vp,
+                                       _P(Sched), _P(Noise), _vp]),
+    "gbsgmc_dense_matvec": (_i, [_i, _i64, _vp, _vp, _vp, _vp]),
+    "gbsgmc_mass_adapt_dense": (_i, [_i64, _i, _i, _vp, _vp, _vp, _vp, _vp,
+                                     _vp, _vp, _vp]),
     "gbsgmc_sghmc_momentum_noise_model": (_i, [_i, _i64, _vp, _vp, _vp, _P(Sched),
                                                _P(Noise), _vp]),
     "gbsgmc_resgld_swap_f64": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _vp, _vp,

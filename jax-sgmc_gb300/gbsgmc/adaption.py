@@ -17,8 +17,9 @@ them into the parameter update (``gbsgmc_sgld_update``,
 (adaption.py:296-368).  ``fisher_information(diagonal=True)`` is SGHMC's
 empirical-Fisher noise model (adaption.py:371-457) on the generalised-linear
 likelihoods (``gbsgmc_glm_fisher_noise``), and with ``diagonal=False`` its
-dense form for up to 128 parameters (``gbsgmc_glm_fisher_noise_dense``).
-The dense mass matrix is not provided.
+dense form for up to 128 parameters (``gbsgmc_glm_fisher_noise_dense``);
+``mass_matrix(diagonal=False)`` the dense mass for up to 128 parameters
+(``gbsgmc_mass_adapt_dense``, the dense integrator kernels).
 """
 
 from __future__ import annotations
@@ -111,17 +112,71 @@ def _flat_device(tree):
   return torch.from_numpy(flat).cuda()
 
 
+class DenseMassState(NamedTuple):
+  """Dense mass adaption state (adaption.py:321-340): fp32 device mean [P],
+  ssq [P, P], inverse mass inv [P, P] and root sqrt [P, P], with the
+  eigendecomposition buffers of the final update."""
+  iteration: int
+  mean: Any
+  ssq: Any
+  inv: Any
+  sqrt: Any
+  eig_w: Any
+  eig_v: Any
+  burn_in: int
+
+
+def _dense_mass_matrix(burn_in):
+  def init(sample, init_cov=None) -> DenseMassState:
+    import torch
+    x = _flat_device(sample)
+    P = x.numel()
+    if P > 128:
+      raise NotImplementedError("the dense mass is adapted for up to 128 "
+                                f"parameters (got {P})")
+    cov = torch.ones_like(x) if init_cov is None else _flat_device(init_cov)
+    if cov.numel() != P:
+      raise ValueError(f"init_cov has {cov.numel()} entries, the sample {P}")
+    # The reference's initial dense mass: inv = diag(init_cov),
+    # sqrt = diag(1 / sqrt(init_cov)) (adaption.py:333-335).
+    return DenseMassState(
+        iteration=0, mean=torch.zeros_like(x),
+        ssq=torch.zeros((P, P), dtype=torch.float32, device="cuda"),
+        inv=torch.diag(cov).contiguous(),
+        sqrt=torch.diag(1.0 / cov.sqrt()).contiguous(),
+        eig_w=torch.zeros(P, dtype=torch.float32, device="cuda"),
+        eig_v=torch.zeros((P, P), dtype=torch.float32, device="cuda"),
+        burn_in=int(burn_in))
+
+  def update(state: DenseMassState, sample, *args, **kwargs) -> DenseMassState:
+    from . import _lib
+    del args, kwargs
+    x = _flat_device(sample)
+    it = state.iteration + 1
+    _lib.call("gbsgmc_mass_adapt_dense", x.numel(), it, state.burn_in,
+              _lib.ptr(x), _lib.ptr(state.mean), _lib.ptr(state.ssq),
+              _lib.ptr(state.inv), _lib.ptr(state.sqrt), _lib.ptr(state.eig_w),
+              _lib.ptr(state.eig_v), _lib.stream_handle())
+    return state._replace(iteration=it)
+
+  def get(state: DenseMassState) -> MassMatrix:
+    return MassMatrix(inv=state.inv, sqrt=state.sqrt)
+
+  return AdaptionStrategy(init, update, get, "mass_matrix")
+
+
 def mass_matrix(diagonal=True, burn_in=1000) -> AdaptionStrategy:
   """Adapts the mass for the MH samplers from the accepted samples during
   the first ``burn_in`` updates (adaption.py:296-368): a running mean and
   sum of squared deviations, and at update ``burn_in`` the inverse mass
   ssq / burn_in (the sample variance) and sqrt(burn_in / ssq).  Before then
   the mass is the initial one: inverse ``init_cov`` (ones by default).
-  Only the diagonal form is provided."""
+  With ``diagonal=False`` (up to 128 parameters) ssq is the P x P sum of
+  outer products, the inverse mass ssq / burn_in and the root the product
+  V^T diag(sqrt(w)) V of its eigendecomposition, as adaption.py:314-317
+  writes it; the integrators then multiply by these matrices."""
   if not diagonal:
-    raise NotImplementedError("only the diagonal mass is adapted (the dense "
-                              "form needs an eigendecomposition of a P x P "
-                              "matrix and dense-mass integrator kernels)")
+    return _dense_mass_matrix(burn_in)
 
   def init(sample, init_cov=None) -> MassState:
     import torch

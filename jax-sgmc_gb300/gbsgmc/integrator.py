@@ -137,6 +137,17 @@ def _mass_vector(mass, const_mass, P):
   return m
 
 
+def _dense_mass(mass):
+  """(inverse mass [P, P], root mass [P, P]) fp32 device matrices when
+  ``mass`` is a dense MassMatrix (mass_matrix(diagonal=False)), else None."""
+  if isinstance(mass, MassMatrix) and hasattr(mass.inv, "dim") and mass.inv.dim() == 2:
+    import torch
+    inv = _dev(mass.inv).to(torch.float32).contiguous()
+    sq = _dev(mass.sqrt).to(torch.float32).contiguous()
+    return inv, sq
+  return None
+
+
 def _noise(seed, chain, buf=None):
   if buf is not None:
     return _lib.noise(seed, chain, noise_dev=buf, noise_stride=buf.numel())
@@ -321,7 +332,10 @@ def obabo(potential_fn, batch_fn, steps=10, friction=1.0, const_mass=None,
   def integrate(state: ObaboState, parameters, mass=None):
     x, p = state.positions, state.momentum
     P = x.numel()
-    m = _mass_vector(mass, const_mass, P)
+    dense = _dense_mass(mass)
+    m = None if dense is not None else _mass_vector(mass, const_mass, P)
+    if dense is not None and noise_source is not None:
+      raise NotImplementedError("injected noise with a dense mass")
     data_state = state.data_state
     step = state.step
     pot = state.potential
@@ -331,17 +345,29 @@ def obabo(potential_fn, batch_fn, steps=10, friction=1.0, const_mass=None,
       data_state, (b1, i1) = get_data(data_state, information=True)
       r1 = _eval(potential_fn, x, b1, i1)
       buf1 = _injected(noise_source, step, state.chain, _lib.TAG_OBABO_1)
-      _lib.call("gbsgmc_obabo_first", 1, P, _lib.ptr(x), _lib.ptr(p),
-                _lib.ptr(r1.grad), _lib.ptr(m), float(friction),
-                _lib.ptr(state.kinetic_energy_start), sch,
-                _noise(state.key, state.chain, buf1), _lib.stream_handle())
+      if dense is not None:
+        _lib.call("gbsgmc_obabo_first_dense", 1, P, _lib.ptr(x), _lib.ptr(p),
+                  _lib.ptr(r1.grad), _lib.ptr(dense[0]), _lib.ptr(dense[1]),
+                  float(friction), _lib.ptr(state.kinetic_energy_start), sch,
+                  _noise(state.key, state.chain), _lib.stream_handle())
+      else:
+        _lib.call("gbsgmc_obabo_first", 1, P, _lib.ptr(x), _lib.ptr(p),
+                  _lib.ptr(r1.grad), _lib.ptr(m), float(friction),
+                  _lib.ptr(state.kinetic_energy_start), sch,
+                  _noise(state.key, state.chain, buf1), _lib.stream_handle())
       data_state, (b2, i2) = get_data(data_state, information=True)
       r2 = _eval(potential_fn, x, b2, i2)
       buf2 = _injected(noise_source, step, state.chain, _lib.TAG_OBABO_2)
-      _lib.call("gbsgmc_obabo_second", 1, P, _lib.ptr(p), _lib.ptr(r2.grad),
-                _lib.ptr(m), float(friction),
-                _lib.ptr(state.kinetic_energy_end), sch,
-                _noise(state.key, state.chain, buf2), _lib.stream_handle())
+      if dense is not None:
+        _lib.call("gbsgmc_obabo_second_dense", 1, P, _lib.ptr(p), _lib.ptr(r2.grad),
+                  _lib.ptr(dense[0]), _lib.ptr(dense[1]), float(friction),
+                  _lib.ptr(state.kinetic_energy_end), sch,
+                  _noise(state.key, state.chain), _lib.stream_handle())
+      else:
+        _lib.call("gbsgmc_obabo_second", 1, P, _lib.ptr(p), _lib.ptr(r2.grad),
+                  _lib.ptr(m), float(friction),
+                  _lib.ptr(state.kinetic_energy_end), sch,
+                  _noise(state.key, state.chain, buf2), _lib.stream_handle())
       pot = 0.5 * (r1.U[0] + r2.U[0])
       step += 1
     return state._replace(potential=pot, data_state=data_state, step=step)
@@ -463,9 +489,16 @@ def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,
       p = torch.empty(P, dtype=torch.float32, device="cuda")
       _lib.call("gbsgmc_philox_normal", seed, chain, 1, 0,
                 _lib.TAG_AMAGOLD_INIT, P, _lib.ptr(p), P, _lib.stream_handle())
-    m = _mass_vector(mass, const_mass, P)
-    if m is not None:
-      p = p * m.sqrt()
+    dense = _dense_mass(mass)
+    if dense is not None:
+      q = torch.empty_like(p)
+      _lib.call("gbsgmc_dense_matvec", 1, P, _lib.ptr(dense[1]), _lib.ptr(p),
+                _lib.ptr(q), _lib.stream_handle())
+      p = q
+    else:
+      m = _mass_vector(mass, const_mass, P)
+      if m is not None:
+        p = p * m.sqrt()
     return LeapfrogState(
         positions=w, momentum=p,
         potential=torch.zeros(1, dtype=torch.float64, device="cuda"),
@@ -476,7 +509,10 @@ def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,
     import torch
     x, p = state.positions, state.momentum
     P = x.numel()
-    m = _mass_vector(mass, const_mass, P)
+    dense = _dense_mass(mass)
+    m = None if dense is not None else _mass_vector(mass, const_mass, P)
+    if dense is not None and noise_source is not None:
+      raise NotImplementedError("injected noise with a dense mass")
     step = state.step
     energy = torch.zeros(1, dtype=torch.float64, device="cuda")
 
@@ -484,22 +520,33 @@ def reversible_leapfrog(potential_fn, batch_fn, steps: int = 10,
       return _lib.sched(step_size=float(parameters.step_size),
                         temperature=float(parameters.temperature), offset=k)
 
-    _lib.call("gbsgmc_leapfrog_position", 1, P, _lib.ptr(x), _lib.ptr(p),
-              _lib.ptr(m), 0.5, sch(step), _lib.stream_handle())
+    def position(scale, k):
+      if dense is not None:
+        _lib.call("gbsgmc_leapfrog_position_dense", 1, P, _lib.ptr(x), _lib.ptr(p),
+                  _lib.ptr(dense[0]), scale, sch(k), _lib.stream_handle())
+      else:
+        _lib.call("gbsgmc_leapfrog_position", 1, P, _lib.ptr(x), _lib.ptr(p),
+                  _lib.ptr(m), scale, sch(k), _lib.stream_handle())
+
+    position(0.5, step)
     data_state = state.data_state
     for j in range(steps):
       if j > 0:
-        _lib.call("gbsgmc_leapfrog_position", 1, P, _lib.ptr(x), _lib.ptr(p),
-                  _lib.ptr(m), 1.0, sch(step), _lib.stream_handle())
+        position(1.0, step)
       data_state, (b, i) = get_data(data_state, information=True)
       r = _eval(potential_fn, x, b, i)
-      buf = _injected(noise_source, step, state.chain, _lib.TAG_AMAGOLD)
-      _lib.call("gbsgmc_amagold_momentum", 1, P, _lib.ptr(p), _lib.ptr(r.grad),
-                _lib.ptr(m), f, _lib.ptr(energy), sch(step),
-                _noise(state.key, state.chain, buf), _lib.stream_handle())
+      if dense is not None:
+        _lib.call("gbsgmc_amagold_momentum_dense", 1, P, _lib.ptr(p),
+                  _lib.ptr(r.grad), _lib.ptr(dense[0]), _lib.ptr(dense[1]), f,
+                  _lib.ptr(energy), sch(step), _noise(state.key, state.chain),
+                  _lib.stream_handle())
+      else:
+        buf = _injected(noise_source, step, state.chain, _lib.TAG_AMAGOLD)
+        _lib.call("gbsgmc_amagold_momentum", 1, P, _lib.ptr(p), _lib.ptr(r.grad),
+                  _lib.ptr(m), f, _lib.ptr(energy), sch(step),
+                  _noise(state.key, state.chain, buf), _lib.stream_handle())
       step += 1
-    _lib.call("gbsgmc_leapfrog_position", 1, P, _lib.ptr(x), _lib.ptr(p),
-              _lib.ptr(m), 0.5, sch(step), _lib.stream_handle())
+    position(0.5, step)
     return state._replace(potential=energy, data_state=data_state, step=step)
 
   def get_fn(state):

@@ -615,6 +615,51 @@ def reversible_leapfrog(x, p, grad_fn, xis, h, friction, mass=None):
   return x, p, energy
 
 
+def dense_leapfrog_position(x, p, h, scale, minv):
+  """x + (scale h) M^-1 p with a dense inverse mass (integrator.py:383-388
+  with tensor_matmul of an ndim-2 Tensor, util/tree_util.py:38-56); float64,
+  rows [C, P] of chains."""
+  x, p = np.asarray(x, np.float64), np.asarray(p, np.float64)
+  return x + float(scale) * float(h) * (p @ np.asarray(minv, np.float64).T)
+
+
+def dense_amagold_momentum(p, g, xi, h, friction, minv, msqrt):
+  """amagold_momentum with dense matrices (integrator.py:390-458): p' = ((1 -
+  h f) p - h g + sqrt(4 f h) M^1/2 xi) / (1 + h f), energy 0.5 h (p + p') .
+  M^-1 g per chain; float64.  Returns (p', energy [C])."""
+  p, g, xi = (np.asarray(a, np.float64) for a in (p, g, xi))
+  mi, ms = np.asarray(minv, np.float64), np.asarray(msqrt, np.float64)
+  h, f = float(h), float(friction)
+  pn = ((1 - h * f) * p - h * g + math.sqrt(4 * f * h) * (xi @ ms.T)) / (1 + h * f)
+  return pn, 0.5 * h * np.sum((p + pn) * (g @ mi.T), -1)
+
+
+def dense_obabo_first(x, p, g1, xi1, h, T, friction, minv, msqrt):
+  """obabo_first with dense matrices (integrator.py:177-241): O with
+  M^1/2 xi1, the kinetic energy 0.5 p . M^-1 p, B, A with M^-1 p; float64.
+  Returns (x', p', ke_start [C])."""
+  x, p, g1, xi1 = (np.asarray(a, np.float64) for a in (x, p, g1, xi1))
+  mi, ms = np.asarray(minv, np.float64), np.asarray(msqrt, np.float64)
+  h, T, f = float(h), float(T), float(friction)
+  perm = math.exp(-f * h)
+  p = math.sqrt(perm) * p + math.sqrt((1 - perm) * T) * (xi1 @ ms.T)
+  ke = 0.5 * np.sum(p * (p @ mi.T), -1)
+  p = p - 0.5 * h * g1
+  return x + h * (p @ mi.T), p, ke
+
+
+def dense_obabo_second(p, g2, xi2, h, T, friction, minv, msqrt):
+  """obabo_second with dense matrices (integrator.py:243-273): B, the
+  kinetic energy, O with M^1/2 xi2; float64.  Returns (p', ke_end [C])."""
+  p, g2, xi2 = (np.asarray(a, np.float64) for a in (p, g2, xi2))
+  mi, ms = np.asarray(minv, np.float64), np.asarray(msqrt, np.float64)
+  h, T, f = float(h), float(T), float(friction)
+  p = p - 0.5 * h * g2
+  ke = 0.5 * np.sum(p * (p @ mi.T), -1)
+  perm = math.exp(-f * h)
+  return math.sqrt(perm) * p + math.sqrt((1 - perm) * T) * (xi2 @ ms.T), ke
+
+
 def mh_log_alpha(kind, U_old, U_new, energy=0.0, ke_start=0.0, ke_end=0.0,
                  T=1.0):
   """The capped log acceptance of solver.amagold (kind 'amagold',
@@ -753,6 +798,36 @@ def mass_adapt_update(state: MassAdaption, sample, burn_in) -> MassAdaption:
   if it == burn_in:
     inv = (ssq / fi).astype(np.float32)
     sq = np.sqrt(fi / ssq).astype(np.float32)
+  return MassAdaption(it, mean, ssq, inv, sq)
+
+
+def dense_mass_adapt_init(sample, init_cov=None) -> MassAdaption:
+  """mass_matrix(diagonal=False) init (jax_sgmc/adaption.py:321-340): ssq
+  [P, P] zeros, inv = diag(init_cov), sqrt = diag(1 / sqrt(init_cov))."""
+  x = np.asarray(sample, np.float32).reshape(-1)
+  cov = np.ones_like(x) if init_cov is None else np.asarray(init_cov, np.float32)
+  return MassAdaption(0, np.zeros_like(x), np.zeros((x.size, x.size), np.float32),
+                      np.diag(cov), np.diag(np.float32(1) / np.sqrt(cov)))
+
+
+def dense_mass_adapt_update(state: MassAdaption, sample, burn_in) -> MassAdaption:
+  """One dense update (jax_sgmc/adaption.py:342-362): the mean as in
+  :func:`mass_adapt_update`, ssq += outer(x - mean, x - mean') (fp32), and
+  at iteration == burn_in (:309-317) inv = ssq / i and
+  sqrt = V^T diag(sqrt(w)) V with (w, V) = :func:`sym_eig` (inv) (float64,
+  the eigenvectors as V's columns; negative rounding of w counts as 0)."""
+  x = np.asarray(sample, np.float32).reshape(-1)
+  it = state.iteration + 1
+  fi = np.float32(it)
+  a = np.float32(it - 1) / fi
+  b = np.float32(1) / fi
+  mean = (a * state.mean + b * x).astype(np.float32)
+  ssq = (state.ssq + np.outer(x - state.mean, x - mean)).astype(np.float32)
+  inv, sq = state.inv, state.sqrt
+  if it == burn_in:
+    inv = (ssq / fi).astype(np.float32)
+    w, V = sym_eig(inv)
+    sq = V.T @ np.diag(np.sqrt(np.maximum(w, 0.0))) @ V
   return MassAdaption(it, mean, ssq, inv, sq)
 
 

@@ -358,3 +358,46 @@ def test_sym_eig_convention_and_dense_fisher_restatement():
   lam2, U2 = O.sym_eig(2.0 * np.eye(d) - b)
   np.testing.assert_allclose(np.sort(lam2), np.sort(2.0 - lam), rtol=1e-10)
   np.testing.assert_allclose(cb, U2 @ np.sqrt(np.abs(lam2)), rtol=1e-9)
+
+
+def test_dense_mass_oracle_reduces_to_the_diagonal_one():
+  """With diagonal matrices diag(1/m) and diag(sqrt m) the dense restatements
+  are the diagonal ones; the dense adaption's mean, diagonal of ssq and
+  inverse mass are the diagonal adaption's, and its root after burn-in is
+  V^T diag(sqrt w) V of the sample covariance (for a diagonal covariance
+  with distinct entries: diag(sqrt of the variances))."""
+  rng = np.random.default_rng(0)
+  P, C = 5, 2
+  x, p, g, xi, xi2 = (rng.normal(size=(C, P)).astype(np.float32) for _ in range(5))
+  m = rng.uniform(0.5, 2.0, size=P).astype(np.float32)
+  minv = np.diag(1.0 / m.astype(np.float64))
+  msq = np.diag(np.sqrt(m.astype(np.float64)))
+  np.testing.assert_allclose(O.dense_leapfrog_position(x, p, 0.1, 0.5, minv),
+                             O.leapfrog_position(x, p, 0.1, 0.5, m), rtol=1e-6)
+  pn, e = O.dense_amagold_momentum(p, g, xi, 0.1, 0.3, minv, msq)
+  for c in range(C):
+    pw, ew = O.amagold_momentum(p[c], g[c], xi[c], 0.1, 0.3, m)
+    np.testing.assert_allclose(pn[c], pw, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(e[c], ew, rtol=1e-5)
+  xd, pd, k0 = O.dense_obabo_first(x, p, g, xi, 0.1, 0.9, 0.4, minv, msq)
+  xw, pw, kw = O.obabo_first(x, p, g, xi, 0.1, 0.9, 0.4, m)
+  np.testing.assert_allclose(xd, xw, rtol=1e-5, atol=1e-6)
+  np.testing.assert_allclose(pd, pw, rtol=1e-5, atol=1e-6)
+  np.testing.assert_allclose(k0, kw, rtol=1e-5)
+  pd2, k1 = O.dense_obabo_second(pd, g, xi2, 0.1, 0.9, 0.4, minv, msq)
+  pw2, kw1 = O.obabo_second(pw, g, xi2, 0.1, 0.9, 0.4, m)
+  np.testing.assert_allclose(pd2, pw2, rtol=1e-5, atol=1e-6)
+  np.testing.assert_allclose(k1, kw1, rtol=1e-5)
+  # Adaption: samples with independent coordinates of distinct scales.
+  xs = (rng.normal(size=(400, 3)) * np.array([0.5, 1.0, 2.0])).astype(np.float32)
+  dn, dg = O.dense_mass_adapt_init(xs[0]), O.mass_adapt_init(xs[0])
+  for s in xs:
+    dn = O.dense_mass_adapt_update(dn, s, 400)
+    dg = O.mass_adapt_update(dg, s, 400)
+  np.testing.assert_array_equal(dn.mean, dg.mean)
+  np.testing.assert_allclose(np.diag(dn.ssq), dg.ssq, rtol=1e-6)
+  np.testing.assert_allclose(np.diag(dn.inv), dg.inv, rtol=1e-6)
+  # The scales are in ascending order, so V is close to the identity and
+  # the root close to diag(0.5, 1, 2).
+  np.testing.assert_allclose(np.diag(dn.sqrt), [0.5, 1.0, 2.0], rtol=0.15)
+  assert np.max(np.abs(dn.sqrt - np.diag(np.diag(dn.sqrt)))) < 0.2
