@@ -575,6 +575,29 @@ int gbsgmc_mlp_value_and_grad_ragged(const gbsgmc_mlp* model, int chains,
                                      void* workspace_dev, size_t workspace_bytes,
                                      int* status_dev, gbsgmc_stream_t stream);
 
+/* The empirical-Fisher noise model of fisher_information(diagonal=True)
+ * (jax_sgmc/adaption.py:371-457) on the MLP likelihood, per chain: with
+ * G = grad_dev (dU/dw at w) and the per-observation gradients d_i of the
+ * likelihoods lk_i of the n rows idx,
+ *   ssq = sum_i (d_i - G / N)^2 = S2 - 2 (G / N) S1 + n (G / N)^2,
+ *   S1 = sum_i d_i, S2 = sum_i d_i^2 (clamped at 0 against rounding),
+ *   b = 0.5 step_size ssq / (n - 1), corr = friction - b, corr <= 0 replaced
+ *   by the chain's smallest positive corr; cb_diff_sqrt = sqrt(corr),
+ *   b_sqrt = sqrt(friction - corr)   (both [chains, P], both required).
+ * S1 comes from the adjoint GEMMs seeded with d lk_i / d out, S2 from GEMMs
+ * on the squared BF16 operands ((Z1^2)^T (G2^2), (G1^2)^T (X^2)) on the
+ * tcgen05 tensor cores.  friction_dev [P] or NULL (scalar friction).  n a
+ * positive multiple of 128; workspace gbsgmc_mlp_fisher_workspace_bytes. */
+size_t gbsgmc_mlp_fisher_workspace_bytes(const gbsgmc_mlp* model, int chains, int n);
+int gbsgmc_mlp_fisher_noise(const gbsgmc_mlp* model, int chains, int n,
+                            const int32_t* idx_dev, int64_t idx_stride,
+                            const float* w_dev, const float* grad_dev,
+                            const float* friction_dev, float friction,
+                            float step_size, float* cb_diff_sqrt_dev,
+                            float* b_sqrt_dev, void* workspace_dev,
+                            size_t workspace_bytes, int* status_dev,
+                            gbsgmc_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Convolutional classifier with a softmax likelihood (CNN)                  */
 /* ------------------------------------------------------------------------ */

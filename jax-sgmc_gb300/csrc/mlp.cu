@@ -31,8 +31,20 @@
 //   9 mlp_finalize_kernel db1, db2, dW3, db3 (with their prior terms), U and
 //                         var(lk)
 // Without a gradient only 1-5 and 9 run.
+//
+// The empirical-Fisher noise model (fisher_information(diagonal=True),
+// adaption.py:371-457) runs the same sequence with the adjoint seeded by
+// d lk_i / d out = (y - out) / sigma^2 (the likelihood's, unscaled), so that
+// the GEMMs sum the per-observation gradients d_i, and adds GEMMs on
+// squared operands for sum_i d_i^2: (Z1^2)^T (G2^2) after step 6 and
+// (G1^2)^T (Xb^2) after step 8 (the squares of the BF16 operands, rounded
+// to BF16 by mlp_square_kernel), the output layer's and the biases' sums of
+// squares in mlp_out_kernel and mlp_square_kernel.  Then
+//   ssq = sum_i (d_i - gbar)^2 = S2 - 2 gbar S1 + n gbar^2,  gbar = G / N
+// (clamped at 0 against rounding), and the reference's correction.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -133,10 +145,13 @@ struct MlpLayout {
   size_t yv, outp, pw3, pb2, pb1;   // fp32
   size_t psq, plk;                  // fp64
   size_t rag;                       // int tables of a ragged batch
+  // Fisher noise model only: squared operands (BF16), partial sums of
+  // squares (fp32), U and the smallest positive correction per chain.
+  size_t sqa, sqb, pw3sq, pb2sq, pb1sq, fU, fmin;
   size_t total;
 };
 
-MlpLayout mlp_layout(const MlpShape& s, int chains, int n) {
+MlpLayout mlp_layout(const MlpShape& s, int chains, int n, bool fisher = false) {
   MlpLayout L;
   size_t off = 0;
   auto take = [&](size_t bytes_per_chain) {
@@ -157,6 +172,16 @@ MlpLayout mlp_layout(const MlpShape& s, int chains, int n) {
   L.psq = take(8 * static_cast<size_t>(prep_blocks(s)));
   L.plk = take(8 * 4 * (N / kTile));
   L.rag = take(4 * 5);  // tile prefixes [C + 1] x 2, K slices [C]
+  L.sqa = L.sqb = L.pw3sq = L.pb2sq = L.pb1sq = L.fU = L.fmin = 0;
+  if (fisher) {
+    L.sqa = take(2 * N * H1);
+    L.sqb = take(2 * N * (H2 > D ? H2 : D));
+    L.pw3sq = take(4 * (N / kTile) * H2);
+    L.pb2sq = take(4 * (N / kTile) * H2);
+    L.pb1sq = take(4 * (N / kTile) * H1);
+    L.fU = take(8);
+    L.fmin = take(4);
+  }
   L.total = off;
   return L;
 }
@@ -182,6 +207,13 @@ struct MlpArgs {
   // (sq_count per chain in psq) are supplied, the prior's gradient is the
   // update's.
   int fused, sq_count;
+  // Fisher noise model: the adjoint is the likelihood's (grad receives
+  // sum_i d_i), grad_sq receives sum_i d_i^2.
+  int fisher;
+  float* grad_sq;
+  float *pw3sq, *pb2sq, *pb1sq;
+  bf16 *sqa, *sqb;
+  uint32_t* fmin;
   int *prefix1, *prefix2, *kblocks;
   // workspace views
   bf16 *wb, *xb, *z1, *z2g;
@@ -509,10 +541,12 @@ __global__ void __launch_bounds__(256) mlp_prior_kernel(const MlpArgs a, float p
 //    64 x H2 block of Z2 in 16-byte vectors, writes G2 over it and leaves
 //    per-block column sums for dW3 (sum_i g_i Z2_ij) and db2 (sum_i G2_ij).
 // ---------------------------------------------------------------------------
+template <bool kFisher>
 __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
+  constexpr int kParts = kFisher ? 4 : 2;
   __shared__ float g_s[kTile];
   __shared__ double red[2][4];
-  __shared__ float colp[2][256 * 8];
+  __shared__ float colp[kParts][256 * 8];
   const MlpShape& s = a.s;
   const int c = blockIdx.y, rb = blockIdx.x, i0 = rb * kTile;
   const int t = threadIdx.x, lane = t & 31;
@@ -535,12 +569,15 @@ __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
     const float m = !live ? 0.f
                     : a.mask != nullptr ? __ldg(a.mask + static_cast<int64_t>(c) * a.n + i)
                                         : 1.f;
-    const float g = -scale * m * r * inv_s2;
+    // The Fisher model differentiates lk_i itself: d lk_i / d out = r / s^2.
+    const float g = kFisher ? (live ? r * inv_s2 : 0.f) : -scale * m * r * inv_s2;
     g_s[t] = g;
     if (a.lk != nullptr) a.lk[static_cast<int64_t>(c) * a.n + i] = live ? lk : 0.f;
     // var(lk) is over all n values, masked or not (jnp.var, integrator.py:880).
     const double lkl = live ? lk : 0.0;
-    double v4[4] = {static_cast<double>(m) * lkl, lkl, lkl * lkl, g};
+    // Slot 0 is sum_i g_i^2 (b3's sum of squares) in the Fisher model.
+    double v4[4] = {kFisher ? static_cast<double>(g) * g : static_cast<double>(m) * lkl, lkl,
+                    lkl * lkl, g};
 #pragma unroll
     for (int k = 0; k < 4; ++k) v4[k] = warp_sum(v4[k]);
     if (lane == 0)
@@ -561,12 +598,14 @@ __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
   for (int base = 0; base < cpr; base += CT) {
     const int ch = base + ct;
     const bool active = ch < cpr;
-    float w3[8], aw[8], ab[8];
+    float w3[8], aw[8], ab[8], aw2[8], ab2[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       w3[k] = active ? __ldg(w + s.oW3 + 8 * ch + k) : 0.f;
       aw[k] = 0.f;
       ab[k] = 0.f;
+      aw2[k] = 0.f;
+      ab2[k] = 0.f;
     }
     for (int r0 = rg; active && r0 < kTile; r0 += 8 * RG) {
       uint4 cell[8];
@@ -589,6 +628,13 @@ __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
           aw[2 * h + 1] = fmaf(g, zb, aw[2 * h + 1]);
           ab[2 * h] += ga;
           ab[2 * h + 1] += gb;
+          if (kFisher) {
+            const float da = g * za, db = g * zb;
+            aw2[2 * h] = fmaf(da, da, aw2[2 * h]);
+            aw2[2 * h + 1] = fmaf(db, db, aw2[2 * h + 1]);
+            ab2[2 * h] = fmaf(ga, ga, ab2[2 * h]);
+            ab2[2 * h + 1] = fmaf(gb, gb, ab2[2 * h + 1]);
+          }
           u[h] = pack_bf16x2(ga, gb);
         }
         z2[static_cast<int64_t>(r) * cpr + ch] = cell[k];
@@ -600,19 +646,31 @@ __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
     for (int k = 0; k < 8; ++k) {
       colp[0][t * 8 + k] = aw[k];
       colp[1][t * 8 + k] = ab[k];
+      if (kFisher) {
+        colp[kParts - 2][t * 8 + k] = aw2[k];
+        colp[kParts - 1][t * 8 + k] = ab2[k];
+      }
     }
     __syncthreads();
     if (rg == 0 && active) {
       const int64_t pr = (static_cast<int64_t>(c) * (a.n / kTile) + rb) * s.H2 + 8 * ch;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        float sw = 0.f, sb = 0.f;
+        float sw = 0.f, sb = 0.f, sw2 = 0.f, sb2 = 0.f;
         for (int q = 0; q < RG; ++q) {
           sw += colp[0][(q * CT + ct) * 8 + k];
           sb += colp[1][(q * CT + ct) * 8 + k];
+          if (kFisher) {
+            sw2 += colp[kParts - 2][(q * CT + ct) * 8 + k];
+            sb2 += colp[kParts - 1][(q * CT + ct) * 8 + k];
+          }
         }
         a.pw3[pr + k] = sw;
         a.pb2[pr + k] = sb;
+        if (kFisher) {
+          a.pw3sq[pr + k] = sw2;
+          a.pb2sq[pr + k] = sb2;
+        }
       }
     }
   }
@@ -628,7 +686,7 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
   const int c = blockIdx.y, t = threadIdx.x;
   const float* w = a.w + static_cast<int64_t>(c) * s.P;
   const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;
-  const float pf = a.prior_scale > 0.f && !a.fused
+  const float pf = a.prior_scale > 0.f && !a.fused && !a.fisher
                        ? static_cast<float>(1.0 / (s2 * a.temperature))
                        : 0.f;
   const int nc = chain_rows(a, c), npad = chain_rows_padded(a, c);
@@ -641,6 +699,12 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
       float acc = 0.f;
       for (int r = 0; r < nb32; ++r) acc += p[static_cast<int64_t>(r) * s.H1];
       g[s.ob1 + j] = fmaf(pf, __ldg(w + s.ob1 + j), acc);
+      if (a.fisher) {
+        const float* q = a.pb1sq + static_cast<int64_t>(c) * (a.n / kTile) * s.H1 + j;
+        float sq = 0.f;
+        for (int r = 0; r < nb64; ++r) sq += q[static_cast<int64_t>(r) * s.H1];
+        a.grad_sq[static_cast<int64_t>(c) * s.P + s.ob1 + j] = sq;
+      }
     }
     if (j < s.H2) {
       const int64_t base = static_cast<int64_t>(c) * (a.n / kTile) * s.H2 + j;
@@ -651,6 +715,15 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
       }
       g[s.ob2 + j] = fmaf(pf, __ldg(w + s.ob2 + j), acc2);
       g[s.oW3 + j] = fmaf(pf, __ldg(w + s.oW3 + j), acc3);
+      if (a.fisher) {
+        float sq2 = 0.f, sq3 = 0.f;
+        for (int r = 0; r < nb64; ++r) {
+          sq2 += a.pb2sq[base + static_cast<int64_t>(r) * s.H2];
+          sq3 += a.pw3sq[base + static_cast<int64_t>(r) * s.H2];
+        }
+        a.grad_sq[static_cast<int64_t>(c) * s.P + s.ob2 + j] = sq2;
+        a.grad_sq[static_cast<int64_t>(c) * s.P + s.oW3 + j] = sq3;
+      }
     }
   }
   if (blockIdx.x != 0) return;
@@ -669,6 +742,13 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
   l2 = block_sum(l2, red);
   gs = block_sum(gs, red);
   if (t != 0) return;
+  if (a.fisher) {
+    // b3: sum_i g_i and sum_i g_i^2; the correction's minimum starts at +inf.
+    a.grad[static_cast<int64_t>(c) * s.P + s.ob3] = static_cast<float>(gs);
+    a.grad_sq[static_cast<int64_t>(c) * s.P + s.ob3] = static_cast<float>(lm);
+    a.fmin[c] = 0x7f800000u;
+    return;
+  }
   double log_prior = 0.0;
   if (a.prior_scale > 0.f)
     log_prior = -0.5 * sq / s2 -
@@ -686,6 +766,97 @@ __global__ void __launch_bounds__(256) mlp_finalize_kernel(const MlpArgs a, int 
   if (a.want_grad)
     a.grad[static_cast<int64_t>(c) * s.P + s.ob3] =
         static_cast<float>(gs) + pf * __ldg(w + s.ob3);
+}
+
+// Squares of a BF16 matrix [n, H] per chain (blockIdx.z), rounded to BF16,
+// and with `colsq` the fp32 column sums of the squares of each 64-row block
+// -> colsq [chains, n / 64, H].  Grid (n / 64, H / 64, chains).
+__global__ void __launch_bounds__(256) mlp_square_kernel(const bf16* __restrict__ src,
+                                                         bf16* __restrict__ dst, int n, int H,
+                                                         float* colsq) {
+  __shared__ float part[32][65];
+  const int t = threadIdx.x, cc = t & 7, rg = t >> 3;
+  const int64_t base = static_cast<int64_t>(blockIdx.z) * n * H;
+  const int r0 = blockIdx.x * kTile, col = blockIdx.y * 64 + 8 * cc;
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int64_t e = base + static_cast<int64_t>(r0 + rg + 32 * k) * H + col;
+    uint4 v = *reinterpret_cast<const uint4*>(src + e);
+    uint32_t* u = reinterpret_cast<uint32_t*>(&v);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      float x0, x1;
+      unpack_bf16x2(u[h], x0, x1);
+      const float q0 = x0 * x0, q1 = x1 * x1;  // exact: 8-bit significands
+      acc[2 * h] += q0;
+      acc[2 * h + 1] += q1;
+      u[h] = pack_bf16x2(q0, q1);
+    }
+    *reinterpret_cast<uint4*>(dst + e) = v;
+  }
+  if (colsq == nullptr) return;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) part[rg][8 * cc + k] = acc[k];
+  __syncthreads();
+  if (t < 64) {
+    float sum = 0.f;
+    for (int r = 0; r < 32; ++r) sum += part[r][t];
+    colsq[(static_cast<int64_t>(blockIdx.z) * (n / kTile) + blockIdx.x) * H + blockIdx.y * 64 + t] =
+        sum;
+  }
+}
+
+// Fisher noise, first pass: with S1 = sum_i d_i (in bs) and S2 = sum_i d_i^2
+// (in cb), corr = friction - 0.5 h max(S2 - 2 gbar S1 + n gbar^2, 0) / (n - 1)
+// is written over S2 and the chain's smallest positive corr is kept in
+// fmin (as its bit pattern: positive floats order like their bits).  Grid
+// (blocks over P, chains).
+__global__ void __launch_bounds__(256) mlp_fisher_corr_kernel(
+    int64_t P, int n, float n_obs, float h, const float* __restrict__ grad,
+    const float* __restrict__ fric, float friction, const float* __restrict__ s1, float* s2,
+    uint32_t* fmin) {
+  __shared__ float red[8];
+  const int c = blockIdx.y;
+  const float scale_v = 1.0f / static_cast<float>(n - 1);
+  const float nf = static_cast<float>(n);
+  float m = INFINITY;
+  for (int64_t p = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x; p < P;
+       p += static_cast<int64_t>(gridDim.x) * 256) {
+    const int64_t e = static_cast<int64_t>(c) * P + p;
+    const float gbar = grad[e] / n_obs;
+    const float ssq = fmaxf(fmaf(nf * gbar, gbar, fmaf(-2.0f * gbar, s1[e], s2[e])), 0.f);
+    const float b = 0.5f * h * (scale_v * ssq);
+    const float corr = (fric != nullptr ? fric[p] : friction) - b;
+    s2[e] = corr;
+    if (corr > 0.f) m = fminf(m, corr);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) m = fminf(m, red[w]);
+    if (m < INFINITY) atomicMin(fmin + c, __float_as_uint(m));
+  }
+}
+
+// Second pass: corr <= 0 -> the smallest positive corr (+inf when none, as
+// jnp.min over an all-inf array gives); cb = sqrt(corr), bs = sqrt(f - corr).
+__global__ void __launch_bounds__(256) mlp_fisher_apply_kernel(int64_t P,
+                                                               const float* __restrict__ fric,
+                                                               float friction,
+                                                               const uint32_t* __restrict__ fmin,
+                                                               float* cb, float* bs) {
+  const int c = blockIdx.y;
+  const float smallest = __uint_as_float(fmin[c]);
+  for (int64_t p = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x; p < P;
+       p += static_cast<int64_t>(gridDim.x) * 256) {
+    const int64_t e = static_cast<int64_t>(c) * P + p;
+    const float corr = cb[e];
+    const float pc = corr <= 0.f ? smallest : corr;
+    cb[e] = sqrtf(pc);
+    bs[e] = sqrtf((fric != nullptr ? fric[p] : friction) - pc);
+  }
 }
 
 }  // namespace
@@ -733,6 +904,14 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   a.pb1 = view<float>(ws, L.pb1);
   if (!a.fused) a.psq = view<double>(ws, L.psq);
   a.plk = view<double>(ws, L.plk);
+  if (a.fisher) {
+    a.sqa = view<bf16>(ws, L.sqa);
+    a.sqb = view<bf16>(ws, L.sqb);
+    a.pw3sq = view<float>(ws, L.pw3sq);
+    a.pb2sq = view<float>(ws, L.pb2sq);
+    a.pb1sq = view<float>(ws, L.pb1sq);
+    a.fmin = view<uint32_t>(ws, L.fmin);
+  }
   a.prefix1 = view<int>(ws, L.rag);
   a.prefix2 = a.prefix1 + (a.chains + 1);
   a.kblocks = a.prefix2 + (a.chains + 1);
@@ -778,7 +957,10 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   if ((rc = launch_gemm<kBN, false, true>(m_z1, m_w2, C, n, H2, H1, a.status, e2, st, rows_h2)))
     return rc;
 
-  mlp_out_kernel<<<dim3(n / kTile, C), 256, 0, st>>>(a);
+  if (a.fisher)
+    mlp_out_kernel<true><<<dim3(n / kTile, C), 256, 0, st>>>(a);
+  else
+    mlp_out_kernel<false><<<dim3(n / kTile, C), 256, 0, st>>>(a);
   if ((rc = check_launch("mlp_out_kernel")) != GBSGMC_OK) return rc;
 
   if (a.want_grad) {
@@ -796,6 +978,20 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     const EpiGradRows e6{a.grad, s.P, s.oW2, H2};
     if ((rc = launch_gemm<kBN, true, true>(m_z1mn, m_g2mn, C, H1, H2, n, a.status, e6, st, ksl)))
       return rc;
+    if (a.fisher) {
+      // 6b: sum_i d_i^2 of W2 = (Z1^2)^T (G2^2).
+      mlp_square_kernel<<<dim3(n / kTile, H1 / 64, C), 256, 0, st>>>(a.z1, a.sqa, n, H1, nullptr);
+      if ((rc = check_launch("mlp_square_kernel")) != GBSGMC_OK) return rc;
+      mlp_square_kernel<<<dim3(n / kTile, H2 / 64, C), 256, 0, st>>>(a.z2g, a.sqb, n, H2, nullptr);
+      if ((rc = check_launch("mlp_square_kernel")) != GBSGMC_OK) return rc;
+      CUtensorMap m_qa, m_qb;
+      if ((rc = make_tmap_bf16_3d(&m_qa, a.sqa, H1, n, C, H1, s1, 64, 64)) ||
+          (rc = make_tmap_bf16_3d(&m_qb, a.sqb, H2, n, C, H2, s2, 64, 64)))
+        return rc;
+      const EpiGradRows e6q{a.grad_sq, s.P, s.oW2, H2};
+      if ((rc = launch_gemm<kBN, true, true>(m_qa, m_qb, C, H1, H2, n, a.status, e6q, st, ksl)))
+        return rc;
+    }
     // 7: G1 = (G2 W2^T) * (1 - Z1^2); W2 [H1, H2] is the K-major B operand.
     const EpiAdjoint1 e7{a.z1, a.pb1, H1, n};
     if ((rc = launch_gemm<kBN, false, false>(m_g2, m_w2k, C, n, H1, H2, a.status, e7, st,
@@ -806,7 +1002,21 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     const EpiGradCols e8{a.grad, s.P, s.oW1, H1};
     if ((rc = launch_gemm<64, true, true>(m_z1mn, m_xbmn, C, H1, D, n, a.status, e8, st, ksl)))
       return rc;
-    if (pf != 0.f && !a.fused) {
+    if (a.fisher) {
+      // 8b: sum_i d_i^2 of W1 = (G1^2)^T (Xb^2), and b1's sums of squares.
+      mlp_square_kernel<<<dim3(n / kTile, H1 / 64, C), 256, 0, st>>>(a.z1, a.sqa, n, H1, a.pb1sq);
+      if ((rc = check_launch("mlp_square_kernel")) != GBSGMC_OK) return rc;
+      mlp_square_kernel<<<dim3(n / kTile, D / 64, C), 256, 0, st>>>(a.xb, a.sqb, n, D, nullptr);
+      if ((rc = check_launch("mlp_square_kernel")) != GBSGMC_OK) return rc;
+      CUtensorMap m_qa, m_qx;
+      if ((rc = make_tmap_bf16_3d(&m_qa, a.sqa, H1, n, C, H1, s1, 64, 64)) ||
+          (rc = make_tmap_bf16_3d(&m_qx, a.sqb, D, n, C, D, sx, 64, 64)))
+        return rc;
+      const EpiGradCols e8q{a.grad_sq, s.P, s.oW1, H1};
+      if ((rc = launch_gemm<64, true, true>(m_qa, m_qx, C, H1, D, n, a.status, e8q, st, ksl)))
+        return rc;
+    }
+    if (pf != 0.f && !a.fused && !a.fisher) {
       mlp_prior_kernel<<<dim3(prep_blocks(s) - 1, C), 256, 0, st>>>(a, pf);
       if ((rc = check_launch("mlp_prior_kernel")) != GBSGMC_OK) return rc;
     }
@@ -941,4 +1151,73 @@ extern "C" int gbsgmc_mlp_value_and_grad_ragged(
   return mlp_call(model, chains, n_max, n_dev, idx_dev, idx_stride, mask_dev, w_dev, U_dev,
                   grad_dev, lk_dev, lk_var_dev, workspace_dev, workspace_bytes, status_dev,
                   stream);
+}
+
+extern "C" size_t gbsgmc_mlp_fisher_workspace_bytes(const gbsgmc_mlp* model, int chains, int n) {
+  if (model == nullptr || chains <= 0 || n <= 0 || n % 128 != 0 ||
+      model->d_in % 64 != 0 || model->h1 % 256 != 0 || model->h2 % 256 != 0)
+    return 0;
+  return mlp_layout(mlp_shape(model->d_in, model->h1, model->h2), chains, n, true).total;
+}
+
+extern "C" int gbsgmc_mlp_fisher_noise(const gbsgmc_mlp* model, int chains, int n,
+                                       const int32_t* idx_dev, int64_t idx_stride,
+                                       const float* w_dev, const float* grad_dev,
+                                       const float* friction_dev, float friction,
+                                       float step_size, float* cb_diff_sqrt_dev,
+                                       float* b_sqrt_dev, void* workspace_dev,
+                                       size_t workspace_bytes, int* status_dev,
+                                       gbsgmc_stream_t stream) {
+  int rc = check_model(model, "mlp_fisher_noise");
+  if (rc != GBSGMC_OK) return rc;
+  if (chains < 0) return set_error(GBSGMC_ERR_ARG, "mlp_fisher_noise: negative size");
+  if (chains == 0) return GBSGMC_OK;
+  if (n <= 0 || n % 128 != 0 || chains > 65535 || n > (1 << 24))
+    return set_error(GBSGMC_ERR_SHAPE,
+                     "mlp_fisher_noise: n must be a positive multiple of 128 (got %d), "
+                     "chains <= 65535", n);
+  if (idx_dev == nullptr || w_dev == nullptr || grad_dev == nullptr ||
+      cb_diff_sqrt_dev == nullptr || b_sqrt_dev == nullptr || workspace_dev == nullptr ||
+      status_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "mlp_fisher_noise: null pointer");
+  if (idx_stride < n) return set_error(GBSGMC_ERR_ARG, "mlp_fisher_noise: idx_stride < n");
+  if (reinterpret_cast<uintptr_t>(workspace_dev) % 256 != 0)
+    return set_error(GBSGMC_ERR_ARG, "mlp_fisher_noise: workspace must be 256-byte aligned");
+  const MlpShape s = mlp_shape(model->d_in, model->h1, model->h2);
+  const MlpLayout L = mlp_layout(s, chains, n, true);
+  if (workspace_bytes < L.total)
+    return set_error(GBSGMC_ERR_ARG, "mlp_fisher_noise: workspace of %zu bytes, need %zu",
+                     workspace_bytes, L.total);
+  MlpArgs a{};
+  a.s = s;
+  a.chains = chains;
+  a.n = n;
+  a.y_inline = model->y_inline ? 1 : 0;
+  a.want_grad = 1;
+  a.n_obs = model->n_obs;
+  a.n_rows = model->n_rows > 0 ? model->n_rows : model->n_obs;
+  a.ld = model->ld;
+  a.idx_stride = idx_stride;
+  a.X = model->X;
+  a.y = model->y;
+  a.idx = idx_dev;
+  a.w = w_dev;
+  a.sigma = model->sigma;
+  a.prior_scale = model->prior_scale;
+  a.temperature = model->temperature;
+  a.U = view<double>(workspace_dev, L.fU);
+  a.status = status_dev;
+  a.fisher = 1;
+  a.grad = b_sqrt_dev;           // S1, then b_sqrt
+  a.grad_sq = cb_diff_sqrt_dev;  // S2, then corr, then cb_diff_sqrt
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if ((rc = run_mlp(a, L, workspace_dev, st)) != GBSGMC_OK) return rc;
+  const int gx = static_cast<int>(std::min<int64_t>((s.P + 1023) / 1024, 1024));
+  mlp_fisher_corr_kernel<<<dim3(gx, chains), 256, 0, st>>>(
+      s.P, n, static_cast<float>(model->n_obs), step_size, grad_dev, friction_dev, friction,
+      b_sqrt_dev, cb_diff_sqrt_dev, a.fmin);
+  if ((rc = check_launch("mlp_fisher_corr_kernel")) != GBSGMC_OK) return rc;
+  mlp_fisher_apply_kernel<<<dim3(gx, chains), 256, 0, st>>>(s.P, friction_dev, friction, a.fmin,
+                                                            cb_diff_sqrt_dev, b_sqrt_dev);
+  return check_launch("mlp_fisher_apply_kernel");
 }

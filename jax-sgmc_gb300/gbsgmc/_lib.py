@@ -136,6 +136,9 @@ SIGNATURES = {
     "gbsgmc_mlp_value_and_grad_ragged": (_i, [_P(Mlp), _i, _i, _vp, _vp, _i64,
                                               _vp, _vp, _vp, _vp, _vp, _vp,
                                               _vp, _sz, _vp, _vp]),
+    "gbsgmc_mlp_fisher_workspace_bytes": (_sz, [_P(Mlp), _i, _i]),
+    "gbsgmc_mlp_fisher_noise": (_i, [_P(Mlp), _i, _i, _vp, _i64, _vp, _vp, _vp,
+                                     _f, _f, _vp, _vp, _vp, _sz, _vp, _vp]),
     "gbsgmc_cnn_param_count": (_i64, []),
     "gbsgmc_cnn_workspace_bytes": (_sz, [_i, _i]),
     "gbsgmc_cnn_value_and_grad": (_i, [_P(Cnn), _i, _i, _vp, _i64, _vp, _vp,

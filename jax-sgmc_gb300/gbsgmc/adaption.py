@@ -16,8 +16,10 @@ them into the parameter update (``gbsgmc_sgld_update``,
 (AMAGOLD, SGGMC) on the device with ``gbsgmc_mass_adapt``
 (adaption.py:296-368).  ``fisher_information(diagonal=True)`` is SGHMC's
 empirical-Fisher noise model (adaption.py:371-457) on the generalised-linear
-likelihoods (``gbsgmc_glm_fisher_noise``), and with ``diagonal=False`` its
-dense form for up to 128 parameters (``gbsgmc_glm_fisher_noise_dense``);
+likelihoods (``gbsgmc_glm_fisher_noise``) and the MLP
+(``gbsgmc_mlp_fisher_noise``), and with ``diagonal=False`` its dense form
+for up to 128 parameters of a generalised-linear likelihood
+(``gbsgmc_glm_fisher_noise_dense``);
 ``mass_matrix(diagonal=False)`` the dense mass for up to 128 parameters
 (``gbsgmc_mass_adapt_dense``, the dense integrator kernels).
 """
@@ -211,14 +213,19 @@ def fisher_information(minibatch_potential=None, diagonal=True) -> AdaptionStrat
   (adaption.py:371-457, after https://arxiv.org/abs/1206.6380).  Stateless:
   ``get(state, sample, sample_grad, friction, mini_batch=..., step_size=...)``
   returns the :class:`NoiseModel` of the current minibatch, computed on the
-  device from the per-observation likelihood gradients (the
-  generalised-linear families): elementwise (``diagonal=True``), or from
-  the d x d matrices (``diagonal=False``, d <= 128) through their
-  eigendecompositions (``gbsgmc_glm_fisher_noise_dense``)."""
+  device from the per-observation likelihood gradients: for the
+  generalised-linear families elementwise (``diagonal=True``) or from the
+  d x d matrices (``diagonal=False``, d <= 128) through their
+  eigendecompositions (``gbsgmc_glm_fisher_noise_dense``); for the MLP
+  elementwise, the sums of the gradients and of their squares from GEMMs
+  on the tensor cores (``gbsgmc_mlp_fisher_noise``)."""
   assert minibatch_potential, "Fisher information requires potential function."
-  if getattr(minibatch_potential, "is_network", False):
+  if getattr(minibatch_potential, "is_cnn", False):
     raise NotImplementedError("per-observation gradients are provided for the "
-                              "generalised-linear likelihoods")
+                              "generalised-linear and MLP likelihoods")
+  if getattr(minibatch_potential, "is_mlp", False) and not diagonal:
+    raise NotImplementedError("the dense Fisher noise model is built for the "
+                              "generalised-linear likelihoods (d <= 128)")
   pot = minibatch_potential
 
   def init(*args, **kwargs):
@@ -248,6 +255,15 @@ def fisher_information(minibatch_potential=None, diagonal=True) -> AdaptionStrat
       fric, f = _flat_device(friction), 0.0
     cb = torch.empty(P, dtype=torch.float32, device="cuda")
     bs = torch.empty(P, dtype=torch.float32, device="cuda")
+    if pot.is_mlp:
+      n = idx.numel()
+      ws = pot.fisher_workspace(1, n, m)
+      _lib.call("gbsgmc_mlp_fisher_noise", m, 1, n, _lib.ptr(idx), n,
+                _lib.ptr(x), _lib.ptr(g), _lib.ptr(fric), f, float(step_size),
+                _lib.ptr(cb), _lib.ptr(bs), _lib.ptr(ws), ws.numel(),
+                _lib.ptr(pot.status()), _lib.stream_handle())
+      del keep
+      return NoiseModel(cb_diff_sqrt=cb, b_sqrt=bs)
     _lib.call("gbsgmc_glm_fisher_noise" if diagonal else "gbsgmc_glm_fisher_noise_dense",
               m, 1, idx.numel(), _lib.ptr(idx),
               idx.numel(), _lib.ptr(x), _lib.ptr(g), _lib.ptr(fric), f,

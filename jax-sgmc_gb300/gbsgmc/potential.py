@@ -163,6 +163,21 @@ class StochasticPotential:
       self._ws[key] = ws
     return ws
 
+  def fisher_workspace(self, chains, n, model):
+    """Device workspace of gbsgmc_mlp_fisher_noise, cached per shape."""
+    import torch
+    key = ("fisher", chains, n)
+    ws = self._ws.get(key)
+    if ws is None:
+      nbytes = int(_lib.load().gbsgmc_mlp_fisher_workspace_bytes(model, chains, n))
+      if nbytes == 0:
+        raise _lib.GbsgmcError(_lib.ERR_SHAPE,
+                               f"MLP minibatch of {n} rows: needs a positive "
+                               "multiple of 128")
+      ws = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+      self._ws[key] = ws
+    return ws
+
   # -- batched evaluation --------------------------------------------------
   def evaluate(self, W, idx, dataset, mask=None, grad=True, lk=False,
                observation_count=None, model=None, rows=None):

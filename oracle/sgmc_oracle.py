@@ -236,18 +236,26 @@ def fisher_variance(w, X, y, idx, grad, n_obs, family, sigma):
   return 1.0 / (len(idx) - 1) * ssq
 
 
-def fisher_noise(w, X, y, idx, grad, n_obs, family, sigma, friction, step_size):
-  """fisher_information(diagonal=True).get (jax_sgmc/adaption.py:403-455),
-  float64, one chain: b = 0.5 h v (v from :func:`fisher_variance`),
+def fisher_noise_from_ssq(ssq, n, friction, step_size):
+  """The diagonal branch of fisher_information's get (jax_sgmc/adaption.py
+  432-445) from ssq [P] of one chain: v = ssq / (n - 1), b = 0.5 h v,
   corr = friction - b with corr <= 0 replaced by the smallest positive corr;
   returns (sqrt(corr), sqrt(friction - corr))."""
-  v = fisher_variance(w, X, y, idx, grad, n_obs, family, sigma)
-  b = 0.5 * step_size * v
+  b = 0.5 * step_size * (np.asarray(ssq, np.float64) / (n - 1))
   f = np.broadcast_to(np.asarray(friction, np.float64), b.shape)
   corr = f - b
   smallest = np.min(np.where(corr <= 0, np.inf, corr))
   pc = np.where(corr <= 0, smallest, corr)
   return np.sqrt(pc), np.sqrt(f - pc)
+
+
+def fisher_noise(w, X, y, idx, grad, n_obs, family, sigma, friction, step_size):
+  """fisher_information(diagonal=True).get (jax_sgmc/adaption.py:403-455),
+  float64, one chain: :func:`fisher_noise_from_ssq` of the ssq of
+  :func:`fisher_variance`."""
+  n = len(idx)
+  v = fisher_variance(w, X, y, idx, grad, n_obs, family, sigma)
+  return fisher_noise_from_ssq(v * (n - 1), n, friction, step_size)
 
 
 def sym_eig(A):
@@ -353,6 +361,55 @@ def mlp_potential(W, X, y, idx, n_obs, d_in, h1, h2, sigma, prior_scale=0.0,
       G1.sum(1), G2.sum(1), g.sum(1, keepdims=True)], axis=1)
   grad = grad - dlp / temperature
   return Potential(U, grad, lk, np.var(lk, axis=-1))
+
+
+def mlp_fisher_sums(W, X, y, idx, d_in, h1, h2, sigma):
+  """Sums over the minibatch of the per-observation likelihood gradients
+  d_i = d lk_i / d w and of their squares (S1, S2 [C, P]), float64: the
+  adjoint of mlp_potential seeded with d lk_i / d out = (y_i - out_i) /
+  sigma^2, and d_i^2 summed leaf by leaf (for W2: (Z1^2)^T (G2^2))."""
+  W = np.atleast_2d(np.asarray(W, np.float64))
+  idx = np.atleast_2d(np.asarray(idx))
+  C = W.shape[0]
+  _, W2, W3, _, _, _ = mlp_unravel(W, d_in, h1, h2)
+  Xb = np.asarray(X, np.float64)[idx][..., :d_in]
+  yb = np.asarray(y, np.float64)[idx]
+  out, Z1, Z2 = mlp_forward(W, Xb, d_in, h1, h2)
+  g = (yb - out) / sigma ** 2
+  G2 = g[..., None] * W3[:, None, :] * (1.0 - Z2 ** 2)
+  G1 = (G2 @ W2.transpose(0, 2, 1)) * (1.0 - Z1 ** 2)
+  tr = lambda a: a.transpose(0, 2, 1)
+  S1 = np.concatenate([(tr(Xb) @ G1).reshape(C, -1), (tr(Z1) @ G2).reshape(C, -1),
+                       (g[:, None, :] @ Z2)[:, 0, :], G1.sum(1), G2.sum(1),
+                       g.sum(1, keepdims=True)], axis=1)
+  S2 = np.concatenate([(tr(Xb ** 2) @ G1 ** 2).reshape(C, -1),
+                       (tr(Z1 ** 2) @ G2 ** 2).reshape(C, -1),
+                       ((g ** 2)[:, None, :] @ Z2 ** 2)[:, 0, :], (G1 ** 2).sum(1),
+                       (G2 ** 2).sum(1), (g ** 2).sum(1, keepdims=True)], axis=1)
+  return S1, S2
+
+
+def mlp_fisher_noise(W, X, y, idx, grad, n_obs, d_in, h1, h2, sigma, friction,
+                     step_size):
+  """fisher_information(diagonal=True).get (jax_sgmc/adaption.py:403-455) on
+  the tanh network, float64, C chains: ssq = sum_i (d_i - grad / N)^2 from
+  :func:`mlp_fisher_sums` as S2 - 2 gbar S1 + n gbar^2 (exact algebra; fp64
+  holds it without cancellation here), then the correction of
+  :func:`fisher_noise`.  Returns (cb_diff_sqrt, b_sqrt) [C, P]."""
+  S1, S2 = mlp_fisher_sums(W, X, y, idx, d_in, h1, h2, sigma)
+  n = np.atleast_2d(idx).shape[-1]
+  gbar = np.atleast_2d(np.asarray(grad, np.float64)) / n_obs
+  ssq = np.maximum(S2 - 2.0 * gbar * S1 + n * gbar ** 2, 0.0)
+  b = 0.5 * step_size * ssq / (n - 1)
+  f = np.broadcast_to(np.asarray(friction, np.float64), (b.shape[-1],))
+  corr = f - b
+  cb, bs = np.empty_like(b), np.empty_like(b)
+  for c in range(b.shape[0]):
+    pos = corr[c] > 0
+    smallest = np.min(corr[c][pos]) if pos.any() else np.inf
+    pc = np.where(corr[c] <= 0, smallest, corr[c])
+    cb[c], bs[c] = np.sqrt(pc), np.sqrt(f - pc)
+  return cb, bs
 
 
 # ---------------------------------------------------------------------------

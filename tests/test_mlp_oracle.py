@@ -79,3 +79,28 @@ def test_mlp_offsets_follow_sorted_ravel():
   assert P == 1_117_185
   assert offs == [0, 65536, 65536 + 1048576, 65536 + 1048576 + 1024,
                   65536 + 1048576 + 2048, 65536 + 1048576 + 3072]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_mlp_fisher_oracle_matches_per_observation_gradients(shape):
+  """mlp_fisher_sums and mlp_fisher_noise against per-observation gradients
+  taken one row at a time from mlp_potential (n = 1, N = 1, no prior: the
+  gradient is -d lk_i / d w), the reference's vmap over grad of
+  likelihoods[i] (adaption.py:420-437) written as a loop."""
+  D, H1, H2, n, C = shape
+  W, X, y, idx, _ = problem(D, H1, H2, n, C, seed=11)
+  sigma, N, h = 0.7, 500, 0.02
+  S1, S2 = O.mlp_fisher_sums(W, X, y, idx, D, H1, H2, sigma)
+  grad = O.mlp_potential(W, X, y, idx, N, D, H1, H2, sigma, prior_scale=2.0).grad
+  rng = np.random.default_rng(3)
+  friction = rng.uniform(0.5, 2.0, size=W.shape[1])
+  cb, bs = O.mlp_fisher_noise(W, X, y, idx, grad, N, D, H1, H2, sigma, friction, h)
+  for c in range(C):
+    d = np.stack([-O.mlp_potential(W[c:c + 1], X, y, idx[c:c + 1, i:i + 1], 1, D, H1, H2,
+                                   sigma).grad[0] for i in range(n)])
+    np.testing.assert_allclose(S1[c], d.sum(0), rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(S2[c], (d ** 2).sum(0), rtol=1e-10, atol=1e-12)
+    ssq = ((d - grad[c] / N) ** 2).sum(0)
+    wcb, wbs = O.fisher_noise_from_ssq(ssq, n, friction, h)
+    np.testing.assert_allclose(cb[c], wcb, rtol=1e-9)
+    np.testing.assert_allclose(bs[c], wbs, rtol=1e-9, atol=1e-12)
