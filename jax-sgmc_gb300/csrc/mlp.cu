@@ -27,7 +27,7 @@
 //   7 GEMM G2 . W2^T      epilogue *(1 - Z1^2) -> G1 in place of Z1,
 //                         partial db1
 //   8 GEMM G1^T . Xb      epilogue -> dW1 (written transposed)
-//   8b mlp_prior_kernel   dW1, dW2 += w / (s^2 T)
+//   (steps 6 and 8 add the prior's w / (s^2 T) in their epilogues)
 //   9 mlp_finalize_kernel db1, db2, dW3, db3 (with their prior terms), U and
 //                         var(lk)
 // Without a gradient only 1-5 and 9 run.
@@ -336,23 +336,34 @@ __global__ void __launch_bounds__(256) mlp_gather_kernel(const MlpArgs a) {
 
 // Bias + tanh over one 64-column block of the lane's row, packed to BF16
 // pairs: pk[j] holds columns 2j, 2j + 1 of the block.  With w3 the fp32 dot
-// product of the block with w3 is added to `dot`.
+// product of the block with w3 is added to `dot`.  The column vectors are
+// read once per 32 columns, lane l holding column l, and broadcast by
+// shuffles (a load per element kept the warps waiting on L1).
 template <class Load>
 __device__ __forceinline__ void tanh_block(const Load& load, int blk, const float* bias,
                                            uint32_t (&pk)[32], const float* w3, float& dot) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  float dot2 = 0.f;  // odd columns: two independent FMA chains
 #pragma unroll
   for (int half = 0; half < 2; ++half) {
+    const int k0 = 64 * blk + 32 * half;
+    const float bl = __ldg(bias + k0 + lane);
+    const float wl = w3 != nullptr ? __ldg(w3 + k0 + lane) : 0.f;
     float v[32];
     load(2 * blk + half, v);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const int k = 64 * blk + 32 * half + 2 * j;
-      const float z0 = tanh_approx(v[2 * j] + __ldg(bias + k));
-      const float z1 = tanh_approx(v[2 * j + 1] + __ldg(bias + k + 1));
-      if (w3 != nullptr) dot = fmaf(z0, __ldg(w3 + k), fmaf(z1, __ldg(w3 + k + 1), dot));
+      const float z0 = tanh_approx(v[2 * j] + __shfl_sync(full, bl, 2 * j));
+      const float z1 = tanh_approx(v[2 * j + 1] + __shfl_sync(full, bl, 2 * j + 1));
+      if (w3 != nullptr) {
+        dot = fmaf(z0, __shfl_sync(full, wl, 2 * j), dot);
+        dot2 = fmaf(z1, __shfl_sync(full, wl, 2 * j + 1), dot2);
+      }
       pk[16 * half + j] = pack_bf16x2(z0, z1);
     }
   }
+  dot += dot2;
 }
 
 // Writes the packed 64-column block of the warp's 32 rows, one 128-byte row
@@ -462,78 +473,82 @@ struct EpiAdjoint1 {
   }
 };
 
-// 6: likelihood gradient of a row-major weight matrix (GEMM row = matrix
-//    row), grad[b*P + off + row*ld + col]; the prior term is added by
-//    mlp_prior_kernel.
+// 6: gradient of a row-major weight matrix (GEMM row = matrix row),
+//    grad[b*P + off + row*ld + col] = acc + pf w at the same index (pf the
+//    prior's 1 / (s^2 T); 0 leaves the likelihood term alone and reads no w).
 struct EpiGradRows {
   float* grad;
   int64_t P, off, ld;
+  const float* w = nullptr;
+  float pf = 0.f;
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
-    float* dst = grad + b * P + off + row0 * ld + col0 + epi::lane_id();
+    const int64_t at = b * P + off + row0 * ld + col0 + epi::lane_id();
+    float* dst = grad + at;
+    const float* src = w + at;
 #pragma unroll 1
     for (int c = 0; c < NC / 32; ++c) {
+      // The prior's w of the 32 x 32 block (row r in wv[r], lane = column)
+      // is requested before the accumulator load, whose wait covers it.
+      float wv[32];
+      if (pf != 0.f) {
+#pragma unroll
+        for (int r = 0; r < 32; ++r) wv[r] = __ldg(src + r * ld + 32 * c);
+      }
       float v[32];
       uint32_t u[32];
       load(c, v);
 #pragma unroll
       for (int j = 0; j < 32; ++j) u[j] = __float_as_uint(v[j]);
       epi::put_rows(st, u);
+      if (pf != 0.f) {
+#pragma unroll
+        for (int r = 0; r < 32; ++r)
+          dst[r * ld + 32 * c] = fmaf(pf, wv[r], __uint_as_float(epi::get(st, r)));
+      } else {
 #pragma unroll 4
-      for (int r = 0; r < 32; ++r) dst[r * ld + 32 * c] = __uint_as_float(epi::get(st, r));
+        for (int r = 0; r < 32; ++r) dst[r * ld + 32 * c] = __uint_as_float(epi::get(st, r));
+      }
     }
   }
 };
 
-// 8: likelihood gradient of a matrix stored transposed to the GEMM (GEMM row
-//    = matrix column): grad[b*P + off + col*ld + row]; lanes hold consecutive
-//    rows, so each store is already one contiguous segment.
+// 8: gradient of a matrix stored transposed to the GEMM (GEMM row = matrix
+//    column): grad[b*P + off + col*ld + row] = acc + pf w; lanes hold
+//    consecutive rows, so each access is already one contiguous segment.
 struct EpiGradCols {
   float* grad;
   int64_t P, off, ld;
+  const float* w = nullptr;
+  float pf = 0.f;
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t*) const {
-    float* dst = grad + b * P + off + row0 + epi::lane_id();
+    const int64_t at = b * P + off + row0 + epi::lane_id();
+    float* dst = grad + at;
+    const float* src = w + at;
 #pragma unroll 1
     for (int c = 0; c < NC / 32; ++c) {
+      float wv[32];
+      if (pf != 0.f) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          wv[j] = __ldg(src + static_cast<int64_t>(col0 + 32 * c + j) * ld);
+      }
       float v[32];
       load(c, v);
+      if (pf != 0.f) {
 #pragma unroll
-      for (int j = 0; j < 32; ++j) dst[static_cast<int64_t>(col0 + 32 * c + j) * ld] = v[j];
+        for (int j = 0; j < 32; ++j)
+          dst[static_cast<int64_t>(col0 + 32 * c + j) * ld] = fmaf(pf, wv[j], v[j]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) dst[static_cast<int64_t>(col0 + 32 * c + j) * ld] = v[j];
+      }
     }
   }
 };
-
-// grad[W1 | W2] += w / (s^2 T) for every chain.  Grid (prep_blocks - 1,
-// chains); same element pairing as mlp_prep_kernel.
-__global__ void __launch_bounds__(256) mlp_prior_kernel(const MlpArgs a, float pf) {
-  const MlpShape& s = a.s;
-  const int c = blockIdx.y, t = threadIdx.x;
-  const int64_t pw = matrix_params(s);
-  const float* w = a.w + static_cast<int64_t>(c) * s.P;
-  float* g = a.grad + static_cast<int64_t>(c) * s.P;
-  const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kPrepPerBlock + 2 * t;
-  float v0[kPrepPairs], v1[kPrepPairs], g0[kPrepPairs], g1[kPrepPairs];
-#pragma unroll
-  for (int k = 0; k < kPrepPairs; ++k) {
-    const int64_t e = e0 + 512 * k;
-    const bool in = e < pw;
-    v0[k] = in ? __ldg(w + e) : 0.f;
-    v1[k] = in ? __ldg(w + e + 1) : 0.f;
-    g0[k] = in ? g[e] : 0.f;
-    g1[k] = in ? g[e + 1] : 0.f;
-  }
-#pragma unroll
-  for (int k = 0; k < kPrepPairs; ++k) {
-    const int64_t e = e0 + 512 * k;
-    if (e < pw) {
-      g[e] = fmaf(pf, v0[k], g0[k]);
-      g[e + 1] = fmaf(pf, v1[k], g1[k]);
-    }
-  }
-}
 
 // ---------------------------------------------------------------------------
 // 5. Output layer, likelihood and the first adjoint for 64 rows of a chain.
@@ -975,7 +990,11 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     const float pf = a.prior_scale > 0.f ? static_cast<float>(1.0 / (sc2 * a.temperature)) : 0.f;
     // 6: dW2 [H1, H2] = Z1^T G2 (both operands MN-major), before step 7
     //    overwrites Z1.
-    const EpiGradRows e6{a.grad, s.P, s.oW2, H2};
+    // The prior's term pf w of W1 and W2 is added in the gradient GEMMs'
+    // epilogues (not in the fused plans, whose update adds it, nor in the
+    // Fisher model, which differentiates the likelihood alone).
+    const float pf_epi = a.fused || a.fisher ? 0.f : pf;
+    const EpiGradRows e6{a.grad, s.P, s.oW2, H2, a.w, pf_epi};
     if ((rc = launch_gemm<kBN, true, true>(m_z1mn, m_g2mn, C, H1, H2, n, a.status, e6, st, ksl)))
       return rc;
     if (a.fisher) {
@@ -999,7 +1018,7 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
       return rc;
     // 8: dW1^T [H1, D] = G1^T Xb: GEMM row i (hidden unit), column f
     //    (feature) lands at dW1[f, i].
-    const EpiGradCols e8{a.grad, s.P, s.oW1, H1};
+    const EpiGradCols e8{a.grad, s.P, s.oW1, H1, a.w, pf_epi};
     if ((rc = launch_gemm<64, true, true>(m_z1mn, m_xbmn, C, H1, D, n, a.status, e8, st, ksl)))
       return rc;
     if (a.fisher) {
@@ -1015,10 +1034,6 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
       const EpiGradCols e8q{a.grad_sq, s.P, s.oW1, H1};
       if ((rc = launch_gemm<64, true, true>(m_qa, m_qx, C, H1, D, n, a.status, e8q, st, ksl)))
         return rc;
-    }
-    if (pf != 0.f && !a.fused && !a.fisher) {
-      mlp_prior_kernel<<<dim3(prep_blocks(s) - 1, C), 256, 0, st>>>(a, pf);
-      if ((rc = check_launch("mlp_prior_kernel")) != GBSGMC_OK) return rc;
     }
   }
   const int fx = a.want_grad ? ceil_div(H1 > H2 ? H1 : H2, 256) : 1;
