@@ -1257,6 +1257,59 @@ def run_mlp(args):
     }), flush=True)
 
 
+def run_gemm(args):
+  """The tcgen05 BF16 GEMM alone on the tanh network's hidden-layer shape,
+  64 x (2048 x 1024 x 1024), C fp32: the CTA-pair kernel and the single-CTA
+  kernel (GBSGMC_GEMM_PAIR=0) in the four operand layouts, and torch.bmm
+  (cuBLAS, BF16 output) beside them; CUDA events over `--steps` calls after
+  `--warmup`, one JSON line."""
+  import os
+  import torch
+  from gbsgmc import _lib
+  batch, M, N, K = 64, 2048, 1024, 1024
+  flop = 2.0 * batch * M * N * K
+  g = torch.Generator(device="cuda").manual_seed(5)
+  A = torch.randn((batch, M, K), generator=g, device="cuda").to(torch.bfloat16)
+  B = torch.randn((batch, N, K), generator=g, device="cuda").to(torch.bfloat16)
+  At, Bt = A.transpose(1, 2).contiguous(), B.transpose(1, 2).contiguous()
+  C = torch.empty((batch, M, N), device="cuda")
+  status = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+  def timed(fn):
+    for _ in range(args.warmup):
+      fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+      fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / args.steps
+
+  out = {}
+  for pair in ("1", "0"):
+    os.environ["GBSGMC_GEMM_PAIR"] = pair
+    for a_mn, b_mn in ((0, 0), (0, 1), (1, 0), (1, 1)):
+      Ap, Bp = (At if a_mn else A), (Bt if b_mn else B)
+
+      def call():
+        _lib.call("gbsgmc_gemm_bf16", a_mn, b_mn, Ap.data_ptr(), M if a_mn else K, M * K,
+                  Bp.data_ptr(), N if b_mn else K, N * K, C.data_ptr(), N, M * N, batch,
+                  M, N, K, status.data_ptr(), _lib.stream_handle())
+
+      ms = timed(call)
+      out[f"{'pair' if pair == '1' else 'single'}_{'mn' if a_mn else 'k'}{'mn' if b_mn else 'k'}"] = \
+          round(flop / (ms / 1e3) / 1e12, 1)
+  os.environ.pop("GBSGMC_GEMM_PAIR", None)
+  assert int(status.item()) == 0
+  ms = timed(lambda: torch.bmm(A, B.transpose(1, 2)))
+  out["torch_bmm_bf16_out"] = round(flop / (ms / 1e3) / 1e12, 1)
+  print(json.dumps({"metric": "bf16 GEMM throughput", "unit": "TFLOP/s",
+                    "shape": {"batch": batch, "M": M, "N": N, "K": K},
+                    "steps": args.steps, "warmup": args.warmup, "results": out}), flush=True)
+
+
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument("--gpus", type=int, default=1)
@@ -1264,16 +1317,19 @@ def main():
   ap.add_argument("--warmup", type=int, default=5)
   ap.add_argument("--impl", default="gbsgmc", choices=["gbsgmc", "reference"])
   ap.add_argument("--workload", default="logistic",
-                  choices=["logistic", "mlp", "resgld", "cnn"],
+                  choices=["logistic", "mlp", "resgld", "cnn", "gemm"],
                   help="logistic: 256-chain SGLD headline; mlp: 64-chain OBABO "
                        "on the tanh network; resgld: 32-replica exchange on it; "
-                       "cnn: 8-chain OBABO on the conv classifier")
+                       "cnn: 8-chain OBABO on the conv classifier; gemm: the "
+                       "tcgen05 GEMM alone on the network's hidden-layer shape")
   ap.add_argument("--kernel-only", action="store_true",
                   help="short run of the fused kernel for profilers; no JSON line")
   args = ap.parse_args()
   if args.warmup < 3:
     ap.error("--warmup must be at least 3")
-  if args.workload == "cnn":
+  if args.workload == "gemm":
+    run_gemm(args)
+  elif args.workload == "cnn":
     if args.impl == "reference":
       run_mlp_reference(args)
     elif args.kernel_only:

@@ -906,6 +906,18 @@ T* view(void* ws, size_t off) {
   return reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + off);
 }
 
+// A 256-wide GEMM of the network: on CTA pairs (tc_gemm2_kernel) for uniform
+// batches whose M is a multiple of 256, else on single CTAs.  tb_pair is the
+// B map for pairs (a K-major B is loaded in 128-row halves there).
+template <bool A_MN, bool B_MN, class Epi>
+int gemm256(const CUtensorMap& ta, const CUtensorMap& tb, const CUtensorMap& tb_pair, int C,
+            int M, int N, int K, int* status, const Epi& e, cudaStream_t st,
+            const GemmRagged& rg, bool uniform) {
+  if (uniform && M % 256 == 0 && gemm_pair_enabled())
+    return launch_gemm2<kBN, A_MN, B_MN>(ta, tb_pair, C, M, N, K, status, e, st);
+  return launch_gemm<kBN, A_MN, B_MN>(ta, tb, C, M, N, K, status, e, st, rg);
+}
+
 int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   const MlpShape& s = a.s;
   a.wb = view<bf16>(ws, L.wb);
@@ -963,13 +975,16 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
       (rc = make_tmap_bf16_3d(&m_z1, a.z1, H1, n, C, H1, s1, kGemmBK, kGemmBM)) ||
       (rc = make_tmap_bf16_3d(&m_w2, w2b, H2, H1, C, H2, pw, 64, 64)))
     return rc;
+  const bool uniform = a.n_true == nullptr;
   // 3: A1 = Xb W1 (W1 [D, H1] is the MN-major B operand).
   const EpiHidden1 e1{a.w, s.P, s.ob1, H1, n, a.z1};
-  if ((rc = launch_gemm<kBN, false, true>(m_xb, m_w1, C, n, H1, D, a.status, e1, st, rows_h1)))
+  if ((rc = gemm256<false, true>(m_xb, m_w1, m_w1, C, n, H1, D, a.status, e1, st, rows_h1,
+                                 uniform)))
     return rc;
   // 4: A2 = Z1 W2.
   const EpiHidden2 e2{a.w, s.P, s.ob2, s.oW3, H2, n, a.z2g, a.outp};
-  if ((rc = launch_gemm<kBN, false, true>(m_z1, m_w2, C, n, H2, H1, a.status, e2, st, rows_h2)))
+  if ((rc = gemm256<false, true>(m_z1, m_w2, m_w2, C, n, H2, H1, a.status, e2, st, rows_h2,
+                                 uniform)))
     return rc;
 
   if (a.fisher)
@@ -979,11 +994,12 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
   if ((rc = check_launch("mlp_out_kernel")) != GBSGMC_OK) return rc;
 
   if (a.want_grad) {
-    CUtensorMap m_z1mn, m_g2mn, m_g2, m_w2k, m_xbmn;
+    CUtensorMap m_z1mn, m_g2mn, m_g2, m_w2k, m_w2k_half, m_xbmn;
     if ((rc = make_tmap_bf16_3d(&m_z1mn, a.z1, H1, n, C, H1, s1, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_g2mn, a.z2g, H2, n, C, H2, s2, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_g2, a.z2g, H2, n, C, H2, s2, kGemmBK, kGemmBM)) ||
         (rc = make_tmap_bf16_3d(&m_w2k, w2b, H2, H1, C, H2, pw, kGemmBK, kBN)) ||
+        (rc = make_tmap_bf16_3d(&m_w2k_half, w2b, H2, H1, C, H2, pw, kGemmBK, kBN / 2)) ||
         (rc = make_tmap_bf16_3d(&m_xbmn, a.xb, D, n, C, D, sx, 64, 64)))
       return rc;
     const double sc2 = static_cast<double>(a.prior_scale) * a.prior_scale;
@@ -995,7 +1011,8 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     // Fisher model, which differentiates the likelihood alone).
     const float pf_epi = a.fused || a.fisher ? 0.f : pf;
     const EpiGradRows e6{a.grad, s.P, s.oW2, H2, a.w, pf_epi};
-    if ((rc = launch_gemm<kBN, true, true>(m_z1mn, m_g2mn, C, H1, H2, n, a.status, e6, st, ksl)))
+    if ((rc = gemm256<true, true>(m_z1mn, m_g2mn, m_g2mn, C, H1, H2, n, a.status, e6, st, ksl,
+                                  uniform)))
       return rc;
     if (a.fisher) {
       // 6b: sum_i d_i^2 of W2 = (Z1^2)^T (G2^2).
@@ -1008,13 +1025,14 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
           (rc = make_tmap_bf16_3d(&m_qb, a.sqb, H2, n, C, H2, s2, 64, 64)))
         return rc;
       const EpiGradRows e6q{a.grad_sq, s.P, s.oW2, H2};
-      if ((rc = launch_gemm<kBN, true, true>(m_qa, m_qb, C, H1, H2, n, a.status, e6q, st, ksl)))
+      if ((rc = gemm256<true, true>(m_qa, m_qb, m_qb, C, H1, H2, n, a.status, e6q, st, ksl,
+                                    uniform)))
         return rc;
     }
     // 7: G1 = (G2 W2^T) * (1 - Z1^2); W2 [H1, H2] is the K-major B operand.
     const EpiAdjoint1 e7{a.z1, a.pb1, H1, n};
-    if ((rc = launch_gemm<kBN, false, false>(m_g2, m_w2k, C, n, H1, H2, a.status, e7, st,
-                                             rows_h1)))
+    if ((rc = gemm256<false, false>(m_g2, m_w2k, m_w2k_half, C, n, H1, H2, a.status, e7, st,
+                                    rows_h1, uniform)))
       return rc;
     // 8: dW1^T [H1, D] = G1^T Xb: GEMM row i (hidden unit), column f
     //    (feature) lands at dW1[f, i].

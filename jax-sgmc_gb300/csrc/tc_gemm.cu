@@ -7,6 +7,8 @@
 // the tensor-map encoder and the plain fp32-output entry points.
 #include <cuda.h>
 
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -103,11 +105,32 @@ size_t gemm_smem_bytes(int bn) {
          static_cast<size_t>(kGemmEpiWarps) * kStageWords * 4 + (2 * kGemmStages + 5) * 8 + 16;
 }
 
+size_t gemm2_smem_bytes(int bn) {
+  return 1024 + static_cast<size_t>(kGemm2Stages) *
+                    (kGemmBM * kGemmBK * 2 + static_cast<size_t>(bn / 2) * kGemmBK * 2) +
+         static_cast<size_t>(kGemmEpiWarps) * kStageWords * 4 + (2 * kGemm2Stages + 5) * 8 + 16;
+}
+
+bool gemm_pair_enabled() {
+  const char* v = std::getenv("GBSGMC_GEMM_PAIR");
+  return v == nullptr || std::strcmp(v, "0") != 0;
+}
+
 }  // namespace gbsgmc
 
 using namespace gbsgmc;
 
 namespace {
+
+int dispatch_pair(bool a_mn, bool b_mn, const CUtensorMap& ta, const CUtensorMap& tb,
+                  int batch, int M, int N, int K, int* status, const StoreF32& epi,
+                  cudaStream_t st, uint64_t wait_ns) {
+  if (a_mn)
+    return b_mn ? launch_gemm2<256, true, true>(ta, tb, batch, M, N, K, status, epi, st, wait_ns)
+                : launch_gemm2<256, true, false>(ta, tb, batch, M, N, K, status, epi, st, wait_ns);
+  return b_mn ? launch_gemm2<256, false, true>(ta, tb, batch, M, N, K, status, epi, st, wait_ns)
+              : launch_gemm2<256, false, false>(ta, tb, batch, M, N, K, status, epi, st, wait_ns);
+}
 
 template <int BN>
 int dispatch_layout(bool a_mn, bool b_mn, const CUtensorMap& ta, const CUtensorMap& tb,
@@ -149,16 +172,21 @@ extern "C" int gbsgmc_gemm_bf16_wait_limit(
       reinterpret_cast<uintptr_t>(C_dev) % 16 != 0 || c_batch_stride % 4 != 0)
     return set_error(GBSGMC_ERR_ARG, "gemm_bf16: bad leading dimension");
   const int bn = N % 256 == 0 ? 256 : 128;
+  // CTA pairs for 256 x 256 tiles; a K-major B is then loaded in halves.
+  const bool pair = bn == 256 && M % 256 == 0 && gemm_pair_enabled();
   CUtensorMap ta, tb;
   int rc = a_mn ? make_tmap_bf16_3d(&ta, A_dev, M, K, batch, lda, a_batch_stride, 64, 64)
                 : make_tmap_bf16_3d(&ta, A_dev, K, M, batch, lda, a_batch_stride,
                                     kGemmBK, kGemmBM);
   if (rc != GBSGMC_OK) return rc;
   rc = b_mn ? make_tmap_bf16_3d(&tb, B_dev, N, K, batch, ldb, b_batch_stride, 64, 64)
-            : make_tmap_bf16_3d(&tb, B_dev, K, N, batch, ldb, b_batch_stride, kGemmBK, bn);
+            : make_tmap_bf16_3d(&tb, B_dev, K, N, batch, ldb, b_batch_stride, kGemmBK,
+                                pair ? bn / 2 : bn);
   if (rc != GBSGMC_OK) return rc;
   const StoreF32 epi{C_dev, ldc, c_batch_stride};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (pair)
+    return dispatch_pair(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st, wait_limit_ns);
   GemmRagged rg;
   rg.wait_ns = wait_limit_ns;
   return bn == 256

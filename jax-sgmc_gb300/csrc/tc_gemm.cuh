@@ -65,6 +65,13 @@ int make_tmap_bf16_3d(CUtensorMap* map, const void* base, int64_t cols,
 
 size_t gemm_smem_bytes(int bn);
 
+// CTA-pair GEMM (tc_gemm2_kernel): shared-memory ring depth, bytes, and
+// whether it is used where it applies (the GBSGMC_GEMM_PAIR environment
+// variable set to 0 turns it off; read at each launch).
+constexpr int kGemm2Stages = 6;
+size_t gemm2_smem_bytes(int bn);
+bool gemm_pair_enabled();
+
 // Ragged batches: chain b may use only the first m_b rows (row-ragged: its
 // output tiles are counted by tile_prefix[b + 1] - tile_prefix[b]) or only
 // the first kblocks[b] 64-wide K slices (K-ragged).  Null pointers mean the
@@ -337,6 +344,246 @@ int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, int batch, int M,
   const int grid = static_cast<int>(tiles < int64_t(sms) * per_sm ? tiles : int64_t(sms) * per_sm);
   kern<<<grid, kGemmThreads, smem, st>>>(ta, tb, M, N, K, batch, status, epi, rg);
   return check_launch("tc_gemm_kernel");
+}
+
+// Persistent batched GEMM on CTA pairs (tcgen05 .cta_group::2): each
+// cluster of two CTAs computes 256 x BN output tiles, C[b] = A[b] B[b]^T as
+// tc_gemm_kernel, with the same operand layouts and epilogue interface.
+// Per pair tile and 64-wide K slice, CTA r (its rank in the cluster) loads
+// rows [128 r, 128 r + 128) of the tile's A rows and rows [BN/2 r, BN/2 r +
+// BN/2) of its B rows into its own ring stage; both CTAs' copies complete on
+// the leader's (rank 0) `full` barrier.  The leader's MMA warp issues
+// M = 256 x N = BN MMAs that read both CTAs' halves and accumulate rows
+// [128 r, 128 r + 128) in CTA r's TMEM, and commits to the `empty` and
+// `tfull` barriers of both CTAs at once.  Each CTA's epilogue warps drain
+// their own TMEM rows and report to the leader's `tempty` barrier.  Against
+// the single-CTA kernel a B row is read once per 256 output rows instead of
+// once per 128, halving the B operand's shared-memory reads and copies, and
+// a stage holds 32 KB, so the ring is six stages deep.
+//
+// Every wait is bounded as in tc_gemm_kernel; a CTA that times out sets its
+// own and its partner's abort flags, and both leave their loops, wait 2 ms
+// for copies in flight, meet at a cluster barrier, free the TMEM and return.
+template <int BN, bool A_MN, bool B_MN, class Epi>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
+    tc_gemm2_kernel(const __grid_constant__ CUtensorMap ta,
+                    const __grid_constant__ CUtensorMap tb, int M, int N, int K, int batch,
+                    int* status, Epi epi, uint64_t wait_ns) {
+  constexpr int BM = 2 * kGemmBM;  // rows of a pair tile, kGemmBM per CTA
+  constexpr int BK = kGemmBK, STAGES = kGemm2Stages;
+  constexpr int BNH = BN / 2;      // B rows held by each CTA
+  constexpr uint32_t A_BYTES = kGemmBM * BK * 2, B_BYTES = BNH * BK * 2;
+  constexpr uint32_t BLOCK_BYTES = 64 * BK * 2;  // one 64 x 64 MN-major box
+  constexpr uint32_t TMEM_COLS = 2 * BN;
+  static_assert(BN == 256, "pair tiles are 256 x 256");
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint8_t* sa = smem;
+  uint8_t* sb = smem + STAGES * A_BYTES;
+  uint32_t* stage_all = reinterpret_cast<uint32_t*>(sb + STAGES * B_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(stage_all + kGemmEpiWarps * kStageWords);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;  // [2] accumulator ready (both CTAs)
+  uint64_t* tempty = tfull + 2;      // [2] accumulator drained (leader: both CTAs' warps)
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const uint32_t rank = tc::cluster_rank();
+  const bool leader = rank == 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tiles_n = N / BN, per_batch = (M / BM) * tiles_n;
+  const int tiles = per_batch * batch;
+  const int KB = K / BK;
+  const int first = static_cast<int>(tc::cluster_id());
+  const int step = static_cast<int>(tc::cluster_count());
+  const uint32_t peer_abort = tc::peer_addr(const_cast<int*>(abort_flag), rank ^ 1u);
+  auto fail = [&]() {
+    raise_status(status, GBSGMC_ERR_TIMEOUT);
+    *abort_flag = 1;
+    tc::st_cluster_u32(peer_abort, 1u);
+  };
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 2 * kGemmEpiWarps);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    mbar_fence_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc2(tmem_slot, TMEM_COLS);
+    tc::tmem_relinquish2();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::cluster_sync();  // both CTAs' barriers and flags are initialised
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = first; ok && t < tiles; t += step) {
+        const int b = t / per_batch, r = t % per_batch;
+        const int m0 = (r / tiles_n) * BM + kGemmBM * static_cast<int>(rank);
+        const int n0 = (r % tiles_n) * BN + BNH * static_cast<int>(rank);
+        for (int kb = 0; kb < KB; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1u;
+          if (!mbar_wait_bounded(&empty[s], ph ^ 1u, abort_flag, wait_ns)) {
+            fail();
+            ok = false;
+            break;
+          }
+          const uint32_t fb = tc::peer_addr(&full[s], 0);
+          if (leader) mbar_arrive_expect_tx(&full[s], 2 * (A_BYTES + B_BYTES));
+          const int k0 = kb * BK;
+          if constexpr (A_MN) {
+#pragma unroll
+            for (int j = 0; j < kGemmBM / 64; ++j)
+              tc::tma_load_3d_pair(sa + s * A_BYTES + j * BLOCK_BYTES, &ta, m0 + 64 * j, k0, b, fb);
+          } else {
+            tc::tma_load_3d_pair(sa + s * A_BYTES, &ta, k0, m0, b, fb);
+          }
+          if constexpr (B_MN) {
+#pragma unroll
+            for (int j = 0; j < BNH / 64; ++j)
+              tc::tma_load_3d_pair(sb + s * B_BYTES + j * BLOCK_BYTES, &tb, n0 + 64 * j, k0, b, fb);
+          } else {
+            tc::tma_load_3d_pair(sb + s * B_BYTES, &tb, k0, n0, b, fb);
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (leader && lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(BM, BN, A_MN, B_MN);
+      uint32_t it = 0, acc = 0;
+      bool ok = true;
+      for (int t = first; ok && t < tiles; t += step, ++acc) {
+        const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
+        if (!tc::mbar_wait_cluster_bounded(&tempty[buf], aph ^ 1u, abort_flag, wait_ns)) {
+          fail();
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t d = tmem + buf * BN;
+        for (int kb = 0; kb < KB; ++kb, ++it) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1u;
+          if (!mbar_wait_bounded(&full[s], ph, abort_flag, wait_ns)) {
+            fail();
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint64_t a0 = A_MN ? tc::sdesc_mn_sw128(sa + s * A_BYTES, BLOCK_BYTES)
+                                   : tc::sdesc_k_sw128(sa + s * A_BYTES);
+          const uint64_t b0 = B_MN ? tc::sdesc_mn_sw128(sb + s * B_BYTES, BLOCK_BYTES)
+                                   : tc::sdesc_k_sw128(sb + s * B_BYTES);
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint64_t da = A_MN ? 128u * k : 2u * k;
+            const uint64_t db = B_MN ? 128u * k : 2u * k;
+            tc::mma2_bf16(d, a0 + da, b0 + db, idesc, (kb | k) != 0);
+          }
+          tc::mma2_commit_multicast(&empty[s], 0x3);
+        }
+        if (ok) tc::mma2_commit_multicast(&tfull[buf], 0x3);
+      }
+      tc::mma2_commit(drain);
+      mbar_wait_bounded(drain, 0, nullptr);
+    }
+  } else {
+    constexpr int NC = BN / kGemmSplit;
+    const int q = warp & 3;
+    const int h = (warp - 2) >> 2;
+    uint32_t* stage = stage_all + (warp - 2) * kStageWords;
+    const uint32_t drained0 = tc::peer_addr(&tempty[0], 0);
+    const uint32_t drained1 = tc::peer_addr(&tempty[1], 0);
+    uint32_t acc = 0;
+    for (int t = first; t < tiles; t += step, ++acc) {
+      const uint32_t buf = acc & 1u, aph = (acc >> 1) & 1u;
+      const bool ok = mbar_wait_bounded(&tfull[buf], aph, abort_flag, wait_ns);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0 && !*abort_flag) fail();
+        break;
+      }
+      tc::fence_after_sync();
+      const int b = t / per_batch, r = t % per_batch;
+      const int row0 = (r / tiles_n) * BM + kGemmBM * static_cast<int>(rank) + q * 32;
+      const uint32_t tbase =
+          tmem + buf * BN + h * NC + (static_cast<uint32_t>(q * 32) << 16);
+      auto load = [tbase](int c, float(&v)[32]) {
+        tc::tmem_ld32(tbase + static_cast<uint32_t>(c * 32), v);
+      };
+      epi.template tile<NC>(b, row0, (r % tiles_n) * BN + h * NC, load, stage);
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive_cluster(buf ? drained1 : drained0);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (*abort_flag && threadIdx.x == 0) {
+    // Copies already issued complete within microseconds.
+    const uint64_t t0 = global_ns();
+    while (global_ns() - t0 < 2000000ull) {
+    }
+  }
+  __syncthreads();
+  tc::cluster_sync();  // no further access to the partner's shared memory
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc2(tmem, TMEM_COLS);
+  }
+}
+
+// Launches the pair GEMM on `st` (uniform batches; M a multiple of 256, N of
+// BN, K of 64): one cluster per co-resident pair slot, at most one per pair
+// tile.  Tensor maps as for launch_gemm except that a K-major B map has
+// boxes of 64 x BN/2.
+template <int BN, bool A_MN, bool B_MN, class Epi>
+int launch_gemm2(const CUtensorMap& ta, const CUtensorMap& tb, int batch, int M, int N, int K,
+                 int* status, const Epi& epi, cudaStream_t st,
+                 uint64_t wait_ns = kWaitLimitNs) {
+  auto kern = tc_gemm2_kernel<BN, A_MN, B_MN, Epi>;
+  const size_t smem = gemm2_smem_bytes(BN);
+  static int max_clusters = 0;
+  if (max_clusters == 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    int dev = 0, sms = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * (sms / 2), 1, 1);
+      cfg.blockDim = dim3(kGemmThreads, 1, 1);
+      cfg.dynamicSmemBytes = smem;
+      e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
+    }
+    if (e != cudaSuccess || max_clusters < 1) {
+      max_clusters = 0;
+      return set_error(GBSGMC_ERR_CUDA, "gemm (pairs): cannot configure the kernel: %s",
+                       cudaGetErrorString(e));
+    }
+  }
+  if (M % (2 * kGemmBM) != 0 || N % BN != 0 || K % kGemmBK != 0)
+    return set_error(GBSGMC_ERR_SHAPE, "gemm (pairs): needs M %% 256, N %% %d, K %% 64", BN);
+  const int64_t tiles = static_cast<int64_t>(M / (2 * kGemmBM)) * (N / BN) * batch;
+  const int clusters = static_cast<int>(tiles < max_clusters ? tiles : max_clusters);
+  kern<<<2 * clusters, kGemmThreads, smem, st>>>(ta, tb, M, N, K, batch, status, epi, wait_ns);
+  return check_launch("tc_gemm2_kernel");
 }
 
 }  // namespace gbsgmc

@@ -102,3 +102,35 @@ def test_gemm_progress_wait_bound_runs_out_cleanly(lib):
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     assert bool(((C - ref).abs() <= 1e-3 * bound + 1e-4).all())
+
+
+@pytest.mark.parametrize("a_mn,b_mn", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_pair_and_single_cta_gemms_agree(lib, monkeypatch, a_mn, b_mn):
+  """The CTA-pair kernel (256 x 256 tiles on two SMs, tcgen05 cta_group::2,
+  used where M % 256 == 0 and N % 256 == 0) and the single-CTA kernel
+  (GBSGMC_GEMM_PAIR=0) both meet the fp32-summation bound against torch, in
+  every operand layout, and agree with each other to that bound."""
+  import torch
+  from gbsgmc import _lib
+  batch, M, N, K = 3, 512, 768, 576
+  g = torch.Generator(device="cuda").manual_seed(31 + 2 * a_mn + b_mn)
+  A = torch.randn((batch, M, K), generator=g, device="cuda").to(torch.bfloat16)
+  B = torch.randn((batch, N, K), generator=g, device="cuda").to(torch.bfloat16)
+  As = A.transpose(1, 2).contiguous() if a_mn else A
+  Bs = B.transpose(1, 2).contiguous() if b_mn else B
+  ref = torch.bmm(A.float(), B.float().transpose(1, 2))
+  bound = torch.bmm(A.float().abs(), B.float().abs().transpose(1, 2))
+  out = []
+  for pair in ("1", "0"):
+    monkeypatch.setenv("GBSGMC_GEMM_PAIR", pair)
+    C = torch.full((batch, M, N), float("nan"), device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("gbsgmc_gemm_bf16", a_mn, b_mn, As.data_ptr(), M if a_mn else K,
+              M * K, Bs.data_ptr(), N if b_mn else K, N * K, C.data_ptr(), N,
+              M * N, batch, M, N, K, status.data_ptr(), _lib.stream_handle())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert torch.isfinite(C).all()
+    assert bool(((C - ref).abs() <= 1e-3 * bound + 1e-4).all())
+    out.append(C)
+  assert bool(((out[0] - out[1]).abs() <= 1e-3 * bound + 1e-4).all())
