@@ -207,9 +207,13 @@ __device__ __forceinline__ uint32_t peer_addr(const void* p, uint32_t rank) {
   return r;
 }
 
-// One arrival on an mbarrier of either CTA (shared::cluster address).
-__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar)
+// One arrival on an mbarrier of either CTA (shared::cluster address), with no
+// ordering of this thread's earlier memory accesses: for signals whose only
+// precondition is complete (e.g. TMEM reads already waited for with
+// tcgen05.wait::ld), which a release would make wait for every store the
+// thread has in flight.
+__device__ __forceinline__ void mbar_arrive_cluster_relaxed(uint32_t bar) {
+  asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar)
                : "memory");
 }
 

@@ -529,7 +529,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
       epi.template tile<NC>(b, row0, (r % tiles_n) * BN + h * NC, load, stage);
       tc::fence_before_sync();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive_cluster(buf ? drained1 : drained0);
+      // The accumulator's rows are in registers (tcgen05.wait::ld): nothing
+      // else has to be ordered before the leader may overwrite them.
+      if (lane == 0) tc::mbar_arrive_cluster_relaxed(buf ? drained1 : drained0);
     }
   }
   tc::fence_before_sync();
