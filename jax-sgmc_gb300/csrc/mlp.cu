@@ -345,13 +345,17 @@ __device__ __forceinline__ void tanh_block(const Load& load, int blk, const floa
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   float dot2 = 0.f;  // odd columns: two independent FMA chains
+  const float bl0 = __ldg(bias + 64 * blk + lane);
+  const float bl1 = __ldg(bias + 64 * blk + 32 + lane);
+  const float wl0 = w3 != nullptr ? __ldg(w3 + 64 * blk + lane) : 0.f;
+  const float wl1 = w3 != nullptr ? __ldg(w3 + 64 * blk + 32 + lane) : 0.f;
+  float vv[64];
+  load.wide(blk, vv);  // one wait for the block's 64 columns
 #pragma unroll
   for (int half = 0; half < 2; ++half) {
-    const int k0 = 64 * blk + 32 * half;
-    const float bl = __ldg(bias + k0 + lane);
-    const float wl = w3 != nullptr ? __ldg(w3 + k0 + lane) : 0.f;
-    float v[32];
-    load(2 * blk + half, v);
+    const float bl = half ? bl1 : bl0;
+    const float wl = half ? wl1 : wl0;
+    const float* v = vv + 32 * half;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const float z0 = tanh_approx(v[2 * j] + __shfl_sync(full, bl, 2 * j));
@@ -439,16 +443,23 @@ struct EpiAdjoint1 {
     float* part = pb1 + (static_cast<int64_t>(b) * (n / 32) + row0 / 32) * H1 + col0;
 #pragma unroll 1
     for (int blk = 0; blk < NC / 64; ++blk) {
+      // The accumulator's 64 columns are requested first; the Z1 block is
+      // read and transposed while they arrive.
+      uint32_t acc[64];
+      load.wide_start(blk, acc);
       uint32_t zw[32];
 #pragma unroll
       for (int r = 0; r < 32; ++r) zw[r] = zrow[static_cast<int64_t>(r) * (H1 / 2) + 32 * blk];
 #pragma unroll
       for (int r = 0; r < 32; ++r) epi::set(st, r, zw[r]);
       epi::get_row(st, zw);
+      tc::tmem_ld64_wait(acc);
+      float vv[64];
+#pragma unroll
+      for (int i = 0; i < 64; ++i) vv[i] = __uint_as_float(acc[i]);
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
-        float v[32];
-        load(2 * blk + half, v);
+        float* v = vv + 32 * half;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           float za, zb;

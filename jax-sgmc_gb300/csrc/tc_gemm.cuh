@@ -299,9 +299,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const int row0 = (r / tiles_n) * BM + q * 32;
       const uint32_t tbase =
           tmem + buf * BN + h * NC + (static_cast<uint32_t>(q * 32) << 16);
-      auto load = [tbase](int c, float(&v)[32]) {
-        tc::tmem_ld32(tbase + static_cast<uint32_t>(c * 32), v);
-      };
+      const tc::TmemRows load{tbase};
       epi.template tile<NC>(b, row0, (r % tiles_n) * BN + h * NC, load, stage);
       tc::fence_before_sync();
       __syncwarp();
@@ -523,9 +521,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
       const int row0 = (r / tiles_n) * BM + kGemmBM * static_cast<int>(rank) + q * 32;
       const uint32_t tbase =
           tmem + buf * BN + h * NC + (static_cast<uint32_t>(q * 32) << 16);
-      auto load = [tbase](int c, float(&v)[32]) {
-        tc::tmem_ld32(tbase + static_cast<uint32_t>(c * 32), v);
-      };
+      const tc::TmemRows load{tbase};
       epi.template tile<NC>(b, row0, (r % tiles_n) * BN + h * NC, load, stage);
       tc::fence_before_sync();
       __syncwarp();
