@@ -876,6 +876,24 @@ int gbsgmc_glm_resgld_plan_create(gbsgmc_plan** plan, const gbsgmc_glm* model,
                                   double* sample_lik_dev, int block_steps,
                                   int* status_dev);
 
+/* As gbsgmc_glm_resgld_plan_create on the dense network (MLP): the same pair
+ * layout, identities, exchange rule, uniforms, kept samples and counts; per
+ * step one batched value-and-gradient of all 2 pairs chains (row c reads its
+ * minibatch from identity ident_dev[c]'s index stream), one SGLD update
+ * (noise drawn as identity ident_dev[c]) and one exchange launch.  n a
+ * positive multiple of 128.  Replaces alias.re_sgld (jax_sgmc/alias.py:
+ * 122-208) through solver.mcmc on a network likelihood. */
+int gbsgmc_mlp_resgld_pairs_plan_create(gbsgmc_plan** plan, const gbsgmc_mlp* model,
+                                        int pairs, int n, float* x_dev, float* v_dev,
+                                        float alpha, float lmbd, const gbsgmc_sched* sched,
+                                        const gbsgmc_noise* noise,
+                                        const gbsgmc_index_src* index_src,
+                                        const gbsgmc_tempering* tempering,
+                                        const int32_t* pair_chain_dev, int32_t* ident_dev,
+                                        double* U_dev, double* lk_var_dev, float* samples_dev,
+                                        double* sample_lik_dev, int block_steps,
+                                        int* status_dev);
+
 /* Runs steps [first_step, first_step + steps) of the plan, ordered after prior
  * work on `stream`; later work on `stream` waits for it.  Does not block the
  * host. */

@@ -44,6 +44,12 @@ int glm_sgld_step(const gbsgmc_glm* model, int chains, int n,
 // swapped; then, at kept steps, the normal slots' rows and -U stored as the
 // step's samples.  Pair p's uniform is Philox(counter (0, k + 1), key
 // (seed << 32) | pair_chain[p]).
+// The MLP's value and gradient (gbsgmc_mlp_value_and_grad) where row c of
+// the batch reads its minibatch from row ident_dev[c] of idx.
+int mlp_value_and_grad_ident(const gbsgmc_mlp* model, int chains, int n, const int32_t* idx,
+                             int64_t idx_stride, const int32_t* ident_dev, const float* w,
+                             double* U, float* grad, double* lk_var, void* ws, size_t ws_bytes,
+                             int* status, cudaStream_t st);
 int resgld_pairs_exchange(int pairs, int d, float* x, float* v, double* U,
                           double* var, int32_t* ident, const gbsgmc_sched* sched,
                           double F, uint64_t seed, const int32_t* pair_chain,
@@ -58,6 +64,8 @@ struct UpdateFusion {
   int64_t mirror_stride = 0;  //   (elements; both multiples of 4)
   double* sq_parts = nullptr; // per-block sums of squares of the new x,
                               //   [chains, update_blocks(chains, P)]
+  const int32_t* ident = nullptr;  // [chains] noise chain of each row (row
+                                   //   c draws as chain ident[c]); null: c
 };
 int update_blocks(int chains, int64_t P);
 int sgld_update_fused(int chains, int64_t P, float* x, const float* g, float* v,

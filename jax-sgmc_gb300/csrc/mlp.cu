@@ -203,6 +203,8 @@ struct MlpArgs {
   int* status;
   // Ragged batch: rows of chain c are n_true[c] <= n (null: all n).
   const int32_t* n_true;
+  // Row c of the batch reads its minibatch from row ident[c] of idx (null: c).
+  const int32_t* ident;
   // Fused with the integrator: the BF16 weights and the sums of squares
   // (sq_count per chain in psq) are supplied, the prior's gradient is the
   // update's.
@@ -301,7 +303,8 @@ __global__ void __launch_bounds__(256) mlp_gather_kernel(const MlpArgs a) {
     // Rows past the chain's minibatch (ragged batches) are zero.
     int64_t o = -1;
     if (i0 + t < nc) {
-      o = a.idx[static_cast<int64_t>(c) * a.idx_stride + i0 + t];
+      const int ic = a.ident != nullptr ? __ldg(a.ident + c) : c;
+      o = a.idx[static_cast<int64_t>(ic) * a.idx_stride + i0 + t];
       if (o < 0 || o >= a.n_rows) {
         raise_status(a.status, GBSGMC_ERR_INDEX);
         o = 0;
@@ -1094,7 +1097,7 @@ int mlp_call(const gbsgmc_mlp* model, int chains, int n, const int32_t* n_dev,
              const float* w_dev, double* U_dev, float* grad_dev, float* lk_dev,
              double* lk_var_dev, void* workspace_dev, size_t workspace_bytes,
              int* status_dev, gbsgmc_stream_t stream, const double* sq_parts = nullptr,
-             int sq_count = 0) {
+             int sq_count = 0, const int32_t* ident_dev = nullptr) {
   int rc = check_model(model, "mlp_value_and_grad");
   if (rc != GBSGMC_OK) return rc;
   if (chains < 0 || n < 0)
@@ -1141,6 +1144,7 @@ int mlp_call(const gbsgmc_mlp* model, int chains, int n, const int32_t* n_dev,
   a.lk_var = lk_var_dev;
   a.status = status_dev;
   a.n_true = n_dev;
+  a.ident = ident_dev;
   a.fused = sq_parts != nullptr ? 1 : 0;
   a.sq_count = sq_count;
   a.psq = const_cast<double*>(sq_parts);
@@ -1159,6 +1163,15 @@ int mlp_mirror_region(const gbsgmc_mlp* model, int chains, int n, void* ws, void
   *count = matrix_params(s);
   *stride = matrix_params(s);
   return GBSGMC_OK;
+}
+
+int mlp_value_and_grad_ident(const gbsgmc_mlp* model, int chains, int n, const int32_t* idx,
+                             int64_t idx_stride, const int32_t* ident_dev, const float* w,
+                             double* U, float* grad, double* lk_var, void* ws, size_t ws_bytes,
+                             int* status, cudaStream_t st) {
+  if (ident_dev == nullptr) return set_error(GBSGMC_ERR_ARG, "mlp (identities): null map");
+  return mlp_call(model, chains, n, nullptr, idx, idx_stride, nullptr, w, U, grad, nullptr,
+                  lk_var, ws, ws_bytes, status, st, nullptr, 0, ident_dev);
 }
 
 int mlp_value_and_grad_fused(const gbsgmc_mlp* model, int chains, int n, const int32_t* idx,

@@ -317,6 +317,74 @@ struct ResgldPlan final : gbsgmc_plan {
   }
 };
 
+// alias.re_sgld on the dense network: `pairs` (normal, hot) pairs of SGLD
+// chains and each pair's exchange after every step, as GlmPairsPlan runs them
+// on a generalised-linear potential.  Row c of x holds the chain identity
+// ident[c]: the minibatch rows are read from that identity's index stream
+// and the noise is drawn as that chain, so streams travel with the states.
+struct MlpPairsPlan final : gbsgmc_plan {
+  gbsgmc_mlp model{};
+  int pairs = 0, n = 0;
+  int64_t P = 0, rows = 0;
+  float* x = nullptr;
+  float* v = nullptr;
+  float alpha = 0.9f, lmbd = 1e-5f;
+  float* grad = nullptr;  // owned [2 pairs, P]
+  gbsgmc_sched sched{};
+  gbsgmc_noise noise{};
+  gbsgmc_index_src isrc{};
+  gbsgmc_tempering temp{};
+  const int32_t* pair_chain = nullptr;
+  int32_t* ident = nullptr;
+  double* U = nullptr;
+  double* lk_var = nullptr;
+  float* samples = nullptr;
+  double* sample_lik = nullptr;
+  int* status = nullptr;
+  int32_t* idx = nullptr;  // owned [G, 2 pairs, n], by identity
+  void* ws = nullptr;      // owned
+  size_t ws_size = 0;
+
+  ~MlpPairsPlan() override {
+    if (stream != nullptr) cudaStreamSynchronize(stream);
+    plan_free(this, grad);
+    plan_free(this, idx);
+    plan_free(this, ws);
+  }
+
+  // Per block the index draw and the step counter; per step the update and
+  // the exchange (the value-and-gradient launches are counted by the caller).
+  int64_t launches_per_block(int g) const override { return 2 + 2 * static_cast<int64_t>(g); }
+
+  int enqueue(int g, cudaStream_t s) override {
+    const int chains = 2 * pairs;
+    const int64_t cn = static_cast<int64_t>(chains) * n;
+    int rc = gbsgmc_index_draw_pcg64(isrc.pcg_dev, chains, rows, static_cast<int64_t>(g) * n, n,
+                                     idx, n, cn, status, s);
+    if (rc != GBSGMC_OK) return rc;
+    UpdateFusion by_identity;
+    by_identity.ident = ident;
+    for (int j = 0; j < g; ++j) {
+      gbsgmc_sched sj = sched;
+      sj.base_dev = base;
+      sj.offset = j;
+      gbsgmc_sched step_sched = sj;
+      step_sched.keep_slot_dev = nullptr;  // the exchange stores the samples
+      if ((rc = mlp_value_and_grad_ident(&model, chains, n, idx + j * cn, n, ident, x, U, grad,
+                                         lk_var, ws, ws_size, status, s)))
+        return rc;
+      if ((rc = sgld_update_fused(chains, P, x, grad, v, alpha, lmbd, &step_sched, &noise,
+                                  by_identity, s)))
+        return rc;
+      if ((rc = resgld_pairs_exchange(pairs, static_cast<int>(P), x, v, U, lk_var, ident, &sj,
+                                      temp.F, temp.seed, pair_chain, temp.ssq_dev, temp.k_dev,
+                                      temp.counts_dev, samples, sample_lik, s)))
+        return rc;
+    }
+    return plan_advance(this, g, s);
+  }
+};
+
 int check_common(const gbsgmc_integrator* integ, int chains, int n, float* x, float* aux,
                  const gbsgmc_sched* sched, const gbsgmc_noise* noise,
                  const gbsgmc_index_src* isrc, double* U, int block_steps, int* status) {
@@ -558,6 +626,86 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
                                               x, U, grad, nullptr, var, wsp, ws, status_dev,
                                               s);
     };
+    rc = plan_capture(p);
+  } while (false);
+  if (rc != GBSGMC_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return GBSGMC_OK;
+}
+
+extern "C" int gbsgmc_mlp_resgld_pairs_plan_create(
+    gbsgmc_plan** out, const gbsgmc_mlp* model, int pairs, int n, float* x_dev, float* v_dev,
+    float alpha, float lmbd, const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+    const gbsgmc_index_src* index_src, const gbsgmc_tempering* tempering,
+    const int32_t* pair_chain_dev, int32_t* ident_dev, double* U_dev, double* lk_var_dev,
+    float* samples_dev, double* sample_lik_dev, int block_steps, int* status_dev) {
+  if (out == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "mlp_resgld_pairs_plan_create: null plan");
+  *out = nullptr;
+  if (model == nullptr || sched == nullptr || noise == nullptr || index_src == nullptr ||
+      tempering == nullptr || x_dev == nullptr || pair_chain_dev == nullptr ||
+      ident_dev == nullptr || U_dev == nullptr || lk_var_dev == nullptr ||
+      status_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "mlp_resgld_pairs_plan_create: null argument");
+  if (pairs <= 0 || 2 * pairs > 65535 || n <= 0 || block_steps <= 0 || block_steps > 100000)
+    return set_error(GBSGMC_ERR_ARG, "mlp_resgld_pairs_plan_create: bad pairs/n/block_steps");
+  if (index_src->pcg_dev == nullptr || index_src->external)
+    return set_error(GBSGMC_ERR_ARG,
+                     "mlp_resgld_pairs_plan_create: needs PCG64 index streams (one per chain)");
+  if (sched->chain_temperature_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG,
+                     "mlp_resgld_pairs_plan_create: needs the per-chain temperatures");
+  if (tempering->ssq_dev == nullptr || tempering->k_dev == nullptr || !(tempering->F != 0.0))
+    return set_error(GBSGMC_ERR_ARG, "mlp_resgld_pairs_plan_create: bad tempering state");
+  if (sched->keep_slot_dev != nullptr && samples_dev == nullptr)
+    return set_error(GBSGMC_ERR_ARG,
+                     "mlp_resgld_pairs_plan_create: keep table given without sample buffer");
+  const size_t ws = gbsgmc_mlp_workspace_bytes(model, 2 * pairs, n);
+  if (ws == 0)
+    return set_error(GBSGMC_ERR_SHAPE,
+                     "mlp_resgld_pairs_plan_create: unsupported shape (n %% 128)");
+  const int64_t P = gbsgmc_mlp_param_count(model);
+  if (P <= 0 || P > (1ll << 31) - 1)
+    return set_error(GBSGMC_ERR_SHAPE, "mlp_resgld_pairs_plan_create: parameter count");
+  MlpPairsPlan* p = new (std::nothrow) MlpPairsPlan();
+  if (p == nullptr)
+    return set_error(GBSGMC_ERR_ARG, "mlp_resgld_pairs_plan_create: out of memory");
+  p->model = *model;
+  p->pairs = pairs;
+  p->n = n;
+  p->P = P;
+  p->rows = model->n_rows > 0 ? model->n_rows : model->n_obs;
+  p->x = x_dev;
+  p->v = v_dev;
+  p->alpha = alpha;
+  p->lmbd = lmbd;
+  p->sched = *sched;
+  p->noise = *noise;
+  p->isrc = *index_src;
+  p->temp = *tempering;
+  p->pair_chain = pair_chain_dev;
+  p->ident = ident_dev;
+  p->U = U_dev;
+  p->lk_var = lk_var_dev;
+  p->samples = samples_dev;
+  p->sample_lik = sample_lik_dev;
+  p->status = status_dev;
+  p->ws_size = ws;
+  int rc = GBSGMC_OK;
+  do {
+    if ((rc = plan_init(p, block_steps))) break;
+    const int chains = 2 * pairs;
+    if ((rc = plan_alloc(p, &p->grad, sizeof(float) * static_cast<size_t>(chains) * P,
+                         "mlp_resgld_pairs_plan_create: gradient")))
+      break;
+    if ((rc = plan_alloc(p, &p->idx,
+                         sizeof(int32_t) * static_cast<size_t>(block_steps) * chains * n,
+                         "mlp_resgld_pairs_plan_create: index buffer")))
+      break;
+    if ((rc = plan_alloc(p, &p->ws, ws, "mlp_resgld_pairs_plan_create: workspace"))) break;
     rc = plan_capture(p);
   } while (false);
   if (rc != GBSGMC_OK) {

@@ -52,16 +52,18 @@ struct Fuse {
   uint32_t* mirror;  // BF16 pairs
   int64_t mcount, mstride;
   double* sq;
+  const int32_t* ident;  // noise chain of each row, or null
 };
 
 Fuse to_fuse(const UpdateFusion* f) {
-  Fuse r{0.f, nullptr, 0, 0, nullptr};
+  Fuse r{0.f, nullptr, 0, 0, nullptr, nullptr};
   if (f != nullptr) {
     r.pf = f->prior_pf;
     r.mirror = static_cast<uint32_t*>(f->mirror);
     r.mcount = f->mirror_count;
     r.mstride = f->mirror_stride;
     r.sq = f->sq_parts;
+    r.ident = f->ident;
   }
   return r;
 }
@@ -143,7 +145,7 @@ sgld_update_kernel(int chains, int64_t P, float* x, const float* g, float* v, fl
     load4(xc, j0, P, xv);
     load4(gc, j0, P, gv);
     if (vc != nullptr) load4(vc, j0, P, vv);
-    noise4(noise, c, j0, P, k, GBSGMC_TAG_SGLD, xi);
+    noise4(noise, fz.ident != nullptr ? __ldg(fz.ident + c) : c, j0, P, k, GBSGMC_TAG_SGLD, xi);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const float gj = fz.pf != 0.f ? fmaf(fz.pf, xv[e], gv[e]) : gv[e];

@@ -642,12 +642,13 @@ def try_fused_sgld(solver, scheduler, states, schedulers, iterations, saving):
 
 
 class ResgldPairsPlan:
-  """Owns a ``gbsgmc_glm_resgld_plan``: P (normal, hot) pairs of SGLD chains
-  on a GLM potential with the pairs' exchange after every step on the
-  device (alias.re_sgld).  X [2P, d] holds the normal chains in rows [0, P)
-  and their hot partners in rows [P, 2P); ``ident`` [2P] maps each row to
-  the chain identity (index stream ``pcg[i]``, noise chain id chain_base + i)
-  it holds after the exchanges so far."""
+  """Owns a ``gbsgmc_glm_resgld_plan`` (or, on the MLP likelihood,
+  ``gbsgmc_mlp_resgld_pairs_plan``): P (normal, hot) pairs of SGLD chains
+  with the pairs' exchange after every step on the device (alias.re_sgld).
+  X [2P, d] holds the normal chains in rows [0, P) and their hot partners in
+  rows [P, 2P); ``ident`` [2P] maps each row to the chain identity (index
+  stream ``pcg[i]``, noise chain id chain_base + i) it holds after the
+  exchanges so far."""
 
   def __init__(self, potential, dataset, X, V, alpha, lmbd, n, h_tab, t_tab,
                keep_tab, ladder, n_kept, pcg, ident, pair_chain, ssq, k, F,
@@ -674,7 +675,10 @@ class ResgldPairsPlan:
     self.temp = _lib.Tempering(1, 0, float(F), int(swap_seed) & (2**64 - 1),
                                _lib.ptr(ssq), _lib.ptr(k), _lib.ptr(self.counts), None)
     handle = _lib.C.c_void_p()
-    _lib.call("gbsgmc_glm_resgld_plan_create", _lib.C.byref(handle), self.model,
+    self.network = bool(potential.is_mlp)
+    fn = "gbsgmc_mlp_resgld_pairs_plan_create" if self.network else \
+        "gbsgmc_glm_resgld_plan_create"
+    _lib.call(fn, _lib.C.byref(handle), self.model,
               self.pairs, int(n), _lib.ptr(X), _lib.ptr(V), float(alpha), float(lmbd),
               self.sched, self.noise, self.isrc, self.temp, _lib.ptr(pair_chain),
               _lib.ptr(ident), _lib.ptr(self.U), _lib.ptr(self.lk_var),
@@ -687,7 +691,10 @@ class ResgldPairsPlan:
               _lib.stream_handle())
 
   def launches(self, steps) -> int:
-    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps)))
+    # The MLP plan counts its value-and-gradient calls here: prep, gather,
+    # four GEMMs and the dW1 GEMM, the output pass and the finalisation.
+    extra = 9 * int(steps) if self.network else 0
+    return int(_lib.load().gbsgmc_plan_launches(self.handle, int(steps))) + extra
 
   def check_status(self):
     code = int(self.status.item())
@@ -708,7 +715,7 @@ class ResgldPairsPlan:
 
 def try_fused_resgld(solver, scheduler, states, schedulers, iterations, saving):
   """Runs alias.re_sgld's pairs (solver.parallel_tempering over
-  langevin_diffusion, solver.py:220-299) on a GLM potential as one
+  langevin_diffusion, solver.py:220-299) on a GLM or MLP potential as one
   :class:`ResgldPairsPlan`: every pair steps, exchanges and keeps its normal
   chain's samples on the device, and the chains' index streams and noise
   are the per-pair path's, so the samples are the same.  Returns None when
@@ -716,7 +723,7 @@ def try_fused_resgld(solver, scheduler, states, schedulers, iterations, saving):
   have consecutive ids (normal, hot, normal, hot, ...), fresh numpy PCG64
   pipelines, one hot schedule whose temperatures are the normal schedule's
   times a constant factor and whose step sizes are the same, no injected
-  noise."""
+  noise; on the MLP, minibatches of a multiple of 128 rows."""
   import torch
   from .integrator import LangevinState, key_to_seed
   from .potential import StochasticPotential
@@ -729,12 +736,14 @@ def try_fused_resgld(solver, scheduler, states, schedulers, iterations, saving):
   if im.get("kind") != "langevin" or im.get("noise_source") is not None:
     return None
   pot, bfn = im.get("potential"), im.get("batch_fn")
-  if not isinstance(pot, StochasticPotential) or pot.is_network:
+  if not isinstance(pot, StochasticPotential) or pot.is_cnn:
     return None
   if not isinstance(bfn, tuple) or not isinstance(bfn[1], RandomBatchFn) \
       or bfn[1].kind != "host":
     return None
   rbf = bfn[1]
+  if pot.is_mlp and rbf.mb_size % 128 != 0:
+    return None
   P = len(states)
   chains = []
   for s in states:
