@@ -841,6 +841,22 @@ int gbsgmc_mlp_resgld_plan_create(gbsgmc_plan** plan, const gbsgmc_mlp* model,
                                   double* U_dev, double* lk_var_dev,
                                   int block_steps, int* status_dev);
 
+/* As gbsgmc_mlp_resgld_plan_create with kept samples: at the steps whose
+ * keep slot (sched->keep_slot_dev) is >= 0, after that step's exchange
+ * attempt, replica 0's positions go to samples_dev [slot, P] and its -U to
+ * sample_lik_dev [slot] (may be NULL).  A keep table needs a sample buffer
+ * and the other way round.  This is the ladder that alias.re_sgld_ladder
+ * runs; the reference samples pairs of one normal and one hot chain only. */
+int gbsgmc_mlp_resgld_plan_create_keep(gbsgmc_plan** plan, const gbsgmc_mlp* model,
+                                       int replicas, int n_max, const int32_t* n_dev,
+                                       float* x_dev, float* v_dev, float alpha, float lmbd,
+                                       const gbsgmc_sched* sched, const gbsgmc_noise* noise,
+                                       const gbsgmc_index_src* index_src,
+                                       const gbsgmc_tempering* tempering, double* U_dev,
+                                       double* lk_var_dev, float* samples_dev,
+                                       double* sample_lik_dev, int block_steps,
+                                       int* status_dev);
+
 /* reSGLD on a generalised-linear potential as alias.re_sgld runs it: `pairs`
  * pairs of a normal and a hot chain, plain SGLD (rms_prop when v_dev is not
  * NULL), and after every step each pair's exchange in FP64 with the rule of

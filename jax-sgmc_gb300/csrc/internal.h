@@ -68,6 +68,10 @@ struct UpdateFusion {
                                    //   c draws as chain ident[c]); null: c
 };
 int update_blocks(int chains, int64_t P);
+// At the schedule's kept steps: row 0 of x to samples[slot], -U[0] to
+// sample_lik[slot] (may be null).
+int keep_row(int64_t P, const float* x, const double* U, const gbsgmc_sched* sched,
+             float* samples, double* sample_lik, cudaStream_t st);
 int sgld_update_fused(int chains, int64_t P, float* x, const float* g, float* v,
                       float alpha, float lmbd, const gbsgmc_sched* sched,
                       const gbsgmc_noise* noise, const UpdateFusion& f,

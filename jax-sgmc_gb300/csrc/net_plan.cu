@@ -266,6 +266,8 @@ struct ResgldPlan final : gbsgmc_plan {
   double* U = nullptr;
   double* lk_var = nullptr;
   double* var_own = nullptr;  // owned when the caller passes no lk_var buffer
+  float* samples = nullptr;     // kept states of replica 0 [n_kept, P], or null
+  double* sample_lik = nullptr; // their -U [n_kept]
   int* status = nullptr;
   int32_t* idx = nullptr;  // owned [G, R, n_max]
   void* ws = nullptr;      // owned
@@ -282,7 +284,7 @@ struct ResgldPlan final : gbsgmc_plan {
   int step_multiple() const override { return temp.every; }
 
   int64_t launches_per_block(int g) const override {
-    return 2 + 2 * static_cast<int64_t>(g) + 3 * (g / temp.every);
+    return 2 + (samples != nullptr ? 3 : 2) * static_cast<int64_t>(g) + 3 * (g / temp.every);
   }
 
   int enqueue(int g, cudaStream_t s) override {
@@ -301,16 +303,22 @@ struct ResgldPlan final : gbsgmc_plan {
       gbsgmc_sched sj = sched;
       sj.base_dev = base;
       sj.offset = j;
+      gbsgmc_sched step_sched = sj;
+      step_sched.keep_slot_dev = nullptr;  // kept samples are taken after the exchange
       if ((rc = grad_fn(idx + j * cn, n_max, U, lk_var, grad, s))) return rc;
-      if ((rc = gbsgmc_sgld_update(replicas, P, x, grad, v, alpha, lmbd, &sj, &noise, nullptr,
-                                   s)))
+      if ((rc = gbsgmc_sgld_update(replicas, P, x, grad, v, alpha, lmbd, &step_sched, &noise,
+                                   nullptr, s)))
         return rc;
       if ((rc = gbsgmc_resgld_sa_update(replicas, lk_var, temp.ssq_dev, temp.k_dev, s)))
         return rc;
       if ((j + 1) % temp.every == 0 &&
-          (rc = gbsgmc_resgld_exchange_adjacent(replicas, P, x, v, U, lk_var, &sj, temp.every,
-                                                temp.ssq_dev, temp.F, temp.seed, nullptr,
-                                                temp.flags_dev, temp.counts_dev, nullptr, s)))
+          (rc = gbsgmc_resgld_exchange_adjacent(replicas, P, x, v, U, lk_var, &step_sched,
+                                                temp.every, temp.ssq_dev, temp.F, temp.seed,
+                                                nullptr, temp.flags_dev, temp.counts_dev,
+                                                nullptr, s)))
+        return rc;
+      if (samples != nullptr &&
+          (rc = keep_row(P, x, U, &sj, samples, sample_lik, s)))
         return rc;
     }
     return plan_advance(this, g, s);
@@ -561,6 +569,22 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
     float* x_dev, float* v_dev, float alpha, float lmbd, const gbsgmc_sched* sched,
     const gbsgmc_noise* noise, const gbsgmc_index_src* isrc, const gbsgmc_tempering* temp,
     double* U_dev, double* lk_var_dev, int block_steps, int* status_dev) {
+  if (sched != nullptr && sched->keep_slot_dev != nullptr)
+    return set_error(GBSGMC_ERR_UNSUPPORTED,
+                     "mlp_resgld_plan_create: kept samples need "
+                     "gbsgmc_mlp_resgld_plan_create_keep");
+  return gbsgmc_mlp_resgld_plan_create_keep(out, model, replicas, n_max, n_dev, x_dev, v_dev,
+                                            alpha, lmbd, sched, noise, isrc, temp, U_dev,
+                                            lk_var_dev, nullptr, nullptr, block_steps,
+                                            status_dev);
+}
+
+extern "C" int gbsgmc_mlp_resgld_plan_create_keep(
+    gbsgmc_plan** out, const gbsgmc_mlp* model, int replicas, int n_max, const int32_t* n_dev,
+    float* x_dev, float* v_dev, float alpha, float lmbd, const gbsgmc_sched* sched,
+    const gbsgmc_noise* noise, const gbsgmc_index_src* isrc, const gbsgmc_tempering* temp,
+    double* U_dev, double* lk_var_dev, float* samples_dev, double* sample_lik_dev,
+    int block_steps, int* status_dev) {
   if (out == nullptr) return set_error(GBSGMC_ERR_ARG, "mlp_resgld_plan_create: null plan");
   *out = nullptr;
   if (model == nullptr || n_dev == nullptr || x_dev == nullptr || sched == nullptr ||
@@ -574,9 +598,9 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
     return set_error(GBSGMC_ERR_ARG,
                      "mlp_resgld_plan_create: bad replicas, sizes or exchange period "
                      "(block_steps must be a multiple of every)");
-  if (sched->keep_slot_dev != nullptr)
-    return set_error(GBSGMC_ERR_UNSUPPORTED,
-                     "mlp_resgld_plan_create: samples are collected by the caller");
+  if ((sched->keep_slot_dev != nullptr) != (samples_dev != nullptr))
+    return set_error(GBSGMC_ERR_ARG,
+                     "mlp_resgld_plan_create: a keep table and a sample buffer go together");
   if (isrc->external)
     return set_error(GBSGMC_ERR_UNSUPPORTED,
                      "mlp_resgld_plan_create: external index sources");
@@ -599,6 +623,8 @@ extern "C" int gbsgmc_mlp_resgld_plan_create(
   p->temp = *temp;
   p->U = U_dev;
   p->lk_var = lk_var_dev;
+  p->samples = samples_dev;
+  p->sample_lik = sample_lik_dev;
   p->status = status_dev;
   p->ws_size = ws;
   int rc = GBSGMC_OK;

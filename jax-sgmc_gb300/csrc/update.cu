@@ -973,6 +973,27 @@ namespace gbsgmc {
 
 int update_blocks(int chains, int64_t P) { return static_cast<int>(grid4(chains, P).grid.x); }
 
+// At kept steps (the schedule's keep slot >= 0) row 0 of x [., P] is copied to
+// samples [slot, P] and -U[0] to sample_lik[slot].
+__global__ void keep_row_kernel(int64_t P, const float* __restrict__ x,
+                                const double* __restrict__ U, Sched sched, float* samples,
+                                double* sample_lik) {
+  const int slot = sched.keep_slot(sched.step());
+  if (slot < 0) return;
+  for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < P;
+       j += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    samples[static_cast<int64_t>(slot) * P + j] = x[j];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && sample_lik != nullptr)
+    sample_lik[slot] = -U[0];
+}
+
+int keep_row(int64_t P, const float* x, const double* U, const gbsgmc_sched* sched,
+             float* samples, double* sample_lik, cudaStream_t st) {
+  const int blocks = static_cast<int>(std::min<int64_t>((P + 1023) / 1024, 1024));
+  keep_row_kernel<<<blocks, 256, 0, st>>>(P, x, U, to_sched(sched), samples, sample_lik);
+  return check_launch("keep_row");
+}
+
 int sgld_update_fused(int chains, int64_t P, float* x, const float* g, float* v,
                       float alpha, float lmbd, const gbsgmc_sched* sched,
                       const gbsgmc_noise* noise, const UpdateFusion& f, cudaStream_t st) {

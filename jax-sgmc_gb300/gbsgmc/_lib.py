@@ -219,6 +219,10 @@ SIGNATURES = {
                                            _vp, _f, _f, _P(Sched), _P(Noise),
                                            _P(IndexSrc), _P(Tempering), _vp,
                                            _vp, _i, _vp]),
+    "gbsgmc_mlp_resgld_plan_create_keep": (_i, [_P(_vp), _P(Mlp), _i, _i, _vp, _vp,
+                                                _vp, _f, _f, _P(Sched), _P(Noise),
+                                                _P(IndexSrc), _P(Tempering), _vp,
+                                                _vp, _vp, _vp, _i, _vp]),
     "gbsgmc_mlp_resgld_pairs_plan_create": (_i, [_P(_vp), _P(Mlp), _i, _i, _vp, _vp,
                                                  _f, _f, _P(Sched), _P(Noise),
                                                  _P(IndexSrc), _P(Tempering), _vp, _vp,

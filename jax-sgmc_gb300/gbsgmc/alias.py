@@ -97,6 +97,98 @@ def re_sgld(potential_fn, data_loader, cache_size: int = 512,
   return run_fn
 
 
+def re_sgld_ladder(potential_fn, data_loader, temperatures,
+                   batch_sizes=None, batch_size: int = 32,
+                   exchange_every: int = 1, F: float = 1.0,
+                   first_step_size: float = 0.05, last_step_size: float = 0.001,
+                   burn_in: int = 0, accepted_samples: int = 100,
+                   rms_prop: bool = False, alpha: float = 0.9,
+                   lmbd: float = 1e-5, save_to_numpy: bool = True,
+                   seed: int = 0):
+  """Replica-exchange SGLD over a ladder of R >= 2 temperatures: the
+  generalisation of :func:`re_sgld`'s (normal, hot) pair (alias.py:122-208,
+  solver.py:220-299) to R replicas at ``temperatures`` (coldest first; the
+  first is the sampled chain, usually 1), each with its own minibatch size
+  (``batch_sizes``, default ``batch_size`` for all), in which adjacent
+  replicas attempt the reference's FP64 exchange every ``exchange_every``
+  steps (pair parity alternating), each pair keeping its own stochastic-
+  approximation variance estimate.  SGLD, with RMSprop when ``rms_prop``.
+  No reference counterpart beyond R = 2.  On the MLP likelihood the ladder
+  runs as one graph-captured plan (``gbsgmc_mlp_resgld_plan_create_keep``);
+  ``run_fn(init_sample, iterations=K)`` starts every replica at
+  ``init_sample`` (or at ``init_samples`` given one per replica) and
+  returns one result dict, the kept samples of the coldest replica, in the
+  reference's format.  K must be a multiple of ``exchange_every``.  Index
+  streams are the loader's numpy pipelines, one per replica, each drawing
+  ``max(batch_sizes)`` rounded up to 128 rows per step of which the replica
+  uses its own count."""
+  import numpy as np
+  from . import engine, util
+  from . import scheduler as sched_mod
+  temps = np.asarray(temperatures, np.float32).reshape(-1)
+  R = temps.size
+  if R < 2:
+    raise ValueError("a ladder needs at least two temperatures")
+  if not getattr(potential_fn, "is_mlp", False):
+    raise NotImplementedError("the replica ladder runs on the MLP likelihood")
+  rows = np.full(R, batch_size, np.int32) if batch_sizes is None else \
+      np.asarray(batch_sizes, np.int32).reshape(-1)
+  if rows.size != R or (rows < 1).any():
+    raise ValueError("one positive minibatch size per temperature")
+  n_max = int((rows.max() + 127) // 128 * 128)
+  every = int(exchange_every)
+  if every < 1:
+    raise ValueError("exchange_every must be positive")
+  schedule = _schedule(first_step_size, last_step_size, burn_in,
+                       accepted_samples, False)
+
+  def run_fn(*init_samples, iterations=1000):
+    import torch
+    if iterations % every != 0:
+      raise ValueError(f"iterations ({iterations}) must be a multiple of "
+                       f"exchange_every ({every})")
+    if len(init_samples) not in (1, R):
+      raise ValueError(f"one initial sample, or one per replica ({R})")
+    flats = [util.ravel(s) for s in init_samples]
+    tdef = flats[0][1]
+    Xh = np.stack([f[0] for f in flats]).astype(np.float32)
+    if Xh.shape[0] == 1:
+      Xh = np.repeat(Xh, R, axis=0)
+    ds = data_loader.device_dataset()
+    if Xh.shape[1] != potential_fn.dim(ds):
+      raise ValueError(f"samples have {Xh.shape[1]} parameters, the network "
+                       f"{potential_fn.dim(ds)}")
+    ids, words = data_loader.register_random_pipelines(R, cache_size=1,
+                                                       mb_size=n_max)
+    pcg = torch.from_numpy(np.ascontiguousarray(words).view(np.int64)).cuda()
+    h, t, keep, n_kept, _ = sched_mod.tables(schedule, iterations)
+    tabs = [torch.from_numpy(np.ascontiguousarray(a)).cuda()
+            for a in (np.asarray(h, np.float32), np.asarray(t, np.float32),
+                      np.asarray(keep, np.int32))]
+    X = torch.from_numpy(Xh).cuda()
+    V = torch.ones_like(X) if rms_prop else None
+    plan = engine.ResgldPlan(potential_fn, ds, X, V, rows, n_max, temps, tabs[0],
+                             tabs[1], engine.IndexSource(pcg=pcg, chain_base=int(ids[0])),
+                             noise_seed=seed, swap_seed=seed, every=every, F=F,
+                             alpha=alpha, lmbd=lmbd, chain_base=int(ids[0]),
+                             keep_tab=tabs[2], n_kept=n_kept)
+    try:
+      if iterations:
+        plan.run(0, iterations)
+      plan.check_status()
+      samples = plan.samples[:n_kept].reshape(n_kept, 1, -1)
+      lik = plan.sample_lik[:n_kept].reshape(n_kept, 1)
+      run_fn.exchanges = plan.counts.cpu().numpy()
+    finally:
+      plan.close()
+    return io.postprocess_chains(io.save(io.MemoryCollector()) if save_to_numpy
+                                 else io.no_save(), n_kept, samples, [tdef],
+                                 {"likelihood": lik}, [None])
+
+  run_fn.exchanges = None
+  return run_fn
+
+
 def sghmc(potential_fn, data_loader, cache_size: int = 512,
           batch_size: int = 32, integration_steps: int = 10,
           friction: Union[float, Pytree] = 1.0, mass: Pytree = None,

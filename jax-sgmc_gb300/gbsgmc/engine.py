@@ -329,7 +329,7 @@ class ResgldPlan:
   def __init__(self, potential, dataset, X, V, rows, n_max, ladder, h_tab,
                t_tab, index_src, noise_seed, swap_seed, every=50, F=1.0,
                alpha=0.9, lmbd=1e-5, chain_base=0, block_steps=None,
-               observation_count=None):
+               observation_count=None, keep_tab=None, n_kept=0):
     import torch
     R, P = X.shape
     self.R, self.P = R, P
@@ -344,10 +344,15 @@ class ResgldPlan:
     self.counts = torch.zeros(R - 1, dtype=torch.int32, device="cuda")
     self.flags = torch.zeros(R - 1, dtype=torch.int32, device="cuda")
     self.status = torch.zeros(1, dtype=torch.int32, device="cuda")
-    self.h_tab, self.t_tab = h_tab, t_tab
+    self.h_tab, self.t_tab, self.keep_tab = h_tab, t_tab, keep_tab
     self.index_src = index_src
+    # Kept states of replica 0 (after each kept step's exchange attempt).
+    self.samples = self.sample_lik = None
+    if keep_tab is not None:
+      self.samples = torch.empty((max(int(n_kept), 1), P), dtype=torch.float32, device="cuda")
+      self.sample_lik = torch.empty(max(int(n_kept), 1), dtype=torch.float64, device="cuda")
     self.sched = _lib.sched(step_size_dev=h_tab, temperature_dev=t_tab,
-                            chain_temperature_dev=self.ladder)
+                            keep_slot_dev=keep_tab, chain_temperature_dev=self.ladder)
     self.noise = _lib.noise(noise_seed, chain_base)
     self.temp = _lib.Tempering(int(every), 0, float(F), int(swap_seed) & (2**64 - 1),
                                _lib.ptr(self.ssq), _lib.ptr(self.k),
@@ -355,11 +360,12 @@ class ResgldPlan:
     if block_steps is None:
       block_steps = every * max(1, DEFAULT_BLOCK_STEPS // every)
     handle = _lib.C.c_void_p()
-    _lib.call("gbsgmc_mlp_resgld_plan_create", _lib.C.byref(handle), self.model,
+    _lib.call("gbsgmc_mlp_resgld_plan_create_keep", _lib.C.byref(handle), self.model,
               R, int(n_max), _lib.ptr(self.rows), _lib.ptr(X), _lib.ptr(V),
               float(alpha), float(lmbd), self.sched, self.noise,
               index_src.struct, self.temp, _lib.ptr(self.U),
-              _lib.ptr(self.lk_var), int(block_steps), _lib.ptr(self.status))
+              _lib.ptr(self.lk_var), _lib.ptr(self.samples), _lib.ptr(self.sample_lik),
+              int(block_steps), _lib.ptr(self.status))
     self.handle = handle
 
   def run(self, first_step, steps):
