@@ -22,8 +22,14 @@
 //                                         HWIO gradient directly
 //   inputs   dCol = dY W^T                 A = dY (K-major), B = W (K-major)
 // then col2im (the 9-tap sum), the pooling's argmax routing and the ReLU
-// mask in one pass.  The ReLU outputs are kept in fp32 so that the pooling
-// picks its maximum from unrounded values; everything a GEMM reads is BF16.  Channel and K padding come from the tensor maps'
+// mask in one pass.  The forward GEMMs' epilogues apply bias and ReLU and
+// the 2x2 max-pool to the fp32 accumulators themselves (EpiConvPool): each
+// epilogue warp holds whole pool windows in its 32 rows, so it writes the
+// pooled BF16 map and the argmax marks and no pre-pool activation is
+// stored.  For that the rows of conv1's GEMM (32 x 32 pixels) are ordered in
+// 16-pixel half rows, two image rows per 32 GEMM rows (conv1_row); conv2's
+// natural order (16 x 16) and conv3's (8 x 8) already have that property.
+// Everything a GEMM reads is BF16.  Channel and K padding come from the tensor maps'
 // out-of-bounds zero fill; epilogues drop rows and columns past the real
 // extents.  The dense layer, softmax and their adjoints are small and run on
 // the CUDA cores in fp32.
@@ -58,7 +64,6 @@ static_assert(kP == 113738, "parameter count");
 struct CnnLayout {
   size_t w1b, w2b, w3b;               // BF16 HWIO copies
   size_t col1, p1, col2, p2, col3, p3;  // BF16 GEMM operands
-  size_t a1, a2, a3;                  // fp32 pre-pool activations (ReLU output)
   size_t dy1, dy2, dy3;               // BF16 output gradients of the convs
   size_t m1, m2, m3;                  // uint8 argmax of each pool window
   size_t dcol3, dcol2;                // BF16 input-gradient columns
@@ -90,15 +95,12 @@ CnnLayout cnn_layout(int chains, int n) {
   L.w2b = take(2 * kK2 * kC2);
   L.w3b = take(2 * kK3 * kC3);
   L.col1 = take(2 * N * 1024 * kK1p);
-  L.a1 = take(4 * N * 1024 * kC1);
   L.dy1 = take(2 * N * 1024 * kA1ld);
   L.p1 = take(2 * N * 256 * kC1);
   L.col2 = take(2 * N * 256 * kK2p);
-  L.a2 = take(4 * N * 256 * kC2);
   L.dy2 = take(2 * N * 256 * kC2);
   L.p2 = take(2 * N * 64 * kC2);
   L.col3 = take(2 * N * 64 * kK3p);
-  L.a3 = take(4 * N * 64 * kC3);
   L.dy3 = take(2 * N * 64 * kC3);
   L.p3 = take(2 * N * 16 * kC3);
   L.m1 = take(N * 256 * kC1);
@@ -141,7 +143,6 @@ struct CnnArgs {
   double* lk_var;
   int* status;
   bf16 *w1b, *w2b, *w3b, *col1, *p1, *col2, *p2, *col3, *p3, *dcol3, *dcol2;
-  float *a1, *a2, *a3;
   bf16 *dy1, *dy2, *dy3;
   uint8_t *m1, *m2, *m3;
   int32_t* lab;
@@ -175,9 +176,19 @@ __global__ void __launch_bounds__(256) cnn_prep_kernel(const CnnArgs a) {
   if (threadIdx.x == 0) a.psq[c * kPrepBlocks + blockIdx.x] = tot;
 }
 
+// Row of pixel (h, w) of a 32 x 32 image in conv1's GEMM (and in its output
+// gradient dY1): rows come in blocks of 32, block b holding the half row
+// w in [16 (b & 1), 16 (b & 1) + 16) of image rows 2 (b >> 1) (lanes 0-15)
+// and 2 (b >> 1) + 1 (lanes 16-31), so that every 2 x 2 pool window lies in
+// one block, at lanes (l, l ^ 1, l ^ 16, l ^ 17).
+__host__ __device__ __forceinline__ int conv1_row(int h, int w) {
+  return (((h >> 1) << 1) | (w >> 4)) * 32 + ((h & 1) << 4) + (w & 15);
+}
+
 // ---------------------------------------------------------------------------
 // Gather of the minibatch images straight into conv1's im2col matrix
-// Col1 [n*1024, 64] (K = (kh, kw, ci), 27 real), plus labels.
+// Col1 [n*1024, 64] (K = (kh, kw, ci), 27 real; rows in conv1_row order),
+// plus labels.
 // Grid (n*1024/256, chains): one thread per output pixel.  (Eight threads
 // per row, each storing one 16-byte group, measured twice as slow.)
 // ---------------------------------------------------------------------------
@@ -222,57 +233,11 @@ __global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
     const __nv_bfloat162 pr = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
     out[k] = *reinterpret_cast<const uint32_t*>(&pr);
   }
-  uint4* dst = reinterpret_cast<uint4*>(a.col1 + (static_cast<int64_t>(c) * a.n * 1024 + p) * kK1p);
+  uint4* dst = reinterpret_cast<uint4*>(
+      a.col1 + (static_cast<int64_t>(c) * a.n * 1024 + i * 1024 + conv1_row(h, wq)) * kK1p);
 #pragma unroll
   for (int k = 0; k < kK1p / 8; ++k)
     dst[k] = make_uint4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
-}
-
-// ---------------------------------------------------------------------------
-// 2x2 max-pool: A [n, H, W, ld] (C real channels) -> P [n, H/2, W/2, C], and
-// per output the argmax (bits 0-1: 0..3, row-major in the window, first
-// maximum) and bit 2 = (maximum > 0), the ReLU mask of the element the
-// backward pass routes the gradient to.  One thread per output pixel and four
-// channels (128-bit loads of A, 64-bit stores of P, 32-bit of M); C and ld
-// are multiples of 4.  Grid (ceil(n*H*W*C/16 / 256), chains).
-// ---------------------------------------------------------------------------
-template <int H, int W, int C, int ld>
-__global__ void __launch_bounds__(256) cnn_pool_kernel(const float* A, bf16* Pout, uint8_t* M,
-                                                      int n) {
-  // Per-chain element counts stay below 2^31: 32-bit index arithmetic.
-  const int c = blockIdx.y;
-  const int Ho = H / 2, Wo = W / 2;
-  const int per = n * Ho * Wo * C;
-  const int e = (blockIdx.x * 256 + threadIdx.x) * 4;
-  if (e >= per) return;
-  const int ch = e % C;
-  const int pix = e / C;
-  const int x = pix % Wo, y = (pix / Wo) % Ho;
-  const int i = pix / (Wo * Ho);
-  const float* src = A + static_cast<int64_t>(c) * n * H * W * ld +
-                     ((i * H + 2 * y) * W + 2 * x) * ld + ch;
-  const float4 w0 = *reinterpret_cast<const float4*>(src);
-  const float4 w1 = *reinterpret_cast<const float4*>(src + ld);
-  const float4 w2 = *reinterpret_cast<const float4*>(src + W * ld);
-  const float4 w3 = *reinterpret_cast<const float4*>(src + W * ld + ld);
-  const float a0[4] = {w0.x, w0.y, w0.z, w0.w}, a1[4] = {w1.x, w1.y, w1.z, w1.w};
-  const float a2[4] = {w2.x, w2.y, w2.z, w2.w}, a3[4] = {w3.x, w3.y, w3.z, w3.w};
-  __nv_bfloat162 out[2];
-  uint32_t marks = 0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    float best = a0[k];
-    int arg = 0;
-    if (a1[k] > best) { best = a1[k]; arg = 1; }
-    if (a2[k] > best) { best = a2[k]; arg = 2; }
-    if (a3[k] > best) { best = a3[k]; arg = 3; }
-    marks |= static_cast<uint32_t>(arg | (best > 0.f ? 4 : 0)) << (8 * k);
-    const bf16 b = __float2bfloat16_rn(best);
-    if (k & 1) out[k >> 1].y = b; else out[k >> 1].x = b;
-  }
-  *reinterpret_cast<uint2*>(Pout + static_cast<int64_t>(c) * per + e) =
-      *reinterpret_cast<const uint2*>(out);
-  *reinterpret_cast<uint32_t*>(M + static_cast<int64_t>(c) * per + e) = marks;
 }
 
 // ---------------------------------------------------------------------------
@@ -420,7 +385,8 @@ __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
 //        layer's input-gradient columns dCol [n*Ho*Wo, Kp])
 // goes to the window element its argmax chose if that element was positive
 // (the pool's mark byte, bits 0-1 and 2); the three others (and channels
-// C..ld-1) get 0:  dY [n, H, W, ld] BF16.  One thread per pooled pixel and
+// C..ld-1) get 0:  dY [n, H, W, ld] BF16 (rows in conv1_row order for
+// layer 1, kConv1Rows).  One thread per pooled pixel and
 // eight channels: 128-bit loads of dCol / dp, 64-bit of the marks, 128-bit
 // stores of dY; C, ld and Kp are multiples of 8.  32-bit index arithmetic
 // (per-chain counts < 2^31).  Grid (ceil(n*Ho*Wo*C/8 / 256), chains).
@@ -431,7 +397,7 @@ __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
 // blocks.  2048 / C threads of a block share a channel group (256 * 8 is a
 // multiple of C, so the channel of thread t is 8 t mod C).
 // ---------------------------------------------------------------------------
-template <int H, int W, int C, int ld, int Kp>
+template <int H, int W, int C, int ld, int Kp, bool kConv1Rows = false>
 __global__ void __launch_bounds__(256) cnn_unpool_kernel(bf16* dY, const uint8_t* M,
                                                         const float* dp, const bf16* dcol,
                                                         int n, float* bpart) {
@@ -479,7 +445,7 @@ __global__ void __launch_bounds__(256) cnn_unpool_kernel(bf16* dY, const uint8_t
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int y = 2 * py + (q >> 1), x = 2 * px + (q & 1);
-    const int off = ((i * H + y) * W + x) * ld;
+    const int off = (kConv1Rows ? i * H * W + conv1_row(y, x) : (i * H + y) * W + x) * ld;
     __nv_bfloat162 o[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -606,33 +572,85 @@ __device__ __forceinline__ void store_block32(uint32_t* dst, int64_t ld_words,
   }
 }
 
-// Forward: Y = ReLU(acc + b) in fp32 into [rows, ldo]; columns >= C get 0.
-// (fp32 so that the pooling's maximum is taken over unrounded values.)
-struct EpiConvRelu {
+// Forward: ReLU(acc + b) in fp32 and the 2 x 2 max-pool of it, straight from
+// the accumulator.  A warp's 32 rows hold whole pool windows: the window of
+// lane l is lanes (base, base + 1, base + V, base + V + 1), base = l & ~(V | 1),
+// in row-major window order, with V = 16 for conv1 (conv1_row order) and
+// conv2 (16 pixels per image row) and V = 8 for conv3 (8 per row).  Per
+// output the maximum (first one in window order, as jax's max-pool argmax
+// routes the gradient) goes to P [n, Ho, Wo, C] as BF16 and the mark byte
+// to M: bits 0-1 the argmax, bit 2 (maximum > 0), the ReLU mask of the
+// element the backward pass routes the gradient to.  The four lanes of a
+// window each write 8 of every 32 channels (16-byte P stores, 8-byte mark
+// stores).  Columns >= C (conv1's padding to N = 64) are skipped.
+template <int H, int W, int V, bool kConv1Rows>
+struct EpiConvPool {
   const float* w;
   int64_t boff;
-  int C, ldo;
-  int64_t rows;  // rows per chain
-  float* y;
+  int C;
+  bf16* P;
+  uint8_t* M;
+  int n;
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
-                                       uint32_t* st) const {
-    if (col0 >= ldo) return;  // columns past the stored width (warp-uniform)
+                                       uint32_t*) const {
+    if (col0 >= C) return;  // padding columns (warp-uniform)
+    const unsigned full = 0xffffffffu;
+    const int lane = epi::lane_id();
+    const int base = lane & ~(V | 1);
+    const int wp = ((lane & V) ? 2 : 0) | (lane & 1);
+    // The window's pooled pixel, from the row of its first lane.
+    const int r = row0 + base;
+    const int i = r / (H * W), rr = r % (H * W);
+    int yp, xp;
+    if (kConv1Rows) {
+      const int blk = rr >> 5, l = rr & 31;
+      yp = blk >> 1;
+      xp = ((blk & 1) * 16 + (l & 15)) >> 1;
+    } else {
+      yp = (rr / W) >> 1;
+      xp = (rr % W) >> 1;
+    }
+    const int64_t pix = (static_cast<int64_t>(b) * n + i) * (H / 2) * (W / 2) +
+                        yp * (W / 2) + xp;
     const float* bias = w + b * kP + boff;
-    float* dst = y + (b * rows + row0) * ldo + col0 + epi::lane_id();
 #pragma unroll 1
     for (int cb = 0; cb < NC / 32; ++cb) {
+      const int k0 = col0 + 32 * cb;
+      const float bl = __ldg(bias + k0 + lane);
       float v[32];
-      uint32_t u[32];
       load(cb, v);
+      float best_mine[8];
+      uint32_t mark_mine[8];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const int k = col0 + 32 * cb + j;
-        u[j] = __float_as_uint(k < C ? fmaxf(v[j] + __ldg(bias + k), 0.f) : 0.f);
+        const float x = fmaxf(v[j] + __shfl_sync(full, bl, j), 0.f);
+        const float a0 = __shfl_sync(full, x, base);
+        const float a1 = __shfl_sync(full, x, base + 1);
+        const float a2 = __shfl_sync(full, x, base + V);
+        const float a3 = __shfl_sync(full, x, base + V + 1);
+        float best = a0;
+        uint32_t arg = 0;
+        if (a1 > best) { best = a1; arg = 1; }
+        if (a2 > best) { best = a2; arg = 2; }
+        if (a3 > best) { best = a3; arg = 3; }
+        if ((j >> 3) == wp) {
+          best_mine[j & 7] = best;
+          mark_mine[j & 7] = arg | (best > 0.f ? 4u : 0u);
+        }
       }
-      epi::put_rows(st, u);
-#pragma unroll 4
-      for (int r = 0; r < 32; ++r) dst[r * ldo + 32 * cb] = __uint_as_float(epi::get(st, r));
+      uint32_t pk[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const __nv_bfloat162 pr = __floats2bfloat162_rn(best_mine[2 * e], best_mine[2 * e + 1]);
+        pk[e] = *reinterpret_cast<const uint32_t*>(&pr);
+      }
+      const int64_t at = pix * C + k0 + 8 * wp;
+      *reinterpret_cast<uint4*>(P + at) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      uint2 mk;
+      mk.x = mark_mine[0] | (mark_mine[1] << 8) | (mark_mine[2] << 16) | (mark_mine[3] << 24);
+      mk.y = mark_mine[4] | (mark_mine[5] << 8) | (mark_mine[6] << 16) | (mark_mine[7] << 24);
+      *reinterpret_cast<uint2*>(M + at) = mk;
     }
   }
 };
@@ -699,15 +717,12 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   a.w2b = view<bf16>(ws, L.w2b);
   a.w3b = view<bf16>(ws, L.w3b);
   a.col1 = view<bf16>(ws, L.col1);
-  a.a1 = view<float>(ws, L.a1);
   a.dy1 = view<bf16>(ws, L.dy1);
   a.p1 = view<bf16>(ws, L.p1);
   a.col2 = view<bf16>(ws, L.col2);
-  a.a2 = view<float>(ws, L.a2);
   a.dy2 = view<bf16>(ws, L.dy2);
   a.p2 = view<bf16>(ws, L.p2);
   a.col3 = view<bf16>(ws, L.col3);
-  a.a3 = view<float>(ws, L.a3);
   a.dy3 = view<bf16>(ws, L.dy3);
   a.p3 = view<bf16>(ws, L.p3);
   a.m1 = view<uint8_t>(ws, L.m1);
@@ -766,33 +781,25 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
       (rc = make_tmap_bf16_3d(&m_w3, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, 64, 64)))
     return rc;
 
-  // conv1 -> pool1 -> im2col2 -> conv2 -> pool2 -> im2col3 -> conv3 -> pool3.
-  // conv1 runs as N = 64 (the weight map's zero fill beyond 32 channels);
-  // the epilogue stores the 32 real columns.
-  const EpiConvRelu e1{a.w, ob1, kC1, kC1, r1, a.a1};
+  // conv1+pool1 -> im2col2 -> conv2+pool2 -> im2col3 -> conv3+pool3: each
+  // conv GEMM's epilogue writes the pooled BF16 map and the marks.  conv1
+  // runs as N = 64 (the weight map's zero fill beyond 32 channels); its
+  // epilogue skips the padding columns.
+  const EpiConvPool<32, 32, 16, true> e1{a.w, ob1, kC1, a.p1, a.m1, n};
   if ((rc = launch_gemm<64, false, true>(m_col1, m_w1, C, r1, 64, kK1p, a.status, e1, st)))
     return rc;
-  cnn_pool_kernel<32, 32, kC1, kC1><<<dim3(grid1(r2 * kC1 / 4), C), 256, 0, st>>>(a.a1, a.p1,
-                                                                                 a.m1, n);
-  if ((rc = launched("cnn_pool_kernel 1"))) return rc;
   cnn_im2col_kernel<16, 16, kC1, kK2p><<<dim3(grid1(r2 * kK2p / 8), C), 256, 0, st>>>(
       a.p1, a.col2, n);
   if ((rc = launched("cnn_im2col_kernel 2"))) return rc;
-  const EpiConvRelu e2{a.w, ob2, kC2, kC2, r2, a.a2};
+  const EpiConvPool<16, 16, 16, false> e2{a.w, ob2, kC2, a.p2, a.m2, n};
   if ((rc = launch_gemm<64, false, true>(m_col2, m_w2, C, r2, kC2, kK2p, a.status, e2, st)))
     return rc;
-  cnn_pool_kernel<16, 16, kC2, kC2><<<dim3(grid1(r3 * kC2 / 4), C), 256, 0, st>>>(a.a2, a.p2,
-                                                                                 a.m2, n);
-  if ((rc = launched("cnn_pool_kernel 2"))) return rc;
   cnn_im2col_kernel<8, 8, kC2, kK3p><<<dim3(grid1(r3 * kK3p / 8), C), 256, 0, st>>>(
       a.p2, a.col3, n);
   if ((rc = launched("cnn_im2col_kernel 3"))) return rc;
-  const EpiConvRelu e3{a.w, ob3, kC3, kC3, r3, a.a3};
+  const EpiConvPool<8, 8, 8, false> e3{a.w, ob3, kC3, a.p3, a.m3, n};
   if ((rc = launch_gemm<128, false, true>(m_col3, m_w3, C, r3, kC3, kK3p, a.status, e3, st)))
     return rc;
-  cnn_pool_kernel<8, 8, kC3, kC3><<<dim3(grid1(int64_t(n) * 16 * kC3 / 4), C), 256, 0, st>>>(
-      a.a3, a.p3, a.m3, n);
-  if ((rc = launched("cnn_pool_kernel 3"))) return rc;
   cnn_dense_kernel<<<dim3(n, C), 128, 0, st>>>(a);
   if ((rc = launched("cnn_dense_kernel"))) return rc;
 
@@ -828,7 +835,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     if ((rc = launch_gemm<64, false, false>(m_dy2, m_w2k, C, r2, kK2p, kC2, a.status, d2, st)))
       return rc;
     // Layer 1.
-    cnn_unpool_kernel<32, 32, kC1, kA1ld, kK2p><<<unpool_grid(32, kC1), 256, 0, st>>>(
+    cnn_unpool_kernel<32, 32, kC1, kA1ld, kK2p, true><<<unpool_grid(32, kC1), 256, 0, st>>>(
         a.dy1, a.m1, nullptr, a.dcol2, n, a.bpart);
     if ((rc = launched("cnn_unpool_kernel 1")) || (rc = bias_sum(32, kC1, ob1))) return rc;
     CUtensorMap m_dy1t, m_col1t;
