@@ -14,15 +14,21 @@
 //   b1 32 | W1 [3,3,3,32] | b2 64 | W2 [3,3,32,64] | b3 128 | W3 [3,3,64,128]
 //   | bd 10 | Wd [2048,10],   P = 113,738.
 //
-// Each convolution is a GEMM over an im2col matrix Col [pixels, K] with K
+// Each convolution is a GEMM over the im2col matrix Col [pixels, K] with K
 // ordered (kh, kw, ci) and zero-padded to a multiple of 64:
 //   forward  Y = ReLU(Col W + b)          A = Col (K-major), B = W (HWIO rows
 //                                         = K, MN-major)
 //   weights  dW = dY^T Col                 both MN-major; written into the
 //                                         HWIO gradient directly
-//   inputs   dCol = dY W^T                 A = dY (K-major), B = W (K-major)
-// then col2im (the 9-tap sum), the pooling's argmax routing and the ReLU
-// mask in one pass.  The forward GEMMs' epilogues apply bias and ReLU and
+//   inputs   dX = sum over taps of dY shifted back by the tap times the tap's
+//            W^T (the transposed convolution), A = dY (K-major), B = W
+//            (K-major), then the pooling's argmax routing and the ReLU mask.
+// Col is materialised for conv1 and conv2 (3 and 32 input channels).  Where
+// a tap's input channels fill a 128-byte row (64 BF16: conv3's input P2 and
+// the output gradients dY2, dY3 of the transposed convolutions) the GEMMs
+// are implicit: each 64-wide K slice of A (or 64-wide N block of dW's B) is
+// one tap's box of the NHWC map, shifted by the tap and read by TMA from a
+// 4-D tensor map, whose out-of-bounds zero fill is the SAME padding.  The forward GEMMs' epilogues apply bias and ReLU and
 // the 2x2 max-pool to the fp32 accumulators themselves (EpiConvPool): each
 // epilogue warp holds whole pool windows in its 32 rows, so it writes the
 // pooled BF16 map and the argmax marks and no pre-pool activation is
@@ -52,7 +58,7 @@ constexpr int kC1 = 32, kC2 = 64, kC3 = 128;
 constexpr int kFlat = 4 * 4 * kC3;  // 2048
 constexpr int kK1 = 27, kK1p = 64;  // im2col widths (real, padded)
 constexpr int kK2 = 9 * kC1, kK2p = 320;
-constexpr int kK3 = 9 * kC2, kK3p = 576;
+constexpr int kK3 = 9 * kC2;  // conv3 reads P2 by tap: no padded im2col
 constexpr int kA1ld = 64;  // conv1 output-gradient channels as stored (32 real)
 
 // Offsets of the leaves in a chain's flat parameter vector.
@@ -63,10 +69,10 @@ static_assert(kP == 113738, "parameter count");
 
 struct CnnLayout {
   size_t w1b, w2b, w3b;               // BF16 HWIO copies
-  size_t col1, p1, col2, p2, col3, p3;  // BF16 GEMM operands
+  size_t col1, p1, col2, p2, p3;        // BF16 GEMM operands
   size_t dy1, dy2, dy3;               // BF16 output gradients of the convs
   size_t m1, m2, m3;                  // uint8 argmax of each pool window
-  size_t dcol3, dcol2;                // BF16 input-gradient columns
+  size_t dp2, dp1;                    // fp32 input gradients of conv3, conv2
   size_t labels;                      // int32
   size_t dp3, gl;                     // fp32 dP3 [n, 2048], dlogits [n, 10]
   size_t psq, plk;                    // fp64 partial sums
@@ -100,14 +106,13 @@ CnnLayout cnn_layout(int chains, int n) {
   L.col2 = take(2 * N * 256 * kK2p);
   L.dy2 = take(2 * N * 256 * kC2);
   L.p2 = take(2 * N * 64 * kC2);
-  L.col3 = take(2 * N * 64 * kK3p);
   L.dy3 = take(2 * N * 64 * kC3);
   L.p3 = take(2 * N * 16 * kC3);
   L.m1 = take(N * 256 * kC1);
   L.m2 = take(N * 64 * kC2);
   L.m3 = take(N * 16 * kC3);
-  L.dcol3 = take(2 * N * 64 * kK3p);
-  L.dcol2 = take(2 * N * 256 * kK2p);
+  L.dp2 = take(4 * N * 64 * kC2);
+  L.dp1 = take(4 * N * 256 * kC1);
   L.labels = take(4 * N);
   L.dp3 = take(4 * N * kFlat);
   L.gl = take(4 * N * kClasses);
@@ -142,7 +147,8 @@ struct CnnArgs {
   float* lk;
   double* lk_var;
   int* status;
-  bf16 *w1b, *w2b, *w3b, *col1, *p1, *col2, *p2, *col3, *p3, *dcol3, *dcol2;
+  bf16 *w1b, *w2b, *w3b, *col1, *p1, *col2, *p2, *p3;
+  float *dp2, *dp1;
   bf16 *dy1, *dy2, *dy3;
   uint8_t *m1, *m2, *m3;
   int32_t* lab;
@@ -379,17 +385,15 @@ __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
 
 // ---------------------------------------------------------------------------
 // Pool-window routing + ReLU mask: for each pooled element (i, py, px, ch),
-//   dP = dp[i, py, px, ch]                       (layer 3: fp32 dP3), or
-//   dP = sum over taps (kh, kw) of dCol[(i, py - kh + 1, px - kw + 1),
-//                                      (kh, kw, ch)]  (col2im of the next
-//        layer's input-gradient columns dCol [n*Ho*Wo, Kp])
-// goes to the window element its argmax chose if that element was positive
-// (the pool's mark byte, bits 0-1 and 2); the three others (and channels
+// the gradient dP = dp[i, py, px, ch] (fp32: the dense layer's adjoint for
+// layer 3, the transposed convolution's output for layers 2 and 1) goes to
+// the window element its argmax chose if that element was positive (the
+// pool's mark byte, bits 0-1 and 2); the three others (and channels
 // C..ld-1) get 0:  dY [n, H, W, ld] BF16 (rows in conv1_row order for
-// layer 1, kConv1Rows).  One thread per pooled pixel and
-// eight channels: 128-bit loads of dCol / dp, 64-bit of the marks, 128-bit
-// stores of dY; C, ld and Kp are multiples of 8.  32-bit index arithmetic
-// (per-chain counts < 2^31).  Grid (ceil(n*Ho*Wo*C/8 / 256), chains).
+// layer 1, kConv1Rows).  One thread per pooled pixel and eight channels:
+// 128-bit loads of dp, 64-bit of the marks, 128-bit stores of dY; C and ld
+// are multiples of 8.  32-bit index arithmetic (per-chain counts < 2^31).
+// Grid (ceil(n*Ho*Wo*C/8 / 256), chains).
 // The bias gradient is the column sum of dY, i.e. the sum over pooled
 // elements of the routed (BF16-rounded) values: each block adds its threads'
 // values per channel in a fixed order and writes
@@ -397,10 +401,9 @@ __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
 // blocks.  2048 / C threads of a block share a channel group (256 * 8 is a
 // multiple of C, so the channel of thread t is 8 t mod C).
 // ---------------------------------------------------------------------------
-template <int H, int W, int C, int ld, int Kp, bool kConv1Rows = false>
+template <int H, int W, int C, int ld, bool kConv1Rows = false>
 __global__ void __launch_bounds__(256) cnn_unpool_kernel(bf16* dY, const uint8_t* M,
-                                                        const float* dp, const bf16* dcol,
-                                                        int n, float* bpart) {
+                                                        const float* dp, int n, float* bpart) {
   __shared__ float red[256 * 8];
   const int c = blockIdx.y;
   const int Ho = H / 2, Wo = W / 2;
@@ -413,31 +416,11 @@ __global__ void __launch_bounds__(256) cnn_unpool_kernel(bf16* dY, const uint8_t
   const int pix = e / C;
   const int px = pix % Wo, py = (pix / Wo) % Ho, i = pix / (Wo * Ho);
   float g[8];
-  if (dp != nullptr) {
+  {
     const float4* d4 = reinterpret_cast<const float4*>(dp + static_cast<int64_t>(c) * pper + e);
     const float4 u = d4[0], v = d4[1];
     g[0] = u.x; g[1] = u.y; g[2] = u.z; g[3] = u.w;
     g[4] = v.x; g[5] = v.y; g[6] = v.z; g[7] = v.w;
-  } else {
-    const bf16* dc = dcol + static_cast<int64_t>(c) * n * Ho * Wo * Kp;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) g[k] = 0.f;
-#pragma unroll
-    for (int kh = 0; kh < 3; ++kh)
-#pragma unroll
-      for (int kw = 0; kw < 3; ++kw) {
-        const int oy = py - kh + 1, ox = px - kw + 1;
-        if (oy >= 0 && oy < Ho && ox >= 0 && ox < Wo) {
-          const uint4 t = *reinterpret_cast<const uint4*>(
-              dc + ((i * Ho + oy) * Wo + ox) * Kp + (kh * 3 + kw) * C + ch);
-          const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&t);
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            g[2 * k] += __low2float(h[k]);
-            g[2 * k + 1] += __high2float(h[k]);
-          }
-        }
-      }
   }
   const uint2 mk = *reinterpret_cast<const uint2*>(M + static_cast<int64_t>(c) * pper + e);
   const uint32_t marks[2] = {mk.x, mk.y};
@@ -554,24 +537,6 @@ __global__ void __launch_bounds__(256) cnn_finalize_kernel(const CnnArgs a, floa
 // GEMM epilogues.
 // ---------------------------------------------------------------------------
 
-// Stores 32 BF16 columns of the warp's 32 rows: lane l holds its row's 16
-// packed pairs w[16]; through the staging tile, each store instruction writes
-// 64 contiguous bytes of two rows.  dst points at (row0, first column) as
-// 32-bit words, rows ld_words apart.
-__device__ __forceinline__ void store_block32(uint32_t* dst, int64_t ld_words,
-                                              const uint32_t (&w)[16], uint32_t* st) {
-  const int lane = epi::lane_id(), h = lane >> 4, l = lane & 15;
-  __syncwarp();
-#pragma unroll
-  for (int j = 0; j < 16; ++j) st[lane * 33 + j] = w[j];
-  __syncwarp();
-#pragma unroll 4
-  for (int rr = 0; rr < 16; ++rr) {
-    const int r = 2 * rr + h;
-    dst[r * ld_words + l] = st[r * 33 + l];
-  }
-}
-
 // Forward: ReLU(acc + b) in fp32 and the 2 x 2 max-pool of it, straight from
 // the accumulator.  A warp's 32 rows hold whole pool windows: the window of
 // lane l is lanes (base, base + 1, base + V, base + V + 1), base = l & ~(V | 1),
@@ -681,27 +646,83 @@ struct EpiConvGradW {
   }
 };
 
-// dCol as BF16 into [rows, ldo] (all columns < ldo).
-struct EpiStoreBf16 {
-  bf16* y;
-  int ldo;
-  int64_t rows;
+// The transposed convolution's output dX as fp32 [rows, C] (columns >= C of
+// the N = 64 tile are skipped), one 128-byte row segment per store.
+struct EpiStoreDX {
+  float* dx;
+  int C;
+  int64_t rows;  // rows per chain
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
-    uint32_t* dst = reinterpret_cast<uint32_t*>(y + (b * rows + row0) * ldo + col0);
+    if (col0 >= C) return;  // padding columns (warp-uniform)
+    float* dst = dx + (b * rows + row0) * C + col0 + epi::lane_id();
 #pragma unroll 1
     for (int cb = 0; cb < NC / 32; ++cb) {
+      if (col0 + 32 * cb >= C) break;
       float v[32];
-      uint32_t pk[16];
+      uint32_t u[32];
       load(cb, v);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-        pk[j] = *reinterpret_cast<const uint32_t*>(&pr);
-      }
-      store_block32(dst + 16 * cb, ldo / 2, pk, st);
+      for (int j = 0; j < 32; ++j) u[j] = __float_as_uint(v[j]);
+      epi::put_rows(st, u);
+#pragma unroll 4
+      for (int r = 0; r < 32; ++r) dst[r * C + 32 * cb] = __uint_as_float(epi::get(st, r));
     }
+  }
+};
+
+// Implicit A operand: the K slice k0 of a GEMM over pixels (rows) and taps x
+// channels (K) is tap t = k0 / Ck, channels [k0 % Ck, + 64), of the NHWC map
+// shifted by the tap: the box (64 channels, W, rows / W, images) of a 4-D map
+// (Ck, W, H, chains * n) at (k0 % Ck, s (kw - 1), h0 + s (kh - 1), image),
+// s = +1 for a convolution and -1 for its transpose (the box reads zeros
+// outside the image: SAME padding).  A tile of 128 rows covers whole image
+// rows (W | 128) of one image, or whole images (H W | 128).
+template <class Inner>
+struct ImplicitA : Inner {
+  int H, W, Ck, sign, n;
+  static constexpr bool kLoadA = true;
+  __device__ __forceinline__ void load_a(void* dst, const CUtensorMap* map, int k0, int m0,
+                                         int b, uint64_t* bar) const {
+    const int tap = k0 / Ck, c0 = k0 - tap * Ck;
+    const int kh = tap / 3, kw = tap - 3 * kh;
+    const int img = m0 / (H * W), h0 = (m0 - img * H * W) / W;
+    tc::tma_load_4d(dst, map, c0, sign * (kw - 1), h0 + sign * (kh - 1), b * n + img, bar);
+  }
+};
+
+// Implicit MN-major B operand of a weight gradient dW = dY^T Col: the
+// 64-wide N block starting at column nn is tap t = nn / Ck, input channels
+// [nn % Ck, + 64), and the K slice k0 is 64 pixels (whole rows of one
+// image): the box (64 channels, W, 64 / W, 1) of the 4-D map of the
+// layer's input, shifted by the tap.
+template <class Inner>
+struct ImplicitBmn : Inner {
+  int H, W, Ck, n;
+  static constexpr bool kLoadB = true;
+  __device__ __forceinline__ void load_b(void* dst, const CUtensorMap* map, int nn, int k0,
+                                         int b, uint64_t* bar) const {
+    const int tap = nn / Ck, c0 = nn - tap * Ck;
+    const int kh = tap / 3, kw = tap - 3 * kh;
+    const int img = k0 / (H * W), h0 = (k0 - img * H * W) / W;
+    tc::tma_load_4d(dst, map, c0, kw - 1, h0 + kh - 1, b * n + img, bar);
+  }
+};
+
+// K-major B operand of a transposed convolution: for the K slice k0 (tap
+// t = k0 / Ckb, output channels [k0 % Ckb, + 64)) the rows n.. of W^T, i.e.
+// the box (64 output channels, 64 input channels, 1, 1) of the HWIO weights
+// as a 4-D map (Cout, Cin, 9, chains) at (k0 % Ckb, n, t, chain); input
+// channels past Cin read zeros.
+template <class Inner>
+struct TransposedB : Inner {
+  int Ckb;
+  static constexpr bool kLoadB = true;
+  __device__ __forceinline__ void load_b(void* dst, const CUtensorMap* map, int nn, int k0,
+                                         int b, uint64_t* bar) const {
+    const int tap = k0 / Ckb, c0 = k0 - tap * Ckb;
+    tc::tma_load_4d(dst, map, c0, nn, tap, b, bar);
   }
 };
 
@@ -722,14 +743,13 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   a.col2 = view<bf16>(ws, L.col2);
   a.dy2 = view<bf16>(ws, L.dy2);
   a.p2 = view<bf16>(ws, L.p2);
-  a.col3 = view<bf16>(ws, L.col3);
   a.dy3 = view<bf16>(ws, L.dy3);
   a.p3 = view<bf16>(ws, L.p3);
   a.m1 = view<uint8_t>(ws, L.m1);
   a.m2 = view<uint8_t>(ws, L.m2);
   a.m3 = view<uint8_t>(ws, L.m3);
-  a.dcol3 = view<bf16>(ws, L.dcol3);
-  a.dcol2 = view<bf16>(ws, L.dcol2);
+  a.dp2 = view<float>(ws, L.dp2);
+  a.dp1 = view<float>(ws, L.dp1);
   a.lab = view<int32_t>(ws, L.labels);
   a.dp3 = view<float>(ws, L.dp3);
   a.gl = view<float>(ws, L.gl);
@@ -771,17 +791,20 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   cnn_im2col1_kernel<<<dim3(grid1(r1), C), 256, 0, st>>>(a);
   if ((rc = launched("cnn_im2col1_kernel"))) return rc;
 
-  // Tensor maps (columns, rows, chains).
-  CUtensorMap m_col1, m_w1, m_col2, m_w2, m_col3, m_w3;
+  // Tensor maps (columns, rows, chains), and 4-D maps (channels, W, H,
+  // images) of the NHWC maps the implicit GEMMs read by tap.
+  const int64_t imgs = int64_t(C) * n;
+  CUtensorMap m_col1, m_w1, m_col2, m_w2, m_w3, m_p2a;
   if ((rc = make_tmap_bf16_3d(&m_col1, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, kGemmBK, kGemmBM)) ||
       (rc = make_tmap_bf16_3d(&m_w1, a.w1b, kC1, kK1, C, kC1, kK1 * kC1, 64, 64)) ||
       (rc = make_tmap_bf16_3d(&m_col2, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, kGemmBK, kGemmBM)) ||
       (rc = make_tmap_bf16_3d(&m_w2, a.w2b, kC2, kK2, C, kC2, kK2 * kC2, 64, 64)) ||
-      (rc = make_tmap_bf16_3d(&m_col3, a.col3, kK3p, r3, C, kK3p, r3 * kK3p, kGemmBK, kGemmBM)) ||
-      (rc = make_tmap_bf16_3d(&m_w3, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, 64, 64)))
+      (rc = make_tmap_bf16_3d(&m_w3, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, 64, 64)) ||
+      (rc = make_tmap_bf16_4d(&m_p2a, a.p2, {kC2, 8, 8, imgs}, {kC2, 8 * kC2, 64 * kC2},
+                              {64, 8, 8, 2})))
     return rc;
 
-  // conv1+pool1 -> im2col2 -> conv2+pool2 -> im2col3 -> conv3+pool3: each
+  // conv1+pool1 -> im2col2 -> conv2+pool2 -> conv3+pool3 (implicit): each
   // conv GEMM's epilogue writes the pooled BF16 map and the marks.  conv1
   // runs as N = 64 (the weight map's zero fill beyond 32 channels); its
   // epilogue skips the padding columns.
@@ -794,11 +817,10 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   const EpiConvPool<16, 16, 16, false> e2{a.w, ob2, kC2, a.p2, a.m2, n};
   if ((rc = launch_gemm<64, false, true>(m_col2, m_w2, C, r2, kC2, kK2p, a.status, e2, st)))
     return rc;
-  cnn_im2col_kernel<8, 8, kC2, kK3p><<<dim3(grid1(r3 * kK3p / 8), C), 256, 0, st>>>(
-      a.p2, a.col3, n);
-  if ((rc = launched("cnn_im2col_kernel 3"))) return rc;
-  const EpiConvPool<8, 8, 8, false> e3{a.w, ob3, kC3, a.p3, a.m3, n};
-  if ((rc = launch_gemm<128, false, true>(m_col3, m_w3, C, r3, kC3, kK3p, a.status, e3, st)))
+  // conv3, implicit: A tiles are P2's tap-shifted 2-image boxes.
+  const ImplicitA<EpiConvPool<8, 8, 8, false>> e3{{a.w, ob3, kC3, a.p3, a.m3, n},
+                                                   8, 8, kC2, 1, n};
+  if ((rc = launch_gemm<128, false, true>(m_p2a, m_w3, C, r3, kC3, kK3, a.status, e3, st)))
     return rc;
   cnn_dense_kernel<<<dim3(n, C), 128, 0, st>>>(a);
   if ((rc = launched("cnn_dense_kernel"))) return rc;
@@ -806,37 +828,57 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   if (a.want_grad) {
     cnn_dense_grad_kernel<<<dim3(kFlat / 128 + 1, C), 128, 0, st>>>(a);
     if ((rc = launched("cnn_dense_grad_kernel"))) return rc;
-    // Layer 3: dY3 over A3, db3, dW3 = dY3^T Col3, dCol3 = dY3 W3^T.
-    cnn_unpool_kernel<8, 8, kC3, kC3, 0><<<unpool_grid(8, kC3), 256, 0, st>>>(
-        a.dy3, a.m3, a.dp3, nullptr, n, a.bpart);
+    // Layer 3: dY3 (routing of dP3), db3, dW3 = dY3^T Col3 (implicit: B
+    // blocks are P2's tap-shifted images), dP2 = the transposed convolution
+    // of dY3 (implicit: A tiles are dY3's tap-shifted 2-image boxes).
+    cnn_unpool_kernel<8, 8, kC3, kC3><<<unpool_grid(8, kC3), 256, 0, st>>>(
+        a.dy3, a.m3, a.dp3, n, a.bpart);
     if ((rc = launched("cnn_unpool_kernel 3")) || (rc = bias_sum(8, kC3, ob3))) return rc;
-    CUtensorMap m_dy3t, m_col3t, m_dy3, m_w3k;
+    CUtensorMap m_dy3t, m_p2b, m_dy3a, m_w3t;
     if ((rc = make_tmap_bf16_3d(&m_dy3t, a.dy3, kC3, r3, C, kC3, r3 * kC3, 64, 64)) ||
-        (rc = make_tmap_bf16_3d(&m_col3t, a.col3, kK3p, r3, C, kK3p, r3 * kK3p, 64, 64)) ||
-        (rc = make_tmap_bf16_3d(&m_dy3, a.dy3, kC3, r3, C, kC3, r3 * kC3, kGemmBK, kGemmBM)) ||
-        (rc = make_tmap_bf16_3d(&m_w3k, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, kGemmBK, 64)))
+        (rc = make_tmap_bf16_4d(&m_p2b, a.p2, {kC2, 8, 8, imgs}, {kC2, 8 * kC2, 64 * kC2},
+                                {64, 8, 8, 1})) ||
+        (rc = make_tmap_bf16_4d(&m_dy3a, a.dy3, {kC3, 8, 8, imgs}, {kC3, 8 * kC3, 64 * kC3},
+                                {64, 8, 8, 2})) ||
+        (rc = make_tmap_bf16_4d(&m_w3t, a.w3b, {kC3, kC2, 9, C}, {kC3, kC2 * kC3, kK3 * kC3},
+                                {64, 64, 1, 1})))
       return rc;
-    if ((rc = weight_grad(m_dy3t, m_col3t, 3, kC3, kK3, kK3p, r3, oW3))) return rc;
-    const EpiStoreBf16 d3{a.dcol3, kK3p, r3};
-    if ((rc = launch_gemm<64, false, false>(m_dy3, m_w3k, C, r3, kK3p, kC3, a.status, d3, st)))
+    {
+      GemmRagged rg;
+      rg.ksplit = wsplit(3, n);
+      const ImplicitBmn<EpiConvGradW> e{{a.part, kC3, kK3}, 8, 8, kC2, n};
+      if ((rc = launch_gemm<64, true, true>(m_dy3t, m_p2b, C, 128, kK3, static_cast<int>(r3),
+                                            a.status, e, st, rg)))
+        return rc;
+      cnn_wsum_kernel<<<dim3(grid1(int64_t(kK3) * kC3), C), 256, 0, st>>>(a.part, rg.ksplit,
+                                                                          kK3 * kC3, a.grad, oW3);
+      if ((rc = launched("cnn_wsum_kernel"))) return rc;
+    }
+    const TransposedB<ImplicitA<EpiStoreDX>> d3{{{a.dp2, kC2, r3}, 8, 8, kC3, -1, n}, kC3};
+    if ((rc = launch_gemm<64, false, false>(m_dy3a, m_w3t, C, r3, kC2, 9 * kC3, a.status, d3,
+                                            st)))
       return rc;
-    // Layer 2.
-    cnn_unpool_kernel<16, 16, kC2, kC2, kK3p><<<unpool_grid(16, kC2), 256, 0, st>>>(
-        a.dy2, a.m2, nullptr, a.dcol3, n, a.bpart);
+    // Layer 2: dY2 (routing of dP2), db2, dW2 = dY2^T Col2, dP1 = the
+    // transposed convolution of dY2 (implicit).
+    cnn_unpool_kernel<16, 16, kC2, kC2><<<unpool_grid(16, kC2), 256, 0, st>>>(
+        a.dy2, a.m2, a.dp2, n, a.bpart);
     if ((rc = launched("cnn_unpool_kernel 2")) || (rc = bias_sum(16, kC2, ob2))) return rc;
-    CUtensorMap m_dy2t, m_col2t, m_dy2, m_w2k;
+    CUtensorMap m_dy2t, m_col2t, m_dy2a, m_w2t;
     if ((rc = make_tmap_bf16_3d(&m_dy2t, a.dy2, kC2, r2, C, kC2, r2 * kC2, 64, 64)) ||
         (rc = make_tmap_bf16_3d(&m_col2t, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, 64, 64)) ||
-        (rc = make_tmap_bf16_3d(&m_dy2, a.dy2, kC2, r2, C, kC2, r2 * kC2, kGemmBK, kGemmBM)) ||
-        (rc = make_tmap_bf16_3d(&m_w2k, a.w2b, kC2, kK2, C, kC2, kK2 * kC2, kGemmBK, 64)))
+        (rc = make_tmap_bf16_4d(&m_dy2a, a.dy2, {kC2, 16, 16, imgs},
+                                {kC2, 16 * kC2, 256 * kC2}, {64, 16, 8, 1})) ||
+        (rc = make_tmap_bf16_4d(&m_w2t, a.w2b, {kC2, kC1, 9, C}, {kC2, kC1 * kC2, kK2 * kC2},
+                                {64, 64, 1, 1})))
       return rc;
     if ((rc = weight_grad(m_dy2t, m_col2t, 2, kC2, kK2, kK2p, r2, oW2))) return rc;
-    const EpiStoreBf16 d2{a.dcol2, kK2p, r2};
-    if ((rc = launch_gemm<64, false, false>(m_dy2, m_w2k, C, r2, kK2p, kC2, a.status, d2, st)))
+    const TransposedB<ImplicitA<EpiStoreDX>> d2{{{a.dp1, kC1, r2}, 16, 16, kC2, -1, n}, kC2};
+    if ((rc = launch_gemm<64, false, false>(m_dy2a, m_w2t, C, r2, 64, 9 * kC2, a.status, d2,
+                                            st)))
       return rc;
     // Layer 1.
-    cnn_unpool_kernel<32, 32, kC1, kA1ld, kK2p, true><<<unpool_grid(32, kC1), 256, 0, st>>>(
-        a.dy1, a.m1, nullptr, a.dcol2, n, a.bpart);
+    cnn_unpool_kernel<32, 32, kC1, kA1ld, true><<<unpool_grid(32, kC1), 256, 0, st>>>(
+        a.dy1, a.m1, a.dp1, n, a.bpart);
     if ((rc = launched("cnn_unpool_kernel 1")) || (rc = bias_sum(32, kC1, ob1))) return rc;
     CUtensorMap m_dy1t, m_col1t;
     if ((rc = make_tmap_bf16_3d(&m_dy1t, a.dy1, kA1ld, r1, C, kA1ld, r1 * kA1ld, 64, 64)) ||
@@ -844,6 +886,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
       return rc;
     if ((rc = weight_grad(m_dy1t, m_col1t, 1, kC1, kK1, kK1p, r1, oW1))) return rc;
   }
+
   const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;
   const float pf = a.prior_scale > 0.f ? static_cast<float>(1.0 / (s2 * a.temperature)) : 0.f;
   cnn_finalize_kernel<<<dim3(a.want_grad ? grid1(kP) : 1, C), 256, 0, st>>>(a, pf);

@@ -207,6 +207,19 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 // TMA.
 // ---------------------------------------------------------------------------
 
+// 4-D tiled load (x innermost), completing on `bar`; coordinates may be
+// negative or past the extents (the box reads zeros there), x a multiple of
+// 8 for BF16.
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int x, int y,
+                                            int z, int w, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w),
+      "r"(smem_addr(bar))
+      : "memory");
+}
+
 // 3-D tiled load (x = innermost, K elements; y = rows; z = batch), completing
 // on `bar`.  x must be a multiple of 8 for BF16 (16 bytes).
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map,

@@ -5,6 +5,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "internal.h"
 #include "tc.cuh"
@@ -63,7 +65,31 @@ int make_tmap_bf16_3d(CUtensorMap* map, const void* base, int64_t cols,
                       int64_t rows, int64_t batch, int64_t row_stride,
                       int64_t batch_stride, int box_cols, int box_rows);
 
+// 4-D BF16 tensor map (dims[0] innermost, strides of dims 1..3 in elements)
+// with a 128-byte swizzled box; dims[0] x 2 bytes of a box row must be 128.
+int make_tmap_bf16_4d(CUtensorMap* map, const void* base, const int64_t (&dims)[4],
+                      const int64_t (&strides)[3], const int (&box)[4]);
+
 size_t gemm_smem_bytes(int bn);
+
+// Operand loaders.  An epilogue type may replace the tiled 3-D loads of the
+// single-CTA GEMM's operands: with `static constexpr bool kLoadA = true` and
+//   load_a(dst, map, k0, m0, b, bar)  (a K-major 128 x 64 A tile)
+// and with `kLoadB = true` and
+//   load_b(dst, map, n, k0, b, bar)   (a B tile: for an MN-major B one
+//                                      64 x 64 block starting at column n,
+//                                      for a K-major B the BN x 64 tile)
+// the producer calls these instead, e.g. to read shifted boxes of an NHWC
+// map for an implicit convolution.  They must load the bytes the default
+// loads would.
+template <class E, class = void>
+struct LoadsA : std::false_type {};
+template <class E>
+struct LoadsA<E, std::void_t<decltype(E::kLoadA)>> : std::bool_constant<E::kLoadA> {};
+template <class E, class = void>
+struct LoadsB : std::false_type {};
+template <class E>
+struct LoadsB<E, std::void_t<decltype(E::kLoadB)>> : std::bool_constant<E::kLoadB> {};
 
 // CTA-pair GEMM (tc_gemm2_kernel): shared-memory ring depth, bytes, and
 // whether it is used where it applies (the GBSGMC_GEMM_PAIR environment
@@ -212,14 +238,23 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             for (int j = 0; j < BM / 64; ++j)
               tc::tma_load_3d(sa + s * A_BYTES + j * BLOCK_BYTES, &ta, m0 + 64 * j, k0, b,
                               &full[s]);
+          } else if constexpr (LoadsA<Epi>::value) {
+            epi.load_a(sa + s * A_BYTES, &ta, k0, m0, b, &full[s]);
           } else {
             tc::tma_load_3d(sa + s * A_BYTES, &ta, k0, m0, b, &full[s]);
           }
           if constexpr (B_MN) {
 #pragma unroll
-            for (int j = 0; j < BN / 64; ++j)
-              tc::tma_load_3d(sb + s * B_BYTES + j * BLOCK_BYTES, &tb, n0 + 64 * j, k0, b,
-                              &full[s]);
+            for (int j = 0; j < BN / 64; ++j) {
+              if constexpr (LoadsB<Epi>::value)
+                epi.load_b(sb + s * B_BYTES + j * BLOCK_BYTES, &tb, n0 + 64 * j, k0, b,
+                           &full[s]);
+              else
+                tc::tma_load_3d(sb + s * B_BYTES + j * BLOCK_BYTES, &tb, n0 + 64 * j, k0, b,
+                                &full[s]);
+            }
+          } else if constexpr (LoadsB<Epi>::value) {
+            epi.load_b(sb + s * B_BYTES, &tb, n0, k0, b, &full[s]);
           } else {
             tc::tma_load_3d(sb + s * B_BYTES, &tb, k0, n0, b, &full[s]);
           }
