@@ -126,9 +126,10 @@ int make_tmap_bf16_4d(CUtensorMap* map, const void* base, const int64_t (&dims)[
 }
 
 size_t gemm_smem_bytes(int bn) {
-  return 1024 + static_cast<size_t>(kGemmStages) *
+  const int stages = gemm_stages(bn);
+  return 1024 + static_cast<size_t>(stages) *
                     (kGemmBM * kGemmBK * 2 + static_cast<size_t>(bn) * kGemmBK * 2) +
-         static_cast<size_t>(kGemmEpiWarps) * kStageWords * 4 + (2 * kGemmStages + 5) * 8 + 16;
+         static_cast<size_t>(kGemmEpiWarps) * kStageWords * 4 + (2 * stages + 5) * 8 + 16;
 }
 
 size_t gemm2_smem_bytes(int bn) {

@@ -15,7 +15,14 @@ namespace gbsgmc {
 
 constexpr int kGemmBM = 128;     // rows of a CTA tile (UMMA M)
 constexpr int kGemmBK = 64;      // K per stage: one 128-byte swizzle row
-constexpr int kGemmStages = 4;   // shared-memory ring depth
+constexpr int kGemmStages = 4;   // shared-memory ring depth at BN = 256
+// Ring depth of the single-CTA kernel: as many stages as fit beside the
+// epilogue staging (one CTA per SM either way), so that short-N GEMMs keep
+// more copies in flight: 4 at BN = 256 (48 KB stages), 6 at BN = 128, 8 at
+// BN = 64.
+__host__ __device__ constexpr int gemm_stages(int bn) {
+  return bn == 256 ? kGemmStages : bn == 128 ? 6 : 8;
+}
 constexpr int kGemmSplit = 2;    // epilogue warps per TMEM lane quarter
 constexpr int kGemmEpiWarps = 4 * kGemmSplit;
 constexpr int kGemmThreads = 64 + 32 * kGemmEpiWarps;  // producer, MMA, epilogue
@@ -133,7 +140,7 @@ __device__ __forceinline__ int ragged_batch(const GemmRagged& rg, int t, int per
 // rows of M or N contiguous elements).  The grid holds at most one CTA per
 // resident slot; CTA i takes output tiles i, i + gridDim.x, ... in the order
 // (batch, M tile, N tile), N fastest.  Roles:
-//   warp 0 (one lane)  TMA producer into a kGemmStages-deep ring of 64-wide
+//   warp 0 (one lane)  TMA producer into a gemm_stages(BN)-deep ring of 64-wide
 //                      K slices (128-byte swizzle)
 //   warp 1             allocates two BN-column TMEM accumulators; one lane
 //                      issues tcgen05.mma (M=128, N=BN, K=16) into them
@@ -158,7 +165,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta,
                    const __grid_constant__ CUtensorMap tb, int M, int N, int K,
                    int batch, int* status, Epi epi, GemmRagged rg) {
-  constexpr int BM = kGemmBM, BK = kGemmBK, STAGES = kGemmStages;
+  constexpr int BM = kGemmBM, BK = kGemmBK, STAGES = gemm_stages(BN);
   constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
   constexpr uint32_t BLOCK_BYTES = 64 * BK * 2;  // one 64 x 64 MN-major box
   constexpr uint32_t TMEM_COLS = 2 * BN;
