@@ -59,7 +59,8 @@ constexpr int kFlat = 4 * 4 * kC3;  // 2048
 constexpr int kK1 = 27, kK1p = 64;  // im2col widths (real, padded)
 constexpr int kK2 = 9 * kC1, kK2p = 320;
 constexpr int kK3 = 9 * kC2;  // conv3 reads P2 by tap: no padded im2col
-constexpr int kA1ld = 64;  // conv1 output-gradient channels as stored (32 real)
+constexpr int kA1ld = kC1;  // conv1 output-gradient channels as stored (the dW1
+                            // GEMM's 64-wide box reads zeros past them)
 
 // Offsets of the leaves in a chain's flat parameter vector.
 constexpr int64_t ob1 = 0, oW1 = ob1 + kC1, ob2 = oW1 + kK1 * kC1, oW2 = ob2 + kC2,
