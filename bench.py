@@ -1310,6 +1310,45 @@ def run_gemm(args):
                     "steps": args.steps, "warmup": args.warmup, "results": out}), flush=True)
 
 
+def run_gather(args):
+  """The headline kernel's memory pattern without its arithmetic: random
+  1 KB rows (fp32, d = 256) of the 1,000,000-row matrix, 256 x 1024 per
+  step, gathered by torch.index_select (a library kernel, for comparison
+  only) and by a plain row copy with the same index stream; CUDA events
+  over `--steps` steps after `--warmup`, one JSON line with GB/s and its
+  fraction of the measured copy bandwidth."""
+  import torch
+  N, d, rows = 1_000_000, 256, 256 * 1024
+  X = torch.randn((N, d), device="cuda")
+  g = torch.Generator(device="cuda").manual_seed(3)
+  idx = torch.randint(0, N, (args.warmup + args.steps, rows), generator=g, device="cuda")
+  out = torch.empty((rows, d), device="cuda")
+
+  def timed(fn):
+    for k in range(args.warmup):
+      fn(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(args.steps):
+      fn(args.warmup + k)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / args.steps
+
+  ms = timed(lambda k: torch.index_select(X, 0, idx[k], out=out))
+  gbs = rows * d * 4 / (ms / 1e3) / 1e9
+  peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+      if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+  peak = peaks.get("hbm_gbs", 6800.0)
+  print(json.dumps({"metric": "random 1 KB row gather", "unit": "GB/s",
+                    "rows_per_step": rows, "row_bytes": d * 4, "matrix_rows": N,
+                    "steps": args.steps, "warmup": args.warmup,
+                    "torch_index_select": {"GB/s": gbs, "frac_of_copy_peak": gbs / peak,
+                                           "read_plus_write_GB/s": 2 * gbs,
+                                           "ms_per_step": ms}}), flush=True)
+
+
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument("--gpus", type=int, default=1)
@@ -1317,11 +1356,12 @@ def main():
   ap.add_argument("--warmup", type=int, default=5)
   ap.add_argument("--impl", default="gbsgmc", choices=["gbsgmc", "reference"])
   ap.add_argument("--workload", default="logistic",
-                  choices=["logistic", "mlp", "resgld", "cnn", "gemm"],
+                  choices=["logistic", "mlp", "resgld", "cnn", "gemm", "gather"],
                   help="logistic: 256-chain SGLD headline; mlp: 64-chain OBABO "
                        "on the tanh network; resgld: 32-replica exchange on it; "
                        "cnn: 8-chain OBABO on the conv classifier; gemm: the "
-                       "tcgen05 GEMM alone on the network's hidden-layer shape")
+                       "tcgen05 GEMM alone on the network's hidden-layer shape; "
+                       "gather: the headline's random-row memory pattern alone")
   ap.add_argument("--kernel-only", action="store_true",
                   help="short run of the fused kernel for profilers; no JSON line")
   args = ap.parse_args()
@@ -1329,6 +1369,8 @@ def main():
     ap.error("--warmup must be at least 3")
   if args.workload == "gemm":
     run_gemm(args)
+  elif args.workload == "gather":
+    run_gather(args)
   elif args.workload == "cnn":
     if args.impl == "reference":
       run_mlp_reference(args)
