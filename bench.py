@@ -1259,10 +1259,10 @@ def run_mlp(args):
 
 def run_gemm(args):
   """The tcgen05 BF16 GEMM alone on the tanh network's hidden-layer shape,
-  64 x (2048 x 1024 x 1024), C fp32: the CTA-pair kernel and the single-CTA
-  kernel (GBSGMC_GEMM_PAIR=0) in the four operand layouts, and torch.bmm
-  (cuBLAS, BF16 output) beside them; CUDA events over `--steps` calls after
-  `--warmup`, one JSON line."""
+  64 x (2048 x 1024 x 1024): C fp32 from the CTA-pair kernel and the
+  single-CTA kernel (GBSGMC_GEMM_PAIR=0) in the four operand layouts, C BF16
+  from both (K-major operands), and torch.bmm (cuBLAS, BF16 output) beside
+  them; CUDA events over `--steps` calls after `--warmup`, one JSON line."""
   import os
   import torch
   from gbsgmc import _lib
@@ -1301,6 +1301,19 @@ def run_gemm(args):
       ms = timed(call)
       out[f"{'pair' if pair == '1' else 'single'}_{'mn' if a_mn else 'k'}{'mn' if b_mn else 'k'}"] = \
           round(flop / (ms / 1e3) / 1e12, 1)
+  # BF16 C (as torch.bmm writes it): half the output bytes.
+  C16 = torch.empty((batch, M, N), dtype=torch.bfloat16, device="cuda")
+  for pair in ("1", "0"):
+    os.environ["GBSGMC_GEMM_PAIR"] = pair
+
+    def call16():
+      _lib.call("gbsgmc_gemm_bf16_c16", 0, 0, A.data_ptr(), K, M * K, B.data_ptr(), K, N * K,
+                C16.data_ptr(), N, M * N, batch, M, N, K, status.data_ptr(),
+                _lib.stream_handle())
+
+    ms = timed(call16)
+    out[f"{'pair' if pair == '1' else 'single'}_kk_bf16_out"] = \
+        round(flop / (ms / 1e3) / 1e12, 1)
   os.environ.pop("GBSGMC_GEMM_PAIR", None)
   assert int(status.item()) == 0
   ms = timed(lambda: torch.bmm(A, B.transpose(1, 2)))

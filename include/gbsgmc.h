@@ -501,6 +501,14 @@ int gbsgmc_gemm_bf16(int a_mn, int b_mn, const void* A_dev, int64_t lda,
                      int64_t c_batch_stride, int batch, int M, int N, int K,
                      int* status_dev, gbsgmc_stream_t stream);
 
+/* As gbsgmc_gemm_bf16 with C stored as BF16 (rounded to nearest even; ldc and
+ * the C batch stride multiples of 8 elements, C 16-byte aligned). */
+int gbsgmc_gemm_bf16_c16(int a_mn, int b_mn, const void* A_dev, int64_t lda,
+                         int64_t a_batch_stride, const void* B_dev, int64_t ldb,
+                         int64_t b_batch_stride, void* C_dev, int64_t ldc,
+                         int64_t c_batch_stride, int batch, int M, int N, int K,
+                         int* status_dev, gbsgmc_stream_t stream);
+
 /* As gbsgmc_gemm_bf16 with the bound of each wait for pipeline progress (the
  * TMA operands of a stage, a free stage, a finished or drained TMEM
  * accumulator) given in nanoseconds instead of the default 1 s.  A CTA whose

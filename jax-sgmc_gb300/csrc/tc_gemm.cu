@@ -6,6 +6,7 @@
 // translation units instantiate it with fused epilogues; this file holds
 // the tensor-map encoder and the plain fp32-output entry points.
 #include <cuda.h>
+#include <cuda_bf16.h>
 
 #include <cstdlib>
 #include <cstring>
@@ -97,6 +98,34 @@ struct StoreF32 {
   }
 };
 
+// Plain BF16 store of the accumulator (round to nearest even), 64 columns
+// per 128-byte row segment.
+struct StoreBF16 {
+  __nv_bfloat16* C;
+  int64_t ldc, batch_stride;
+  template <int NC, class Load>
+  __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
+                                       uint32_t* st) const {
+    uint32_t* dst = reinterpret_cast<uint32_t*>(C + b * batch_stride +
+                                                static_cast<int64_t>(row0) * ldc + col0) +
+                    epi::lane_id();
+#pragma unroll 1
+    for (int blk = 0; blk < NC / 64; ++blk) {
+      float v[64];
+      uint32_t w[32];
+      load.wide(blk, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        w[j] = *reinterpret_cast<const uint32_t*>(&pr);
+      }
+      epi::put_rows(st, w);
+#pragma unroll 4
+      for (int r = 0; r < 32; ++r) dst[r * (ldc / 2) + 32 * blk] = epi::get(st, r);
+    }
+  }
+};
+
 }  // namespace
 
 int make_tmap_bf16_4d(CUtensorMap* map, const void* base, const int64_t (&dims)[4],
@@ -149,8 +178,9 @@ using namespace gbsgmc;
 
 namespace {
 
+template <class Epi>
 int dispatch_pair(bool a_mn, bool b_mn, const CUtensorMap& ta, const CUtensorMap& tb,
-                  int batch, int M, int N, int K, int* status, const StoreF32& epi,
+                  int batch, int M, int N, int K, int* status, const Epi& epi,
                   cudaStream_t st, uint64_t wait_ns) {
   if (a_mn)
     return b_mn ? launch_gemm2<256, true, true>(ta, tb, batch, M, N, K, status, epi, st, wait_ns)
@@ -159,9 +189,9 @@ int dispatch_pair(bool a_mn, bool b_mn, const CUtensorMap& ta, const CUtensorMap
               : launch_gemm2<256, false, false>(ta, tb, batch, M, N, K, status, epi, st, wait_ns);
 }
 
-template <int BN>
+template <int BN, class Epi>
 int dispatch_layout(bool a_mn, bool b_mn, const CUtensorMap& ta, const CUtensorMap& tb,
-                    int batch, int M, int N, int K, int* status, const StoreF32& epi,
+                    int batch, int M, int N, int K, int* status, const Epi& epi,
                     cudaStream_t st, const GemmRagged& rg) {
   if (a_mn)
     return b_mn ? launch_gemm<BN, true, true>(ta, tb, batch, M, N, K, status, epi, st, rg)
@@ -182,11 +212,16 @@ extern "C" int gbsgmc_gemm_bf16(int a_mn, int b_mn, const void* A_dev, int64_t l
                                      N, K, kWaitLimitNs, status_dev, stream);
 }
 
-extern "C" int gbsgmc_gemm_bf16_wait_limit(
-    int a_mn, int b_mn, const void* A_dev, int64_t lda, int64_t a_batch_stride,
-    const void* B_dev, int64_t ldb, int64_t b_batch_stride, float* C_dev, int64_t ldc,
-    int64_t c_batch_stride, int batch, int M, int N, int K, uint64_t wait_limit_ns,
-    int* status_dev, gbsgmc_stream_t stream) {
+namespace {
+
+// The plain GEMM with C in fp32 (StoreF32) or BF16 (StoreBF16): checks,
+// tensor maps, and the pair or single-CTA kernel.
+template <class Epi>
+int plain_gemm(int a_mn, int b_mn, const void* A_dev, int64_t lda, int64_t a_batch_stride,
+               const void* B_dev, int64_t ldb, int64_t b_batch_stride, const void* C_dev,
+               int64_t ldc, int64_t c_batch_stride, int batch, int M, int N, int K,
+               uint64_t wait_limit_ns, int* status_dev, gbsgmc_stream_t stream,
+               const Epi& epi) {
   if (A_dev == nullptr || B_dev == nullptr || C_dev == nullptr || status_dev == nullptr)
     return set_error(GBSGMC_ERR_ARG, "gemm_bf16: null pointer");
   if (batch <= 0 || M <= 0 || N <= 0 || K <= 0 || batch > (1 << 20))
@@ -210,7 +245,6 @@ extern "C" int gbsgmc_gemm_bf16_wait_limit(
             : make_tmap_bf16_3d(&tb, B_dev, K, N, batch, ldb, b_batch_stride, kGemmBK,
                                 pair ? bn / 2 : bn);
   if (rc != GBSGMC_OK) return rc;
-  const StoreF32 epi{C_dev, ldc, c_batch_stride};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (pair)
     return dispatch_pair(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st, wait_limit_ns);
@@ -219,6 +253,31 @@ extern "C" int gbsgmc_gemm_bf16_wait_limit(
   return bn == 256
              ? dispatch_layout<256>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st, rg)
              : dispatch_layout<128>(a_mn, b_mn, ta, tb, batch, M, N, K, status_dev, epi, st, rg);
+}
+
+}  // namespace
+
+extern "C" int gbsgmc_gemm_bf16_wait_limit(
+    int a_mn, int b_mn, const void* A_dev, int64_t lda, int64_t a_batch_stride,
+    const void* B_dev, int64_t ldb, int64_t b_batch_stride, float* C_dev, int64_t ldc,
+    int64_t c_batch_stride, int batch, int M, int N, int K, uint64_t wait_limit_ns,
+    int* status_dev, gbsgmc_stream_t stream) {
+  const StoreF32 epi{C_dev, ldc, c_batch_stride};
+  return plain_gemm(a_mn, b_mn, A_dev, lda, a_batch_stride, B_dev, ldb, b_batch_stride, C_dev,
+                    ldc, c_batch_stride, batch, M, N, K, wait_limit_ns, status_dev, stream, epi);
+}
+
+extern "C" int gbsgmc_gemm_bf16_c16(int a_mn, int b_mn, const void* A_dev, int64_t lda,
+                                    int64_t a_batch_stride, const void* B_dev, int64_t ldb,
+                                    int64_t b_batch_stride, void* C_dev, int64_t ldc,
+                                    int64_t c_batch_stride, int batch, int M, int N, int K,
+                                    int* status_dev, gbsgmc_stream_t stream) {
+  if (ldc % 8 != 0 || c_batch_stride % 8 != 0)
+    return set_error(GBSGMC_ERR_ARG, "gemm_bf16_c16: ldc and the C batch stride must be "
+                     "multiples of 8");
+  const StoreBF16 epi{static_cast<__nv_bfloat16*>(C_dev), ldc, c_batch_stride};
+  return plain_gemm(a_mn, b_mn, A_dev, lda, a_batch_stride, B_dev, ldb, b_batch_stride, C_dev,
+                    ldc, c_batch_stride, batch, M, N, K, kWaitLimitNs, status_dev, stream, epi);
 }
 
 extern "C" int gbsgmc_gemm_bf16_nt(const void* A_dev, int64_t lda,

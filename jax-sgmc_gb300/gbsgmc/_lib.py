@@ -239,6 +239,8 @@ SIGNATURES = {
     "gbsgmc_plan_destroy": (_i, [_vp]),
     "gbsgmc_gemm_bf16": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64, _vp,
                               _i64, _i64, _i, _i, _i, _i, _vp, _vp]),
+    "gbsgmc_gemm_bf16_c16": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64, _vp,
+                              _i64, _i64, _i, _i, _i, _i, _vp, _vp]),
     "gbsgmc_gemm_bf16_wait_limit": (_i, [_i, _i, _vp, _i64, _i64, _vp, _i64, _i64,
                                          _vp, _i64, _i64, _i, _i, _i, _i,
                                          C.c_uint64, _vp, _vp]),

@@ -134,3 +134,28 @@ def test_pair_and_single_cta_gemms_agree(lib, monkeypatch, a_mn, b_mn):
     assert bool(((C - ref).abs() <= 1e-3 * bound + 1e-4).all())
     out.append(C)
   assert bool(((out[0] - out[1]).abs() <= 1e-3 * bound + 1e-4).all())
+
+
+@pytest.mark.parametrize("pair", ["1", "0"])
+def test_gemm_with_bf16_output(lib, monkeypatch, pair):
+  """gbsgmc_gemm_bf16_c16: C rounded to BF16 (nearest even) from the same
+  accumulators: within the fp32-summation bound plus half a BF16 ulp of
+  the result, on the pair kernel and the single-CTA one."""
+  import torch
+  from gbsgmc import _lib
+  monkeypatch.setenv("GBSGMC_GEMM_PAIR", pair)
+  batch, M, N, K = 2, 512, 768, 320
+  g = torch.Generator(device="cuda").manual_seed(77)
+  A = torch.randn((batch, M, K), generator=g, device="cuda").to(torch.bfloat16)
+  B = torch.randn((batch, N, K), generator=g, device="cuda").to(torch.bfloat16)
+  C = torch.full((batch, M, N), float("nan"), dtype=torch.bfloat16, device="cuda")
+  status = torch.zeros(1, dtype=torch.int32, device="cuda")
+  _lib.call("gbsgmc_gemm_bf16_c16", 0, 0, A.data_ptr(), K, M * K, B.data_ptr(), K, N * K,
+            C.data_ptr(), N, M * N, batch, M, N, K, status.data_ptr(), _lib.stream_handle())
+  torch.cuda.synchronize()
+  assert int(status.item()) == 0
+  ref = torch.bmm(A.float(), B.float().transpose(1, 2))
+  bound = torch.bmm(A.float().abs(), B.float().abs().transpose(1, 2))
+  err = (C.float() - ref).abs()
+  assert torch.isfinite(C.float()).all()
+  assert bool((err <= 1e-3 * bound + 2.0 ** -8 * ref.abs() + 1e-4).all())
