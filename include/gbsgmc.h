@@ -73,6 +73,15 @@ typedef struct gbsgmc_pcg64 {
   uint32_t has_uint32, uinteger;
 } gbsgmc_pcg64;
 
+/* Host function: the fresh gbsgmc_pcg64 words ([count, 5] uint64: state
+ * high/low, increment high/low, buffered half 0) of the numpy PCG64 streams
+ * numpy.random.default_rng(SeedSequence(seed).spawn(1)[0]) starts with, for
+ * seeds seeds_lo[c] + 2^64 seeds_hi[c] (seeds_hi may be NULL: seeds below
+ * 2^64).  The index streams NumpyDataLoader.register_random_pipeline gives
+ * its chains (jax_sgmc/data/numpy_loader.py:261-265). */
+int gbsgmc_pcg64_seed(const uint64_t* seeds_lo, const uint64_t* seeds_hi, int count,
+                      uint64_t* words);
+
 /* Draws `draws` indices in [0, n_obs) for each of `chains` numpy PCG64 streams,
  * bit-identical to numpy's Generator.choice(arange(n_obs), draws,
  * replace=True) (== Generator.integers(0, n_obs, dtype=int64)), and advances

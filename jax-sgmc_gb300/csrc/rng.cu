@@ -260,6 +260,87 @@ int launch_philox_index(uint64_t seed, int chain_base, int chains,
 
 using namespace gbsgmc;
 
+// Fresh numpy PCG64 streams of chains registered with the given seeds: the
+// generator numpy.random.default_rng(SeedSequence(seed).spawn(1)[0]) starts
+// with.  SeedSequence is M. O'Neill's seed_seq_fe entropy mixer ("Developing
+// a seed_seq Alternative", 2015) over a pool of four 32-bit words with its
+// published hash and mix constants; the assembled entropy of a chain is its
+// seed as four little-endian 32-bit words (zero-padded to the pool size, as
+// SeedSequence does when a spawn key follows) and the spawn key word 0.  Four 64-bit words generated from the pool seed
+// PCG64 as numpy does: state = 0, inc = 2 initseq + 1, one LCG step,
+// state += initstate, one LCG step.
+namespace {
+
+struct SeedSeqFe {
+  uint32_t hash_a = 0x43B0D7E5u;
+  uint32_t hashmix(uint32_t v) {
+    v ^= hash_a;
+    hash_a *= 0x931E8875u;
+    v *= hash_a;
+    return v ^ (v >> 16);
+  }
+  static uint32_t mix(uint32_t x, uint32_t y) {
+    const uint32_t r = 0xCA01F9DDu * x - 0x4973F715u * y;
+    return r ^ (r >> 16);
+  }
+};
+
+void pcg64_seed_one(uint64_t lo, uint64_t hi, uint64_t (&out)[5]) {
+  // With a spawn key the run entropy is zero-padded to the pool size, so
+  // the assembled entropy is always the four seed limbs and the key word.
+  const int n = 5;
+  const uint32_t ent[5] = {static_cast<uint32_t>(lo), static_cast<uint32_t>(lo >> 32),
+                           static_cast<uint32_t>(hi), static_cast<uint32_t>(hi >> 32),
+                           0u};  // spawn key (0,)
+  SeedSeqFe h;
+  uint32_t pool[4];
+  for (int i = 0; i < 4; ++i) pool[i] = h.hashmix(ent[i]);
+  for (int s = 0; s < 4; ++s)
+    for (int d = 0; d < 4; ++d)
+      if (s != d) pool[d] = SeedSeqFe::mix(pool[d], h.hashmix(pool[s]));
+  for (int i = 4; i < n; ++i)
+    for (int d = 0; d < 4; ++d) pool[d] = SeedSeqFe::mix(pool[d], h.hashmix(ent[i]));
+  uint32_t hash_b = 0x8B51F9DDu;
+  uint32_t w[8];
+  for (int i = 0; i < 8; ++i) {
+    uint32_t v = pool[i % 4] ^ hash_b;
+    hash_b *= 0x58F38DEDu;
+    v *= hash_b;
+    w[i] = v ^ (v >> 16);
+  }
+  using u128 = unsigned __int128;
+  const auto word64 = [&](int k) {
+    return static_cast<uint64_t>(w[2 * k]) | (static_cast<uint64_t>(w[2 * k + 1]) << 32);
+  };
+  const u128 initstate = (static_cast<u128>(word64(0)) << 64) | word64(1);
+  const u128 initseq = (static_cast<u128>(word64(2)) << 64) | word64(3);
+  const u128 mult = (static_cast<u128>(0x2360ED051FC65DA4ull) << 64) | 0x4385DF649FCCF645ull;
+  const u128 inc = (initseq << 1) | 1u;
+  u128 state = inc;                 // 0 * mult + inc
+  state += initstate;
+  state = state * mult + inc;
+  out[0] = static_cast<uint64_t>(state >> 64);
+  out[1] = static_cast<uint64_t>(state);
+  out[2] = static_cast<uint64_t>(inc >> 64);
+  out[3] = static_cast<uint64_t>(inc);
+  out[4] = 0;  // no buffered 32-bit half
+}
+
+}  // namespace
+
+extern "C" int gbsgmc_pcg64_seed(const uint64_t* seeds_lo, const uint64_t* seeds_hi, int count,
+                                 uint64_t* words) {
+  if (count < 0) return set_error(GBSGMC_ERR_ARG, "pcg64_seed: negative count");
+  if (count > 0 && (seeds_lo == nullptr || words == nullptr))
+    return set_error(GBSGMC_ERR_ARG, "pcg64_seed: null pointer");
+  for (int c = 0; c < count; ++c) {
+    uint64_t out[5];
+    pcg64_seed_one(seeds_lo[c], seeds_hi != nullptr ? seeds_hi[c] : 0, out);
+    for (int k = 0; k < 5; ++k) words[5 * static_cast<int64_t>(c) + k] = out[k];
+  }
+  return GBSGMC_OK;
+}
+
 extern "C" int gbsgmc_index_draw_pcg64(gbsgmc_pcg64* states_dev, int chains,
                                        int64_t n_obs, int64_t draws,
                                        int per_step, int32_t* idx_dev,

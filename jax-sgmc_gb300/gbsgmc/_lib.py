@@ -136,6 +136,7 @@ SIGNATURES = {
     "gbsgmc_mlp_value_and_grad_ragged": (_i, [_P(Mlp), _i, _i, _vp, _vp, _i64,
                                               _vp, _vp, _vp, _vp, _vp, _vp,
                                               _vp, _sz, _vp, _vp]),
+    "gbsgmc_pcg64_seed": (_i, [_vp, _vp, _i, _vp]),
     "gbsgmc_mlp_fisher_workspace_bytes": (_sz, [_P(Mlp), _i, _i]),
     "gbsgmc_mlp_fisher_noise": (_i, [_P(Mlp), _i, _i, _vp, _i64, _vp, _vp, _vp,
                                      _f, _f, _vp, _vp, _vp, _sz, _vp, _vp]),

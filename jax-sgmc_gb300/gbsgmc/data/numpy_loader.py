@@ -54,6 +54,28 @@ _PCG64_MULT = 0x2360ED051FC65DA44385DF649FCCF645   # PCG's 128-bit LCG multiplie
 _M32, _M64, _M128 = (1 << 32) - 1, (1 << 64) - 1, (1 << 128) - 1
 
 
+def pcg64_words_fast(seeds) -> onp.ndarray:
+  """:func:`pcg64_words_many` through the library's host function
+  ``gbsgmc_pcg64_seed`` (the same mixing in C, about a microsecond for a few
+  hundred chains); :func:`pcg64_words_many` itself when the library is not
+  loaded or a seed is negative or of 2**128 and above."""
+  seeds = [int(s) for s in seeds]
+  if not seeds or any(s < 0 or s >> 128 for s in seeds):
+    return pcg64_words_many(seeds)
+  try:
+    from .. import _lib
+    lib = _lib.load()
+  except Exception:   # no library in this process: the numpy restatement
+    return pcg64_words_many(seeds)
+  lo = onp.array([s & _M64 for s in seeds], onp.uint64)
+  hi = onp.array([s >> 64 for s in seeds], onp.uint64)
+  out = onp.empty((len(seeds), 5), onp.uint64)
+  rc = lib.gbsgmc_pcg64_seed(lo.ctypes.data, hi.ctypes.data, len(seeds), out.ctypes.data)
+  if rc != 0:
+    raise _lib.GbsgmcError(rc, "gbsgmc_pcg64_seed")
+  return out
+
+
 def pcg64_words_many(seeds) -> onp.ndarray:
   """:func:`pcg64_words` of many chains at once, ``[C, 5]`` uint64.
 
@@ -299,7 +321,7 @@ class NumpyDataLoader(NumpyBase, HostDataLoader):
                        f"{self._observation_count}")
     first = len(self._chains)
     seeds = [kwargs.get("seed", first + i) for i in range(count)]
-    words = pcg64_words_many(seeds)
+    words = pcg64_words_fast(seeds)
     draws = math.ceil(self._observation_count / mb_size)
     for seed in seeds:
       rec = _RandomChain(type='random', idx_offset=None, in_epochs=False,

@@ -336,6 +336,29 @@ def postprocess_chains(saving: Saving, count: int, variables, treedefs,
       torch.from_numpy(h).copy_(v.contiguous())
     hext[k] = h
   host = host[0]
+  td0 = treedefs[0] if C else None
+  if C and td0.kind == "dict" and td0.children and \
+      all(ch.kind == "leaf" for ch in td0.children) and \
+      all(td is td0 for td in treedefs):
+    # One tree definition of array leaves for all chains: each leaf is one
+    # [count, C, *shape] view of the host buffer, and chain c's arrays are
+    # its views [:, c] -- the arrays unravel() would give, without
+    # re-deriving the layout per chain.
+    views, o = [], 0
+    for k, ch in zip(td0.keys, td0.children):
+      n = int(np.prod(ch.shape, dtype=np.int64))
+      views.append((k, host[:, :, o:o + n].reshape((count, C) + tuple(ch.shape))))
+      o += n
+    fin = saving.collector.finalize
+    ext = list(hext.items())
+    out = []
+    for c in range(C):
+      samples = {"variables": {k: v[:, c] for k, v in views}}
+      for k, v in ext:
+        samples[k] = v[:, c]
+      samples["model_state"] = model_states[c]
+      out.append({"sample_count": count, "samples": fin(samples)})
+    return out
   # What postprocess() does for host saving, with each tree definition's
   # leaf layout worked out once for all chains that share it.
   unravelers = {}

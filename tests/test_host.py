@@ -521,3 +521,19 @@ def test_ravel_many_and_unraveler_match_ravel_and_unravel():
     util.ravel_many([{"w": np.ones(2)}, {"v": np.ones(2)}])
   with pytest.raises(ValueError):
     util.ravel_many([{"w": np.ones(2)}, {"w": np.ones(3)}])
+
+
+def test_pcg64_seed_in_c_matches_numpy():
+  """gbsgmc_pcg64_seed (the library's host restatement of SeedSequence
+  mixing and PCG64 seeding) gives the words of numpy's own fresh
+  generators, for seeds below 2**32, below 2**64 and up to 2**128."""
+  import numpy as np
+  from gbsgmc.data import numpy_loader as nl
+  rng = np.random.default_rng(4)
+  seeds = list(range(0, 300)) + [2**32 - 1, 2**32, 2**40 + 7, 2**63 + 5, 2**64 - 1, 2**64,
+                                 2**100 + 3, 2**128 - 1]
+  seeds += [int(x) for x in rng.integers(0, 2**63, size=50)]
+  fast = nl.pcg64_words_fast(seeds)
+  np.testing.assert_array_equal(fast, nl.pcg64_words_many(seeds))
+  for s in seeds[::7] + seeds[-12:]:
+    np.testing.assert_array_equal(fast[seeds.index(s)], np.array(nl.pcg64_words(s), np.uint64))
