@@ -373,70 +373,59 @@ __device__ __forceinline__ void tanh_block(const Load& load, int blk, const floa
   dot += dot2;
 }
 
-// Writes the packed 64-column block of the warp's 32 rows, one 128-byte row
-// segment per store.
-__device__ __forceinline__ void store_block(uint32_t* dst, int64_t ld_words, int blk,
-                                            const uint32_t (&pk)[32], uint32_t* st) {
-  epi::put_rows(st, pk);
-#pragma unroll 4
-  for (int r = 0; r < 32; ++r) dst[r * ld_words + 32 * blk] = epi::get(st, r);
-}
-
-// 3: Z1 = tanh(acc + b1) -> Z1 [n, H1].
+// 3: Z1 = tanh(acc + b1) -> Z1 [n, H1]; each packed 64-column block of the
+//    warp's rows leaves as one TMA store box of zmap (Z1 as [chains, n, H1]).
 struct EpiHidden1 {
   const float* w;
   int64_t P, ob1;
-  int H1, n;
-  bf16* z1;
+  CUtensorMap zmap;
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
     const float* b1 = w + b * P + ob1 + col0;
-    uint32_t* dst = reinterpret_cast<uint32_t*>(z1 + (static_cast<int64_t>(b) * n + row0) * H1 +
-                                                col0) + epi::lane_id();
     float unused = 0.f;
 #pragma unroll 1
     for (int blk = 0; blk < NC / 64; ++blk) {
       uint32_t pk[32];
       tanh_block(load, blk, b1, pk, nullptr, unused);
-      store_block(dst, H1 / 2, blk, pk, st);
+      epi::store_box(st, pk, &zmap, col0 + 64 * blk, row0, b);
     }
   }
 };
 
-// 4: Z2 = tanh(acc + b2) -> Z2 [n, H2]; the fp32 partial Z2 . W3 over the
-//    warp's NC columns -> outp [H2 / NC, n].
+// 4: Z2 = tanh(acc + b2) -> Z2 [n, H2] (TMA store boxes of zmap, Z2 as
+//    [chains, n, H2]); the fp32 partial Z2 . W3 over the warp's NC columns
+//    -> outp [H2 / NC, n].
 struct EpiHidden2 {
   const float* w;
   int64_t P, ob2, oW3;
   int H2, n;
-  bf16* z2;
   float* outp;
+  CUtensorMap zmap;
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
     const float* b2 = w + b * P + ob2 + col0;
     const float* w3 = w + b * P + oW3 + col0;
-    uint32_t* dst = reinterpret_cast<uint32_t*>(z2 + (static_cast<int64_t>(b) * n + row0) * H2 +
-                                                col0) + epi::lane_id();
     float dot = 0.f;
 #pragma unroll 1
     for (int blk = 0; blk < NC / 64; ++blk) {
       uint32_t pk[32];
       tanh_block(load, blk, b2, pk, w3, dot);
-      store_block(dst, H2 / 2, blk, pk, st);
+      epi::store_box(st, pk, &zmap, col0 + 64 * blk, row0, b);
     }
     outp[(static_cast<int64_t>(b) * (H2 / NC) + col0 / NC) * n + row0 + epi::lane_id()] = dot;
   }
 };
 
 // 7: G1 = acc * (1 - Z1^2) written over Z1 [n, H1] (the block is read and
-//    then rewritten by the same warp); per-warp column sums -> pb1
+//    then rewritten, as a TMA store box, by the same warp); per-warp column sums -> pb1
 //    [n/32, H1].
 struct EpiAdjoint1 {
   bf16* z1;
   float* pb1;
   int H1, n;
+  CUtensorMap zmap;  // Z1 as [chains, n, H1], boxes of 64 columns x 32 rows
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
@@ -453,6 +442,7 @@ struct EpiAdjoint1 {
       uint32_t zw[32];
 #pragma unroll
       for (int r = 0; r < 32; ++r) zw[r] = zrow[static_cast<int64_t>(r) * (H1 / 2) + 32 * blk];
+      epi::reclaim();
 #pragma unroll
       for (int r = 0; r < 32; ++r) epi::set(st, r, zw[r]);
       epi::get_row(st, zw);
@@ -480,9 +470,7 @@ struct EpiAdjoint1 {
           if ((lane & 1) == 0) part[64 * blk + 32 * half + 16 * g + (lane >> 1)] = cs;
         }
       }
-      epi::put_rows(st, zw);
-#pragma unroll 4
-      for (int r = 0; r < 32; ++r) zrow[static_cast<int64_t>(r) * (H1 / 2) + 32 * blk] = epi::get(st, r);
+      epi::store_box(st, zw, &zmap, col0 + 64 * blk, row0, b);
     }
   }
 };
@@ -991,12 +979,14 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
     return rc;
   const bool uniform = a.n_true == nullptr;
   // 3: A1 = Xb W1 (W1 [D, H1] is the MN-major B operand).
-  const EpiHidden1 e1{a.w, s.P, s.ob1, H1, n, a.z1};
+  EpiHidden1 e1{a.w, s.P, s.ob1};
+  if ((rc = make_tmap_rows(&e1.zmap, a.z1, false, H1, n, C, H1, s1))) return rc;
   if ((rc = gemm256<false, true>(m_xb, m_w1, m_w1, C, n, H1, D, a.status, e1, st, rows_h1,
                                  uniform)))
     return rc;
   // 4: A2 = Z1 W2.
-  const EpiHidden2 e2{a.w, s.P, s.ob2, s.oW3, H2, n, a.z2g, a.outp};
+  EpiHidden2 e2{a.w, s.P, s.ob2, s.oW3, H2, n, a.outp};
+  if ((rc = make_tmap_rows(&e2.zmap, a.z2g, false, H2, n, C, H2, s2))) return rc;
   if ((rc = gemm256<false, true>(m_z1, m_w2, m_w2, C, n, H2, H1, a.status, e2, st, rows_h2,
                                  uniform)))
     return rc;
@@ -1044,7 +1034,8 @@ int run_mlp(MlpArgs& a, const MlpLayout& L, void* ws, cudaStream_t st) {
         return rc;
     }
     // 7: G1 = (G2 W2^T) * (1 - Z1^2); W2 [H1, H2] is the K-major B operand.
-    const EpiAdjoint1 e7{a.z1, a.pb1, H1, n};
+    EpiAdjoint1 e7{a.z1, a.pb1, H1, n};
+    if ((rc = make_tmap_rows(&e7.zmap, a.z1, false, H1, n, C, H1, s1))) return rc;
     if ((rc = gemm256<false, false>(m_g2, m_w2k, m_w2k_half, C, n, H1, H2, a.status, e7, st,
                                     rows_h1, uniform)))
       return rc;

@@ -98,17 +98,14 @@ struct StoreF32 {
   }
 };
 
-// Plain BF16 store of the accumulator (round to nearest even), 64 columns
-// per 128-byte row segment.
+// Plain BF16 store of the accumulator (round to nearest even): each 64-column
+// block of the warp's 32 rows is one TMA store box of `map` (C as [batch,
+// M, N]).
 struct StoreBF16 {
-  __nv_bfloat16* C;
-  int64_t ldc, batch_stride;
+  CUtensorMap map;
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
-    uint32_t* dst = reinterpret_cast<uint32_t*>(C + b * batch_stride +
-                                                static_cast<int64_t>(row0) * ldc + col0) +
-                    epi::lane_id();
 #pragma unroll 1
     for (int blk = 0; blk < NC / 64; ++blk) {
       float v[64];
@@ -119,14 +116,40 @@ struct StoreBF16 {
         const __nv_bfloat162 pr = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
         w[j] = *reinterpret_cast<const uint32_t*>(&pr);
       }
-      epi::put_rows(st, w);
-#pragma unroll 4
-      for (int r = 0; r < 32; ++r) dst[r * (ldc / 2) + 32 * blk] = epi::get(st, r);
+      epi::store_box(st, w, &map, col0 + 64 * blk, row0, b);
     }
   }
 };
 
 }  // namespace
+
+int make_tmap_rows(CUtensorMap* map, const void* base, bool f32, int64_t cols, int64_t rows,
+                   int64_t batch, int64_t row_stride, int64_t batch_stride) {
+  auto fn = encode_fn();
+  if (fn == nullptr)
+    return set_error(GBSGMC_ERR_CUDA, "tensor map: cuTensorMapEncodeTiled unavailable");
+  const int es = f32 ? 4 : 2;
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0 || (row_stride * es) % 16 != 0 ||
+      (batch_stride * es) % 16 != 0 || (cols * es) % 128 != 0 || rows % 32 != 0)
+    return set_error(GBSGMC_ERR_ARG,
+                     "output tensor map: base 16-byte aligned, 16-byte strides, rows of "
+                     "whole 128-byte boxes, 32-row boxes");
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows),
+                              static_cast<cuuint64_t>(batch)};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(row_stride) * es,
+                                 static_cast<cuuint64_t>(batch_stride) * es};
+  const cuuint32_t box[3] = {static_cast<cuuint32_t>(128 / es), 32, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r =
+      fn(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+         const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return set_error(GBSGMC_ERR_CUDA, "cuTensorMapEncodeTiled (output) failed (%d)",
+                     static_cast<int>(r));
+  return GBSGMC_OK;
+}
 
 int make_tmap_bf16_4d(CUtensorMap* map, const void* base, const int64_t (&dims)[4],
                       const int64_t (&strides)[3], const int (&box)[4]) {
@@ -275,7 +298,16 @@ extern "C" int gbsgmc_gemm_bf16_c16(int a_mn, int b_mn, const void* A_dev, int64
   if (ldc % 8 != 0 || c_batch_stride % 8 != 0)
     return set_error(GBSGMC_ERR_ARG, "gemm_bf16_c16: ldc and the C batch stride must be "
                      "multiples of 8");
-  const StoreBF16 epi{static_cast<__nv_bfloat16*>(C_dev), ldc, c_batch_stride};
+  if (batch > 0 && M > 0 && N > 0 && ldc >= N && c_batch_stride >= 0 &&
+      (M % 32 != 0 || N % 64 != 0 || reinterpret_cast<uintptr_t>(C_dev) % 16 != 0))
+    return set_error(GBSGMC_ERR_SHAPE, "gemm_bf16_c16: needs M %% 32, N %% 64 and a 16-byte "
+                     "aligned C");
+  StoreBF16 epi;
+  if (batch > 0 && M > 0 && N > 0 && ldc >= N && C_dev != nullptr) {
+    const int rc = make_tmap_rows(&epi.map, C_dev, false, N, M, batch, ldc,
+                                  batch > 1 ? c_batch_stride : int64_t(M) * ldc);
+    if (rc != GBSGMC_OK) return rc;
+  }
   return plain_gemm(a_mn, b_mn, A_dev, lda, a_batch_stride, B_dev, ldb, b_batch_stride, C_dev,
                     ldc, c_batch_stride, batch, M, N, K, kWaitLimitNs, status_dev, stream, epi);
 }

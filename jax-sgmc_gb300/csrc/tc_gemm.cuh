@@ -26,42 +26,74 @@ __host__ __device__ constexpr int gemm_stages(int bn) {
 constexpr int kGemmSplit = 2;    // epilogue warps per TMEM lane quarter
 constexpr int kGemmEpiWarps = 4 * kGemmSplit;
 constexpr int kGemmThreads = 64 + 32 * kGemmEpiWarps;  // producer, MMA, epilogue
-constexpr int kStageWords = 32 * 33;  // per-warp staging tile (32 x 32 words, padded)
+constexpr int kStageWords = 32 * 32;  // per-warp staging tile (32 x 32 words, 4 KB)
 
 // Epilogue staging helpers.  A warp's 32 lanes own 32 consecutive
 // accumulator rows; these move a 32-row block between that row-per-lane form
-// and row-contiguous global memory through the warp's staging tile, so that
-// every global access is one 128-byte row segment.
+// and row-contiguous global memory through the warp's 4 KB staging tile
+// (1024-byte aligned), so that every global access is one 128-byte row
+// segment.  Word j of row r sits at r * 32 + (j ^ r): a row written by one
+// lane and a column read across lanes both touch 32 distinct banks.  The
+// tile may also hold a TMA store's box (store_box); the helpers that write
+// it first wait until such a store has read it.
 namespace epi {
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
+// Waits until the warp's last TMA store (store_box) has read the staging
+// tile; warp-collective.
+__device__ __forceinline__ void reclaim() {
+  if (lane_id() == 0) tc::bulk_wait_read();
+  __syncwarp();
+}
 
 // Lane l's 32 words go to staging row l; afterwards any lane may read row r.
 __device__ __forceinline__ void put_rows(uint32_t* st, const uint32_t (&w)[32]) {
   const int l = lane_id();
-  __syncwarp();
+  reclaim();
 #pragma unroll
-  for (int j = 0; j < 32; ++j) st[l * 33 + j] = w[j];
+  for (int j = 0; j < 32; ++j) st[l * 32 + (j ^ l)] = w[j];
   __syncwarp();
 }
 
 // Word `lane` of staging row r.
 __device__ __forceinline__ uint32_t get(const uint32_t* st, int r) {
-  return st[r * 33 + lane_id()];
+  return st[r * 32 + (lane_id() ^ r)];
 }
 
-// The reverse: word `lane` of row r was written by the whole warp (set),
-// and lane l collects its own row.
+// The reverse: word `lane` of row r was written by the whole warp (set,
+// after reclaim), and lane l collects its own row.
 __device__ __forceinline__ void set(uint32_t* st, int r, uint32_t v) {
-  st[r * 33 + lane_id()] = v;
+  st[r * 32 + (lane_id() ^ r)] = v;
 }
 __device__ __forceinline__ void get_row(const uint32_t* st, uint32_t (&w)[32]) {
   const int l = lane_id();
   __syncwarp();
 #pragma unroll
-  for (int j = 0; j < 32; ++j) w[j] = st[l * 33 + j];
+  for (int j = 0; j < 32; ++j) w[j] = st[l * 32 + (j ^ l)];
   __syncwarp();
+}
+
+// Stores the warp's 32 rows of 128 bytes (lane l's words w = row l) as one
+// box of a tensor map with a 128-byte swizzle and a box of 128 bytes x 32
+// rows, at coordinates (x, y, z): the rows are written to the staging tile
+// in the swizzled order (16-byte chunk q of row r at chunk q ^ (r & 7)) and
+// one lane issues the TMA store, which runs on while the warp continues.
+// The epilogue kernels wait for the stores before they exit.
+__device__ __forceinline__ void store_box(uint32_t* st, const uint32_t (&w)[32],
+                                          const CUtensorMap* map, int x, int y, int z) {
+  const int l = lane_id();
+  reclaim();
+  uint8_t* row = reinterpret_cast<uint8_t*>(st) + l * 128;
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    tc::sts128(row + ((q ^ (l & 7)) << 4), w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+  tc::fence_async_shared();
+  __syncwarp();
+  if (l == 0) {
+    tc::tma_store_3d(map, st, x, y, z);
+    tc::bulk_commit();
+  }
 }
 
 }  // namespace epi
@@ -76,6 +108,12 @@ int make_tmap_bf16_3d(CUtensorMap* map, const void* base, int64_t cols,
 // with a 128-byte swizzled box; dims[0] x 2 bytes of a box row must be 128.
 int make_tmap_bf16_4d(CUtensorMap* map, const void* base, const int64_t (&dims)[4],
                       const int64_t (&strides)[3], const int (&box)[4]);
+
+// 3-D tensor map (cols innermost, rows, batch) of an epilogue's output for
+// epi::store_box: 128-byte swizzle, boxes of 128 bytes x 32 rows (64 BF16 or
+// 32 fp32 columns); strides in elements.
+int make_tmap_rows(CUtensorMap* map, const void* base, bool f32, int64_t cols, int64_t rows,
+                   int64_t batch, int64_t row_stride, int64_t batch_stride);
 
 size_t gemm_smem_bytes(int bn);
 
@@ -154,7 +192,7 @@ __device__ __forceinline__ int ragged_batch(const GemmRagged& rg, int t, int per
 // with row0 the first of the warp's 32 rows (lane l holds row row0 + l),
 // col0 its first column, load(c, v) filling v[32] with columns
 // [32c, 32c + 32) of the lane's row (warp-collective), and stage a private
-// 32 x 33-word shared-memory tile for the epi:: helpers.
+// 4 KB shared-memory tile (1024-byte aligned) for the epi:: helpers.
 //
 // Every wait is bounded (rg.wait_ns, kWaitLimitNs by default): on a timeout
 // the CTA records GBSGMC_ERR_TIMEOUT, stops issuing work, waits (bounded by
@@ -164,7 +202,7 @@ template <int BN, bool A_MN, bool B_MN, class Epi>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap ta,
                    const __grid_constant__ CUtensorMap tb, int M, int N, int K,
-                   int batch, int* status, Epi epi, GemmRagged rg) {
+                   int batch, int* status, const __grid_constant__ Epi epi, GemmRagged rg) {
   constexpr int BM = kGemmBM, BK = kGemmBK, STAGES = gemm_stages(BN);
   constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
   constexpr uint32_t BLOCK_BYTES = 64 * BK * 2;  // one 64 x 64 MN-major box
@@ -347,6 +385,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty[buf]);
     }
+    if (lane == 0) tc::bulk_wait();  // the epilogue's TMA stores
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -408,7 +447,7 @@ template <int BN, bool A_MN, bool B_MN, class Epi>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
     tc_gemm2_kernel(const __grid_constant__ CUtensorMap ta,
                     const __grid_constant__ CUtensorMap tb, int M, int N, int K, int batch,
-                    int* status, Epi epi, uint64_t wait_ns) {
+                    int* status, const __grid_constant__ Epi epi, uint64_t wait_ns) {
   constexpr int BM = 2 * kGemmBM;  // rows of a pair tile, kGemmBM per CTA
   constexpr int BK = kGemmBK, STAGES = kGemm2Stages;
   constexpr int BNH = BN / 2;      // B rows held by each CTA
@@ -571,6 +610,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
       // else has to be ordered before the leader may overwrite them.
       if (lane == 0) tc::mbar_arrive_cluster_relaxed(buf ? drained1 : drained0);
     }
+    if (lane == 0) tc::bulk_wait();  // the epilogue's TMA stores
   }
   tc::fence_before_sync();
   __syncthreads();
