@@ -23,7 +23,14 @@
 //   inputs   dX = sum over taps of dY shifted back by the tap times the tap's
 //            W^T (the transposed convolution), A = dY (K-major), B = W
 //            (K-major), then the pooling's argmax routing and the ReLU mask.
-// Col is materialised for conv1 and conv2 (3 and 32 input channels).  Where
+// conv1 reads its input by tap pairs from the images gathered as X8 [n, 32,
+// 32, 8]: pixel (h, w) holds the 3 channels of (h, w - 1), then its own 3,
+// then 2 zeros, so that one 16-byte core-matrix row of the unswizzled
+// layout serves the taps (kh, 0) and (kh, 1) together and another (kh, 2):
+// K = 3 kernel rows x 2 groups x 8 = 48 (padded to one 64-wide slice), each
+// group a shifted (16 W, 8 H) box; its weight gradient reads the same
+// boxes as an MN-major B.  Col is materialised for conv2 (32 input
+// channels).  Where
 // a tap's input channels fill a 128-byte row (64 BF16: conv3's input P2 and
 // the output gradients dY2, dY3 of the transposed convolutions) the GEMMs
 // are implicit: each 64-wide K slice of A (or 64-wide N block of dW's B) is
@@ -56,7 +63,10 @@ using bf16 = __nv_bfloat16;
 constexpr int kImg = 32, kInC = 3, kClasses = 10;
 constexpr int kC1 = 32, kC2 = 64, kC3 = 128;
 constexpr int kFlat = 4 * 4 * kC3;  // 2048
-constexpr int kK1 = 27, kK1p = 64;  // im2col widths (real, padded)
+constexpr int kK1 = 27;  // conv1's K (3 x 3 taps x 3 channels)
+constexpr int kX8 = 8;   // channels per gathered pixel: its left neighbour's 3, its own 3, 0, 0
+constexpr int kG1 = 8;   // conv1's K groups of 8 (6 real: kernel row kh, columns {0, 1} or {2})
+constexpr int kK1i = kG1 * kX8;  // conv1's GEMM K (one 64-wide slice)
 constexpr int kK2 = 9 * kC1, kK2p = 320;
 constexpr int kK3 = 9 * kC2;  // conv3 reads P2 by tap: no padded im2col
 constexpr int kA1ld = kC1;  // conv1 output-gradient channels as stored (the dW1
@@ -69,8 +79,8 @@ constexpr int64_t ob1 = 0, oW1 = ob1 + kC1, ob2 = oW1 + kK1 * kC1, oW2 = ob2 + k
 static_assert(kP == 113738, "parameter count");
 
 struct CnnLayout {
-  size_t w1b, w2b, w3b;               // BF16 HWIO copies
-  size_t col1, p1, col2, p2, p3;        // BF16 GEMM operands
+  size_t w1i, w2b, w3b;               // BF16 weights (conv1 unswizzled, others HWIO)
+  size_t x8, p1, col2, p2, p3;        // BF16 GEMM operands
   size_t dy1, dy2, dy3;               // BF16 output gradients of the convs
   size_t m1, m2, m3;                  // uint8 argmax of each pool window
   size_t dp2, dp1;                    // fp32 input gradients of conv3, conv2
@@ -98,10 +108,10 @@ CnnLayout cnn_layout(int chains, int n) {
     return at;
   };
   const size_t N = n;
-  L.w1b = take(2 * kK1 * kC1);
+  L.w1i = take(2 * kG1 * 64 * kX8);
   L.w2b = take(2 * kK2 * kC2);
   L.w3b = take(2 * kK3 * kC3);
-  L.col1 = take(2 * N * 1024 * kK1p);
+  L.x8 = take(2 * N * 1024 * kX8);
   L.dy1 = take(2 * N * 1024 * kA1ld);
   L.p1 = take(2 * N * 256 * kC1);
   L.col2 = take(2 * N * 256 * kK2p);
@@ -148,7 +158,7 @@ struct CnnArgs {
   float* lk;
   double* lk_var;
   int* status;
-  bf16 *w1b, *w2b, *w3b, *col1, *p1, *col2, *p2, *p3;
+  bf16 *w1i, *w2b, *w3b, *x8, *p1, *col2, *p2, *p3;
   float *dp2, *dp1;
   bf16 *dy1, *dy2, *dy3;
   uint8_t *m1, *m2, *m3;
@@ -161,20 +171,28 @@ struct CnnArgs {
 __device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
 
 // ---------------------------------------------------------------------------
-// Weights to BF16 (HWIO layout unchanged) and partial sums of squares.
-// Grid (kPrepBlocks, chains).
+// Weights to BF16 and partial sums of squares: conv2 and conv3 in HWIO
+// order, conv1 as the unswizzled K-major B of its GEMM, W1i [8 K groups][64
+// output channels][8 slots]: group g = 2 kh + p, slot s weighs input channel
+// s % 3 of tap (kh, p + s / 3); zero for s >= 6, for (p = 1, s < 3), for
+// groups >= 6 and outputs >= 32.  Grid (kPrepBlocks, chains).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) cnn_prep_kernel(const CnnArgs a) {
   __shared__ double red[32];
   const int c = blockIdx.y;
   const float* w = a.w + static_cast<int64_t>(c) * kP;
+  for (int e = blockIdx.x * 256 + threadIdx.x; e < kG1 * 64 * kX8; e += kPrepBlocks * 256) {
+    const int g = e / (64 * kX8), co = (e / kX8) % 64, sl = e % kX8;
+    const int kh = g >> 1, pp = g & 1, kw = pp + sl / kInC, ci = sl % kInC;
+    const bool real = g < 6 && co < kC1 && sl < 2 * kInC && (pp == 0 || sl >= kInC);
+    const float v = real ? __ldg(w + oW1 + ((kh * 3 + kw) * kInC + ci) * kC1 + co) : 0.f;
+    a.w1i[static_cast<int64_t>(c) * kG1 * 64 * kX8 + e] = __float2bfloat16_rn(v);
+  }
   float sq = 0.f;
   for (int64_t i = blockIdx.x * 256 + threadIdx.x; i < kP; i += kPrepBlocks * 256) {
     const float v = __ldg(w + i);
     sq = fmaf(v, v, sq);
-    if (i >= oW1 && i < ob2)
-      a.w1b[static_cast<int64_t>(c) * kK1 * kC1 + (i - oW1)] = __float2bfloat16_rn(v);
-    else if (i >= oW2 && i < ob3)
+    if (i >= oW2 && i < ob3)
       a.w2b[static_cast<int64_t>(c) * kK2 * kC2 + (i - oW2)] = __float2bfloat16_rn(v);
     else if (i >= oW3 && i < obd)
       a.w3b[static_cast<int64_t>(c) * kK3 * kC3 + (i - oW3)] = __float2bfloat16_rn(v);
@@ -184,27 +202,31 @@ __global__ void __launch_bounds__(256) cnn_prep_kernel(const CnnArgs a) {
 }
 
 // Row of pixel (h, w) of a 32 x 32 image in conv1's GEMM (and in its output
-// gradient dY1): rows come in blocks of 32, block b holding the half row
-// w in [16 (b & 1), 16 (b & 1) + 16) of image rows 2 (b >> 1) (lanes 0-15)
-// and 2 (b >> 1) + 1 (lanes 16-31), so that every 2 x 2 pool window lies in
-// one block, at lanes (l, l ^ 1, l ^ 16, l ^ 17).
+// gradient dY1): a 128-row tile holds the 16 columns w0 .. w0 + 15 (w0 = 0
+// or 16) of image rows 8u .. 8u + 7, the (16 W, 8 H) box of one TMA load
+// in row-major order.  Every 32 rows hold image rows 2k (lanes 0-15) and
+// 2k + 1 (lanes 16-31), so that every 2 x 2 pool window lies in one warp's
+// rows, at lanes (l, l ^ 1, l ^ 16, l ^ 17).
 __host__ __device__ __forceinline__ int conv1_row(int h, int w) {
-  return (((h >> 1) << 1) | (w >> 4)) * 32 + ((h & 1) << 4) + (w & 15);
+  return ((h >> 3) << 8) | ((w >> 4) << 7) | ((h & 7) << 4) | (w & 15);
+}
+// Its inverse: the pixel of row r (0 <= r < 1024).
+__host__ __device__ __forceinline__ void conv1_pixel(int r, int& h, int& w) {
+  h = ((r >> 8) << 3) | ((r >> 4) & 7);
+  w = (((r >> 7) & 1) << 4) | (r & 15);
 }
 
 // ---------------------------------------------------------------------------
-// Gather of the minibatch images straight into conv1's im2col matrix
-// Col1 [n*1024, 64] (K = (kh, kw, ci), 27 real; rows in conv1_row order),
-// plus labels.
-// Grid (n*1024/256, chains): one thread per output pixel.  (Eight threads
-// per row, each storing one 16-byte group, measured twice as slow.)
+// Gather of the minibatch images as BF16 X8 [n, 32, 32, 8] in natural pixel
+// order, pixel (h, w) holding channels 0-2 of (h, w - 1) (zero at w = 0),
+// channels 0-2 of (h, w) and two zeros, plus labels.
+// Grid (n*1024/256, chains): one thread per pixel, one 16-byte store each.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
+__global__ void __launch_bounds__(256) cnn_gather1_kernel(const CnnArgs a) {
   const int c = blockIdx.y;
   const int p = blockIdx.x * 256 + threadIdx.x;
   if (p >= a.n * 1024) return;
   const int i = p >> 10, hw = p & 1023;
-  const int h = hw >> 5, wq = hw & 31;
   int64_t o = a.idx[static_cast<int64_t>(c) * a.idx_stride + i];
   if (o < 0 || o >= a.n_rows) {
     raise_status(a.status, GBSGMC_ERR_INDEX);
@@ -219,32 +241,16 @@ __global__ void __launch_bounds__(256) cnn_im2col1_kernel(const CnnArgs a) {
     }
     a.lab[static_cast<int64_t>(c) * a.n + i] = lab;
   }
-  const float* img = a.X + o * a.ld;
-  uint32_t out[kK1p / 2];
-  float v[kK1p];
-#pragma unroll
-  for (int k = 0; k < kK1p; ++k) v[k] = 0.f;
-#pragma unroll
-  for (int kh = 0; kh < 3; ++kh)
-#pragma unroll
-    for (int kw = 0; kw < 3; ++kw) {
-      const int y = h + kh - 1, x = wq + kw - 1;
-      if (y >= 0 && y < kImg && x >= 0 && x < kImg) {
-#pragma unroll
-        for (int ci = 0; ci < kInC; ++ci)
-          v[(kh * 3 + kw) * kInC + ci] = __ldg(img + (y * kImg + x) * kInC + ci);
-      }
-    }
-#pragma unroll
-  for (int k = 0; k < kK1p / 2; ++k) {
-    const __nv_bfloat162 pr = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
-    out[k] = *reinterpret_cast<const uint32_t*>(&pr);
-  }
-  uint4* dst = reinterpret_cast<uint4*>(
-      a.col1 + (static_cast<int64_t>(c) * a.n * 1024 + i * 1024 + conv1_row(h, wq)) * kK1p);
-#pragma unroll
-  for (int k = 0; k < kK1p / 8; ++k)
-    dst[k] = make_uint4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+  const float* px = a.X + o * a.ld + hw * kInC;
+  const bool left = (hw & 31) != 0;
+  const float l0 = left ? __ldg(px - 3) : 0.f, l1 = left ? __ldg(px - 2) : 0.f,
+              l2 = left ? __ldg(px - 1) : 0.f;
+  const __nv_bfloat162 q0 = __floats2bfloat162_rn(l0, l1);
+  const __nv_bfloat162 q1 = __floats2bfloat162_rn(l2, __ldg(px));
+  const __nv_bfloat162 q2 = __floats2bfloat162_rn(__ldg(px + 1), __ldg(px + 2));
+  reinterpret_cast<uint4*>(a.x8)[static_cast<int64_t>(c) * a.n * 1024 + p] =
+      make_uint4(*reinterpret_cast<const uint32_t*>(&q0), *reinterpret_cast<const uint32_t*>(&q1),
+                 *reinterpret_cast<const uint32_t*>(&q2), 0u);
 }
 
 // ---------------------------------------------------------------------------
@@ -570,9 +576,10 @@ struct EpiConvPool {
     const int i = r / (H * W), rr = r % (H * W);
     int yp, xp;
     if (kConv1Rows) {
-      const int blk = rr >> 5, l = rr & 31;
-      yp = blk >> 1;
-      xp = ((blk & 1) * 16 + (l & 15)) >> 1;
+      int h, x;
+      conv1_pixel(rr, h, x);
+      yp = h >> 1;
+      xp = x >> 1;
     } else {
       yp = (rr / W) >> 1;
       xp = (rr % W) >> 1;
@@ -623,10 +630,14 @@ struct EpiConvPool {
 
 // Weights: element (row = output channel co, col = im2col column k) of the
 // split-K partial product of (virtual) batch bv = chain * splits + split
-// lands at part[bv][k][co] (HWIO order), rows < Cout, cols < K.
+// lands at part[bv][k][co] (HWIO order), rows < Cout, cols < K.  With x8 the
+// columns are conv1's K groups x 8 slots: column 8 g + s (g = 2 kh + p) is
+// input channel s % 3 of tap (kh, p + s / 3), for g < 6, s < 6, and p = 0
+// or s >= 3.
 struct EpiConvGradW {
   float* part;
   int Cout, K;
+  bool x8 = false;
   template <int NC, class Load>
   __device__ __forceinline__ void tile(int bv, int row0, int col0, const Load& load,
                                        uint32_t*) const {
@@ -640,7 +651,14 @@ struct EpiConvGradW {
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int k = col0 + 32 * cb + j;
-          if (k < K) dst[static_cast<int64_t>(k) * Cout] = v[j];
+          if (x8) {
+            const int g = k >> 3, sl = k & 7;
+            const int kw = (g & 1) + sl / kInC;
+            if (g < 6 && sl < 2 * kInC && ((g & 1) == 0 || sl >= kInC))
+              dst[static_cast<int64_t>(((g >> 1) * 3 + kw) * kInC + sl % kInC) * Cout] = v[j];
+          } else if (k < K) {
+            dst[static_cast<int64_t>(k) * Cout] = v[j];
+          }
         }
       }
     }
@@ -727,6 +745,84 @@ struct TransposedB : Inner {
   }
 };
 
+// conv1's operands, read by K group from the gathered images X8 and from its
+// weights W1i, unswizzled: a pixel's 8 slots (16 bytes) are one core-matrix
+// row.  X8 is mapped as image rows of 256 elements (32 pixels x 8 slots):
+// 4-D map (256, 32, chains * n, 1) with boxes (128, R, 1, 1), 16 pixels of
+// R rows (8 for the forward GEMM, 4 for the weight gradient), whose shift by
+// a group's column offset is 8 elements (16 bytes) per pixel; a box is R
+// rows of 256 bytes for TMA.  K group g = 2 kh + p of output pixel (h, w)
+// is the pixel (h + kh - 1, w + p) of X8 (zeros outside the image).
+// Groups 6 and 7 read a box wholly below the image (zeros).  W1i is mapped
+// as (256, 2, 8, chains), a group's 64 x 8 weights as two rows of 256, box
+// (256, 2, 8, 1).  Forward: the 128-row tile at m0 (columns w0 .. w0 + 15 of
+// image rows 8u .. 8u + 7, conv1_row order) is, per group, one box 2 KB
+// apart; B is the weights' box.
+template <class Inner>
+struct Conv1Fwd : Inner {
+  int n;
+  static constexpr bool kLoadA = true, kLoadB = true, kInterleaveA = true,
+                        kInterleaveB = true;
+  __device__ __forceinline__ void load_a(void* dst, const CUtensorMap* map, int, int m0, int b,
+                                         uint64_t* bar) const {
+    const int img = b * n + m0 / 1024, t = (m0 % 1024) / 128;
+    const int u = t >> 1, w0 = (t & 1) * 16;
+    uint8_t* d = static_cast<uint8_t*>(dst);
+#pragma unroll
+    for (int g = 0; g < kG1; ++g) {
+      const int kh = g >> 1, dx = g & 1;
+      const int y = g < 6 ? 8 * u + kh - 1 : 64;
+      tc::tma_load_4d(d + g * 2048, map, (w0 + dx) * kX8, y, img, 0, bar);
+    }
+  }
+  __device__ __forceinline__ void load_b(void* dst, const CUtensorMap* map, int nn, int, int b,
+                                         uint64_t* bar) const {
+    tc::tma_load_4d(dst, map, 0, nn / 32, 0, b, bar);
+  }
+};
+
+// conv1's weight gradient dW1 = dY1^T Col1 with Col1 read from X8: the
+// 64-pixel K slice k0 (the upper or lower 4 rows of a conv1 tile, conv1_row
+// order) of the MN-major B is, per real K group (0-5), that slice's (16 W,
+// 4 H) box shifted by the group, 1 KB apart.  Only the parts of the stage
+// whose products are stored are loaded: A's first 64 rows (output channels;
+// 32 real) and B's first 48 columns; the MMAs' other rows and columns read
+// whatever the stage held and the epilogue drops them.
+template <class Inner>
+struct Conv1Bmn : Inner {
+  int n;
+  static constexpr bool kLoadA = true, kLoadB = true, kInterleaveB = true;
+  static constexpr uint32_t kStageBytes = 64 * kGemmBK * 2 + 6 * 1024;
+  __device__ __forceinline__ void load_a(void* dst, const CUtensorMap* map, int k0, int m0,
+                                         int b, uint64_t* bar) const {
+    tc::tma_load_3d(dst, map, m0, k0, b, bar);
+  }
+  __device__ __forceinline__ void load_b(void* dst, const CUtensorMap* map, int, int k0, int b,
+                                         uint64_t* bar) const {
+    const int img = b * n + k0 / 1024, rr = k0 % 1024, t = rr >> 7;
+    const int h0 = 8 * (t >> 1) + 4 * ((rr >> 6) & 1), w0 = (t & 1) * 16;
+    uint8_t* d = static_cast<uint8_t*>(dst);
+#pragma unroll
+    for (int g = 0; g < 6; ++g) {
+      const int kh = g >> 1, dx = g & 1;
+      tc::tma_load_4d(d + g * 1024, map, (w0 + dx) * kX8, h0 + kh - 1, img, 0, bar);
+    }
+  }
+};
+
+// A weight gradient whose output channels fill only the first 64 of the
+// GEMM's 128 rows: A's first 64 rows are loaded (one MN-major box), the
+// MMAs' other rows read whatever the stage held and the epilogue drops them.
+template <class Inner>
+struct HalfA : Inner {
+  static constexpr bool kLoadA = true;
+  static constexpr uint32_t kStageBytes = 2 * 64 * kGemmBK * 2;
+  __device__ __forceinline__ void load_a(void* dst, const CUtensorMap* map, int k0, int m0,
+                                         int b, uint64_t* bar) const {
+    tc::tma_load_3d(dst, map, m0, k0, b, bar);
+  }
+};
+
 template <class T>
 T* view(void* ws, size_t off) {
   return reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + off);
@@ -735,10 +831,10 @@ T* view(void* ws, size_t off) {
 int grid1(int64_t work) { return static_cast<int>((work + 255) / 256); }
 
 int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
-  a.w1b = view<bf16>(ws, L.w1b);
+  a.w1i = view<bf16>(ws, L.w1i);
   a.w2b = view<bf16>(ws, L.w2b);
   a.w3b = view<bf16>(ws, L.w3b);
-  a.col1 = view<bf16>(ws, L.col1);
+  a.x8 = view<bf16>(ws, L.x8);
   a.dy1 = view<bf16>(ws, L.dy1);
   a.p1 = view<bf16>(ws, L.p1);
   a.col2 = view<bf16>(ws, L.col2);
@@ -778,7 +874,8 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
                          int K, int Kp, int64_t rows, int64_t off) {
     GemmRagged rg;
     rg.ksplit = wsplit(layer, n);
-    const EpiConvGradW e{a.part, Cout, K};
+    if (Cout > 64) return set_error(GBSGMC_ERR_ARG, "cnn: weight gradient with %d outputs", Cout);
+    const HalfA<EpiConvGradW> e{{a.part, Cout, K}};
     int r = launch_gemm<64, true, true>(mdy, mcol, C, 128, Kp, static_cast<int>(rows), a.status,
                                         e, st, rg);
     if (r) return r;
@@ -789,15 +886,22 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
 
   cnn_prep_kernel<<<dim3(kPrepBlocks, C), 256, 0, st>>>(a);
   if ((rc = launched("cnn_prep_kernel"))) return rc;
-  cnn_im2col1_kernel<<<dim3(grid1(r1), C), 256, 0, st>>>(a);
-  if ((rc = launched("cnn_im2col1_kernel"))) return rc;
+  cnn_gather1_kernel<<<dim3(grid1(r1), C), 256, 0, st>>>(a);
+  if ((rc = launched("cnn_gather1_kernel"))) return rc;
 
   // Tensor maps (columns, rows, chains), and 4-D maps (channels, W, H,
   // images) of the NHWC maps the implicit GEMMs read by tap.
   const int64_t imgs = int64_t(C) * n;
-  CUtensorMap m_col1, m_w1, m_col2, m_w2, m_w3, m_p2a;
-  if ((rc = make_tmap_bf16_3d(&m_col1, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, kGemmBK, kGemmBM)) ||
-      (rc = make_tmap_bf16_3d(&m_w1, a.w1b, kC1, kK1, C, kC1, kK1 * kC1, 64, 64)) ||
+  CUtensorMap m_x8, m_x8h, m_w1i, m_col2, m_w2, m_w3, m_p2a;
+  if ((rc = make_tmap_bf16_4d_plain(&m_x8, a.x8, {32 * kX8, 32, imgs, 1},
+                                    {32 * kX8, 1024 * kX8, imgs * 1024 * kX8},
+                                    {16 * kX8, 8, 1, 1})) ||
+      (rc = make_tmap_bf16_4d_plain(&m_x8h, a.x8, {32 * kX8, 32, imgs, 1},
+                                    {32 * kX8, 1024 * kX8, imgs * 1024 * kX8},
+                                    {16 * kX8, 4, 1, 1})) ||
+      (rc = make_tmap_bf16_4d_plain(&m_w1i, a.w1i, {32 * kX8, 2, kG1, C},
+                                    {32 * kX8, 64 * kX8, kG1 * 64 * kX8},
+                                    {32 * kX8, 2, kG1, 1})) ||
       (rc = make_tmap_bf16_3d(&m_col2, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, kGemmBK, kGemmBM)) ||
       (rc = make_tmap_bf16_3d(&m_w2, a.w2b, kC2, kK2, C, kC2, kK2 * kC2, 64, 64)) ||
       (rc = make_tmap_bf16_3d(&m_w3, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, 64, 64)) ||
@@ -805,12 +909,12 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
                               {64, 8, 8, 2})))
     return rc;
 
-  // conv1+pool1 -> im2col2 -> conv2+pool2 -> conv3+pool3 (implicit): each
-  // conv GEMM's epilogue writes the pooled BF16 map and the marks.  conv1
-  // runs as N = 64 (the weight map's zero fill beyond 32 channels); its
-  // epilogue skips the padding columns.
-  const EpiConvPool<32, 32, 16, true> e1{a.w, ob1, kC1, a.p1, a.m1, n};
-  if ((rc = launch_gemm<64, false, true>(m_col1, m_w1, C, r1, 64, kK1p, a.status, e1, st)))
+  // conv1+pool1 (implicit) -> im2col2 -> conv2+pool2 -> conv3+pool3
+  // (implicit): each conv GEMM's epilogue writes the pooled BF16 map and the
+  // marks.  conv1 runs as N = 64 (W1i's zero output channels past 32) and
+  // K = 8 groups x 8 slots; its epilogue skips the padding columns.
+  const Conv1Fwd<EpiConvPool<32, 32, 16, true>> e1{{a.w, ob1, kC1, a.p1, a.m1, n}, n};
+  if ((rc = launch_gemm<64, false, false>(m_x8, m_w1i, C, r1, 64, kK1i, a.status, e1, st)))
     return rc;
   cnn_im2col_kernel<16, 16, kC1, kK2p><<<dim3(grid1(r2 * kK2p / 8), C), 256, 0, st>>>(
       a.p1, a.col2, n);
@@ -881,11 +985,21 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     cnn_unpool_kernel<32, 32, kC1, kA1ld, true><<<unpool_grid(32, kC1), 256, 0, st>>>(
         a.dy1, a.m1, a.dp1, n, a.bpart);
     if ((rc = launched("cnn_unpool_kernel 1")) || (rc = bias_sum(32, kC1, ob1))) return rc;
-    CUtensorMap m_dy1t, m_col1t;
-    if ((rc = make_tmap_bf16_3d(&m_dy1t, a.dy1, kA1ld, r1, C, kA1ld, r1 * kA1ld, 64, 64)) ||
-        (rc = make_tmap_bf16_3d(&m_col1t, a.col1, kK1p, r1, C, kK1p, r1 * kK1p, 64, 64)))
+    // dW1 = dY1^T Col1, Col1 read by K group from X8 (N = 8 groups x 8 slots).
+    CUtensorMap m_dy1t;
+    if ((rc = make_tmap_bf16_3d(&m_dy1t, a.dy1, kA1ld, r1, C, kA1ld, r1 * kA1ld, 64, 64)))
       return rc;
-    if ((rc = weight_grad(m_dy1t, m_col1t, 1, kC1, kK1, kK1p, r1, oW1))) return rc;
+    {
+      GemmRagged rg;
+      rg.ksplit = wsplit(1, n);
+      const Conv1Bmn<EpiConvGradW> e{{a.part, kC1, kK1, true}, n};
+      if ((rc = launch_gemm<64, true, true>(m_dy1t, m_x8h, C, 128, kK1i, static_cast<int>(r1),
+                                            a.status, e, st, rg)))
+        return rc;
+      cnn_wsum_kernel<<<dim3(grid1(int64_t(kK1) * kC1), C), 256, 0, st>>>(a.part, rg.ksplit,
+                                                                          kK1 * kC1, a.grad, oW1);
+      if ((rc = launched("cnn_wsum_kernel"))) return rc;
+    }
   }
 
   const double s2 = static_cast<double>(a.prior_scale) * a.prior_scale;

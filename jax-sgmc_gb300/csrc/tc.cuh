@@ -183,6 +183,18 @@ __device__ __forceinline__ uint64_t sdesc_mn_sw128(const void* tile,
   return d;
 }
 
+// Shared-memory descriptor of a tile in the unswizzled layout: core matrices
+// of 8 rows x 16 bytes (128 contiguous bytes), `lbo` bytes apart along K and
+// `sbo` bytes apart along M or N (for K-major and MN-major tiles alike).
+__device__ __forceinline__ uint64_t sdesc_none(const void* tile, uint32_t lbo, uint32_t sbo) {
+  const uint64_t addr = smem_addr(tile);
+  uint64_t d = (addr >> 4) & 0x3FFFull;
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+  d |= 1ull << 46;  // descriptor version; layout type 0: no swizzle
+  return d;
+}
+
 // D[tmem] (+)= A[smem] * B[smem]^T for one K=16 slice (single thread).
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc,
                                          uint64_t b_desc, uint32_t idesc,

@@ -123,6 +123,32 @@ struct StoreBF16 {
 
 }  // namespace
 
+int make_tmap_bf16_4d_plain(CUtensorMap* map, const void* base, const int64_t (&dims)[4],
+                            const int64_t (&strides)[3], const int (&box)[4]) {
+  auto fn = encode_fn();
+  if (fn == nullptr)
+    return set_error(GBSGMC_ERR_CUDA, "tensor map: cuTensorMapEncodeTiled unavailable");
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0 || strides[0] % 8 != 0 ||
+      strides[1] % 8 != 0 || strides[2] % 8 != 0 || box[0] % 8 != 0)
+    return set_error(GBSGMC_ERR_ARG,
+                     "tensor map (4-D, unswizzled): base 16-byte aligned, strides multiples "
+                     "of 8 elements, box rows of whole 16-byte units");
+  cuuint64_t d[4], st[3];
+  cuuint32_t bx[4], es[4] = {1, 1, 1, 1};
+  for (int i = 0; i < 4; ++i) {
+    d[i] = static_cast<cuuint64_t>(dims[i]);
+    bx[i] = static_cast<cuuint32_t>(box[i]);
+  }
+  for (int i = 0; i < 3; ++i) st[i] = static_cast<cuuint64_t>(strides[i]) * 2;
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), d,
+                        st, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return set_error(GBSGMC_ERR_CUDA, "cuTensorMapEncodeTiled (4-D, unswizzled) failed (%d)",
+                     static_cast<int>(r));
+  return GBSGMC_OK;
+}
+
 int make_tmap_rows(CUtensorMap* map, const void* base, bool f32, int64_t cols, int64_t rows,
                    int64_t batch, int64_t row_stride, int64_t batch_stride) {
   auto fn = encode_fn();

@@ -109,6 +109,12 @@ int make_tmap_bf16_3d(CUtensorMap* map, const void* base, int64_t cols,
 int make_tmap_bf16_4d(CUtensorMap* map, const void* base, const int64_t (&dims)[4],
                       const int64_t (&strides)[3], const int (&box)[4]);
 
+// 4-D BF16 tensor map without swizzle (dims[0] innermost, strides of dims
+// 1..3 in elements), for the unswizzled operand layouts: a box row of
+// box[0] BF16 (a multiple of 8) lands as box[0] * 2 contiguous bytes.
+int make_tmap_bf16_4d_plain(CUtensorMap* map, const void* base, const int64_t (&dims)[4],
+                            const int64_t (&strides)[3], const int (&box)[4]);
+
 // 3-D tensor map (cols innermost, rows, batch) of an epilogue's output for
 // epi::store_box: 128-byte swizzle, boxes of 128 bytes x 32 rows (64 BF16 or
 // 32 fp32 columns); strides in elements.
@@ -127,6 +133,35 @@ size_t gemm_smem_bytes(int bn);
 // the producer calls these instead, e.g. to read shifted boxes of an NHWC
 // map for an implicit convolution.  They must load the bytes the default
 // loads would.
+// Partial stages.  An epilogue type whose loaders fill only part of a stage
+// (rows of A or columns of B whose products it never stores) declares the
+// bytes they deliver per stage as `static constexpr uint32_t kStageBytes`;
+// the producer expects that many instead of the full A and B tiles.  An
+// MN-major A is then loaded by its load_a too.
+template <class E, class = void>
+struct StageBytes : std::integral_constant<uint32_t, 0> {};
+template <class E>
+struct StageBytes<E, std::void_t<decltype(E::kStageBytes)>>
+    : std::integral_constant<uint32_t, E::kStageBytes> {};
+
+// Unswizzled operand layouts.  With `static constexpr bool kInterleaveA =
+// true` (kInterleaveB) the epilogue type's load_a (load_b) fills the stage in
+// the unswizzled core-matrix layout instead of the 128-byte swizzle: for a
+// K-major operand of R rows (128 for A, BN for B) the core matrix of row
+// group g and K group j (8 rows x 8 BF16) at j * R * 16 + g * 128 bytes; for
+// an MN-major B the core matrix of N group j and K group g at j * 1024 +
+// g * 128 (each 64-row K slice of 8 N columns is 1 KB).
+template <class E, class = void>
+struct InterleaveA : std::false_type {};
+template <class E>
+struct InterleaveA<E, std::void_t<decltype(E::kInterleaveA)>>
+    : std::bool_constant<E::kInterleaveA> {};
+template <class E, class = void>
+struct InterleaveB : std::false_type {};
+template <class E>
+struct InterleaveB<E, std::void_t<decltype(E::kInterleaveB)>>
+    : std::bool_constant<E::kInterleaveB> {};
+
 template <class E, class = void>
 struct LoadsA : std::false_type {};
 template <class E>
@@ -276,9 +311,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             ok = false;
             break;
           }
-          mbar_arrive_expect_tx(&full[s], A_BYTES + B_BYTES);
+          constexpr uint32_t TX =
+              StageBytes<Epi>::value != 0 ? StageBytes<Epi>::value : A_BYTES + B_BYTES;
+          mbar_arrive_expect_tx(&full[s], TX);
           const int k0 = (kb0 + kb) * BK;
-          if constexpr (A_MN) {
+          if constexpr (A_MN && LoadsA<Epi>::value) {
+            epi.load_a(sa + s * A_BYTES, &ta, k0, m0, b, &full[s]);
+          } else if constexpr (A_MN) {
 #pragma unroll
             for (int j = 0; j < BM / 64; ++j)
               tc::tma_load_3d(sa + s * A_BYTES + j * BLOCK_BYTES, &ta, m0 + 64 * j, k0, b,
@@ -337,16 +376,24 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             break;
           }
           tc::fence_after_sync();
-          const uint64_t a0 = A_MN ? tc::sdesc_mn_sw128(sa + s * A_BYTES, BLOCK_BYTES)
-                                   : tc::sdesc_k_sw128(sa + s * A_BYTES);
-          const uint64_t b0 = B_MN ? tc::sdesc_mn_sw128(sb + s * B_BYTES, BLOCK_BYTES)
-                                   : tc::sdesc_k_sw128(sb + s * B_BYTES);
+          constexpr bool IA = InterleaveA<Epi>::value, IB = InterleaveB<Epi>::value;
+          static_assert(!(IA && A_MN), "an unswizzled A is K-major");
+          // Descriptor steps per K = 16 slice, in 16-byte units: 32 bytes
+          // along a swizzled K-major row, two 8-row groups (2048 bytes) of a
+          // swizzled MN-major tile, two K groups of an unswizzled tile.
+          constexpr uint32_t step_a = IA ? 2 * BM : A_MN ? 128 : 2;
+          constexpr uint32_t step_b = IB ? (B_MN ? 16 : 2 * BN) : B_MN ? 128 : 2;
+          const uint64_t a0 = IA     ? tc::sdesc_none(sa + s * A_BYTES, BM * 16, 128)
+                              : A_MN ? tc::sdesc_mn_sw128(sa + s * A_BYTES, BLOCK_BYTES)
+                                     : tc::sdesc_k_sw128(sa + s * A_BYTES);
+          const uint64_t b0 = IB     ? (B_MN ? tc::sdesc_none(sb + s * B_BYTES, 128, 1024)
+                                             : tc::sdesc_none(sb + s * B_BYTES, BN * 16, 128))
+                              : B_MN ? tc::sdesc_mn_sw128(sb + s * B_BYTES, BLOCK_BYTES)
+                                     : tc::sdesc_k_sw128(sb + s * B_BYTES);
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {
-            // K=16 advances 32 bytes along a K-major row, or two 8-row
-            // groups (2048 bytes) of an MN-major tile; descriptors count 16 B.
-            const uint64_t da = A_MN ? 128u * k : 2u * k;
-            const uint64_t db = B_MN ? 128u * k : 2u * k;
+            const uint64_t da = static_cast<uint64_t>(step_a) * k;
+            const uint64_t db = static_cast<uint64_t>(step_b) * k;
             tc::mma_bf16(d, a0 + da, b0 + db, idesc, (kb | k) != 0);
           }
           tc::mma_commit(&empty[s]);
@@ -455,6 +502,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
   constexpr uint32_t BLOCK_BYTES = 64 * BK * 2;  // one 64 x 64 MN-major box
   constexpr uint32_t TMEM_COLS = 2 * BN;
   static_assert(BN == 256, "pair tiles are 256 x 256");
+  static_assert(!LoadsA<Epi>::value && !LoadsB<Epi>::value && !InterleaveA<Epi>::value &&
+                    !InterleaveB<Epi>::value,
+                "pair tiles take no operand loaders");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
