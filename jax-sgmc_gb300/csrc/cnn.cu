@@ -280,35 +280,65 @@ __global__ void __launch_bounds__(256) cnn_im2col_kernel(const bf16* Pin, bf16* 
 }
 
 // ---------------------------------------------------------------------------
-// Dense layer, softmax likelihood and its adjoint: one block of 128 threads
-// per (image, chain).  Writes lk, dlogits g = dU/dlogits (fp32), dP3 = g Wd^T
-// and the per-image likelihood terms.
+// Dense layer, softmax likelihood and its adjoint for kDenseImgs images of a
+// chain per block.  Writes lk, dlogits g = dU/dlogits (fp32), dP3 = g Wd^T
+// and the per-image likelihood terms.  Grid (ceil(n / kDenseImgs), chains),
+// 16 threads per image: thread (image j = t / 16, slice s = t % 16) handles
+// the features f = s, s + 16, ...; an image's 16 threads are one half-warp
+// and reduce by shuffles.  The block first copies Wd (80 KB) and its images'
+// P3 rows (4 KB each) into shared memory with all loads in flight: a
+// half-warp then reads 16 Wd rows 40 bytes apart, 16 distinct banks (the
+// other half-warp the same words), and 16 consecutive P3 features.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) cnn_dense_kernel(const CnnArgs a) {
-  __shared__ float part[kClasses][4];
-  __shared__ float g_s[kClasses];
-  const int i = blockIdx.x, c = blockIdx.y, t = threadIdx.x;
+constexpr int kDenseImgs = 16;
+static_assert(oWd % 2 == 0 && kP % 2 == 0, "Wd is copied as float2");
+constexpr size_t kDenseSmem =
+    sizeof(float) * kFlat * kClasses + sizeof(bf16) * kDenseImgs * kFlat;
+
+__global__ void __launch_bounds__(kDenseImgs * 16) cnn_dense_kernel(const CnnArgs a) {
+  extern __shared__ float wd_s[];  // Wd [2048][10], then P3 rows [kDenseImgs][2048]
+  bf16* x_s = reinterpret_cast<bf16*>(wd_s + kFlat * kClasses);
+  __shared__ float g_s[kDenseImgs][kClasses];
+  const unsigned full = 0xffffffffu;
+  const int c = blockIdx.y, t = threadIdx.x, j = t >> 4, sl = t & 15;
+  const int i = blockIdx.x * kDenseImgs + j;
+  const bool live = i < a.n;
   const float* w = a.w + static_cast<int64_t>(c) * kP;
-  const bf16* x = a.p3 + (static_cast<int64_t>(c) * a.n + i) * kFlat;
+  {
+    // oWd and kP are even: the chain's Wd starts 8-byte aligned.
+    const float2* src = reinterpret_cast<const float2*>(w + oWd);
+    float2* dst = reinterpret_cast<float2*>(wd_s);
+#pragma unroll 8
+    for (int e = t; e < kFlat * kClasses / 2; e += kDenseImgs * 16) dst[e] = __ldg(src + e);
+    // The block's images, 16 bytes per load (rows past n are not read).
+    const int i0 = blockIdx.x * kDenseImgs;
+    const int rows = min(kDenseImgs, a.n - i0);
+    const uint4* xs = reinterpret_cast<const uint4*>(a.p3 + (static_cast<int64_t>(c) * a.n + i0) * kFlat);
+    uint4* xd = reinterpret_cast<uint4*>(x_s);
+#pragma unroll 8
+    for (int e = t; e < kDenseImgs * kFlat / 8; e += kDenseImgs * 16)
+      if (e < rows * (kFlat / 8)) xd[e] = __ldg(xs + e);
+  }
+  __syncthreads();
+  const bf16* x = x_s + j * kFlat;
   float acc[kClasses];
 #pragma unroll
   for (int k = 0; k < kClasses; ++k) acc[k] = 0.f;
-  for (int f = t; f < kFlat; f += 128) {
-    const float xv = bf(x[f]);
-    const float* wr = w + oWd + static_cast<int64_t>(f) * kClasses;
+#pragma unroll 4
+  for (int f = sl; f < kFlat; f += 16) {
+    const float xv = live ? bf(x[f]) : 0.f;
+    const float* wr = wd_s + f * kClasses;
 #pragma unroll
-    for (int k = 0; k < kClasses; ++k) acc[k] = fmaf(xv, __ldg(wr + k), acc[k]);
+    for (int k = 0; k < kClasses; ++k) acc[k] = fmaf(xv, wr[k], acc[k]);
   }
 #pragma unroll
-  for (int k = 0; k < kClasses; ++k) {
-    const float s = warp_sum(acc[k]);
-    if ((t & 31) == 0) part[k][t >> 5] = s;
-  }
-  __syncthreads();
-  if (t == 0) {
+  for (int k = 0; k < kClasses; ++k)
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(full, acc[k], off);
+  if (sl == 0 && live) {
     float logit[kClasses], mx = -INFINITY;
     for (int k = 0; k < kClasses; ++k) {
-      logit[k] = part[k][0] + part[k][1] + part[k][2] + part[k][3] + __ldg(w + obd + k);
+      logit[k] = acc[k] + __ldg(w + obd + k);
       mx = fmaxf(mx, logit[k]);
     }
     float se = 0.f;
@@ -321,7 +351,7 @@ __global__ void __launch_bounds__(128) cnn_dense_kernel(const CnnArgs a) {
     for (int k = 0; k < kClasses; ++k) {
       const float pk = expf(logit[k] - lse);
       const float g = -scale * m * ((k == lab ? 1.f : 0.f) - pk);
-      g_s[k] = g;
+      g_s[j][k] = g;
       a.gl[(static_cast<int64_t>(c) * a.n + i) * kClasses + k] = g;
     }
     if (a.lk != nullptr) a.lk[static_cast<int64_t>(c) * a.n + i] = lk;
@@ -333,22 +363,30 @@ __global__ void __launch_bounds__(128) cnn_dense_kernel(const CnnArgs a) {
   }
   if (!a.want_grad) return;
   __syncthreads();
-  float* dx = a.dp3 + (static_cast<int64_t>(c) * a.n + i) * kFlat;
-  for (int f = t; f < kFlat; f += 128) {
-    const float* wr = w + oWd + static_cast<int64_t>(f) * kClasses;
-    float s = 0.f;
+  if (!live) return;
+  float gk[kClasses];
 #pragma unroll
-    for (int k = 0; k < kClasses; ++k) s = fmaf(g_s[k], __ldg(wr + k), s);
-    dx[f] = s;
+  for (int k = 0; k < kClasses; ++k) gk[k] = g_s[j][k];
+  float* dx = a.dp3 + (static_cast<int64_t>(c) * a.n + i) * kFlat;
+#pragma unroll 4
+  for (int f = sl; f < kFlat; f += 16) {
+    const float* wr = wd_s + f * kClasses;
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < kClasses; ++k) sum = fmaf(gk[k], wr[k], sum);
+    dx[f] = sum;
   }
 }
 
 // dWd [2048, 10] = sum_i P3_i (x) g_i and dbd = sum_i g_i (likelihood part).
-// Grid (kFlat / 128 + 1, chains), 128 threads; dlogits staged in shared
-// memory (n <= 1024 images per pass).
-__global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
-  __shared__ float gs[1024 * kClasses];
-  const int c = blockIdx.y, t = threadIdx.x;
+// Grid (kFlat / 128 + 1, chains), 512 threads: feature f = 128 x + t % 128,
+// image group q = t / 128 adds the images i = q (mod 4) in order; the four
+// partial sums are added in group order.  dlogits are staged in shared
+// memory 512 images at a time.
+__global__ void __launch_bounds__(512) cnn_dense_grad_kernel(const CnnArgs a) {
+  __shared__ float gs[512 * kClasses];
+  __shared__ float red[3][128 * kClasses];
+  const int c = blockIdx.y, t = threadIdx.x, q = t >> 7;
   float* g = a.grad + static_cast<int64_t>(c) * kP;
   const float* gl = a.gl + static_cast<int64_t>(c) * a.n * kClasses;
   if (blockIdx.x == kFlat / 128) {
@@ -359,35 +397,46 @@ __global__ void __launch_bounds__(128) cnn_dense_grad_kernel(const CnnArgs a) {
     }
     return;
   }
-  const int f = blockIdx.x * 128 + t;
+  const int f = blockIdx.x * 128 + (t & 127);
   const bf16* x = a.p3 + static_cast<int64_t>(c) * a.n * kFlat + f;
   float acc[kClasses];
 #pragma unroll
   for (int k = 0; k < kClasses; ++k) acc[k] = 0.f;
-  for (int i0 = 0; i0 < a.n; i0 += 1024) {
-    const int cnt = min(1024, a.n - i0);
+  for (int i0 = 0; i0 < a.n; i0 += 512) {
+    const int cnt = min(512, a.n - i0);
     __syncthreads();
-    for (int j = t; j < cnt * kClasses; j += 128) gs[j] = gl[i0 * kClasses + j];
+    for (int e = t; e < cnt * kClasses; e += 512) gs[e] = gl[i0 * kClasses + e];
     __syncthreads();
-    int i = 0;
-    for (; i + 8 <= cnt; i += 8) {
-      float xv[8];
+    int i = q;
+    for (; i + 12 < cnt; i += 16) {
+      float xv[4];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) xv[u] = bf(x[static_cast<int64_t>(i0 + i + u) * kFlat]);
+      for (int u = 0; u < 4; ++u) xv[u] = bf(x[static_cast<int64_t>(i0 + i + 4 * u) * kFlat]);
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
+      for (int u = 0; u < 4; ++u)
 #pragma unroll
         for (int k = 0; k < kClasses; ++k)
-          acc[k] = fmaf(xv[u], gs[(i + u) * kClasses + k], acc[k]);
+          acc[k] = fmaf(xv[u], gs[(i + 4 * u) * kClasses + k], acc[k]);
     }
-    for (; i < cnt; ++i) {
+    for (; i < cnt; i += 4) {
       const float xv = bf(x[static_cast<int64_t>(i0 + i) * kFlat]);
 #pragma unroll
       for (int k = 0; k < kClasses; ++k) acc[k] = fmaf(xv, gs[i * kClasses + k], acc[k]);
     }
   }
+  if (q > 0) {
 #pragma unroll
-  for (int k = 0; k < kClasses; ++k) g[oWd + static_cast<int64_t>(f) * kClasses + k] = acc[k];
+    for (int k = 0; k < kClasses; ++k) red[q - 1][(t & 127) * kClasses + k] = acc[k];
+  }
+  __syncthreads();
+  if (q == 0) {
+#pragma unroll
+    for (int k = 0; k < kClasses; ++k) {
+      float s = acc[k];
+      for (int r = 0; r < 3; ++r) s += red[r][t * kClasses + k];
+      g[oWd + static_cast<int64_t>(f) * kClasses + k] = s;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -927,11 +976,16 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
                                                    8, 8, kC2, 1, n};
   if ((rc = launch_gemm<128, false, true>(m_p2a, m_w3, C, r3, kC3, kK3, a.status, e3, st)))
     return rc;
-  cnn_dense_kernel<<<dim3(n, C), 128, 0, st>>>(a);
+  static const cudaError_t dense_attr = cudaFuncSetAttribute(
+      cnn_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kDenseSmem));
+  if (dense_attr != cudaSuccess)
+    return set_error(GBSGMC_ERR_CUDA, "cnn_dense_kernel: %s", cudaGetErrorString(dense_attr));
+  cnn_dense_kernel<<<dim3((n + kDenseImgs - 1) / kDenseImgs, C), kDenseImgs * 16, kDenseSmem,
+                     st>>>(a);
   if ((rc = launched("cnn_dense_kernel"))) return rc;
 
   if (a.want_grad) {
-    cnn_dense_grad_kernel<<<dim3(kFlat / 128 + 1, C), 128, 0, st>>>(a);
+    cnn_dense_grad_kernel<<<dim3(kFlat / 128 + 1, C), 512, 0, st>>>(a);
     if ((rc = launched("cnn_dense_grad_kernel"))) return rc;
     // Layer 3: dY3 (routing of dP3), db3, dW3 = dY3^T Col3 (implicit: B
     // blocks are P2's tap-shifted images), dP2 = the transposed convolution
