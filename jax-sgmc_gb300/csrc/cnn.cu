@@ -603,7 +603,14 @@ __global__ void __launch_bounds__(256) cnn_finalize_kernel(const CnnArgs a, floa
 // to M: bits 0-1 the argmax, bit 2 (maximum > 0), the ReLU mask of the
 // element the backward pass routes the gradient to.  The four lanes of a
 // window each write 8 of every 32 channels (16-byte P stores, 8-byte mark
-// stores).  Columns >= C (conv1's padding to N = 64) are skipped.
+// stores).  Columns >= C (conv1's padding to N = 64) are skipped.  The
+// window maxima of a 32-channel chunk take two exchange stages instead of
+// four shuffles per channel: the two pixels of a window row swap the
+// halves of the channels they do not keep (16 shuffles) and keep the
+// pairwise maximum, then the two rows swap halves again (8 shuffles), so
+// that each lane ends with the maxima of its 8 channels; comparisons are
+// strict in window order (left before right, top before bottom), which
+// keeps the first maximum of the window as the sequential scan does.
 template <int H, int W, int V, bool kConv1Rows>
 struct EpiConvPool {
   const float* w;
@@ -642,24 +649,43 @@ struct EpiConvPool {
       const float bl = __ldg(bias + k0 + lane);
       float v[32];
       load(cb, v);
+      float x[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] = fmaxf(v[j] + __shfl_sync(full, bl, j), 0.f);
+      // Stage 1, the window row's two pixels (lanes l, l ^ 1): keep the
+      // chunks {cbit, cbit + 2} of 8 channels (kept channel i: i < 8 in
+      // the first, i >= 8 in the second), send the other two.
+      const bool cbit = (lane & 1) != 0, rbit = (lane & V) != 0;
+      float m1[16];
+      uint32_t col_bits = 0;  // bit i: kept channel i's maximum is the right pixel
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int lo = q < 8 ? q : 8 + q, hi = lo + 8;
+        const float mine = cbit ? x[hi] : x[lo];
+        const float other = __shfl_xor_sync(full, cbit ? x[lo] : x[hi], 1);
+        const float left = cbit ? other : mine, right = cbit ? mine : other;
+        const bool rt = right > left;
+        m1[q] = rt ? right : left;
+        col_bits |= (rt ? 1u : 0u) << q;
+      }
+      // Stage 2, the window's two rows (lanes l, l ^ V): the top row keeps
+      // kept channels 0-7 (chunk cbit), the bottom row 8-15 (chunk
+      // cbit + 2): chunk wp of the 32 channels.
+      const uint32_t other_bits = __shfl_xor_sync(full, col_bits, V);
       float best_mine[8];
       uint32_t mark_mine[8];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const float x = fmaxf(v[j] + __shfl_sync(full, bl, j), 0.f);
-        const float a0 = __shfl_sync(full, x, base);
-        const float a1 = __shfl_sync(full, x, base + 1);
-        const float a2 = __shfl_sync(full, x, base + V);
-        const float a3 = __shfl_sync(full, x, base + V + 1);
-        float best = a0;
-        uint32_t arg = 0;
-        if (a1 > best) { best = a1; arg = 1; }
-        if (a2 > best) { best = a2; arg = 2; }
-        if (a3 > best) { best = a3; arg = 3; }
-        if ((j >> 3) == wp) {
-          best_mine[j & 7] = best;
-          mark_mine[j & 7] = arg | (best > 0.f ? 4u : 0u);
-        }
+      for (int q = 0; q < 8; ++q) {
+        const int ki = rbit ? 8 + q : q;
+        const float mine = rbit ? m1[8 + q] : m1[q];
+        const float other = __shfl_xor_sync(full, rbit ? m1[q] : m1[8 + q], V);
+        const uint32_t my_col = (col_bits >> ki) & 1u, ot_col = (other_bits >> ki) & 1u;
+        const float top = rbit ? other : mine, bot = rbit ? mine : other;
+        const uint32_t top_col = rbit ? ot_col : my_col, bot_col = rbit ? my_col : ot_col;
+        const bool b2 = bot > top;
+        const float best = b2 ? bot : top;
+        best_mine[q] = best;
+        mark_mine[q] = (b2 ? 2u + bot_col : top_col) | (best > 0.f ? 4u : 0u);
       }
       uint32_t pk[4];
 #pragma unroll
