@@ -559,11 +559,16 @@ def run_gbsgmc(args):
   cpu = None
   if rank == 0:
     threads = os.cpu_count() or 1
-    val, _ = cpu_chain_steps(s.X, s.y, 2 * threads, 2, threads)
+    # A short probe sizes a sample of about 10 s: the workload's chains for
+    # as many steps as that takes (2 to 200).  The probe's rate, with its
+    # fixed costs, is about half the sustained one, hence 20 s of it.
+    probe, _ = cpu_chain_steps(s.X, s.y, 2 * threads, 2, threads)
+    cpu_steps = int(min(200, max(2, round(20.0 * probe / CHAINS))))
+    val, cpu_dt = cpu_chain_steps(s.X, s.y, CHAINS, cpu_steps, threads)
     cpu = {"value": val, "unit": "chain-steps/s", "cores": threads,
            "kind": "port",
-           "sample": f"{2 * threads} chains x 2 steps (numpy restatement, "
-                     f"{threads} threads)"}
+           "sample": f"{CHAINS} chains x {cpu_steps} steps, {cpu_dt:.1f} s "
+                     f"(numpy restatement, {threads} threads)"}
 
   if rank == 0:
     line = {
