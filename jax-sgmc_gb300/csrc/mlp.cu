@@ -573,6 +573,15 @@ __global__ void __launch_bounds__(256) mlp_out_kernel(const MlpArgs a) {
     if (a.lk != nullptr && t < kTile) a.lk[static_cast<int64_t>(c) * a.n + i0 + t] = 0.f;
     return;
   }
+  if (a.want_grad) {
+    // The block's 64 x H2 tile of Z2 is brought into L2 while the output
+    // layer below runs (one 128-byte line per prefetch).
+    const char* zt = reinterpret_cast<const char*>(a.z2g + (static_cast<int64_t>(c) * a.n + i0) *
+                                                              s.H2);
+    const int lines = kTile * s.H2 * 2 / 128;
+    for (int q = t; q < lines; q += 256)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(zt + static_cast<int64_t>(q) * 128));
+  }
   if (t < kTile) {
     const float inv_s2 = 1.f / (a.sigma * a.sigma);
     const float scale = static_cast<float>(static_cast<double>(a.n_obs) / nc / a.temperature);
