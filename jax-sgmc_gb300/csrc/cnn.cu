@@ -94,9 +94,12 @@ struct CnnLayout {
 constexpr int kPrepBlocks = 64;  // Σw² partial sums per chain
 
 // Split-K factors of the weight-gradient GEMMs (K = pixels of n images:
-// 16n, 4n and n slices of 64 for the three layers; n is even).
+// 16n, 4n and n slices of 64 for the three layers; n is even; a factor
+// divides the slice count).  Layer 2 has 5 N tiles per chain: 16 splits
+// make 640 tiles for 8 chains (4.3 waves of 148 CTAs) where 8 made 320
+// (2.2 waves, the third one sixth full).
 inline int wsplit(int layer, int n) {
-  return layer == 1 ? 32 : layer == 2 ? 8 : (n % 4 == 0 ? 4 : 2);
+  return layer == 1 ? 32 : layer == 2 ? (n % 4 == 0 ? 16 : 8) : (n % 4 == 0 ? 4 : 2);
 }
 
 CnnLayout cnn_layout(int chains, int n) {
