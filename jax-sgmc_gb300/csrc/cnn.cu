@@ -516,14 +516,17 @@ __global__ void __launch_bounds__(256) cnn_unpool_kernel(bf16* dY, const uint8_t
 }
 
 // Bias gradient: grad[off + ch] = sum over the unpool blocks' partials in a
-// fixed order: thread t adds channel t % C of blocks t / C, t / C + 256 / C,
-// ... (coalesced along channels, eight loads in flight), then the 256 / C
-// partial sums of a channel are added in order.  Grid (chains), 256 threads;
-// C divides 256.
-__global__ void __launch_bounds__(256) cnn_bias_sum_kernel(const float* bpart, int blocks,
-                                                           int C, float* grad, int64_t off) {
-  __shared__ float acc[256];
-  const int c = blockIdx.x, t = threadIdx.x, ch = t % C, g0 = t / C, step = 256 / C;
+// fixed order: thread t adds channel t % C of blocks t / C, t / C + kBiasT /
+// C, ... (coalesced along channels, eight loads in flight), then the
+// kBiasT / C partial sums of a channel are added in order.  Grid (chains),
+// kBiasT threads (enough loads in flight for the few blocks this grid has);
+// C divides kBiasT.
+constexpr int kBiasT = 1024;
+
+__global__ void __launch_bounds__(kBiasT) cnn_bias_sum_kernel(const float* bpart, int blocks,
+                                                              int C, float* grad, int64_t off) {
+  __shared__ float acc[kBiasT];
+  const int c = blockIdx.x, t = threadIdx.x, ch = t % C, g0 = t / C, step = kBiasT / C;
   const float* p = bpart + static_cast<int64_t>(c) * blocks * C + ch;
   float s = 0.f;
 #pragma unroll 8
@@ -941,7 +944,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   // gradient from the unpool blocks' partials.
   auto bias_sum = [&](int H, int Cr, int64_t off) {
     const int blocks = grid1(int64_t(n) * (H / 2) * (H / 2) * Cr / 8);
-    cnn_bias_sum_kernel<<<C, 256, 0, st>>>(a.bpart, blocks, Cr, a.grad, off);
+    cnn_bias_sum_kernel<<<C, kBiasT, 0, st>>>(a.bpart, blocks, Cr, a.grad, off);
     return launched("cnn_bias_sum_kernel");
   };
   auto unpool_grid = [&](int H, int Cr) {
