@@ -3,9 +3,9 @@ accumulation) against the FP64 oracle and torch fp32 autograd, through the
 C ABI; the CNN network plan against the per-chain step path.
 
 Tolerances.  GEMM operands (images, conv weights, pooled maps, output
-gradients dY, input-gradient columns dCol) are BF16 with fp32
-accumulation; the ReLU outputs the 2x2 max-pool compares, the dense layer
-and the col2im sums stay fp32.  The oracle run with ``bf16_operands=True``
+gradients dY) are BF16 with fp32 accumulation; the ReLU outputs the 2x2
+max-pool compares, the dense layer and the transposed convolutions' input
+gradients stay fp32.  The oracle run with ``bf16_operands=True``
 rounds the same values at the same places, so against it only summation
 order differs:
   U         |U - U_ref| <= 1e-4 (N/n sum_i |lk_i|) / T
