@@ -489,10 +489,11 @@ def cnn_potential(w, images, labels, idx, n_obs, prior_scale=0.0,
   pooling: a 2x2 max over BF16-rounded values can pick a different window
   element than the exact maximum, and that changes where the gradient flows.
   ``bf16_operands`` rounds, to BF16, exactly the values a BF16 GEMM pipeline
-  feeds its tensor cores -- the images, the conv weights, the pooled maps,
-  the conv output gradients dY and the input-gradient columns dCol -- and
-  keeps everything else (accumulation, ReLU outputs, the dense layer, col2im
-  sums) in float64: the arithmetic of the GPU kernels up to summation order.
+  feeds its tensor cores -- the images, the conv weights, the pooled maps and
+  the conv output gradients dY -- and keeps everything else (accumulation,
+  ReLU outputs, the dense layer, the input gradients dY W^T summed over the
+  taps, which the kernels compute as one transposed convolution into fp32)
+  in float64: the arithmetic of the GPU kernels up to summation order.
   """
   off, P = cnn_offsets()
   w = np.asarray(w, np.float64)
@@ -538,7 +539,7 @@ def cnn_potential(w, images, labels, idx, n_obs, prior_scale=0.0,
     grad[off[f"W{l + 1}"][0]:off[f"W{l + 1}"][1]] = (cols.T @ dz).reshape(-1)
     grad[off[f"b{l + 1}"][0]:off[f"b{l + 1}"][1]] = dz.sum(0)
     if l > 0:
-      dh = _col2im(rnd(dz @ wl.T), shape_in)
+      dh = _col2im(dz @ wl.T, shape_in)
   grad = grad - dlp[0] / temperature
   return Potential(np.array([U]), grad[None], lk[None], np.array([np.var(lk)]))
 
