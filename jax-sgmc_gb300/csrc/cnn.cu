@@ -257,29 +257,30 @@ __global__ void __launch_bounds__(256) cnn_gather1_kernel(const CnnArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// im2col of a pooled map P [n, H, W, C] -> Col [n*H*W, Kp], K = (kh, kw, ci)
-// (9C real).  One thread per 8 consecutive K entries (C is a multiple of 8).
-// Grid (ceil(n*H*W*Kp/8 / 256), chains).
+// im2col of a pooled map P [n, H, W, C] -> Col [n*H*W, Kp], K = (kh, kw, ci):
+// the 9C real columns of each row (row stride Kp); the columns 9C..Kp-1 are
+// never written (the tensor maps that read Col end at 9C, so their boxes
+// read zeros there).  One thread per 8 consecutive K entries (C is a
+// multiple of 8).  Grid (ceil(n*H*W*9C/8 / 256), chains).
 // ---------------------------------------------------------------------------
 template <int H, int W, int C, int Kp>
 __global__ void __launch_bounds__(256) cnn_im2col_kernel(const bf16* Pin, bf16* Col, int n) {
+  constexpr int G = 9 * C / 8;  // 8-column groups per row
   const int c = blockIdx.y;
-  const int groups = n * H * W * (Kp / 8);
+  const int groups = n * H * W * G;
   const int e = blockIdx.x * 256 + threadIdx.x;
   if (e >= groups) return;
-  const int k0 = (e % (Kp / 8)) * 8;
-  const int pix = e / (Kp / 8);
+  const int k0 = (e % G) * 8;
+  const int pix = e / G;
   const int x = pix % W, y = (pix / W) % H;
   const int i = pix / (W * H);
   uint4 v = make_uint4(0, 0, 0, 0);
-  if (k0 < 9 * C) {
-    const int tap = k0 / C, ci = k0 % C;
-    const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-    if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-      v = *reinterpret_cast<const uint4*>(Pin + static_cast<int64_t>(c) * n * H * W * C +
-                                          ((i * H + yy) * W + xx) * C + ci);
-  }
-  reinterpret_cast<uint4*>(Col + static_cast<int64_t>(c) * n * H * W * Kp)[e] = v;
+  const int tap = k0 / C, ci = k0 % C;
+  const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+  if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+    v = *reinterpret_cast<const uint4*>(Pin + static_cast<int64_t>(c) * n * H * W * C +
+                                        ((i * H + yy) * W + xx) * C + ci);
+  *reinterpret_cast<uint4*>(Col + (static_cast<int64_t>(c) * n * H * W + pix) * Kp + k0) = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -983,7 +984,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
       (rc = make_tmap_bf16_4d_plain(&m_w1i, a.w1i, {32 * kX8, 2, kG1, C},
                                     {32 * kX8, 64 * kX8, kG1 * 64 * kX8},
                                     {32 * kX8, 2, kG1, 1})) ||
-      (rc = make_tmap_bf16_3d(&m_col2, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, kGemmBK, kGemmBM)) ||
+      (rc = make_tmap_bf16_3d(&m_col2, a.col2, kK2, r2, C, kK2p, r2 * kK2p, kGemmBK, kGemmBM)) ||
       (rc = make_tmap_bf16_3d(&m_w2, a.w2b, kC2, kK2, C, kC2, kK2 * kC2, 64, 64)) ||
       (rc = make_tmap_bf16_3d(&m_w3, a.w3b, kC3, kK3, C, kC3, kK3 * kC3, 64, 64)) ||
       (rc = make_tmap_bf16_4d(&m_p2a, a.p2, {kC2, 8, 8, imgs}, {kC2, 8 * kC2, 64 * kC2},
@@ -997,7 +998,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
   const Conv1Fwd<EpiConvPool<32, 32, 16, true>> e1{{a.w, ob1, kC1, a.p1, a.m1, n}, n};
   if ((rc = launch_gemm<64, false, false>(m_x8, m_w1i, C, r1, 64, kK1i, a.status, e1, st)))
     return rc;
-  cnn_im2col_kernel<16, 16, kC1, kK2p><<<dim3(grid1(r2 * kK2p / 8), C), 256, 0, st>>>(
+  cnn_im2col_kernel<16, 16, kC1, kK2p><<<dim3(grid1(r2 * kK2 / 8), C), 256, 0, st>>>(
       a.p1, a.col2, n);
   if ((rc = launched("cnn_im2col_kernel 2"))) return rc;
   const EpiConvPool<16, 16, 16, false> e2{a.w, ob2, kC2, a.p2, a.m2, n};
@@ -1056,7 +1057,7 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
     if ((rc = launched("cnn_unpool_kernel 2")) || (rc = bias_sum(16, kC2, ob2))) return rc;
     CUtensorMap m_dy2t, m_col2t, m_dy2a, m_w2t;
     if ((rc = make_tmap_bf16_3d(&m_dy2t, a.dy2, kC2, r2, C, kC2, r2 * kC2, 64, 64)) ||
-        (rc = make_tmap_bf16_3d(&m_col2t, a.col2, kK2p, r2, C, kK2p, r2 * kK2p, 64, 64)) ||
+        (rc = make_tmap_bf16_3d(&m_col2t, a.col2, kK2, r2, C, kK2p, r2 * kK2p, 64, 64)) ||
         (rc = make_tmap_bf16_4d(&m_dy2a, a.dy2, {kC2, 16, 16, imgs},
                                 {kC2, 16 * kC2, 256 * kC2}, {64, 16, 8, 1})) ||
         (rc = make_tmap_bf16_4d(&m_w2t, a.w2b, {kC2, kC1, 9, C}, {kC2, kC1 * kC2, kK2 * kC2},
