@@ -905,6 +905,15 @@ struct HalfA : Inner {
   }
 };
 
+// A transposed convolution whose output channels fill only kRows of the
+// GEMM's N = 64 columns: B's box holds those kRows rows (the map's box is
+// 64 x kRows), the MMAs' other columns read whatever the stage held and the
+// epilogue drops them; the stage expects A's bytes and kRows rows of B.
+template <class Inner, int kRows>
+struct TransposedBRows : TransposedB<Inner> {
+  static constexpr uint32_t kStageBytes = (kGemmBM + kRows) * kGemmBK * 2;
+};
+
 template <class T>
 T* view(void* ws, size_t off) {
   return reinterpret_cast<T*>(static_cast<unsigned char*>(ws) + off);
@@ -1061,10 +1070,11 @@ int run_cnn(CnnArgs& a, const CnnLayout& L, void* ws, cudaStream_t st) {
         (rc = make_tmap_bf16_4d(&m_dy2a, a.dy2, {kC2, 16, 16, imgs},
                                 {kC2, 16 * kC2, 256 * kC2}, {64, 16, 8, 1})) ||
         (rc = make_tmap_bf16_4d(&m_w2t, a.w2b, {kC2, kC1, 9, C}, {kC2, kC1 * kC2, kK2 * kC2},
-                                {64, 64, 1, 1})))
+                                {64, kC1, 1, 1})))
       return rc;
     if ((rc = weight_grad(m_dy2t, m_col2t, 2, kC2, kK2, kK2p, r2, oW2))) return rc;
-    const TransposedB<ImplicitA<EpiStoreDX>> d2{{{a.dp1, kC1, r2}, 16, 16, kC2, -1, n}, kC2};
+    const TransposedBRows<ImplicitA<EpiStoreDX>, kC1> d2{
+        {{{a.dp1, kC1, r2}, 16, 16, kC2, -1, n}, kC2}};
     if ((rc = launch_gemm<64, false, false>(m_dy2a, m_w2t, C, r2, 64, 9 * kC2, a.status, d2,
                                             st)))
       return rc;
