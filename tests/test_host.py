@@ -537,3 +537,27 @@ def test_pcg64_seed_in_c_matches_numpy():
   np.testing.assert_array_equal(fast, nl.pcg64_words_many(seeds))
   for s in seeds[::7] + seeds[-12:]:
     np.testing.assert_array_equal(fast[seeds.index(s)], np.array(nl.pcg64_words(s), np.uint64))
+
+
+def test_seeding_and_bf16_gemm_validation_without_a_gpu():
+  """gbsgmc_pcg64_seed rejects a negative count and missing buffers (a zero
+  count is a no-op), and gbsgmc_gemm_bf16_c16 rejects a C it cannot write
+  with TMA store boxes -- a row stride that is not a multiple of 8 elements,
+  a C that is not 16-byte aligned -- before touching the device (the
+  pointers are never dereferenced)."""
+  from gbsgmc import _lib
+  lib = _lib.load()
+  assert lib.gbsgmc_pcg64_seed(None, None, -1, None) == _lib.ERR_ARG
+  assert lib.gbsgmc_pcg64_seed(None, None, 3, None) == _lib.ERR_ARG
+  assert b"null" in lib.gbsgmc_last_error()
+  assert lib.gbsgmc_pcg64_seed(None, None, 0, None) == 0
+
+  def gemm(C_ptr, ldc):
+    return lib.gbsgmc_gemm_bf16_c16(0, 0, 4096, 128, 128 * 128, 4096, 128,
+                                    128 * 128, C_ptr, ldc, 128 * ldc, 2, 128,
+                                    128, 128, 4096, None)
+
+  assert gemm(8192, 100) == _lib.ERR_ARG
+  assert b"multiples of 8" in lib.gbsgmc_last_error()
+  assert gemm(8192 + 8, 128) == _lib.ERR_SHAPE
+  assert b"16-byte" in lib.gbsgmc_last_error()
