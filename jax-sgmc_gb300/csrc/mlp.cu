@@ -418,8 +418,9 @@ struct EpiHidden2 {
   }
 };
 
-// 7: G1 = acc * (1 - Z1^2) written over Z1 [n, H1] (the block is read and
-//    then rewritten, as a TMA store box, by the same warp); per-warp column sums -> pb1
+// 7: G1 = acc * (1 - Z1^2) written over Z1 [n, H1] (the block is read with
+//    asynchronous copies into the warp's staging tile and rewritten, as a
+//    TMA store box, by the same warp); per-warp column sums -> pb1
 //    [n/32, H1].
 struct EpiAdjoint1 {
   bf16* z1;
@@ -430,22 +431,19 @@ struct EpiAdjoint1 {
   __device__ __forceinline__ void tile(int b, int row0, int col0, const Load& load,
                                        uint32_t* st) const {
     const int lane = epi::lane_id();
-    uint32_t* zrow = reinterpret_cast<uint32_t*>(z1 + (static_cast<int64_t>(b) * n + row0) * H1 +
-                                                 col0) + lane;
+    const char* zsrc = reinterpret_cast<const char*>(z1 + (static_cast<int64_t>(b) * n + row0) * H1 +
+                                                     col0);
     float* part = pb1 + (static_cast<int64_t>(b) * (n / 32) + row0 / 32) * H1 + col0;
 #pragma unroll 1
     for (int blk = 0; blk < NC / 64; ++blk) {
-      // The accumulator's 64 columns are requested first; the Z1 block is
-      // read and transposed while they arrive.
+      // The Z1 block is copied into the staging tile (cp.async) and the
+      // accumulator's 64 columns requested; both arrive together.
+      epi::fetch_box(st, zsrc + 128 * blk, static_cast<int64_t>(H1) * 2);
       uint32_t acc[64];
       load.wide_start(blk, acc);
       uint32_t zw[32];
-#pragma unroll
-      for (int r = 0; r < 32; ++r) zw[r] = zrow[static_cast<int64_t>(r) * (H1 / 2) + 32 * blk];
-      epi::reclaim();
-#pragma unroll
-      for (int r = 0; r < 32; ++r) epi::set(st, r, zw[r]);
-      epi::get_row(st, zw);
+      epi::fetch_wait();
+      epi::read_row(st, zw);
       tc::tmem_ld64_wait(acc);
       float vv[64];
 #pragma unroll

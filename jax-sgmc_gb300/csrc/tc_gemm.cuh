@@ -96,6 +96,41 @@ __device__ __forceinline__ void store_box(uint32_t* st, const uint32_t (&w)[32],
   }
 }
 
+// The reverse of store_box for a warp's reads: copies a block of 32 rows of
+// 128 bytes (row r at src + r * ld_bytes, 16-byte aligned) into the staging
+// tile in store_box's swizzled order with asynchronous 16-byte copies
+// (eight per lane, 8 lanes per row), once the tile's last TMA store has read
+// it; fetch_wait completes them for the whole warp and read_row gives lane
+// l its row.
+__device__ __forceinline__ void fetch_box(uint32_t* st, const void* src, int64_t ld_bytes) {
+  const int l = lane_id(), q = l & 7;
+  reclaim();
+  uint8_t* tile = reinterpret_cast<uint8_t*>(st);
+  const char* s = static_cast<const char*>(src);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = 4 * i + (l >> 3);
+    tc::cp_async16(tile + r * 128 + ((q ^ (r & 7)) << 4), s + r * ld_bytes + q * 16);
+  }
+  tc::cp_async_commit();
+}
+__device__ __forceinline__ void fetch_wait() {
+  tc::cp_async_wait_all();
+  __syncwarp();
+}
+__device__ __forceinline__ void read_row(const uint32_t* st, uint32_t (&w)[32]) {
+  const int l = lane_id();
+  const uint8_t* row = reinterpret_cast<const uint8_t*>(st) + l * 128;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const uint4 x = tc::lds128(row + ((q ^ (l & 7)) << 4));
+    w[4 * q] = x.x;
+    w[4 * q + 1] = x.y;
+    w[4 * q + 2] = x.z;
+    w[4 * q + 3] = x.w;
+  }
+}
+
 }  // namespace epi
 
 // 3-D BF16 tensor map (cols innermost, rows, batch) with a 128-byte swizzled
