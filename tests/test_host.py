@@ -561,3 +561,37 @@ def test_seeding_and_bf16_gemm_validation_without_a_gpu():
   assert b"multiples of 8" in lib.gbsgmc_last_error()
   assert gemm(8192 + 8, 128) == _lib.ERR_SHAPE
   assert b"16-byte" in lib.gbsgmc_last_error()
+
+
+def test_postprocess_chains_shared_layout_equals_per_chain_unravel():
+  """The result dicts built from per-leaf views of the host buffer (all
+  chains share one tree definition) equal those of the general path, which
+  unravels each chain with its own definition (forced here by equal but
+  distinct definition objects), for host saving and for no saving."""
+  import torch
+  from gbsgmc import io, util
+  rng = np.random.default_rng(5)
+  tree = {"w": np.zeros((3, 4), np.float32), "b": np.zeros(5, np.float32),
+          "s": np.zeros((), np.float32)}
+  flat, td = util.ravel(tree)
+  count, C, P = 6, 4, flat.size
+  variables = torch.from_numpy(rng.normal(size=(count, C, P)).astype(np.float32))
+  extras = {"likelihood": torch.from_numpy(rng.normal(size=(count, C)))}
+  states = [None] * C
+  distinct = [util.ravel(tree)[1] for _ in range(C)]
+  for make_saving in (lambda: io.save(io.MemoryCollector()), io.no_save):
+    fast = io.postprocess_chains(make_saving(), count, variables, [td] * C, extras, states)
+    slow = io.postprocess_chains(make_saving(), count, variables, distinct, extras, states)
+    assert len(fast) == len(slow) == C
+    for a, b in zip(fast, slow):
+      assert a["sample_count"] == b["sample_count"] == count
+      va, vb = a["samples"]["variables"], b["samples"]["variables"]
+      assert sorted(va) == sorted(vb) == ["b", "s", "w"]
+      for k in va:
+        assert va[k].shape == vb[k].shape
+        np.testing.assert_array_equal(va[k], vb[k])
+      np.testing.assert_array_equal(a["samples"]["likelihood"], b["samples"]["likelihood"])
+    # chain 1's first sample is row (0, 1) of the buffer in ravel order
+    v = fast[1]["samples"]["variables"]
+    again, _ = util.ravel({k: v[k][0] for k in v})
+    np.testing.assert_array_equal(again, variables[0, 1].numpy())
