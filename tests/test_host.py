@@ -595,3 +595,15 @@ def test_postprocess_chains_shared_layout_equals_per_chain_unravel():
     v = fast[1]["samples"]["variables"]
     again, _ = util.ravel({k: v[k][0] for k in v})
     np.testing.assert_array_equal(again, variables[0, 1].numpy())
+
+
+def test_pcg64_seed_above_2_128_takes_the_numpy_restatement():
+  """Seeds of 2**128 and above (more than four entropy words) are outside
+  the C function's range; pcg64_words_fast then gives the numpy
+  restatement's words, which equal numpy's own generators."""
+  from gbsgmc.data import numpy_loader as nl
+  seeds = [2**128, 2**200 + 5, 3]
+  fast = nl.pcg64_words_fast(seeds)
+  np.testing.assert_array_equal(fast, nl.pcg64_words_many(seeds))
+  for i, s in enumerate(seeds):
+    np.testing.assert_array_equal(fast[i], np.array(nl.pcg64_words(s), np.uint64))
